@@ -1,0 +1,201 @@
+/*
+ * faz_gb300.h - C ABI of the GB300-native FAZ interpolation compressor.
+ *
+ * The entry points below are what a foreign-function binding of FAZ's
+ * compress/decompress path attaches to.  They replace the C++ template
+ * entry points of the reference:
+ *
+ *   template<class T> char *SZ_compress(QoZ::Config&, const T*, size_t&)
+ *       include/QoZ/api/sz.hpp:54-108           -> faz_compress()
+ *   template<class T> void SZ_decompress(QoZ::Config&, char*, size_t, T*&)
+ *       include/QoZ/api/sz.hpp:159-205          -> faz_decompress()
+ *   template<class T> T *SZ_decompress(QoZ::Config&, char*, size_t)
+ *       include/QoZ/api/sz.hpp:220-225          -> faz_decompress() with *out == NULL
+ *   QoZ::Config::Config(Dims...)  include/QoZ/utils/Config.hpp:64-74  -> faz_config_init()
+ *   QoZ::Config::loadcfg(path)    include/QoZ/utils/Config.hpp:91-233 -> faz_config_load_ini()
+ *   QoZ::calAbsErrorBound         include/QoZ/utils/Statistic.hpp:34-66 (run inside faz_compress)
+ *
+ * Plain C types only: pointers, sizes and a POD configuration struct whose
+ * fields carry the names, meaning and defaults of QoZ::Config.
+ *
+ * Ownership: buffers returned through `char **out` / `void **out` are
+ * allocated by the library and released with faz_free().
+ * Errors: every call returns FAZ_OK (0) or a negative status; the message of
+ * the last failure on the calling thread is available from faz_last_error().
+ * The reference terminates the process on bad input (e.g.
+ * include/QoZ/api/impl/SZDispatcher.hpp:49-50); this library returns instead.
+ * Threading: calls on different threads are independent; each call uses its
+ * own CUDA stream on the current device.
+ */
+#ifndef FAZ_GB300_H
+#define FAZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FAZ_OK 0
+#define FAZ_ERR_ARG (-1)        /* invalid argument or configuration */
+#define FAZ_ERR_UNSUPPORTED (-2) /* configuration outside the implemented path */
+#define FAZ_ERR_CUDA (-3)       /* CUDA runtime failure */
+#define FAZ_ERR_FORMAT (-4)     /* malformed or truncated stream */
+#define FAZ_ERR_ZSTD (-5)       /* host zstd library missing or failed */
+#define FAZ_ERR_DEVICE (-6)     /* a kernel reported an error status */
+
+/* data types, as the reference CLI numbers them (test/faz.cpp:10-11) */
+#define FAZ_FLOAT 0
+#define FAZ_DOUBLE 1
+
+/* QoZ::ALGO (include/QoZ/utils/Config.hpp:24-26) */
+#define FAZ_ALGO_LORENZO_REG 0
+#define FAZ_ALGO_INTERP_LORENZO 1
+#define FAZ_ALGO_INTERP 2
+#define FAZ_ALGO_INTERP_BLOCKED 3
+/* QoZ::EB (Config.hpp:18-20) */
+#define FAZ_EB_ABS 0
+#define FAZ_EB_REL 1
+#define FAZ_EB_PSNR 2
+#define FAZ_EB_L2NORM 3
+#define FAZ_EB_ABS_AND_REL 4
+#define FAZ_EB_ABS_OR_REL 5
+/* QoZ::INTERP_ALGO (Config.hpp:30-31) */
+#define FAZ_INTERP_ALGO_LINEAR 0
+#define FAZ_INTERP_ALGO_CUBIC 1
+
+#define FAZ_MAX_LEVELS 64
+
+/*
+ * Mirror of QoZ::Config (include/QoZ/utils/Config.hpp:394-499): the fields
+ * written to the stream trailer by Config::save (Config.hpp:240-309) plus the
+ * knobs the interpolation path reads.  faz_config_init() sets the reference
+ * defaults.  Booleans are uint8_t (0/1).
+ */
+typedef struct faz_config {
+    int32_t N;                      /* char N */
+    uint64_t dims[4];               /* dims[0] is the slowest dimension */
+    uint64_t num;
+    uint8_t cmprAlgo;               /* default ALGO_INTERP_LORENZO */
+    uint8_t errorBoundMode;         /* default EB_ABS */
+    uint8_t tuningTarget;           /* default TUNING_TARGET_RD */
+    double absErrorBound;
+    double relErrorBound;           /* default -1 */
+    double psnrErrorBound;
+    double l2normErrorBound;
+    double rng;                     /* default -1 */
+    double alpha;                   /* default -1 */
+    double beta;                    /* default -1 */
+    double autoTuningRate;          /* default 0 */
+    double predictorTuningRate;     /* default 0 */
+    uint8_t lorenzo;                /* default 1 */
+    uint8_t lorenzo2;               /* default 0 */
+    uint8_t regression;             /* default 1 */
+    uint8_t regression2;            /* default 0 */
+    uint8_t openmp;                 /* default 0 */
+    uint8_t lossless;               /* default 1 */
+    uint8_t encoder;                /* default 1 */
+    uint8_t interpAlgo;             /* default INTERP_ALGO_CUBIC */
+    uint8_t interpDirection;        /* default 0 */
+    int32_t levelwisePredictionSelection;
+    int32_t interp_list_len;        /* size of interpAlgo_list / interpDirection_list */
+    uint8_t interpAlgo_list[FAZ_MAX_LEVELS];
+    uint8_t interpDirection_list[FAZ_MAX_LEVELS];
+    uint64_t maxStep;               /* default 0 (no anchor grid) */
+    int32_t interpBlockSize;        /* default 32 */
+    int32_t quantbinCnt;            /* default 65536 */
+    int32_t blockSize;              /* 128 (1D) / 16 (2D) / 6 (3D, 4D) */
+    int32_t testLorenzo;
+    int32_t sampleBlockSize;
+    uint8_t blockwiseTuning;
+    int32_t stride;                 /* = blockSize */
+    int32_t pred_dim;               /* = N */
+    int32_t profiling;
+    int32_t SSIMBlockSize;          /* default 8 */
+    int32_t fixBlockSize;
+    int32_t blockwiseSampleBlockSize;
+    uint8_t verbose;                /* default 1 */
+    uint8_t QoZ;
+    uint8_t FZ;
+    int32_t abList;
+    int32_t crossBlock;
+    int32_t sampleBlockSampleBlockSize;
+    uint8_t peTracking;
+    int32_t wavelet;
+    uint64_t coeffs_num;            /* = num */
+    int32_t coeffs_dims_len;        /* = N */
+    uint64_t coeffs_dims[4];        /* = dims */
+    double wavelet_rel_coeff;       /* default 0.75 */
+    uint64_t firstSize;             /* never set on this path; written as 0 */
+    int32_t pid;
+    int32_t offsetPredictor;
+    int32_t trimToZero;
+    double preTrim;
+    int32_t blockOrder;
+    int32_t sperr;                  /* default -1 */
+    uint8_t sperrWithoutWave;
+    uint8_t pyBind;                 /* default 1; metadata string is empty */
+    int32_t conditioning;
+    uint8_t meta[17];
+    uint8_t pybind_activated;
+} faz_config;
+
+/* Per-call timings in milliseconds, filled when a non-NULL pointer is given. */
+typedef struct faz_timings {
+    double total_ms;       /* whole call, host clock */
+    double h2d_ms;         /* host -> device copy of the input / payload */
+    double gpu_ms;         /* device work between the copies (CUDA events) */
+    double d2h_ms;         /* device -> host copy of the result */
+    double zstd_ms;        /* host zstd stage */
+    double host_ms;        /* host codebook / stream assembly */
+    uint64_t payload_bytes;    /* pre-zstd payload */
+    uint64_t unpred_count;
+    uint64_t kernel_launches;  /* kernels this library launched in the call */
+} faz_timings;
+
+/* QoZ::Config::Config(dims...) - Config.hpp:64-74.  dims[0] slowest. */
+int faz_config_init(faz_config *conf, int N, const uint64_t *dims);
+
+/* QoZ::Config::loadcfg - Config.hpp:91-233 ([GlobalSettings]/[AlgoSettings]). */
+int faz_config_load_ini(faz_config *conf, const char *path);
+
+/* SZ_compress<T> - sz.hpp:54-108.  `data` is host memory holding conf->num
+ * values of `dtype`.  On success *out is a library-allocated stream of
+ * *out_size bytes: payload | Config trailer | int32 trailer size.  conf is
+ * read, not modified, as in the reference (which compresses a copy). */
+int faz_compress(const faz_config *conf, int dtype, const void *data,
+                 char **out, size_t *out_size, faz_timings *timings);
+
+/* SZ_decompress<T> - sz.hpp:159-205.  Reads the trailer into *conf, then
+ * decodes.  If *out is NULL the library allocates conf->num values (release
+ * with faz_free); otherwise *out must hold conf->num values.  Unlike the
+ * reference, no side file is written. */
+int faz_decompress(faz_config *conf, int dtype, const char *cmp, size_t cmp_size,
+                   void **out, faz_timings *timings);
+
+/* Same as faz_compress with the input already in device memory (d_data) and
+ * work issued on `stream` (a cudaStream_t, or NULL for a library stream). */
+int faz_compress_device(const faz_config *conf, int dtype, const void *d_data,
+                        void *stream, char **out, size_t *out_size,
+                        faz_timings *timings);
+
+/* Same as faz_decompress writing conf->num values into device memory d_out. */
+int faz_decompress_device(faz_config *conf, int dtype, const char *cmp,
+                          size_t cmp_size, void *d_out, void *stream,
+                          faz_timings *timings);
+
+/* Release a buffer returned by this library. */
+void faz_free(void *p);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *faz_last_error(void);
+
+/* Host zstd library in use: its ZSTD_versionNumber(), or 0 if none loaded.
+ * The library is found as libzstd.so.1 unless FAZ_ZSTD_LIBRARY names a path. */
+unsigned faz_zstd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FAZ_GB300_H */

@@ -1,0 +1,923 @@
+/*
+ * faz_oracle.c - CPU oracle for FAZ's interpolation-predictor path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain C restatement of the reference
+ * algorithm used to check the CUDA path; tests/, __graft_entry__.smoke() and
+ * the CPU-baseline leg of bench.py are its only users.  The product library
+ * (faz_gb300/) never links or calls it.
+ *
+ * Parity of this restatement is pinned against streams written by the
+ * reference's own build (tests/golden/, generated by
+ * tests/golden/make_golden.py from oracle/_ref/faz).
+ *
+ * Covered (reference file:line, paths relative to the reference root):
+ *   error bound      include/QoZ/utils/Statistic.hpp:12-66
+ *   interpolation    include/QoZ/compressor/SZInterpolationCompressor.hpp:42-199, 324-529,
+ *                    820-923, 1306-1417, 3076-3442; include/QoZ/utils/Interpolators.hpp:9-36
+ *   quantiser        include/QoZ/quantizer/IntegerQuantizer.hpp:69-226
+ *   Huffman          include/QoZ/encoder/HuffmanEncoder.hpp:93-296, 455-633
+ *   map order        include/QoZ/utils/ska_hash/unordered_map.hpp:295-304, 412-450, 605-643
+ *                    and flat_hash_map.hpp:1268-1300 (fibonacci_hash_policy)
+ *   zstd framing     include/QoZ/lossless/Lossless_zstd.hpp:22-47
+ *   trailer          include/QoZ/utils/Config.hpp:240-388, include/QoZ/api/sz.hpp:54-205
+ */
+#define _GNU_SOURCE
+#include <dlfcn.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/faz_gb300.h"
+
+/* ------------------------------------------------------------------ utils */
+
+typedef struct {
+    uint8_t *p;
+    size_t n, cap;
+} bytes_t;
+
+static void b_reserve(bytes_t *b, size_t more) {
+    if (b->n + more > b->cap) {
+        size_t c = b->cap ? b->cap : 4096;
+        while (c < b->n + more) c *= 2;
+        b->p = (uint8_t *)realloc(b->p, c);
+        b->cap = c;
+    }
+}
+static void b_put(bytes_t *b, const void *src, size_t len) {
+    b_reserve(b, len);
+    memcpy(b->p + b->n, src, len);
+    b->n += len;
+}
+#define PUT(b, v)                      \
+    do {                               \
+        __typeof__(v) _t = (v);        \
+        b_put((b), &_t, sizeof(_t));   \
+    } while (0)
+
+typedef struct {
+    const uint8_t *p;
+    size_t n, pos;
+    int bad;
+} rd_t;
+static void r_get(rd_t *r, void *dst, size_t len) {
+    if (r->pos + len > r->n) { r->bad = 1; memset(dst, 0, len); return; }
+    memcpy(dst, r->p + r->pos, len);
+    r->pos += len;
+}
+
+static void put_be32(bytes_t *b, int32_t v) {
+    uint8_t t[4] = {(uint8_t)(v >> 24), (uint8_t)(v >> 16), (uint8_t)(v >> 8), (uint8_t)v};
+    b_put(b, t, 4);
+}
+static int32_t get_be32(rd_t *r) {
+    uint8_t t[4];
+    r_get(r, t, 4);
+    return (int32_t)(((uint32_t)t[0] << 24) | ((uint32_t)t[1] << 16) | ((uint32_t)t[2] << 8) | t[3]);
+}
+
+static char g_err[512];
+static void set_err(const char *m) { snprintf(g_err, sizeof g_err, "%s", m); }
+const char *orc_last_error(void) { return g_err; }
+
+/* ------------------------------------------------------------------- zstd */
+
+typedef size_t (*zcomp_t)(void *, size_t, const void *, size_t, int);
+typedef size_t (*zdecomp_t)(void *, size_t, const void *, size_t);
+typedef unsigned (*ziserr_t)(size_t);
+typedef size_t (*zbound_t)(size_t);
+typedef unsigned (*zver_t)(void);
+static void *g_z;
+static zcomp_t z_comp;
+static zdecomp_t z_decomp;
+static ziserr_t z_iserr;
+static zbound_t z_bound;
+static zver_t z_ver;
+static char g_zpath[1024] = "libzstd.so.1";
+
+int orc_set_zstd(const char *path) {
+    if (g_z) { dlclose(g_z); g_z = NULL; }
+    snprintf(g_zpath, sizeof g_zpath, "%s", path && *path ? path : "libzstd.so.1");
+    return 0;
+}
+static int z_load(void) {
+    if (g_z) return 0;
+    g_z = dlopen(g_zpath, RTLD_NOW | RTLD_LOCAL);
+    if (!g_z) { set_err("cannot load zstd library"); return -1; }
+    z_comp = (zcomp_t)dlsym(g_z, "ZSTD_compress");
+    z_decomp = (zdecomp_t)dlsym(g_z, "ZSTD_decompress");
+    z_iserr = (ziserr_t)dlsym(g_z, "ZSTD_isError");
+    z_bound = (zbound_t)dlsym(g_z, "ZSTD_compressBound");
+    z_ver = (zver_t)dlsym(g_z, "ZSTD_versionNumber");
+    if (!z_comp || !z_decomp || !z_iserr || !z_bound || !z_ver) { set_err("zstd symbols missing"); return -1; }
+    return 0;
+}
+unsigned orc_zstd_version(void) { return z_load() ? 0 : z_ver(); }
+
+/* ------------------------------------------------------------ core context */
+
+typedef struct {
+    int N;
+    size_t dims[4], offs[4], num;
+    int levels;       /* interpolation_level after init() */
+    int anchor;
+    size_t maxStep;
+    int perms[24][4];
+    int nperm;
+    int *codes;
+    size_t ncodes, capcodes, qidx;
+} orc_ctx;
+
+typedef struct {
+    int interp, dir, blocksize, fixBlockSize;
+    double alpha, beta;
+    int nlist;
+    const uint8_t *interp_list, *dir_list;
+} orc_params;
+
+static void codes_push(orc_ctx *c, int v) {
+    if (c->ncodes == c->capcodes) {
+        c->capcodes = c->capcodes ? c->capcodes * 2 : 4096;
+        c->codes = (int *)realloc(c->codes, c->capcodes * sizeof(int));
+    }
+    c->codes[c->ncodes++] = v;
+}
+
+/* smallest L with 2^L >= d, i.e. ceil(log2(d)) for d >= 1 */
+static int ceil_log2(size_t d) {
+    int l = 0;
+    while (((size_t)1 << l) < d) l++;
+    return l;
+}
+
+/* SZInterpolationCompressor::init - SZInterpolationCompressor.hpp:820-852 */
+static void ctx_init(orc_ctx *c, int N, const size_t *dims, size_t maxStep) {
+    memset(c, 0, sizeof *c);
+    c->N = N;
+    c->num = 1;
+    c->levels = 0;
+    for (int i = 0; i < N; i++) {
+        c->dims[i] = dims[i];
+        c->num *= dims[i];
+        int l = ceil_log2(dims[i]);
+        if (l > c->levels) c->levels = l;
+    }
+    c->maxStep = maxStep;
+    if (maxStep > 0) {
+        c->anchor = 1;
+        c->levels += 1;
+        int lm = 0;
+        while (((size_t)1 << (lm + 1)) <= maxStep) lm++; /* floor(log2(maxStep)) */
+        lm += 1;
+        if (lm <= c->levels) c->levels = lm;
+    }
+    c->offs[N - 1] = 1;
+    for (int i = N - 2; i >= 0; i--) c->offs[i] = c->offs[i + 1] * dims[i + 1];
+    /* all permutations of 0..N-1 in lexicographic order (std::next_permutation) */
+    int seq[4];
+    for (int i = 0; i < N; i++) seq[i] = i;
+    c->nperm = 0;
+    for (;;) {
+        memcpy(c->perms[c->nperm++], seq, sizeof seq);
+        int i = N - 2;
+        while (i >= 0 && seq[i] >= seq[i + 1]) i--;
+        if (i < 0) break;
+        int j = N - 1;
+        while (seq[j] <= seq[i]) j--;
+        int t = seq[i]; seq[i] = seq[j]; seq[j] = t;
+        for (int a = i + 1, b = N - 1; a < b; a++, b--) { t = seq[a]; seq[a] = seq[b]; seq[b] = t; }
+    }
+}
+
+#define T float
+#define SFX f32
+#include "oracle_interp.inc"
+#undef T
+#undef SFX
+#define T double
+#define SFX f64
+#include "oracle_interp.inc"
+#undef T
+#undef SFX
+
+/* --------------------------------------------------------------- Huffman */
+
+/*
+ * Order in which ska::unordered_map<int,size_t> (filled by frequency[s[i]]++,
+ * HuffmanEncoder.hpp:534-537) yields its keys.  The table chains entries in
+ * power-of-two bucket arrays; a key's bucket is the top log2(B) bits of
+ * key * 11400714819323198485 (fibonacci_hash_policy); new keys go to the head
+ * of their chain; the table doubles (minimum 4 buckets) when an insert would
+ * exceed one entry per bucket, moving entries bucket 0..B-1, each chain head
+ * to tail, to the head of their new chain; iteration walks buckets from B-1
+ * down to 0, each chain head to tail.
+ */
+static void ska_order(const int *keys, size_t nkeys, int *order_out) {
+    size_t B = 0;       /* 0 = initial empty state (one sentinel bucket) */
+    int shift = 63;
+    int *head = NULL;
+    int *next = (int *)malloc((nkeys ? nkeys : 1) * sizeof(int));
+    for (size_t k = 0; k < nkeys; k++) {
+        if (B == 0 || k + 1 > B) {
+            size_t nbkt = B == 0 ? 4 : 2 * B;
+            if (nbkt < 4) nbkt = 4;
+            int lg = 0;
+            while (((size_t)1 << lg) < nbkt) lg++;
+            int *nh = (int *)malloc(nbkt * sizeof(int));
+            for (size_t i = 0; i < nbkt; i++) nh[i] = -1;
+            int nshift = 64 - lg;
+            for (size_t b = 0; b < B; b++) {
+                int e = head[b];
+                while (e >= 0) {
+                    int nx = next[e];
+                    size_t idx = (size_t)((uint64_t)(int64_t)keys[e] * 11400714819323198485ull >> nshift);
+                    next[e] = nh[idx];
+                    nh[idx] = e;
+                    e = nx;
+                }
+            }
+            free(head);
+            head = nh;
+            B = nbkt;
+            shift = nshift;
+        }
+        size_t idx = (size_t)((uint64_t)(int64_t)keys[k] * 11400714819323198485ull >> shift);
+        next[k] = head[idx];
+        head[idx] = (int)k;
+    }
+    size_t o = 0;
+    for (size_t b = B; b-- > 0;) {
+        for (int e = head[b]; e >= 0; e = next[e]) order_out[o++] = e;
+    }
+    free(head);
+    free(next);
+}
+
+typedef struct hnode {
+    struct hnode *left, *right;
+    size_t freq;
+    char t;
+    int c;
+} hnode;
+
+typedef struct {
+    hnode *pool;
+    int npool;
+    hnode **qq; /* heap, entries 1..qend-1 */
+    int qend;
+    uint64_t *code;
+    uint8_t *len;
+    int stateNum;
+    int offset;
+    int nodeCount;
+    hnode *root;
+} huff_t;
+
+/* qinsert / qremove - HuffmanEncoder.hpp:455-485 */
+static void h_insert(huff_t *h, hnode *n) {
+    int j, i = h->qend++;
+    while ((j = i >> 1)) {
+        if (h->qq[j]->freq <= n->freq) break;
+        h->qq[i] = h->qq[j];
+        i = j;
+    }
+    h->qq[i] = n;
+}
+static hnode *h_remove(huff_t *h) {
+    int i = 1, l;
+    hnode *n = h->qq[1];
+    if (h->qend < 2) return NULL;
+    h->qend--;
+    h->qq[1] = h->qq[h->qend];
+    while ((l = i << 1) < h->qend) {
+        if (l + 1 < h->qend && h->qq[l + 1]->freq < h->qq[l]->freq) l++;
+        if (h->qq[i]->freq > h->qq[l]->freq) {
+            hnode *p = h->qq[i];
+            h->qq[i] = h->qq[l];
+            h->qq[l] = p;
+            i = l;
+        } else break;
+    }
+    return n;
+}
+
+/* build_code - HuffmanEncoder.hpp:493-521, codes up to 64 bits */
+static void h_build(huff_t *h, hnode *n, int len, uint64_t out) {
+    if (n->t) {
+        h->code[n->c] = len == 0 ? 0 : (len <= 64 ? out << (64 - len) : out);
+        h->len[n->c] = (uint8_t)len;
+        return;
+    }
+    h_build(h, n->left, len + 1, out << 1);
+    h_build(h, n->right, len + 1, (out << 1) | 1);
+}
+
+/* init / preprocess_encode - HuffmanEncoder.hpp:93-116, 529-566 */
+static int huff_build(huff_t *h, const int *s, size_t n) {
+    memset(h, 0, sizeof *h);
+    int mx = s[0], mn = s[0];
+    for (size_t i = 0; i < n; i++) {
+        if (s[i] > mx) mx = s[i];
+        if (s[i] < mn) mn = s[i];
+    }
+    size_t range = (size_t)((int64_t)mx - mn + 1);
+    size_t *cnt = (size_t *)calloc(range, sizeof(size_t));
+    int *keys = (int *)malloc(range * sizeof(int));
+    size_t nk = 0;
+    for (size_t i = 0; i < n; i++) {
+        size_t k = (size_t)((int64_t)s[i] - mn);
+        if (cnt[k]++ == 0) keys[nk++] = s[i];
+    }
+    int *ord = (int *)malloc(nk * sizeof(int));
+    ska_order(keys, nk, ord);
+    h->offset = mn;
+    h->stateNum = mx - mn + 2;
+    h->pool = (hnode *)calloc((size_t)h->stateNum * 4, sizeof(hnode));
+    h->qq = (hnode **)calloc((size_t)h->stateNum * 4 + 2, sizeof(hnode *));
+    h->qend = 1;
+    h->code = (uint64_t *)calloc(h->stateNum, sizeof(uint64_t));
+    h->len = (uint8_t *)calloc(h->stateNum, 1);
+    for (size_t i = 0; i < nk; i++) {
+        int key = keys[ord[i]];
+        hnode *nd = &h->pool[h->npool++];
+        nd->c = key - mn;
+        nd->freq = cnt[key - mn];
+        nd->t = 1;
+        h_insert(h, nd);
+    }
+    while (h->qend > 2) {
+        /* new_node(0, 0, qremove(), qremove()): the reference's compiler
+         * evaluates the right argument first, so the first node removed
+         * becomes the right child. */
+        hnode *b = h_remove(h);
+        hnode *a = h_remove(h);
+        hnode *nd = &h->pool[h->npool++];
+        nd->left = a;
+        nd->right = b;
+        nd->freq = a->freq + b->freq;
+        nd->t = 0;
+        h_insert(h, nd);
+    }
+    h->root = h->qq[1];
+    h_build(h, h->root, 0, 0);
+    h->nodeCount = (int)(2 * nk - 1);
+    free(cnt);
+    free(keys);
+    free(ord);
+    return 0;
+}
+static void huff_free(huff_t *h) {
+    free(h->pool);
+    free(h->qq);
+    free(h->code);
+    free(h->len);
+}
+
+/* pad_tree preorder numbering - HuffmanEncoder.hpp:569-584 */
+static void h_pad(hnode *n, uint32_t i, uint32_t *L, uint32_t *R, int *C, uint8_t *t, uint32_t *ninode) {
+    C[i] = n->c;
+    t[i] = (uint8_t)n->t;
+    if (n->left) {
+        (*ninode)++;
+        L[i] = *ninode;
+        h_pad(n->left, *ninode, L, R, C, t, ninode);
+    }
+    if (n->right) {
+        (*ninode)++;
+        R[i] = *ninode;
+        h_pad(n->right, *ninode, L, R, C, t, ninode);
+    }
+}
+
+/* save - HuffmanEncoder.hpp:119-137, 607-633 */
+static void huff_save(huff_t *h, bytes_t *b) {
+    PUT(b, (int32_t)h->offset);
+    put_be32(b, h->nodeCount);
+    put_be32(b, h->stateNum / 2);
+    uint32_t nc = (uint32_t)h->nodeCount;
+    uint32_t *L = (uint32_t *)calloc(nc, 4), *R = (uint32_t *)calloc(nc, 4);
+    int *C = (int *)calloc(nc, 4);
+    uint8_t *t = (uint8_t *)calloc(nc, 1);
+    uint32_t ninode = 0;
+    h_pad(h->root, 0, L, R, C, t, &ninode);
+    uint8_t endian = 0;
+    b_put(b, &endian, 1);
+    int w = nc <= 256 ? 1 : (nc <= 65536 ? 2 : 4);
+    for (int pass = 0; pass < 2; pass++) {
+        uint32_t *A = pass ? R : L;
+        for (uint32_t i = 0; i < nc; i++) {
+            if (w == 1) { uint8_t v = (uint8_t)A[i]; b_put(b, &v, 1); }
+            else if (w == 2) { uint16_t v = (uint16_t)A[i]; b_put(b, &v, 2); }
+            else b_put(b, &A[i], 4);
+        }
+    }
+    b_put(b, C, (size_t)nc * 4);
+    b_put(b, t, nc);
+    free(L); free(R); free(C); free(t);
+}
+
+/* encode - HuffmanEncoder.hpp:150-227: size_t byte count, then the codes
+ * concatenated most-significant bit first. */
+static void huff_encode(huff_t *h, const int *s, size_t n, bytes_t *b) {
+    uint64_t bits = 0;
+    for (size_t i = 0; i < n; i++) bits += h->len[s[i] - h->offset];
+    uint64_t nbytes = (bits + 7) / 8;
+    PUT(b, (uint64_t)nbytes);
+    b_reserve(b, nbytes);
+    uint8_t *o = b->p + b->n;
+    memset(o, 0, nbytes);
+    uint64_t pos = 0;
+    for (size_t i = 0; i < n; i++) {
+        int st = s[i] - h->offset;
+        int l = h->len[st];
+        uint64_t c = h->code[st];
+        for (int k = 0; k < l; k++, pos++)
+            if ((c >> (63 - k)) & 1) o[pos >> 3] |= (uint8_t)(0x80 >> (pos & 7));
+    }
+    b->n += nbytes;
+}
+
+/* load + decode - HuffmanEncoder.hpp:236-296 */
+static int huff_decode(rd_t *r, size_t target, int *out) {
+    int32_t offset;
+    r_get(r, &offset, 4);
+    int32_t nodeCount = get_be32(r);
+    (void)get_be32(r);
+    if (r->bad || nodeCount <= 0) return -1;
+    uint32_t nc = (uint32_t)nodeCount;
+    int w = nc <= 256 ? 1 : (nc <= 65536 ? 2 : 4);
+    uint8_t endian;
+    r_get(r, &endian, 1);
+    uint32_t *L = (uint32_t *)calloc(nc, 4), *R = (uint32_t *)calloc(nc, 4);
+    int *C = (int *)calloc(nc, 4);
+    uint8_t *t = (uint8_t *)calloc(nc, 1);
+    for (int pass = 0; pass < 2; pass++) {
+        uint32_t *A = pass ? R : L;
+        for (uint32_t i = 0; i < nc; i++) {
+            if (w == 1) { uint8_t v; r_get(r, &v, 1); A[i] = v; }
+            else if (w == 2) { uint16_t v; r_get(r, &v, 2); A[i] = v; }
+            else r_get(r, &A[i], 4);
+        }
+    }
+    r_get(r, C, (size_t)nc * 4);
+    r_get(r, t, nc);
+    uint64_t enc;
+    r_get(r, &enc, 8);
+    if (r->bad || r->pos + enc > r->n) { free(L); free(R); free(C); free(t); return -1; }
+    const uint8_t *bits = r->p + r->pos;
+    int rc = 0;
+    /* a tree of more than 256 nodes is rebuilt with a non-leaf root */
+    int root_leaf = nc <= 256 ? t[0] : 0;
+    if (root_leaf) {
+        for (size_t i = 0; i < target; i++) out[i] = C[0] + offset;
+    } else {
+        uint32_t nd = 0;
+        size_t cnt = 0;
+        uint64_t i = 0;
+        while (cnt < target) {
+            if ((i >> 3) >= enc) { rc = -1; break; }
+            int bit = (bits[i >> 3] >> (7 - (i & 7))) & 1;
+            i++;
+            nd = bit ? R[nd] : L[nd];
+            if (nd == 0 || nd >= nc) { rc = -1; break; }
+            if (t[nd]) {
+                out[cnt++] = C[nd] + offset;
+                nd = 0;
+            }
+        }
+    }
+    r->pos += enc;
+    free(L); free(R); free(C); free(t);
+    return rc;
+}
+
+/* ----------------------------------------------------- config and trailer */
+
+/* Config::Config(Dims...) - Config.hpp:64-74, member defaults 394-499 */
+int orc_config_init(faz_config *c, int N, const uint64_t *dims) {
+    memset(c, 0, sizeof *c);
+    c->N = N;
+    c->num = 1;
+    for (int i = 0; i < N; i++) {
+        c->dims[i] = dims[i];
+        c->coeffs_dims[i] = dims[i];
+        c->num *= dims[i];
+    }
+    c->coeffs_dims_len = N;
+    c->coeffs_num = c->num;
+    c->cmprAlgo = FAZ_ALGO_INTERP_LORENZO;
+    c->errorBoundMode = FAZ_EB_ABS;
+    c->relErrorBound = -1.0;
+    c->rng = -1;
+    c->alpha = -1;
+    c->beta = -1;
+    c->lorenzo = 1;
+    c->regression = 1;
+    c->lossless = 1;
+    c->encoder = 1;
+    c->interpAlgo = FAZ_INTERP_ALGO_CUBIC;
+    c->interpBlockSize = 32;
+    c->quantbinCnt = 65536;
+    c->blockSize = N == 1 ? 128 : (N == 2 ? 16 : 6);
+    c->pred_dim = N;
+    c->stride = c->blockSize;
+    c->SSIMBlockSize = 8;
+    c->verbose = 1;
+    c->wavelet_rel_coeff = 0.75;
+    c->sperr = -1;
+    c->pyBind = 1;
+    return 0;
+}
+
+/* Config::save - Config.hpp:240-309 */
+static void conf_save(const faz_config *c, bytes_t *b) {
+    PUT(b, (char)c->N);
+    for (int i = 0; i < c->N; i++) PUT(b, (uint64_t)c->dims[i]);
+    PUT(b, (uint64_t)c->num);
+    PUT(b, c->cmprAlgo);
+    PUT(b, c->errorBoundMode);
+    PUT(b, c->tuningTarget);
+    PUT(b, c->absErrorBound);
+    PUT(b, c->relErrorBound);
+    PUT(b, c->alpha);
+    PUT(b, c->beta);
+    PUT(b, c->lorenzo);
+    PUT(b, c->lorenzo2);
+    PUT(b, c->regression);
+    PUT(b, c->regression2);
+    PUT(b, c->interpAlgo);
+    PUT(b, c->interpDirection);
+    PUT(b, c->interpBlockSize);
+    PUT(b, c->lossless);
+    PUT(b, c->encoder);
+    PUT(b, c->quantbinCnt);
+    PUT(b, c->blockSize);
+    PUT(b, c->levelwisePredictionSelection);
+    PUT(b, c->blockwiseTuning);
+    PUT(b, c->stride);
+    PUT(b, (uint64_t)c->maxStep);
+    PUT(b, c->pred_dim);
+    PUT(b, c->openmp);
+    PUT(b, c->fixBlockSize);
+    PUT(b, c->blockwiseSampleBlockSize);
+    PUT(b, c->crossBlock);
+    PUT(b, c->wavelet);
+    PUT(b, (uint64_t)c->firstSize);
+    PUT(b, c->offsetPredictor);
+    PUT(b, (uint64_t)c->coeffs_num);
+    if (c->coeffs_num > 0) {
+        PUT(b, (uint64_t)c->coeffs_dims_len);
+        for (int i = 0; i < c->coeffs_dims_len; i++) PUT(b, (uint64_t)c->coeffs_dims[i]);
+    }
+    PUT(b, c->pid);
+    PUT(b, c->blockOrder);
+    PUT(b, c->sperr);
+    PUT(b, c->sperrWithoutWave);
+    PUT(b, c->pyBind);
+    if (c->pyBind) PUT(b, (uint64_t)0); /* empty metadata string */
+    PUT(b, c->conditioning);
+    if (c->conditioning > 0) b_put(b, c->meta, 17);
+}
+
+/* Config::load - Config.hpp:311-388 */
+static int conf_load(faz_config *c, rd_t *r) {
+    char n;
+    r_get(r, &n, 1);
+    if (n < 1 || n > 4) return -1;
+    c->N = n;
+    for (int i = 0; i < n; i++) r_get(r, &c->dims[i], 8);
+    r_get(r, &c->num, 8);
+    r_get(r, &c->cmprAlgo, 1);
+    r_get(r, &c->errorBoundMode, 1);
+    r_get(r, &c->tuningTarget, 1);
+    r_get(r, &c->absErrorBound, 8);
+    r_get(r, &c->relErrorBound, 8);
+    r_get(r, &c->alpha, 8);
+    r_get(r, &c->beta, 8);
+    r_get(r, &c->lorenzo, 1);
+    r_get(r, &c->lorenzo2, 1);
+    r_get(r, &c->regression, 1);
+    r_get(r, &c->regression2, 1);
+    r_get(r, &c->interpAlgo, 1);
+    r_get(r, &c->interpDirection, 1);
+    r_get(r, &c->interpBlockSize, 4);
+    r_get(r, &c->lossless, 1);
+    r_get(r, &c->encoder, 1);
+    r_get(r, &c->quantbinCnt, 4);
+    r_get(r, &c->blockSize, 4);
+    r_get(r, &c->levelwisePredictionSelection, 4);
+    r_get(r, &c->blockwiseTuning, 1);
+    r_get(r, &c->stride, 4);
+    r_get(r, &c->maxStep, 8);
+    r_get(r, &c->pred_dim, 4);
+    r_get(r, &c->openmp, 1);
+    r_get(r, &c->fixBlockSize, 4);
+    r_get(r, &c->blockwiseSampleBlockSize, 4);
+    r_get(r, &c->crossBlock, 4);
+    r_get(r, &c->wavelet, 4);
+    r_get(r, &c->firstSize, 8);
+    r_get(r, &c->offsetPredictor, 4);
+    r_get(r, &c->coeffs_num, 8);
+    if (c->coeffs_num > 0) {
+        uint64_t len;
+        r_get(r, &len, 8);
+        if (len > 4) return -1;
+        c->coeffs_dims_len = (int)len;
+        for (uint64_t i = 0; i < len; i++) r_get(r, &c->coeffs_dims[i], 8);
+    }
+    r_get(r, &c->pid, 4);
+    r_get(r, &c->blockOrder, 4);
+    r_get(r, &c->sperr, 4);
+    r_get(r, &c->sperrWithoutWave, 1);
+    r_get(r, &c->pyBind, 1);
+    if (c->pyBind) {
+        uint64_t ms;
+        r_get(r, &ms, 8);
+        r->pos += ms;
+    }
+    r_get(r, &c->conditioning, 4);
+    if (c->conditioning > 0) r_get(r, c->meta, 17);
+    return r->bad ? -1 : 0;
+}
+
+/* data_range + calAbsErrorBound - Statistic.hpp:12-66 */
+static int eb_resolve(faz_config *c, int dtype, const void *data) {
+    if (c->errorBoundMode == FAZ_EB_ABS) return 0;
+    double rng;
+    if (dtype == FAZ_FLOAT) {
+        const float *d = (const float *)data;
+        float mx = d[0], mn = d[0];
+        for (size_t i = 1; i < c->num; i++) {
+            if (mx < d[i]) mx = d[i];
+            if (mn > d[i]) mn = d[i];
+        }
+        rng = (double)(float)(mx - mn);
+    } else {
+        const double *d = (const double *)data;
+        double mx = d[0], mn = d[0];
+        for (size_t i = 1; i < c->num; i++) {
+            if (mx < d[i]) mx = d[i];
+            if (mn > d[i]) mn = d[i];
+        }
+        rng = mx - mn;
+    }
+    switch (c->errorBoundMode) {
+    case FAZ_EB_REL:
+        c->absErrorBound = c->relErrorBound * rng;
+        break;
+    case FAZ_EB_PSNR: {
+        double v1 = c->psnrErrorBound + 10 * log10(1 - 2.0 / 3.0 * 0.99);
+        c->absErrorBound = rng * pow(10, v1 / (-20));
+        c->relErrorBound = c->absErrorBound / rng;
+        break;
+    }
+    case FAZ_EB_L2NORM:
+        c->absErrorBound = sqrt(3.0 / c->num) * c->l2normErrorBound;
+        break;
+    case FAZ_EB_ABS_AND_REL: {
+        double rr = c->relErrorBound * rng;
+        c->absErrorBound = c->absErrorBound < rr ? c->absErrorBound : rr;
+        break;
+    }
+    case FAZ_EB_ABS_OR_REL: {
+        double rr = c->relErrorBound * rng;
+        c->absErrorBound = c->absErrorBound > rr ? c->absErrorBound : rr;
+        break;
+    }
+    default:
+        set_err("error bound mode not supported");
+        return -1;
+    }
+    if (c->errorBoundMode != FAZ_EB_L2NORM) c->rng = rng;
+    c->errorBoundMode = FAZ_EB_ABS;
+    return 0;
+}
+
+/* ----------------------------------------------------------- public calls */
+
+/*
+ * Interpolation-only compression (the ALGO_INTERP body of
+ * SZInterpolationCompressor::compress, lines 324-529): returns the quantisation
+ * codes and unpredictable values in stream order plus the pre-zstd payload.
+ * `conf` must already hold an absolute error bound.
+ */
+int orc_interp_compress(const faz_config *conf, int dtype, const void *data, int **codes_out,
+                        size_t *ncodes, void **unpred_out, size_t *nunpred, uint8_t **payload,
+                        size_t *payload_size) {
+    orc_ctx c;
+    size_t dims[4];
+    for (int i = 0; i < conf->N; i++) dims[i] = conf->dims[i];
+    ctx_init(&c, conf->N, dims, conf->maxStep);
+    orc_params p = {conf->interpAlgo, conf->interpDirection, conf->interpBlockSize, conf->fixBlockSize,
+                    conf->alpha, conf->beta, conf->interp_list_len, conf->interpAlgo_list,
+                    conf->interpDirection_list};
+    if (conf->interpDirection >= c.nperm) { set_err("bad direction"); return -1; }
+    for (int i = 0; i < conf->interp_list_len; i++)
+        if (conf->interpDirection_list[i] >= c.nperm) { set_err("bad direction"); return -1; }
+    size_t es = dtype == FAZ_FLOAT ? 4 : 8;
+    void *work = malloc(c.num * es);
+    memcpy(work, data, c.num * es);
+    void *unpred;
+    size_t nun;
+    double eb;
+    int radius = conf->quantbinCnt / 2;
+    if (dtype == FAZ_FLOAT) {
+        run_f32 r; memset(&r, 0, sizeof r); r.c = &c; r.data = (float *)work;
+        r.q.radius = radius;
+        r.q.trim = conf->trimToZero;
+        q_set_eb_f32(&r.q, conf->absErrorBound);
+        levels_f32(&r, &p);
+        unpred = r.q.unpred;
+        nun = r.q.nunpred;
+        eb = r.q.eb;
+    } else {
+        run_f64 r; memset(&r, 0, sizeof r); r.c = &c; r.data = (double *)work;
+        r.q.radius = radius;
+        r.q.trim = conf->trimToZero;
+        q_set_eb_f64(&r.q, conf->absErrorBound);
+        levels_f64(&r, &p);
+        unpred = r.q.unpred;
+        nun = r.q.nunpred;
+        eb = r.q.eb;
+    }
+    free(work);
+    /* stream header - SZInterpolationCompressor.hpp:485-512 */
+    bytes_t b = {0};
+    for (int i = 0; i < conf->N; i++) PUT(&b, (uint64_t)conf->dims[i]);
+    PUT(&b, (uint32_t)conf->interpBlockSize);
+    PUT(&b, (int32_t)conf->interpAlgo);
+    PUT(&b, (int32_t)conf->interpDirection);
+    PUT(&b, conf->alpha);
+    PUT(&b, conf->beta);
+    PUT(&b, (uint64_t)conf->maxStep);
+    PUT(&b, (int32_t)conf->interp_list_len);
+    PUT(&b, (uint8_t)conf->blockwiseTuning);
+    PUT(&b, (int32_t)conf->fixBlockSize);
+    PUT(&b, (uint64_t)conf->crossBlock);
+    PUT(&b, (int32_t)conf->trimToZero);
+    PUT(&b, (int32_t)conf->blockOrder);
+    if (conf->interp_list_len > 0) {
+        b_put(&b, conf->interpAlgo_list, conf->interp_list_len);
+        b_put(&b, conf->interpDirection_list, conf->interp_list_len);
+    }
+    /* LinearQuantizer::save - IntegerQuantizer.hpp:185-201 */
+    PUT(&b, (uint8_t)2);
+    PUT(&b, eb);
+    PUT(&b, (int32_t)radius);
+    PUT(&b, (uint64_t)nun);
+    b_put(&b, unpred, nun * es);
+    huff_t h;
+    huff_build(&h, c.codes, c.ncodes);
+    huff_save(&h, &b);
+    huff_encode(&h, c.codes, c.ncodes, &b);
+    huff_free(&h);
+    if (codes_out) *codes_out = c.codes; else free(c.codes);
+    if (ncodes) *ncodes = c.ncodes;
+    if (unpred_out) *unpred_out = unpred; else free(unpred);
+    if (nunpred) *nunpred = nun;
+    *payload = b.p;
+    *payload_size = b.n;
+    return 0;
+}
+
+/* SZ_compress<T> with cmprAlgo == ALGO_INTERP: error bound, interpolation
+ * payload, Lossless_zstd framing, Config trailer, int32 trailer size. */
+int orc_compress(const faz_config *conf_in, int dtype, const void *data, uint8_t **out, size_t *out_size,
+                 uint8_t **payload_out, size_t *payload_size_out) {
+    faz_config conf = *conf_in;
+    if (conf.N < 1 || conf.N > 4) { set_err("N must be 1..4"); return -1; }
+    if (conf.cmprAlgo != FAZ_ALGO_INTERP) { set_err("oracle covers ALGO_INTERP"); return -2; }
+    if (eb_resolve(&conf, dtype, data)) return -1;
+    uint8_t *payload;
+    size_t psize;
+    if (orc_interp_compress(&conf, dtype, data, NULL, NULL, NULL, NULL, &payload, &psize)) return -1;
+    if (z_load()) { free(payload); return -5; }
+    bytes_t b = {0};
+    PUT(&b, (uint64_t)psize);
+    size_t bound = z_bound(psize);
+    b_reserve(&b, bound);
+    size_t zs = z_comp(b.p + b.n, bound, payload, psize, 3);
+    if (z_iserr(zs)) { free(payload); free(b.p); set_err("zstd compress failed"); return -5; }
+    b.n += zs;
+    size_t before = b.n;
+    conf_save(&conf, &b);
+    PUT(&b, (int32_t)(b.n - before));
+    if (payload_out) { *payload_out = payload; *payload_size_out = psize; }
+    else free(payload);
+    *out = b.p;
+    *out_size = b.n;
+    return 0;
+}
+
+/* Split a stream into payload (zstd-decompressed) and trailer config. */
+int orc_read_stream(const uint8_t *cmp, size_t cmp_size, faz_config *conf, uint8_t **payload,
+                    size_t *payload_size) {
+    if (cmp_size < 4) { set_err("stream too short"); return -4; }
+    int32_t cs;
+    memcpy(&cs, cmp + cmp_size - 4, 4);
+    if (cs <= 0 || (size_t)cs + 4 > cmp_size) { set_err("bad trailer size"); return -4; }
+    rd_t r = {cmp + cmp_size - 4 - cs, (size_t)cs, 0, 0};
+    memset(conf, 0, sizeof *conf);
+    if (conf_load(conf, &r)) { set_err("bad trailer"); return -4; }
+    size_t body = cmp_size - 4 - cs;
+    if (body < 8) { set_err("stream too short"); return -4; }
+    uint64_t raw;
+    memcpy(&raw, cmp, 8);
+    if (z_load()) return -5;
+    uint8_t *p = (uint8_t *)malloc(raw ? raw : 1);
+    size_t got = z_decomp(p, raw, cmp + 8, body - 8);
+    if (z_iserr(got) || got != raw) { free(p); set_err("zstd decompress failed"); return -5; }
+    *payload = p;
+    *payload_size = raw;
+    return 0;
+}
+
+/* SZ_decompress<T> / SZInterpolationCompressor::decompress (lines 42-199) */
+int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, faz_config *conf_out) {
+    faz_config conf;
+    uint8_t *payload;
+    size_t psize;
+    int rc = orc_read_stream(cmp, cmp_size, &conf, &payload, &psize);
+    if (rc) return rc;
+    if (conf.cmprAlgo != FAZ_ALGO_INTERP || conf.blockwiseTuning) {
+        free(payload);
+        set_err("oracle decodes ALGO_INTERP streams");
+        return -2;
+    }
+    rd_t r = {payload, psize, 0, 0};
+    int N = conf.N;
+    size_t dims[4];
+    for (int i = 0; i < N; i++) { uint64_t v; r_get(&r, &v, 8); dims[i] = v; }
+    uint32_t bsz;
+    int32_t interp, dir, nlist, fixbs, trim, border;
+    double alpha, beta;
+    uint64_t maxStep, cross;
+    uint8_t bwt;
+    r_get(&r, &bsz, 4);
+    r_get(&r, &interp, 4);
+    r_get(&r, &dir, 4);
+    r_get(&r, &alpha, 8);
+    r_get(&r, &beta, 8);
+    r_get(&r, &maxStep, 8);
+    r_get(&r, &nlist, 4);
+    r_get(&r, &bwt, 1);
+    r_get(&r, &fixbs, 4);
+    r_get(&r, &cross, 8);
+    r_get(&r, &trim, 4);
+    r_get(&r, &border, 4);
+    uint8_t il[FAZ_MAX_LEVELS], dl[FAZ_MAX_LEVELS];
+    if (nlist < 0 || nlist > FAZ_MAX_LEVELS) { free(payload); set_err("bad level list"); return -4; }
+    if (nlist > 0) { r_get(&r, il, nlist); r_get(&r, dl, nlist); }
+    uint8_t qtag;
+    double eb;
+    int32_t radius;
+    uint64_t nun;
+    r_get(&r, &qtag, 1);
+    r_get(&r, &eb, 8);
+    r_get(&r, &radius, 4);
+    r_get(&r, &nun, 8);
+    size_t es = dtype == FAZ_FLOAT ? 4 : 8;
+    if (r.bad || r.pos + nun * es > r.n) { free(payload); set_err("truncated payload"); return -4; }
+    const uint8_t *unp = r.p + r.pos;
+    r.pos += nun * es;
+    orc_ctx c;
+    ctx_init(&c, N, dims, maxStep);
+    c.codes = (int *)malloc(c.num * sizeof(int));
+    c.ncodes = c.num;
+    if (huff_decode(&r, c.num, c.codes)) { free(payload); free(c.codes); set_err("bad Huffman data"); return -4; }
+    orc_params p = {interp, dir, (int)bsz, fixbs, alpha, beta, nlist, il, dl};
+    void *dec = malloc(c.num * es);
+    if (dtype == FAZ_FLOAT) {
+        run_f32 rr; memset(&rr, 0, sizeof rr); rr.c = &c; rr.data = (float *)dec; rr.decompress = 1;
+        rr.q.radius = radius;
+        rr.q.trim = trim;
+        rr.q.unpred = (float *)malloc(nun * 4 + 4);
+        memcpy(rr.q.unpred, unp, nun * 4);
+        rr.q.nunpred = nun;
+        q_set_eb_f32(&rr.q, eb);
+        levels_f32(&rr, &p);
+        free(rr.q.unpred);
+    } else {
+        run_f64 rr; memset(&rr, 0, sizeof rr); rr.c = &c; rr.data = (double *)dec; rr.decompress = 1;
+        rr.q.radius = radius;
+        rr.q.trim = trim;
+        rr.q.unpred = (double *)malloc(nun * 8 + 8);
+        memcpy(rr.q.unpred, unp, nun * 8);
+        rr.q.nunpred = nun;
+        q_set_eb_f64(&rr.q, eb);
+        levels_f64(&rr, &p);
+        free(rr.q.unpred);
+    }
+    free(c.codes);
+    free(payload);
+    *out = dec;
+    if (conf_out) *conf_out = conf;
+    return 0;
+}
+
+void orc_free(void *p) { free(p); }
+
+/* The order ska_order() gives, exposed for tests. */
+void orc_ska_order(const int *keys, size_t n, int *order) { ska_order(keys, n, order); }

@@ -1,0 +1,151 @@
+"""ctypes front end of the CPU oracle (oracle/faz_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the checker for the CUDA path.  Used by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg; never by the product.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SRC = [os.path.join(HERE, "faz_oracle.c"), os.path.join(HERE, "oracle_interp.inc"),
+       os.path.join(HERE, "..", "include", "faz_gb300.h")]
+REF_ZSTD = os.path.join(HERE, "_ref", "libzstd145.so")
+
+_lib = None
+
+
+def build(force=False):
+    """Compile liboracle.so with gcc (no FMA contraction, IEEE semantics)."""
+    stale = force or not os.path.exists(LIB) or any(
+        os.path.getmtime(s) > os.path.getmtime(LIB) for s in SRC)
+    if stale:
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+                               "-o", LIB, SRC[0], "-ldl", "-lm"])
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        from faz_gb300.config import FazConfigStruct  # noqa: F401  (layout shared with the C ABI)
+        P = ctypes.POINTER
+        L.orc_compress.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, P(ctypes.c_void_p),
+                                   P(ctypes.c_size_t), P(ctypes.c_void_p), P(ctypes.c_size_t)]
+        L.orc_interp_compress.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, P(ctypes.c_void_p),
+                                          P(ctypes.c_size_t), P(ctypes.c_void_p), P(ctypes.c_size_t),
+                                          P(ctypes.c_void_p), P(ctypes.c_size_t)]
+        L.orc_decompress.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, P(ctypes.c_void_p),
+                                     ctypes.c_void_p]
+        L.orc_read_stream.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, P(ctypes.c_void_p),
+                                      P(ctypes.c_size_t)]
+        L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_zstd_version.restype = ctypes.c_uint
+        L.orc_set_zstd.argtypes = [ctypes.c_char_p]
+        L.orc_free.argtypes = [ctypes.c_void_p]
+        L.orc_ska_order.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def set_zstd(path=None):
+    """Point the oracle at a zstd library (default: the system libzstd.so.1)."""
+    lib().orc_set_zstd(path.encode() if path else None)
+
+
+def zstd_version():
+    return lib().orc_zstd_version()
+
+
+def _dtype_code(arr):
+    if arr.dtype == np.float32:
+        return 0
+    if arr.dtype == np.float64:
+        return 1
+    raise TypeError("float32 or float64 only")
+
+
+def _take(ptr, n):
+    if n == 0:
+        lib().orc_free(ptr)
+        return b""
+    out = ctypes.string_at(ptr, n)
+    lib().orc_free(ptr)
+    return out
+
+
+def compress(conf, data):
+    """Full stream (payload | trailer | int32) and the pre-zstd payload."""
+    data = np.ascontiguousarray(data)
+    s = conf.to_struct()
+    out, osz, pay, psz = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_void_p(), ctypes.c_size_t()
+    rc = lib().orc_compress(ctypes.byref(s), _dtype_code(data), data.ctypes.data, ctypes.byref(out),
+                            ctypes.byref(osz), ctypes.byref(pay), ctypes.byref(psz))
+    if rc:
+        raise RuntimeError(f"oracle compress failed ({rc}): {lib().orc_last_error().decode()}")
+    return _take(out, osz.value), _take(pay, psz.value)
+
+
+def interp_codes(conf, data):
+    """Quantisation codes (int32, stream order), unpredictable values and payload.
+
+    `conf` must carry an absolute error bound (errorBoundMode ABS)."""
+    data = np.ascontiguousarray(data)
+    s = conf.to_struct()
+    codes, nc = ctypes.c_void_p(), ctypes.c_size_t()
+    unp, nu = ctypes.c_void_p(), ctypes.c_size_t()
+    pay, psz = ctypes.c_void_p(), ctypes.c_size_t()
+    rc = lib().orc_interp_compress(ctypes.byref(s), _dtype_code(data), data.ctypes.data, ctypes.byref(codes),
+                                   ctypes.byref(nc), ctypes.byref(unp), ctypes.byref(nu), ctypes.byref(pay),
+                                   ctypes.byref(psz))
+    if rc:
+        raise RuntimeError(f"oracle compress failed ({rc}): {lib().orc_last_error().decode()}")
+    c = np.frombuffer(_take(codes, nc.value * 4), dtype=np.int32).copy()
+    u = np.frombuffer(_take(unp, nu.value * data.itemsize), dtype=data.dtype).copy()
+    return c, u, _take(pay, psz.value)
+
+
+def decompress(stream, dtype=np.float32):
+    from faz_gb300.config import Config, FazConfigStruct
+    dtype = np.dtype(dtype)
+    buf = ctypes.create_string_buffer(bytes(stream), len(stream))
+    out = ctypes.c_void_p()
+    cs = FazConfigStruct()
+    rc = lib().orc_decompress(buf, len(stream), 0 if dtype == np.float32 else 1, ctypes.byref(out),
+                              ctypes.byref(cs))
+    if rc:
+        raise RuntimeError(f"oracle decompress failed ({rc}): {lib().orc_last_error().decode()}")
+    num = int(cs.num)
+    arr = np.frombuffer(_take(out, num * dtype.itemsize), dtype=dtype).copy()
+    conf = Config.from_struct(cs)
+    return arr.reshape(conf.dims), conf
+
+
+def read_stream(stream):
+    """(Config, pre-zstd payload) of a stream."""
+    from faz_gb300.config import Config, FazConfigStruct
+    buf = ctypes.create_string_buffer(bytes(stream), len(stream))
+    cs = FazConfigStruct()
+    pay, psz = ctypes.c_void_p(), ctypes.c_size_t()
+    rc = lib().orc_read_stream(buf, len(stream), ctypes.byref(cs), ctypes.byref(pay), ctypes.byref(psz))
+    if rc:
+        raise RuntimeError(f"oracle read_stream failed ({rc}): {lib().orc_last_error().decode()}")
+    return Config.from_struct(cs), _take(pay, psz.value)
+
+
+def ska_order(keys):
+    keys = np.ascontiguousarray(keys, dtype=np.int32)
+    order = np.zeros(len(keys), dtype=np.int32)
+    lib().orc_ska_order(keys.ctypes.data, len(keys), order.ctypes.data)
+    return order
+
+
+def trailer_firstsize_span(N):
+    """Byte range of Config::firstSize inside the trailer (never initialised
+    by the reference on this path)."""
+    return 102 + 8 * N, 110 + 8 * N

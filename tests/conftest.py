@@ -1,0 +1,154 @@
+import configparser
+import json
+import os
+import struct
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
+
+
+def pytest_collection_modifyitems(config, items):
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        return
+    skip = pytest.mark.skip(reason="no CUDA device")
+    for it in items:
+        if "gpu" in it.keywords:
+            it.add_marker(skip)
+
+
+def golden_manifest():
+    with open(os.path.join(GOLDEN, "manifest.json")) as f:
+        return json.load(f)["cases"]
+
+
+def golden_case(name):
+    for c in golden_manifest():
+        if c["name"] == name:
+            return c
+    raise KeyError(name)
+
+
+def golden_input(case):
+    arr = np.fromfile(os.path.join(GOLDEN, case["name"] + ".in"), dtype=np.dtype(case["dtype"]))
+    return arr.reshape(case["dims"])
+
+
+def golden_stream(case):
+    with open(os.path.join(GOLDEN, case["name"] + ".faz"), "rb") as f:
+        return f.read()
+
+
+# INI keys of QoZ::Config::loadcfg (include/QoZ/utils/Config.hpp:91-233) used by the fixtures
+_INI_INT = {"InterpDirection": "interpDirection", "InterpBlockSize": "interpBlockSize",
+            "fixBlockSize": "fixBlockSize", "trimToZero": "trimToZero", "maxStep": "maxStep",
+            "QuantizationBinTotal": "quantbinCnt", "blockOrder": "blockOrder"}
+_INI_REAL = {"alpha": "alpha", "beta": "beta"}
+
+
+def cli_config(case):
+    """Config as the reference CLI builds it from the case's flags and INI."""
+    from faz_gb300.config import (Config, ALGO_STR, INTERP_ALGO_STR, EB_ABS, EB_REL, EB_ABS_AND_REL)
+    conf = Config(*case["dims"])
+    flags = list(case["flags"])
+    if "-q" in flags:
+        conf.QoZ = 1
+    if "-C" in flags:
+        conf.maxStep = int(flags[flags.index("-C") + 1])
+    ini = case["ini"]
+    if ini:
+        cp = configparser.ConfigParser()
+        cp.optionxform = str
+        cp.read_dict(ini)
+        g = cp["GlobalSettings"] if cp.has_section("GlobalSettings") else {}
+        a = cp["AlgoSettings"] if cp.has_section("AlgoSettings") else {}
+        if "CmprAlgo" in g:
+            conf.cmprAlgo = ALGO_STR.index(g["CmprAlgo"])
+        if "InterpolationAlgo" in a:
+            conf.interpAlgo = INTERP_ALGO_STR.index(a["InterpolationAlgo"])
+        for k, f in _INI_INT.items():
+            if k in a:
+                setattr(conf, f, int(a[k]))
+        for k, f in _INI_REAL.items():
+            if k in a:
+                setattr(conf, f, float(a[k]))
+    m = flags.index("-M")
+    mode = flags[m + 1]
+    val = flags[m + 2] if m + 2 < len(flags) and not flags[m + 2].startswith("-") else None
+    if "-A" in flags:
+        conf.absErrorBound = float(flags[flags.index("-A") + 1])
+    if "-R" in flags:
+        conf.relErrorBound = float(flags[flags.index("-R") + 1])
+    if mode == "ABS":
+        conf.errorBoundMode = EB_ABS
+        if val:
+            conf.absErrorBound = float(val)
+    elif mode == "REL":
+        conf.errorBoundMode = EB_REL
+        if val:
+            conf.relErrorBound = float(val)
+    elif mode == "ABS_AND_REL":
+        conf.errorBoundMode = EB_ABS_AND_REL
+    else:
+        raise ValueError(mode)
+    return conf
+
+
+def parse_interp_header(payload, N):
+    """Decisions recorded in an interpolation stream header
+    (include/QoZ/compressor/SZInterpolationCompressor.hpp:489-512)."""
+    o = 8 * N
+    bs, interp, direction = struct.unpack_from("<Iii", payload, o)
+    o += 12
+    alpha, beta, max_step = struct.unpack_from("<ddQ", payload, o)
+    o += 24
+    (nlist,) = struct.unpack_from("<i", payload, o)
+    o += 4
+    bwt = payload[o]
+    o += 1
+    (fixbs,) = struct.unpack_from("<i", payload, o)
+    o += 4
+    (cross,) = struct.unpack_from("<Q", payload, o)
+    o += 8
+    trim, border = struct.unpack_from("<ii", payload, o)
+    o += 8
+    il = list(payload[o:o + nlist])
+    dl = list(payload[o + nlist:o + 2 * nlist])
+    return dict(blocksize=bs, interp=interp, direction=direction, alpha=alpha, beta=beta, maxStep=max_step,
+                nlist=nlist, blockwise=bwt, fixBlockSize=fixbs, crossBlock=cross, trimToZero=trim,
+                blockOrder=border, interp_list=il, dir_list=dl)
+
+
+def tuned_config(case):
+    """Config that reproduces a tuner-written interpolation stream without
+    running the tuner: the trailer's settings plus the header's decisions."""
+    import oracle.oracle as O
+    stream = golden_stream(case)
+    conf, payload = O.read_stream(stream)
+    h = parse_interp_header(payload, conf.N)
+    conf.interpAlgo_list = h["interp_list"]
+    conf.interpDirection_list = h["dir_list"]
+    return conf
+
+
+def mask_first_size(stream):
+    """Zero the trailer's Config::firstSize bytes (never set by the reference)."""
+    (cs,) = struct.unpack_from("<i", stream, len(stream) - 4)
+    t0 = len(stream) - 4 - cs
+    N = stream[t0]
+    a, b = 102 + 8 * N, 110 + 8 * N
+    return stream[:t0 + a] + b"\0" * (b - a) + stream[t0 + b:]

@@ -1,0 +1,145 @@
+"""Generate the golden fixtures in this folder from the reference build.
+
+Each case: a seeded input field (<name>.in, raw little-endian) and the stream
+the reference `faz` tool writes for it (<name>.faz).  The array the reference
+decompresses from that stream is recorded by its SHA-256 (dec_sha256 in
+manifest.json), which also lists the command line, INI settings, dtype and
+dims of every case.  (A single-point field is not a case: the reference
+aborts in free() on it.)
+
+The reference tool is oracle/_ref/faz, built from the reference sources by
+oracle/build_ref.sh (with its bundled zstd 1.4.5).  Run from the repository
+root:  python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+from faz_gb300.fields import spectral_field  # noqa: E402
+
+FAZ = os.path.join(ROOT, "oracle", "_ref", "faz")
+
+
+def random_walk(shape, seed, dtype=np.float32):
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal(shape)
+    for ax in range(len(shape)):
+        a = np.cumsum(a, axis=ax)
+    return a.astype(dtype)
+
+
+def cases():
+    """(name, array, cli flags, ini dict)"""
+    interp_cubic = {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP"},
+                    "AlgoSettings": {"InterpolationAlgo": "INTERP_ALGO_CUBIC"}}
+    interp_linear = {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP"},
+                     "AlgoSettings": {"InterpolationAlgo": "INTERP_ALGO_LINEAR"}}
+
+    def ini(extra_algo=None, base=interp_cubic):
+        d = {k: dict(v) for k, v in base.items()}
+        if extra_algo:
+            d["AlgoSettings"].update(extra_algo)
+        return d
+
+    out = []
+    out.append(("c3d_cubic_walk", random_walk((20, 30, 40), 1), ["-M", "REL", "1e-3"], ini()))
+    out.append(("c3d_linear", spectral_field((33, 17, 65), slope=-3.0, seed=2), ["-M", "REL", "1e-2"],
+                ini(base=interp_linear)))
+    out.append(("c3d_noisy_1e4", spectral_field((48, 48, 48), slope=-2.0, noise=0.05, seed=3),
+                ["-M", "REL", "1e-4"], ini()))
+    out.append(("c3d_spec_1e3", spectral_field((40, 56, 72), slope=-3.5, aniso=(1, 2, 4), seed=4),
+                ["-M", "REL", "1e-3"], ini()))
+    out.append(("c2d_cubic", spectral_field((100, 150), slope=-3.0, seed=5), ["-M", "REL", "1e-3"], ini()))
+    out.append(("c1d_cubic", spectral_field((5000,), slope=-2.5, seed=6), ["-M", "REL", "1e-3"], ini()))
+    out.append(("c3d_f64", spectral_field((20, 30, 40), slope=-3.0, seed=7, dtype=np.float64),
+                ["-M", "REL", "1e-5"], ini()))
+    out.append(("c3d_anchor_ab", spectral_field((40, 40, 40), slope=-3.0, seed=8), ["-M", "REL", "1e-3", "-C", "16"],
+                ini({"alpha": "1.5", "beta": "2.0"})))
+    out.append(("c3d_alpha_lt1", spectral_field((36, 28, 44), slope=-3.0, seed=9), ["-M", "REL", "1e-3"],
+                ini({"alpha": "0.5", "beta": "0.25"})))
+    out.append(("c3d_dir5_abs", spectral_field((24, 36, 20), slope=-3.0, seed=10), ["-M", "ABS", "0.05"],
+                ini({"InterpDirection": "5"})))
+    out.append(("c3d_dir3_linear", spectral_field((24, 20, 36), slope=-3.0, seed=11), ["-M", "REL", "1e-3"],
+                ini({"InterpDirection": "3"}, base=interp_linear)))
+    out.append(("c3d_fixbs8", spectral_field((30, 30, 30), slope=-3.0, seed=12), ["-M", "REL", "1e-3"],
+                ini({"fixBlockSize": "8"})))
+    out.append(("c3d_ibs16", spectral_field((34, 30, 50), slope=-3.0, seed=13), ["-M", "REL", "1e-3"],
+                ini({"InterpBlockSize": "16"})))
+    out.append(("c4d_cubic", spectral_field((6, 7, 8, 9), slope=-3.0, seed=14), ["-M", "REL", "1e-3"], ini()))
+    out.append(("tiny_2x3x4", spectral_field((2, 3, 4), slope=-3.0, seed=15), ["-M", "REL", "1e-3"], ini()))
+    out.append(("tiny_5x5x5", spectral_field((5, 5, 5), slope=-3.0, seed=16), ["-M", "REL", "1e-3"], ini()))
+    out.append(("tiny_7x1x9", spectral_field((7, 1, 9), slope=-3.0, seed=17), ["-M", "REL", "1e-3"], ini()))
+    out.append(("const_16", np.full((16, 16, 16), 7.5, dtype=np.float32), ["-M", "ABS", "0.01"], ini()))
+    out.append(("trim1", spectral_field((32, 32, 32), slope=-3.0, seed=18, lo=-1, hi=1), ["-M", "ABS", "0.05"],
+                ini({"trimToZero": "1"})))
+    out.append(("trim2", spectral_field((32, 32, 32), slope=-3.0, seed=19, lo=-1, hi=1), ["-M", "ABS", "0.05"],
+                ini({"trimToZero": "2"})))
+    out.append(("c2d_abs_and_rel", spectral_field((64, 96), slope=-3.0, seed=20),
+                ["-M", "ABS_AND_REL", "-A", "0.5", "-R", "1e-3"], ini()))
+    out.append(("c3d_spikes", spectral_field((40, 40, 40), slope=-3.0, seed=21, spikes=0.05),
+                ["-M", "REL", "1e-3"], ini()))
+    out.append(("c3d_odd_65", spectral_field((65, 33, 17), slope=-3.0, seed=22), ["-M", "REL", "1e-3"], ini()))
+    # tuner-driven streams: the stream header records the tuner's decisions
+    out.append(("qoz_48", spectral_field((48, 48, 48), slope=-3.0, seed=23), ["-M", "REL", "1e-3", "-q"],
+                None))
+    out.append(("sz3_48", spectral_field((48, 48, 48), slope=-3.0, seed=24), ["-M", "REL", "1e-3"], None))
+    return out
+
+
+def write_ini(path, d):
+    with open(path, "w") as f:
+        for sec, kv in d.items():
+            f.write(f"[{sec}]\n")
+            for k, v in kv.items():
+                f.write(f"{k} = {v}\n")
+
+
+def sha(path):
+    return hashlib.sha256(open(path, "rb").read()).hexdigest()
+
+
+def main():
+    if not os.path.exists(FAZ):
+        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    manifest = []
+    for name, arr, flags, ini in cases():
+        arr = np.ascontiguousarray(arr)
+        dims = list(arr.shape)
+        inp = os.path.join(HERE, name + ".in")
+        arr.tofile(inp)
+        dt = "-f" if arr.dtype == np.float32 else "-d"
+        cli_dims = [f"-{len(dims)}"] + [str(d) for d in reversed(dims)]
+        with tempfile.TemporaryDirectory() as td:
+            # "-F 0" goes first: the reference parses it with sscanf("%d") into
+            # a bool, which overwrites neighbouring option variables
+            # (test/faz.cpp:327-332), so options given before it can be lost.
+            cmd = [FAZ, dt, "-F", "0", "-i", inp, "-z", os.path.join(HERE, name + ".faz")] + cli_dims + flags
+            if ini is not None:
+                ip = os.path.join(td, "cfg.ini")
+                write_ini(ip, ini)
+                cmd += ["-c", ip]
+            subprocess.check_call(cmd, cwd=td, stdout=subprocess.DEVNULL)
+            dcmd = [FAZ, dt, "-z", os.path.join(HERE, name + ".faz"), "-o", os.path.join(HERE, name + ".dec")] + \
+                cli_dims + ["-M", "ABS", "1"]
+            subprocess.check_call(dcmd, cwd=td, stdout=subprocess.DEVNULL)
+        decp = os.path.join(HERE, name + ".dec")
+        manifest.append({"name": name, "dtype": str(arr.dtype), "dims": dims, "flags": flags, "ini": ini,
+                         "sha256": {ext: sha(os.path.join(HERE, name + ext)) for ext in (".in", ".faz")},
+                         "dec_sha256": sha(decp)})
+        os.remove(decp)
+        print(name, os.path.getsize(os.path.join(HERE, name + ".faz")))
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "reference_tool": "oracle/_ref/faz (zstd 1.4.5)",
+                   "cases": manifest}, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
