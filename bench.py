@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""FAZ interpolation compress/decompress benchmark on GB300.
+
+Workload: one 512x512x512 float32 spectral field (k^-3.5, anisotropic
+correlation lengths 1:2:4, 1% noise, seeded, synthetic), relative error bound
+1e-3, cubic interpolation (ALGO_INTERP).  A step is one compression of the
+field; decompression is timed the same way and reported beside it.
+
+  value       compress GB/s (input bytes / time) with the field resident in
+              HBM, through the GPU path up to the pre-zstd payload in host
+              memory (CUDA events on the call's stream).
+  e2e         compress GB/s through SZ_compress (host input in pinned
+              memory, host->device copy, GPU path, payload copy back, host
+              zstd, trailer), host clock.
+  roofline    the finest interpolation level kernel (the dominant kernel):
+              algorithmic bytes per launch / CUDA-event duration vs the
+              measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (a restatement of the reference) on a slab
+              of the same field, one thread.
+
+--impl reference times the CPU restatement of the reference on all host
+cores (one slab per worker process) on the same metric.
+Under torchrun every rank compresses its own field (independent replicas,
+weak scaling); rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "compress/decompress GB/s + ratio at rel eb 1e-3; learned vs sampled autotune"
+L2_BYTES = 129e6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dims", default="512,512,512")
+    ap.add_argument("--eb", type=float, default=1e-3)
+    ap.add_argument("--interp", default="cubic", choices=["cubic", "linear"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        if self.p is None:
+            return None
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_conf(F, dims, eb, interp):
+    c = F.Config(*dims)
+    c.cmprAlgo = F.ALGO_INTERP
+    c.interpAlgo = F.INTERP_ALGO_CUBIC if interp == "cubic" else F.INTERP_ALGO_LINEAR
+    c.errorBoundMode = F.EB_REL
+    c.relErrorBound = eb
+    return c
+
+
+def finest_level_bytes(dims, itemsize):
+    """Algorithmic bytes of the finest level kernel: each target point read
+    once and its 2-byte code written once, each coarse point read once."""
+    n = 1
+    coarse = 1
+    for d in dims:
+        n *= d
+        coarse *= (d + 1) // 2
+    return (n - coarse) * (itemsize + 2) + coarse * itemsize
+
+
+# ------------------------------------------------------------- CPU oracle
+def _cpu_slab_job(args):
+    path, shape, offset, eb, interp, reps = args
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    import faz_gb300.config as C
+    x = np.fromfile(path, dtype=np.float32, count=int(np.prod(shape)), offset=offset).reshape(shape)
+    conf = C.Config(*shape)
+    conf.cmprAlgo = C.ALGO_INTERP
+    conf.interpAlgo = C.INTERP_ALGO_CUBIC if interp == "cubic" else C.INTERP_ALGO_LINEAR
+    conf.errorBoundMode = C.EB_REL
+    conf.relErrorBound = eb
+    tc = td = 0.0
+    size = 0
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        s, _ = O.compress(conf, x)
+        tc += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.decompress(s)
+        td += time.perf_counter() - t0
+        size = len(s)
+    return tc, td, size, x.nbytes
+
+
+def cpu_oracle_single(field_np, slab, eb, interp):
+    """One thread, one slab of the field."""
+    shape = (slab,) + tuple(field_np.shape[1:])
+    with tempfile.NamedTemporaryFile(suffix=".f32", delete=False) as f:
+        field_np[:slab].tofile(f)
+        path = f.name
+    try:
+        tc, td, size, nb = _cpu_slab_job((path, shape, 0, eb, interp, 1))
+    finally:
+        os.unlink(path)
+    return nb / tc / 1e9, nb / td / 1e9, shape
+
+
+def reference_arm(args, dims):
+    """CPU restatement of the reference on all host cores: one slab per worker."""
+    import multiprocessing as mp
+    import numpy as np
+    from faz_gb300.fields import spectral_field
+    cores = os.cpu_count() or 1
+    slab = max(8, min(64, dims[0] // max(1, cores)))
+    nslab = min(cores, dims[0] // slab)
+    sdims = (slab * nslab,) + tuple(dims[1:])
+    x = spectral_field(sdims, slope=-3.5, aniso=(1, 2, 4), noise=0.01, seed=2024)
+    with tempfile.NamedTemporaryFile(suffix=".f32", delete=False, dir="/dev/shm" if os.path.isdir("/dev/shm") else None) as f:
+        x.tofile(f)
+        path = f.name
+    plane = int(np.prod(dims[1:])) * 4
+    jobs = [(path, (slab,) + tuple(dims[1:]), i * slab * plane, args.eb, args.interp, 1) for i in range(nslab)]
+    ctx = mp.get_context("spawn")
+    times_c, times_d, sizes = [], [], []
+    try:
+        with ctx.Pool(nslab) as pool:
+            for step in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                res = pool.map(_cpu_slab_job, jobs)
+                wall = time.perf_counter() - t0
+                if step >= args.warmup:
+                    # workers run compress then decompress; split the wall time by their ratio
+                    tc = sum(r[0] for r in res)
+                    td = sum(r[1] for r in res)
+                    times_c.append(wall * tc / (tc + td))
+                    times_d.append(wall * td / (tc + td))
+                    sizes.append(sum(r[2] for r in res))
+    finally:
+        os.unlink(path)
+    nbytes = x.nbytes
+    tc = statistics.median(times_c)
+    td = statistics.median(times_d)
+    v = nbytes / tc / 1e9
+    sample = f"{nslab} slabs of {slab}x{dims[1]}x{dims[2]} float32 ({nbytes / 1e6:.0f} MB) per step, one per process"
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GB/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tc * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded spectral field k^-3.5, aniso 1:2:4, 1% noise",
+            "config": {"workload": f"{dims[0]}x{dims[1]}x{dims[2]} float32 spectral field, rel eb {args.eb:g}, "
+                                   f"ALGO_INTERP {args.interp}", "eb_mode": "REL", "eb": args.eb},
+            "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": nslab, "kind": "port", "sample": sample},
+            "e2e": {"value": round(v, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "decompress": {"value": round(nbytes / td / 1e9, 4), "unit": "GB/s", "ms_per_step": round(td * 1e3, 3)},
+            "ratio": round(nbytes / statistics.median(sizes), 3)}
+    return line
+
+
+# ------------------------------------------------------------------ GPU arm
+def main():
+    args = parse()
+    dims = tuple(int(d) for d in args.dims.split(","))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(reference_arm(args, dims)), flush=True)
+        return
+
+    import numpy as np
+    import torch
+    import faz_gb300 as F
+    from faz_gb300.fields import spectral_field
+    from faz_gb300 import build as B
+    B.build()
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    conf = make_conf(F, dims, args.eb, args.interp)
+    x = spectral_field(dims, slope=-3.5, aniso=(1, 2, 4), noise=0.01, seed=1000 + rank, device="cuda")
+    nbytes = x.numel() * x.element_size()
+    stream = torch.cuda.Stream()
+    out = torch.empty_like(x)
+
+    # ---- device-resident compress (value) and decompress
+    launches = 0
+    for _ in range(args.warmup):
+        payload, conf_out = F.compress_payload_device(conf, x, stream)
+        F.decompress_payload_device(len(dims), payload, out, stream)
+    barrier()
+    t_steps, phases = [], []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        barrier()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            payload, conf_out = F.compress_payload_device(conf, x, stream)
+            tm = F.last_timings()
+            launches += tm["kernel_launches"]
+            phases.append(tm)
+        ev1.record(stream)
+        barrier()
+        t_comp = ev0.elapsed_time(ev1) / 1e3 / args.steps
+        dphases = []
+        ev0.record(stream)
+        for _ in range(args.steps):
+            F.decompress_payload_device(len(dims), payload, out, stream)
+            tm = F.last_timings()
+            launches += tm["kernel_launches"]
+            dphases.append(tm)
+        ev1.record(stream)
+        barrier()
+        t_dec = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    clocks = clk.summary()
+    err = (out.double() - x.double()).abs().max().item()
+    assert err <= conf_out.absErrorBound, (err, conf_out.absErrorBound)
+
+    # ---- end to end through the public API with host buffers
+    host_in = torch.empty(dims, dtype=torch.float32, pin_memory=True)
+    host_in.copy_(x.cpu())
+    host_np = host_in.numpy()
+    for _ in range(max(1, args.warmup // 2)):
+        s = F.SZ_compress(conf, host_np)
+        F.SZ_decompress(None, s)
+    barrier()
+    e2e_c, e2e_d, zc, zd, d2h_bytes = [], [], [], [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        s = F.SZ_compress(conf, host_np)
+        e2e_c.append(time.perf_counter() - t0)
+        tm = F.last_timings()
+        zc.append(tm["zstd_ms"])
+        d2h_bytes = tm["payload_bytes"]
+        t0 = time.perf_counter()
+        dec, _ = F.SZ_decompress(None, s)
+        e2e_d.append(time.perf_counter() - t0)
+        zd.append(F.last_timings()["zstd_ms"])
+    ratio = nbytes / len(s)
+    assert np.abs(dec.astype(np.float64) - host_np.astype(np.float64)).max() <= conf_out.absErrorBound
+
+    # ---- max over ranks
+    vals = torch.tensor([t_comp, t_dec, statistics.median(e2e_c), statistics.median(e2e_d)], device="cuda",
+                        dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
+    t_comp, t_dec, te2e_c, te2e_d = vals.tolist()
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    peak, peak_kind = peaks()
+    fin = statistics.median(p["finest_level_ms"] for p in phases) / 1e3
+    fin_bytes = finest_level_bytes(dims, 4)
+    achieved = fin_bytes / fin / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        slab = 64
+        cc, cd, shape = cpu_oracle_single(x[:slab].cpu().numpy(), slab, args.eb, args.interp)
+        cpu = {"value": round(cc, 4), "unit": "GB/s", "cores": 1, "kind": "port",
+               "sample": f"compress of a {shape[0]}x{shape[1]}x{shape[2]} slab of the same field, one thread "
+                         f"(decompress {cd:.4f} GB/s)"}
+    med = lambda k, ph: round(statistics.median(p[k] for p in ph), 4)  # noqa: E731
+    line = {
+        "metric": METRIC,
+        "value": round(world * nbytes / t_comp / 1e9, 3),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(t_comp * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: seeded spectral field k^-3.5, aniso 1:2:4, 1% noise, scaled to [-50,80]",
+        "config": {"workload": f"{dims[0]}x{dims[1]}x{dims[2]} float32 spectral field, rel eb {args.eb:g}, "
+                               f"ALGO_INTERP {args.interp} (one field per GPU)",
+                   "eb_mode": "REL", "eb": args.eb, "abs_eb": conf_out.absErrorBound,
+                   "l2": "inputs larger than L2 (field %.0f MB vs 129 MB L2)" % (nbytes / 1e6),
+                   "parallelism": f"replicas x{world}"},
+        "ratio": round(ratio, 3),
+        "decompress": {"value": round(world * nbytes / t_dec / 1e9, 3), "unit": "GB/s",
+                       "ms_per_step": round(t_dec * 1e3, 3),
+                       "e2e": round(world * nbytes / te2e_d / 1e9, 3)},
+        "e2e": {"value": round(world * nbytes / te2e_c / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": int(d2h_bytes), "ms_per_step": round(te2e_c * 1e3, 3),
+                "zstd_ms_compress": round(statistics.median(zc), 3),
+                "zstd_ms_decompress": round(statistics.median(zd), 3)},
+        "roofline": {"kernel": "k_interp_level<float,compress> finest level", "bound": "hbm",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "bytes_per_launch": fin_bytes, "traffic": None},
+        "phases_ms": {"compress": {k: med(k, phases) for k in ("predict_ms", "finest_level_ms", "huffman_ms",
+                                                               "host_ms", "gpu_ms")},
+                      "decompress": {k: med(k, dphases) for k in ("huffman_ms", "predict_ms", "finest_level_ms",
+                                                                  "gpu_ms")}},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+        "max_abs_err": err,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -101,6 +101,9 @@ class FazTimings(ctypes.Structure):
         ("d2h_ms", _f64),
         ("zstd_ms", _f64),
         ("host_ms", _f64),
+        ("predict_ms", _f64),
+        ("finest_level_ms", _f64),
+        ("huffman_ms", _f64),
         ("payload_bytes", _u64),
         ("unpred_count", _u64),
         ("kernel_launches", _u64),

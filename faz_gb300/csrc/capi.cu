@@ -1,0 +1,1078 @@
+// capi.cu - host orchestration of the GPU compress/decompress path and the
+// extern "C" entry points declared in include/faz_gb300.h.
+//
+// compress (SZ_compress -> SZInterpolationCompressor::compress, reference
+// include/QoZ/api/sz.hpp:54-108, SZInterpolationCompressor.hpp:324-529):
+//   range (for relative bounds) -> first point / anchor grid -> one kernel per
+//   level -> histogram -> codebook (host) -> unpredictable gather -> Huffman
+//   encode -> payload assembled in pinned memory -> host zstd -> trailer.
+// decompress (sz.hpp:159-205, SZInterpolationCompressor.hpp:42-199):
+//   trailer -> host zstd -> header / unpredictables / tree -> GPU Huffman
+//   decode -> zero positions -> first point / anchors -> one kernel per level.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace faz {
+
+const char *last_error();
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+double ms_since(clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); }
+
+struct Fail {
+    int code;
+    std::string msg;
+};
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t _e = (call);                                                              \
+        if (_e != cudaSuccess) throw Fail{FAZ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)}; \
+    } while (0)
+
+// ----------------------------------------------------- memory management
+// Device memory comes from the stream-ordered pool (cached across calls);
+// pinned host staging is cached per thread and grows on demand.
+struct DevMem {
+    cudaStream_t st;
+    std::vector<void *> ptrs;
+    explicit DevMem(cudaStream_t s) : st(s) {}
+    template <typename T>
+    T *alloc(size_t count) {
+        void *p = nullptr;
+        size_t bytes = count * sizeof(T);
+        if (bytes == 0) bytes = 16;
+        CK(cudaMallocAsync(&p, bytes, st));
+        ptrs.push_back(p);
+        return (T *)p;
+    }
+    ~DevMem() {
+        for (void *p : ptrs) cudaFreeAsync(p, st);
+    }
+};
+
+void init_pool_once() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    });
+}
+
+struct Pinned {
+    uint8_t *p = nullptr;
+    size_t cap = 0;
+    uint8_t *get(size_t n) {
+        if (n > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            cap = 0;
+            size_t c = std::max<size_t>(n + n / 4, 1 << 20);
+            if (cudaHostAlloc((void **)&p, c, cudaHostAllocDefault) != cudaSuccess)
+                throw Fail{FAZ_ERR_CUDA, "cudaHostAlloc failed"};
+            cap = c;
+        }
+        return p;
+    }
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+};
+thread_local Pinned t_pin_payload;
+thread_local Pinned t_pin_small;
+
+struct StreamGuard {
+    cudaStream_t st = nullptr;
+    bool own = false;
+    explicit StreamGuard(void *user) {
+        if (user) {
+            st = (cudaStream_t)user;
+        } else {
+            CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            own = true;
+        }
+    }
+    ~StreamGuard() {
+        if (own) cudaStreamDestroy(st);
+    }
+};
+
+struct Events {
+    cudaEvent_t a = nullptr, b = nullptr;
+    Events() {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    }
+    ~Events() {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    float ms() {
+        float t = 0;
+        cudaEventElapsedTime(&t, a, b);
+        return t;
+    }
+};
+
+template <typename V>
+void put(std::vector<uint8_t> &o, V v) {
+    uint8_t b[sizeof(V)];
+    std::memcpy(b, &v, sizeof(V));
+    o.insert(o.end(), b, b + sizeof(V));
+}
+void put_be32(std::vector<uint8_t> &o, int32_t v) {
+    o.push_back((uint8_t)(v >> 24));
+    o.push_back((uint8_t)(v >> 16));
+    o.push_back((uint8_t)(v >> 8));
+    o.push_back((uint8_t)v);
+}
+
+// --------------------------------------------------------------- geometry
+struct LevelPlan {
+    LevelArgs args;
+    int64_t nblocks;
+    uint64_t off_index;  // first entry of this level in the block-offset table
+};
+
+struct Plan {
+    int N = 0;
+    int64_t dims3[3], offs3[3];
+    uint64_t num = 0;
+    int levels = 0;      // interpolation_level after init()
+    bool anchor = false;
+    uint64_t maxStep = 0;
+    int64_t na[3] = {1, 1, 1};
+    uint64_t nanchor = 0;  // codes before the first level
+    std::vector<LevelPlan> lv;
+    std::vector<uint64_t> block_off;
+    uint64_t total_codes = 0;
+    size_t max_smem = 0;
+};
+
+int ceil_log2(uint64_t d) {
+    int l = 0;
+    while (((uint64_t)1 << l) < d) l++;
+    return l;
+}
+
+// permutations of 0..N-1 in lexicographic order (std::next_permutation)
+std::vector<std::vector<int>> permutations(int N) {
+    std::vector<int> s(N);
+    for (int i = 0; i < N; i++) s[i] = i;
+    std::vector<std::vector<int>> out;
+    do {
+        out.push_back(s);
+    } while (std::next_permutation(s.begin(), s.end()));
+    return out;
+}
+
+// Level error bound (SZInterpolationCompressor.hpp:386-406, eb_ratio 0.5)
+double level_eb(double eb, double alpha, double beta, int level) {
+    if (alpha < 0) return level >= 3 ? eb * 0.5 : eb;
+    if (alpha >= 1) {
+        double cr = std::pow(alpha, level - 1);
+        if (cr > beta) cr = beta;
+        return eb / cr;
+    }
+    double cr = 1 - (level - 1) * alpha;
+    if (cr < beta) cr = beta;
+    return eb * cr;
+}
+
+template <typename T>
+Plan make_plan(int N, const uint64_t *dims, uint64_t maxStep, int blocksize, int fixbs, int interp, int dir,
+               const std::vector<uint8_t> &ilist, const std::vector<uint8_t> &dlist, double eb, double alpha,
+               double beta, int radius, int trim, size_t smem_limit) {
+    Plan p;
+    p.N = N;
+    p.num = 1;
+    int e = 3 - N;
+    for (int i = 0; i < 3; i++) p.dims3[i] = 1;
+    for (int i = 0; i < N; i++) {
+        p.dims3[e + i] = (int64_t)dims[i];
+        p.num *= dims[i];
+    }
+    p.offs3[2] = 1;
+    p.offs3[1] = p.dims3[2];
+    p.offs3[0] = p.dims3[1] * p.dims3[2];
+    p.levels = 0;
+    for (int i = 0; i < N; i++) p.levels = std::max(p.levels, ceil_log2(dims[i]));
+    p.maxStep = maxStep;
+    if (maxStep > 0) {
+        p.anchor = true;
+        p.levels += 1;
+        int lm = 0;
+        while (((uint64_t)1 << (lm + 1)) <= maxStep) lm++;
+        lm += 1;
+        if (lm <= p.levels) p.levels = lm;
+        if (maxStep & (maxStep - 1)) throw Fail{FAZ_ERR_UNSUPPORTED, "maxStep must be a power of two on the GPU path"};
+        if (N != 2 && N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "an anchor grid needs 2-D or 3-D data"};
+        for (int i = 0; i < 3; i++) p.na[i] = 1;
+        for (int i = 0; i < N; i++) p.na[e + i] = (int64_t)((dims[i] - 1) / maxStep + 1);
+        p.nanchor = (uint64_t)(p.na[0] * p.na[1] * p.na[2]);
+    } else {
+        p.nanchor = 1;
+    }
+    if (blocksize <= 0 || (blocksize & 1)) throw Fail{FAZ_ERR_UNSUPPORTED, "interpBlockSize must be a positive even number"};
+    auto perms = permutations(N);
+    int top = p.anchor ? p.levels - 1 : p.levels;
+    if (fixbs > 0) {
+        // block begins must stay on the coarse lattice of every level
+        if (top > 0 && (fixbs % (1 << top)) != 0)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "fixBlockSize must be a multiple of 2^levels on the GPU path"};
+    }
+    uint64_t pos = p.nanchor;
+    for (int level = top; level > 0; level--) {
+        LevelPlan L;
+        LevelArgs &a = L.args;
+        std::memset(&a, 0, sizeof(a));
+        int cur_interp = interp, cur_dir = dir;
+        if (!ilist.empty()) {
+            size_t li = (size_t)(level - 1) < ilist.size() ? (size_t)(level - 1) : ilist.size() - 1;
+            cur_interp = ilist[li];
+            cur_dir = dlist[li];
+        }
+        if (cur_dir < 0 || cur_dir >= (int)perms.size()) throw Fail{FAZ_ERR_ARG, "interpolation direction out of range"};
+        for (int i = 0; i < 3; i++) {
+            a.dims[i] = p.dims3[i];
+            a.offs[i] = p.offs3[i];
+        }
+        for (int i = 0; i < e; i++) a.perm[i] = i;
+        for (int i = 0; i < N; i++) a.perm[e + i] = perms[cur_dir][i] + e;
+        a.s = (int64_t)1 << (level - 1);
+        a.bs = fixbs > 0 ? fixbs : (int64_t)blocksize * a.s;
+        a.cubic = cur_interp == FAZ_INTERP_ALGO_CUBIC;
+        a.radius = radius;
+        a.trim = trim;
+        a.eb = level_eb(eb, alpha, beta, level);
+        a.recip = 1.0 / a.eb;
+        a.write_back = level > 1;
+        int64_t nmax[3];
+        L.nblocks = 1;
+        for (int i = 0; i < 3; i++) {
+            a.nb[i] = (a.dims[i] - 1) / a.bs + 1;
+            L.nblocks *= a.nb[i];
+            int64_t ext = std::min<int64_t>(a.bs, a.dims[i] - 1);
+            nmax[i] = ext / a.s + 1;
+        }
+        int64_t m0 = nmax[a.perm[0]], m1 = nmax[a.perm[1]], m2 = nmax[a.perm[2]];
+        int64_t vw = m0 * m1 * ((m2 + 1) / 2);
+        int64_t stage = std::max({((m1 + 1) / 2) * ((m2 + 1) / 2) * (m0 / 2), m0 * ((m2 + 1) / 2) * (m1 / 2),
+                                  m0 * m1 * (m2 / 2)});
+        a.vwords = (int)vw;
+        a.stage_cap = (int)std::max<int64_t>(stage, 1);
+        size_t sm = level_smem_bytes<T>(a);
+        if (sm > smem_limit)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "interpolation block does not fit in shared memory (block size too large)"};
+        p.max_smem = std::max(p.max_smem, sm);
+        L.off_index = p.block_off.size();
+        int64_t bc[3];
+        for (int64_t b = 0; b < L.nblocks; b++) {
+            block_coords(a, b, bc);
+            BlockGeom g;
+            block_geom(a, bc, g);
+            p.block_off.push_back(pos);
+            pos += (uint64_t)(g.c1 + g.c2 + g.c3);
+        }
+        p.lv.push_back(L);
+    }
+    p.total_codes = pos;
+    if (p.total_codes != p.num && !(p.anchor && (N == 1 || N == 4)))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "block decomposition does not cover the field exactly"};
+    return p;
+}
+
+size_t smem_limit() {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return (size_t)v;
+}
+
+// --------------------------------------------------------------- compress
+struct Counter {
+    uint64_t n = 0;
+    void operator()(cudaError_t e) {
+        if (e != cudaSuccess) throw Fail{FAZ_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e)};
+        n++;
+    }
+};
+
+void check_config(const faz_config &c) {
+    if (c.N < 1 || c.N > 4) throw Fail{FAZ_ERR_ARG, "N must be 1..4"};
+    uint64_t num = 1;
+    for (int i = 0; i < c.N; i++) {
+        if (c.dims[i] == 0) throw Fail{FAZ_ERR_ARG, "zero dimension"};
+        num *= c.dims[i];
+    }
+    if (num != c.num) throw Fail{FAZ_ERR_ARG, "num does not match dims"};
+    if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
+    if (c.cmprAlgo != FAZ_ALGO_INTERP)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "only cmprAlgo = ALGO_INTERP is implemented on the GPU path"};
+    if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};
+    if (c.wavelet != 0 || ((c.wavelet > 0 || c.sperrWithoutWave) && c.sperr >= c.wavelet))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet / SPERR modes are not part of the interpolation path"};
+    if (c.quantbinCnt < 2 || c.quantbinCnt > 65536)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt must be in [2, 65536] on the GPU path"};
+    if (c.interp_list_len < 0 || c.interp_list_len > FAZ_MAX_LEVELS) throw Fail{FAZ_ERR_ARG, "bad level list length"};
+}
+
+// calAbsErrorBound (include/QoZ/utils/Statistic.hpp:34-66); `rng` computed
+// on the device when the mode needs it.
+template <typename T>
+void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) {
+    if (c.errorBoundMode == FAZ_EB_ABS) return;
+    double rng = 0;
+    if (c.errorBoundMode != FAZ_EB_L2NORM) {
+        int nb = (int)std::min<uint64_t>(1024, (c.num + 511) / 512);
+        if (nb < 1) nb = 1;
+        DevMem m(st);
+        T *pmin = m.alloc<T>(nb), *pmax = m.alloc<T>(nb);
+        launches(launch_minmax<T>(dX, c.num, pmin, pmax, nb, st));
+        std::vector<T> hmin(nb), hmax(nb);
+        CK(cudaMemcpyAsync(hmin.data(), pmin, nb * sizeof(T), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hmax.data(), pmax, nb * sizeof(T), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        T mn = hmin[0], mx = hmax[0];
+        for (int i = 0; i < nb; i++) {
+            if (hmin[i] < mn) mn = hmin[i];
+            if (hmax[i] > mx) mx = hmax[i];
+        }
+        T r = mx - mn;
+        rng = (double)r;
+    }
+    switch (c.errorBoundMode) {
+    case FAZ_EB_REL:
+        c.absErrorBound = c.relErrorBound * rng;
+        break;
+    case FAZ_EB_PSNR: {
+        double v1 = c.psnrErrorBound + 10 * std::log10(1 - 2.0 / 3.0 * 0.99);
+        double v3 = std::pow(10, v1 / (-20));
+        c.absErrorBound = rng * v3;
+        c.relErrorBound = c.absErrorBound / rng;
+        break;
+    }
+    case FAZ_EB_L2NORM:
+        c.absErrorBound = std::sqrt(3.0 / (double)c.num) * c.l2normErrorBound;
+        break;
+    case FAZ_EB_ABS_AND_REL:
+        c.absErrorBound = std::min(c.absErrorBound, c.relErrorBound * rng);
+        break;
+    case FAZ_EB_ABS_OR_REL:
+        c.absErrorBound = std::max(c.absErrorBound, c.relErrorBound * rng);
+        break;
+    default:
+        throw Fail{FAZ_ERR_ARG, "error bound mode not supported"};
+    }
+    if (c.errorBoundMode != FAZ_EB_L2NORM) c.rng = rng;
+    c.errorBoundMode = FAZ_EB_ABS;
+}
+
+constexpr uint64_t kHistChunk = 1 << 18;
+
+// GPU part of compression: returns the pre-zstd payload in a pinned buffer.
+template <typename T>
+void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&payload, size_t &psize,
+                      faz_timings &tm, Counter &launches) {
+    auto th0 = clk::now();
+    resolve_eb<T>(c, dX, st, launches);
+    const double eb = c.absErrorBound;
+    if (!(eb > 0) || !std::isfinite(eb)) throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
+    const int radius = c.quantbinCnt / 2;
+    std::vector<uint8_t> il(c.interpAlgo_list, c.interpAlgo_list + c.interp_list_len);
+    std::vector<uint8_t> dl(c.interpDirection_list, c.interpDirection_list + c.interp_list_len);
+    Plan p = make_plan<T>(c.N, c.dims, c.maxStep, c.interpBlockSize, c.fixBlockSize, c.interpAlgo, c.interpDirection,
+                          il, dl, eb, c.alpha, c.beta, radius, c.trimToZero, smem_limit());
+    const uint64_t n = p.num;
+    DevMem m(st);
+    T *W = m.alloc<T>(n);
+    T *scratch = m.alloc<T>(n);
+    uint16_t *codes = m.alloc<uint16_t>(n);
+    uint64_t *boff = m.alloc<uint64_t>(p.block_off.size());
+    CK(cudaMemcpyAsync(boff, p.block_off.data(), p.block_off.size() * 8, cudaMemcpyHostToDevice, st));
+    // first point / anchors
+    if (!p.anchor) {
+        launches(launch_first_point<T>(false, dX, W, codes, scratch, eb, radius, c.trimToZero, nullptr, 0, nullptr, st));
+    } else {
+        int64_t step[3] = {1, 1, 1};
+        int e = 3 - p.N;
+        for (int i = 0; i < p.N; i++) step[e + i] = (int64_t)p.maxStep;
+        launches(launch_anchors<T>(false, dX, W, codes, scratch, nullptr, p.na, step, p.offs3, st));
+    }
+    Events ev_pred, ev_fin, ev_huff;
+    CK(cudaEventRecord(ev_pred.a, st));
+    for (size_t li = 0; li < p.lv.size(); li++) {
+        const LevelPlan &L = p.lv[li];
+        LevelArgs a = L.args;
+        a.block_off = boff + L.off_index;
+        a.ncodes = n;
+        a.err = nullptr;
+        if (li + 1 == p.lv.size()) CK(cudaEventRecord(ev_fin.a, st));
+        launches(launch_level<T>(a, L.nblocks, false, dX, W, codes, scratch, nullptr, 0, nullptr, st));
+    }
+    CK(cudaEventRecord(ev_fin.b, st));
+    CK(cudaEventRecord(ev_pred.b, st));
+    CK(cudaEventRecord(ev_huff.a, st));
+    // histogram
+    const uint64_t nchunk = (n + kHistChunk - 1) / kHistChunk;
+    const int nsym = 65536;
+    unsigned long long *hist = m.alloc<unsigned long long>(nsym);
+    unsigned long long *first = m.alloc<unsigned long long>(nsym);
+    unsigned long long *zc = m.alloc<unsigned long long>(nchunk + 1);
+    unsigned long long *zoff = m.alloc<unsigned long long>(nchunk + 1);
+    CK(cudaMemsetAsync(hist, 0, nsym * 8, st));
+    CK(cudaMemsetAsync(first, 0xff, nsym * 8, st));
+    launches(launch_histogram(codes, n, kHistChunk, radius, hist, first, zc, st));
+    launches(launch_scan_u64(zc, zoff, nchunk, st));
+    uint8_t *hb = t_pin_small.get((size_t)nsym * 16 + 8);
+    CK(cudaMemcpyAsync(hb, hist, nsym * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hb + nsym * 8, first, nsym * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hb + nsym * 16, zoff + nchunk, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    auto th1 = clk::now();
+    const unsigned long long *hh = (const unsigned long long *)hb;
+    const unsigned long long *hf = (const unsigned long long *)(hb + nsym * 8);
+    uint64_t nunpred;
+    std::memcpy(&nunpred, hb + nsym * 16, 8);
+    std::vector<int> syms;
+    std::vector<uint64_t> cnts, firsts;
+    for (int s = 0; s < nsym; s++)
+        if (hh[s]) {
+            syms.push_back(s);
+            cnts.push_back(hh[s]);
+            firsts.push_back(hf[s]);
+        }
+    Codebook cb;
+    std::string err;
+    int rc = build_codebook(syms, cnts, firsts, cb, err);
+    if (rc) throw Fail{rc, err};
+    tm.host_ms += ms_since(th1);
+    // unpredictable values in stream order
+    T *unpred = m.alloc<T>(nunpred ? nunpred : 1);
+    if (nunpred) launches(launch_gather_unpred<T>(codes, n, kHistChunk, zc, zoff, scratch, unpred, st));
+    // Huffman encode
+    unsigned long long *dcode = m.alloc<unsigned long long>(cb.stateNum);
+    uint8_t *dlen = m.alloc<uint8_t>(cb.stateNum);
+    CK(cudaMemcpyAsync(dcode, cb.code.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dlen, cb.len.data(), cb.stateNum, cudaMemcpyHostToDevice, st));
+    const uint64_t nech = encode_chunks(n);
+    unsigned long long *cbits = m.alloc<unsigned long long>(nech + 1);
+    unsigned long long *coff = m.alloc<unsigned long long>(nech + 1);
+    launches(launch_encode_bits(codes, n, cb.offset, dlen, cbits, st));
+    launches(launch_scan_u64(cbits, coff, nech, st));
+    uint64_t total_bits;
+    CK(cudaMemcpyAsync(hb, coff + nech, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::memcpy(&total_bits, hb, 8);
+    const uint64_t nbytes = (total_bits + 7) / 8;
+    const uint64_t nwords = (total_bits + 31) / 32 + 1;
+    uint32_t *bits = m.alloc<uint32_t>(nwords);
+    CK(cudaMemsetAsync(bits, 0, nwords * 4, st));
+    if (total_bits) launches(launch_encode_pack(codes, n, cb.offset, dcode, dlen, coff, bits, std::max(cb.maxlen, 1), st));
+    CK(cudaEventRecord(ev_huff.b, st));
+    // payload layout (SZInterpolationCompressor.hpp:485-512, IntegerQuantizer.hpp:185-201,
+    // HuffmanEncoder.hpp:119-137 and 150-227)
+    auto th2 = clk::now();
+    std::vector<uint8_t> head;
+    for (int i = 0; i < c.N; i++) put<uint64_t>(head, c.dims[i]);
+    put<uint32_t>(head, (uint32_t)c.interpBlockSize);
+    put<int32_t>(head, (int32_t)c.interpAlgo);
+    put<int32_t>(head, (int32_t)c.interpDirection);
+    put<double>(head, c.alpha);
+    put<double>(head, c.beta);
+    put<uint64_t>(head, c.maxStep);
+    put<int32_t>(head, c.interp_list_len);
+    put<uint8_t>(head, c.blockwiseTuning);
+    put<int32_t>(head, c.fixBlockSize);
+    put<uint64_t>(head, (uint64_t)(int64_t)c.crossBlock);
+    put<int32_t>(head, c.trimToZero);
+    put<int32_t>(head, c.blockOrder);
+    head.insert(head.end(), il.begin(), il.end());
+    head.insert(head.end(), dl.begin(), dl.end());
+    put<uint8_t>(head, 2);
+    put<double>(head, eb);
+    put<int32_t>(head, radius);
+    put<uint64_t>(head, nunpred);
+    std::vector<uint8_t> tree;
+    put<int32_t>(tree, cb.offset);
+    put_be32(tree, cb.nodeCount);
+    put_be32(tree, cb.stateNum / 2);
+    tree.insert(tree.end(), cb.tree.begin(), cb.tree.end());
+    put<uint64_t>(tree, nbytes);
+    psize = head.size() + nunpred * sizeof(T) + tree.size() + nbytes;
+    payload = t_pin_payload.get(psize + 8);
+    std::memcpy(payload, head.data(), head.size());
+    size_t o = head.size();
+    tm.host_ms += ms_since(th2);
+    if (nunpred) CK(cudaMemcpyAsync(payload + o, unpred, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
+    o += nunpred * sizeof(T);
+    std::memcpy(payload + o, tree.data(), tree.size());
+    o += tree.size();
+    if (nbytes) CK(cudaMemcpyAsync(payload + o, bits, nbytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    tm.unpred_count = nunpred;
+    tm.payload_bytes = psize;
+    tm.predict_ms = ev_pred.ms();
+    tm.finest_level_ms = p.lv.empty() ? 0.0 : ev_fin.ms();
+    tm.huffman_ms = ev_huff.ms();
+    (void)th0;
+}
+
+// Lossless_zstd::compress framing (include/QoZ/lossless/Lossless_zstd.hpp:22-32),
+// then Config::save + int32 trailer size (include/QoZ/api/sz.hpp:77-91).
+void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, char **out, size_t *out_size,
+                   faz_timings &tm) {
+    std::string err;
+    const Zstd &z = zstd_lib(err);
+    if (!z.ok) throw Fail{FAZ_ERR_ZSTD, err};
+    auto t0 = clk::now();
+    std::vector<uint8_t> trailer;
+    config_save(c, trailer);
+    size_t bound = z.bound(psize);
+    size_t cap = 8 + bound + trailer.size() + 4;
+    char *buf = (char *)std::malloc(cap);
+    if (!buf) throw Fail{FAZ_ERR_ARG, "out of host memory"};
+    uint64_t raw = psize;
+    std::memcpy(buf, &raw, 8);
+    size_t zs = z.compress(buf + 8, bound, payload, psize, 3);
+    if (z.isError(zs)) {
+        std::free(buf);
+        throw Fail{FAZ_ERR_ZSTD, "ZSTD_compress failed"};
+    }
+    tm.zstd_ms += ms_since(t0);
+    size_t pos = 8 + zs;
+    std::memcpy(buf + pos, trailer.data(), trailer.size());
+    pos += trailer.size();
+    int32_t ts = (int32_t)trailer.size();
+    std::memcpy(buf + pos, &ts, 4);
+    pos += 4;
+    *out = buf;
+    *out_size = pos;
+}
+
+template <typename T>
+int compress_payload_impl(const faz_config *conf_in, const void *d_data, void *user_stream, char **out,
+                          size_t *out_size, faz_config *conf_out, faz_timings *tmo) {
+    faz_timings tm;
+    std::memset(&tm, 0, sizeof(tm));
+    auto t0 = clk::now();
+    try {
+        if (!conf_in || !d_data || !out || !out_size) throw Fail{FAZ_ERR_ARG, "null argument"};
+        faz_config c = *conf_in;
+        check_config(c);
+        init_pool_once();
+        StreamGuard sg(user_stream);
+        Counter launches;
+        Events ev_gpu;
+        uint8_t *payload;
+        size_t psize;
+        CK(cudaEventRecord(ev_gpu.a, sg.st));
+        compress_payload<T>(c, (const T *)d_data, sg.st, payload, psize, tm, launches);
+        CK(cudaEventRecord(ev_gpu.b, sg.st));
+        CK(cudaStreamSynchronize(sg.st));
+        tm.gpu_ms = ev_gpu.ms();
+        char *buf = (char *)std::malloc(psize ? psize : 1);
+        if (!buf) throw Fail{FAZ_ERR_ARG, "out of host memory"};
+        std::memcpy(buf, payload, psize);
+        *out = buf;
+        *out_size = psize;
+        if (conf_out) *conf_out = c;
+        tm.kernel_launches = launches.n;
+    } catch (const Fail &f) {
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return FAZ_ERR_ARG;
+    }
+    tm.total_ms = ms_since(t0);
+    if (tmo) *tmo = tm;
+    return FAZ_OK;
+}
+
+template <typename T>
+int compress_impl(const faz_config *conf_in, const void *data, bool on_device, void *user_stream, char **out,
+                  size_t *out_size, faz_timings *tmo) {
+    faz_timings tm;
+    std::memset(&tm, 0, sizeof(tm));
+    auto t0 = clk::now();
+    try {
+        if (!conf_in || !data || !out || !out_size) throw Fail{FAZ_ERR_ARG, "null argument"};
+        faz_config c = *conf_in;
+        check_config(c);
+        init_pool_once();
+        StreamGuard sg(user_stream);
+        cudaStream_t st = sg.st;
+        Counter launches;
+        Events ev_h2d, ev_gpu;
+        const T *dX;
+        DevMem m(st);
+        if (!on_device) {
+            T *tmp = m.alloc<T>(c.num);
+            CK(cudaEventRecord(ev_h2d.a, st));
+            CK(cudaMemcpyAsync(tmp, data, c.num * sizeof(T), cudaMemcpyHostToDevice, st));
+            CK(cudaEventRecord(ev_h2d.b, st));
+            dX = tmp;
+        } else {
+            dX = (const T *)data;
+        }
+        uint8_t *payload;
+        size_t psize;
+        CK(cudaEventRecord(ev_gpu.a, st));
+        compress_payload<T>(c, dX, st, payload, psize, tm, launches);
+        CK(cudaEventRecord(ev_gpu.b, st));
+        CK(cudaStreamSynchronize(st));
+        if (!on_device) tm.h2d_ms = ev_h2d.ms();
+        tm.gpu_ms = ev_gpu.ms();
+        finish_stream(c, payload, psize, out, out_size, tm);
+        tm.kernel_launches = launches.n;
+    } catch (const Fail &f) {
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return FAZ_ERR_ARG;
+    }
+    tm.total_ms = ms_since(t0);
+    if (tmo) *tmo = tm;
+    return FAZ_OK;
+}
+
+// -------------------------------------------------------------- decompress
+struct Parsed {
+    faz_config conf;
+    int N;
+    uint64_t dims[4];
+    uint32_t blocksize;
+    int32_t interp, dir, nlist, fixbs, trim, border;
+    double alpha, beta, eb;
+    uint64_t maxStep, cross;
+    uint8_t bwt;
+    std::vector<uint8_t> il, dl;
+    int32_t radius;
+    uint64_t nunpred;
+    const uint8_t *unpred;
+    DecodeTablesHost tables;
+    uint64_t nbytes;
+    const uint8_t *bits;
+};
+
+template <typename V>
+V rd(const uint8_t *&p, const uint8_t *end) {
+    if ((size_t)(end - p) < sizeof(V)) throw Fail{FAZ_ERR_FORMAT, "truncated stream header"};
+    V v;
+    std::memcpy(&v, p, sizeof(V));
+    p += sizeof(V);
+    return v;
+}
+
+// SZInterpolationCompressor::decompress header reads (lines 53-88),
+// LinearQuantizer::load (IntegerQuantizer.hpp:203-226), HuffmanEncoder::load.
+void parse_payload(const uint8_t *pl, size_t n, int N, Parsed &P) {
+    const uint8_t *p = pl, *end = pl + n;
+    P.N = N;
+    for (int i = 0; i < N; i++) P.dims[i] = rd<uint64_t>(p, end);
+    P.blocksize = rd<uint32_t>(p, end);
+    P.interp = rd<int32_t>(p, end);
+    P.dir = rd<int32_t>(p, end);
+    P.alpha = rd<double>(p, end);
+    P.beta = rd<double>(p, end);
+    P.maxStep = rd<uint64_t>(p, end);
+    P.nlist = rd<int32_t>(p, end);
+    P.bwt = rd<uint8_t>(p, end);
+    P.fixbs = rd<int32_t>(p, end);
+    P.cross = rd<uint64_t>(p, end);
+    P.trim = rd<int32_t>(p, end);
+    P.border = rd<int32_t>(p, end);
+    if (P.bwt) throw Fail{FAZ_ERR_UNSUPPORTED, "block-wise tuned streams are not implemented"};
+    if (P.nlist < 0 || P.nlist > FAZ_MAX_LEVELS) throw Fail{FAZ_ERR_FORMAT, "bad level list length"};
+    if ((size_t)(end - p) < (size_t)2 * P.nlist) throw Fail{FAZ_ERR_FORMAT, "truncated level lists"};
+    P.il.assign(p, p + P.nlist);
+    p += P.nlist;
+    P.dl.assign(p, p + P.nlist);
+    p += P.nlist;
+    rd<uint8_t>(p, end);
+    P.eb = rd<double>(p, end);
+    P.radius = rd<int32_t>(p, end);
+    P.nunpred = rd<uint64_t>(p, end);
+    P.unpred = p;
+}
+
+template <typename T>
+void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStream_t st, faz_timings &tm,
+                       Counter &launches) {
+    const uint8_t *end = pl + n;
+    const uint8_t *p = P.unpred;
+    if ((size_t)(end - p) / sizeof(T) < P.nunpred) throw Fail{FAZ_ERR_FORMAT, "truncated unpredictable values"};
+    p += P.nunpred * sizeof(T);
+    std::string err;
+    int rc = parse_tree(p, end, P.tables, err);
+    if (rc) throw Fail{rc, err};
+    P.nbytes = rd<uint64_t>(p, end);
+    if ((size_t)(end - p) < P.nbytes) throw Fail{FAZ_ERR_FORMAT, "truncated Huffman bits"};
+    P.bits = p;
+    if (!(P.eb > 0)) throw Fail{FAZ_ERR_FORMAT, "bad error bound"};
+    Plan pl_ = make_plan<T>(P.N, P.dims, P.maxStep, (int)P.blocksize, P.fixbs, P.interp, P.dir, P.il, P.dl, P.eb, P.alpha,
+                            P.beta, P.radius, P.trim, smem_limit());
+    const uint64_t num = pl_.num;
+    DevMem m(st);
+    uint16_t *codes = m.alloc<uint16_t>(num);
+    T *dunpred = m.alloc<T>(P.nunpred ? P.nunpred : 1);
+    if (P.nunpred) CK(cudaMemcpyAsync(dunpred, P.unpred, P.nunpred * sizeof(T), cudaMemcpyHostToDevice, st));
+    const auto &t = P.tables;
+    Events ev_dec, ev_pred, ev_fin;
+    CK(cudaEventRecord(ev_dec.a, st));
+    if (t.constant || P.nbytes == 0) {
+        int v = t.constant_state + t.offset;
+        launches(launch_fill_u16(codes, num, (uint16_t)v, st));
+    } else {
+        const uint64_t words = (P.nbytes + 7) / 8 + 8;
+        uint64_t *dbits = m.alloc<uint64_t>(words);
+        CK(cudaMemsetAsync(dbits, 0, words * 8, st));
+        CK(cudaMemcpyAsync(dbits, P.bits, P.nbytes, cudaMemcpyHostToDevice, st));
+        uint32_t *lut = m.alloc<uint32_t>(t.lut.size());
+        uint32_t *dl = m.alloc<uint32_t>(t.nodeCount), *dr = m.alloc<uint32_t>(t.nodeCount);
+        int32_t *ds = m.alloc<int32_t>(t.nodeCount);
+        uint8_t *dleaf = m.alloc<uint8_t>(t.nodeCount);
+        CK(cudaMemcpyAsync(lut, t.lut.data(), t.lut.size() * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dl, t.left.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dr, t.right.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ds, t.sym.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dleaf, t.leaf.data(), t.nodeCount, cudaMemcpyHostToDevice, st));
+        DecodeTablesDev td{lut, dl, dr, ds, dleaf};
+        const uint64_t nbits = P.nbytes * 8;
+        const uint64_t unit = 2048;
+        const uint64_t nunits = (nbits + unit - 1) / unit;
+        uint64_t *start = m.alloc<uint64_t>(nunits);
+        uint64_t *ea = m.alloc<uint64_t>(nunits), *eb2 = m.alloc<uint64_t>(nunits);
+        unsigned int *cnt = m.alloc<unsigned int>(nunits);
+        unsigned long long *cnt64 = m.alloc<unsigned long long>(nunits + 1);
+        unsigned long long *off = m.alloc<unsigned long long>(nunits + 1);
+        int *changed = m.alloc<int>(1);
+        CK(cudaMemsetAsync(changed, 0, 4, st));
+        launches(launch_decode_sync(td, dbits, nbits, unit, nunits, nullptr, start, ea, cnt, 0, changed, st));
+        int *hflag = (int *)t_pin_small.get(64);
+        bool converged = false;
+        for (int it = 0; it < 256; it++) {
+            CK(cudaMemsetAsync(changed, 0, 4, st));
+            launches(launch_decode_sync(td, dbits, nbits, unit, nunits, ea, start, eb2, cnt, 1, changed, st));
+            CK(cudaMemcpyAsync(hflag, changed, 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            std::swap(ea, eb2);
+            if (*hflag < 0) throw Fail{FAZ_ERR_FORMAT, "Huffman stream decodes outside the tree"};
+            if (*hflag == 0) {
+                converged = true;
+                break;
+            }
+        }
+        if (!converged) throw Fail{FAZ_ERR_UNSUPPORTED, "Huffman stream did not synchronise within 256 passes"};
+        launches(launch_widen_counts(cnt, cnt64, nunits, st));
+        launches(launch_scan_u64(cnt64, off, nunits, st));
+        uint64_t total;
+        CK(cudaMemcpyAsync(hflag, off + nunits, 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::memcpy(&total, hflag, 8);
+        if (total < num) throw Fail{FAZ_ERR_FORMAT, "Huffman stream holds fewer symbols than the field"};
+        launches(launch_decode_write(td, dbits, nbits, unit, nunits, start, off, num, t.offset, codes, st));
+    }
+    CK(cudaEventRecord(ev_dec.b, st));
+    // zero positions for the unpredictable values
+    const uint64_t nchunk = (num + kHistChunk - 1) / kHistChunk;
+    unsigned long long *zc = m.alloc<unsigned long long>(nchunk + 1);
+    unsigned long long *zoff = m.alloc<unsigned long long>(nchunk + 1);
+    launches(launch_count_zeros(codes, num, kHistChunk, zc, st));
+    launches(launch_scan_u64(zc, zoff, nchunk, st));
+    uint64_t nz;
+    uint64_t *hz = (uint64_t *)t_pin_small.get(64);
+    CK(cudaMemcpyAsync(hz, zoff + nchunk, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    nz = *hz;
+    if (nz != P.nunpred)
+        throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
+    uint64_t *zpos = m.alloc<uint64_t>(nz ? nz : 1);
+    if (nz) launches(launch_zero_positions(codes, num, kHistChunk, zc, zoff, zpos, st));
+    if (!pl_.anchor) {
+        launches(launch_first_point<T>(true, nullptr, dOut, codes, nullptr, P.eb, P.radius, P.trim, zpos, nz, dunpred, st));
+    } else {
+        int64_t step[3] = {1, 1, 1};
+        int e = 3 - pl_.N;
+        for (int i = 0; i < pl_.N; i++) step[e + i] = (int64_t)pl_.maxStep;
+        launches(launch_anchors<T>(true, nullptr, dOut, codes, nullptr, dunpred, pl_.na, step, pl_.offs3, st));
+    }
+    uint64_t *boff = m.alloc<uint64_t>(pl_.block_off.size());
+    CK(cudaMemcpyAsync(boff, pl_.block_off.data(), pl_.block_off.size() * 8, cudaMemcpyHostToDevice, st));
+    int *kerr = m.alloc<int>(1);
+    CK(cudaMemsetAsync(kerr, 0, 4, st));
+    CK(cudaEventRecord(ev_pred.a, st));
+    for (size_t li = 0; li < pl_.lv.size(); li++) {
+        const LevelPlan &L = pl_.lv[li];
+        LevelArgs a = L.args;
+        a.block_off = boff + L.off_index;
+        a.ncodes = num;
+        a.err = kerr;
+        if (li + 1 == pl_.lv.size()) CK(cudaEventRecord(ev_fin.a, st));
+        launches(launch_level<T>(a, L.nblocks, true, nullptr, dOut, codes, nullptr, zpos, nz, dunpred, st));
+    }
+    CK(cudaEventRecord(ev_fin.b, st));
+    CK(cudaEventRecord(ev_pred.b, st));
+    int *hk = (int *)t_pin_small.get(64);
+    CK(cudaMemcpyAsync(hk, kerr, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (*hk) throw Fail{FAZ_ERR_DEVICE, "level kernel met an out-of-range stream position"};
+    tm.huffman_ms = ev_dec.ms();
+    tm.predict_ms = ev_pred.ms();
+    tm.finest_level_ms = pl_.lv.empty() ? 0.0 : ev_fin.ms();
+}
+
+// Split a stream into trailer config and zstd-decompressed payload (pinned).
+void open_stream(const char *cmp, size_t cmp_size, faz_config &conf, uint8_t *&payload, size_t &psize,
+                 faz_timings &tm) {
+    if (!cmp || cmp_size < 4) throw Fail{FAZ_ERR_FORMAT, "stream too short"};
+    int32_t cs;
+    std::memcpy(&cs, cmp + cmp_size - 4, 4);
+    if (cs <= 0 || (size_t)cs + 4 > cmp_size) throw Fail{FAZ_ERR_FORMAT, "bad trailer size"};
+    int rc = config_load(conf, (const uint8_t *)cmp + cmp_size - 4 - cs, (size_t)cs);
+    if (rc) throw Fail{rc, "bad stream trailer"};
+    size_t body = cmp_size - 4 - cs;
+    if (body < 8) throw Fail{FAZ_ERR_FORMAT, "stream too short"};
+    uint64_t raw;
+    std::memcpy(&raw, cmp, 8);
+    std::string err;
+    const Zstd &z = zstd_lib(err);
+    if (!z.ok) throw Fail{FAZ_ERR_ZSTD, err};
+    if (raw > ((uint64_t)1 << 46)) throw Fail{FAZ_ERR_FORMAT, "implausible payload size"};
+    payload = t_pin_payload.get(raw + 64);
+    auto t0 = clk::now();
+    size_t got = z.decompress(payload, raw, cmp + 8, body - 8);
+    tm.zstd_ms += ms_since(t0);
+    if (z.isError(got) || got != raw) throw Fail{FAZ_ERR_ZSTD, "ZSTD_decompress failed"};
+    psize = raw;
+}
+
+template <typename T>
+int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void **out, bool on_device, void *dOutUser,
+                    void *user_stream, faz_timings *tmo) {
+    faz_timings tm;
+    std::memset(&tm, 0, sizeof(tm));
+    auto t0 = clk::now();
+    try {
+        if (!conf_io) throw Fail{FAZ_ERR_ARG, "null config"};
+        // a caller-provided output holds conf->num values
+        const uint64_t cap = conf_io->num;
+        const bool caller_buffer = on_device || (out && *out);
+        faz_config c;
+        uint8_t *payload;
+        size_t psize;
+        open_stream(cmp, cmp_size, c, payload, psize, tm);
+        if (c.cmprAlgo != FAZ_ALGO_INTERP)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "only ALGO_INTERP streams are implemented on the GPU path"};
+        if (c.wavelet != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet streams are not part of the interpolation path"};
+        if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
+        if (caller_buffer && cap < c.num)
+            throw Fail{FAZ_ERR_ARG, "output buffer holds fewer values than the stream's field"};
+        Parsed P;
+        P.conf = c;
+        parse_payload(payload, psize, c.N, P);
+        for (int i = 0; i < c.N; i++)
+            if (P.dims[i] != c.dims[i]) throw Fail{FAZ_ERR_FORMAT, "header dims differ from trailer dims"};
+        init_pool_once();
+        StreamGuard sg(user_stream);
+        cudaStream_t st = sg.st;
+        Counter launches;
+        Events ev_gpu, ev_d2h;
+        DevMem m(st);
+        T *dOut;
+        if (on_device) {
+            if (!dOutUser) throw Fail{FAZ_ERR_ARG, "null output"};
+            dOut = (T *)dOutUser;
+        } else {
+            if (!out) throw Fail{FAZ_ERR_ARG, "null output"};
+            dOut = m.alloc<T>(c.num);
+        }
+        CK(cudaEventRecord(ev_gpu.a, st));
+        decompress_device<T>(payload, psize, P, dOut, st, tm, launches);
+        CK(cudaEventRecord(ev_gpu.b, st));
+        if (!on_device) {
+            bool alloc = *out == nullptr;
+            T *h = alloc ? (T *)std::malloc(c.num * sizeof(T)) : (T *)*out;
+            if (!h) throw Fail{FAZ_ERR_ARG, "out of host memory"};
+            CK(cudaEventRecord(ev_d2h.a, st));
+            cudaError_t e = cudaMemcpyAsync(h, dOut, c.num * sizeof(T), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaEventRecord(ev_d2h.b, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
+                if (alloc) std::free(h);
+                throw Fail{FAZ_ERR_CUDA, std::string("device to host copy: ") + cudaGetErrorString(e)};
+            }
+            tm.d2h_ms = ev_d2h.ms();
+            *out = h;
+        } else {
+            CK(cudaStreamSynchronize(st));
+        }
+        tm.gpu_ms = ev_gpu.ms();
+        tm.payload_bytes = psize;
+        tm.unpred_count = P.nunpred;
+        tm.kernel_launches = launches.n;
+        *conf_io = c;
+        conf_io->interp_list_len = P.nlist;
+        for (int i = 0; i < P.nlist; i++) {
+            conf_io->interpAlgo_list[i] = P.il[i];
+            conf_io->interpDirection_list[i] = P.dl[i];
+        }
+    } catch (const Fail &f) {
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return FAZ_ERR_ARG;
+    }
+    tm.total_ms = ms_since(t0);
+    if (tmo) *tmo = tm;
+    return FAZ_OK;
+}
+
+template <typename T>
+int decompress_payload_impl(int N, const char *payload, size_t psize, void *d_out, uint64_t cap, void *user_stream,
+                            faz_timings *tmo) {
+    faz_timings tm;
+    std::memset(&tm, 0, sizeof(tm));
+    auto t0 = clk::now();
+    try {
+        if (N < 1 || N > 3) throw Fail{N == 4 ? FAZ_ERR_UNSUPPORTED : FAZ_ERR_ARG, "N must be 1..3 on the GPU path"};
+        if (!payload || !d_out) throw Fail{FAZ_ERR_ARG, "null argument"};
+        Parsed P;
+        std::memset(&P.conf, 0, sizeof(P.conf));
+        parse_payload((const uint8_t *)payload, psize, N, P);
+        uint64_t num = 1;
+        for (int i = 0; i < N; i++) num *= P.dims[i];
+        if (cap < num) throw Fail{FAZ_ERR_ARG, "output buffer holds fewer values than the payload's field"};
+        init_pool_once();
+        StreamGuard sg(user_stream);
+        Counter launches;
+        Events ev_gpu;
+        CK(cudaEventRecord(ev_gpu.a, sg.st));
+        decompress_device<T>((const uint8_t *)payload, psize, P, (T *)d_out, sg.st, tm, launches);
+        CK(cudaEventRecord(ev_gpu.b, sg.st));
+        CK(cudaStreamSynchronize(sg.st));
+        tm.gpu_ms = ev_gpu.ms();
+        tm.payload_bytes = psize;
+        tm.unpred_count = P.nunpred;
+        tm.kernel_launches = launches.n;
+    } catch (const Fail &f) {
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return FAZ_ERR_ARG;
+    }
+    tm.total_ms = ms_since(t0);
+    if (tmo) *tmo = tm;
+    return FAZ_OK;
+}
+
+}  // namespace
+}  // namespace faz
+
+// ================================================================= C ABI
+extern "C" {
+
+int faz_config_init(faz_config *conf, int N, const uint64_t *dims) {
+    int rc = faz::config_init(conf, N, dims);
+    if (rc) faz::set_error("faz_config_init: N must be 1..4");
+    return rc;
+}
+
+int faz_config_load_ini(faz_config *conf, const char *path) {
+    if (!conf) return FAZ_ERR_ARG;
+    std::string err;
+    int rc = faz::config_load_ini(conf, path, err);
+    if (rc) faz::set_error(err);
+    return rc;
+}
+
+int faz_compress(const faz_config *conf, int dtype, const void *data, char **out, size_t *out_size,
+                 faz_timings *timings) {
+    if (dtype == FAZ_FLOAT) return faz::compress_impl<float>(conf, data, false, nullptr, out, out_size, timings);
+    if (dtype == FAZ_DOUBLE) return faz::compress_impl<double>(conf, data, false, nullptr, out, out_size, timings);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
+
+int faz_compress_device(const faz_config *conf, int dtype, const void *d_data, void *stream, char **out,
+                        size_t *out_size, faz_timings *timings) {
+    if (dtype == FAZ_FLOAT) return faz::compress_impl<float>(conf, d_data, true, stream, out, out_size, timings);
+    if (dtype == FAZ_DOUBLE) return faz::compress_impl<double>(conf, d_data, true, stream, out, out_size, timings);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
+
+int faz_decompress(faz_config *conf, int dtype, const char *cmp, size_t cmp_size, void **out, faz_timings *timings) {
+    if (dtype == FAZ_FLOAT) return faz::decompress_impl<float>(conf, cmp, cmp_size, out, false, nullptr, nullptr, timings);
+    if (dtype == FAZ_DOUBLE)
+        return faz::decompress_impl<double>(conf, cmp, cmp_size, out, false, nullptr, nullptr, timings);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
+
+int faz_decompress_device(faz_config *conf, int dtype, const char *cmp, size_t cmp_size, void *d_out, void *stream,
+                          faz_timings *timings) {
+    if (dtype == FAZ_FLOAT)
+        return faz::decompress_impl<float>(conf, cmp, cmp_size, nullptr, true, d_out, stream, timings);
+    if (dtype == FAZ_DOUBLE)
+        return faz::decompress_impl<double>(conf, cmp, cmp_size, nullptr, true, d_out, stream, timings);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
+
+int faz_compress_device_payload(const faz_config *conf, int dtype, const void *d_data, void *stream, char **out,
+                                size_t *out_size, faz_config *conf_out, faz_timings *timings) {
+    if (dtype == FAZ_FLOAT)
+        return faz::compress_payload_impl<float>(conf, d_data, stream, out, out_size, conf_out, timings);
+    if (dtype == FAZ_DOUBLE)
+        return faz::compress_payload_impl<double>(conf, d_data, stream, out, out_size, conf_out, timings);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
+
+int faz_decompress_payload_device(int N, int dtype, const char *payload, size_t size, void *d_out, uint64_t capacity,
+                                  void *stream, faz_timings *timings) {
+    if (dtype == FAZ_FLOAT)
+        return faz::decompress_payload_impl<float>(N, payload, size, d_out, capacity, stream, timings);
+    if (dtype == FAZ_DOUBLE)
+        return faz::decompress_payload_impl<double>(N, payload, size, d_out, capacity, stream, timings);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
+
+size_t faz_config_size(void) { return sizeof(faz_config); }
+
+void faz_free(void *p) { std::free(p); }
+
+const char *faz_last_error(void) { return faz::last_error(); }
+
+unsigned faz_zstd_version(void) {
+    std::string err;
+    const faz::Zstd &z = faz::zstd_lib(err);
+    return z.ok ? z.version : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+// internal.h - host-side declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/faz_gb300.h"
+#include "common.cuh"
+
+namespace faz {
+
+// ---------------------------------------------------------------- kernels
+template <typename T>
+cudaError_t launch_minmax(const T *X, uint64_t n, T *pmin, T *pmax, int nblocks, cudaStream_t st);
+template <typename T>
+size_t level_smem_bytes(const LevelArgs &a);
+template <typename T>
+cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const T *X, T *W, uint16_t *codes,
+                         T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st);
+template <typename T>
+cudaError_t launch_first_point(bool decomp, const T *X, T *W, uint16_t *codes, T *scratch, double eb, int radius,
+                               int trim, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st);
+template <typename T>
+cudaError_t launch_anchors(bool decomp, const T *X, T *W, uint16_t *codes, T *scratch, const T *unpred,
+                           const int64_t *na, const int64_t *step, const int64_t *offs, cudaStream_t st);
+
+cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, uint64_t chunk, int center,
+                             unsigned long long *hist, unsigned long long *first, unsigned long long *zcount,
+                             cudaStream_t st);
+template <typename T>
+cudaError_t launch_gather_unpred(const uint16_t *codes, uint64_t n, uint64_t chunk, const unsigned long long *zcount,
+                                 const unsigned long long *zoff, const T *scratch, T *unpred, cudaStream_t st);
+cudaError_t launch_count_zeros(const uint16_t *codes, uint64_t n, uint64_t chunk, unsigned long long *zcount,
+                               cudaStream_t st);
+cudaError_t launch_zero_positions(const uint16_t *codes, uint64_t n, uint64_t chunk, const unsigned long long *zcount,
+                                  const unsigned long long *zoff, uint64_t *zpos, cudaStream_t st);
+cudaError_t launch_scan_u64(const unsigned long long *in, unsigned long long *out, uint64_t n, cudaStream_t st);
+uint64_t encode_chunks(uint64_t n);
+cudaError_t launch_encode_bits(const uint16_t *codes, uint64_t n, int offset, const uint8_t *len,
+                               unsigned long long *chunkbits, cudaStream_t st);
+cudaError_t launch_encode_pack(const uint16_t *codes, uint64_t n, int offset, const unsigned long long *code64,
+                               const uint8_t *len, const unsigned long long *chunkoff, uint32_t *out, int maxlen,
+                               cudaStream_t st);
+
+struct DecodeTablesDev {
+    const uint32_t *lut;
+    const uint32_t *left, *right;
+    const int32_t *sym;
+    const uint8_t *leaf;
+};
+cudaError_t launch_decode_sync(const DecodeTablesDev &t, const uint64_t *w, uint64_t nbits, uint64_t unit,
+                               uint64_t nunits, const uint64_t *end_in, uint64_t *start, uint64_t *end_out,
+                               unsigned int *cnt, int refine, int *changed, cudaStream_t st);
+cudaError_t launch_decode_write(const DecodeTablesDev &t, const uint64_t *w, uint64_t nbits, uint64_t unit,
+                                uint64_t nunits, const uint64_t *start, const unsigned long long *off, uint64_t nout,
+                                int offset, uint16_t *out, cudaStream_t st);
+cudaError_t launch_fill_u16(uint16_t *out, uint64_t n, uint16_t v, cudaStream_t st);
+cudaError_t launch_widen_counts(const unsigned int *cnt, unsigned long long *out, uint64_t n, cudaStream_t st);
+
+// ------------------------------------------------------------ Huffman host
+struct Codebook {
+    int offset = 0;          // smallest symbol
+    int stateNum = 0;        // max - min + 2
+    int nodeCount = 0;       // 2 * distinct - 1
+    int maxlen = 0;
+    std::vector<uint64_t> code;  // per state, MSB-aligned
+    std::vector<uint8_t> len;    // per state
+    std::vector<uint8_t> tree;   // serialised tree (HuffmanEncoder::save body after the two ints)
+};
+// Build the reference codebook from symbol counts and first-occurrence
+// positions (symbols with count 0 are absent).
+int build_codebook(const std::vector<int> &syms, const std::vector<uint64_t> &counts,
+                   const std::vector<uint64_t> &first, Codebook &cb, std::string &err);
+
+struct DecodeTablesHost {
+    int offset = 0;
+    int nodeCount = 0;
+    bool constant = false;       // single-symbol stream
+    int constant_state = 0;
+    std::vector<uint32_t> lut, left, right;
+    std::vector<int32_t> sym;
+    std::vector<uint8_t> leaf;
+};
+// Parse HuffmanEncoder::save output at p (advances p); builds decode tables.
+int parse_tree(const uint8_t *&p, const uint8_t *end, DecodeTablesHost &t, std::string &err);
+constexpr int kLutBits = 12;
+
+// -------------------------------------------------------------- stream/io
+void config_save(const faz_config &c, std::vector<uint8_t> &out);
+int config_load(faz_config &c, const uint8_t *p, size_t n);
+int config_init(faz_config *c, int N, const uint64_t *dims);
+int config_load_ini(faz_config *c, const char *path, std::string &err);
+
+struct Zstd {
+    bool ok = false;
+    unsigned version = 0;
+    size_t (*compress)(void *, size_t, const void *, size_t, int) = nullptr;
+    size_t (*decompress)(void *, size_t, const void *, size_t) = nullptr;
+    unsigned (*isError)(size_t) = nullptr;
+    size_t (*bound)(size_t) = nullptr;
+    unsigned long long (*frameContentSize)(const void *, size_t) = nullptr;
+};
+const Zstd &zstd_lib(std::string &err);
+
+// ------------------------------------------------------------------ errors
+void set_error(const std::string &msg);
+
+}  // namespace faz

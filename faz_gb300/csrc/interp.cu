@@ -1,0 +1,472 @@
+// interp.cu - multilevel interpolation predictor + linear quantiser kernels.
+//
+// One CTA per interpolation block and level (SZInterpolationCompressor.hpp
+// 384-461 compress, 106-196 decompress).  The block's lattice points with an
+// even index along the last sweep axis live in shared memory; sweep 1 and 2
+// targets are computed there, sweep 3 targets stream from global memory.
+// Lines on the block's first planes, which the reference assigns to the
+// previous block, are recomputed (never emitted) so that every block of a
+// level runs independently.  Codes of a sweep are staged in shared memory and
+// written to their stream positions in one coalesced pass.
+//
+// Arithmetic follows the reference's types and operation order (compiled with
+// -fmad=false): stencils in T (include/QoZ/utils/Interpolators.hpp:9-36),
+// quantiser in the T/double mix of include/QoZ/quantizer/IntegerQuantizer.hpp:69-179.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cfloat>
+#include "common.cuh"
+#include "internal.h"
+
+namespace faz {
+
+// ---------------------------------------------------------------- stencils
+// x/2^k is exact scaling, identical to the reference's division.
+template <typename T> __device__ __forceinline__ T i_linear(T a, T b) { return (a + b) * (T)0.5; }
+template <typename T> __device__ __forceinline__ T i_linear1(T a, T b) {
+    return (T)(-0.5 * (double)a + 1.5 * (double)b);
+}
+template <typename T> __device__ __forceinline__ T i_quad1(T a, T b, T c) {
+    return ((T)3 * a + (T)6 * b - c) * (T)0.125;
+}
+template <typename T> __device__ __forceinline__ T i_quad2(T a, T b, T c) {
+    return (-a + (T)6 * b + (T)3 * c) * (T)0.125;
+}
+template <typename T> __device__ __forceinline__ T i_quad3(T a, T b, T c) {
+    return ((T)3 * a - (T)10 * b + (T)15 * c) * (T)0.125;
+}
+template <typename T> __device__ __forceinline__ T i_cubic(T a, T b, T c, T d) {
+    return (-a + (T)9 * b + (T)9 * c - d) * (T)0.0625;
+}
+
+// Prediction of odd index m on a line of n lattice points; value at index k
+// is p[(k >> sh) * st].
+template <typename T>
+__device__ __forceinline__ T predict(const T *p, int st, int sh, int m, int n, int cubic) {
+#define V_(k) p[((k) >> sh) * st]
+    if (!cubic || n < 5) {
+        if (m + 1 < n) return i_linear(V_(m - 1), V_(m + 1));
+        return n < 4 ? V_(m - 1) : i_linear1(V_(m - 3), V_(m - 1));
+    }
+    int ia = (n & 1) ? n - 2 : n - 3;
+    if (m == 1) return i_quad1(V_(0), V_(2), V_(4));
+    if (m == ia) return i_quad2(V_(m - 3), V_(m - 1), V_(m + 1));
+    if (m == n - 1) return i_quad3(V_(m - 5), V_(m - 3), V_(m - 1));
+    return i_cubic(V_(m - 3), V_(m - 1), V_(m + 1), V_(m + 3));
+#undef V_
+}
+
+// LinearQuantizer::quantize_and_overwrite (IntegerQuantizer.hpp:69-108).
+// Returns the code; v becomes the reconstruction when predictable; uval is
+// the value recorded as unpredictable when the code is 0.
+template <typename T>
+__device__ __forceinline__ int quantize(T &v, T pred, double eb, double recip, int radius, int trim, T &uval) {
+    T orig = v;
+    if (trim > 0 && fabs((double)orig) <= eb) {
+        v = 0;
+        uval = 0;
+        return trim - 1;
+    }
+    T diff = orig - pred;
+    double x = (double)(diff < 0 ? -diff : diff) * recip;
+    uval = orig;
+    if (!(x < 2147483647.0)) return 0;
+    int qi = (int)x + 1;
+    if (qi >= 2 * radius) return 0;
+    int half = qi >> 1;
+    int q2 = half << 1;
+    int code;
+    if (diff < 0) {
+        q2 = -q2;
+        code = radius - half;
+    } else {
+        code = radius + half;
+    }
+    T dec = (T)((double)pred + (double)q2 * eb);
+    T err = dec - orig;
+    if (fabs((double)err) > eb || (trim == 2 && code == 1)) return 0;
+    v = dec;
+    return code;
+}
+
+// LinearQuantizer::recover (IntegerQuantizer.hpp:160-179); code 0 reads the
+// unpredictable value of stream position pos.
+template <typename T>
+__device__ __forceinline__ T recover(T pred, int code, uint64_t pos, double eb, int radius, int trim,
+                                     const uint64_t *zpos, uint64_t nz, const T *unpred) {
+    if (trim == 2 && code == 1) return 0;
+    if (code) return (T)((double)pred + (double)(2 * (code - radius)) * eb);
+    uint64_t lo = 0, hi = nz;
+    while (lo < hi) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (zpos[mid] < pos) lo = mid + 1; else hi = mid;
+    }
+    return lo < nz ? unpred[lo] : (T)0;
+}
+
+// --------------------------------------------------------- level kernel
+template <typename T, bool DECOMP>
+__global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
+                                                      uint16_t *__restrict__ codes, T *__restrict__ scratch,
+                                                      const uint64_t *__restrict__ zpos, uint64_t nz,
+                                                      const T *__restrict__ unpred) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *V = reinterpret_cast<T *>(smem_raw);
+    uint16_t *stg = reinterpret_cast<uint16_t *>(smem_raw + (size_t)a.vwords * sizeof(T));
+    const int64_t bid = blockIdx.x;
+    int64_t bc[3];
+    block_coords(a, bid, bc);
+    BlockGeom g;
+    block_geom(a, bc, g);
+    const int P0 = a.perm[0], P1 = a.perm[1], P2 = a.perm[2];
+    const int n0 = g.n0, n1 = g.n1, n2 = g.n2, h2 = g.h2;
+    const int k0 = g.k0, k1 = g.k1, k2 = g.k2;
+    const int64_t G0 = a.s * a.offs[P0], G1 = a.s * a.offs[P1], G2 = a.s * a.offs[P2];
+    const int64_t gbase = g.beg[0] * a.offs[0] + g.beg[1] * a.offs[1] + g.beg[2] * a.offs[2];
+    const uint64_t base = a.block_off[bid];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const double eb = a.eb, recip = a.recip;
+    const int radius = a.radius, trim = a.trim, cubic = a.cubic;
+
+    // phase 0: lattice points with even index along P2
+    const int nv = n0 * n1 * h2;
+    for (int i = tid; i < nv; i += nt) {
+        int e = i % h2;
+        int q = i / h2;
+        int m1 = q % n1;
+        int m0 = q / n1;
+        int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)(2 * e) * G2;
+        bool coarse = !(m0 & 1) && !(m1 & 1);
+        if (coarse) V[i] = W[gi];
+        else if (!DECOMP) V[i] = X[gi];
+    }
+    __syncthreads();
+
+    // sweep 1: lines along P0 at even (m1, m2), including first-plane lines
+    const int hh1 = (n1 + 1) / 2;
+    if (g.t0 > 0) {
+        const int64_t cnt = g.c1;
+        if (DECOMP) {
+            for (int64_t i = tid; i < cnt; i += nt) stg[i] = codes[base + i];
+            __syncthreads();
+        }
+        const int st = n1 * h2;
+        const int total = g.t0 * hh1 * h2;
+        for (int w = tid; w < total; w += nt) {
+            int e2 = w % h2;
+            int q = w / h2;
+            int e1 = q % hh1;
+            int t = q / hh1;
+            int m0 = 2 * t + 1, m1 = 2 * e1;
+            int col = m1 * h2 + e2;
+            T pred = predict(V + col, st, 0, m0, n0, cubic);
+            int idx = m0 * st + col;
+            bool emit = e1 >= k1 && e2 >= k2;
+            int rank = 0;
+            if (emit) rank = ((e1 - k1) * g.ne2 + (e2 - k2)) * g.t0 + line_rank(m0, n0, cubic);
+            int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)(2 * e2) * G2;
+            if (!DECOMP) {
+                T v = V[idx], uv;
+                int code = quantize(v, pred, eb, recip, radius, trim, uv);
+                V[idx] = v;
+                if (emit) {
+                    stg[rank] = (uint16_t)code;
+                    if (code == 0) scratch[base + rank] = uv;
+                    if (a.write_back) W[gi] = v;
+                }
+            } else {
+                uint64_t pos;
+                int code;
+                if (emit) {
+                    pos = base + rank;
+                    code = stg[rank];
+                } else {
+                    // the previous block along P1 and/or P2 owns this line
+                    int64_t ob[3] = {bc[0], bc[1], bc[2]};
+                    bool s1 = e1 < k1, s2 = e2 < k2;
+                    if (s1) ob[P1] -= 1;
+                    if (s2) ob[P2] -= 1;
+                    int nf = (int)(a.bs / a.s) + 1;
+                    int on2 = s2 ? nf : n2;
+                    int ok1 = ob[P1] != 0, ok2 = ob[P2] != 0;
+                    int oe1 = s1 ? (nf - 1) / 2 : e1;
+                    int oe2 = s2 ? (nf - 1) / 2 : e2;
+                    int one2 = (on2 + 1) / 2 - ok2;
+                    int64_t oid = (ob[0] * a.nb[1] + ob[1]) * a.nb[2] + ob[2];
+                    pos = a.block_off[oid] + (uint64_t)((oe1 - ok1) * one2 + (oe2 - ok2)) * g.t0 +
+                          line_rank(m0, n0, cubic);
+                    if (pos >= a.ncodes) {
+                        atomicExch(a.err, 1);
+                        pos = 0;
+                    }
+                    code = codes[pos];
+                }
+                T v = recover(pred, code, pos, eb, radius, trim, zpos, nz, unpred);
+                V[idx] = v;
+                if (emit) W[gi] = v;
+            }
+        }
+        __syncthreads();
+        if (!DECOMP) {
+            for (int64_t i = tid; i < cnt; i += nt) codes[base + i] = stg[i];
+            __syncthreads();
+        }
+    }
+
+    // sweep 2: lines along P1 at (m0 any, m2 even); the m0 = 0 plane of a
+    // non-first block is not needed by sweep 3 and is skipped.
+    if (g.t1 > 0) {
+        const int64_t cnt = g.c2;
+        const uint64_t sbase = base + g.c1;
+        if (DECOMP) {
+            for (int64_t i = tid; i < cnt; i += nt) stg[i] = codes[sbase + i];
+            __syncthreads();
+        }
+        const int total = (n0 - k0) * g.t1 * h2;
+        for (int w = tid; w < total; w += nt) {
+            int e2 = w % h2;
+            int q = w / h2;
+            int t = q % g.t1;
+            int m0 = k0 + q / g.t1;
+            int m1 = 2 * t + 1;
+            int col = m0 * n1 * h2 + e2;
+            T pred = predict(V + col, h2, 0, m1, n1, cubic);
+            int idx = col + m1 * h2;
+            bool emit = e2 >= k2;
+            int rank = 0;
+            if (emit) rank = ((m0 - k0) * g.ne2 + (e2 - k2)) * g.t1 + line_rank(m1, n1, cubic);
+            int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)(2 * e2) * G2;
+            if (!DECOMP) {
+                T v = V[idx], uv;
+                int code = quantize(v, pred, eb, recip, radius, trim, uv);
+                V[idx] = v;
+                if (emit) {
+                    stg[rank] = (uint16_t)code;
+                    if (code == 0) scratch[sbase + rank] = uv;
+                    if (a.write_back) W[gi] = v;
+                }
+            } else {
+                uint64_t pos;
+                int code;
+                if (emit) {
+                    pos = sbase + rank;
+                    code = stg[rank];
+                } else {
+                    // the previous block along P2 owns this line
+                    int64_t ob[3] = {bc[0], bc[1], bc[2]};
+                    ob[P2] -= 1;
+                    int nf = (int)(a.bs / a.s) + 1;
+                    int ok2 = ob[P2] != 0;
+                    int oe2 = (nf - 1) / 2;
+                    int one2 = (nf + 1) / 2 - ok2;
+                    int64_t oc1 = (int64_t)g.ne1 * one2 * g.t0;
+                    int64_t oid = (ob[0] * a.nb[1] + ob[1]) * a.nb[2] + ob[2];
+                    pos = a.block_off[oid] + oc1 + (uint64_t)((m0 - k0) * one2 + (oe2 - ok2)) * g.t1 +
+                          line_rank(m1, n1, cubic);
+                    if (pos >= a.ncodes) {
+                        atomicExch(a.err, 1);
+                        pos = 0;
+                    }
+                    code = codes[pos];
+                }
+                T v = recover(pred, code, pos, eb, radius, trim, zpos, nz, unpred);
+                V[idx] = v;
+                if (emit) W[gi] = v;
+            }
+        }
+        __syncthreads();
+        if (!DECOMP) {
+            for (int64_t i = tid; i < cnt; i += nt) codes[sbase + i] = stg[i];
+            __syncthreads();
+        }
+    }
+
+    // sweep 3: lines along P2 at (m0, m1), emitted lines only
+    if (g.t2 > 0) {
+        const int64_t cnt = g.c3;
+        const uint64_t sbase = base + g.c1 + g.c2;
+        if (DECOMP) {
+            for (int64_t i = tid; i < cnt; i += nt) stg[i] = codes[sbase + i];
+            __syncthreads();
+        }
+        const int w1 = n1 - k1;
+        const int total = (int)cnt;
+        for (int w = tid; w < total; w += nt) {
+            int t = w % g.t2;
+            int q = w / g.t2;
+            int m1 = k1 + q % w1;
+            int m0 = k0 + q / w1;
+            int m2 = 2 * t + 1;
+            const T *row = V + (m0 * n1 + m1) * h2;
+            T pred = predict(row, 1, 1, m2, n2, cubic);
+            int rank = q * g.t2 + line_rank(m2, n2, cubic);
+            int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)m2 * G2;
+            if (!DECOMP) {
+                T v = X[gi], uv;
+                int code = quantize(v, pred, eb, recip, radius, trim, uv);
+                stg[rank] = (uint16_t)code;
+                if (code == 0) scratch[sbase + rank] = uv;
+                if (a.write_back) W[gi] = v;
+            } else {
+                uint64_t pos = sbase + rank;
+                W[gi] = recover(pred, (int)stg[rank], pos, eb, radius, trim, zpos, nz, unpred);
+            }
+        }
+        __syncthreads();
+        if (!DECOMP) {
+            for (int64_t i = tid; i < cnt; i += nt) codes[sbase + i] = stg[i];
+        }
+    }
+}
+
+// ------------------------------------------------- first point / anchors
+// First point quantised against prediction 0 with the base bound
+// (SZInterpolationCompressor.hpp:372-374), or the anchor grid of build_grid
+// (854-900) as unpredictable values with code 0.
+template <typename T>
+__global__ void k_first_point(const T *X, T *W, uint16_t *codes, T *scratch, double eb, double recip, int radius,
+                              int trim) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        T v = X[0], uv;
+        int code = quantize(v, (T)0, eb, recip, radius, trim, uv);
+        codes[0] = (uint16_t)code;
+        if (code == 0) scratch[0] = uv;
+        W[0] = v;
+    }
+}
+
+template <typename T>
+__global__ void k_first_point_dec(const uint16_t *codes, T *W, double eb, int radius, int trim,
+                                  const uint64_t *zpos, uint64_t nz, const T *unpred) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) W[0] = recover((T)0, (int)codes[0], 0, eb, radius, trim, zpos, nz, unpred);
+}
+
+// anchors at multiples of maxStep on axes 0..2 (3-D view); na0..na2 anchors per axis
+template <typename T, bool DECOMP>
+__global__ void k_anchors(const T *X, T *W, uint16_t *codes, T *scratch, const T *unpred, int64_t na0, int64_t na1,
+                          int64_t na2, int64_t step0, int64_t step1, int64_t step2, int64_t o0, int64_t o1,
+                          int64_t o2) {
+    int64_t total = na0 * na1 * na2;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t z = i % na2, r = i / na2;
+        int64_t y = r % na1, x = r / na1;
+        int64_t gi = x * step0 * o0 + y * step1 * o1 + z * step2 * o2;
+        if (!DECOMP) {
+            T v = X[gi];
+            codes[i] = 0;
+            scratch[i] = v;
+            W[gi] = v;
+        } else {
+            W[gi] = unpred[i];
+        }
+    }
+}
+
+// ------------------------------------------------------------- min / max
+template <typename T>
+__global__ void k_minmax(const T *__restrict__ X, uint64_t n, T *pmin, T *pmax) {
+    T mn = X[0], mx = X[0];
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        T v = X[i];
+        mn = v < mn ? v : mn;
+        mx = v > mx ? v : mx;
+    }
+    __shared__ T smn[32], smx[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        T a = __shfl_down_sync(0xffffffffu, mn, o);
+        T b = __shfl_down_sync(0xffffffffu, mx, o);
+        mn = a < mn ? a : mn;
+        mx = b > mx ? b : mx;
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { smn[wid] = mn; smx[wid] = mx; }
+    __syncthreads();
+    if (wid == 0) {
+        int nw = blockDim.x >> 5;
+        mn = lane < nw ? smn[lane] : smn[0];
+        mx = lane < nw ? smx[lane] : smx[0];
+        for (int o = 16; o > 0; o >>= 1) {
+            T a = __shfl_down_sync(0xffffffffu, mn, o);
+            T b = __shfl_down_sync(0xffffffffu, mx, o);
+            mn = a < mn ? a : mn;
+            mx = b > mx ? b : mx;
+        }
+        if (lane == 0) { pmin[blockIdx.x] = mn; pmax[blockIdx.x] = mx; }
+    }
+}
+
+// ------------------------------------------------------------ launchers
+
+template <typename T>
+cudaError_t launch_minmax(const T *X, uint64_t n, T *pmin, T *pmax, int nblocks, cudaStream_t st) {
+    k_minmax<T><<<nblocks, 512, 0, st>>>(X, n, pmin, pmax);
+    return cudaGetLastError();
+}
+
+template <typename T>
+size_t level_smem_bytes(const LevelArgs &a) {
+    size_t vb = ((size_t)a.vwords * sizeof(T) + 15) / 16 * 16;
+    return vb + (size_t)a.stage_cap * sizeof(uint16_t);
+}
+
+template <typename T>
+cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const T *X, T *W, uint16_t *codes,
+                         T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st) {
+    size_t sm = level_smem_bytes<T>(a);
+    int threads = 512;
+    int64_t vol = (int64_t)a.vwords * 2;
+    if (vol < 2048) threads = 256;
+    if (vol < 512) threads = 128;
+    if (vol < 128) threads = 64;
+    if (!decomp) {
+        auto k = k_interp_level<T, false>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        k<<<(unsigned)nblocks, threads, sm, st>>>(a, X, W, codes, scratch, zpos, nz, unpred);
+    } else {
+        auto k = k_interp_level<T, true>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        k<<<(unsigned)nblocks, threads, sm, st>>>(a, X, W, codes, scratch, zpos, nz, unpred);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_first_point(bool decomp, const T *X, T *W, uint16_t *codes, T *scratch, double eb, int radius,
+                               int trim, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st) {
+    if (!decomp) k_first_point<T><<<1, 32, 0, st>>>(X, W, codes, scratch, eb, 1.0 / eb, radius, trim);
+    else k_first_point_dec<T><<<1, 32, 0, st>>>(codes, W, eb, radius, trim, zpos, nz, unpred);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_anchors(bool decomp, const T *X, T *W, uint16_t *codes, T *scratch, const T *unpred,
+                           const int64_t *na, const int64_t *step, const int64_t *offs, cudaStream_t st) {
+    int64_t total = na[0] * na[1] * na[2];
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    if (blocks < 1) blocks = 1;
+    if (!decomp)
+        k_anchors<T, false><<<blocks, 256, 0, st>>>(X, W, codes, scratch, unpred, na[0], na[1], na[2], step[0], step[1],
+                                                     step[2], offs[0], offs[1], offs[2]);
+    else
+        k_anchors<T, true><<<blocks, 256, 0, st>>>(X, W, codes, scratch, unpred, na[0], na[1], na[2], step[0], step[1],
+                                                    step[2], offs[0], offs[1], offs[2]);
+    return cudaGetLastError();
+}
+
+#define INST(T)                                                                                                  \
+    template cudaError_t launch_minmax<T>(const T *, uint64_t, T *, T *, int, cudaStream_t);                     \
+    template size_t level_smem_bytes<T>(const LevelArgs &);                                                      \
+    template cudaError_t launch_level<T>(const LevelArgs &, int64_t, bool, const T *, T *, uint16_t *, T *,      \
+                                         const uint64_t *, uint64_t, const T *, cudaStream_t);                   \
+    template cudaError_t launch_first_point<T>(bool, const T *, T *, uint16_t *, T *, double, int, int,          \
+                                               const uint64_t *, uint64_t, const T *, cudaStream_t);             \
+    template cudaError_t launch_anchors<T>(bool, const T *, T *, uint16_t *, T *, const T *, const int64_t *,   \
+                                           const int64_t *, const int64_t *, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace faz

@@ -149,6 +149,9 @@ typedef struct faz_timings {
     double d2h_ms;         /* device -> host copy of the result */
     double zstd_ms;        /* host zstd stage */
     double host_ms;        /* host codebook / stream assembly */
+    double predict_ms;     /* interpolation level kernels (CUDA events) */
+    double finest_level_ms;    /* the finest (last) level kernel alone */
+    double huffman_ms;     /* histogram + codebook + encode, or decode */
     uint64_t payload_bytes;    /* pre-zstd payload */
     uint64_t unpred_count;
     uint64_t kernel_launches;  /* kernels this library launched in the call */
@@ -167,10 +170,11 @@ int faz_config_load_ini(faz_config *conf, const char *path);
 int faz_compress(const faz_config *conf, int dtype, const void *data,
                  char **out, size_t *out_size, faz_timings *timings);
 
-/* SZ_decompress<T> - sz.hpp:159-205.  Reads the trailer into *conf, then
- * decodes.  If *out is NULL the library allocates conf->num values (release
- * with faz_free); otherwise *out must hold conf->num values.  Unlike the
- * reference, no side file is written. */
+/* SZ_decompress<T> - sz.hpp:159-205.  Decodes the stream and returns its
+ * trailer configuration in *conf.  If *out is NULL the library allocates the
+ * output (release with faz_free); otherwise *out must hold conf->num values
+ * (conf->num on entry is the capacity; a larger field is rejected).  Unlike
+ * the reference, no side file is written. */
 int faz_decompress(faz_config *conf, int dtype, const char *cmp, size_t cmp_size,
                    void **out, faz_timings *timings);
 
@@ -180,10 +184,30 @@ int faz_compress_device(const faz_config *conf, int dtype, const void *d_data,
                         void *stream, char **out, size_t *out_size,
                         faz_timings *timings);
 
-/* Same as faz_decompress writing conf->num values into device memory d_out. */
+/* Same as faz_decompress writing into device memory d_out, which holds
+ * conf->num values on entry (a stream with a larger field is rejected). */
 int faz_decompress_device(faz_config *conf, int dtype, const char *cmp,
                           size_t cmp_size, void *d_out, void *stream,
                           faz_timings *timings);
+
+/* The GPU path without the host zstd stage, for callers that run their own
+ * lossless stage and for measuring the device work: compress device data to
+ * the pre-zstd payload (the bytes the reference hands to ZSTD_compress in
+ * SZInterpolationCompressor::compress, SZInterpolationCompressor.hpp:485-517).
+ * *conf_out (may be NULL) receives the configuration the trailer would hold. */
+int faz_compress_device_payload(const faz_config *conf, int dtype, const void *d_data,
+                                void *stream, char **out, size_t *out_size,
+                                faz_config *conf_out, faz_timings *timings);
+
+/* Decode a pre-zstd payload of an N-dimensional field into device memory
+ * d_out holding `capacity` values. */
+int faz_decompress_payload_device(int N, int dtype, const char *payload, size_t size,
+                                  void *d_out, uint64_t capacity, void *stream,
+                                  faz_timings *timings);
+
+/* sizeof(faz_config) as this library was compiled, for bindings that
+ * mirror the struct (ctypes, cgo, JNI) to check their layout. */
+size_t faz_config_size(void);
 
 /* Release a buffer returned by this library. */
 void faz_free(void *p);

@@ -1,0 +1,146 @@
+"""GPU path vs oracle and vs the reference's golden streams.
+
+Integer/byte work (codes, Huffman bits, stream bytes) and the decompressed
+arrays are compared bit for bit.  Full streams are compared where oracle and
+library use the same host zstd; the pre-zstd payloads always.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import faz_gb300 as F
+from faz_gb300.fields import spectral_field
+from conftest import (cli_config, golden_case, golden_input, golden_manifest, golden_stream, mask_first_size,
+                      tuned_config)
+
+import oracle.oracle as O
+
+pytestmark = pytest.mark.gpu
+
+# cases outside the GPU path: 4-D fields, and fixBlockSize values that break
+# the coarse-lattice alignment of blocks
+GPU_UNSUPPORTED = {"c4d_cubic", "c3d_fixbs8"}
+INI_CASES = [c["name"] for c in golden_manifest() if c["ini"] is not None and c["name"] not in GPU_UNSUPPORTED]
+TUNED_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None]
+DEC_CASES = [c["name"] for c in golden_manifest() if c["name"] not in GPU_UNSUPPORTED]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def system_zstd():
+    O.set_zstd(None)  # the oracle uses the same host zstd as the library
+    yield
+
+
+def payload_of(stream):
+    return O.read_stream(stream)[1]
+
+
+@pytest.mark.parametrize("name", INI_CASES)
+def test_gpu_stream_matches_reference_payload(name):
+    case = golden_case(name)
+    x = golden_input(case)
+    conf = cli_config(case)
+    stream = F.SZ_compress(conf, x)
+    assert payload_of(stream) == payload_of(golden_stream(case))
+    ref, _ = O.compress(conf, x)
+    assert mask_first_size(stream) == mask_first_size(ref)
+
+
+@pytest.mark.parametrize("name", TUNED_CASES)
+def test_gpu_payload_matches_tuned_reference(name):
+    case = golden_case(name)
+    conf = tuned_config(case)
+    stream = F.SZ_compress(conf, golden_input(case))
+    assert payload_of(stream) == payload_of(golden_stream(case))
+
+
+@pytest.mark.parametrize("name", DEC_CASES)
+def test_gpu_decompress_matches_reference(name):
+    case = golden_case(name)
+    dec, conf = F.SZ_decompress(None, golden_stream(case), dtype=np.dtype(case["dtype"]))
+    assert hashlib.sha256(dec.tobytes()).hexdigest() == case["dec_sha256"]
+
+
+def _conf(dims, rel=None, abs_=None, interp=F.INTERP_ALGO_CUBIC, direction=0, **kw):
+    c = F.Config(*dims)
+    c.cmprAlgo = F.ALGO_INTERP
+    c.interpAlgo = interp
+    c.interpDirection = direction
+    if rel is not None:
+        c.errorBoundMode = F.EB_REL
+        c.relErrorBound = rel
+    else:
+        c.errorBoundMode = F.EB_ABS
+        c.absErrorBound = abs_
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+RANDOM_CASES = [
+    ((97, 130, 161), dict(rel=1e-3), np.float32, -3.0),
+    ((64, 96, 128), dict(rel=1e-4, direction=5), np.float32, -2.5),
+    ((65, 66, 67), dict(rel=1e-2, interp=F.INTERP_ALGO_LINEAR, direction=2), np.float32, -3.5),
+    ((33, 200, 70), dict(rel=1e-5), np.float32, -2.0),
+    ((300, 400), dict(rel=1e-3, direction=1), np.float32, -3.0),
+    ((100000,), dict(rel=1e-3), np.float32, -2.0),
+    ((48, 50, 52), dict(rel=1e-6), np.float64, -3.0),
+    ((64, 64, 64), dict(rel=1e-3, maxStep=32, alpha=1.25, beta=2.0), np.float32, -3.0),
+    ((70, 80, 90), dict(rel=1e-3, interpAlgo_list=[1, 0, 1, 1], interpDirection_list=[0, 5, 3, 1],
+                        alpha=1.0, beta=1.5), np.float32, -3.0),
+]
+
+
+@pytest.mark.parametrize("dims,kw,dtype,slope", RANDOM_CASES)
+def test_gpu_matches_oracle_random_fields(dims, kw, dtype, slope):
+    lists = {k: kw.pop(k) for k in ("interpAlgo_list", "interpDirection_list") if k in kw}
+    conf = _conf(dims, **kw)
+    for k, v in lists.items():
+        setattr(conf, k, v)
+    x = spectral_field(dims, slope=slope, noise=0.02, seed=sum(dims), dtype=dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    assert payload_of(stream) == ref_payload
+    assert mask_first_size(stream) == mask_first_size(ref)
+    dec, c2 = F.SZ_decompress(None, stream, dtype=dtype)
+    ref_dec, _ = O.decompress(ref, dtype=dtype)
+    assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
+
+
+def test_device_tensor_api_roundtrip():
+    import torch
+    dims = (80, 90, 100)
+    x = spectral_field(dims, slope=-3.0, seed=5)
+    conf = _conf(dims, rel=1e-3)
+    t = torch.from_numpy(x).cuda()
+    s1 = F.SZ_compress(conf, t)
+    s2 = F.SZ_compress(conf, x)
+    assert mask_first_size(s1) == mask_first_size(s2)
+    out = torch.empty(dims, dtype=torch.float32, device="cuda")
+    c = F.decompress_device(s1, out)
+    ref_dec, _ = O.decompress(s1)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), ref_dec.view(np.uint32))
+    small = torch.empty(10, dtype=torch.float32, device="cuda")
+    with pytest.raises(F.FazError):
+        F.decompress_device(s1, small)
+    assert c.dims == list(dims)
+
+
+def test_large_field_round_trip_properties():
+    """512x512x256 float32: error bound holds everywhere, the stream decodes
+    to the oracle's array, and compressing twice gives the same bytes."""
+    import torch
+    dims = (256, 512, 512)
+    t = F.fields.spectral_field(dims, slope=-3.5, aniso=(1, 2, 4), noise=0.01, seed=11, device="cuda")
+    conf = _conf(dims, rel=1e-3)
+    s1 = F.SZ_compress(conf, t)
+    s2 = F.SZ_compress(conf, t)
+    assert s1 == s2
+    out = torch.empty(dims, dtype=torch.float32, device="cuda")
+    c = F.decompress_device(s1, out)
+    err = (out.double() - t.double()).abs().max().item()
+    assert err <= c.absErrorBound
+    ref_dec, _ = O.decompress(s1)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), ref_dec.view(np.uint32))
