@@ -19,6 +19,7 @@ STATUS = {0: "FAZ_OK", -1: "FAZ_ERR_ARG", -2: "FAZ_ERR_UNSUPPORTED", -3: "FAZ_ER
 
 EXPORTED = ["faz_config_init", "faz_config_load_ini", "faz_compress", "faz_decompress", "faz_compress_device",
             "faz_decompress_device", "faz_compress_device_payload", "faz_decompress_payload_device",
+            "faz_stream_info",
             "faz_config_size", "faz_free", "faz_last_error", "faz_zstd_version"]
 
 
@@ -49,7 +50,8 @@ def library():
         L.faz_last_error.restype = ctypes.c_char_p
         L.faz_zstd_version.restype = ctypes.c_uint
         L.faz_config_size.restype = ctypes.c_size_t
-        L.faz_compress_device_payload.argtypes = [vp, ctypes.c_int, vp, vp, P(vp), P(sz), vp, vp]
+        L.faz_compress_device_payload.argtypes = [vp, ctypes.c_int, vp, vp, vp, sz, P(sz), vp, vp]
+        L.faz_stream_info.argtypes = [vp, sz, vp]
         L.faz_decompress_payload_device.argtypes = [ctypes.c_int, ctypes.c_int, vp, sz, vp, ctypes.c_uint64, vp, vp]
         _lib = L
         return L
@@ -135,19 +137,32 @@ def compress_device(conf, tensor, stream=None):
     return _take_bytes(out, osz.value)
 
 
-def SZ_decompress(conf, stream_bytes, dtype=np.float32):
-    """Decompress a FAZ stream into a new numpy array shaped by the stream's
-    dims.  Returns (array, Config loaded from the stream's trailer)."""
-    buf = bytes(stream_bytes)
+def stream_info(stream_bytes):
+    """Config stored in a stream's trailer (dims, error bound, algorithm)."""
     s = FazConfigStruct()
-    out, tm = ctypes.c_void_p(), FazTimings()
-    _check(library().faz_decompress(ctypes.byref(s), _dtype_code(dtype), buf, len(buf), ctypes.byref(out),
+    _check(library().faz_stream_info(bytes(stream_bytes), len(stream_bytes), ctypes.byref(s)))
+    return Config.from_struct(s)
+
+
+def SZ_decompress(conf, stream_bytes, dtype=np.float32, out=None):
+    """Decompress a FAZ stream.  Writes into `out` (a contiguous numpy array
+    of the stream's size, e.g. in pinned memory) or a new array.  Returns
+    (array shaped by the stream's dims, Config loaded from the trailer)."""
+    buf = bytes(stream_bytes)
+    dtype = np.dtype(dtype)
+    info = stream_info(buf)
+    if out is None:
+        out = np.empty(info.num, dtype=dtype)
+    if out.dtype != dtype or not out.flags.c_contiguous or out.size < info.num:
+        raise ValueError("output array must be contiguous, of the stream's dtype and size")
+    s = FazConfigStruct()
+    s.num = out.size
+    ptr, tm = ctypes.c_void_p(out.ctypes.data), FazTimings()
+    _check(library().faz_decompress(ctypes.byref(s), _dtype_code(dtype), buf, len(buf), ctypes.byref(ptr),
                                     ctypes.byref(tm)))
     _tls.timings = tm
     c = Config.from_struct(s)
-    n = c.num * np.dtype(dtype).itemsize
-    arr = np.frombuffer(_take_bytes(out, n), dtype=dtype).copy()
-    return arr.reshape(c.dims), c
+    return out[:c.num].reshape(c.dims), c
 
 
 def decompress_device(stream_bytes, out_tensor, stream=None):
@@ -172,9 +187,12 @@ def decompress_device(stream_bytes, out_tensor, stream=None):
     return c
 
 
-def compress_payload_device(conf, tensor, stream=None):
-    """GPU path without the host zstd stage: (pre-zstd payload bytes, Config
-    the trailer would hold).  For measurement and custom lossless stages."""
+def compress_payload_device(conf, tensor, stream=None, out=None):
+    """GPU path without the host zstd stage, for measurement and custom
+    lossless stages.  Writes the pre-zstd payload into `out` (a host uint8
+    buffer: numpy array or pinned torch tensor; a pinned buffer of the
+    input's size is allocated when None).  Returns (memoryview of the payload,
+    Config the trailer would hold)."""
     import torch
     t = tensor.contiguous()
     dt = {torch.float32: FAZ_FLOAT, torch.float64: FAZ_DOUBLE}.get(t.dtype)
@@ -183,25 +201,45 @@ def compress_payload_device(conf, tensor, stream=None):
     st = (stream or torch.cuda.current_stream(t.device)).cuda_stream
     s = conf.to_struct()
     co = FazConfigStruct()
-    out, osz, tm = ctypes.c_void_p(), ctypes.c_size_t(), FazTimings()
-    with torch.cuda.device(t.device):
-        _check(library().faz_compress_device_payload(ctypes.byref(s), dt, ctypes.c_void_p(t.data_ptr()),
-                                                     ctypes.c_void_p(st), ctypes.byref(out), ctypes.byref(osz),
-                                                     ctypes.byref(co), ctypes.byref(tm)))
+    osz, tm = ctypes.c_size_t(), FazTimings()
+    for _ in range(2):
+        if out is None:
+            out = torch.empty(t.numel() * t.element_size() + (1 << 20), dtype=torch.uint8, pin_memory=True)
+        if isinstance(out, torch.Tensor):
+            ptr, cap = out.data_ptr(), out.numel()
+            view = out.numpy()
+        else:
+            ptr, cap = out.ctypes.data, out.nbytes
+            view = out
+        with torch.cuda.device(t.device):
+            rc = library().faz_compress_device_payload(ctypes.byref(s), dt, ctypes.c_void_p(t.data_ptr()),
+                                                       ctypes.c_void_p(st), ctypes.c_void_p(ptr), cap,
+                                                       ctypes.byref(osz), ctypes.byref(co), ctypes.byref(tm))
+        if rc == -1 and osz.value > cap:
+            out = torch.empty(osz.value, dtype=torch.uint8, pin_memory=True)
+            continue
+        _check(rc)
+        break
     _tls.timings = tm
-    return _take_bytes(out, osz.value), Config.from_struct(co)
+    return memoryview(view)[:osz.value], Config.from_struct(co)
 
 
 def decompress_payload_device(N, payload, out_tensor, stream=None):
-    """Decode a pre-zstd payload into a preallocated contiguous CUDA tensor."""
+    """Decode a pre-zstd payload (bytes-like, ideally a view of pinned memory)
+    into a preallocated contiguous CUDA tensor."""
     import torch
     dt = {torch.float32: FAZ_FLOAT, torch.float64: FAZ_DOUBLE}.get(out_tensor.dtype)
     if dt is None or not out_tensor.is_contiguous():
         raise TypeError("output must be a contiguous float32/float64 CUDA tensor")
     st = (stream or torch.cuda.current_stream(out_tensor.device)).cuda_stream
     tm = FazTimings()
+    if isinstance(payload, memoryview):
+        arr = np.frombuffer(payload, dtype=np.uint8)
+        pptr = ctypes.c_void_p(arr.ctypes.data)
+    else:
+        pptr = bytes(payload)
     with torch.cuda.device(out_tensor.device):
-        _check(library().faz_decompress_payload_device(int(N), dt, payload, len(payload),
+        _check(library().faz_decompress_payload_device(int(N), dt, pptr, len(payload),
                                                        ctypes.c_void_p(out_tensor.data_ptr()), out_tensor.numel(),
                                                        ctypes.c_void_p(st), ctypes.byref(tm)))
     _tls.timings = tm

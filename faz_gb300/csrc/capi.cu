@@ -198,6 +198,30 @@ double level_eb(double eb, double alpha, double beta, int level) {
     return eb * cr;
 }
 
+// Float-pair split of eb and 1/eb for the exact float quantiser (interp.cu).
+// Enabled for float data with eb within [2^-60, 2^60]; FAZ_FASTPATH=0 turns it off.
+template <typename T>
+void set_fast_path(LevelArgs &a) {
+    a.fast = 0;
+    if (sizeof(T) != 4) return;
+    const char *env = std::getenv("FAZ_FASTPATH");
+    if (env && env[0] == '0') return;
+    if (!(a.eb >= 0x1p-60 && a.eb <= 0x1p60)) return;
+    a.eh = (float)a.eb;
+    a.el = (float)(a.eb - (double)a.eh);
+    a.rh = (float)a.recip;
+    a.rl = (float)(a.recip - (double)a.rh);
+    float lo = (float)a.eb;
+    if ((double)lo > a.eb) lo = std::nextafter(lo, 0.0f);
+    a.eblo = lo;
+    a.fast = 1;
+}
+
+bool verify_fast_path() {
+    const char *env = std::getenv("FAZ_VERIFY_FASTPATH");
+    return env && env[0] == '1';
+}
+
 template <typename T>
 Plan make_plan(int N, const uint64_t *dims, uint64_t maxStep, int blocksize, int fixbs, int interp, int dir,
                const std::vector<uint8_t> &ilist, const std::vector<uint8_t> &dlist, double eb, double alpha,
@@ -265,6 +289,7 @@ Plan make_plan(int N, const uint64_t *dims, uint64_t maxStep, int blocksize, int
         a.trim = trim;
         a.eb = level_eb(eb, alpha, beta, level);
         a.recip = 1.0 / a.eb;
+        set_fast_path<T>(a);
         a.write_back = level > 1;
         int64_t nmax[3];
         L.nblocks = 1;
@@ -390,9 +415,17 @@ void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
 constexpr uint64_t kHistChunk = 1 << 18;
 
 // GPU part of compression: returns the pre-zstd payload in a pinned buffer.
+// Where the payload goes: a caller buffer of `cap` bytes, or (dst == nullptr)
+// the thread's pinned staging buffer.
+struct Sink {
+    uint8_t *dst = nullptr;
+    size_t cap = 0;
+    bool too_small = false;
+};
+
 template <typename T>
 void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&payload, size_t &psize,
-                      faz_timings &tm, Counter &launches) {
+                      faz_timings &tm, Counter &launches, Sink *sink = nullptr) {
     auto th0 = clk::now();
     resolve_eb<T>(c, dX, st, launches);
     const double eb = c.absErrorBound;
@@ -418,6 +451,11 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
         for (int i = 0; i < p.N; i++) step[e + i] = (int64_t)p.maxStep;
         launches(launch_anchors<T>(false, dX, W, codes, scratch, nullptr, p.na, step, p.offs3, st));
     }
+    unsigned long long *vcount = nullptr;
+    if (verify_fast_path()) {
+        vcount = m.alloc<unsigned long long>(1);
+        CK(cudaMemsetAsync(vcount, 0, 8, st));
+    }
     Events ev_pred, ev_fin, ev_huff;
     CK(cudaEventRecord(ev_pred.a, st));
     for (size_t li = 0; li < p.lv.size(); li++) {
@@ -426,6 +464,7 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
         a.block_off = boff + L.off_index;
         a.ncodes = n;
         a.err = nullptr;
+        a.verify = vcount;
         if (li + 1 == p.lv.size()) CK(cudaEventRecord(ev_fin.a, st));
         launches(launch_level<T>(a, L.nblocks, false, dX, W, codes, scratch, nullptr, 0, nullptr, st));
     }
@@ -453,6 +492,11 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     const unsigned long long *hf = (const unsigned long long *)(hb + nsym * 8);
     uint64_t nunpred;
     std::memcpy(&nunpred, hb + nsym * 16, 8);
+    if (vcount) {
+        unsigned long long vc = 0;
+        CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
+        if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
+    }
     std::vector<int> syms;
     std::vector<uint64_t> cnts, firsts;
     for (int s = 0; s < nsym; s++)
@@ -519,7 +563,15 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     tree.insert(tree.end(), cb.tree.begin(), cb.tree.end());
     put<uint64_t>(tree, nbytes);
     psize = head.size() + nunpred * sizeof(T) + tree.size() + nbytes;
-    payload = t_pin_payload.get(psize + 8);
+    if (sink && sink->dst) {
+        if (psize > sink->cap) {
+            sink->too_small = true;
+            throw Fail{FAZ_ERR_ARG, "payload buffer too small: need " + std::to_string(psize) + " bytes"};
+        }
+        payload = sink->dst;
+    } else {
+        payload = t_pin_payload.get(psize + 8);
+    }
     std::memcpy(payload, head.data(), head.size());
     size_t o = head.size();
     tm.host_ms += ms_since(th2);
@@ -570,11 +622,14 @@ void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, ch
 }
 
 template <typename T>
-int compress_payload_impl(const faz_config *conf_in, const void *d_data, void *user_stream, char **out,
+int compress_payload_impl(const faz_config *conf_in, const void *d_data, void *user_stream, char *out, size_t cap,
                           size_t *out_size, faz_config *conf_out, faz_timings *tmo) {
     faz_timings tm;
     std::memset(&tm, 0, sizeof(tm));
     auto t0 = clk::now();
+    Sink sink;
+    sink.dst = (uint8_t *)out;
+    sink.cap = cap;
     try {
         if (!conf_in || !d_data || !out || !out_size) throw Fail{FAZ_ERR_ARG, "null argument"};
         faz_config c = *conf_in;
@@ -586,14 +641,15 @@ int compress_payload_impl(const faz_config *conf_in, const void *d_data, void *u
         uint8_t *payload;
         size_t psize;
         CK(cudaEventRecord(ev_gpu.a, sg.st));
-        compress_payload<T>(c, (const T *)d_data, sg.st, payload, psize, tm, launches);
+        try {
+            compress_payload<T>(c, (const T *)d_data, sg.st, payload, psize, tm, launches, &sink);
+        } catch (const Fail &f) {
+            if (sink.too_small) *out_size = psize;
+            throw;
+        }
         CK(cudaEventRecord(ev_gpu.b, sg.st));
         CK(cudaStreamSynchronize(sg.st));
         tm.gpu_ms = ev_gpu.ms();
-        char *buf = (char *)std::malloc(psize ? psize : 1);
-        if (!buf) throw Fail{FAZ_ERR_ARG, "out of host memory"};
-        std::memcpy(buf, payload, psize);
-        *out = buf;
         *out_size = psize;
         if (conf_out) *conf_out = c;
         tm.kernel_launches = launches.n;
@@ -822,6 +878,11 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
     CK(cudaMemcpyAsync(boff, pl_.block_off.data(), pl_.block_off.size() * 8, cudaMemcpyHostToDevice, st));
     int *kerr = m.alloc<int>(1);
     CK(cudaMemsetAsync(kerr, 0, 4, st));
+    unsigned long long *vcount = nullptr;
+    if (verify_fast_path()) {
+        vcount = m.alloc<unsigned long long>(1);
+        CK(cudaMemsetAsync(vcount, 0, 8, st));
+    }
     CK(cudaEventRecord(ev_pred.a, st));
     for (size_t li = 0; li < pl_.lv.size(); li++) {
         const LevelPlan &L = pl_.lv[li];
@@ -829,6 +890,7 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
         a.block_off = boff + L.off_index;
         a.ncodes = num;
         a.err = kerr;
+        a.verify = vcount;
         if (li + 1 == pl_.lv.size()) CK(cudaEventRecord(ev_fin.a, st));
         launches(launch_level<T>(a, L.nblocks, true, nullptr, dOut, codes, nullptr, zpos, nz, dunpred, st));
     }
@@ -838,6 +900,11 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
     CK(cudaMemcpyAsync(hk, kerr, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (*hk) throw Fail{FAZ_ERR_DEVICE, "level kernel met an out-of-range stream position"};
+    if (vcount) {
+        unsigned long long vc = 0;
+        CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
+        if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
+    }
     tm.huffman_ms = ev_dec.ms();
     tm.predict_ms = ev_pred.ms();
     tm.finest_level_ms = pl_.lv.empty() ? 0.0 : ev_fin.ms();
@@ -1043,12 +1110,12 @@ int faz_decompress_device(faz_config *conf, int dtype, const char *cmp, size_t c
     return FAZ_ERR_ARG;
 }
 
-int faz_compress_device_payload(const faz_config *conf, int dtype, const void *d_data, void *stream, char **out,
-                                size_t *out_size, faz_config *conf_out, faz_timings *timings) {
+int faz_compress_device_payload(const faz_config *conf, int dtype, const void *d_data, void *stream, char *out,
+                                size_t capacity, size_t *out_size, faz_config *conf_out, faz_timings *timings) {
     if (dtype == FAZ_FLOAT)
-        return faz::compress_payload_impl<float>(conf, d_data, stream, out, out_size, conf_out, timings);
+        return faz::compress_payload_impl<float>(conf, d_data, stream, out, capacity, out_size, conf_out, timings);
     if (dtype == FAZ_DOUBLE)
-        return faz::compress_payload_impl<double>(conf, d_data, stream, out, out_size, conf_out, timings);
+        return faz::compress_payload_impl<double>(conf, d_data, stream, out, capacity, out_size, conf_out, timings);
     faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
     return FAZ_ERR_ARG;
 }
@@ -1061,6 +1128,22 @@ int faz_decompress_payload_device(int N, int dtype, const char *payload, size_t 
         return faz::decompress_payload_impl<double>(N, payload, size, d_out, capacity, stream, timings);
     faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
     return FAZ_ERR_ARG;
+}
+
+int faz_stream_info(const char *cmp, size_t cmp_size, faz_config *conf) {
+    if (!cmp || !conf || cmp_size < 4) {
+        faz::set_error("faz_stream_info: stream too short");
+        return FAZ_ERR_FORMAT;
+    }
+    int32_t cs;
+    std::memcpy(&cs, cmp + cmp_size - 4, 4);
+    if (cs <= 0 || (size_t)cs + 4 > cmp_size) {
+        faz::set_error("faz_stream_info: bad trailer size");
+        return FAZ_ERR_FORMAT;
+    }
+    int rc = faz::config_load(*conf, (const uint8_t *)cmp + cmp_size - 4 - cs, (size_t)cs);
+    if (rc) faz::set_error("faz_stream_info: bad trailer");
+    return rc;
 }
 
 size_t faz_config_size(void) { return sizeof(faz_config); }

@@ -1,0 +1,102 @@
+// fastq.cuh - exact float emulation of the reference quantiser's double steps.
+//
+// For float data the reference rounds through double
+// (include/QoZ/quantizer/IntegerQuantizer.hpp:80-97):
+//   x = (double)|data - pred| * (1.0 / eb);  qi = (int)x + 1;  half = qi >> 1
+//   dec = (float)((double)pred + (double)q2 * eb),  q2 = +-2*half
+// GB300 runs double arithmetic at a small fraction of its float rate.  The
+// functions below compute the same integers and floats from float-float
+// products (eb and 1/eb split into float pairs, exact products via fmaf) and
+// report "undecided" whenever the float computation cannot prove the result:
+//   - floor(x) only matters where it changes (floor(x) + 1) >> 1, i.e. near odd
+//     integers; within 2^-20 of one the double path decides;
+//   - the final rounding to float only matters where the exact value lies near
+//     a midpoint between two floats; within 2^-12 ulp of one, on cancellation
+//     (|result| < |terms| / 256), at powers of two, zero, tiny or huge values
+//     the double path decides.
+// Both functions are __host__ __device__ so that tests can check them on the
+// CPU against the double computation.
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace faz {
+
+FAZ_HD uint32_t f32_bits(float x) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(x);
+#else
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    return u;
+#endif
+}
+FAZ_HD float f32_from_bits(uint32_t u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float x;
+    std::memcpy(&x, &u, 4);
+    return x;
+#endif
+}
+
+// floor((floor(x) + 1) / 2) for x = RN_double(d * recip), recip = rh + rl.
+// Returns -1 when undecided, -2 when floor(x) + 1 >= twor (unpredictable).
+FAZ_HD int half_index_f32(float d, float rh, float rl, float twor_f, int twor) {
+    float ph = d * rh;
+    if (!(ph < twor_f)) return ph != ph ? -1 : -2;
+    float pl = fmaf(d, rh, -ph);
+    float c = fmaf(d, rl, pl);
+    float k = floorf(ph);
+    float f = (ph - k) + c;
+    float fi = floorf(f);
+    float fr = f - fi;
+    int fl;
+    if (fr > 0x1p-20f && fr < 1.0f - 0x1p-20f) {
+        fl = (int)k + (int)fi;
+    } else {
+        int B = (int)k + (int)rintf(f);
+        if (B & 1) return -1;  // floor is B-1 or B, with different halves
+        fl = B;                // floor is B-1 or B, same half B/2
+    }
+    int qi = fl + 1;
+    if (qi >= twor) return -2;
+    return qi >> 1;
+}
+
+// RN_float(RN_double(pred + RN_double(q2 * eb))), eb = eh + el (+ a residual
+// below 2^-48 eb).  Returns false when undecided.
+FAZ_HD bool dequant_f32(float pred, int q2, float eh, float el, float &out) {
+    if (q2 == 0) {
+        out = pred + 0.0f;
+        return true;
+    }
+    float q = (float)q2;
+    float p1 = q * eh;
+    float e1 = fmaf(q, eh, -p1);
+    float p2 = q * el;
+    float s = pred + p1;
+    float bb = s - pred;
+    float t = (pred - (s - bb)) + (p1 - bb);
+    float lo = t + (e1 + p2);
+    float r = s + lo;
+    float res = (s - r) + lo;
+    float ar = fabsf(r);
+    uint32_t ri = f32_bits(ar);
+    float big = fmaxf(fabsf(pred), fabsf(p1));
+    // Error budget in units of u = ulp(r), with cancellation C = big/|r| <= 2^8:
+    // double roundings of the reference <= 2^-29 C, float-pair product and
+    // the sum of the low parts <= 2^-24 C each, res itself <= 2^-25; total
+    // < 2^-14.5, against a 2^-12 margin.
+    if (!(ar >= 0x1p-100f) || ar * 256.0f < big || (ri & 0x7fffffu) == 0 || ri >= 0x7f000000u) return false;
+    float u = f32_from_bits(ri & 0x7f800000u) * 0x1p-23f;
+    if (fabsf(fabsf(res) - 0.5f * u) < u * 0x1p-12f) return false;
+    out = r;
+    return true;
+}
+
+}  // namespace faz

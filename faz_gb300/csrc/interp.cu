@@ -16,6 +16,7 @@
 #include <cstdint>
 #include <cfloat>
 #include "common.cuh"
+#include "fastq.cuh"
 #include "internal.h"
 
 namespace faz {
@@ -89,6 +90,68 @@ __device__ __forceinline__ int quantize(T &v, T pred, double eb, double recip, i
     return code;
 }
 
+// ----------------------------------------------------- exact float path
+// For float data the reference rounds through double: x = (double)|diff| *
+// (1/eb) truncated to int, and dec = (float)((double)pred + (double)q2 * eb).
+// GB300 runs double arithmetic at a small fraction of its float rate, so the
+// float path below computes both results from float-float products (eb and
+// 1/eb held as float pairs, Dekker products via fmaf) and proves each result
+// equal to the double computation: floor(x) only matters where it changes
+// (floor(x)+1)>>1, i.e. near odd integers, and the final float rounding only
+// where the exact value lies near a midpoint between floats.  Within 2^-20
+// (floor) or 2^-18 ulp (rounding) of such a boundary, on cancellation, at
+// powers of two, zero or non-finite values, the double computation is used.
+
+// Float specialisation of the quantiser: fast path with the double path as
+// the fallback (and, in verify mode, as the check).
+__device__ __forceinline__ int quantize_fast(float &v, float pred, const LevelArgs &a, float &uval) {
+    float orig = v;
+    if (a.trim > 0 && !(fabsf(orig) > a.eblo)) {
+        v = 0;
+        uval = 0;
+        return a.trim - 1;
+    }
+    float diff = orig - pred;
+    int twor = 2 * a.radius;
+    int half = half_index_f32(fabsf(diff), a.rh, a.rl, (float)twor, twor);
+    if (half == -1) return quantize<float>(v, pred, a.eb, a.recip, a.radius, a.trim, uval);
+    uval = orig;
+    if (half == -2) return 0;
+    int q2 = half << 1;
+    int code;
+    if (diff < 0) {
+        q2 = -q2;
+        code = a.radius - half;
+    } else {
+        code = a.radius + half;
+    }
+    float dec;
+    if (!dequant_f32(pred, q2, a.eh, a.el, dec)) dec = (float)((double)pred + (double)q2 * a.eb);
+    float err = dec - orig;
+    if (fabsf(err) > a.eblo || (a.trim == 2 && code == 1)) return 0;
+    v = dec;
+    return code;
+}
+
+template <typename T>
+__device__ __forceinline__ int quantize_any(T &v, T pred, const LevelArgs &a, T &uval) {
+    if constexpr (sizeof(T) == 4) {
+        if (a.fast) {
+            if (a.verify) {
+                float v2 = v, u2;
+                int c2 = quantize<float>(v2, pred, a.eb, a.recip, a.radius, a.trim, u2);
+                int c = quantize_fast(v, pred, a, uval);
+                if (c != c2 || __float_as_uint(v) != __float_as_uint(v2) ||
+                    (c == 0 && __float_as_uint(uval) != __float_as_uint(u2)))
+                    atomicAdd(a.verify, 1ull);
+                return c;
+            }
+            return quantize_fast(v, pred, a, uval);
+        }
+    }
+    return quantize<T>(v, pred, a.eb, a.recip, a.radius, a.trim, uval);
+}
+
 // LinearQuantizer::recover (IntegerQuantizer.hpp:160-179); code 0 reads the
 // unpredictable value of stream position pos.
 template <typename T>
@@ -102,6 +165,24 @@ __device__ __forceinline__ T recover(T pred, int code, uint64_t pos, double eb, 
         if (zpos[mid] < pos) lo = mid + 1; else hi = mid;
     }
     return lo < nz ? unpred[lo] : (T)0;
+}
+
+template <typename T>
+__device__ __forceinline__ T recover_any(T pred, int code, uint64_t pos, const LevelArgs &a, const uint64_t *zpos,
+                                         uint64_t nz, const T *unpred) {
+    if constexpr (sizeof(T) == 4) {
+        if (a.fast && code != 0 && !(a.trim == 2 && code == 1)) {
+            float out;
+            if (dequant_f32(pred, 2 * (code - a.radius), a.eh, a.el, out)) {
+                if (a.verify) {
+                    float ref = recover<float>(pred, code, pos, a.eb, a.radius, a.trim, zpos, nz, unpred);
+                    if (__float_as_uint(ref) != __float_as_uint(out)) atomicAdd(a.verify, 1ull);
+                }
+                return out;
+            }
+        }
+    }
+    return recover<T>(pred, code, pos, a.eb, a.radius, a.trim, zpos, nz, unpred);
 }
 
 // --------------------------------------------------------- level kernel
@@ -125,8 +206,7 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
     const int64_t gbase = g.beg[0] * a.offs[0] + g.beg[1] * a.offs[1] + g.beg[2] * a.offs[2];
     const uint64_t base = a.block_off[bid];
     const int tid = threadIdx.x, nt = blockDim.x;
-    const double eb = a.eb, recip = a.recip;
-    const int radius = a.radius, trim = a.trim, cubic = a.cubic;
+    const int cubic = a.cubic;
 
     // phase 0: lattice points with even index along P2
     const int nv = n0 * n1 * h2;
@@ -167,7 +247,7 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
             int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)(2 * e2) * G2;
             if (!DECOMP) {
                 T v = V[idx], uv;
-                int code = quantize(v, pred, eb, recip, radius, trim, uv);
+                int code = quantize_any(v, pred, a, uv);
                 V[idx] = v;
                 if (emit) {
                     stg[rank] = (uint16_t)code;
@@ -201,7 +281,7 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
                     }
                     code = codes[pos];
                 }
-                T v = recover(pred, code, pos, eb, radius, trim, zpos, nz, unpred);
+                T v = recover_any(pred, code, pos, a, zpos, nz, unpred);
                 V[idx] = v;
                 if (emit) W[gi] = v;
             }
@@ -238,7 +318,7 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
             int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)(2 * e2) * G2;
             if (!DECOMP) {
                 T v = V[idx], uv;
-                int code = quantize(v, pred, eb, recip, radius, trim, uv);
+                int code = quantize_any(v, pred, a, uv);
                 V[idx] = v;
                 if (emit) {
                     stg[rank] = (uint16_t)code;
@@ -269,7 +349,7 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
                     }
                     code = codes[pos];
                 }
-                T v = recover(pred, code, pos, eb, radius, trim, zpos, nz, unpred);
+                T v = recover_any(pred, code, pos, a, zpos, nz, unpred);
                 V[idx] = v;
                 if (emit) W[gi] = v;
             }
@@ -303,13 +383,13 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
             int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)m2 * G2;
             if (!DECOMP) {
                 T v = X[gi], uv;
-                int code = quantize(v, pred, eb, recip, radius, trim, uv);
+                int code = quantize_any(v, pred, a, uv);
                 stg[rank] = (uint16_t)code;
                 if (code == 0) scratch[sbase + rank] = uv;
                 if (a.write_back) W[gi] = v;
             } else {
                 uint64_t pos = sbase + rank;
-                W[gi] = recover(pred, (int)stg[rank], pos, eb, radius, trim, zpos, nz, unpred);
+                W[gi] = recover_any(pred, (int)stg[rank], pos, a, zpos, nz, unpred);
             }
         }
         __syncthreads();

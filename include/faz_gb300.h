@@ -178,6 +178,10 @@ int faz_compress(const faz_config *conf, int dtype, const void *data,
 int faz_decompress(faz_config *conf, int dtype, const char *cmp, size_t cmp_size,
                    void **out, faz_timings *timings);
 
+/* Read a stream's trailer (Config::load, include/QoZ/utils/Config.hpp:311-388)
+ * into *conf without decoding, e.g. to size the output of faz_decompress. */
+int faz_stream_info(const char *cmp, size_t cmp_size, faz_config *conf);
+
 /* Same as faz_compress with the input already in device memory (d_data) and
  * work issued on `stream` (a cudaStream_t, or NULL for a library stream). */
 int faz_compress_device(const faz_config *conf, int dtype, const void *d_data,
@@ -193,10 +197,14 @@ int faz_decompress_device(faz_config *conf, int dtype, const char *cmp,
 /* The GPU path without the host zstd stage, for callers that run their own
  * lossless stage and for measuring the device work: compress device data to
  * the pre-zstd payload (the bytes the reference hands to ZSTD_compress in
- * SZInterpolationCompressor::compress, SZInterpolationCompressor.hpp:485-517).
- * *conf_out (may be NULL) receives the configuration the trailer would hold. */
+ * SZInterpolationCompressor::compress, SZInterpolationCompressor.hpp:485-517),
+ * written to the caller's host buffer `out` of `capacity` bytes (pinned memory
+ * copies fastest).  *out_size receives the payload size; if it exceeds
+ * `capacity` the call returns FAZ_ERR_ARG with *out_size set and writes
+ * nothing.  *conf_out (may be NULL) receives the configuration the trailer
+ * would hold. */
 int faz_compress_device_payload(const faz_config *conf, int dtype, const void *d_data,
-                                void *stream, char **out, size_t *out_size,
+                                void *stream, char *out, size_t capacity, size_t *out_size,
                                 faz_config *conf_out, faz_timings *timings);
 
 /* Decode a pre-zstd payload of an N-dimensional field into device memory

@@ -144,3 +144,64 @@ def test_large_field_round_trip_properties():
     assert err <= c.absErrorBound
     ref_dec, _ = O.decompress(s1)
     assert np.array_equal(out.cpu().numpy().view(np.uint32), ref_dec.view(np.uint32))
+
+
+@pytest.fixture
+def verify_fast_path(monkeypatch):
+    """Every float quantisation also runs the double path; the library fails
+    the call if any point differs (FAZ_VERIFY_FASTPATH)."""
+    monkeypatch.setenv("FAZ_VERIFY_FASTPATH", "1")
+    yield
+
+
+def _grid_field(dims, step, seed, lo=-50.0, hi=80.0):
+    """Values on a grid of `step`: differences and linear predictions fall
+    on exact multiples of the grid, i.e. on quantiser boundaries."""
+    rng = np.random.default_rng(seed)
+    x = spectral_field(dims, slope=-3.0, seed=seed, lo=lo, hi=hi).astype(np.float64)
+    x = np.round(x / step) * step
+    x[rng.random(dims) < 0.01] = 0.0
+    return x.astype(np.float32)
+
+
+ADVERSARIAL = [
+    ("grid_pow2_eb", (64, 72, 80), 2.0 ** -6, dict(abs_=2.0 ** -6)),
+    ("grid_half_eb", (64, 72, 80), 2.0 ** -7, dict(abs_=2.0 ** -6, interp=F.INTERP_ALGO_LINEAR)),
+    ("grid_decimal_eb", (50, 60, 70), 1e-3, dict(abs_=1e-3)),
+    ("grid_rel", (50, 60, 70), 1e-2, dict(rel=1e-4)),
+    ("zeros_trim2", (40, 50, 60), 1e-3, dict(abs_=0.05, trimToZero=2)),
+]
+
+
+@pytest.mark.parametrize("name,dims,step,kw", ADVERSARIAL)
+def test_fast_path_agrees_with_double_path(name, dims, step, kw, verify_fast_path):
+    x = _grid_field(dims, step, seed=len(name))
+    conf = _conf(dims, **kw)
+    stream = F.SZ_compress(conf, x)  # raises FazError on any disagreement
+    ref, _ = O.compress(conf, x)
+    assert mask_first_size(stream) == mask_first_size(ref)
+    dec, c2 = F.SZ_decompress(None, stream)
+    ref_dec, _ = O.decompress(ref)
+    assert np.array_equal(dec.view(np.uint32), ref_dec.view(np.uint32))
+
+
+def test_fast_path_verified_on_golden_cases(verify_fast_path):
+    for name in INI_CASES:
+        case = golden_case(name)
+        if case["dtype"] != "float32":
+            continue
+        stream = F.SZ_compress(cli_config(case), golden_input(case))
+        assert payload_of(stream) == payload_of(golden_stream(case)), name
+        dec, _ = F.SZ_decompress(None, golden_stream(case))
+        assert hashlib.sha256(dec.tobytes()).hexdigest() == case["dec_sha256"], name
+
+
+def test_double_path_only_matches(monkeypatch):
+    """FAZ_FASTPATH=0 forces the double path; streams are identical."""
+    dims = (60, 70, 80)
+    x = spectral_field(dims, slope=-3.0, seed=3)
+    conf = _conf(dims, rel=1e-3)
+    s_fast = F.SZ_compress(conf, x)
+    monkeypatch.setenv("FAZ_FASTPATH", "0")
+    s_dp = F.SZ_compress(conf, x)
+    assert s_fast == s_dp
