@@ -368,7 +368,7 @@ void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     if (c.errorBoundMode == FAZ_EB_ABS) return;
     double rng = 0;
     if (c.errorBoundMode != FAZ_EB_L2NORM) {
-        int nb = (int)std::min<uint64_t>(1024, (c.num + 511) / 512);
+        int nb = (int)std::min<uint64_t>(152 * 4, (c.num + 4095) / 4096);
         if (nb < 1) nb = 1;
         DevMem m(st);
         T *pmin = m.alloc<T>(nb), *pmax = m.alloc<T>(nb);
@@ -412,7 +412,6 @@ void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     c.errorBoundMode = FAZ_EB_ABS;
 }
 
-constexpr uint64_t kHistChunk = 1 << 18;
 
 // GPU part of compression: returns the pre-zstd payload in a pinned buffer.
 // Where the payload goes: a caller buffer of `cap` bytes, or (dst == nullptr)
@@ -472,20 +471,21 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     CK(cudaEventRecord(ev_pred.b, st));
     CK(cudaEventRecord(ev_huff.a, st));
     // histogram
-    const uint64_t nchunk = (n + kHistChunk - 1) / kHistChunk;
+    const uint64_t nsub = hist_subchunks(n);
     const int nsym = 65536;
     unsigned long long *hist = m.alloc<unsigned long long>(nsym);
     unsigned long long *first = m.alloc<unsigned long long>(nsym);
-    unsigned long long *zc = m.alloc<unsigned long long>(nchunk + 1);
-    unsigned long long *zoff = m.alloc<unsigned long long>(nchunk + 1);
+    unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1);
+    unsigned long long *zoff = m.alloc<unsigned long long>(nsub + 1);
+    unsigned long long *stmp = m.alloc<unsigned long long>(scan_temp_words(std::max<uint64_t>(nsub, encode_chunks(n))) + 1);
     CK(cudaMemsetAsync(hist, 0, nsym * 8, st));
     CK(cudaMemsetAsync(first, 0xff, nsym * 8, st));
-    launches(launch_histogram(codes, n, kHistChunk, radius, hist, first, zc, st));
-    launches(launch_scan_u64(zc, zoff, nchunk, st));
+    launches(launch_histogram(codes, n, radius, hist, first, zc, st));
+    launches(launch_scan_u64(zc, zoff, nsub, stmp, st));
     uint8_t *hb = t_pin_small.get((size_t)nsym * 16 + 8);
     CK(cudaMemcpyAsync(hb, hist, nsym * 8, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(hb + nsym * 8, first, nsym * 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(hb + nsym * 16, zoff + nchunk, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hb + nsym * 16, zoff + nsub, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     auto th1 = clk::now();
     const unsigned long long *hh = (const unsigned long long *)hb;
@@ -512,7 +512,7 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     tm.host_ms += ms_since(th1);
     // unpredictable values in stream order
     T *unpred = m.alloc<T>(nunpred ? nunpred : 1);
-    if (nunpred) launches(launch_gather_unpred<T>(codes, n, kHistChunk, zc, zoff, scratch, unpred, st));
+    if (nunpred) launches(launch_compact_zeros<T>(codes, n, zc, zoff, nullptr, scratch, unpred, st));
     // Huffman encode
     unsigned long long *dcode = m.alloc<unsigned long long>(cb.stateNum);
     uint8_t *dlen = m.alloc<uint8_t>(cb.stateNum);
@@ -522,7 +522,7 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     unsigned long long *cbits = m.alloc<unsigned long long>(nech + 1);
     unsigned long long *coff = m.alloc<unsigned long long>(nech + 1);
     launches(launch_encode_bits(codes, n, cb.offset, dlen, cbits, st));
-    launches(launch_scan_u64(cbits, coff, nech, st));
+    launches(launch_scan_u64(cbits, coff, nech, stmp, st));
     uint64_t total_bits;
     CK(cudaMemcpyAsync(hb, coff + nech, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -801,9 +801,9 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
         int v = t.constant_state + t.offset;
         launches(launch_fill_u16(codes, num, (uint16_t)v, st));
     } else {
-        const uint64_t words = (P.nbytes + 7) / 8 + 8;
-        uint64_t *dbits = m.alloc<uint64_t>(words);
-        CK(cudaMemsetAsync(dbits, 0, words * 8, st));
+        const uint64_t nwords = (P.nbytes + 3) / 4;
+        uint32_t *dbits = m.alloc<uint32_t>(nwords + 16);
+        CK(cudaMemsetAsync(dbits, 0, (nwords + 16) * 4, st));
         CK(cudaMemcpyAsync(dbits, P.bits, P.nbytes, cudaMemcpyHostToDevice, st));
         uint32_t *lut = m.alloc<uint32_t>(t.lut.size());
         uint32_t *dl = m.alloc<uint32_t>(t.nodeCount), *dr = m.alloc<uint32_t>(t.nodeCount);
@@ -816,56 +816,59 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
         CK(cudaMemcpyAsync(dleaf, t.leaf.data(), t.nodeCount, cudaMemcpyHostToDevice, st));
         DecodeTablesDev td{lut, dl, dr, ds, dleaf};
         const uint64_t nbits = P.nbytes * 8;
-        const uint64_t unit = 2048;
-        const uint64_t nunits = (nbits + unit - 1) / unit;
+        const uint64_t nunits = decode_units(nbits);
         uint64_t *start = m.alloc<uint64_t>(nunits);
         uint64_t *ea = m.alloc<uint64_t>(nunits), *eb2 = m.alloc<uint64_t>(nunits);
         unsigned int *cnt = m.alloc<unsigned int>(nunits);
+        uint16_t *bnd = m.alloc<uint16_t>(nunits * decode_boundaries());
         unsigned long long *cnt64 = m.alloc<unsigned long long>(nunits + 1);
         unsigned long long *off = m.alloc<unsigned long long>(nunits + 1);
-        int *changed = m.alloc<int>(1);
-        CK(cudaMemsetAsync(changed, 0, 4, st));
-        launches(launch_decode_sync(td, dbits, nbits, unit, nunits, nullptr, start, ea, cnt, 0, changed, st));
+        unsigned long long *dtmp = m.alloc<unsigned long long>(scan_temp_words(nunits) + 1);
+        int *flags = m.alloc<int>(2);  // [0] changed, [1] damaged tree
+        CK(cudaMemsetAsync(flags, 0, 8, st));
+        launches(launch_init_starts(start, nunits, st));
+        launches(launch_decode_spec(td, dbits, nwords, nbits, nunits, ea, cnt, bnd, flags + 1, st));
         int *hflag = (int *)t_pin_small.get(64);
         bool converged = false;
-        for (int it = 0; it < 256; it++) {
-            CK(cudaMemsetAsync(changed, 0, 4, st));
-            launches(launch_decode_sync(td, dbits, nbits, unit, nunits, ea, start, eb2, cnt, 1, changed, st));
-            CK(cudaMemcpyAsync(hflag, changed, 4, cudaMemcpyDeviceToHost, st));
+        for (int it = 0; it < 1024; it++) {
+            CK(cudaMemsetAsync(flags, 0, 4, st));
+            launches(launch_decode_resync(td, dbits, nwords, nbits, nunits, ea, eb2, cnt, bnd, start, flags, st));
+            CK(cudaMemcpyAsync(hflag, flags, 8, cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             std::swap(ea, eb2);
-            if (*hflag < 0) throw Fail{FAZ_ERR_FORMAT, "Huffman stream decodes outside the tree"};
-            if (*hflag == 0) {
+            if (hflag[0] < 0 || hflag[1]) throw Fail{FAZ_ERR_FORMAT, "Huffman stream decodes outside the tree"};
+            if (hflag[0] == 0) {
                 converged = true;
                 break;
             }
         }
-        if (!converged) throw Fail{FAZ_ERR_UNSUPPORTED, "Huffman stream did not synchronise within 256 passes"};
+        if (!converged) throw Fail{FAZ_ERR_UNSUPPORTED, "Huffman stream did not synchronise within 1024 passes"};
         launches(launch_widen_counts(cnt, cnt64, nunits, st));
-        launches(launch_scan_u64(cnt64, off, nunits, st));
+        launches(launch_scan_u64(cnt64, off, nunits, dtmp, st));
         uint64_t total;
         CK(cudaMemcpyAsync(hflag, off + nunits, 8, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         std::memcpy(&total, hflag, 8);
         if (total < num) throw Fail{FAZ_ERR_FORMAT, "Huffman stream holds fewer symbols than the field"};
-        launches(launch_decode_write(td, dbits, nbits, unit, nunits, start, off, num, t.offset, codes, st));
+        launches(launch_decode_write(td, dbits, nwords, nbits, nunits, start, off, num, t.offset, codes, st));
     }
     CK(cudaEventRecord(ev_dec.b, st));
     // zero positions for the unpredictable values
-    const uint64_t nchunk = (num + kHistChunk - 1) / kHistChunk;
-    unsigned long long *zc = m.alloc<unsigned long long>(nchunk + 1);
-    unsigned long long *zoff = m.alloc<unsigned long long>(nchunk + 1);
-    launches(launch_count_zeros(codes, num, kHistChunk, zc, st));
-    launches(launch_scan_u64(zc, zoff, nchunk, st));
+    const uint64_t nsub = hist_subchunks(num);
+    unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1);
+    unsigned long long *zoff = m.alloc<unsigned long long>(nsub + 1);
+    unsigned long long *ztmp = m.alloc<unsigned long long>(scan_temp_words(nsub) + 1);
+    launches(launch_count_zeros(codes, num, zc, st));
+    launches(launch_scan_u64(zc, zoff, nsub, ztmp, st));
     uint64_t nz;
     uint64_t *hz = (uint64_t *)t_pin_small.get(64);
-    CK(cudaMemcpyAsync(hz, zoff + nchunk, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hz, zoff + nsub, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     nz = *hz;
     if (nz != P.nunpred)
         throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
     uint64_t *zpos = m.alloc<uint64_t>(nz ? nz : 1);
-    if (nz) launches(launch_zero_positions(codes, num, kHistChunk, zc, zoff, zpos, st));
+    if (nz) launches(launch_compact_zeros<T>(codes, num, zc, zoff, zpos, nullptr, nullptr, st));
     if (!pl_.anchor) {
         launches(launch_first_point<T>(true, nullptr, dOut, codes, nullptr, P.eb, P.radius, P.trim, zpos, nz, dunpred, st));
     } else {

@@ -14,43 +14,48 @@
 namespace faz {
 
 // --------------------------------------------------------------- histogram
+// A CTA takes a chunk of HCHUNK codes; warp w of the CTA takes the contiguous
+// sub-chunk [w*HSUB, (w+1)*HSUB) of it, so that zero codes can later be
+// compacted per warp with one running offset and no block barriers.
 // Counts of every symbol, the stream position of its first occurrence, and
-// the number of zero codes per chunk.  Symbols within +-HWIN/2 of `center`
-// are counted in shared memory.
+// the number of zero codes per warp sub-chunk.  Symbols within +-HWIN/2 of
+// `center` are counted in shared memory.
 static constexpr int HWIN = 4096;
+static constexpr int HWARPS = 32;
+static constexpr uint64_t HSUB = 8192;
+static constexpr uint64_t HCHUNK = HSUB * HWARPS;
 
-__global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__ codes, uint64_t n, uint64_t chunk,
-                                                    int center, unsigned long long *hist,
-                                                    unsigned long long *first, unsigned long long *zcount) {
+__global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__ codes, uint64_t n, int center,
+                                                    unsigned long long *hist, unsigned long long *first,
+                                                    unsigned long long *zcount) {
     __shared__ unsigned int scnt[HWIN];
     __shared__ unsigned int sfirst[HWIN];
-    __shared__ unsigned int szero;
     for (int i = threadIdx.x; i < HWIN; i += blockDim.x) {
         scnt[i] = 0;
         sfirst[i] = 0xffffffffu;
     }
-    if (threadIdx.x == 0) szero = 0;
     __syncthreads();
-    const uint64_t c0 = (uint64_t)blockIdx.x * chunk;
-    uint64_t c1 = c0 + chunk;
-    if (c1 > n) c1 = n;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t c0 = (uint64_t)blockIdx.x * HCHUNK;
+    const uint64_t s0 = c0 + (uint64_t)w * HSUB;
+    uint64_t s1 = s0 + HSUB;
+    if (s1 > n) s1 = n;
     const int lo = center - HWIN / 2;
     unsigned int zc = 0;
-    for (uint64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+    for (uint64_t i = s0 + lane; i < s1; i += 32) {
         int v = codes[i];
-        unsigned int off = (unsigned int)(i - c0);
         if (v == 0) zc++;
         int b = v - lo;
         if (b >= 0 && b < HWIN) {
             atomicAdd(&scnt[b], 1u);
-            atomicMin(&sfirst[b], off);
+            atomicMin(&sfirst[b], (unsigned int)(i - c0));
         } else {
             atomicAdd(&hist[v], 1ull);
             atomicMin(&first[v], (unsigned long long)i);
         }
     }
     for (int o = 16; o > 0; o >>= 1) zc += __shfl_down_sync(0xffffffffu, zc, o);
-    if ((threadIdx.x & 31) == 0 && zc) atomicAdd(&szero, zc);
+    if (lane == 0) zcount[(uint64_t)blockIdx.x * HWARPS + w] = zc;
     __syncthreads();
     for (int b = threadIdx.x; b < HWIN; b += blockDim.x) {
         if (scnt[b]) {
@@ -58,118 +63,130 @@ __global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__
             atomicMin(&first[lo + b], (unsigned long long)(c0 + sfirst[b]));
         }
     }
-    if (threadIdx.x == 0) zcount[blockIdx.x] = szero;
 }
 
-// Gather the unpredictable values (stream order) from the per-position
-// scratch: chunk c's zero codes go to unpred[zoff[c]...].
-template <typename T>
-__global__ void __launch_bounds__(1024) k_gather_unpred(const uint16_t *__restrict__ codes, uint64_t n, uint64_t chunk,
-                                                        const unsigned long long *zcount,
-                                                        const unsigned long long *zoff, const T *scratch, T *unpred) {
-    if (zcount[blockIdx.x] == 0) return;
-    __shared__ unsigned int wsum[32];
-    __shared__ unsigned long long run;
-    const uint64_t c0 = (uint64_t)blockIdx.x * chunk;
-    uint64_t c1 = c0 + chunk;
-    if (c1 > n) c1 = n;
-    if (threadIdx.x == 0) run = zoff[blockIdx.x];
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (uint64_t b = c0; b < c1; b += blockDim.x) {
-        uint64_t i = b + threadIdx.x;
-        bool z = i < c1 && codes[i] == 0;
-        unsigned int bal = __ballot_sync(0xffffffffu, z);
-        unsigned int before = __popc(bal & ((1u << lane) - 1));
-        if (lane == 0) wsum[wid] = __popc(bal);
-        __syncthreads();
-        unsigned long long wbase = run;
-        for (int w = 0; w < wid; w++) wbase += wsum[w];
-        if (z) unpred[wbase + before] = scratch[i];
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long s = 0;
-            for (int w = 0; w < nw; w++) s += wsum[w];
-            run += s;
-        }
-        __syncthreads();
-    }
-}
-
-// Stream positions of the zero codes (for recovery of unpredictable values).
-__global__ void __launch_bounds__(1024) k_zero_positions(const uint16_t *__restrict__ codes, uint64_t n,
-                                                         uint64_t chunk, const unsigned long long *zcount,
-                                                         const unsigned long long *zoff, uint64_t *zpos) {
-    if (zcount[blockIdx.x] == 0) return;
-    __shared__ unsigned int wsum[32];
-    __shared__ unsigned long long run;
-    const uint64_t c0 = (uint64_t)blockIdx.x * chunk;
-    uint64_t c1 = c0 + chunk;
-    if (c1 > n) c1 = n;
-    if (threadIdx.x == 0) run = zoff[blockIdx.x];
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (uint64_t b = c0; b < c1; b += blockDim.x) {
-        uint64_t i = b + threadIdx.x;
-        bool z = i < c1 && codes[i] == 0;
-        unsigned int bal = __ballot_sync(0xffffffffu, z);
-        unsigned int before = __popc(bal & ((1u << lane) - 1));
-        if (lane == 0) wsum[wid] = __popc(bal);
-        __syncthreads();
-        unsigned long long wbase = run;
-        for (int w = 0; w < wid; w++) wbase += wsum[w];
-        if (z) zpos[wbase + before] = i;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long s = 0;
-            for (int w = 0; w < nw; w++) s += wsum[w];
-            run += s;
-        }
-        __syncthreads();
-    }
-}
-
-// Zero-code count per chunk (decompress side).
-__global__ void __launch_bounds__(1024) k_count_zeros(const uint16_t *__restrict__ codes, uint64_t n, uint64_t chunk,
+// Zero-code count per warp sub-chunk (decompress side).
+__global__ void __launch_bounds__(1024) k_count_zeros(const uint16_t *__restrict__ codes, uint64_t n,
                                                       unsigned long long *zcount) {
-    __shared__ unsigned int s;
-    if (threadIdx.x == 0) s = 0;
-    __syncthreads();
-    const uint64_t c0 = (uint64_t)blockIdx.x * chunk;
-    uint64_t c1 = c0 + chunk;
-    if (c1 > n) c1 = n;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t s0 = (uint64_t)blockIdx.x * HCHUNK + (uint64_t)w * HSUB;
+    uint64_t s1 = s0 + HSUB;
+    if (s1 > n) s1 = n;
     unsigned int zc = 0;
-    for (uint64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) zc += codes[i] == 0;
+    for (uint64_t i = s0 + lane; i < s1; i += 32) zc += codes[i] == 0;
     for (int o = 16; o > 0; o >>= 1) zc += __shfl_down_sync(0xffffffffu, zc, o);
-    if ((threadIdx.x & 31) == 0 && zc) atomicAdd(&s, zc);
-    __syncthreads();
-    if (threadIdx.x == 0) zcount[blockIdx.x] = s;
+    if (lane == 0) zcount[(uint64_t)blockIdx.x * HWARPS + w] = zc;
 }
 
-// Exclusive scan of n 64-bit values in one CTA; total written to out[n].
-__global__ void __launch_bounds__(1024) k_scan_u64(const unsigned long long *in, unsigned long long *out, uint64_t n) {
-    __shared__ unsigned long long part[1024];
-    const uint64_t per = (n + blockDim.x - 1) / blockDim.x;
-    const uint64_t a = threadIdx.x * per;
-    uint64_t b = a + per;
-    if (b > n) b = n;
-    unsigned long long s = 0;
-    for (uint64_t i = a; i < b; i++) s += in[i];
-    part[threadIdx.x] = s;
+// Compaction of the zero codes of each warp sub-chunk, in stream order,
+// starting at zoff[sub-chunk]: positions (zpos) and/or the values recorded at
+// those positions (vals from scratch).
+template <typename T>
+__global__ void __launch_bounds__(1024) k_compact_zeros(const uint16_t *__restrict__ codes, uint64_t n,
+                                                        const unsigned long long *zcount,
+                                                        const unsigned long long *zoff, uint64_t *zpos,
+                                                        const T *scratch, T *vals) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t sub = (uint64_t)blockIdx.x * HWARPS + w;
+    if (zcount[sub] == 0) return;
+    const uint64_t s0 = sub * HSUB;
+    uint64_t s1 = s0 + HSUB;
+    if (s1 > n) s1 = n;
+    unsigned long long run = zoff[sub];
+    for (uint64_t b = s0; b < s1; b += 32) {
+        uint64_t i = b + lane;
+        bool z = i < s1 && codes[i] == 0;
+        unsigned int bal = __ballot_sync(0xffffffffu, z);
+        if (z) {
+            unsigned long long o = run + __popc(bal & ((1u << lane) - 1));
+            if (zpos) zpos[o] = i;
+            if (vals) vals[o] = scratch[i];
+        }
+        run += __popc(bal);
+    }
+}
+
+// ------------------------------------------------------------------- scan
+// Exclusive scan of n 64-bit values (out[n] = total): per-block totals,
+// one-block scan of the totals, per-block scan with the block's offset.
+static constexpr int SCAN_T = 512;
+static constexpr int SCAN_E = 8;
+static constexpr int SCAN_B = SCAN_T * SCAN_E;
+
+__device__ __forceinline__ unsigned long long block_excl_scan(unsigned long long v, unsigned long long *sh,
+                                                              unsigned long long &total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned long long x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[w] = x;
     __syncthreads();
-    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-        unsigned long long v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+    if (w == 0) {
+        unsigned long long y = lane < nw ? sh[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long z = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) y += z;
+        }
+        sh[lane] = y;
     }
-    unsigned long long run = threadIdx.x ? part[threadIdx.x - 1] : 0;
-    for (uint64_t i = a; i < b; i++) {
-        unsigned long long v = in[i];
-        out[i] = run;
-        run += v;
+    __syncthreads();
+    total = sh[nw - 1];
+    unsigned long long wbase = w ? sh[w - 1] : 0;
+    __syncthreads();
+    return wbase + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_reduce(const unsigned long long *in, uint64_t n,
+                                                       unsigned long long *bsum) {
+    __shared__ unsigned long long sh[32];
+    uint64_t b0 = (uint64_t)blockIdx.x * SCAN_B;
+    unsigned long long s = 0;
+    for (int k = 0; k < SCAN_E; k++) {
+        uint64_t i = b0 + (uint64_t)threadIdx.x * SCAN_E + k;
+        if (i < n) s += in[i];
     }
-    if (threadIdx.x == blockDim.x - 1) out[n] = part[threadIdx.x];
+    unsigned long long tot;
+    block_excl_scan(s, sh, tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+// one block: exclusive scan of nb block totals in place (nb <= any), total in bsum[nb]
+__global__ void __launch_bounds__(1024) k_scan_top(unsigned long long *bsum, uint64_t nb) {
+    __shared__ unsigned long long sh[32];
+    unsigned long long carry = 0;
+    for (uint64_t c = 0; c < nb; c += blockDim.x) {
+        uint64_t i = c + threadIdx.x;
+        unsigned long long v = i < nb ? bsum[i] : 0;
+        unsigned long long tot;
+        unsigned long long e = block_excl_scan(v, sh, tot);
+        if (i < nb) bsum[i] = carry + e;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) bsum[nb] = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_down(const unsigned long long *in, uint64_t n,
+                                                     const unsigned long long *bsum, unsigned long long *out,
+                                                     uint64_t nb) {
+    __shared__ unsigned long long sh[32];
+    uint64_t b0 = (uint64_t)blockIdx.x * SCAN_B;
+    unsigned long long v[SCAN_E];
+    unsigned long long s = 0;
+    for (int k = 0; k < SCAN_E; k++) {
+        uint64_t i = b0 + (uint64_t)threadIdx.x * SCAN_E + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    unsigned long long tot;
+    unsigned long long e = block_excl_scan(s, sh, tot) + bsum[blockIdx.x];
+    for (int k = 0; k < SCAN_E; k++) {
+        uint64_t i = b0 + (uint64_t)threadIdx.x * SCAN_E + k;
+        if (i < n) out[i] = e;
+        e += v[k];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = bsum[nb];
 }
 
 // ------------------------------------------------------------------ encode
@@ -265,6 +282,10 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
 }
 
 // ------------------------------------------------------------------ decode
+// A CTA decodes DEC_T consecutive units of DEC_UNIT bits from a copy of its
+// segment of the bit string (plus a halo) in shared memory, with the
+// 2^LUT_BITS-entry table beside it.  DEC_UNIT is an odd number of 32-bit
+// words so that the units of a warp start in different banks.
 struct DecTables {
     const uint32_t *lut;     // 2^LUT_BITS entries: (len << 24) | state, or DEC_NODE | node
     const uint32_t *left, *right;
@@ -273,28 +294,25 @@ struct DecTables {
 };
 static constexpr int LUT_BITS = 12;
 static constexpr uint32_t DEC_NODE = 0x80000000u;
+static constexpr int DEC_T = 256;
+static constexpr int DEC_WORDS = 33;                 // words per unit
+static constexpr uint64_t DEC_UNIT = DEC_WORDS * 32; // bits per unit
+static constexpr int DEC_HALO = 8;                   // words past the last unit
+static constexpr int DEC_SEG = DEC_T * DEC_WORDS + DEC_HALO;
+static constexpr int DEC_NB = 16;                    // boundaries recorded per unit
 
-__device__ __forceinline__ uint64_t bswap64(uint64_t x) {
-    uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
-    return ((uint64_t)bswap32(lo) << 32) | bswap32(hi);
+// bits [p, p+64) of the segment (word-grid relative), MSB first
+__device__ __forceinline__ uint64_t seg_peek(const uint32_t *sw, uint32_t p) {
+    uint32_t w = p >> 5, b = p & 31;
+    uint64_t hi = ((uint64_t)sw[w] << 32) | sw[w + 1];
+    if (!b) return hi;
+    return (hi << b) | (sw[w + 2] >> (32 - b));
 }
 
-// 64 bits of the stream starting at bit p (the buffer is padded by 16 bytes).
-__device__ __forceinline__ uint64_t peek64(const uint64_t *__restrict__ w, uint64_t p) {
-    uint64_t i = p >> 6;
-    int sh = (int)(p & 63);
-    uint64_t a = bswap64(w[i]);
-    if (!sh) return a;
-    uint64_t b = bswap64(w[i + 1]);
-    return (a << sh) | (b >> (64 - sh));
-}
-
-// Decode one symbol at bit p; returns its state and advances p.  Codes are
-// at most 64 bits long; a walk that finds no leaf within 64 bits (a damaged
-// tree) returns -1 and moves p past `stop`.
-__device__ __forceinline__ int dec_one(const DecTables &t, const uint32_t *slut, const uint64_t *w, uint64_t &p,
-                                       uint64_t stop) {
-    uint64_t win = peek64(w, p);
+// one symbol at segment bit p: returns its state (or -1 on a damaged tree)
+// and advances p.  Codes are at most 64 bits long.
+__device__ __forceinline__ int dec_sym(const DecTables &t, const uint32_t *slut, const uint32_t *sw, uint32_t &p) {
+    uint64_t win = seg_peek(sw, p);
     uint32_t e = slut[win >> (64 - LUT_BITS)];
     if (!(e & DEC_NODE)) {
         p += e >> 24;
@@ -309,63 +327,137 @@ __device__ __forceinline__ int dec_one(const DecTables &t, const uint32_t *slut,
             return t.sym[node];
         }
     }
-    p = stop + 64;
     return -1;
 }
 
-// Pass over units: decode from start[u] (unit 0 from bit 0) until the bit
-// position reaches the end of the unit; record the end position and count.
-// With `refine`, only units whose recorded start differs from the previous
-// unit's end are decoded again; `changed` is set when any end moves.
-__global__ void __launch_bounds__(256) k_decode_sync(DecTables t, const uint64_t *__restrict__ w, uint64_t nbits,
-                                                    uint64_t unit, uint64_t nunits, const uint64_t *end_in,
-                                                    uint64_t *start, uint64_t *end_out, unsigned int *cnt,
-                                                    int refine, int *changed) {
-    __shared__ uint32_t slut[1 << LUT_BITS];
+__device__ __forceinline__ uint32_t bswap_w(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
+
+// Stage the CTA's segment (as big-endian words) and the lookup table.
+__device__ __forceinline__ void dec_stage(const DecTables &t, const uint32_t *__restrict__ w32, uint64_t nwords,
+                                          uint32_t *slut, uint32_t *sw, uint64_t wbase) {
     for (int i = threadIdx.x; i < (1 << LUT_BITS); i += blockDim.x) slut[i] = t.lut[i];
-    __syncthreads();
-    uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (u >= nunits) return;
-    uint64_t lim = (u + 1) * unit;
-    if (lim > nbits) lim = nbits;
-    uint64_t s;
-    if (!refine) {
-        s = u * unit;
-    } else {
-        s = u == 0 ? 0 : end_in[u - 1];
-        if (s == start[u]) {
-            end_out[u] = end_in[u];
-            return;
-        }
+    for (int i = threadIdx.x; i < DEC_SEG; i += blockDim.x) {
+        uint64_t gi = wbase + i;
+        sw[i] = gi < nwords ? bswap_w(w32[gi]) : 0u;
     }
-    uint64_t p = s;
+    __syncthreads();
+}
+
+// Speculative pass: unit u decodes from its nominal start u*DEC_UNIT to the
+// first codeword end at or past the unit's end; records the end, the symbol
+// count, and the first DEC_NB codeword boundaries (offsets from the start).
+__global__ void __launch_bounds__(DEC_T) k_decode_spec(DecTables t, const uint32_t *__restrict__ w32, uint64_t nwords,
+                                                      uint64_t nbits, uint64_t nunits, uint64_t *end,
+                                                      unsigned int *cnt, uint16_t *bnd, int *err) {
+    __shared__ uint32_t slut[1 << LUT_BITS];
+    __shared__ uint32_t sw[DEC_SEG];
+    const uint64_t u0 = (uint64_t)blockIdx.x * DEC_T;
+    dec_stage(t, w32, nwords, slut, sw, u0 * DEC_WORDS);
+    const uint64_t u = u0 + threadIdx.x;
+    if (u >= nunits) return;
+    const uint64_t g0 = u0 * DEC_UNIT;
+    uint64_t lim = (u + 1) * DEC_UNIT;
+    if (lim > nbits) lim = nbits;
+    const uint32_t start = (uint32_t)(u * DEC_UNIT - g0);
+    const uint32_t stop = (uint32_t)(lim - g0);
+    uint32_t p = start;
     unsigned int c = 0;
-    while (p < lim) {
-        if (dec_one(t, slut, w, p, lim) < 0) atomicExch(changed, -1);
+    uint16_t *b = bnd + u * DEC_NB;
+    while (p < stop) {
+        if (c < DEC_NB) b[c] = (uint16_t)(p - start);
+        if (dec_sym(t, slut, sw, p) < 0) {
+            atomicExch(err, 1);
+            break;
+        }
         c++;
     }
-    start[u] = s;
-    end_out[u] = p;
+    for (unsigned int k = c; k < DEC_NB; k++) b[k] = 0xffff;
+    end[u] = g0 + p;
     cnt[u] = c;
-    if (refine && p != end_in[u]) atomicCAS(changed, 0, 1);
+}
+
+// Synchronisation pass: unit u restarts at the true end of unit u-1 (given
+// in `start_in`, a copy of the previous pass's ends) and decodes until its
+// position meets a boundary of its speculative decode; from there the two
+// decodes coincide.  Units that do not meet one within the recorded window
+// decode to the end.  Sets *changed when any end moved.
+__global__ void __launch_bounds__(DEC_T) k_decode_resync(DecTables t, const uint32_t *__restrict__ w32,
+                                                        uint64_t nwords, uint64_t nbits, uint64_t nunits,
+                                                        const uint64_t *end_in, uint64_t *end_out,
+                                                        unsigned int *cnt, const uint16_t *bnd, uint64_t *start,
+                                                        int *changed) {
+    __shared__ uint32_t slut[1 << LUT_BITS];
+    __shared__ uint32_t sw[DEC_SEG];
+    const uint64_t u0 = (uint64_t)blockIdx.x * DEC_T;
+    dec_stage(t, w32, nwords, slut, sw, u0 * DEC_WORDS);
+    const uint64_t u = u0 + threadIdx.x;
+    if (u >= nunits) return;
+    const uint64_t g0 = u0 * DEC_UNIT;
+    const uint64_t s_true = u == 0 ? 0 : end_in[u - 1];
+    if (s_true == start[u]) {
+        end_out[u] = end_in[u];
+        return;
+    }
+    uint64_t lim = (u + 1) * DEC_UNIT;
+    if (lim > nbits) lim = nbits;
+    const uint32_t nominal = (uint32_t)(u * DEC_UNIT - g0);
+    const uint32_t stop = (uint32_t)(lim - g0);
+    if (s_true < g0 || s_true - g0 > stop + 64) {
+        atomicExch(changed, -1);
+        return;
+    }
+    uint32_t p = (uint32_t)(s_true - g0);
+    const uint16_t *b = bnd + u * DEC_NB;
+    const bool first_pass = start[u] == u * DEC_UNIT;
+    unsigned int c = 0;
+    bool synced = false;
+    while (p < stop) {
+        if (first_pass) {
+            uint32_t off = p - nominal;
+            if (off < 0xffff) {
+                for (int k = 0; k < DEC_NB; k++) {
+                    if (b[k] == off) {
+                        c += cnt[u] - k;
+                        synced = true;
+                        break;
+                    }
+                    if (b[k] > off) break;
+                }
+            }
+            if (synced) break;
+        }
+        if (dec_sym(t, slut, sw, p) < 0) {
+            atomicExch(changed, -1);
+            return;
+        }
+        c++;
+    }
+    const uint64_t e = synced ? end_in[u] : g0 + p;
+    start[u] = s_true;
+    cnt[u] = c;
+    end_out[u] = e;
+    if (e != end_in[u]) atomicCAS(changed, 0, 1);
 }
 
 // Final pass: decode unit u from its true start into out[off[u]...].
-__global__ void __launch_bounds__(256) k_decode_write(DecTables t, const uint64_t *__restrict__ w, uint64_t nbits,
-                                                     uint64_t unit, uint64_t nunits, const uint64_t *start,
-                                                     const unsigned long long *off, uint64_t nout, int offset,
-                                                     uint16_t *out) {
+__global__ void __launch_bounds__(DEC_T) k_decode_write(DecTables t, const uint32_t *__restrict__ w32, uint64_t nwords,
+                                                       uint64_t nbits, uint64_t nunits, const uint64_t *start,
+                                                       const unsigned long long *off, uint64_t nout, int offset,
+                                                       uint16_t *out) {
     __shared__ uint32_t slut[1 << LUT_BITS];
-    for (int i = threadIdx.x; i < (1 << LUT_BITS); i += blockDim.x) slut[i] = t.lut[i];
-    __syncthreads();
-    uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    __shared__ uint32_t sw[DEC_SEG];
+    const uint64_t u0 = (uint64_t)blockIdx.x * DEC_T;
+    dec_stage(t, w32, nwords, slut, sw, u0 * DEC_WORDS);
+    const uint64_t u = u0 + threadIdx.x;
     if (u >= nunits) return;
-    uint64_t lim = (u + 1) * unit;
+    const uint64_t g0 = u0 * DEC_UNIT;
+    uint64_t lim = (u + 1) * DEC_UNIT;
     if (lim > nbits) lim = nbits;
-    uint64_t p = start[u];
+    uint32_t p = (uint32_t)(start[u] - g0);
+    const uint32_t stop = (uint32_t)(lim - g0);
     uint64_t o = off[u];
-    while (p < lim && o < nout) {
-        int s = dec_one(t, slut, w, p, lim);
+    while (p < stop && o < nout) {
+        int s = dec_sym(t, slut, sw, p);
         if (s < 0) break;
         out[o++] = (uint16_t)(s + offset);
     }
@@ -385,39 +477,42 @@ __global__ void k_widen_counts(const unsigned int *cnt, unsigned long long *out,
 
 static inline unsigned grid_for(uint64_t n, uint64_t per) { return (unsigned)((n + per - 1) / per); }
 
-cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, uint64_t chunk, int center,
-                             unsigned long long *hist, unsigned long long *first, unsigned long long *zcount,
-                             cudaStream_t st) {
-    k_histogram<<<grid_for(n, chunk), 1024, 0, st>>>(codes, n, chunk, center, hist, first, zcount);
+uint64_t hist_subchunks(uint64_t n) { return ((n + HCHUNK - 1) / HCHUNK) * HWARPS; }
+
+cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, int center, unsigned long long *hist,
+                             unsigned long long *first, unsigned long long *zcount, cudaStream_t st) {
+    k_histogram<<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, center, hist, first, zcount);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_zeros(const uint16_t *codes, uint64_t n, unsigned long long *zcount, cudaStream_t st) {
+    k_count_zeros<<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, zcount);
     return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_gather_unpred(const uint16_t *codes, uint64_t n, uint64_t chunk, const unsigned long long *zcount,
-                                 const unsigned long long *zoff, const T *scratch, T *unpred, cudaStream_t st) {
-    k_gather_unpred<T><<<grid_for(n, chunk), 1024, 0, st>>>(codes, n, chunk, zcount, zoff, scratch, unpred);
+cudaError_t launch_compact_zeros(const uint16_t *codes, uint64_t n, const unsigned long long *zcount,
+                                 const unsigned long long *zoff, uint64_t *zpos, const T *scratch, T *vals,
+                                 cudaStream_t st) {
+    k_compact_zeros<T><<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, zcount, zoff, zpos, scratch, vals);
     return cudaGetLastError();
 }
-template cudaError_t launch_gather_unpred<float>(const uint16_t *, uint64_t, uint64_t, const unsigned long long *,
-                                                 const unsigned long long *, const float *, float *, cudaStream_t);
-template cudaError_t launch_gather_unpred<double>(const uint16_t *, uint64_t, uint64_t, const unsigned long long *,
-                                                  const unsigned long long *, const double *, double *,
+template cudaError_t launch_compact_zeros<float>(const uint16_t *, uint64_t, const unsigned long long *,
+                                                 const unsigned long long *, uint64_t *, const float *, float *,
+                                                 cudaStream_t);
+template cudaError_t launch_compact_zeros<double>(const uint16_t *, uint64_t, const unsigned long long *,
+                                                  const unsigned long long *, uint64_t *, const double *, double *,
                                                   cudaStream_t);
 
-cudaError_t launch_count_zeros(const uint16_t *codes, uint64_t n, uint64_t chunk, unsigned long long *zcount,
-                               cudaStream_t st) {
-    k_count_zeros<<<grid_for(n, chunk), 1024, 0, st>>>(codes, n, chunk, zcount);
-    return cudaGetLastError();
-}
+uint64_t scan_temp_words(uint64_t n) { return (n + SCAN_B - 1) / SCAN_B + 1; }
 
-cudaError_t launch_zero_positions(const uint16_t *codes, uint64_t n, uint64_t chunk, const unsigned long long *zcount,
-                                  const unsigned long long *zoff, uint64_t *zpos, cudaStream_t st) {
-    k_zero_positions<<<grid_for(n, chunk), 1024, 0, st>>>(codes, n, chunk, zcount, zoff, zpos);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_scan_u64(const unsigned long long *in, unsigned long long *out, uint64_t n, cudaStream_t st) {
-    k_scan_u64<<<1, 1024, 0, st>>>(in, out, n);
+cudaError_t launch_scan_u64(const unsigned long long *in, unsigned long long *out, uint64_t n,
+                            unsigned long long *temp, cudaStream_t st) {
+    uint64_t nb = (n + SCAN_B - 1) / SCAN_B;
+    if (nb == 0) nb = 1;
+    k_scan_reduce<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, temp);
+    k_scan_top<<<1, 1024, 0, st>>>(temp, nb);
+    k_scan_down<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, temp, out, nb);
     return cudaGetLastError();
 }
 
@@ -441,20 +536,45 @@ cudaError_t launch_encode_pack(const uint16_t *codes, uint64_t n, int offset, co
     return cudaGetLastError();
 }
 
-cudaError_t launch_decode_sync(const DecodeTablesDev &td, const uint64_t *w, uint64_t nbits, uint64_t unit,
-                               uint64_t nunits, const uint64_t *end_in, uint64_t *start, uint64_t *end_out,
-                               unsigned int *cnt, int refine, int *changed, cudaStream_t st) {
+uint64_t decode_units(uint64_t nbits) { return (nbits + DEC_UNIT - 1) / DEC_UNIT; }
+uint64_t decode_unit_bits() { return DEC_UNIT; }
+int decode_boundaries() { return DEC_NB; }
+
+cudaError_t launch_decode_spec(const DecodeTablesDev &td, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
+                               uint64_t nunits, uint64_t *end, unsigned int *cnt, uint16_t *bnd, int *err,
+                               cudaStream_t st) {
     DecTables t{td.lut, td.left, td.right, td.sym, td.leaf};
-    k_decode_sync<<<grid_for(nunits, 256), 256, 0, st>>>(t, w, nbits, unit, nunits, end_in, start, end_out, cnt,
-                                                          refine, changed);
+    k_decode_spec<<<grid_for(nunits, DEC_T), DEC_T, 0, st>>>(t, w32, nwords, nbits, nunits, end, cnt, bnd, err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_decode_write(const DecodeTablesDev &td, const uint64_t *w, uint64_t nbits, uint64_t unit,
+cudaError_t launch_decode_resync(const DecodeTablesDev &td, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
+                                 uint64_t nunits, const uint64_t *end_in, uint64_t *end_out, unsigned int *cnt,
+                                 const uint16_t *bnd, uint64_t *start, int *changed, cudaStream_t st) {
+    DecTables t{td.lut, td.left, td.right, td.sym, td.leaf};
+    k_decode_resync<<<grid_for(nunits, DEC_T), DEC_T, 0, st>>>(t, w32, nwords, nbits, nunits, end_in, end_out, cnt,
+                                                                bnd, start, changed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_decode_write(const DecodeTablesDev &td, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
                                 uint64_t nunits, const uint64_t *start, const unsigned long long *off, uint64_t nout,
                                 int offset, uint16_t *out, cudaStream_t st) {
     DecTables t{td.lut, td.left, td.right, td.sym, td.leaf};
-    k_decode_write<<<grid_for(nunits, 256), 256, 0, st>>>(t, w, nbits, unit, nunits, start, off, nout, offset, out);
+    k_decode_write<<<grid_for(nunits, DEC_T), DEC_T, 0, st>>>(t, w32, nwords, nbits, nunits, start, off, nout, offset,
+                                                               out);
+    return cudaGetLastError();
+}
+
+__global__ void k_init_starts(uint64_t *start, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        start[i] = i * DEC_UNIT;
+}
+cudaError_t launch_init_starts(uint64_t *start, uint64_t n, cudaStream_t st) {
+    unsigned g = grid_for(n, 1024);
+    if (g > 4096) g = 4096;
+    if (g == 0) g = 1;
+    k_init_starts<<<g, 1024, 0, st>>>(start, n);
     return cudaGetLastError();
 }
 

@@ -26,17 +26,17 @@ template <typename T>
 cudaError_t launch_anchors(bool decomp, const T *X, T *W, uint16_t *codes, T *scratch, const T *unpred,
                            const int64_t *na, const int64_t *step, const int64_t *offs, cudaStream_t st);
 
-cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, uint64_t chunk, int center,
-                             unsigned long long *hist, unsigned long long *first, unsigned long long *zcount,
-                             cudaStream_t st);
+uint64_t hist_subchunks(uint64_t n);
+cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, int center, unsigned long long *hist,
+                             unsigned long long *first, unsigned long long *zcount, cudaStream_t st);
+cudaError_t launch_count_zeros(const uint16_t *codes, uint64_t n, unsigned long long *zcount, cudaStream_t st);
 template <typename T>
-cudaError_t launch_gather_unpred(const uint16_t *codes, uint64_t n, uint64_t chunk, const unsigned long long *zcount,
-                                 const unsigned long long *zoff, const T *scratch, T *unpred, cudaStream_t st);
-cudaError_t launch_count_zeros(const uint16_t *codes, uint64_t n, uint64_t chunk, unsigned long long *zcount,
-                               cudaStream_t st);
-cudaError_t launch_zero_positions(const uint16_t *codes, uint64_t n, uint64_t chunk, const unsigned long long *zcount,
-                                  const unsigned long long *zoff, uint64_t *zpos, cudaStream_t st);
-cudaError_t launch_scan_u64(const unsigned long long *in, unsigned long long *out, uint64_t n, cudaStream_t st);
+cudaError_t launch_compact_zeros(const uint16_t *codes, uint64_t n, const unsigned long long *zcount,
+                                 const unsigned long long *zoff, uint64_t *zpos, const T *scratch, T *vals,
+                                 cudaStream_t st);
+uint64_t scan_temp_words(uint64_t n);
+cudaError_t launch_scan_u64(const unsigned long long *in, unsigned long long *out, uint64_t n,
+                            unsigned long long *temp, cudaStream_t st);
 uint64_t encode_chunks(uint64_t n);
 cudaError_t launch_encode_bits(const uint16_t *codes, uint64_t n, int offset, const uint8_t *len,
                                unsigned long long *chunkbits, cudaStream_t st);
@@ -50,10 +50,17 @@ struct DecodeTablesDev {
     const int32_t *sym;
     const uint8_t *leaf;
 };
-cudaError_t launch_decode_sync(const DecodeTablesDev &t, const uint64_t *w, uint64_t nbits, uint64_t unit,
-                               uint64_t nunits, const uint64_t *end_in, uint64_t *start, uint64_t *end_out,
-                               unsigned int *cnt, int refine, int *changed, cudaStream_t st);
-cudaError_t launch_decode_write(const DecodeTablesDev &t, const uint64_t *w, uint64_t nbits, uint64_t unit,
+uint64_t decode_units(uint64_t nbits);
+uint64_t decode_unit_bits();
+int decode_boundaries();
+cudaError_t launch_init_starts(uint64_t *start, uint64_t n, cudaStream_t st);
+cudaError_t launch_decode_spec(const DecodeTablesDev &t, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
+                               uint64_t nunits, uint64_t *end, unsigned int *cnt, uint16_t *bnd, int *err,
+                               cudaStream_t st);
+cudaError_t launch_decode_resync(const DecodeTablesDev &t, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
+                                 uint64_t nunits, const uint64_t *end_in, uint64_t *end_out, unsigned int *cnt,
+                                 const uint16_t *bnd, uint64_t *start, int *changed, cudaStream_t st);
+cudaError_t launch_decode_write(const DecodeTablesDev &t, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
                                 uint64_t nunits, const uint64_t *start, const unsigned long long *off, uint64_t nout,
                                 int offset, uint16_t *out, cudaStream_t st);
 cudaError_t launch_fill_u16(uint16_t *out, uint64_t n, uint16_t v, cudaStream_t st);

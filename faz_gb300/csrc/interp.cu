@@ -40,23 +40,6 @@ template <typename T> __device__ __forceinline__ T i_cubic(T a, T b, T c, T d) {
     return (-a + (T)9 * b + (T)9 * c - d) * (T)0.0625;
 }
 
-// Prediction of odd index m on a line of n lattice points; value at index k
-// is p[(k >> sh) * st].
-template <typename T>
-__device__ __forceinline__ T predict(const T *p, int st, int sh, int m, int n, int cubic) {
-#define V_(k) p[((k) >> sh) * st]
-    if (!cubic || n < 5) {
-        if (m + 1 < n) return i_linear(V_(m - 1), V_(m + 1));
-        return n < 4 ? V_(m - 1) : i_linear1(V_(m - 3), V_(m - 1));
-    }
-    int ia = (n & 1) ? n - 2 : n - 3;
-    if (m == 1) return i_quad1(V_(0), V_(2), V_(4));
-    if (m == ia) return i_quad2(V_(m - 3), V_(m - 1), V_(m + 1));
-    if (m == n - 1) return i_quad3(V_(m - 5), V_(m - 3), V_(m - 1));
-    return i_cubic(V_(m - 3), V_(m - 1), V_(m + 1), V_(m + 3));
-#undef V_
-}
-
 // LinearQuantizer::quantize_and_overwrite (IntegerQuantizer.hpp:69-108).
 // Returns the code; v becomes the reconstruction when predictable; uval is
 // the value recorded as unpredictable when the code is 0.
@@ -186,6 +169,66 @@ __device__ __forceinline__ T recover_any(T pred, int code, uint64_t pos, const L
 }
 
 // --------------------------------------------------------- level kernel
+// Stencil of one target, set up once per lane and sweep: the values it reads
+// (shared-memory offsets from the line origin) and the coefficients of the
+// reference's formula, folded so that one expression evaluates all of them
+// in the reference's operation order:
+//   y = ((k1*x1 + k2*x2) + k3*x3) + k4*x4 with 2, 3 or 4 terms, times scale.
+// k = +-1 multiplies are exact, so -a + 9b equals (-1)*a + 9*b bit for bit
+// and x - c equals x + (-1)*c.
+template <typename T>
+struct Stencil {
+    int i1, i2, i3, i4;  // shared-memory offsets
+    T k1, k2, k3, k4, scale;
+    int nt;              // 1 copy, 2..4 terms, 5 linear1 (double literals)
+};
+
+template <typename T>
+__device__ __forceinline__ Stencil<T> make_stencil(int m, int n, int cubic, int st, int sh) {
+    Stencil<T> S;
+    int o1 = -1, o2 = 1, o3 = -1, o4 = -1;
+    S.k1 = 1; S.k2 = 1; S.k3 = 0; S.k4 = 0; S.scale = (T)0.5; S.nt = 2;
+    if (!cubic || n < 5) {
+        if (m + 1 >= n) {
+            if (n < 4) { S.nt = 1; o1 = -1; o2 = -1; }
+            else { S.nt = 5; o1 = -3; o2 = -1; }
+        }
+    } else {
+        int ia = (n & 1) ? n - 2 : n - 3;
+        if (m == 1) {            // (3a + 6b - c) / 8, a=v0 b=v2 c=v4
+            o1 = -1; o2 = 1; o3 = 3; S.k1 = 3; S.k2 = 6; S.k3 = -1; S.nt = 3; S.scale = (T)0.125;
+        } else if (m == ia) {    // (-a + 6b + 3c) / 8
+            o1 = -3; o2 = -1; o3 = 1; S.k1 = -1; S.k2 = 6; S.k3 = 3; S.nt = 3; S.scale = (T)0.125;
+        } else if (m == n - 1) { // (3a - 10b + 15c) / 8
+            o1 = -5; o2 = -3; o3 = -1; S.k1 = 3; S.k2 = -10; S.k3 = 15; S.nt = 3; S.scale = (T)0.125;
+        } else {                 // (-a + 9b + 9c - d) / 16
+            o1 = -3; o2 = -1; o3 = 1; o4 = 3; S.k1 = -1; S.k2 = 9; S.k3 = 9; S.k4 = -1; S.nt = 4;
+            S.scale = (T)0.0625;
+        }
+    }
+    S.i1 = ((m + o1) >> sh) * st;
+    S.i2 = ((m + o2) >> sh) * st;
+    S.i3 = ((m + o3) >> sh) * st;
+    S.i4 = ((m + o4) >> sh) * st;
+    return S;
+}
+
+template <typename T>
+__device__ __forceinline__ T eval_stencil(const Stencil<T> &S, const T *p) {
+    T x1 = p[S.i1], x2 = p[S.i2];
+    if (S.nt == 5) return i_linear1(x1, x2);
+    T x3 = p[S.i3], x4 = p[S.i4];
+    T s2 = S.k1 * x1 + S.k2 * x2;
+    T s3 = s2 + S.k3 * x3;
+    T s4 = s3 + S.k4 * x4;
+    T y = S.nt == 4 ? s4 : (S.nt == 3 ? s3 : s2);
+    return S.nt == 1 ? x1 : y * S.scale;
+}
+
+// One CTA per block.  Each half-warp takes one line at a time; lane t of the
+// half-warp owns target 2t+1 of the line.  Shared-memory strides along every
+// sweep axis are odd multiples of the lane step, so the half-warps read
+// distinct banks.
 template <typename T, bool DECOMP>
 __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
                                                       uint16_t *__restrict__ codes, T *__restrict__ scratch,
@@ -193,7 +236,7 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
                                                       const T *__restrict__ unpred) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *V = reinterpret_cast<T *>(smem_raw);
-    uint16_t *stg = reinterpret_cast<uint16_t *>(smem_raw + (size_t)a.vwords * sizeof(T));
+    uint16_t *stg = reinterpret_cast<uint16_t *>(smem_raw + (((size_t)a.vwords * sizeof(T) + 15) & ~(size_t)15));
     const int64_t bid = blockIdx.x;
     int64_t bc[3];
     block_coords(a, bid, bc);
@@ -206,24 +249,26 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
     const int64_t gbase = g.beg[0] * a.offs[0] + g.beg[1] * a.offs[1] + g.beg[2] * a.offs[2];
     const uint64_t base = a.block_off[bid];
     const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+    const int t = tid & 15, hw = tid >> 4, nhw = nt >> 4;
     const int cubic = a.cubic;
 
-    // phase 0: lattice points with even index along P2
-    const int nv = n0 * n1 * h2;
-    for (int i = tid; i < nv; i += nt) {
-        int e = i % h2;
-        int q = i / h2;
-        int m1 = q % n1;
-        int m0 = q / n1;
-        int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)(2 * e) * G2;
-        bool coarse = !(m0 & 1) && !(m1 & 1);
-        if (coarse) V[i] = W[gi];
-        else if (!DECOMP) V[i] = X[gi];
+    // phase 0: lattice points with an even index along P2, one warp per row
+    {
+        const int rows = n0 * n1;
+        for (int r = warp; r < rows; r += nwarps) {
+            const int m0 = r / n1, m1 = r - m0 * n1;
+            const bool coarse = !(m0 & 1) && !(m1 & 1);
+            if (DECOMP && !coarse) continue;
+            const T *src = coarse ? W : X;
+            const int64_t rb = gbase + m0 * G0 + m1 * G1;
+            T *dst = V + r * h2;
+            for (int e = lane; e < h2; e += 32) dst[e] = src[rb + (int64_t)(2 * e) * G2];
+        }
     }
     __syncthreads();
 
-    // sweep 1: lines along P0 at even (m1, m2), including first-plane lines
-    const int hh1 = (n1 + 1) / 2;
+    // sweep 1: lines along P0 at even (m1, m2), first planes included
     if (g.t0 > 0) {
         const int64_t cnt = g.c1;
         if (DECOMP) {
@@ -231,20 +276,22 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
             __syncthreads();
         }
         const int st = n1 * h2;
-        const int total = g.t0 * hh1 * h2;
-        for (int w = tid; w < total; w += nt) {
-            int e2 = w % h2;
-            int q = w / h2;
-            int e1 = q % hh1;
-            int t = q / hh1;
-            int m0 = 2 * t + 1, m1 = 2 * e1;
-            int col = m1 * h2 + e2;
-            T pred = predict(V + col, st, 0, m0, n0, cubic);
-            int idx = m0 * st + col;
-            bool emit = e1 >= k1 && e2 >= k2;
-            int rank = 0;
-            if (emit) rank = ((e1 - k1) * g.ne2 + (e2 - k2)) * g.t0 + line_rank(m0, n0, cubic);
-            int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)(2 * e2) * G2;
+        const int hh1 = (n1 + 1) / 2;
+        const int lines = hh1 * h2;
+        const bool act = t < g.t0;
+        const int m0 = 2 * t + 1;
+        Stencil<T> S = make_stencil<T>(act ? m0 : 1, n0, cubic, st, 0);
+        const int rk = act ? line_rank(m0, n0, cubic) : 0;
+        const int64_t gl = (int64_t)m0 * G0;
+        for (int l = hw; l < lines; l += nhw) {
+            if (!act) continue;
+            const int e1 = l / h2, e2 = l - e1 * h2;
+            const int col = 2 * e1 * h2 + e2;
+            const bool emit = e1 >= k1 && e2 >= k2;
+            const int rank = ((e1 - k1) * g.ne2 + (e2 - k2)) * g.t0 + rk;
+            const T pred = eval_stencil(S, V + col);
+            const int idx = m0 * st + col;
+            const int64_t gi = gbase + gl + (2 * e1) * G1 + (int64_t)(2 * e2) * G2;
             if (!DECOMP) {
                 T v = V[idx], uv;
                 int code = quantize_any(v, pred, a, uv);
@@ -263,18 +310,17 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
                 } else {
                     // the previous block along P1 and/or P2 owns this line
                     int64_t ob[3] = {bc[0], bc[1], bc[2]};
-                    bool s1 = e1 < k1, s2 = e2 < k2;
+                    const bool s1 = e1 < k1, s2 = e2 < k2;
                     if (s1) ob[P1] -= 1;
                     if (s2) ob[P2] -= 1;
-                    int nf = (int)(a.bs / a.s) + 1;
-                    int on2 = s2 ? nf : n2;
-                    int ok1 = ob[P1] != 0, ok2 = ob[P2] != 0;
-                    int oe1 = s1 ? (nf - 1) / 2 : e1;
-                    int oe2 = s2 ? (nf - 1) / 2 : e2;
-                    int one2 = (on2 + 1) / 2 - ok2;
-                    int64_t oid = (ob[0] * a.nb[1] + ob[1]) * a.nb[2] + ob[2];
-                    pos = a.block_off[oid] + (uint64_t)((oe1 - ok1) * one2 + (oe2 - ok2)) * g.t0 +
-                          line_rank(m0, n0, cubic);
+                    const int nf = (int)(a.bs / a.s) + 1;
+                    const int on2 = s2 ? nf : n2;
+                    const int ok1 = ob[P1] != 0, ok2 = ob[P2] != 0;
+                    const int oe1 = s1 ? (nf - 1) / 2 : e1;
+                    const int oe2 = s2 ? (nf - 1) / 2 : e2;
+                    const int one2 = (on2 + 1) / 2 - ok2;
+                    const int64_t oid = (ob[0] * a.nb[1] + ob[1]) * a.nb[2] + ob[2];
+                    pos = a.block_off[oid] + (uint64_t)((oe1 - ok1) * one2 + (oe2 - ok2)) * g.t0 + rk;
                     if (pos >= a.ncodes) {
                         atomicExch(a.err, 1);
                         pos = 0;
@@ -302,20 +348,22 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
             for (int64_t i = tid; i < cnt; i += nt) stg[i] = codes[sbase + i];
             __syncthreads();
         }
-        const int total = (n0 - k0) * g.t1 * h2;
-        for (int w = tid; w < total; w += nt) {
-            int e2 = w % h2;
-            int q = w / h2;
-            int t = q % g.t1;
-            int m0 = k0 + q / g.t1;
-            int m1 = 2 * t + 1;
-            int col = m0 * n1 * h2 + e2;
-            T pred = predict(V + col, h2, 0, m1, n1, cubic);
-            int idx = col + m1 * h2;
-            bool emit = e2 >= k2;
-            int rank = 0;
-            if (emit) rank = ((m0 - k0) * g.ne2 + (e2 - k2)) * g.t1 + line_rank(m1, n1, cubic);
-            int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)(2 * e2) * G2;
+        const int lines = (n0 - k0) * h2;
+        const bool act = t < g.t1;
+        const int m1 = 2 * t + 1;
+        Stencil<T> S = make_stencil<T>(act ? m1 : 1, n1, cubic, h2, 0);
+        const int rk = act ? line_rank(m1, n1, cubic) : 0;
+        const int64_t gl = (int64_t)m1 * G1;
+        for (int l = hw; l < lines; l += nhw) {
+            if (!act) continue;
+            const int q = l / h2, e2 = l - q * h2;
+            const int m0 = k0 + q;
+            const int col = m0 * n1 * h2 + e2;
+            const bool emit = e2 >= k2;
+            const int rank = (q * g.ne2 + (e2 - k2)) * g.t1 + rk;
+            const T pred = eval_stencil(S, V + col);
+            const int idx = col + m1 * h2;
+            const int64_t gi = gbase + m0 * G0 + gl + (int64_t)(2 * e2) * G2;
             if (!DECOMP) {
                 T v = V[idx], uv;
                 int code = quantize_any(v, pred, a, uv);
@@ -335,14 +383,13 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
                     // the previous block along P2 owns this line
                     int64_t ob[3] = {bc[0], bc[1], bc[2]};
                     ob[P2] -= 1;
-                    int nf = (int)(a.bs / a.s) + 1;
-                    int ok2 = ob[P2] != 0;
-                    int oe2 = (nf - 1) / 2;
-                    int one2 = (nf + 1) / 2 - ok2;
-                    int64_t oc1 = (int64_t)g.ne1 * one2 * g.t0;
-                    int64_t oid = (ob[0] * a.nb[1] + ob[1]) * a.nb[2] + ob[2];
-                    pos = a.block_off[oid] + oc1 + (uint64_t)((m0 - k0) * one2 + (oe2 - ok2)) * g.t1 +
-                          line_rank(m1, n1, cubic);
+                    const int nf = (int)(a.bs / a.s) + 1;
+                    const int ok2 = ob[P2] != 0;
+                    const int oe2 = (nf - 1) / 2;
+                    const int one2 = (nf + 1) / 2 - ok2;
+                    const int64_t oc1 = (int64_t)g.ne1 * one2 * g.t0;
+                    const int64_t oid = (ob[0] * a.nb[1] + ob[1]) * a.nb[2] + ob[2];
+                    pos = a.block_off[oid] + oc1 + (uint64_t)(q * one2 + (oe2 - ok2)) * g.t1 + rk;
                     if (pos >= a.ncodes) {
                         atomicExch(a.err, 1);
                         pos = 0;
@@ -370,17 +417,20 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
             __syncthreads();
         }
         const int w1 = n1 - k1;
-        const int total = (int)cnt;
-        for (int w = tid; w < total; w += nt) {
-            int t = w % g.t2;
-            int q = w / g.t2;
-            int m1 = k1 + q % w1;
-            int m0 = k0 + q / w1;
-            int m2 = 2 * t + 1;
+        const int lines = (n0 - k0) * w1;
+        const bool act = t < g.t2;
+        const int m2 = 2 * t + 1;
+        Stencil<T> S = make_stencil<T>(act ? m2 : 1, n2, cubic, 1, 1);
+        const int rk = act ? line_rank(m2, n2, cubic) : 0;
+        const int64_t gl = (int64_t)m2 * G2;
+        for (int l = hw; l < lines; l += nhw) {
+            if (!act) continue;
+            const int q0 = l / w1, q1 = l - q0 * w1;
+            const int m0 = k0 + q0, m1 = k1 + q1;
             const T *row = V + (m0 * n1 + m1) * h2;
-            T pred = predict(row, 1, 1, m2, n2, cubic);
-            int rank = q * g.t2 + line_rank(m2, n2, cubic);
-            int64_t gi = gbase + m0 * G0 + m1 * G1 + (int64_t)m2 * G2;
+            const T pred = eval_stencil(S, row);
+            const int rank = l * g.t2 + rk;
+            const int64_t gi = gbase + m0 * G0 + m1 * G1 + gl;
             if (!DECOMP) {
                 T v = X[gi], uv;
                 int code = quantize_any(v, pred, a, uv);
@@ -388,8 +438,7 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
                 if (code == 0) scratch[sbase + rank] = uv;
                 if (a.write_back) W[gi] = v;
             } else {
-                uint64_t pos = sbase + rank;
-                W[gi] = recover_any(pred, (int)stg[rank], pos, a, zpos, nz, unpred);
+                W[gi] = recover_any(pred, (int)stg[rank], sbase + rank, a, zpos, nz, unpred);
             }
         }
         __syncthreads();
@@ -443,10 +492,32 @@ __global__ void k_anchors(const T *X, T *W, uint16_t *codes, T *scratch, const T
 }
 
 // ------------------------------------------------------------- min / max
+// 16-byte loads over the aligned body, scalar loads for the ends.
 template <typename T>
 __global__ void k_minmax(const T *__restrict__ X, uint64_t n, T *pmin, T *pmax) {
     T mn = X[0], mx = X[0];
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    constexpr int V = 16 / sizeof(T);
+    const uint64_t head = ((16 - ((uintptr_t)X & 15)) & 15) / sizeof(T);
+    const uint64_t h = head < n ? head : n;
+    const uint64_t nvec = (n - h) / V;
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nth = (uint64_t)gridDim.x * blockDim.x;
+    const uint4 *xv = reinterpret_cast<const uint4 *>(X + h);
+    for (uint64_t i = tid; i < nvec; i += nth) {
+        uint4 q = __ldg(xv + i);
+        const T *e = reinterpret_cast<const T *>(&q);
+#pragma unroll
+        for (int k = 0; k < V; k++) {
+            T v = e[k];
+            mn = v < mn ? v : mn;
+            mx = v > mx ? v : mx;
+        }
+    }
+    for (uint64_t i = tid; i < h; i += nth) {
+        T v = X[i];
+        mn = v < mn ? v : mn;
+        mx = v > mx ? v : mx;
+    }
+    for (uint64_t i = h + nvec * V + tid; i < n; i += nth) {
         T v = X[i];
         mn = v < mn ? v : mn;
         mx = v > mx ? v : mx;
@@ -493,11 +564,9 @@ template <typename T>
 cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const T *X, T *W, uint16_t *codes,
                          T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st) {
     size_t sm = level_smem_bytes<T>(a);
-    int threads = 512;
+    // half-warps take lines: enough threads for the lines of a block
     int64_t vol = (int64_t)a.vwords * 2;
-    if (vol < 2048) threads = 256;
-    if (vol < 512) threads = 128;
-    if (vol < 128) threads = 64;
+    int threads = vol >= 8192 ? 512 : (vol >= 1024 ? 256 : (vol >= 256 ? 128 : 64));
     if (!decomp) {
         auto k = k_interp_level<T, false>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
