@@ -214,6 +214,7 @@ void set_fast_path(LevelArgs &a) {
     float lo = (float)a.eb;
     if ((double)lo > a.eb) lo = std::nextafter(lo, 0.0f);
     a.eblo = lo;
+    a.twor_f = (float)(2 * a.radius);
     a.fast = 1;
 }
 

@@ -40,7 +40,7 @@ struct LevelArgs {
     uint64_t ncodes;     // codes in the whole stream (bounds every code read)
     int *err;            // set to 1 by a kernel that met an out-of-range position
     // float fast path: eb and 1/eb split into float pairs, largest float <= eb
-    float eh, el, rh, rl, eblo;
+    float eh, el, rh, rl, eblo, twor_f;
     int fast;            // 1: float data uses the exact float fast path
     unsigned long long *verify;  // non-null: count fast/double disagreements here
 };

@@ -44,22 +44,38 @@ FAZ_HD float f32_from_bits(uint32_t u) {
 #endif
 }
 
+// Integer <-> float for |x| < 2^22 with one float add and integer ops
+// (GB300 executes float<->int conversions and float rounding on its narrow
+// double-precision pipe): adding 1.5*2^23 leaves round-to-nearest(x) in the
+// low mantissa bits.
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int32_t kMagicBits = 0x4B400000;
+FAZ_HD int32_t rint_small(float x) { return (int32_t)f32_bits(x + kMagic) - kMagicBits; }
+FAZ_HD float int_to_float_small(int32_t i) { return f32_from_bits((uint32_t)(i + kMagicBits)) - kMagic; }
+
 // floor((floor(x) + 1) / 2) for x = RN_double(d * recip), recip = rh + rl.
 // Returns -1 when undecided, -2 when floor(x) + 1 >= twor (unpredictable).
+// twor <= 65536, so ph < twor keeps every value below 2^22.
 FAZ_HD int half_index_f32(float d, float rh, float rl, float twor_f, int twor) {
     float ph = d * rh;
     if (!(ph < twor_f)) return ph != ph ? -1 : -2;
     float pl = fmaf(d, rh, -ph);
     float c = fmaf(d, rl, pl);
-    float k = floorf(ph);
-    float f = (ph - k) + c;
-    float fi = floorf(f);
-    float fr = f - fi;
+    // k = floor(ph): nearest integer, minus one if it lies above ph
+    int32_t ki = rint_small(ph);
+    float kf = int_to_float_small(ki);
+    if (kf > ph) {
+        ki -= 1;
+        kf -= 1.0f;
+    }
+    float f = (ph - kf) + c;        // in (-1/256, 1 + 1/256)
+    int32_t ri = rint_small(f);     // -1, 0, 1 or 2
+    float fr = f - int_to_float_small(ri);  // in [-1/2, 1/2]
     int fl;
-    if (fr > 0x1p-20f && fr < 1.0f - 0x1p-20f) {
-        fl = (int)k + (int)fi;
+    if (fabsf(fr) > 0x1p-20f) {
+        fl = ki + ri - (fr < 0.0f ? 1 : 0);
     } else {
-        int B = (int)k + (int)rintf(f);
+        int B = ki + ri;
         if (B & 1) return -1;  // floor is B-1 or B, with different halves
         fl = B;                // floor is B-1 or B, same half B/2
     }
@@ -75,7 +91,7 @@ FAZ_HD bool dequant_f32(float pred, int q2, float eh, float el, float &out) {
         out = pred + 0.0f;
         return true;
     }
-    float q = (float)q2;
+    float q = int_to_float_small(q2);  // |q2| <= 65536
     float p1 = q * eh;
     float e1 = fmaf(q, eh, -p1);
     float p2 = q * el;

@@ -237,10 +237,25 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
     uint16_t sym[ENC_PER_THREAD];
     unsigned long long mybits = 0;
     const uint64_t t0 = c0 + (uint64_t)threadIdx.x * ENC_PER_THREAD;
-    for (int k = 0; k < ENC_PER_THREAD; k++) {
-        uint64_t i = t0 + k;
-        sym[k] = i < n ? (uint16_t)(codes[i] - offset) : 0xffff;
-        if (i < n) mybits += len[sym[k]];
+    if (t0 + ENC_PER_THREAD <= n) {
+        // 16 codes = two 16-byte loads (codes is 256-byte aligned, t0 a multiple of 16)
+        const uint4 *cv = reinterpret_cast<const uint4 *>(codes + t0);
+        uint4 a = cv[0], b = cv[1];
+        const uint16_t *pa = reinterpret_cast<const uint16_t *>(&a);
+        const uint16_t *pb = reinterpret_cast<const uint16_t *>(&b);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            sym[k] = (uint16_t)(pa[k] - offset);
+            sym[k + 8] = (uint16_t)(pb[k] - offset);
+        }
+#pragma unroll
+        for (int k = 0; k < ENC_PER_THREAD; k++) mybits += len[sym[k]];
+    } else {
+        for (int k = 0; k < ENC_PER_THREAD; k++) {
+            uint64_t i = t0 + k;
+            sym[k] = i < n ? (uint16_t)(codes[i] - offset) : 0xffff;
+            if (i < n) mybits += len[sym[k]];
+        }
     }
     tsum[threadIdx.x] = mybits;
     __syncthreads();
@@ -407,24 +422,26 @@ __global__ void __launch_bounds__(DEC_T) k_decode_resync(DecTables t, const uint
         return;
     }
     uint32_t p = (uint32_t)(s_true - g0);
-    const uint16_t *b = bnd + u * DEC_NB;
     const bool first_pass = start[u] == u * DEC_UNIT;
+    // the speculative boundaries, ascending (unused entries are 0xffff)
+    uint32_t bw[DEC_NB / 2];
+    const uint32_t *b32 = reinterpret_cast<const uint32_t *>(bnd + u * DEC_NB);
+#pragma unroll
+    for (int k = 0; k < DEC_NB / 2; k++) bw[k] = first_pass ? b32[k] : 0xffffffffu;
     unsigned int c = 0;
     bool synced = false;
+    int j = 0;  // first speculative boundary not yet passed
     while (p < stop) {
-        if (first_pass) {
-            uint32_t off = p - nominal;
-            if (off < 0xffff) {
-                for (int k = 0; k < DEC_NB; k++) {
-                    if (b[k] == off) {
-                        c += cnt[u] - k;
-                        synced = true;
-                        break;
-                    }
-                    if (b[k] > off) break;
-                }
-            }
-            if (synced) break;
+        const uint32_t off = p - nominal;
+        while (j < DEC_NB) {
+            uint32_t bj = (bw[j >> 1] >> ((j & 1) * 16)) & 0xffffu;
+            if (bj >= off) break;
+            j++;
+        }
+        if (j < DEC_NB && ((bw[j >> 1] >> ((j & 1) * 16)) & 0xffffu) == off) {
+            c += cnt[u] - j;
+            synced = true;
+            break;
         }
         if (dec_sym(t, slut, sw, p) < 0) {
             atomicExch(changed, -1);
@@ -456,11 +473,27 @@ __global__ void __launch_bounds__(DEC_T) k_decode_write(DecTables t, const uint3
     uint32_t p = (uint32_t)(start[u] - g0);
     const uint32_t stop = (uint32_t)(lim - g0);
     uint64_t o = off[u];
-    while (p < stop && o < nout) {
+    // 2-byte stores up to a 16-byte boundary, then 8 symbols per store
+    while (p < stop && o < nout && (o & 7)) {
         int s = dec_sym(t, slut, sw, p);
-        if (s < 0) break;
+        if (s < 0) return;
         out[o++] = (uint16_t)(s + offset);
     }
+    uint32_t pk[4];
+    int k = 0;
+    while (p < stop && o + k < nout) {
+        int s = dec_sym(t, slut, sw, p);
+        if (s < 0) break;
+        uint32_t v = (uint32_t)(uint16_t)(s + offset);
+        if (k & 1) pk[k >> 1] |= v << 16;
+        else pk[k >> 1] = v;
+        if (++k == 8) {
+            *reinterpret_cast<uint4 *>(out + o) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            o += 8;
+            k = 0;
+        }
+    }
+    for (int i = 0; i < k; i++) out[o + i] = (uint16_t)(pk[i >> 1] >> ((i & 1) * 16));
 }
 
 __global__ void k_fill_u16(uint16_t *out, uint64_t n, uint16_t v) {

@@ -96,7 +96,7 @@ __device__ __forceinline__ int quantize_fast(float &v, float pred, const LevelAr
     }
     float diff = orig - pred;
     int twor = 2 * a.radius;
-    int half = half_index_f32(fabsf(diff), a.rh, a.rl, (float)twor, twor);
+    int half = half_index_f32(fabsf(diff), a.rh, a.rl, a.twor_f, twor);
     if (half == -1) return quantize<float>(v, pred, a.eb, a.recip, a.radius, a.trim, uval);
     uval = orig;
     if (half == -2) return 0;
@@ -256,8 +256,12 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
     // phase 0: lattice points with an even index along P2, one warp per row
     {
         const int rows = n0 * n1;
-        for (int r = warp; r < rows; r += nwarps) {
-            const int m0 = r / n1, m1 = r - m0 * n1;
+        int m0 = warp / n1, m1 = warp - m0 * n1;
+        for (int r = warp; r < rows; r += nwarps, m1 += nwarps) {
+            while (m1 >= n1) {
+                m1 -= n1;
+                m0++;
+            }
             const bool coarse = !(m0 & 1) && !(m1 & 1);
             if (DECOMP && !coarse) continue;
             const T *src = coarse ? W : X;
@@ -283,9 +287,13 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
         Stencil<T> S = make_stencil<T>(act ? m0 : 1, n0, cubic, st, 0);
         const int rk = act ? line_rank(m0, n0, cubic) : 0;
         const int64_t gl = (int64_t)m0 * G0;
-        for (int l = hw; l < lines; l += nhw) {
+        int e1 = hw / h2, e2 = hw - e1 * h2;
+        for (int l = hw; l < lines; l += nhw, e2 += nhw) {
+            while (e2 >= h2) {
+                e2 -= h2;
+                e1++;
+            }
             if (!act) continue;
-            const int e1 = l / h2, e2 = l - e1 * h2;
             const int col = 2 * e1 * h2 + e2;
             const bool emit = e1 >= k1 && e2 >= k2;
             const int rank = ((e1 - k1) * g.ne2 + (e2 - k2)) * g.t0 + rk;
@@ -354,9 +362,13 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
         Stencil<T> S = make_stencil<T>(act ? m1 : 1, n1, cubic, h2, 0);
         const int rk = act ? line_rank(m1, n1, cubic) : 0;
         const int64_t gl = (int64_t)m1 * G1;
-        for (int l = hw; l < lines; l += nhw) {
+        int q = hw / h2, e2 = hw - q * h2;
+        for (int l = hw; l < lines; l += nhw, e2 += nhw) {
+            while (e2 >= h2) {
+                e2 -= h2;
+                q++;
+            }
             if (!act) continue;
-            const int q = l / h2, e2 = l - q * h2;
             const int m0 = k0 + q;
             const int col = m0 * n1 * h2 + e2;
             const bool emit = e2 >= k2;
@@ -423,9 +435,13 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
         Stencil<T> S = make_stencil<T>(act ? m2 : 1, n2, cubic, 1, 1);
         const int rk = act ? line_rank(m2, n2, cubic) : 0;
         const int64_t gl = (int64_t)m2 * G2;
-        for (int l = hw; l < lines; l += nhw) {
+        int q0 = hw / w1, q1 = hw - q0 * w1;
+        for (int l = hw; l < lines; l += nhw, q1 += nhw) {
+            while (q1 >= w1) {
+                q1 -= w1;
+                q0++;
+            }
             if (!act) continue;
-            const int q0 = l / w1, q1 = l - q0 * w1;
             const int m0 = k0 + q0, m1 = k1 + q1;
             const T *row = V + (m0 * n1 + m1) * h2;
             const T pred = eval_stencil(S, row);
