@@ -85,6 +85,18 @@ __device__ __forceinline__ int quantize(T &v, T pred, double eb, double recip, i
 // (floor) or 2^-18 ulp (rounding) of such a boundary, on cancellation, at
 // powers of two, zero or non-finite values, the double computation is used.
 
+// Double-precision fallbacks of the float path, kept out of line: inlined,
+// the compiler may evaluate them unconditionally (as selects), which on GB300's
+// narrow double pipe costs more than the whole float path.
+__device__ __noinline__ int quantize_dp_f32(float &v, float pred, double eb, double recip, int radius, int trim,
+                                            float &uval) {
+    return quantize<float>(v, pred, eb, recip, radius, trim, uval);
+}
+__device__ __noinline__ float dequant_dp_f32(float pred, int q2, double eb) {
+    return (float)((double)pred + (double)q2 * eb);
+}
+__device__ __noinline__ float linear1_dp_f32(float a, float b) { return i_linear1(a, b); }
+
 // Float specialisation of the quantiser: fast path with the double path as
 // the fallback (and, in verify mode, as the check).
 __device__ __forceinline__ int quantize_fast(float &v, float pred, const LevelArgs &a, float &uval) {
@@ -97,7 +109,7 @@ __device__ __forceinline__ int quantize_fast(float &v, float pred, const LevelAr
     float diff = orig - pred;
     int twor = 2 * a.radius;
     int half = half_index_f32(fabsf(diff), a.rh, a.rl, a.twor_f, twor);
-    if (half == -1) return quantize<float>(v, pred, a.eb, a.recip, a.radius, a.trim, uval);
+    if (half == -1) return quantize_dp_f32(v, pred, a.eb, a.recip, a.radius, a.trim, uval);
     uval = orig;
     if (half == -2) return 0;
     int q2 = half << 1;
@@ -109,7 +121,7 @@ __device__ __forceinline__ int quantize_fast(float &v, float pred, const LevelAr
         code = a.radius + half;
     }
     float dec;
-    if (!dequant_f32(pred, q2, a.eh, a.el, dec)) dec = (float)((double)pred + (double)q2 * a.eb);
+    if (!dequant_f32(pred, q2, a.eh, a.el, dec)) dec = dequant_dp_f32(pred, q2, a.eb);
     float err = dec - orig;
     if (fabsf(err) > a.eblo || (a.trim == 2 && code == 1)) return 0;
     v = dec;
@@ -150,6 +162,11 @@ __device__ __forceinline__ T recover(T pred, int code, uint64_t pos, double eb, 
     return lo < nz ? unpred[lo] : (T)0;
 }
 
+__device__ __noinline__ float recover_dp_f32(float pred, int code, uint64_t pos, double eb, int radius, int trim,
+                                             const uint64_t *zpos, uint64_t nz, const float *unpred) {
+    return recover<float>(pred, code, pos, eb, radius, trim, zpos, nz, unpred);
+}
+
 template <typename T>
 __device__ __forceinline__ T recover_any(T pred, int code, uint64_t pos, const LevelArgs &a, const uint64_t *zpos,
                                          uint64_t nz, const T *unpred) {
@@ -165,7 +182,8 @@ __device__ __forceinline__ T recover_any(T pred, int code, uint64_t pos, const L
             }
         }
     }
-    return recover<T>(pred, code, pos, a.eb, a.radius, a.trim, zpos, nz, unpred);
+    if constexpr (sizeof(T) == 4) return recover_dp_f32(pred, code, pos, a.eb, a.radius, a.trim, zpos, nz, unpred);
+    else return recover<T>(pred, code, pos, a.eb, a.radius, a.trim, zpos, nz, unpred);
 }
 
 // --------------------------------------------------------- level kernel
@@ -214,9 +232,15 @@ __device__ __forceinline__ Stencil<T> make_stencil(int m, int n, int cubic, int 
 }
 
 template <typename T>
+__device__ __forceinline__ T linear1_any(T a, T b) {
+    if constexpr (sizeof(T) == 4) return linear1_dp_f32(a, b);
+    else return i_linear1(a, b);
+}
+
+template <typename T>
 __device__ __forceinline__ T eval_stencil(const Stencil<T> &S, const T *p) {
     T x1 = p[S.i1], x2 = p[S.i2];
-    if (S.nt == 5) return i_linear1(x1, x2);
+    if (S.nt == 5) return linear1_any(x1, x2);
     T x3 = p[S.i3], x4 = p[S.i4];
     T s2 = S.k1 * x1 + S.k2 * x2;
     T s3 = s2 + S.k3 * x3;
