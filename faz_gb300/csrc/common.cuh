@@ -65,6 +65,10 @@ FAZ_HD void block_coords(const LevelArgs &a, int64_t bid, int64_t *bc) {
     bc[0] = r / a.nb[1];
 }
 
+// element i of (x0, x1, x2) without a runtime-indexed array
+template <typename V>
+FAZ_HD V pick3(int i, V x0, V x1, V x2) { return i == 0 ? x0 : (i == 1 ? x1 : x2); }
+
 FAZ_HD void block_geom(const LevelArgs &a, const int64_t *bc, BlockGeom &g) {
     for (int d = 0; d < 3; d++) {
         int64_t b = bc[d] * a.bs;
@@ -74,12 +78,12 @@ FAZ_HD void block_geom(const LevelArgs &a, const int64_t *bc, BlockGeom &g) {
         g.n[d] = (int)((e - b) / a.s + 1);
         g.sk[d] = b != 0;
     }
-    g.n0 = g.n[a.perm[0]];
-    g.n1 = g.n[a.perm[1]];
-    g.n2 = g.n[a.perm[2]];
-    g.k0 = g.sk[a.perm[0]];
-    g.k1 = g.sk[a.perm[1]];
-    g.k2 = g.sk[a.perm[2]];
+    g.n0 = pick3(a.perm[0], g.n[0], g.n[1], g.n[2]);
+    g.n1 = pick3(a.perm[1], g.n[0], g.n[1], g.n[2]);
+    g.n2 = pick3(a.perm[2], g.n[0], g.n[1], g.n[2]);
+    g.k0 = pick3(a.perm[0], g.sk[0], g.sk[1], g.sk[2]);
+    g.k1 = pick3(a.perm[1], g.sk[0], g.sk[1], g.sk[2]);
+    g.k2 = pick3(a.perm[2], g.sk[0], g.sk[1], g.sk[2]);
     g.h2 = (g.n2 + 1) / 2;
     g.ne1 = (g.n1 + 1) / 2 - g.k1;
     g.ne2 = (g.n2 + 1) / 2 - g.k2;

@@ -254,7 +254,7 @@ __device__ __forceinline__ T eval_stencil(const Stencil<T> &S, const T *p) {
 // sweep axis are odd multiples of the lane step, so the half-warps read
 // distinct banks.
 template <typename T, bool DECOMP>
-__global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
+__global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
                                                       uint16_t *__restrict__ codes, T *__restrict__ scratch,
                                                       const uint64_t *__restrict__ zpos, uint64_t nz,
                                                       const T *__restrict__ unpred) {
@@ -269,7 +269,9 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
     const int P0 = a.perm[0], P1 = a.perm[1], P2 = a.perm[2];
     const int n0 = g.n0, n1 = g.n1, n2 = g.n2, h2 = g.h2;
     const int k0 = g.k0, k1 = g.k1, k2 = g.k2;
-    const int64_t G0 = a.s * a.offs[P0], G1 = a.s * a.offs[P1], G2 = a.s * a.offs[P2];
+    const int64_t G0 = a.s * pick3(P0, a.offs[0], a.offs[1], a.offs[2]);
+    const int64_t G1 = a.s * pick3(P1, a.offs[0], a.offs[1], a.offs[2]);
+    const int64_t G2 = a.s * pick3(P2, a.offs[0], a.offs[1], a.offs[2]);
     const int64_t gbase = g.beg[0] * a.offs[0] + g.beg[1] * a.offs[1] + g.beg[2] * a.offs[2];
     const uint64_t base = a.block_off[bid];
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -281,6 +283,7 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
     {
         const int rows = n0 * n1;
         int m0 = warp / n1, m1 = warp - m0 * n1;
+#pragma unroll 4
         for (int r = warp; r < rows; r += nwarps, m1 += nwarps) {
             while (m1 >= n1) {
                 m1 -= n1;
@@ -341,17 +344,17 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
                     code = stg[rank];
                 } else {
                     // the previous block along P1 and/or P2 owns this line
-                    int64_t ob[3] = {bc[0], bc[1], bc[2]};
                     const bool s1 = e1 < k1, s2 = e2 < k2;
-                    if (s1) ob[P1] -= 1;
-                    if (s2) ob[P2] -= 1;
+                    const int64_t ob0 = bc[0] - ((s1 && P1 == 0) || (s2 && P2 == 0));
+                    const int64_t ob1 = bc[1] - ((s1 && P1 == 1) || (s2 && P2 == 1));
+                    const int64_t ob2 = bc[2] - ((s1 && P1 == 2) || (s2 && P2 == 2));
                     const int nf = (int)(a.bs / a.s) + 1;
                     const int on2 = s2 ? nf : n2;
-                    const int ok1 = ob[P1] != 0, ok2 = ob[P2] != 0;
+                    const int ok1 = pick3(P1, ob0, ob1, ob2) != 0, ok2 = pick3(P2, ob0, ob1, ob2) != 0;
                     const int oe1 = s1 ? (nf - 1) / 2 : e1;
                     const int oe2 = s2 ? (nf - 1) / 2 : e2;
                     const int one2 = (on2 + 1) / 2 - ok2;
-                    const int64_t oid = (ob[0] * a.nb[1] + ob[1]) * a.nb[2] + ob[2];
+                    const int64_t oid = (ob0 * a.nb[1] + ob1) * a.nb[2] + ob2;
                     pos = a.block_off[oid] + (uint64_t)((oe1 - ok1) * one2 + (oe2 - ok2)) * g.t0 + rk;
                     if (pos >= a.ncodes) {
                         atomicExch(a.err, 1);
@@ -417,14 +420,13 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
                     code = stg[rank];
                 } else {
                     // the previous block along P2 owns this line
-                    int64_t ob[3] = {bc[0], bc[1], bc[2]};
-                    ob[P2] -= 1;
+                    const int64_t ob0 = bc[0] - (P2 == 0), ob1 = bc[1] - (P2 == 1), ob2 = bc[2] - (P2 == 2);
                     const int nf = (int)(a.bs / a.s) + 1;
-                    const int ok2 = ob[P2] != 0;
+                    const int ok2 = pick3(P2, ob0, ob1, ob2) != 0;
                     const int oe2 = (nf - 1) / 2;
                     const int one2 = (nf + 1) / 2 - ok2;
                     const int64_t oc1 = (int64_t)g.ne1 * one2 * g.t0;
-                    const int64_t oid = (ob[0] * a.nb[1] + ob[1]) * a.nb[2] + ob[2];
+                    const int64_t oid = (ob0 * a.nb[1] + ob1) * a.nb[2] + ob2;
                     pos = a.block_off[oid] + oc1 + (uint64_t)(q * one2 + (oe2 - ok2)) * g.t1 + rk;
                     if (pos >= a.ncodes) {
                         atomicExch(a.err, 1);
@@ -444,7 +446,8 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
         }
     }
 
-    // sweep 3: lines along P2 at (m0, m1), emitted lines only
+    // sweep 3: lines along P2 at (m0, m1), emitted lines only.  Compression
+    // reads the targets from global memory; the loads run three lines ahead.
     if (g.t2 > 0) {
         const int64_t cnt = g.c3;
         const uint64_t sbase = base + g.c1 + g.c2;
@@ -458,28 +461,43 @@ __global__ void __launch_bounds__(512) k_interp_level(LevelArgs a, const T *__re
         const int m2 = 2 * t + 1;
         Stencil<T> S = make_stencil<T>(act ? m2 : 1, n2, cubic, 1, 1);
         const int rk = act ? line_rank(m2, n2, cubic) : 0;
-        const int64_t gl = (int64_t)m2 * G2;
-        int q0 = hw / w1, q1 = hw - q0 * w1;
-        for (int l = hw; l < lines; l += nhw, q1 += nhw) {
-            while (q1 >= w1) {
-                q1 -= w1;
-                q0++;
-            }
+        const int64_t gl = gbase + (int64_t)m2 * G2 + (int64_t)k0 * G0 + (int64_t)k1 * G1;
+        int q0 = hw / w1, q1 = hw - q0 * w1;  // line being computed
+        int p0 = q0, p1 = q1;                 // line being loaded
+        T xa = 0, xb = 0, xc = 0;
+        int lp = hw;
+        if (!DECOMP && act) {
+            if (lp < lines) xa = X[gl + p0 * G0 + p1 * G1];
+            lp += nhw; p1 += nhw;
+            while (p1 >= w1) { p1 -= w1; p0++; }
+            if (lp < lines) xb = X[gl + p0 * G0 + p1 * G1];
+            lp += nhw; p1 += nhw;
+            while (p1 >= w1) { p1 -= w1; p0++; }
+        }
+        for (int l = hw; l < lines; l += nhw) {
             if (!act) continue;
-            const int m0 = k0 + q0, m1 = k1 + q1;
-            const T *row = V + (m0 * n1 + m1) * h2;
+            if (!DECOMP) {
+                xc = lp < lines ? X[gl + p0 * G0 + p1 * G1] : (T)0;
+                lp += nhw; p1 += nhw;
+                while (p1 >= w1) { p1 -= w1; p0++; }
+            }
+            const T *row = V + ((k0 + q0) * n1 + (k1 + q1)) * h2;
             const T pred = eval_stencil(S, row);
             const int rank = l * g.t2 + rk;
-            const int64_t gi = gbase + m0 * G0 + m1 * G1 + gl;
+            const int64_t gi = gl + q0 * G0 + q1 * G1;
             if (!DECOMP) {
-                T v = X[gi], uv;
+                T v = xa, uv;
                 int code = quantize_any(v, pred, a, uv);
                 stg[rank] = (uint16_t)code;
                 if (code == 0) scratch[sbase + rank] = uv;
                 if (a.write_back) W[gi] = v;
+                xa = xb;
+                xb = xc;
             } else {
                 W[gi] = recover_any(pred, (int)stg[rank], sbase + rank, a, zpos, nz, unpred);
             }
+            q1 += nhw;
+            while (q1 >= w1) { q1 -= w1; q0++; }
         }
         __syncthreads();
         if (!DECOMP) {
