@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
 
     // sweep 2: lines along P1 at (m0 any, m2 even); the m0 = 0 plane of a
     // non-first block is not needed by sweep 3 and is skipped.
-    if (g.t1 > 0) {
+    if (g.t1 > 0 && n0 - k0 > 0) {
         const int64_t cnt = g.c2;
         const uint64_t sbase = base + g.c1;
         if (DECOMP) {
@@ -448,7 +448,9 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
 
     // sweep 3: lines along P2 at (m0, m1), emitted lines only.  Compression
     // reads the targets from global memory; the loads run three lines ahead.
-    if (g.t2 > 0) {
+    // A block that begins on the last element of an axis has no sweep-3
+    // lines (n - k = 0); the carried line counters below divide by n1 - k1.
+    if (g.t2 > 0 && n0 - k0 > 0 && n1 - k1 > 0) {
         const int64_t cnt = g.c3;
         const uint64_t sbase = base + g.c1 + g.c2;
         if (DECOMP) {

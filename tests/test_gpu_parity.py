@@ -89,6 +89,15 @@ RANDOM_CASES = [
     ((64, 64, 64), dict(rel=1e-3, maxStep=32, alpha=1.25, beta=2.0), np.float32, -3.0),
     ((70, 80, 90), dict(rel=1e-3, interpAlgo_list=[1, 0, 1, 1], interpDirection_list=[0, 5, 3, 1],
                         alpha=1.0, beta=1.5), np.float32, -3.0),
+    # blocks that begin on the last element of an axis (dim - 1 a multiple of
+    # the block edge), extents 1 and 2, every direction
+    ((33, 65, 17), dict(rel=1e-3, direction=4), np.float32, -3.0),
+    ((1, 33, 65), dict(rel=1e-3, direction=3), np.float32, -3.0),
+    ((2, 33, 3), dict(rel=1e-3), np.float32, -3.0),
+    ((129, 2, 33), dict(rel=1e-3, direction=5), np.float32, -3.0),
+    ((65, 65, 65), dict(rel=1e-3, interp=F.INTERP_ALGO_LINEAR, direction=1), np.float64, -3.0),
+    ((33,), dict(rel=1e-3), np.float32, -3.0),
+    ((65, 1), dict(rel=1e-3, direction=1), np.float32, -3.0),
 ]
 
 
