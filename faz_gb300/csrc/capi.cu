@@ -215,6 +215,10 @@ void set_fast_path(LevelArgs &a) {
     if ((double)lo > a.eb) lo = std::nextafter(lo, 0.0f);
     a.eblo = lo;
     a.twor_f = (float)(2 * a.radius);
+    // d < eb * (1 - 2^-20) gives d * (1/eb) < 1 - 2^-20 + 2^-52, so floor(x) = 0
+    a.eb_half0 = (float)(a.eb * (1.0 - 0x1p-20));
+    if ((double)a.eb_half0 > a.eb * (1.0 - 0x1p-20)) a.eb_half0 = std::nextafter(a.eb_half0, 0.0f);
+    if (a.radius == 1) a.eb_half0 = 0.0f;  // code 1 may be unpredictable under trimToZero 2
     a.fast = 1;
 }
 

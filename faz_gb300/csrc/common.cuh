@@ -41,6 +41,7 @@ struct LevelArgs {
     int *err;            // set to 1 by a kernel that met an out-of-range position
     // float fast path: eb and 1/eb split into float pairs, largest float <= eb
     float eh, el, rh, rl, eblo, twor_f;
+    float eb_half0;      // |diff| below this float gives half index 0 for sure
     int fast;            // 1: float data uses the exact float fast path
     unsigned long long *verify;  // non-null: count fast/double disagreements here
 };

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cfloat>
+#include <type_traits>
 #include "common.cuh"
 #include "fastq.cuh"
 #include "internal.h"
@@ -107,6 +108,13 @@ __device__ __forceinline__ int quantize_fast(float &v, float pred, const LevelAr
         return a.trim - 1;
     }
     float diff = orig - pred;
+    // |diff| clearly below eb: floor(x) = 0, half = 0, code = radius, and the
+    // reconstruction pred + 0*eb is pred + 0.0f; |pred - orig| = |diff| <= eb.
+    if (fabsf(diff) < a.eb_half0) {
+        uval = orig;
+        v = pred + 0.0f;
+        return a.radius;
+    }
     int twor = 2 * a.radius;
     int half = half_index_f32(fabsf(diff), a.rh, a.rl, a.twor_f, twor);
     if (half == -1) return quantize_dp_f32(v, pred, a.eb, a.recip, a.radius, a.trim, uval);
@@ -186,6 +194,19 @@ __device__ __forceinline__ T recover_any(T pred, int code, uint64_t pos, const L
     else return recover<T>(pred, code, pos, a.eb, a.radius, a.trim, zpos, nz, unpred);
 }
 
+// ------------------------------------------------------- async copies
+// Element copies global -> shared that complete asynchronously (cp.async),
+// so that a CTA has its whole lattice load in flight at once.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (BYTES == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // --------------------------------------------------------- level kernel
 // Stencil of one target, set up once per lane and sweep: the values it reads
 // (shared-memory offsets from the line origin) and the coefficients of the
@@ -253,11 +274,14 @@ __device__ __forceinline__ T eval_stencil(const Stencil<T> &S, const T *p) {
 // half-warp owns target 2t+1 of the line.  Shared-memory strides along every
 // sweep axis are odd multiples of the lane step, so the half-warps read
 // distinct banks.
-template <typename T, bool DECOMP>
+// WIDE selects 64-bit element offsets; fields below 2^31 elements use 32-bit
+// offsets from the block's first element.
+template <typename T, bool DECOMP, bool WIDE>
 __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
                                                       uint16_t *__restrict__ codes, T *__restrict__ scratch,
                                                       const uint64_t *__restrict__ zpos, uint64_t nz,
                                                       const T *__restrict__ unpred) {
+    using Off = typename std::conditional<WIDE, int64_t, int32_t>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *V = reinterpret_cast<T *>(smem_raw);
     uint16_t *stg = reinterpret_cast<uint16_t *>(smem_raw + (((size_t)a.vwords * sizeof(T) + 15) & ~(size_t)15));
@@ -269,10 +293,14 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     const int P0 = a.perm[0], P1 = a.perm[1], P2 = a.perm[2];
     const int n0 = g.n0, n1 = g.n1, n2 = g.n2, h2 = g.h2;
     const int k0 = g.k0, k1 = g.k1, k2 = g.k2;
-    const int64_t G0 = a.s * pick3(P0, a.offs[0], a.offs[1], a.offs[2]);
-    const int64_t G1 = a.s * pick3(P1, a.offs[0], a.offs[1], a.offs[2]);
-    const int64_t G2 = a.s * pick3(P2, a.offs[0], a.offs[1], a.offs[2]);
-    const int64_t gbase = g.beg[0] * a.offs[0] + g.beg[1] * a.offs[1] + g.beg[2] * a.offs[2];
+    const Off G0 = (Off)(a.s * pick3(P0, a.offs[0], a.offs[1], a.offs[2]));
+    const Off G1 = (Off)(a.s * pick3(P1, a.offs[0], a.offs[1], a.offs[2]));
+    const Off G2 = (Off)(a.s * pick3(P2, a.offs[0], a.offs[1], a.offs[2]));
+    {
+        const int64_t gbase = g.beg[0] * a.offs[0] + g.beg[1] * a.offs[1] + g.beg[2] * a.offs[2];
+        X += DECOMP ? 0 : gbase;
+        W += gbase;
+    }
     const uint64_t base = a.block_off[bid];
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
@@ -283,7 +311,6 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     {
         const int rows = n0 * n1;
         int m0 = warp / n1, m1 = warp - m0 * n1;
-#pragma unroll 4
         for (int r = warp; r < rows; r += nwarps, m1 += nwarps) {
             while (m1 >= n1) {
                 m1 -= n1;
@@ -292,10 +319,11 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
             const bool coarse = !(m0 & 1) && !(m1 & 1);
             if (DECOMP && !coarse) continue;
             const T *src = coarse ? W : X;
-            const int64_t rb = gbase + m0 * G0 + m1 * G1;
+            const Off rb = m0 * G0 + m1 * G1;
             T *dst = V + r * h2;
-            for (int e = lane; e < h2; e += 32) dst[e] = src[rb + (int64_t)(2 * e) * G2];
+            for (int e = lane; e < h2; e += 32) cp_async<sizeof(T)>(dst + e, src + rb + (Off)(2 * e) * G2);
         }
+        cp_async_wait_all();
     }
     __syncthreads();
 
@@ -313,7 +341,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
         const int m0 = 2 * t + 1;
         Stencil<T> S = make_stencil<T>(act ? m0 : 1, n0, cubic, st, 0);
         const int rk = act ? line_rank(m0, n0, cubic) : 0;
-        const int64_t gl = (int64_t)m0 * G0;
+        const Off gl = (Off)m0 * G0;
         int e1 = hw / h2, e2 = hw - e1 * h2;
         for (int l = hw; l < lines; l += nhw, e2 += nhw) {
             while (e2 >= h2) {
@@ -326,7 +354,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
             const int rank = ((e1 - k1) * g.ne2 + (e2 - k2)) * g.t0 + rk;
             const T pred = eval_stencil(S, V + col);
             const int idx = m0 * st + col;
-            const int64_t gi = gbase + gl + (2 * e1) * G1 + (int64_t)(2 * e2) * G2;
+            const Off gi = gl + (Off)(2 * e1) * G1 + (Off)(2 * e2) * G2;
             if (!DECOMP) {
                 T v = V[idx], uv;
                 int code = quantize_any(v, pred, a, uv);
@@ -388,7 +416,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
         const int m1 = 2 * t + 1;
         Stencil<T> S = make_stencil<T>(act ? m1 : 1, n1, cubic, h2, 0);
         const int rk = act ? line_rank(m1, n1, cubic) : 0;
-        const int64_t gl = (int64_t)m1 * G1;
+        const Off gl = (Off)m1 * G1;
         int q = hw / h2, e2 = hw - q * h2;
         for (int l = hw; l < lines; l += nhw, e2 += nhw) {
             while (e2 >= h2) {
@@ -402,7 +430,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
             const int rank = (q * g.ne2 + (e2 - k2)) * g.t1 + rk;
             const T pred = eval_stencil(S, V + col);
             const int idx = col + m1 * h2;
-            const int64_t gi = gbase + m0 * G0 + gl + (int64_t)(2 * e2) * G2;
+            const Off gi = (Off)m0 * G0 + gl + (Off)(2 * e2) * G2;
             if (!DECOMP) {
                 T v = V[idx], uv;
                 int code = quantize_any(v, pred, a, uv);
@@ -463,30 +491,30 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
         const int m2 = 2 * t + 1;
         Stencil<T> S = make_stencil<T>(act ? m2 : 1, n2, cubic, 1, 1);
         const int rk = act ? line_rank(m2, n2, cubic) : 0;
-        const int64_t gl = gbase + (int64_t)m2 * G2 + (int64_t)k0 * G0 + (int64_t)k1 * G1;
+        const Off gl = (Off)m2 * G2 + (Off)k0 * G0 + (Off)k1 * G1;
         int q0 = hw / w1, q1 = hw - q0 * w1;  // line being computed
         int p0 = q0, p1 = q1;                 // line being loaded
         T xa = 0, xb = 0, xc = 0;
         int lp = hw;
         if (!DECOMP && act) {
-            if (lp < lines) xa = X[gl + p0 * G0 + p1 * G1];
+            if (lp < lines) xa = X[gl + (Off)p0 * G0 + (Off)p1 * G1];
             lp += nhw; p1 += nhw;
             while (p1 >= w1) { p1 -= w1; p0++; }
-            if (lp < lines) xb = X[gl + p0 * G0 + p1 * G1];
+            if (lp < lines) xb = X[gl + (Off)p0 * G0 + (Off)p1 * G1];
             lp += nhw; p1 += nhw;
             while (p1 >= w1) { p1 -= w1; p0++; }
         }
         for (int l = hw; l < lines; l += nhw) {
             if (!act) continue;
             if (!DECOMP) {
-                xc = lp < lines ? X[gl + p0 * G0 + p1 * G1] : (T)0;
+                xc = lp < lines ? X[gl + (Off)p0 * G0 + (Off)p1 * G1] : (T)0;
                 lp += nhw; p1 += nhw;
                 while (p1 >= w1) { p1 -= w1; p0++; }
             }
             const T *row = V + ((k0 + q0) * n1 + (k1 + q1)) * h2;
             const T pred = eval_stencil(S, row);
             const int rank = l * g.t2 + rk;
-            const int64_t gi = gl + q0 * G0 + q1 * G1;
+            const Off gi = gl + (Off)q0 * G0 + (Off)q1 * G1;
             if (!DECOMP) {
                 T v = xa, uv;
                 int code = quantize_any(v, pred, a, uv);
@@ -627,17 +655,13 @@ cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const
     // half-warps take lines: enough threads for the lines of a block
     int64_t vol = (int64_t)a.vwords * 2;
     int threads = vol >= 8192 ? 512 : (vol >= 1024 ? 256 : (vol >= 256 ? 128 : 64));
-    if (!decomp) {
-        auto k = k_interp_level<T, false>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        k<<<(unsigned)nblocks, threads, sm, st>>>(a, X, W, codes, scratch, zpos, nz, unpred);
-    } else {
-        auto k = k_interp_level<T, true>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        k<<<(unsigned)nblocks, threads, sm, st>>>(a, X, W, codes, scratch, zpos, nz, unpred);
-    }
+    const bool wide = a.dims[0] * a.dims[1] * a.dims[2] >= ((int64_t)1 << 31);
+    void (*k)(LevelArgs, const T *, T *, uint16_t *, T *, const uint64_t *, uint64_t, const T *);
+    if (!decomp) k = wide ? k_interp_level<T, false, true> : k_interp_level<T, false, false>;
+    else k = wide ? k_interp_level<T, true, true> : k_interp_level<T, true, false>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)nblocks, threads, sm, st>>>(a, X, W, codes, scratch, zpos, nz, unpred);
     return cudaGetLastError();
 }
 
