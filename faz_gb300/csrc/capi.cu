@@ -309,7 +309,7 @@ Plan make_plan(int N, const uint64_t *dims, uint64_t maxStep, int blocksize, int
         int64_t stage = std::max({((m1 + 1) / 2) * ((m2 + 1) / 2) * (m0 / 2), m0 * ((m2 + 1) / 2) * (m1 / 2),
                                   m0 * m1 * (m2 / 2)});
         a.vwords = (int)vw;
-        a.stage_cap = (int)std::max<int64_t>(stage, 1);
+        a.stage_cap = (int)std::max<int64_t>(stage, 1) + 16;  // + alignment shift
         size_t sm = level_smem_bytes<T>(a);
         if (sm > smem_limit)
             throw Fail{FAZ_ERR_UNSUPPORTED, "interpolation block does not fit in shared memory (block size too large)"};

@@ -42,16 +42,37 @@ __global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__
     if (s1 > n) s1 = n;
     const int lo = center - HWIN / 2;
     unsigned int zc = 0;
-    for (uint64_t i = s0 + lane; i < s1; i += 32) {
-        int v = codes[i];
+    // lanes take 8 consecutive codes (one 16-byte load); equal codes within a
+    // step are counted with one atomic (__match_any_sync groups the lanes)
+    auto count = [&](int v, uint64_t i) {
         if (v == 0) zc++;
         int b = v - lo;
-        if (b >= 0 && b < HWIN) {
-            atomicAdd(&scnt[b], 1u);
-            atomicMin(&sfirst[b], (unsigned int)(i - c0));
-        } else {
-            atomicAdd(&hist[v], 1ull);
-            atomicMin(&first[v], (unsigned long long)i);
+        unsigned int peers = __match_any_sync(__activemask(), v);
+        int leader = __ffs(peers) - 1;
+        if (lane == leader) {
+            // the leader holds the smallest position of its group in this step
+            if (b >= 0 && b < HWIN) {
+                atomicAdd(&scnt[b], (unsigned int)__popc(peers));
+                if ((unsigned int)(i - c0) < sfirst[b]) atomicMin(&sfirst[b], (unsigned int)(i - c0));
+            } else {
+                atomicAdd(&hist[v], (unsigned long long)__popc(peers));
+                atomicMin(&first[v], (unsigned long long)i);
+            }
+        }
+    };
+    if (s1 - s0 == HSUB) {
+        const uint4 *cv = reinterpret_cast<const uint4 *>(codes + s0);
+        for (int it = 0; it < (int)(HSUB / 256); it++) {
+            uint4 q = cv[it * 32 + lane];
+            const uint16_t *e = reinterpret_cast<const uint16_t *>(&q);
+            const uint64_t i0 = s0 + (uint64_t)(it * 32 + lane) * 8;
+#pragma unroll
+            for (int k = 0; k < 8; k++) count(e[k], i0 + k);
+        }
+    } else {
+        for (uint64_t b0 = s0; b0 < s1; b0 += 32) {
+            uint64_t i = b0 + lane;
+            if (i < s1) count(codes[i], i);
         }
     }
     for (int o = 16; o > 0; o >>= 1) zc += __shfl_down_sync(0xffffffffu, zc, o);
@@ -225,7 +246,7 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
                                                             const unsigned long long *__restrict__ chunkoff,
                                                             uint32_t *out, int smem_words) {
     extern __shared__ uint32_t sw[];
-    __shared__ unsigned long long tsum[ENC_THREADS];
+    __shared__ unsigned long long wtot[ENC_THREADS / 32];
     const uint64_t c0 = (uint64_t)blockIdx.x * ENC_CHUNK;
     const uint64_t gbit = chunkoff[blockIdx.x];
     const uint64_t gend = chunkoff[blockIdx.x + 1];
@@ -235,14 +256,14 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
     const int nwords = (int)(wl - w0 + 1);
     for (int i = threadIdx.x; i < nwords && i < smem_words; i += blockDim.x) sw[i] = 0;
     uint16_t sym[ENC_PER_THREAD];
-    unsigned long long mybits = 0;
+    unsigned int mybits = 0;
     const uint64_t t0 = c0 + (uint64_t)threadIdx.x * ENC_PER_THREAD;
     if (t0 + ENC_PER_THREAD <= n) {
         // 16 codes = two 16-byte loads (codes is 256-byte aligned, t0 a multiple of 16)
         const uint4 *cv = reinterpret_cast<const uint4 *>(codes + t0);
-        uint4 a = cv[0], b = cv[1];
-        const uint16_t *pa = reinterpret_cast<const uint16_t *>(&a);
-        const uint16_t *pb = reinterpret_cast<const uint16_t *>(&b);
+        uint4 qa = cv[0], qb = cv[1];
+        const uint16_t *pa = reinterpret_cast<const uint16_t *>(&qa);
+        const uint16_t *pb = reinterpret_cast<const uint16_t *>(&qb);
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             sym[k] = (uint16_t)(pa[k] - offset);
@@ -257,33 +278,54 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
             if (i < n) mybits += len[sym[k]];
         }
     }
-    tsum[threadIdx.x] = mybits;
-    __syncthreads();
-    for (int o = 1; o < ENC_THREADS; o <<= 1) {
-        unsigned long long v = threadIdx.x >= (unsigned)o ? tsum[threadIdx.x - o] : 0;
-        __syncthreads();
-        tsum[threadIdx.x] += v;
-        __syncthreads();
+    // exclusive scan of the threads' bit counts (warp shuffles + warp totals)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned long long x = mybits;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    uint64_t pos = (gbit & 31) + (tsum[threadIdx.x] - mybits);  // bit position relative to word w0
+    if (lane == 31) wtot[wid] = x;
+    __syncthreads();
+    unsigned long long wbase = 0;
+    for (int w = 0; w < wid; w++) wbase += wtot[w];
+    // bit position relative to word w0
+    uint64_t pos = (gbit & 31) + wbase + x - mybits;
+    // accumulate the thread's bits MSB-first; whole words it owns are stored,
+    // its first and last (possibly shared) words are ORed
+    uint32_t wi = (uint32_t)(pos >> 5);
+    int fill = (int)(pos & 31);        // bits already in the current word (owned by others)
+    unsigned long long acc = 0;        // pending bits, MSB-aligned
+    int nacc = fill;                   // bits in acc including the leading fill
+    bool first_word = true;
     for (int k = 0; k < ENC_PER_THREAD; k++) {
         if (sym[k] == 0xffff) break;
         int l = len[sym[k]];
         if (l == 0) continue;
         unsigned long long c = code64[sym[k]];
-        int wi = (int)(pos >> 5), b = (int)(pos & 31);
-        uint32_t p0 = (uint32_t)(c >> (32 + b));
-        if (p0) atomicOr(&sw[wi], p0);
-        if (l + b > 32) {
-            uint32_t p1 = (uint32_t)((c << (32 - b)) >> 32);
-            if (b == 0) p1 = (uint32_t)c;
-            if (p1) atomicOr(&sw[wi + 1], p1);
+        // append l bits of c (MSB-aligned) at position nacc of acc
+        int take = l;
+        while (take > 0) {
+            int room = 64 - nacc;
+            int t = take < room ? take : room;
+            acc |= (c >> nacc);
+            c = t < 64 ? c << t : 0ull;
+            nacc += t;
+            take -= t;
+            while (nacc >= 32) {
+                uint32_t word = (uint32_t)(acc >> 32);
+                if (first_word && fill) atomicOr(&sw[wi], word);
+                else sw[wi] = word;
+                first_word = false;
+                wi++;
+                acc <<= 32;
+                nacc -= 32;
+            }
         }
-        if (l + b > 64) {
-            uint32_t p2 = (uint32_t)(c << (32 - b));
-            if (p2) atomicOr(&sw[wi + 2], p2);
-        }
-        pos += l;
+    }
+    if (nacc > 0) {
+        uint32_t word = (uint32_t)(acc >> 32);
+        if (word) atomicOr(&sw[wi], word);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nwords; i += blockDim.x) {

@@ -207,6 +207,27 @@ __device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Move cnt codes between global codes[0..cnt) and shared stg[sh..sh+cnt),
+// where sh = (global position & 7): the body moves 8 codes per 16-byte
+// access on both sides.
+template <bool TO_GLOBAL>
+__device__ __forceinline__ void move_codes(uint16_t *g, uint16_t *stg, int64_t cnt, int sh) {
+    const int64_t a0 = (8 - sh) & 7;
+    const int64_t nbody = cnt > a0 ? (cnt - a0) >> 3 : 0;
+    const int64_t tail0 = a0 + (nbody << 3);
+    for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+        if (i < a0 || i >= tail0) {
+            if (TO_GLOBAL) g[i] = stg[sh + i];
+            else stg[sh + i] = g[i];
+        }
+    }
+    for (int64_t j = threadIdx.x; j < nbody; j += blockDim.x) {
+        const int64_t i = a0 + (j << 3);
+        if (TO_GLOBAL) *reinterpret_cast<uint4 *>(g + i) = *reinterpret_cast<const uint4 *>(stg + sh + i);
+        else *reinterpret_cast<uint4 *>(stg + sh + i) = *reinterpret_cast<const uint4 *>(g + i);
+    }
+}
+
 // --------------------------------------------------------- level kernel
 // Stencil of one target, set up once per lane and sweep: the values it reads
 // (shared-memory offsets from the line origin) and the coefficients of the
@@ -330,8 +351,10 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     // sweep 1: lines along P0 at even (m1, m2), first planes included
     if (g.t0 > 0) {
         const int64_t cnt = g.c1;
+        const int sh = (int)(base & 7);
+        uint16_t *sg = stg + sh;
         if (DECOMP) {
-            for (int64_t i = tid; i < cnt; i += nt) stg[i] = codes[base + i];
+            move_codes<false>(codes + base, stg, cnt, sh);
             __syncthreads();
         }
         const int st = n1 * h2;
@@ -360,7 +383,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
                 int code = quantize_any(v, pred, a, uv);
                 V[idx] = v;
                 if (emit) {
-                    stg[rank] = (uint16_t)code;
+                    sg[rank] = (uint16_t)code;
                     if (code == 0) scratch[base + rank] = uv;
                     if (a.write_back) W[gi] = v;
                 }
@@ -369,7 +392,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
                 int code;
                 if (emit) {
                     pos = base + rank;
-                    code = stg[rank];
+                    code = sg[rank];
                 } else {
                     // the previous block along P1 and/or P2 owns this line
                     const bool s1 = e1 < k1, s2 = e2 < k2;
@@ -397,7 +420,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
         }
         __syncthreads();
         if (!DECOMP) {
-            for (int64_t i = tid; i < cnt; i += nt) codes[base + i] = stg[i];
+            move_codes<true>(codes + base, stg, cnt, sh);
             __syncthreads();
         }
     }
@@ -407,8 +430,10 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     if (g.t1 > 0 && n0 - k0 > 0) {
         const int64_t cnt = g.c2;
         const uint64_t sbase = base + g.c1;
+        const int sh = (int)(sbase & 7);
+        uint16_t *sg = stg + sh;
         if (DECOMP) {
-            for (int64_t i = tid; i < cnt; i += nt) stg[i] = codes[sbase + i];
+            move_codes<false>(codes + sbase, stg, cnt, sh);
             __syncthreads();
         }
         const int lines = (n0 - k0) * h2;
@@ -436,7 +461,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
                 int code = quantize_any(v, pred, a, uv);
                 V[idx] = v;
                 if (emit) {
-                    stg[rank] = (uint16_t)code;
+                    sg[rank] = (uint16_t)code;
                     if (code == 0) scratch[sbase + rank] = uv;
                     if (a.write_back) W[gi] = v;
                 }
@@ -445,7 +470,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
                 int code;
                 if (emit) {
                     pos = sbase + rank;
-                    code = stg[rank];
+                    code = sg[rank];
                 } else {
                     // the previous block along P2 owns this line
                     const int64_t ob0 = bc[0] - (P2 == 0), ob1 = bc[1] - (P2 == 1), ob2 = bc[2] - (P2 == 2);
@@ -469,7 +494,7 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
         }
         __syncthreads();
         if (!DECOMP) {
-            for (int64_t i = tid; i < cnt; i += nt) codes[sbase + i] = stg[i];
+            move_codes<true>(codes + sbase, stg, cnt, sh);
             __syncthreads();
         }
     }
@@ -481,8 +506,10 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     if (g.t2 > 0 && n0 - k0 > 0 && n1 - k1 > 0) {
         const int64_t cnt = g.c3;
         const uint64_t sbase = base + g.c1 + g.c2;
+        const int sh = (int)(sbase & 7);
+        uint16_t *sg = stg + sh;
         if (DECOMP) {
-            for (int64_t i = tid; i < cnt; i += nt) stg[i] = codes[sbase + i];
+            move_codes<false>(codes + sbase, stg, cnt, sh);
             __syncthreads();
         }
         const int w1 = n1 - k1;
@@ -518,21 +545,19 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
             if (!DECOMP) {
                 T v = xa, uv;
                 int code = quantize_any(v, pred, a, uv);
-                stg[rank] = (uint16_t)code;
+                sg[rank] = (uint16_t)code;
                 if (code == 0) scratch[sbase + rank] = uv;
                 if (a.write_back) W[gi] = v;
                 xa = xb;
                 xb = xc;
             } else {
-                W[gi] = recover_any(pred, (int)stg[rank], sbase + rank, a, zpos, nz, unpred);
+                W[gi] = recover_any(pred, (int)sg[rank], sbase + rank, a, zpos, nz, unpred);
             }
             q1 += nhw;
             while (q1 >= w1) { q1 -= w1; q0++; }
         }
         __syncthreads();
-        if (!DECOMP) {
-            for (int64_t i = tid; i < cnt; i += nt) codes[sbase + i] = stg[i];
-        }
+        if (!DECOMP) move_codes<true>(codes + sbase, stg, cnt, sh);
     }
 }
 
