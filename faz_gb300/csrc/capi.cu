@@ -520,8 +520,15 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     if (nunpred) launches(launch_compact_zeros<T>(codes, n, zc, zoff, nullptr, scratch, unpred, st));
     // Huffman encode
     unsigned long long *dcode = m.alloc<unsigned long long>(cb.stateNum);
+    unsigned long long *dpacked = m.alloc<unsigned long long>(cb.stateNum);
     uint8_t *dlen = m.alloc<uint8_t>(cb.stateNum);
+    std::vector<unsigned long long> packed(cb.stateNum);
+    for (int i = 0; i < cb.stateNum; i++) {
+        const int l = cb.len[i];
+        packed[i] = ((unsigned long long)l << 32) | (l >= 1 && l <= 32 ? (cb.code[i] >> (64 - l)) : 0ull);
+    }
     CK(cudaMemcpyAsync(dcode, cb.code.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dpacked, packed.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dlen, cb.len.data(), cb.stateNum, cudaMemcpyHostToDevice, st));
     const uint64_t nech = encode_chunks(n);
     unsigned long long *cbits = m.alloc<unsigned long long>(nech + 1);
@@ -536,7 +543,8 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     const uint64_t nwords = (total_bits + 31) / 32 + 1;
     uint32_t *bits = m.alloc<uint32_t>(nwords);
     CK(cudaMemsetAsync(bits, 0, nwords * 4, st));
-    if (total_bits) launches(launch_encode_pack(codes, n, cb.offset, dcode, dlen, coff, bits, std::max(cb.maxlen, 1), st));
+    if (total_bits)
+        launches(launch_encode_pack(codes, n, cb.offset, dcode, dpacked, dlen, coff, bits, std::max(cb.maxlen, 1), st));
     CK(cudaEventRecord(ev_huff.b, st));
     // payload layout (SZInterpolationCompressor.hpp:485-512, IntegerQuantizer.hpp:185-201,
     // HuffmanEncoder.hpp:119-137 and 150-227)

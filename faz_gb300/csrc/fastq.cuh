@@ -115,4 +115,63 @@ FAZ_HD bool dequant_f32(float pred, int q2, float eh, float el, float &out) {
     return true;
 }
 
+// Straight-line form of the float quantiser for trimToZero = 0 (the
+// reference's quantize_and_overwrite, IntegerQuantizer.hpp:69-108, with the
+// double steps replaced by half_index_f32 / dequant_f32 above).  Returns the
+// code and the value the field takes (reconstruction, or orig when the code
+// is 0).  `undecided` is set when the float proofs do not settle the result;
+// the caller then runs the double computation.
+FAZ_HD int quantize_f32_straight(float orig, float pred, float rh, float rl, float eh, float el, float eblo,
+                                 float twor_f, int radius, float &out, bool &undecided) {
+    const float diff = orig - pred;
+    const float d = fabsf(diff);
+    const float ph = d * rh;
+    const bool nan_in = ph != ph;
+    const bool big = !(ph < twor_f) && !nan_in;
+    const float phc = (ph < twor_f) ? ph : 0.0f;
+    const float pl = fmaf(d, rh, -ph);
+    const float c = (ph < twor_f) ? fmaf(d, rl, pl) : 0.0f;
+    int32_t ki = rint_small(phc);
+    float kf = int_to_float_small(ki);
+    const bool over = kf > phc;
+    ki -= over ? 1 : 0;
+    kf -= over ? 1.0f : 0.0f;
+    const float f = (phc - kf) + c;
+    const int32_t ri = rint_small(f);
+    const float fr = f - int_to_float_small(ri);
+    const bool near = !(fabsf(fr) > 0x1p-20f);
+    const int32_t B = ki + ri;
+    const int32_t fl = near ? B : B - (fr < 0.0f ? 1 : 0);
+    const int twor = 2 * radius;
+    const int qi = fl + 1;
+    const bool unpred_q = big || qi >= twor;
+    const int half = qi >> 1;
+    const bool neg = diff < 0;
+    const int q2 = unpred_q ? 0 : (neg ? -(half << 1) : (half << 1));
+    const int code = neg ? radius - half : radius + half;
+    // reconstruction (dequant_f32 without branches)
+    const float q = int_to_float_small(q2);
+    const float p1 = q * eh;
+    const float e1 = fmaf(q, eh, -p1);
+    const float p2 = q * el;
+    const float s = pred + p1;
+    const float bb = s - pred;
+    const float t = (pred - (s - bb)) + (p1 - bb);
+    const float lo = t + (e1 + p2);
+    const float r = s + lo;
+    const float res = (s - r) + lo;
+    const float ar = fabsf(r);
+    const uint32_t rb = f32_bits(ar);
+    const float bigv = fmaxf(fabsf(pred), fabsf(p1));
+    const float u = f32_from_bits(rb & 0x7f800000u) * 0x1p-23f;
+    const bool und_d = q2 != 0 && (!(ar >= 0x1p-100f) || ar * 256.0f < bigv || (rb & 0x7fffffu) == 0 ||
+                                   rb >= 0x7f000000u || fabsf(fabsf(res) - 0.5f * u) < u * 0x1p-12f);
+    const float dec = q2 == 0 ? pred + 0.0f : r;
+    const float err = dec - orig;
+    const bool unpred = unpred_q || fabsf(err) > eblo;
+    undecided = nan_in || (near && (B & 1)) || (!unpred_q && und_d);
+    out = unpred ? orig : dec;
+    return unpred ? 0 : code;
+}
+
 }  // namespace faz

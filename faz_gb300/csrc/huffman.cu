@@ -42,22 +42,18 @@ __global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__
     if (s1 > n) s1 = n;
     const int lo = center - HWIN / 2;
     unsigned int zc = 0;
-    // lanes take 8 consecutive codes (one 16-byte load); equal codes within a
-    // step are counted with one atomic (__match_any_sync groups the lanes)
+    // lanes take 8 consecutive codes (one 16-byte load); the first-position
+    // atomic runs only when the position beats the recorded one
     auto count = [&](int v, uint64_t i) {
         if (v == 0) zc++;
         int b = v - lo;
-        unsigned int peers = __match_any_sync(__activemask(), v);
-        int leader = __ffs(peers) - 1;
-        if (lane == leader) {
-            // the leader holds the smallest position of its group in this step
-            if (b >= 0 && b < HWIN) {
-                atomicAdd(&scnt[b], (unsigned int)__popc(peers));
-                if ((unsigned int)(i - c0) < sfirst[b]) atomicMin(&sfirst[b], (unsigned int)(i - c0));
-            } else {
-                atomicAdd(&hist[v], (unsigned long long)__popc(peers));
-                atomicMin(&first[v], (unsigned long long)i);
-            }
+        if (b >= 0 && b < HWIN) {
+            atomicAdd(&scnt[b], 1u);
+            const unsigned int off = (unsigned int)(i - c0);
+            if (off < sfirst[b]) atomicMin(&sfirst[b], off);
+        } else {
+            atomicAdd(&hist[v], 1ull);
+            atomicMin(&first[v], (unsigned long long)i);
         }
     };
     if (s1 - s0 == HSUB) {
@@ -70,10 +66,7 @@ __global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__
             for (int k = 0; k < 8; k++) count(e[k], i0 + k);
         }
     } else {
-        for (uint64_t b0 = s0; b0 < s1; b0 += 32) {
-            uint64_t i = b0 + lane;
-            if (i < s1) count(codes[i], i);
-        }
+        for (uint64_t i = s0 + lane; i < s1; i += 32) count(codes[i], i);
     }
     for (int o = 16; o > 0; o >>= 1) zc += __shfl_down_sync(0xffffffffu, zc, o);
     if (lane == 0) zcount[(uint64_t)blockIdx.x * HWARPS + w] = zc;
@@ -240,8 +233,11 @@ __device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 
 
 // Pack one chunk: each thread owns ENC_PER_THREAD consecutive symbols.
 // Words in shared memory follow the global 32-bit word grid of the output.
+// packed[state] = (len << 32) | code right-aligned (codes up to 32 bits);
+// longer codes are read from code64 (MSB-aligned).
 __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__restrict__ codes, uint64_t n, int offset,
                                                             const unsigned long long *__restrict__ code64,
+                                                            const unsigned long long *__restrict__ packed,
                                                             const uint8_t *__restrict__ len,
                                                             const unsigned long long *__restrict__ chunkoff,
                                                             uint32_t *out, int smem_words) {
@@ -290,41 +286,42 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
     unsigned long long wbase = 0;
     for (int w = 0; w < wid; w++) wbase += wtot[w];
     // bit position relative to word w0
-    uint64_t pos = (gbit & 31) + wbase + x - mybits;
-    // accumulate the thread's bits MSB-first; whole words it owns are stored,
-    // its first and last (possibly shared) words are ORed
+    const uint64_t pos = (gbit & 31) + wbase + x - mybits;
+    // bits accumulate right-aligned in acc (nacc valid bits, the first word
+    // starting with `fill` zero bits owned by the previous thread); whole
+    // words are stored, the thread's first (shared) and last words are ORed
     uint32_t wi = (uint32_t)(pos >> 5);
-    int fill = (int)(pos & 31);        // bits already in the current word (owned by others)
-    unsigned long long acc = 0;        // pending bits, MSB-aligned
-    int nacc = fill;                   // bits in acc including the leading fill
+    const int fill = (int)(pos & 31);
+    unsigned long long acc = 0;
+    int nacc = fill;
     bool first_word = true;
+    auto push = [&](uint32_t bits, int l) {  // l <= 32
+        acc = (acc << l) | bits;
+        nacc += l;
+        if (nacc >= 32) {
+            nacc -= 32;
+            const uint32_t word = (uint32_t)(acc >> nacc);
+            if (first_word && fill) atomicOr(&sw[wi], word);
+            else sw[wi] = word;
+            first_word = false;
+            wi++;
+        }
+    };
     for (int k = 0; k < ENC_PER_THREAD; k++) {
         if (sym[k] == 0xffff) break;
-        int l = len[sym[k]];
-        if (l == 0) continue;
-        unsigned long long c = code64[sym[k]];
-        // append l bits of c (MSB-aligned) at position nacc of acc
-        int take = l;
-        while (take > 0) {
-            int room = 64 - nacc;
-            int t = take < room ? take : room;
-            acc |= (c >> nacc);
-            c = t < 64 ? c << t : 0ull;
-            nacc += t;
-            take -= t;
-            while (nacc >= 32) {
-                uint32_t word = (uint32_t)(acc >> 32);
-                if (first_word && fill) atomicOr(&sw[wi], word);
-                else sw[wi] = word;
-                first_word = false;
-                wi++;
-                acc <<= 32;
-                nacc -= 32;
-            }
+        const unsigned long long e = packed[sym[k]];
+        const int l = (int)((e >> 32) & 0xff);
+        if (l <= 32) {
+            push((uint32_t)e, l);
+        } else {
+            // codes longer than 32 bits: right-align the MSB-aligned code
+            const unsigned long long c = l == 64 ? code64[sym[k]] : code64[sym[k]] >> (64 - l);
+            push((uint32_t)(c >> 32), l - 32);
+            push((uint32_t)c, 32);
         }
     }
     if (nacc > 0) {
-        uint32_t word = (uint32_t)(acc >> 32);
+        const uint32_t word = (uint32_t)(acc << (32 - nacc));
         if (word) atomicOr(&sw[wi], word);
     }
     __syncthreads();
@@ -600,14 +597,14 @@ cudaError_t launch_encode_bits(const uint16_t *codes, uint64_t n, int offset, co
 }
 
 cudaError_t launch_encode_pack(const uint16_t *codes, uint64_t n, int offset, const unsigned long long *code64,
-                               const uint8_t *len, const unsigned long long *chunkoff, uint32_t *out, int maxlen,
-                               cudaStream_t st) {
+                               const unsigned long long *packed, const uint8_t *len,
+                               const unsigned long long *chunkoff, uint32_t *out, int maxlen, cudaStream_t st) {
     int words = (int)(((uint64_t)ENC_CHUNK * (uint64_t)maxlen + 31) / 32 + 2);
     size_t sm = (size_t)words * 4;
     cudaError_t e = cudaFuncSetAttribute(k_encode_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_encode_pack<<<grid_for(n, ENC_CHUNK), ENC_THREADS, sm, st>>>(codes, n, offset, code64, len, chunkoff, out,
-                                                                    words);
+    k_encode_pack<<<grid_for(n, ENC_CHUNK), ENC_THREADS, sm, st>>>(codes, n, offset, code64, packed, len, chunkoff,
+                                                                    out, words);
     return cudaGetLastError();
 }
 

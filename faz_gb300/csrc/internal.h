@@ -41,8 +41,8 @@ uint64_t encode_chunks(uint64_t n);
 cudaError_t launch_encode_bits(const uint16_t *codes, uint64_t n, int offset, const uint8_t *len,
                                unsigned long long *chunkbits, cudaStream_t st);
 cudaError_t launch_encode_pack(const uint16_t *codes, uint64_t n, int offset, const unsigned long long *code64,
-                               const uint8_t *len, const unsigned long long *chunkoff, uint32_t *out, int maxlen,
-                               cudaStream_t st);
+                               const unsigned long long *packed, const uint8_t *len,
+                               const unsigned long long *chunkoff, uint32_t *out, int maxlen, cudaStream_t st);
 
 struct DecodeTablesDev {
     const uint32_t *lut;

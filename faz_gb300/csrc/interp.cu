@@ -207,6 +207,74 @@ __device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Straight-line reconstruction pred + q2*eb (dequant_f32 without early
+// exits); returns true when undecided.
+__device__ __forceinline__ bool dequant_f32_straight(float pred, int q2, float eh, float el, float &out) {
+    const float q = int_to_float_small(q2);
+    const float p1 = q * eh;
+    const float e1 = fmaf(q, eh, -p1);
+    const float p2 = q * el;
+    const float s = pred + p1;
+    const float bb = s - pred;
+    const float t = (pred - (s - bb)) + (p1 - bb);
+    const float lo = t + (e1 + p2);
+    const float r = s + lo;
+    const float res = (s - r) + lo;
+    const float ar = fabsf(r);
+    const uint32_t rb = f32_bits(ar);
+    const float bigv = fmaxf(fabsf(pred), fabsf(p1));
+    const float u = f32_from_bits(rb & 0x7f800000u) * 0x1p-23f;
+    const bool und = q2 != 0 && (!(ar >= 0x1p-100f) || ar * 256.0f < bigv || (rb & 0x7fffffu) == 0 ||
+                                 rb >= 0x7f000000u || fabsf(fabsf(res) - 0.5f * u) < u * 0x1p-12f);
+    out = q2 == 0 ? pred + 0.0f : r;
+    return und;
+}
+
+// One quantisation: QM 1 is the straight-line float path (trimToZero 0,
+// eb within the fast range) with the double computation for undecided
+// points; QM 0 is the general path.  v becomes the value the field takes,
+// uval the value recorded when the code is 0.
+template <typename T, int QM>
+__device__ __forceinline__ int quant_point(T &v, T pred, const LevelArgs &a, T &uval) {
+    if constexpr (QM == 1 && sizeof(T) == 4) {
+        const float orig = v;
+        float out;
+        bool und;
+        int code = quantize_f32_straight(orig, pred, a.rh, a.rl, a.eh, a.el, a.eblo, a.twor_f, a.radius, out, und);
+        if (und) {
+            out = orig;
+            code = quantize_dp_f32(out, pred, a.eb, a.recip, a.radius, 0, uval);
+        }
+        if (a.verify) {
+            float v2 = orig, u2;
+            int c2 = quantize<float>(v2, pred, a.eb, a.recip, a.radius, 0, u2);
+            if (c2 != code || __float_as_uint(v2) != __float_as_uint(out)) atomicAdd(a.verify, 1ull);
+        }
+        uval = orig;
+        v = out;
+        return code;
+    } else {
+        return quantize_any(v, pred, a, uval);
+    }
+}
+
+template <typename T, int QM>
+__device__ __forceinline__ T recover_point(T pred, int code, uint64_t pos, const LevelArgs &a, const uint64_t *zpos,
+                                           uint64_t nz, const T *unpred) {
+    if constexpr (QM == 1 && sizeof(T) == 4) {
+        float out;
+        const bool und = dequant_f32_straight(pred, 2 * (code - a.radius), a.eh, a.el, out);
+        if (code == 0 || und) out = recover_dp_f32(pred, code, pos, a.eb, a.radius, 0, zpos, nz, unpred);
+        if (a.verify) {
+            float ref = recover<float>(pred, code, pos, a.eb, a.radius, 0, zpos, nz, unpred);
+            if (__float_as_uint(ref) != __float_as_uint(out)) atomicAdd(a.verify, 1ull);
+        }
+        return out;
+    } else {
+        return recover_any(pred, code, pos, a, zpos, nz, unpred);
+    }
+}
+
 // Move cnt codes between global codes[0..cnt) and shared stg[sh..sh+cnt),
 // where sh = (global position & 7): the body moves 8 codes per 16-byte
 // access on both sides.
@@ -291,13 +359,65 @@ __device__ __forceinline__ T eval_stencil(const Stencil<T> &S, const T *p) {
     return S.nt == 1 ? x1 : y * S.scale;
 }
 
+// Line counter (outer, inner) of lines enumerated row-major with `inner`
+// values per outer step, advanced by a fixed stride without division.
+struct LineCursor {
+    int outer, inner, dout, din, width;
+    __device__ __forceinline__ void init(int start, int stride, int w) {
+        width = w;
+        outer = start / w;
+        inner = start - outer * w;
+        dout = stride / w;
+        din = stride - dout * w;
+    }
+    __device__ __forceinline__ void next() {
+        inner += din;
+        outer += dout;
+        const bool wrap = inner >= width;
+        inner -= wrap ? width : 0;
+        outer += wrap ? 1 : 0;
+    }
+};
+
+// Owner of a first-plane line in decompression: the stream position of the
+// line's first code in the previous block that emitted it.
+__device__ __forceinline__ uint64_t owner_pos_sweep1(const LevelArgs &a, const BlockGeom &g, const int64_t *bc,
+                                                     int P1, int P2, int e1, int e2, int n2) {
+    const bool s1 = e1 < g.k1, s2 = e2 < g.k2;
+    const int64_t ob0 = bc[0] - ((s1 && P1 == 0) || (s2 && P2 == 0));
+    const int64_t ob1 = bc[1] - ((s1 && P1 == 1) || (s2 && P2 == 1));
+    const int64_t ob2 = bc[2] - ((s1 && P1 == 2) || (s2 && P2 == 2));
+    const int nf = (int)(a.bs / a.s) + 1;
+    const int on2 = s2 ? nf : n2;
+    const int ok1 = pick3(P1, ob0, ob1, ob2) != 0, ok2 = pick3(P2, ob0, ob1, ob2) != 0;
+    const int oe1 = s1 ? (nf - 1) / 2 : e1;
+    const int oe2 = s2 ? (nf - 1) / 2 : e2;
+    const int one2 = (on2 + 1) / 2 - ok2;
+    const int64_t oid = (ob0 * a.nb[1] + ob1) * a.nb[2] + ob2;
+    return a.block_off[oid] + (uint64_t)((oe1 - ok1) * one2 + (oe2 - ok2)) * g.t0;
+}
+
+__device__ __forceinline__ uint64_t owner_pos_sweep2(const LevelArgs &a, const BlockGeom &g, const int64_t *bc,
+                                                     int P2, int q) {
+    const int64_t ob0 = bc[0] - (P2 == 0), ob1 = bc[1] - (P2 == 1), ob2 = bc[2] - (P2 == 2);
+    const int nf = (int)(a.bs / a.s) + 1;
+    const int ok2 = pick3(P2, ob0, ob1, ob2) != 0;
+    const int oe2 = (nf - 1) / 2;
+    const int one2 = (nf + 1) / 2 - ok2;
+    const int64_t oc1 = (int64_t)g.ne1 * one2 * g.t0;
+    const int64_t oid = (ob0 * a.nb[1] + ob1) * a.nb[2] + ob2;
+    return a.block_off[oid] + oc1 + (uint64_t)(q * one2 + (oe2 - ok2)) * g.t1;
+}
+
 // One CTA per block.  Each half-warp takes one line at a time; lane t of the
 // half-warp owns target 2t+1 of the line.  Shared-memory strides along every
 // sweep axis are odd multiples of the lane step, so the half-warps read
-// distinct banks.
+// distinct banks.  Lanes past the line's targets run the same code on a valid
+// target and store nothing.
 // WIDE selects 64-bit element offsets; fields below 2^31 elements use 32-bit
-// offsets from the block's first element.
-template <typename T, bool DECOMP, bool WIDE>
+// offsets from the block's first element.  QM selects the quantiser path
+// (1: straight-line float path, 0: general).
+template <typename T, bool DECOMP, bool WIDE, int QM>
 __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
                                                       uint16_t *__restrict__ codes, T *__restrict__ scratch,
                                                       const uint64_t *__restrict__ zpos, uint64_t nz,
@@ -327,8 +447,10 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const int t = tid & 15, hw = tid >> 4, nhw = nt >> 4;
     const int cubic = a.cubic;
+    const bool wb = a.write_back;
 
-    // phase 0: lattice points with an even index along P2, one warp per row
+    // phase 0: lattice points with an even index along P2, one warp per row,
+    // copied asynchronously
     {
         const int rows = n0 * n1;
         int m0 = warp / n1, m1 = warp - m0 * n1;
@@ -358,62 +480,46 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
             __syncthreads();
         }
         const int st = n1 * h2;
-        const int hh1 = (n1 + 1) / 2;
-        const int lines = hh1 * h2;
+        const int lines = ((n1 + 1) / 2) * h2;
         const bool act = t < g.t0;
-        const int m0 = 2 * t + 1;
-        Stencil<T> S = make_stencil<T>(act ? m0 : 1, n0, cubic, st, 0);
-        const int rk = act ? line_rank(m0, n0, cubic) : 0;
+        const int m0 = act ? 2 * t + 1 : 1;
+        const Stencil<T> S = make_stencil<T>(m0, n0, cubic, st, 0);
+        const int rk = line_rank(m0, n0, cubic);
         const Off gl = (Off)m0 * G0;
-        int e1 = hw / h2, e2 = hw - e1 * h2;
-        for (int l = hw; l < lines; l += nhw, e2 += nhw) {
-            while (e2 >= h2) {
-                e2 -= h2;
-                e1++;
-            }
-            if (!act) continue;
+        LineCursor lc;
+        lc.init(hw, nhw, h2);  // outer = e1, inner = e2
+        for (int l = hw; l < lines; l += nhw, lc.next()) {
+            const int e1 = lc.outer, e2 = lc.inner;
             const int col = 2 * e1 * h2 + e2;
-            const bool emit = e1 >= k1 && e2 >= k2;
+            const bool emit = act && e1 >= k1 && e2 >= k2;
             const int rank = ((e1 - k1) * g.ne2 + (e2 - k2)) * g.t0 + rk;
             const T pred = eval_stencil(S, V + col);
             const int idx = m0 * st + col;
             const Off gi = gl + (Off)(2 * e1) * G1 + (Off)(2 * e2) * G2;
             if (!DECOMP) {
                 T v = V[idx], uv;
-                int code = quantize_any(v, pred, a, uv);
-                V[idx] = v;
+                const int code = quant_point<T, QM>(v, pred, a, uv);
+                if (act) V[idx] = v;
                 if (emit) {
                     sg[rank] = (uint16_t)code;
                     if (code == 0) scratch[base + rank] = uv;
-                    if (a.write_back) W[gi] = v;
+                    if (wb) W[gi] = v;
                 }
-            } else {
+            } else if (act) {
                 uint64_t pos;
                 int code;
                 if (emit) {
                     pos = base + rank;
                     code = sg[rank];
                 } else {
-                    // the previous block along P1 and/or P2 owns this line
-                    const bool s1 = e1 < k1, s2 = e2 < k2;
-                    const int64_t ob0 = bc[0] - ((s1 && P1 == 0) || (s2 && P2 == 0));
-                    const int64_t ob1 = bc[1] - ((s1 && P1 == 1) || (s2 && P2 == 1));
-                    const int64_t ob2 = bc[2] - ((s1 && P1 == 2) || (s2 && P2 == 2));
-                    const int nf = (int)(a.bs / a.s) + 1;
-                    const int on2 = s2 ? nf : n2;
-                    const int ok1 = pick3(P1, ob0, ob1, ob2) != 0, ok2 = pick3(P2, ob0, ob1, ob2) != 0;
-                    const int oe1 = s1 ? (nf - 1) / 2 : e1;
-                    const int oe2 = s2 ? (nf - 1) / 2 : e2;
-                    const int one2 = (on2 + 1) / 2 - ok2;
-                    const int64_t oid = (ob0 * a.nb[1] + ob1) * a.nb[2] + ob2;
-                    pos = a.block_off[oid] + (uint64_t)((oe1 - ok1) * one2 + (oe2 - ok2)) * g.t0 + rk;
+                    pos = owner_pos_sweep1(a, g, bc, P1, P2, e1, e2, n2) + rk;
                     if (pos >= a.ncodes) {
                         atomicExch(a.err, 1);
                         pos = 0;
                     }
                     code = codes[pos];
                 }
-                T v = recover_any(pred, code, pos, a, zpos, nz, unpred);
+                const T v = recover_point<T, QM>(pred, code, pos, a, zpos, nz, unpred);
                 V[idx] = v;
                 if (emit) W[gi] = v;
             }
@@ -438,56 +544,45 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
         }
         const int lines = (n0 - k0) * h2;
         const bool act = t < g.t1;
-        const int m1 = 2 * t + 1;
-        Stencil<T> S = make_stencil<T>(act ? m1 : 1, n1, cubic, h2, 0);
-        const int rk = act ? line_rank(m1, n1, cubic) : 0;
+        const int m1 = act ? 2 * t + 1 : 1;
+        const Stencil<T> S = make_stencil<T>(m1, n1, cubic, h2, 0);
+        const int rk = line_rank(m1, n1, cubic);
         const Off gl = (Off)m1 * G1;
-        int q = hw / h2, e2 = hw - q * h2;
-        for (int l = hw; l < lines; l += nhw, e2 += nhw) {
-            while (e2 >= h2) {
-                e2 -= h2;
-                q++;
-            }
-            if (!act) continue;
+        LineCursor lc;
+        lc.init(hw, nhw, h2);  // outer = m0 - k0, inner = e2
+        for (int l = hw; l < lines; l += nhw, lc.next()) {
+            const int q = lc.outer, e2 = lc.inner;
             const int m0 = k0 + q;
             const int col = m0 * n1 * h2 + e2;
-            const bool emit = e2 >= k2;
+            const bool emit = act && e2 >= k2;
             const int rank = (q * g.ne2 + (e2 - k2)) * g.t1 + rk;
             const T pred = eval_stencil(S, V + col);
             const int idx = col + m1 * h2;
             const Off gi = (Off)m0 * G0 + gl + (Off)(2 * e2) * G2;
             if (!DECOMP) {
                 T v = V[idx], uv;
-                int code = quantize_any(v, pred, a, uv);
-                V[idx] = v;
+                const int code = quant_point<T, QM>(v, pred, a, uv);
+                if (act) V[idx] = v;
                 if (emit) {
                     sg[rank] = (uint16_t)code;
                     if (code == 0) scratch[sbase + rank] = uv;
-                    if (a.write_back) W[gi] = v;
+                    if (wb) W[gi] = v;
                 }
-            } else {
+            } else if (act) {
                 uint64_t pos;
                 int code;
                 if (emit) {
                     pos = sbase + rank;
                     code = sg[rank];
                 } else {
-                    // the previous block along P2 owns this line
-                    const int64_t ob0 = bc[0] - (P2 == 0), ob1 = bc[1] - (P2 == 1), ob2 = bc[2] - (P2 == 2);
-                    const int nf = (int)(a.bs / a.s) + 1;
-                    const int ok2 = pick3(P2, ob0, ob1, ob2) != 0;
-                    const int oe2 = (nf - 1) / 2;
-                    const int one2 = (nf + 1) / 2 - ok2;
-                    const int64_t oc1 = (int64_t)g.ne1 * one2 * g.t0;
-                    const int64_t oid = (ob0 * a.nb[1] + ob1) * a.nb[2] + ob2;
-                    pos = a.block_off[oid] + oc1 + (uint64_t)(q * one2 + (oe2 - ok2)) * g.t1 + rk;
+                    pos = owner_pos_sweep2(a, g, bc, P2, q) + rk;
                     if (pos >= a.ncodes) {
                         atomicExch(a.err, 1);
                         pos = 0;
                     }
                     code = codes[pos];
                 }
-                T v = recover_any(pred, code, pos, a, zpos, nz, unpred);
+                const T v = recover_point<T, QM>(pred, code, pos, a, zpos, nz, unpred);
                 V[idx] = v;
                 if (emit) W[gi] = v;
             }
@@ -500,9 +595,9 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     }
 
     // sweep 3: lines along P2 at (m0, m1), emitted lines only.  Compression
-    // reads the targets from global memory; the loads run three lines ahead.
+    // reads the targets from global memory; the loads run two lines ahead.
     // A block that begins on the last element of an axis has no sweep-3
-    // lines (n - k = 0); the carried line counters below divide by n1 - k1.
+    // lines (n - k = 0).
     if (g.t2 > 0 && n0 - k0 > 0 && n1 - k1 > 0) {
         const int64_t cnt = g.c3;
         const uint64_t sbase = base + g.c1 + g.c2;
@@ -515,46 +610,43 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
         const int w1 = n1 - k1;
         const int lines = (n0 - k0) * w1;
         const bool act = t < g.t2;
-        const int m2 = 2 * t + 1;
-        Stencil<T> S = make_stencil<T>(act ? m2 : 1, n2, cubic, 1, 1);
-        const int rk = act ? line_rank(m2, n2, cubic) : 0;
+        const int m2 = act ? 2 * t + 1 : 1;
+        const Stencil<T> S = make_stencil<T>(m2, n2, cubic, 1, 1);
+        const int rk = line_rank(m2, n2, cubic);
         const Off gl = (Off)m2 * G2 + (Off)k0 * G0 + (Off)k1 * G1;
-        int q0 = hw / w1, q1 = hw - q0 * w1;  // line being computed
-        int p0 = q0, p1 = q1;                 // line being loaded
-        T xa = 0, xb = 0, xc = 0;
-        int lp = hw;
-        if (!DECOMP && act) {
-            if (lp < lines) xa = X[gl + (Off)p0 * G0 + (Off)p1 * G1];
-            lp += nhw; p1 += nhw;
-            while (p1 >= w1) { p1 -= w1; p0++; }
-            if (lp < lines) xb = X[gl + (Off)p0 * G0 + (Off)p1 * G1];
-            lp += nhw; p1 += nhw;
-            while (p1 >= w1) { p1 -= w1; p0++; }
+        LineCursor lc, lp;  // line being computed / being loaded
+        lc.init(hw, nhw, w1);
+        lp = lc;
+        T xa = 0, xb = 0;
+        int lpi = hw;
+        if (!DECOMP) {
+            if (lpi < lines) xa = X[gl + (Off)lp.outer * G0 + (Off)lp.inner * G1];
+            lpi += nhw;
+            lp.next();
         }
-        for (int l = hw; l < lines; l += nhw) {
-            if (!act) continue;
+        for (int l = hw; l < lines; l += nhw, lc.next()) {
             if (!DECOMP) {
-                xc = lp < lines ? X[gl + (Off)p0 * G0 + (Off)p1 * G1] : (T)0;
-                lp += nhw; p1 += nhw;
-                while (p1 >= w1) { p1 -= w1; p0++; }
+                xb = lpi < lines ? X[gl + (Off)lp.outer * G0 + (Off)lp.inner * G1] : (T)0;
+                lpi += nhw;
+                lp.next();
             }
+            const int q0 = lc.outer, q1 = lc.inner;
             const T *row = V + ((k0 + q0) * n1 + (k1 + q1)) * h2;
             const T pred = eval_stencil(S, row);
             const int rank = l * g.t2 + rk;
             const Off gi = gl + (Off)q0 * G0 + (Off)q1 * G1;
             if (!DECOMP) {
                 T v = xa, uv;
-                int code = quantize_any(v, pred, a, uv);
-                sg[rank] = (uint16_t)code;
-                if (code == 0) scratch[sbase + rank] = uv;
-                if (a.write_back) W[gi] = v;
+                const int code = quant_point<T, QM>(v, pred, a, uv);
+                if (act) {
+                    sg[rank] = (uint16_t)code;
+                    if (code == 0) scratch[sbase + rank] = uv;
+                    if (wb) W[gi] = v;
+                }
                 xa = xb;
-                xb = xc;
-            } else {
-                W[gi] = recover_any(pred, (int)sg[rank], sbase + rank, a, zpos, nz, unpred);
+            } else if (act) {
+                W[gi] = recover_point<T, QM>(pred, (int)sg[rank], sbase + rank, a, zpos, nz, unpred);
             }
-            q1 += nhw;
-            while (q1 >= w1) { q1 -= w1; q0++; }
         }
         __syncthreads();
         if (!DECOMP) move_codes<true>(codes + sbase, stg, cnt, sh);
@@ -681,9 +773,15 @@ cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const
     int64_t vol = (int64_t)a.vwords * 2;
     int threads = vol >= 8192 ? 512 : (vol >= 1024 ? 256 : (vol >= 256 ? 128 : 64));
     const bool wide = a.dims[0] * a.dims[1] * a.dims[2] >= ((int64_t)1 << 31);
+    const bool straight = sizeof(T) == 4 && a.fast && a.trim == 0;
     void (*k)(LevelArgs, const T *, T *, uint16_t *, T *, const uint64_t *, uint64_t, const T *);
-    if (!decomp) k = wide ? k_interp_level<T, false, true> : k_interp_level<T, false, false>;
-    else k = wide ? k_interp_level<T, true, true> : k_interp_level<T, true, false>;
+    if (straight) {
+        if (!decomp) k = wide ? k_interp_level<T, false, true, 1> : k_interp_level<T, false, false, 1>;
+        else k = wide ? k_interp_level<T, true, true, 1> : k_interp_level<T, true, false, 1>;
+    } else {
+        if (!decomp) k = wide ? k_interp_level<T, false, true, 0> : k_interp_level<T, false, false, 0>;
+        else k = wide ? k_interp_level<T, true, true, 0> : k_interp_level<T, true, false, 0>;
+    }
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     k<<<(unsigned)nblocks, threads, sm, st>>>(a, X, W, codes, scratch, zpos, nz, unpred);

@@ -37,6 +37,28 @@ static int ref_half(float d, double recip, int twor) {
     return qi >> 1;
 }
 
+// LinearQuantizer::quantize_and_overwrite for float data, trimToZero = 0,
+// in the reference's float/double arithmetic
+static int ref_quantize(float orig, float pred, double eb, int radius, float &out) {
+    double recip = 1.0 / eb;
+    float diff = orig - pred;
+    double x = (double)std::fabs(diff) * recip;
+    out = orig;
+    if (!(x < 2147483647.0)) return 0;
+    int qi = (int)x + 1;
+    if (qi >= radius * 2) return 0;
+    qi >>= 1;
+    int half = qi;
+    qi <<= 1;
+    int code;
+    if (diff < 0) { qi = -qi; code = radius - half; } else code = radius + half;
+    float dec = (float)((double)pred + (double)qi * eb);
+    float err = dec - orig;
+    if (std::fabs((double)err) > eb) return 0;
+    out = dec;
+    return code;
+}
+
 int main(int argc, char **argv) {
     uint64_t cases = argc > 1 ? strtoull(argv[1], 0, 10) : 1000000;
     uint64_t seed = argc > 2 ? strtoull(argv[2], 0, 10) : 1;
@@ -113,6 +135,43 @@ int main(int argc, char **argv) {
             d_bad++;
         }
     }
+    // ---- straight-line quantiser vs the reference arithmetic
+    uint64_t q_ok = 0, q_und = 0, q_bad = 0;
+    std::mt19937_64 rng2(seed * 7 + 1);
+    for (uint64_t i = 0; i < cases; i++) {
+        double eb;
+        int kind = (int)(rng2() % 3);
+        if (kind == 0) eb = std::pow(10.0, -6 + 8 * U(rng2)) * (1 + U(rng2));
+        else if (kind == 1) eb = std::ldexp(1.0, -20 + (int)(rng2() % 25));
+        else eb = 1e-3 * (double)(float)(130 * U(rng2));
+        Split sp = split(eb);
+        float eblo = (float)eb;
+        if ((double)eblo > eb) eblo = std::nextafter(eblo, 0.0f);
+        float pred = (float)((U(rng2) - 0.5) * 200);
+        float orig;
+        int ok = (int)(rng2() % 6);
+        if (ok == 0) orig = pred + (float)((U(rng2) - 0.5) * 10 * eb);
+        else if (ok == 1) orig = (float)((double)pred + (2.0 * (int)(rng2() % 50) - 49 + (U(rng2) - 0.5) * 1e-6) * eb);
+        else if (ok == 2) orig = (float)((double)pred + (double)(int)(rng2() % 200000 - 100000) * eb);
+        else if (ok == 3) orig = pred;
+        else if (ok == 4) orig = std::nextafter(pred, (rng2() & 1) ? INFINITY : -INFINITY);
+        else orig = (float)((U(rng2) - 0.5) * 1e-3);
+        int radius = (rng2() % 8 == 0) ? 1 + (int)(rng2() % 1000) : 32768;
+        float out_ref, out;
+        bool und;
+        int cref = ref_quantize(orig, pred, eb, radius, out_ref);
+        int c = quantize_f32_straight(orig, pred, sp.rh, sp.rl, sp.eh, sp.el, eblo, (float)(2 * radius), radius, out, und);
+        if (und) q_und++;
+        else if (c == cref && f32_bits(out) == f32_bits(out_ref)) q_ok++;
+        else {
+            if (q_bad < 10)
+                printf("quantize mismatch: orig=%a pred=%a eb=%a r=%d got=(%d,%a) ref=(%d,%a)\n", (double)orig,
+                       (double)pred, eb, radius, c, (double)out, cref, (double)out_ref);
+            q_bad++;
+        }
+    }
+    printf("quantize: ok=%" PRIu64 " undecided=%" PRIu64 " bad=%" PRIu64 "\n", q_ok, q_und, q_bad);
+    if (q_bad) return 1;
     printf("half: ok=%" PRIu64 " undecided=%" PRIu64 " bad=%" PRIu64 "\n", h_ok, h_und, h_bad);
     printf("dequant: ok=%" PRIu64 " undecided=%" PRIu64 " bad=%" PRIu64 "\n", d_ok, d_und, d_bad);
     return (h_bad || d_bad) ? 1 : 0;
