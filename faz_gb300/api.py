@@ -19,7 +19,7 @@ STATUS = {0: "FAZ_OK", -1: "FAZ_ERR_ARG", -2: "FAZ_ERR_UNSUPPORTED", -3: "FAZ_ER
 
 EXPORTED = ["faz_config_init", "faz_config_load_ini", "faz_compress", "faz_decompress", "faz_compress_device",
             "faz_decompress_device", "faz_compress_device_payload", "faz_decompress_payload_device",
-            "faz_stream_info",
+            "faz_stream_info", "faz_resolve_eb_noalloc",
             "faz_config_size", "faz_free", "faz_last_error", "faz_zstd_version"]
 
 
@@ -52,6 +52,7 @@ def library():
         L.faz_config_size.restype = ctypes.c_size_t
         L.faz_compress_device_payload.argtypes = [vp, ctypes.c_int, vp, vp, vp, sz, P(sz), vp, vp]
         L.faz_stream_info.argtypes = [vp, sz, vp]
+        L.faz_resolve_eb_noalloc.argtypes = [vp, ctypes.c_int, vp, vp]
         L.faz_decompress_payload_device.argtypes = [ctypes.c_int, ctypes.c_int, vp, sz, vp, ctypes.c_uint64, vp, vp]
         _lib = L
         return L

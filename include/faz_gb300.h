@@ -213,6 +213,22 @@ int faz_decompress_payload_device(int N, int dtype, const char *payload, size_t 
                                   void *d_out, uint64_t capacity, void *stream,
                                   faz_timings *timings);
 
+/* Resolve the absolute error bound of conf for the field d_data (conf->num
+ * values of `dtype` in device memory, work issued on `stream`) without
+ * allocating any memory.  This has no counterpart in the reference.  It is
+ * for callers that cannot allocate when they need the bound: code under an
+ * allocation ban (pipelines that allocate only at start-up), code that owns
+ * all device memory through its own arena, or threads that must not take the
+ * allocator's locks.  It computes what faz_compress derives before
+ * compressing (value range, then the mode's formula): conf->absErrorBound and
+ * conf->rng are set and conf->errorBoundMode becomes FAZ_EB_ABS.  Its scratch
+ * is a 64 KiB array inside this library that every GPU loading the library
+ * keeps until exit; fields above 2^28 values are rejected with FAZ_ERR_ARG.
+ * All calls share that array: calls whose device work overlaps race.  The
+ * first call on each device looks the array's address up; make it before
+ * any stream capture. */
+int faz_resolve_eb_noalloc(faz_config *conf, int dtype, const void *d_data, void *stream);
+
 /* sizeof(faz_config) as this library was compiled, for bindings that
  * mirror the struct (ctypes, cgo, JNI) to check their layout. */
 size_t faz_config_size(void);
