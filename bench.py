@@ -116,6 +116,14 @@ def make_conf(F, dims, eb, interp):
     return c
 
 
+# DRAM traffic of one finest-level compress launch, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum = 342.43 MB + 100.42 MB) on a
+# 256x512x512 float32 field, cubic, rel eb 1e-3; traffic grows with the number
+# of values, so it is scaled to the benchmarked field by its value count.
+FINEST_TRAFFIC_BYTES = 442849280
+FINEST_TRAFFIC_VALUES = 256 * 512 * 512
+
+
 def finest_level_bytes(dims, itemsize):
     """Algorithmic bytes of the finest level kernel: each target point read
     once and its 2-byte code written once, each coarse point read once."""
@@ -326,6 +334,10 @@ def main():
     fin = statistics.median(p["finest_level_ms"] for p in phases) / 1e3
     fin_bytes = finest_level_bytes(dims, 4)
     achieved = fin_bytes / fin / 1e9
+    nvals = dims[0] * dims[1] * dims[2]
+    traffic = None
+    if args.interp == "cubic" and args.eb == 1e-3:
+        traffic = int(round(FINEST_TRAFFIC_BYTES * nvals / FINEST_TRAFFIC_VALUES))
     cpu = None
     if not args.no_cpu_baseline:
         slab = 64
@@ -363,7 +375,7 @@ def main():
         "roofline": {"kernel": "k_interp_level<float,compress> finest level", "bound": "hbm",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "bytes_per_launch": fin_bytes, "traffic": None},
+                     "bytes_per_launch": fin_bytes, "traffic": traffic},
         "phases_ms": {"compress": {k: med(k, phases) for k in ("predict_ms", "finest_level_ms", "huffman_ms",
                                                                "host_ms", "gpu_ms")},
                       "decompress": {k: med(k, dphases) for k in ("huffman_ms", "predict_ms", "finest_level_ms",
