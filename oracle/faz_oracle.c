@@ -56,6 +56,7 @@ static void b_put(bytes_t *b, const void *src, size_t len) {
         __typeof__(v) _t = (v);        \
         b_put((b), &_t, sizeof(_t));   \
     } while (0)
+#define PUTGET(r, v) r_get((r), &(v), sizeof(v))
 
 typedef struct {
     const uint8_t *p;
@@ -493,6 +494,17 @@ static int huff_decode(rd_t *r, size_t target, int *out) {
     return rc;
 }
 
+#define T float
+#define SFX f32
+#include "oracle_lorenzo.inc"
+#undef T
+#undef SFX
+#define T double
+#define SFX f64
+#include "oracle_lorenzo.inc"
+#undef T
+#undef SFX
+
 /* ----------------------------------------------------- config and trailer */
 
 /* Config::Config(Dims...) - Config.hpp:64-74, member defaults 394-499 */
@@ -782,17 +794,205 @@ int orc_interp_compress(const faz_config *conf, int dtype, const void *data, int
     return 0;
 }
 
-/* SZ_compress<T> with cmprAlgo == ALGO_INTERP: error bound, interpolation
- * payload, Lossless_zstd framing, Config trailer, int32 trailer size. */
+/* Lossless_zstd::compress output size: size_t raw length + zstd frame
+ * (include/QoZ/lossless/Lossless_zstd.hpp:22-32). */
+static int z_framed_size(const uint8_t *p, size_t n, size_t *out) {
+    if (z_load()) return -5;
+    size_t bound = z_bound(n);
+    uint8_t *tmp = (uint8_t *)malloc(bound ? bound : 1);
+    size_t zs = z_comp(tmp, bound, p, n, 3);
+    free(tmp);
+    if (z_iserr(zs)) { set_err("zstd compress failed"); return -5; }
+    *out = zs + 8;
+    return 0;
+}
+
+/* data_range<T> (Statistic.hpp:12-21): max - min in the element type */
+static double data_range(int dtype, const void *data, size_t n) {
+    if (dtype == FAZ_FLOAT) {
+        const float *d = (const float *)data;
+        float mx = d[0], mn = d[0];
+        for (size_t i = 1; i < n; i++) {
+            if (mx < d[i]) mx = d[i];
+            if (mn > d[i]) mn = d[i];
+        }
+        return (double)(float)(mx - mn);
+    }
+    const double *d = (const double *)data;
+    double mx = d[0], mn = d[0];
+    for (size_t i = 1; i < n; i++) {
+        if (mx < d[i]) mx = d[i];
+        if (mn > d[i]) mn = d[i];
+    }
+    return mx - mn;
+}
+
+/* Fast-frontend payload of a 3-D field (SZ_compress_LorenzoReg with N == 3,
+ * include/QoZ/api/impl/SZLorenzoReg.hpp:94-114). */
+static int lorenzo3_payload(int dtype, const void *data, const size_t *dims, int bs, int pd, int lo, int lo2, int reg,
+                            double eb, int radius, bytes_t *out) {
+    if (dtype == FAZ_FLOAT) {
+        fparams_f32 P;
+        fparams_init_f32(&P, bs, pd, lo, lo2, reg, eb);
+        return fast3_compress_f32((const float *)data, dims, &P, eb, radius, out);
+    }
+    fparams_f64 P;
+    fparams_init_f64(&P, bs, pd, lo, lo2, reg, eb);
+    return fast3_compress_f64((const double *)data, dims, &P, eb, radius, out);
+}
+
+/* compressed size (zstd framing included) of a Lorenzo trial on 3-D data */
+static int lorenzo3_size(int dtype, const void *data, const size_t *dims, int bs, int pd, double eb, int radius,
+                         size_t *size) {
+    bytes_t b = {0};
+    int rc = lorenzo3_payload(dtype, data, dims, bs, pd, 1, 1, 0, eb, radius, &b);
+    if (!rc) rc = z_framed_size(b.p, b.n, size);
+    free(b.p);
+    return rc;
+}
+
+/* do_not_use_this_interp_compress_block_test (SZInterp.hpp:558-577) */
+static int blockinterp_ratio(int dtype, const void *data, int N, const size_t *dims, size_t num, double eb, int op,
+                             int dir, int bs, double *ratio) {
+    bytes_t b = {0};
+    int rc = dtype == FAZ_FLOAT ? blockinterp_compress_f32((const float *)data, N, dims, eb, op, dir, bs, &b)
+                                : blockinterp_compress_f64((const double *)data, N, dims, eb, op, dir, bs, &b);
+    size_t sz = 0;
+    if (!rc) rc = z_framed_size(b.p, b.n, &sz);
+    free(b.p);
+    if (!rc) *ratio = num * 1.0 * (dtype == FAZ_FLOAT ? 4 : 8) / sz;
+    return rc;
+}
+
+static void *sample_of(int dtype, const void *data, int N, const size_t *dims, size_t *sn, size_t *sd, size_t *sb) {
+    if (dtype == FAZ_FLOAT) return sampling_f32((const float *)data, N, dims, sn, sd, sb);
+    return sampling_f64((const double *)data, N, dims, sn, sd, sb);
+}
+
+/* Config::setDims side effects (Config.hpp:77-89) */
+static void conf_set_dims_defaults(faz_config *c) {
+    c->blockSize = c->N == 1 ? 128 : (c->N == 2 ? 16 : 6);
+    c->pred_dim = c->N;
+    c->stride = c->blockSize;
+}
+
+/*
+ * ALGO_INTERP_LORENZO without QoZ tuning (SZ_compress_Interp_lorenzo,
+ * SZInterp.hpp:2561-2880, with the SZ3 branch of Tuning, 2115-2187): range and
+ * relative bound, sampling, Lorenzo trial, linear / cubic block-interpolation
+ * trials, direction trial (kept above a 2% gain), interp-or-Lorenzo choice;
+ * for Lorenzo the quantisation-interval estimate and the pred_dim and 16384-bin
+ * trials.  On return conf holds the decisions (cmprAlgo, interpAlgo,
+ * interpDirection, quantbinCnt, Lorenzo settings).  3-D data only when the
+ * field is large enough to be sampled.
+ */
+static int sz3_tune(faz_config *conf, int dtype, const void *data) {
+    int N = conf->N;
+    size_t dims[4];
+    for (int i = 0; i < N; i++) dims[i] = conf->dims[i];
+    size_t es = dtype == FAZ_FLOAT ? 4 : 8;
+    if (conf->rng < 0) conf->rng = data_range(dtype, data, conf->num);
+    if (conf->relErrorBound <= 0) conf->relErrorBound = conf->absErrorBound / conf->rng;
+    if (conf->QoZ || conf->autoTuningRate > 0 || conf->predictorTuningRate > 0 || conf->preTrim > 0 ||
+        conf->wavelet > 0) {
+        set_err("oracle covers the SZ3 tuner only");
+        return -2;
+    }
+    size_t sn, sd[4], sb;
+    void *smp = sample_of(dtype, data, N, dims, &sn, sd, &sb);
+    if (sn == conf->num) {
+        free(smp);
+        conf->cmprAlgo = FAZ_ALGO_INTERP;
+        return 0;
+    }
+    if (N != 3) { free(smp); set_err("oracle tunes sampled 3-D fields"); return -2; }
+    double eb = conf->absErrorBound;
+    size_t osz;
+    int rc = lorenzo3_size(dtype, smp, sd, 5, 3, eb, conf->quantbinCnt / 2, &osz);
+    if (rc) { free(smp); return rc; }
+    double best_l = sn * 1.0 * es / osz, best_i = 0, ratio;
+    for (int op = 0; op <= 1; op++) {
+        rc = blockinterp_ratio(dtype, smp, N, sd, sn, eb, op, conf->interpDirection, (int)sb, &ratio);
+        if (rc) { free(smp); return rc; }
+        if (ratio > best_i) { best_i = ratio; conf->interpAlgo = op; }
+    }
+    int dop = 5;
+    rc = blockinterp_ratio(dtype, smp, N, sd, sn, eb, conf->interpAlgo, dop, (int)sb, &ratio);
+    if (rc) { free(smp); return rc; }
+    if (ratio > best_i * 1.02) { best_i = ratio; conf->interpDirection = dop; }
+    int use_interp = !(best_l > best_i && best_l < 80 && best_i < 80);
+    if (use_interp) {
+        free(smp);
+        conf->cmprAlgo = FAZ_ALGO_INTERP;
+        return 0;
+    }
+    /* Lorenzo follow-up (SZInterp.hpp:2779-2837) */
+    faz_config lc = *conf;
+    lc.cmprAlgo = FAZ_ALGO_LORENZO_REG;
+    lc.lorenzo = 1; lc.lorenzo2 = 1; lc.regression = 0; lc.regression2 = 0; lc.openmp = 0;
+    lc.blockSize = 5;
+    conf_set_dims_defaults(&lc);   /* setDims(sample dims) */
+    if (dtype == FAZ_FLOAT)
+        lc.quantbinCnt = opt_quant_intervals_f32((const float *)data, dims[0], dims[1], dims[2], eb);
+    else
+        lc.quantbinCnt = opt_quant_intervals_f64((const double *)data, dims[0], dims[1], dims[2], eb);
+    lc.pred_dim = 2;
+    rc = lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz);
+    if (rc) { free(smp); return rc; }
+    ratio = sn * 1.0 * es / osz;
+    if (ratio > best_l * 1.02) best_l = ratio; else lc.pred_dim = 3;
+    if (conf->relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
+        int q0 = lc.quantbinCnt;
+        lc.quantbinCnt = 16384;
+        rc = lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz);
+        if (rc) { free(smp); return rc; }
+        ratio = sn * 1.0 * es / osz;
+        if (ratio > best_l * 1.02) best_l = ratio; else lc.quantbinCnt = q0;
+    }
+    conf_set_dims_defaults(&lc);   /* setDims(full dims) */
+    free(smp);
+    *conf = lc;
+    return 0;
+}
+
+/* Pre-zstd payload of a resolved configuration (SZ_compress_dispatcher,
+ * include/QoZ/api/impl/SZDispatcher.hpp:12-36). */
+static int payload_for(faz_config *conf, int dtype, const void *data, uint8_t **payload, size_t *psize) {
+    if (conf->cmprAlgo == FAZ_ALGO_INTERP)
+        return orc_interp_compress(conf, dtype, data, NULL, NULL, NULL, NULL, payload, psize);
+    if (conf->cmprAlgo == FAZ_ALGO_LORENZO_REG) {
+        if (conf->N != 3 || conf->regression2) { set_err("oracle covers the 3-D fast frontend"); return -2; }
+        if (conf->blockSize < 1) { set_err("bad block size"); return -1; }
+        size_t dims[3] = {conf->dims[0], conf->dims[1], conf->dims[2]};
+        bytes_t b = {0};
+        int rc = lorenzo3_payload(dtype, data, dims, conf->blockSize, conf->pred_dim, conf->lorenzo, conf->lorenzo2,
+                                  conf->regression, conf->absErrorBound, conf->quantbinCnt / 2, &b);
+        if (rc) { free(b.p); return rc; }
+        *payload = b.p;
+        *psize = b.n;
+        return 0;
+    }
+    set_err("unsupported cmprAlgo");
+    return -2;
+}
+
+/* SZ_compress<T>: error bound, tuner (ALGO_INTERP_LORENZO), payload,
+ * Lossless_zstd framing, Config trailer, int32 trailer size. */
 int orc_compress(const faz_config *conf_in, int dtype, const void *data, uint8_t **out, size_t *out_size,
                  uint8_t **payload_out, size_t *payload_size_out) {
     faz_config conf = *conf_in;
     if (conf.N < 1 || conf.N > 4) { set_err("N must be 1..4"); return -1; }
-    if (conf.cmprAlgo != FAZ_ALGO_INTERP) { set_err("oracle covers ALGO_INTERP"); return -2; }
+    if (conf.cmprAlgo != FAZ_ALGO_INTERP && conf.cmprAlgo != FAZ_ALGO_LORENZO_REG &&
+        conf.cmprAlgo != FAZ_ALGO_INTERP_LORENZO) { set_err("unsupported cmprAlgo"); return -2; }
     if (eb_resolve(&conf, dtype, data)) return -1;
+    if (conf.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) {
+        int rc = sz3_tune(&conf, dtype, data);
+        if (rc) return rc;
+    }
     uint8_t *payload;
     size_t psize;
-    if (orc_interp_compress(&conf, dtype, data, NULL, NULL, NULL, NULL, &payload, &psize)) return -1;
+    int rc = payload_for(&conf, dtype, data, &payload, &psize);
+    if (rc) return rc;
     if (z_load()) { free(payload); return -5; }
     bytes_t b = {0};
     PUT(&b, (uint64_t)psize);
@@ -809,6 +1009,12 @@ int orc_compress(const faz_config *conf_in, int dtype, const void *data, uint8_t
     *out = b.p;
     *out_size = b.n;
     return 0;
+}
+
+/* The tuner's decisions for a field, without compressing (for tests). */
+int orc_sz3_tune(faz_config *conf, int dtype, const void *data) {
+    if (eb_resolve(conf, dtype, data)) return -1;
+    return sz3_tune(conf, dtype, data);
 }
 
 /* Split a stream into payload (zstd-decompressed) and trailer config. */
@@ -841,6 +1047,25 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
     size_t psize;
     int rc = orc_read_stream(cmp, cmp_size, &conf, &payload, &psize);
     if (rc) return rc;
+    if (conf.cmprAlgo == FAZ_ALGO_LORENZO_REG) {
+        /* SZ_decompress_LorenzoReg with N == 3 (SZLorenzoReg.hpp:117-135) */
+        if (conf.N != 3 || conf.regression2) {
+            free(payload);
+            set_err("oracle decodes 3-D fast-frontend streams");
+            return -2;
+        }
+        size_t dims[3] = {conf.dims[0], conf.dims[1], conf.dims[2]};
+        size_t es = dtype == FAZ_FLOAT ? 4 : 8;
+        void *dec = malloc(conf.num * es + es);
+        rd_t r = {payload, psize, 0, 0};
+        int rc2 = dtype == FAZ_FLOAT ? fast3_decompress_f32(&r, dims, (float *)dec)
+                                     : fast3_decompress_f64(&r, dims, (double *)dec);
+        free(payload);
+        if (rc2) { free(dec); return rc2; }
+        *out = dec;
+        if (conf_out) *conf_out = conf;
+        return 0;
+    }
     if (conf.cmprAlgo != FAZ_ALGO_INTERP || conf.blockwiseTuning) {
         free(payload);
         set_err("oracle decodes ALGO_INTERP streams");

@@ -12,7 +12,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 SRC = [os.path.join(HERE, "faz_oracle.c"), os.path.join(HERE, "oracle_interp.inc"),
-       os.path.join(HERE, "..", "include", "faz_gb300.h")]
+       os.path.join(HERE, "oracle_lorenzo.inc"), os.path.join(HERE, "..", "include", "faz_gb300.h")]
 REF_ZSTD = os.path.join(HERE, "_ref", "libzstd145.so")
 
 _lib = None
@@ -49,6 +49,7 @@ def lib():
         L.orc_set_zstd.argtypes = [ctypes.c_char_p]
         L.orc_free.argtypes = [ctypes.c_void_p]
         L.orc_ska_order.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        L.orc_sz3_tune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -124,6 +125,18 @@ def decompress(stream, dtype=np.float32):
     arr = np.frombuffer(_take(out, num * dtype.itemsize), dtype=dtype).copy()
     conf = Config.from_struct(cs)
     return arr.reshape(conf.dims), conf
+
+
+def sz3_tune(conf, data):
+    """The SZ3 tuner's decisions for `data` (a Config with cmprAlgo,
+    interpAlgo, interpDirection, quantbinCnt and the Lorenzo settings)."""
+    from faz_gb300.config import Config
+    data = np.ascontiguousarray(data)
+    s = conf.to_struct()
+    rc = lib().orc_sz3_tune(ctypes.byref(s), _dtype_code(data), data.ctypes.data)
+    if rc:
+        raise RuntimeError(f"oracle tuner failed ({rc}): {lib().orc_last_error().decode()}")
+    return Config.from_struct(s)
 
 
 def read_stream(stream):

@@ -56,8 +56,10 @@ def golden_stream(case):
 # INI keys of QoZ::Config::loadcfg (include/QoZ/utils/Config.hpp:91-233) used by the fixtures
 _INI_INT = {"InterpDirection": "interpDirection", "InterpBlockSize": "interpBlockSize",
             "fixBlockSize": "fixBlockSize", "trimToZero": "trimToZero", "maxStep": "maxStep",
-            "QuantizationBinTotal": "quantbinCnt", "blockOrder": "blockOrder"}
+            "QuantizationBinTotal": "quantbinCnt", "blockOrder": "blockOrder", "BlockSize": "blockSize"}
 _INI_REAL = {"alpha": "alpha", "beta": "beta"}
+_INI_BOOL = {"Lorenzo": "lorenzo", "Lorenzo2ndOrder": "lorenzo2", "Regression": "regression",
+             "Regression2ndOrder": "regression2"}
 
 
 def cli_config(case):
@@ -86,6 +88,9 @@ def cli_config(case):
         for k, f in _INI_REAL.items():
             if k in a:
                 setattr(conf, f, float(a[k]))
+        for k, f in _INI_BOOL.items():
+            if k in a:
+                setattr(conf, f, 1 if a[k].strip().lower() in ("true", "yes", "on", "1") else 0)
     m = flags.index("-M")
     mode = flags[m + 1]
     val = flags[m + 2] if m + 2 < len(flags) and not flags[m + 2].startswith("-") else None
@@ -143,6 +148,17 @@ def tuned_config(case):
     conf.interpAlgo_list = h["interp_list"]
     conf.interpDirection_list = h["dir_list"]
     return conf
+
+
+def mask_fast_frontend_padding(payload, itemsize):
+    """Zero the padding bytes of the Lorenzo fast frontend's raw structs in a
+    pre-zstd payload: meta_params (bytes 11 and 41-43 of its 44) and
+    meanInfo<T> (the bytes after its bool), which the reference writes from
+    uninitialised memory (include/QoZ/frontend/SZFastFrontend.hpp:48-53)."""
+    b = bytearray(payload)
+    for i in [11, 41, 42, 43] + list(range(53, 52 + itemsize)):
+        b[i] = 0
+    return bytes(b)
 
 
 def mask_first_size(stream):

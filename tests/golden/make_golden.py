@@ -91,7 +91,38 @@ def cases():
     out.append(("qoz_48", spectral_field((48, 48, 48), slope=-3.0, seed=23), ["-M", "REL", "1e-3", "-q"],
                 None))
     out.append(("sz3_48", spectral_field((48, 48, 48), slope=-3.0, seed=24), ["-M", "REL", "1e-3"], None))
+    # default configuration (ALGO_INTERP_LORENZO, SZ3 tuner) on fields large
+    # enough to be sampled: interpolation chosen (direction trial kept / not)
+    out.append(("sz3_interp_dir5", spectral_field((56, 60, 64), slope=-3.5, aniso=(4, 2, 1), seed=41),
+                ["-M", "REL", "1e-3"], None))
+    out.append(("sz3_interp_1e2", spectral_field((56, 60, 64), slope=-3.0, seed=33), ["-M", "REL", "1e-2"], None))
+    # ... and Lorenzo chosen: sums of 2-D functions, which the 3-D Lorenzo
+    # predictor reproduces, plus noise
+    out.append(("sz3_lorenzo_1e3", sum2d((56, 60, 64), 0.0005, seed=51), ["-M", "REL", "1e-3"], None))
+    out.append(("sz3_lorenzo_1e2", sum2d((56, 60, 64), 0.0005, seed=52), ["-M", "REL", "1e-2"], None))
+    out.append(("sz3_lorenzo_abs", sum2d((56, 60, 64), 0.001, seed=53), ["-M", "ABS", "0.02"], None))
+    out.append(("sz3_lorenzo_f64_16384", sum2d((56, 60, 64), 1e-8, seed=54, dtype=np.float64),
+                ["-M", "REL", "5e-7"], None))
+    # explicit Lorenzo / regression fast frontend
+    lor = {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {}}
+    out.append(("lorreg_default", spectral_field((40, 44, 52), slope=-3.0, seed=55), ["-M", "REL", "1e-3"], lor))
+    out.append(("lorreg_l2_bs4", spectral_field((37, 41, 29), slope=-2.5, seed=56), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
+                 "AlgoSettings": {"Lorenzo2ndOrder": "YES", "BlockSize": "4"}}))
+    out.append(("lor_only_f64", spectral_field((30, 33, 35), slope=-3.0, seed=57, dtype=np.float64),
+                ["-M", "REL", "1e-4"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {"Regression": "NO"}}))
     return out
+
+
+def sum2d(shape, noise, seed, dtype=np.float32):
+    """f(i,j) + g(j,k) + h(i,k) plus white noise of `noise` x range."""
+    rng = np.random.default_rng(seed)
+    f = rng.standard_normal((shape[0], shape[1], 1))
+    g = rng.standard_normal((1, shape[1], shape[2]))
+    h = rng.standard_normal((shape[0], 1, shape[2]))
+    base = f + g + h
+    return (base + noise * rng.standard_normal(shape) * (base.max() - base.min())).astype(dtype)
 
 
 def write_ini(path, d):
@@ -106,11 +137,21 @@ def sha(path):
     return hashlib.sha256(open(path, "rb").read()).hexdigest()
 
 
-def main():
+def main(only=None):
+    """Generate every case, or (names given on the command line) only those,
+    replacing their manifest entries."""
     if not os.path.exists(FAZ):
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
     manifest = []
+    old = {}
+    mpath = os.path.join(HERE, "manifest.json")
+    if only and os.path.exists(mpath):
+        old = {c["name"]: c for c in json.load(open(mpath))["cases"]}
     for name, arr, flags, ini in cases():
+        if only and name not in only:
+            if name in old:
+                manifest.append(old[name])
+            continue
         arr = np.ascontiguousarray(arr)
         dims = list(arr.shape)
         inp = os.path.join(HERE, name + ".in")
@@ -142,4 +183,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

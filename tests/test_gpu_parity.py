@@ -21,9 +21,19 @@ pytestmark = pytest.mark.gpu
 # cases outside the GPU path: 4-D fields, and fixBlockSize values that break
 # the coarse-lattice alignment of blocks
 GPU_UNSUPPORTED = {"c4d_cubic", "c3d_fixbs8"}
-INI_CASES = [c["name"] for c in golden_manifest() if c["ini"] is not None and c["name"] not in GPU_UNSUPPORTED]
-TUNED_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None]
-DEC_CASES = [c["name"] for c in golden_manifest() if c["name"] not in GPU_UNSUPPORTED]
+ALGO_INTERP = 2
+
+
+def _trailer_algo(name):
+    return O.read_stream(golden_stream(golden_case(name)))[0].cmprAlgo
+
+
+# interpolation streams (ALGO_INTERP in the trailer)
+_INTERP = {c["name"] for c in golden_manifest() if _trailer_algo(c["name"]) == ALGO_INTERP}
+INI_CASES = [c["name"] for c in golden_manifest()
+             if c["ini"] is not None and c["name"] not in GPU_UNSUPPORTED and c["name"] in _INTERP]
+TUNED_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None and c["name"] in _INTERP]
+DEC_CASES = [c["name"] for c in golden_manifest() if c["name"] not in GPU_UNSUPPORTED and c["name"] in _INTERP]
 
 
 @pytest.fixture(scope="module", autouse=True)

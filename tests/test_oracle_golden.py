@@ -11,13 +11,22 @@ import os
 import numpy as np
 import pytest
 
-from conftest import (cli_config, golden_case, golden_input, golden_manifest, golden_stream, mask_first_size,
-                      tuned_config)
+from conftest import (cli_config, golden_case, golden_input, golden_manifest, golden_stream,
+                      mask_fast_frontend_padding, mask_first_size, tuned_config)
 
 import oracle.oracle as O
 
+ALGO_INTERP, ALGO_LORENZO_REG = 2, 0
+
+
+def _trailer_algo(name):
+    return O.read_stream(golden_stream(golden_case(name)))[0].cmprAlgo
+
+
 INI_CASES = [c["name"] for c in golden_manifest() if c["ini"] is not None]
-TUNED_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None]
+TUNED_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None and _trailer_algo(c["name"]) == ALGO_INTERP]
+# default configuration (ALGO_INTERP_LORENZO) without QoZ tuning: the SZ3 tuner
+SZ3_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None and "-q" not in c["flags"]]
 ALL_CASES = [c["name"] for c in golden_manifest()]
 
 
@@ -32,12 +41,21 @@ def zstd_lib():
     O.set_zstd(None)
 
 
-def _same_stream(ours, ref, zstd_lib):
+def _same_stream(ours, ref, zstd_lib, itemsize=4):
+    c1, p1 = O.read_stream(ours)
+    c2, p2 = O.read_stream(ref)
+    assert c1.cmprAlgo == c2.cmprAlgo
+    if c1.cmprAlgo == ALGO_LORENZO_REG:
+        # the reference writes uninitialised struct padding into these
+        # payloads, so their zstd frames differ; payload and trailer must not
+        assert mask_fast_frontend_padding(p1, itemsize) == mask_fast_frontend_padding(p2, itemsize)
+        n1 = int.from_bytes(ours[-4:], "little", signed=True)
+        n2 = int.from_bytes(ref[-4:], "little", signed=True)
+        assert mask_first_size(ours)[-4 - n1:] == mask_first_size(ref)[-4 - n2:]
+        return
     if zstd_lib == "1.4.5":
         assert mask_first_size(ours) == mask_first_size(ref)
     else:
-        c1, p1 = O.read_stream(ours)
-        c2, p2 = O.read_stream(ref)
         assert p1 == p2
         # trailer bytes
         n1 = int.from_bytes(ours[-4:], "little", signed=True)
@@ -48,8 +66,24 @@ def _same_stream(ours, ref, zstd_lib):
 @pytest.mark.parametrize("name", INI_CASES)
 def test_oracle_stream_matches_reference(name, zstd_lib):
     case = golden_case(name)
-    stream, _ = O.compress(cli_config(case), golden_input(case))
-    _same_stream(stream, golden_stream(case), zstd_lib)
+    x = golden_input(case)
+    stream, _ = O.compress(cli_config(case), x)
+    _same_stream(stream, golden_stream(case), zstd_lib, x.itemsize)
+
+
+@pytest.mark.parametrize("name", SZ3_CASES)
+def test_oracle_sz3_tuner_matches_reference(name, zstd_lib):
+    """The whole default path: tuner decisions, then the chosen compressor."""
+    case = golden_case(name)
+    x = golden_input(case)
+    ref = golden_stream(case)
+    rc, _ = O.read_stream(ref)
+    tuned = O.sz3_tune(cli_config(case), x)
+    for f in ("cmprAlgo", "interpAlgo", "interpDirection", "quantbinCnt", "blockSize", "pred_dim", "lorenzo",
+              "lorenzo2", "regression"):
+        assert getattr(tuned, f) == getattr(rc, f), f
+    stream, _ = O.compress(cli_config(case), x)
+    _same_stream(stream, ref, zstd_lib, x.itemsize)
 
 
 @pytest.mark.parametrize("name", TUNED_CASES)
