@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "host.h"
 #include "internal.h"
 
 namespace faz {
@@ -29,122 +30,6 @@ namespace faz {
 const char *last_error();
 
 namespace {
-
-using clk = std::chrono::steady_clock;
-double ms_since(clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); }
-
-struct Fail {
-    int code;
-    std::string msg;
-};
-
-#define CK(call)                                                                              \
-    do {                                                                                      \
-        cudaError_t _e = (call);                                                              \
-        if (_e != cudaSuccess) throw Fail{FAZ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)}; \
-    } while (0)
-
-// ----------------------------------------------------- memory management
-// Device memory comes from the stream-ordered pool (cached across calls);
-// pinned host staging is cached per thread and grows on demand.
-struct DevMem {
-    cudaStream_t st;
-    std::vector<void *> ptrs;
-    explicit DevMem(cudaStream_t s) : st(s) {}
-    template <typename T>
-    T *alloc(size_t count) {
-        void *p = nullptr;
-        size_t bytes = count * sizeof(T);
-        if (bytes == 0) bytes = 16;
-        CK(cudaMallocAsync(&p, bytes, st));
-        ptrs.push_back(p);
-        return (T *)p;
-    }
-    ~DevMem() {
-        for (void *p : ptrs) cudaFreeAsync(p, st);
-    }
-};
-
-void init_pool_once() {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaMemPool_t pool;
-        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-            uint64_t thr = UINT64_MAX;
-            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-        }
-    });
-}
-
-struct Pinned {
-    uint8_t *p = nullptr;
-    size_t cap = 0;
-    uint8_t *get(size_t n) {
-        if (n > cap) {
-            if (p) cudaFreeHost(p);
-            p = nullptr;
-            cap = 0;
-            size_t c = std::max<size_t>(n + n / 4, 1 << 20);
-            if (cudaHostAlloc((void **)&p, c, cudaHostAllocDefault) != cudaSuccess)
-                throw Fail{FAZ_ERR_CUDA, "cudaHostAlloc failed"};
-            cap = c;
-        }
-        return p;
-    }
-    ~Pinned() {
-        if (p) cudaFreeHost(p);
-    }
-};
-thread_local Pinned t_pin_payload;
-thread_local Pinned t_pin_small;
-
-struct StreamGuard {
-    cudaStream_t st = nullptr;
-    bool own = false;
-    explicit StreamGuard(void *user) {
-        if (user) {
-            st = (cudaStream_t)user;
-        } else {
-            CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-            own = true;
-        }
-    }
-    ~StreamGuard() {
-        if (own) cudaStreamDestroy(st);
-    }
-};
-
-struct Events {
-    cudaEvent_t a = nullptr, b = nullptr;
-    Events() {
-        cudaEventCreate(&a);
-        cudaEventCreate(&b);
-    }
-    ~Events() {
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
-    }
-    float ms() {
-        float t = 0;
-        cudaEventElapsedTime(&t, a, b);
-        return t;
-    }
-};
-
-template <typename V>
-void put(std::vector<uint8_t> &o, V v) {
-    uint8_t b[sizeof(V)];
-    std::memcpy(b, &v, sizeof(V));
-    o.insert(o.end(), b, b + sizeof(V));
-}
-void put_be32(std::vector<uint8_t> &o, int32_t v) {
-    o.push_back((uint8_t)(v >> 24));
-    o.push_back((uint8_t)(v >> 16));
-    o.push_back((uint8_t)(v >> 8));
-    o.push_back((uint8_t)v);
-}
 
 // --------------------------------------------------------------- geometry
 struct LevelPlan {
@@ -196,35 +81,6 @@ double level_eb(double eb, double alpha, double beta, int level) {
     double cr = 1 - (level - 1) * alpha;
     if (cr < beta) cr = beta;
     return eb * cr;
-}
-
-// Float-pair split of eb and 1/eb for the exact float quantiser (interp.cu).
-// Enabled for float data with eb within [2^-60, 2^60]; FAZ_FASTPATH=0 turns it off.
-template <typename T>
-void set_fast_path(LevelArgs &a) {
-    a.fast = 0;
-    if (sizeof(T) != 4) return;
-    const char *env = std::getenv("FAZ_FASTPATH");
-    if (env && env[0] == '0') return;
-    if (!(a.eb >= 0x1p-60 && a.eb <= 0x1p60)) return;
-    a.eh = (float)a.eb;
-    a.el = (float)(a.eb - (double)a.eh);
-    a.rh = (float)a.recip;
-    a.rl = (float)(a.recip - (double)a.rh);
-    float lo = (float)a.eb;
-    if ((double)lo > a.eb) lo = std::nextafter(lo, 0.0f);
-    a.eblo = lo;
-    a.twor_f = (float)(2 * a.radius);
-    // d < eb * (1 - 2^-20) gives d * (1/eb) < 1 - 2^-20 + 2^-52, so floor(x) = 0
-    a.eb_half0 = (float)(a.eb * (1.0 - 0x1p-20));
-    if ((double)a.eb_half0 > a.eb * (1.0 - 0x1p-20)) a.eb_half0 = std::nextafter(a.eb_half0, 0.0f);
-    if (a.radius == 1) a.eb_half0 = 0.0f;  // code 1 may be unpredictable under trimToZero 2
-    a.fast = 1;
-}
-
-bool verify_fast_path() {
-    const char *env = std::getenv("FAZ_VERIFY_FASTPATH");
-    return env && env[0] == '1';
 }
 
 template <typename T>
@@ -331,22 +187,7 @@ Plan make_plan(int N, const uint64_t *dims, uint64_t maxStep, int blocksize, int
     return p;
 }
 
-size_t smem_limit() {
-    int dev = 0, v = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    return (size_t)v;
-}
-
 // --------------------------------------------------------------- compress
-struct Counter {
-    uint64_t n = 0;
-    void operator()(cudaError_t e) {
-        if (e != cudaSuccess) throw Fail{FAZ_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e)};
-        n++;
-    }
-};
-
 void check_config(const faz_config &c) {
     if (c.N < 1 || c.N > 4) throw Fail{FAZ_ERR_ARG, "N must be 1..4"};
     uint64_t num = 1;
@@ -427,6 +268,85 @@ struct Sink {
     bool too_small = false;
 };
 
+}  // namespace
+
+// Histogram, codebook (host) and Huffman encoding of n codes on the device
+// (HuffmanEncoder::preprocess_encode + encode, HuffmanEncoder.hpp:93-227).
+// `center` is the code the histogram's shared-memory window is centred on.
+void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
+                           Counter &launches, HuffEncoded &h, faz_timings &tm) {
+    const uint64_t nsub = hist_subchunks(n);
+    const int nsym = 65536;
+    unsigned long long *hist = m.alloc<unsigned long long>(nsym);
+    unsigned long long *first = m.alloc<unsigned long long>(nsym);
+    h.zc = m.alloc<unsigned long long>(nsub + 1);
+    h.zoff = m.alloc<unsigned long long>(nsub + 1);
+    unsigned long long *stmp = m.alloc<unsigned long long>(scan_temp_words(std::max<uint64_t>(nsub, encode_chunks(n))) + 1);
+    CK(cudaMemsetAsync(hist, 0, nsym * 8, st));
+    CK(cudaMemsetAsync(first, 0xff, nsym * 8, st));
+    launches(launch_histogram(codes, n, center, hist, first, h.zc, st));
+    launches(launch_scan_u64(h.zc, h.zoff, nsub, stmp, st));
+    uint8_t *hb = t_pin_small.get((size_t)nsym * 16 + 8);
+    CK(cudaMemcpyAsync(hb, hist, nsym * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hb + nsym * 8, first, nsym * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hb + nsym * 16, h.zoff + nsub, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    auto th1 = clk::now();
+    const unsigned long long *hh = (const unsigned long long *)hb;
+    const unsigned long long *hf = (const unsigned long long *)(hb + nsym * 8);
+    std::memcpy(&h.nzero, hb + nsym * 16, 8);
+    std::vector<int> syms;
+    std::vector<uint64_t> cnts, firsts;
+    for (int s = 0; s < nsym; s++)
+        if (hh[s]) {
+            syms.push_back(s);
+            cnts.push_back(hh[s]);
+            firsts.push_back(hf[s]);
+        }
+    std::string err;
+    int rc = build_codebook(syms, cnts, firsts, h.cb, err);
+    if (rc) throw Fail{rc, err};
+    tm.host_ms += ms_since(th1);
+    const Codebook &cb = h.cb;
+    unsigned long long *dcode = m.alloc<unsigned long long>(cb.stateNum);
+    unsigned long long *dpacked = m.alloc<unsigned long long>(cb.stateNum);
+    uint8_t *dlen = m.alloc<uint8_t>(cb.stateNum);
+    std::vector<unsigned long long> packed(cb.stateNum);
+    for (int i = 0; i < cb.stateNum; i++) {
+        const int l = cb.len[i];
+        packed[i] = ((unsigned long long)l << 32) | (l >= 1 && l <= 32 ? (cb.code[i] >> (64 - l)) : 0ull);
+    }
+    CK(cudaMemcpyAsync(dcode, cb.code.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dpacked, packed.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dlen, cb.len.data(), cb.stateNum, cudaMemcpyHostToDevice, st));
+    const uint64_t nech = encode_chunks(n);
+    unsigned long long *cbits = m.alloc<unsigned long long>(nech + 1);
+    unsigned long long *coff = m.alloc<unsigned long long>(nech + 1);
+    launches(launch_encode_bits(codes, n, cb.offset, dlen, cbits, st));
+    launches(launch_scan_u64(cbits, coff, nech, stmp, st));
+    uint64_t total_bits;
+    CK(cudaMemcpyAsync(hb, coff + nech, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::memcpy(&total_bits, hb, 8);
+    h.nbytes = (total_bits + 7) / 8;
+    const uint64_t nwords = (total_bits + 31) / 32 + 1;
+    h.bits = m.alloc<uint32_t>(nwords);
+    CK(cudaMemsetAsync(h.bits, 0, nwords * 4, st));
+    if (total_bits)
+        launches(launch_encode_pack(codes, n, cb.offset, dcode, dpacked, dlen, coff, h.bits, std::max(cb.maxlen, 1), st));
+}
+
+// HuffmanEncoder::save header + tree, then the encoded size (HuffmanEncoder.hpp:119-137, 150-227)
+void append_tree(std::vector<uint8_t> &o, const Codebook &cb, uint64_t nbytes) {
+    put<int32_t>(o, cb.offset);
+    put_be32(o, cb.nodeCount);
+    put_be32(o, cb.stateNum / 2);
+    o.insert(o.end(), cb.tree.begin(), cb.tree.end());
+    put<uint64_t>(o, nbytes);
+}
+
+namespace {
+
 template <typename T>
 void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&payload, size_t &psize,
                       faz_timings &tm, Counter &launches, Sink *sink = nullptr) {
@@ -475,76 +395,20 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     CK(cudaEventRecord(ev_fin.b, st));
     CK(cudaEventRecord(ev_pred.b, st));
     CK(cudaEventRecord(ev_huff.a, st));
-    // histogram
-    const uint64_t nsub = hist_subchunks(n);
-    const int nsym = 65536;
-    unsigned long long *hist = m.alloc<unsigned long long>(nsym);
-    unsigned long long *first = m.alloc<unsigned long long>(nsym);
-    unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1);
-    unsigned long long *zoff = m.alloc<unsigned long long>(nsub + 1);
-    unsigned long long *stmp = m.alloc<unsigned long long>(scan_temp_words(std::max<uint64_t>(nsub, encode_chunks(n))) + 1);
-    CK(cudaMemsetAsync(hist, 0, nsym * 8, st));
-    CK(cudaMemsetAsync(first, 0xff, nsym * 8, st));
-    launches(launch_histogram(codes, n, radius, hist, first, zc, st));
-    launches(launch_scan_u64(zc, zoff, nsub, stmp, st));
-    uint8_t *hb = t_pin_small.get((size_t)nsym * 16 + 8);
-    CK(cudaMemcpyAsync(hb, hist, nsym * 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(hb + nsym * 8, first, nsym * 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(hb + nsym * 16, zoff + nsub, 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    auto th1 = clk::now();
-    const unsigned long long *hh = (const unsigned long long *)hb;
-    const unsigned long long *hf = (const unsigned long long *)(hb + nsym * 8);
-    uint64_t nunpred;
-    std::memcpy(&nunpred, hb + nsym * 16, 8);
+    HuffEncoded he;
+    huffman_encode_device(codes, n, radius, m, st, launches, he, tm);
     if (vcount) {
         unsigned long long vc = 0;
         CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
         if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
     }
-    std::vector<int> syms;
-    std::vector<uint64_t> cnts, firsts;
-    for (int s = 0; s < nsym; s++)
-        if (hh[s]) {
-            syms.push_back(s);
-            cnts.push_back(hh[s]);
-            firsts.push_back(hf[s]);
-        }
-    Codebook cb;
-    std::string err;
-    int rc = build_codebook(syms, cnts, firsts, cb, err);
-    if (rc) throw Fail{rc, err};
-    tm.host_ms += ms_since(th1);
+    const uint64_t nunpred = he.nzero;
+    const Codebook &cb = he.cb;
+    const uint64_t nbytes = he.nbytes;
+    uint32_t *bits = he.bits;
     // unpredictable values in stream order
     T *unpred = m.alloc<T>(nunpred ? nunpred : 1);
-    if (nunpred) launches(launch_compact_zeros<T>(codes, n, zc, zoff, nullptr, scratch, unpred, st));
-    // Huffman encode
-    unsigned long long *dcode = m.alloc<unsigned long long>(cb.stateNum);
-    unsigned long long *dpacked = m.alloc<unsigned long long>(cb.stateNum);
-    uint8_t *dlen = m.alloc<uint8_t>(cb.stateNum);
-    std::vector<unsigned long long> packed(cb.stateNum);
-    for (int i = 0; i < cb.stateNum; i++) {
-        const int l = cb.len[i];
-        packed[i] = ((unsigned long long)l << 32) | (l >= 1 && l <= 32 ? (cb.code[i] >> (64 - l)) : 0ull);
-    }
-    CK(cudaMemcpyAsync(dcode, cb.code.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(dpacked, packed.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(dlen, cb.len.data(), cb.stateNum, cudaMemcpyHostToDevice, st));
-    const uint64_t nech = encode_chunks(n);
-    unsigned long long *cbits = m.alloc<unsigned long long>(nech + 1);
-    unsigned long long *coff = m.alloc<unsigned long long>(nech + 1);
-    launches(launch_encode_bits(codes, n, cb.offset, dlen, cbits, st));
-    launches(launch_scan_u64(cbits, coff, nech, stmp, st));
-    uint64_t total_bits;
-    CK(cudaMemcpyAsync(hb, coff + nech, 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    std::memcpy(&total_bits, hb, 8);
-    const uint64_t nbytes = (total_bits + 7) / 8;
-    const uint64_t nwords = (total_bits + 31) / 32 + 1;
-    uint32_t *bits = m.alloc<uint32_t>(nwords);
-    CK(cudaMemsetAsync(bits, 0, nwords * 4, st));
-    if (total_bits)
-        launches(launch_encode_pack(codes, n, cb.offset, dcode, dpacked, dlen, coff, bits, std::max(cb.maxlen, 1), st));
+    if (nunpred) launches(launch_compact_zeros<T>(codes, n, he.zc, he.zoff, nullptr, scratch, unpred, st));
     CK(cudaEventRecord(ev_huff.b, st));
     // payload layout (SZInterpolationCompressor.hpp:485-512, IntegerQuantizer.hpp:185-201,
     // HuffmanEncoder.hpp:119-137 and 150-227)
@@ -570,11 +434,7 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     put<int32_t>(head, radius);
     put<uint64_t>(head, nunpred);
     std::vector<uint8_t> tree;
-    put<int32_t>(tree, cb.offset);
-    put_be32(tree, cb.nodeCount);
-    put_be32(tree, cb.stateNum / 2);
-    tree.insert(tree.end(), cb.tree.begin(), cb.tree.end());
-    put<uint64_t>(tree, nbytes);
+    append_tree(tree, cb, nbytes);
     psize = head.size() + nunpred * sizeof(T) + tree.size() + nbytes;
     if (sink && sink->dst) {
         if (psize > sink->cap) {
@@ -786,6 +646,101 @@ void parse_payload(const uint8_t *pl, size_t n, int N, Parsed &P) {
     P.unpred = p;
 }
 
+}  // namespace
+
+// HuffmanEncoder::load + decode (HuffmanEncoder.hpp:236-296) on the device:
+// reads the tree and bit string at p (advancing it) and writes num codes.
+void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, uint16_t *codes, DevMem &m,
+                           cudaStream_t st, Counter &launches) {
+    DecodeTablesHost t;
+    std::string err;
+    int rc = parse_tree(p, end, t, err);
+    if (rc) throw Fail{rc, err};
+    if ((size_t)(end - p) < 8) throw Fail{FAZ_ERR_FORMAT, "truncated stream header"};
+    uint64_t nbytes;
+    std::memcpy(&nbytes, p, 8);
+    p += 8;
+    if ((size_t)(end - p) < nbytes) throw Fail{FAZ_ERR_FORMAT, "truncated Huffman bits"};
+    const uint8_t *hbits = p;
+    p += nbytes;
+    if (t.constant || nbytes == 0) {
+        int v = t.constant_state + t.offset;
+        launches(launch_fill_u16(codes, num, (uint16_t)v, st));
+        return;
+    }
+    const uint64_t nwords = (nbytes + 3) / 4;
+    uint32_t *dbits = m.alloc<uint32_t>(nwords + 16);
+    CK(cudaMemsetAsync(dbits, 0, (nwords + 16) * 4, st));
+    CK(cudaMemcpyAsync(dbits, hbits, nbytes, cudaMemcpyHostToDevice, st));
+    uint32_t *lut = m.alloc<uint32_t>(t.lut.size());
+    uint32_t *dl = m.alloc<uint32_t>(t.nodeCount), *dr = m.alloc<uint32_t>(t.nodeCount);
+    int32_t *ds = m.alloc<int32_t>(t.nodeCount);
+    uint8_t *dleaf = m.alloc<uint8_t>(t.nodeCount);
+    CK(cudaMemcpyAsync(lut, t.lut.data(), t.lut.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dl, t.left.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dr, t.right.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ds, t.sym.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dleaf, t.leaf.data(), t.nodeCount, cudaMemcpyHostToDevice, st));
+    DecodeTablesDev td{lut, dl, dr, ds, dleaf};
+    const uint64_t nbits = nbytes * 8;
+    const uint64_t nunits = decode_units(nbits);
+    uint64_t *start = m.alloc<uint64_t>(nunits);
+    uint64_t *ea = m.alloc<uint64_t>(nunits), *eb2 = m.alloc<uint64_t>(nunits);
+    unsigned int *cnt = m.alloc<unsigned int>(nunits);
+    uint16_t *bnd = m.alloc<uint16_t>(nunits * decode_boundaries());
+    unsigned long long *cnt64 = m.alloc<unsigned long long>(nunits + 1);
+    unsigned long long *off = m.alloc<unsigned long long>(nunits + 1);
+    unsigned long long *dtmp = m.alloc<unsigned long long>(scan_temp_words(nunits) + 1);
+    int *flags = m.alloc<int>(2);  // [0] changed, [1] damaged tree
+    CK(cudaMemsetAsync(flags, 0, 8, st));
+    launches(launch_init_starts(start, nunits, st));
+    launches(launch_decode_spec(td, dbits, nwords, nbits, nunits, ea, cnt, bnd, flags + 1, st));
+    int *hflag = (int *)t_pin_small.get(64);
+    bool converged = false;
+    for (int it = 0; it < 1024; it++) {
+        CK(cudaMemsetAsync(flags, 0, 4, st));
+        launches(launch_decode_resync(td, dbits, nwords, nbits, nunits, ea, eb2, cnt, bnd, start, flags, st));
+        CK(cudaMemcpyAsync(hflag, flags, 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::swap(ea, eb2);
+        if (hflag[0] < 0 || hflag[1]) throw Fail{FAZ_ERR_FORMAT, "Huffman stream decodes outside the tree"};
+        if (hflag[0] == 0) {
+            converged = true;
+            break;
+        }
+    }
+    if (!converged) throw Fail{FAZ_ERR_UNSUPPORTED, "Huffman stream did not synchronise within 1024 passes"};
+    launches(launch_widen_counts(cnt, cnt64, nunits, st));
+    launches(launch_scan_u64(cnt64, off, nunits, dtmp, st));
+    uint64_t total;
+    CK(cudaMemcpyAsync(hflag, off + nunits, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::memcpy(&total, hflag, 8);
+    if (total < num) throw Fail{FAZ_ERR_FORMAT, "Huffman stream holds fewer symbols than the field"};
+    launches(launch_decode_write(td, dbits, nwords, nbits, nunits, start, off, num, t.offset, codes, st));
+}
+
+// Sorted positions of the zero codes (the unpredictable points); returns
+// their count.
+uint64_t zero_positions(const uint16_t *codes, uint64_t num, DevMem &m, cudaStream_t st, Counter &launches,
+                        uint64_t *&zpos) {
+    const uint64_t nsub = hist_subchunks(num);
+    unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1);
+    unsigned long long *zoff = m.alloc<unsigned long long>(nsub + 1);
+    unsigned long long *ztmp = m.alloc<unsigned long long>(scan_temp_words(nsub) + 1);
+    launches(launch_count_zeros(codes, num, zc, st));
+    launches(launch_scan_u64(zc, zoff, nsub, ztmp, st));
+    uint64_t *hz = (uint64_t *)t_pin_small.get(64);
+    CK(cudaMemcpyAsync(hz, zoff + nsub, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const uint64_t nz = *hz;
+    zpos = m.alloc<uint64_t>(nz ? nz : 1);
+    if (nz) launches(launch_compact_zeros<float>(codes, num, zc, zoff, zpos, nullptr, nullptr, st));
+    return nz;
+}
+
+namespace {
+
 template <typename T>
 void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStream_t st, faz_timings &tm,
                        Counter &launches) {
@@ -793,12 +748,6 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
     const uint8_t *p = P.unpred;
     if ((size_t)(end - p) / sizeof(T) < P.nunpred) throw Fail{FAZ_ERR_FORMAT, "truncated unpredictable values"};
     p += P.nunpred * sizeof(T);
-    std::string err;
-    int rc = parse_tree(p, end, P.tables, err);
-    if (rc) throw Fail{rc, err};
-    P.nbytes = rd<uint64_t>(p, end);
-    if ((size_t)(end - p) < P.nbytes) throw Fail{FAZ_ERR_FORMAT, "truncated Huffman bits"};
-    P.bits = p;
     if (!(P.eb > 0)) throw Fail{FAZ_ERR_FORMAT, "bad error bound"};
     Plan pl_ = make_plan<T>(P.N, P.dims, P.maxStep, (int)P.blocksize, P.fixbs, P.interp, P.dir, P.il, P.dl, P.eb, P.alpha,
                             P.beta, P.radius, P.trim, smem_limit());
@@ -807,81 +756,15 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
     uint16_t *codes = m.alloc<uint16_t>(num);
     T *dunpred = m.alloc<T>(P.nunpred ? P.nunpred : 1);
     if (P.nunpred) CK(cudaMemcpyAsync(dunpred, P.unpred, P.nunpred * sizeof(T), cudaMemcpyHostToDevice, st));
-    const auto &t = P.tables;
     Events ev_dec, ev_pred, ev_fin;
     CK(cudaEventRecord(ev_dec.a, st));
-    if (t.constant || P.nbytes == 0) {
-        int v = t.constant_state + t.offset;
-        launches(launch_fill_u16(codes, num, (uint16_t)v, st));
-    } else {
-        const uint64_t nwords = (P.nbytes + 3) / 4;
-        uint32_t *dbits = m.alloc<uint32_t>(nwords + 16);
-        CK(cudaMemsetAsync(dbits, 0, (nwords + 16) * 4, st));
-        CK(cudaMemcpyAsync(dbits, P.bits, P.nbytes, cudaMemcpyHostToDevice, st));
-        uint32_t *lut = m.alloc<uint32_t>(t.lut.size());
-        uint32_t *dl = m.alloc<uint32_t>(t.nodeCount), *dr = m.alloc<uint32_t>(t.nodeCount);
-        int32_t *ds = m.alloc<int32_t>(t.nodeCount);
-        uint8_t *dleaf = m.alloc<uint8_t>(t.nodeCount);
-        CK(cudaMemcpyAsync(lut, t.lut.data(), t.lut.size() * 4, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(dl, t.left.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(dr, t.right.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(ds, t.sym.data(), t.nodeCount * 4, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(dleaf, t.leaf.data(), t.nodeCount, cudaMemcpyHostToDevice, st));
-        DecodeTablesDev td{lut, dl, dr, ds, dleaf};
-        const uint64_t nbits = P.nbytes * 8;
-        const uint64_t nunits = decode_units(nbits);
-        uint64_t *start = m.alloc<uint64_t>(nunits);
-        uint64_t *ea = m.alloc<uint64_t>(nunits), *eb2 = m.alloc<uint64_t>(nunits);
-        unsigned int *cnt = m.alloc<unsigned int>(nunits);
-        uint16_t *bnd = m.alloc<uint16_t>(nunits * decode_boundaries());
-        unsigned long long *cnt64 = m.alloc<unsigned long long>(nunits + 1);
-        unsigned long long *off = m.alloc<unsigned long long>(nunits + 1);
-        unsigned long long *dtmp = m.alloc<unsigned long long>(scan_temp_words(nunits) + 1);
-        int *flags = m.alloc<int>(2);  // [0] changed, [1] damaged tree
-        CK(cudaMemsetAsync(flags, 0, 8, st));
-        launches(launch_init_starts(start, nunits, st));
-        launches(launch_decode_spec(td, dbits, nwords, nbits, nunits, ea, cnt, bnd, flags + 1, st));
-        int *hflag = (int *)t_pin_small.get(64);
-        bool converged = false;
-        for (int it = 0; it < 1024; it++) {
-            CK(cudaMemsetAsync(flags, 0, 4, st));
-            launches(launch_decode_resync(td, dbits, nwords, nbits, nunits, ea, eb2, cnt, bnd, start, flags, st));
-            CK(cudaMemcpyAsync(hflag, flags, 8, cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            std::swap(ea, eb2);
-            if (hflag[0] < 0 || hflag[1]) throw Fail{FAZ_ERR_FORMAT, "Huffman stream decodes outside the tree"};
-            if (hflag[0] == 0) {
-                converged = true;
-                break;
-            }
-        }
-        if (!converged) throw Fail{FAZ_ERR_UNSUPPORTED, "Huffman stream did not synchronise within 1024 passes"};
-        launches(launch_widen_counts(cnt, cnt64, nunits, st));
-        launches(launch_scan_u64(cnt64, off, nunits, dtmp, st));
-        uint64_t total;
-        CK(cudaMemcpyAsync(hflag, off + nunits, 8, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        std::memcpy(&total, hflag, 8);
-        if (total < num) throw Fail{FAZ_ERR_FORMAT, "Huffman stream holds fewer symbols than the field"};
-        launches(launch_decode_write(td, dbits, nwords, nbits, nunits, start, off, num, t.offset, codes, st));
-    }
+    huffman_decode_device(p, end, num, codes, m, st, launches);
     CK(cudaEventRecord(ev_dec.b, st));
     // zero positions for the unpredictable values
-    const uint64_t nsub = hist_subchunks(num);
-    unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1);
-    unsigned long long *zoff = m.alloc<unsigned long long>(nsub + 1);
-    unsigned long long *ztmp = m.alloc<unsigned long long>(scan_temp_words(nsub) + 1);
-    launches(launch_count_zeros(codes, num, zc, st));
-    launches(launch_scan_u64(zc, zoff, nsub, ztmp, st));
-    uint64_t nz;
-    uint64_t *hz = (uint64_t *)t_pin_small.get(64);
-    CK(cudaMemcpyAsync(hz, zoff + nsub, 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    nz = *hz;
+    uint64_t *zpos = nullptr;
+    const uint64_t nz = zero_positions(codes, num, m, st, launches, zpos);
     if (nz != P.nunpred)
         throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
-    uint64_t *zpos = m.alloc<uint64_t>(nz ? nz : 1);
-    if (nz) launches(launch_compact_zeros<T>(codes, num, zc, zoff, zpos, nullptr, nullptr, st));
     if (!pl_.anchor) {
         launches(launch_first_point<T>(true, nullptr, dOut, codes, nullptr, P.eb, P.radius, P.trim, zpos, nz, dunpred, st));
     } else {

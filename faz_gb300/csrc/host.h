@@ -1,0 +1,199 @@
+// host.h - host-side utilities shared by the library's orchestration files:
+// error type, device memory from the stream-ordered pool, cached pinned
+// staging, stream/event guards, launch counting, byte packing and the float
+// quantiser's parameter split.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace faz {
+
+using clk = std::chrono::steady_clock;
+inline double ms_since(clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); }
+
+struct Fail {
+    int code;
+    std::string msg;
+};
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t _e = (call);                                                              \
+        if (_e != cudaSuccess) throw Fail{FAZ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)}; \
+    } while (0)
+
+// ----------------------------------------------------- memory management
+// Device memory comes from the stream-ordered pool (cached across calls);
+// pinned host staging is cached per thread and grows on demand.
+struct DevMem {
+    cudaStream_t st;
+    std::vector<void *> ptrs;
+    explicit DevMem(cudaStream_t s) : st(s) {}
+    template <typename T>
+    T *alloc(size_t count) {
+        void *p = nullptr;
+        size_t bytes = count * sizeof(T);
+        if (bytes == 0) bytes = 16;
+        CK(cudaMallocAsync(&p, bytes, st));
+        ptrs.push_back(p);
+        return (T *)p;
+    }
+    ~DevMem() {
+        for (void *p : ptrs) cudaFreeAsync(p, st);
+    }
+};
+
+inline void init_pool_once() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    });
+}
+
+struct Pinned {
+    uint8_t *p = nullptr;
+    size_t cap = 0;
+    uint8_t *get(size_t n) {
+        if (n > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            cap = 0;
+            size_t c = std::max<size_t>(n + n / 4, 1 << 20);
+            if (cudaHostAlloc((void **)&p, c, cudaHostAllocDefault) != cudaSuccess)
+                throw Fail{FAZ_ERR_CUDA, "cudaHostAlloc failed"};
+            cap = c;
+        }
+        return p;
+    }
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+};
+inline thread_local Pinned t_pin_payload;
+inline thread_local Pinned t_pin_small;
+
+struct StreamGuard {
+    cudaStream_t st = nullptr;
+    bool own = false;
+    explicit StreamGuard(void *user) {
+        if (user) {
+            st = (cudaStream_t)user;
+        } else {
+            CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            own = true;
+        }
+    }
+    ~StreamGuard() {
+        if (own) cudaStreamDestroy(st);
+    }
+};
+
+struct Events {
+    cudaEvent_t a = nullptr, b = nullptr;
+    Events() {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    }
+    ~Events() {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    float ms() {
+        float t = 0;
+        cudaEventElapsedTime(&t, a, b);
+        return t;
+    }
+};
+
+template <typename V>
+void put(std::vector<uint8_t> &o, V v) {
+    uint8_t b[sizeof(V)];
+    std::memcpy(b, &v, sizeof(V));
+    o.insert(o.end(), b, b + sizeof(V));
+}
+inline void put_be32(std::vector<uint8_t> &o, int32_t v) {
+    o.push_back((uint8_t)(v >> 24));
+    o.push_back((uint8_t)(v >> 16));
+    o.push_back((uint8_t)(v >> 8));
+    o.push_back((uint8_t)v);
+}
+
+struct Counter {
+    uint64_t n = 0;
+    void operator()(cudaError_t e) {
+        if (e != cudaSuccess) throw Fail{FAZ_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e)};
+        n++;
+    }
+};
+
+// Float-pair split of eb and 1/eb for the exact float quantiser (interp.cu).
+// Enabled for float data with eb within [2^-60, 2^60]; FAZ_FASTPATH=0 turns it off.
+template <typename T>
+void set_fast_path(LevelArgs &a) {
+    a.fast = 0;
+    if (sizeof(T) != 4) return;
+    const char *env = std::getenv("FAZ_FASTPATH");
+    if (env && env[0] == '0') return;
+    if (!(a.eb >= 0x1p-60 && a.eb <= 0x1p60)) return;
+    a.eh = (float)a.eb;
+    a.el = (float)(a.eb - (double)a.eh);
+    a.rh = (float)a.recip;
+    a.rl = (float)(a.recip - (double)a.rh);
+    float lo = (float)a.eb;
+    if ((double)lo > a.eb) lo = std::nextafter(lo, 0.0f);
+    a.eblo = lo;
+    a.twor_f = (float)(2 * a.radius);
+    // d < eb * (1 - 2^-20) gives d * (1/eb) < 1 - 2^-20 + 2^-52, so floor(x) = 0
+    a.eb_half0 = (float)(a.eb * (1.0 - 0x1p-20));
+    if ((double)a.eb_half0 > a.eb * (1.0 - 0x1p-20)) a.eb_half0 = std::nextafter(a.eb_half0, 0.0f);
+    if (a.radius == 1) a.eb_half0 = 0.0f;  // code 1 may be unpredictable under trimToZero 2
+    a.fast = 1;
+}
+
+inline bool verify_fast_path() {
+    const char *env = std::getenv("FAZ_VERIFY_FASTPATH");
+    return env && env[0] == '1';
+}
+
+inline size_t smem_limit() {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return (size_t)v;
+}
+
+// ------------------------------------------------------- Huffman stages
+struct HuffEncoded {
+    Codebook cb;
+    uint32_t *bits = nullptr;  // device: the MSB-first bit string
+    uint64_t nbytes = 0;
+    uint64_t nzero = 0;        // codes equal to 0 (unpredictable points)
+    unsigned long long *zc = nullptr, *zoff = nullptr;  // zero counts per sub-chunk and their exclusive scan
+};
+void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
+                           Counter &launches, HuffEncoded &h, faz_timings &tm);
+void append_tree(std::vector<uint8_t> &o, const Codebook &cb, uint64_t nbytes);
+void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, uint16_t *codes, DevMem &m,
+                           cudaStream_t st, Counter &launches);
+uint64_t zero_positions(const uint16_t *codes, uint64_t num, DevMem &m, cudaStream_t st, Counter &launches,
+                        uint64_t *&zpos);
+
+}  // namespace faz
