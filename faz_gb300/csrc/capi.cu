@@ -197,8 +197,10 @@ void check_config(const faz_config &c) {
     }
     if (num != c.num) throw Fail{FAZ_ERR_ARG, "num does not match dims"};
     if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
-    if (c.cmprAlgo != FAZ_ALGO_INTERP)
-        throw Fail{FAZ_ERR_UNSUPPORTED, "only cmprAlgo = ALGO_INTERP is implemented on the GPU path"};
+    if (c.cmprAlgo != FAZ_ALGO_INTERP && c.cmprAlgo != FAZ_ALGO_INTERP_LORENZO && c.cmprAlgo != FAZ_ALGO_LORENZO_REG)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "cmprAlgo must be ALGO_INTERP, ALGO_INTERP_LORENZO or ALGO_LORENZO_REG"};
+    if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && (c.N != 3 || c.regression2))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG is implemented for 3-D data without regression2"};
     if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};
     if (c.wavelet != 0 || ((c.wavelet > 0 || c.sperrWithoutWave) && c.sperr >= c.wavelet))
         throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet / SPERR modes are not part of the interpolation path"};
@@ -207,30 +209,41 @@ void check_config(const faz_config &c) {
     if (c.interp_list_len < 0 || c.interp_list_len > FAZ_MAX_LEVELS) throw Fail{FAZ_ERR_ARG, "bad level list length"};
 }
 
+}  // namespace
+
+// data_range<T> (include/QoZ/utils/Statistic.hpp:12-21) on the device: max - min
+// in the element type.
+template <typename T>
+double device_range(const T *dX, uint64_t n, cudaStream_t st, Counter &launches) {
+    int nb = (int)std::min<uint64_t>(152 * 4, (n + 4095) / 4096);
+    if (nb < 1) nb = 1;
+    DevMem m(st);
+    T *pmin = m.alloc<T>(nb), *pmax = m.alloc<T>(nb);
+    launches(launch_minmax<T>(dX, n, pmin, pmax, nb, st));
+    std::vector<T> hmin(nb), hmax(nb);
+    CK(cudaMemcpyAsync(hmin.data(), pmin, nb * sizeof(T), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hmax.data(), pmax, nb * sizeof(T), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    T mn = hmin[0], mx = hmax[0];
+    for (int i = 0; i < nb; i++) {
+        if (hmin[i] < mn) mn = hmin[i];
+        if (hmax[i] > mx) mx = hmax[i];
+    }
+    T r = mx - mn;
+    return (double)r;
+}
+template double device_range<float>(const float *, uint64_t, cudaStream_t, Counter &);
+template double device_range<double>(const double *, uint64_t, cudaStream_t, Counter &);
+
+namespace {
+
 // calAbsErrorBound (include/QoZ/utils/Statistic.hpp:34-66); `rng` computed
 // on the device when the mode needs it.
 template <typename T>
 void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) {
     if (c.errorBoundMode == FAZ_EB_ABS) return;
     double rng = 0;
-    if (c.errorBoundMode != FAZ_EB_L2NORM) {
-        int nb = (int)std::min<uint64_t>(152 * 4, (c.num + 4095) / 4096);
-        if (nb < 1) nb = 1;
-        DevMem m(st);
-        T *pmin = m.alloc<T>(nb), *pmax = m.alloc<T>(nb);
-        launches(launch_minmax<T>(dX, c.num, pmin, pmax, nb, st));
-        std::vector<T> hmin(nb), hmax(nb);
-        CK(cudaMemcpyAsync(hmin.data(), pmin, nb * sizeof(T), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hmax.data(), pmax, nb * sizeof(T), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        T mn = hmin[0], mx = hmax[0];
-        for (int i = 0; i < nb; i++) {
-            if (hmin[i] < mn) mn = hmin[i];
-            if (hmax[i] > mx) mx = hmax[i];
-        }
-        T r = mx - mn;
-        rng = (double)r;
-    }
+    if (c.errorBoundMode != FAZ_EB_L2NORM) rng = device_range<T>(dX, c.num, st, launches);
     switch (c.errorBoundMode) {
     case FAZ_EB_REL:
         c.absErrorBound = c.relErrorBound * rng;
@@ -462,6 +475,37 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     (void)th0;
 }
 
+// SZ_compress_dispatcher (include/QoZ/api/impl/SZDispatcher.hpp:12-36): error
+// bound, the default configuration's tuner, then the chosen compressor.
+template <typename T>
+void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&payload, size_t &psize,
+                       faz_timings &tm, Counter &launches, Sink *sink = nullptr) {
+    resolve_eb<T>(c, dX, st, launches);
+    if (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))
+        throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
+    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) sz3_tune_device<T>(c, dX, st, launches, tm);
+    if (c.cmprAlgo == FAZ_ALGO_INTERP) {
+        compress_payload<T>(c, dX, st, payload, psize, tm, launches, sink);
+        return;
+    }
+    if (c.N != 3 || c.regression2)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG is implemented for 3-D data without regression2"};
+    std::vector<uint8_t> pl;
+    lorenzo3_compress_payload<T>(c.dims, c.blockSize, c.pred_dim, c.lorenzo, c.lorenzo2, c.regression,
+                                 c.absErrorBound, c.quantbinCnt / 2, dX, st, launches, tm, pl);
+    psize = pl.size();
+    if (sink && sink->dst) {
+        if (psize > sink->cap) {
+            sink->too_small = true;
+            throw Fail{FAZ_ERR_ARG, "payload buffer too small: need " + std::to_string(psize) + " bytes"};
+        }
+        payload = sink->dst;
+    } else {
+        payload = t_pin_payload.get(psize + 8);
+    }
+    std::memcpy(payload, pl.data(), psize);
+}
+
 // Lossless_zstd::compress framing (include/QoZ/lossless/Lossless_zstd.hpp:22-32),
 // then Config::save + int32 trailer size (include/QoZ/api/sz.hpp:77-91).
 void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, char **out, size_t *out_size,
@@ -515,7 +559,7 @@ int compress_payload_impl(const faz_config *conf_in, const void *d_data, void *u
         size_t psize;
         CK(cudaEventRecord(ev_gpu.a, sg.st));
         try {
-            compress_payload<T>(c, (const T *)d_data, sg.st, payload, psize, tm, launches, &sink);
+            compress_dispatch<T>(c, (const T *)d_data, sg.st, payload, psize, tm, launches, &sink);
         } catch (const Fail &f) {
             if (sink.too_small) *out_size = psize;
             throw;
@@ -567,7 +611,7 @@ int compress_impl(const faz_config *conf_in, const void *data, bool on_device, v
         uint8_t *payload;
         size_t psize;
         CK(cudaEventRecord(ev_gpu.a, st));
-        compress_payload<T>(c, dX, st, payload, psize, tm, launches);
+        compress_dispatch<T>(c, dX, st, payload, psize, tm, launches);
         CK(cudaEventRecord(ev_gpu.b, st));
         CK(cudaStreamSynchronize(st));
         if (!on_device) tm.h2d_ms = ev_h2d.ms();
@@ -849,17 +893,25 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
         uint8_t *payload;
         size_t psize;
         open_stream(cmp, cmp_size, c, payload, psize, tm);
-        if (c.cmprAlgo != FAZ_ALGO_INTERP)
-            throw Fail{FAZ_ERR_UNSUPPORTED, "only ALGO_INTERP streams are implemented on the GPU path"};
+        // SZ_decompress_dispatcher (include/QoZ/api/impl/SZDispatcher.hpp:41-52)
+        const bool lor = c.cmprAlgo == FAZ_ALGO_LORENZO_REG;
+        if (!lor && c.cmprAlgo != FAZ_ALGO_INTERP)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "stream algorithm is neither ALGO_INTERP nor ALGO_LORENZO_REG"};
+        if (lor && (c.N != 3 || c.regression2))
+            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG streams are implemented for 3-D data without regression2"};
         if (c.wavelet != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet streams are not part of the interpolation path"};
         if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
         if (caller_buffer && cap < c.num)
             throw Fail{FAZ_ERR_ARG, "output buffer holds fewer values than the stream's field"};
         Parsed P;
         P.conf = c;
-        parse_payload(payload, psize, c.N, P);
-        for (int i = 0; i < c.N; i++)
-            if (P.dims[i] != c.dims[i]) throw Fail{FAZ_ERR_FORMAT, "header dims differ from trailer dims"};
+        P.nlist = 0;
+        P.nunpred = 0;
+        if (!lor) {
+            parse_payload(payload, psize, c.N, P);
+            for (int i = 0; i < c.N; i++)
+                if (P.dims[i] != c.dims[i]) throw Fail{FAZ_ERR_FORMAT, "header dims differ from trailer dims"};
+        }
         init_pool_once();
         StreamGuard sg(user_stream);
         cudaStream_t st = sg.st;
@@ -875,7 +927,8 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
             dOut = m.alloc<T>(c.num);
         }
         CK(cudaEventRecord(ev_gpu.a, st));
-        decompress_device<T>(payload, psize, P, dOut, st, tm, launches);
+        if (lor) lorenzo3_decompress<T>(payload, psize, c.dims, dOut, st, launches, tm);
+        else decompress_device<T>(payload, psize, P, dOut, st, tm, launches);
         CK(cudaEventRecord(ev_gpu.b, st));
         if (!on_device) {
             bool alloc = *out == nullptr;
@@ -899,7 +952,7 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
         tm.unpred_count = P.nunpred;
         tm.kernel_launches = launches.n;
         *conf_io = c;
-        conf_io->interp_list_len = P.nlist;
+        if (!lor) conf_io->interp_list_len = P.nlist;
         for (int i = 0; i < P.nlist; i++) {
             conf_io->interpAlgo_list[i] = P.il[i];
             conf_io->interpDirection_list[i] = P.dl[i];

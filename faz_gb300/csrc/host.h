@@ -180,6 +180,20 @@ inline size_t smem_limit() {
     return (size_t)v;
 }
 
+// Lorenzo fast frontend (lorenzo.cu) and the default configuration's tuner (tuner.cu)
+template <typename T>
+void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int lo2, int reg, double eb, int radius,
+                               const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
+                               std::vector<uint8_t> &out);
+template <typename T>
+void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, T *dOut, cudaStream_t st,
+                         Counter &launches, faz_timings &tm);
+template <typename T>
+void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);
+
+template <typename T>
+double device_range(const T *dX, uint64_t n, cudaStream_t st, Counter &launches);
+
 // ------------------------------------------------------- Huffman stages
 struct HuffEncoded {
     Codebook cb;

@@ -89,11 +89,6 @@ __device__ __forceinline__ Stencil<T> make_stencil(int m, int n, int cubic, int 
     return S;
 }
 
-template <typename T>
-__device__ __forceinline__ T linear1_any(T a, T b) {
-    if constexpr (sizeof(T) == 4) return linear1_dp_f32(a, b);
-    else return i_linear1(a, b);
-}
 
 template <typename T>
 __device__ __forceinline__ T eval_stencil(const Stencil<T> &S, const T *p) {

@@ -1,0 +1,454 @@
+// lorenzo.cu - the Lorenzo fast frontend for 3-D fields on the GPU
+// (SZFastFrontend, include/QoZ/frontend/SZFastFrontend.hpp:170-437, with
+// MetaLorenzoPredictor.hpp) and its stream section (save/load, lines 48-128).
+//
+// The reference walks blocks of bs^3 points in row-major order and predicts
+// every point from reconstructed neighbours (one- or two-layer Lorenzo, chosen
+// per block from the original data), keeping the reconstruction in a slab
+// buffer padded with zeros.  That is the same as predicting from a full
+// reconstructed field that reads as zero before the first plane, row and
+// column, so a block depends only on blocks with smaller or equal block
+// coordinates.  Blocks on one diagonal bi + bj + bk = d are therefore
+// independent: one launch per diagonal, one warp per block.  Inside a block
+// the warp walks the point diagonals i + j + k = s in a shared-memory tile
+// that holds the block and its two-deep halo.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "host.h"
+#include "internal.h"
+#include "quant.cuh"
+
+namespace faz {
+
+namespace {
+
+constexpr int kLorWarps = 8;     // blocks (warps) per CTA
+constexpr int kLorMaxBs = 8;     // largest block edge on the GPU path
+
+struct LorArgs {
+    int64_t d1, d2, d3;   // field dims, slowest first
+    int64_t nx, ny, nz;   // blocks per dim
+    int bs;               // block edge
+    int pd;               // prediction dimension (1, 2, 3)
+    int lo, lo2;          // one- / two-layer Lorenzo allowed
+    LevelArgs q;          // quantiser (eb, 1/eb, radius, float split)
+};
+
+// MetaLorenzoPredictor.hpp:8-73 on a tile with strides (tx, ty, 1)
+template <typename T>
+__device__ __forceinline__ T lor_pred(const T *p, int tx, int ty, int pd, bool two) {
+    if (two) {
+        if (pd == 3)
+            return (T)2 * p[-1] - p[-2] + (T)2 * p[-ty] - (T)4 * p[-ty - 1] + (T)2 * p[-ty - 2] - p[-2 * ty] +
+                   (T)2 * p[-2 * ty - 1] - p[-2 * ty - 2] + (T)2 * p[-tx] - (T)4 * p[-tx - 1] + (T)2 * p[-tx - 2] -
+                   (T)4 * p[-tx - ty] + (T)8 * p[-tx - ty - 1] - (T)4 * p[-tx - ty - 2] + (T)2 * p[-tx - 2 * ty] -
+                   (T)4 * p[-tx - 2 * ty - 1] + (T)2 * p[-tx - 2 * ty - 2] - p[-2 * tx] + (T)2 * p[-2 * tx - 1] -
+                   p[-2 * tx - 2] + (T)2 * p[-2 * tx - ty] - (T)4 * p[-2 * tx - ty - 1] + (T)2 * p[-2 * tx - ty - 2] -
+                   p[-2 * tx - 2 * ty] + (T)2 * p[-2 * tx - 2 * ty - 1] - p[-2 * tx - 2 * ty - 2];
+        if (pd == 2)
+            return (T)2 * p[-tx] - p[-2 * tx] + (T)2 * p[-1] - (T)4 * p[-1 - tx] + (T)2 * p[-1 - 2 * tx] - p[-2] +
+                   (T)2 * p[-2 - tx] - p[-2 - 2 * tx];
+        return (T)2 * p[-1] - p[-2];
+    }
+    if (pd == 3) return p[-1] + p[-ty] + p[-tx] - p[-ty - 1] - p[-tx - 1] - p[-tx - ty] + p[-tx - ty - 1];
+    if (pd == 2) return p[-1] + p[-tx] - p[-1 - tx];
+    return p[-1];
+}
+
+// The same predictors on the original field (strides d0, d1, 1), returned in T
+template <typename T>
+__device__ __forceinline__ T lor_pred_g(const T *p, int64_t d0, int64_t d1, int pd, bool two) {
+    if (two) {
+        if (pd == 3)
+            return (T)2 * p[-1] - p[-2] + (T)2 * p[-d1] - (T)4 * p[-d1 - 1] + (T)2 * p[-d1 - 2] - p[-2 * d1] +
+                   (T)2 * p[-2 * d1 - 1] - p[-2 * d1 - 2] + (T)2 * p[-d0] - (T)4 * p[-d0 - 1] + (T)2 * p[-d0 - 2] -
+                   (T)4 * p[-d0 - d1] + (T)8 * p[-d0 - d1 - 1] - (T)4 * p[-d0 - d1 - 2] + (T)2 * p[-d0 - 2 * d1] -
+                   (T)4 * p[-d0 - 2 * d1 - 1] + (T)2 * p[-d0 - 2 * d1 - 2] - p[-2 * d0] + (T)2 * p[-2 * d0 - 1] -
+                   p[-2 * d0 - 2] + (T)2 * p[-2 * d0 - d1] - (T)4 * p[-2 * d0 - d1 - 1] + (T)2 * p[-2 * d0 - d1 - 2] -
+                   p[-2 * d0 - 2 * d1] + (T)2 * p[-2 * d0 - 2 * d1 - 1] - p[-2 * d0 - 2 * d1 - 2];
+        if (pd == 2)
+            return (T)2 * p[-d0] - p[-2 * d0] + (T)2 * p[-1] - (T)4 * p[-1 - d0] + (T)2 * p[-1 - 2 * d0] - p[-2] +
+                   (T)2 * p[-2 - d0] - p[-2 - 2 * d0];
+        return (T)2 * p[-1] - p[-2];
+    }
+    if (pd == 3) return p[-1] + p[-d1] + p[-d0] - p[-d1 - 1] - p[-d0 - 1] - p[-d0 - d1] + p[-d0 - d1 - 1];
+    if (pd == 2) return p[-1] + p[-d0] - p[-1 - d0];
+    return p[-1];
+}
+
+// meta_block_error_estimation_3d for one point (SZFastFrontend.hpp:440-495),
+// regression off.  Noise constants from include/QoZ/utils/MetaDef.hpp:24-29.
+template <typename T>
+__device__ __forceinline__ void meta_est(const T *c, int64_t d0, int64_t d1, T prec, int pd, int lo, int lo2,
+                                         double &el, double &el2) {
+    const T cd = *c;
+    double lp = 0, lp2 = 0;
+    T noise = 0, noise2 = 0;
+    const double n1 = pd == 3 ? 1.22 : (pd == 2 ? 0.81 : 0.5);
+    const double n2 = pd == 3 ? 6.8 : (pd == 2 ? 2.76 : 1.08);
+    if (lo2) {
+        lp2 = (double)lor_pred_g(c, d0, d1, pd, true);
+        noise2 = (T)(n2 * (double)prec);
+    }
+    if (lo) {
+        lp = (double)lor_pred_g(c, d0, d1, pd, false);
+        noise = (T)(n1 * (double)prec);
+    }
+    el += fabs((double)cd - lp) + (double)noise;
+    el2 += fabs((double)cd - lp2) + (double)noise2;
+}
+
+// meta_blockwise_selection_3d (SZFastFrontend.hpp:498-540), one thread per
+// block: 0 Lorenzo, 2 two-layer Lorenzo.
+template <typename T>
+__global__ void k_lor_select(LorArgs a, const T *__restrict__ X, uint16_t *__restrict__ ind) {
+    const int64_t nb = a.nx * a.ny * a.nz;
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const int64_t bk = b % a.nz, bj = (b / a.nz) % a.ny, bi = b / (a.nz * a.ny);
+    const int bs = a.bs;
+    const int sx = (bi + 1) * bs < a.d1 ? bs : (int)(a.d1 - bi * bs);
+    const int sy = (bj + 1) * bs < a.d2 ? bs : (int)(a.d2 - bj * bs);
+    const int sz = (bk + 1) * bs < a.d3 ? bs : (int)(a.d3 - bk * bs);
+    int ms = sx < sy ? sx : sy;
+    ms = ms < sz ? ms : sz;
+    const int64_t d0 = a.d2 * a.d3, d1 = a.d3;
+    const T *dp = X + bi * bs * d0 + bj * bs * d1 + bk * bs;
+    const T prec = (T)a.q.eb;
+    double el = 0, el2 = 0;
+    for (int i = 2; i < ms - 1; i++) {
+        const int m = ms - i;
+        meta_est(dp + i * d0 + i * d1 + i, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
+        meta_est(dp + i * d0 + i * d1 + m, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
+        meta_est(dp + i * d0 + m * d1 + i, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
+        meta_est(dp + i * d0 + m * d1 + m, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
+    }
+    if (ms > 3) meta_est(dp + (ms - 1) * (d0 + d1 + 1), d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
+    ind[b] = (a.lo2 && (!a.lo || el2 <= el)) ? 2 : 0;
+}
+
+// One block diagonal bi + bj + bk = d; one warp per block.
+template <typename T, bool DECOMP, int QM>
+__global__ void __launch_bounds__(kLorWarps * 32)
+    k_lor_diag(LorArgs a, int64_t d, int64_t bi_lo, const T *__restrict__ X, T *__restrict__ R,
+               uint16_t *__restrict__ codes, T *__restrict__ scratch, const uint16_t *__restrict__ ind,
+               const uint64_t *__restrict__ zpos, uint64_t nzp, const T *__restrict__ unpred) {
+    extern __shared__ __align__(16) unsigned char lor_smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t bi = bi_lo + blockIdx.y;
+    const int64_t bj_lo = d - bi - (a.nz - 1) > 0 ? d - bi - (a.nz - 1) : 0;
+    const int64_t bj = bj_lo + (int64_t)blockIdx.x * kLorWarps + w;
+    const int64_t bk = d - bi - bj;
+    if (bi >= a.nx || bj >= a.ny || bk < 0 || bk >= a.nz) return;
+    const int bs = a.bs;
+    const int sx = (bi + 1) * bs < a.d1 ? bs : (int)(a.d1 - bi * bs);
+    const int sy = (bj + 1) * bs < a.d2 ? bs : (int)(a.d2 - bj * bs);
+    const int sz = (bk + 1) * bs < a.d3 ? bs : (int)(a.d3 - bk * bs);
+    const int64_t x0 = bi * bs, y0 = bj * bs, z0 = bk * bs;
+    const int64_t d0 = a.d2 * a.d3, dd1 = a.d3;
+    // tile strides: (tx, ty, 1) over (sx + 2) x (sy + 2) x (sz + 2)
+    const int tz = sz + 2, ty = tz, tx = (sy + 2) * tz;
+    T *t = reinterpret_cast<T *>(lor_smem) + (size_t)w * (size_t)((bs + 2) * (bs + 2) * (bs + 2));
+    const int tn = (sx + 2) * (sy + 2) * tz;
+    for (int e = lane; e < tn; e += 32) {
+        const int i = e / tx, r = e - i * tx, j = r / tz, k = r - j * tz;
+        const int64_t gx = x0 + i - 2, gy = y0 + j - 2, gz = z0 + k - 2;
+        T v = 0;
+        const bool inside = i >= 2 && j >= 2 && k >= 2;
+        if (!inside && gx >= 0 && gy >= 0 && gz >= 0) v = R[gx * d0 + gy * dd1 + gz];
+        t[e] = v;
+    }
+    __syncwarp();
+    const int sel = ind[(bi * a.ny + bj) * a.nz + bk];
+    const bool two = sel == 2;
+    const uint64_t boff = (uint64_t)(bi * bs) * (uint64_t)d0 + (uint64_t)(bj * bs) * (uint64_t)(sx * a.d3) +
+                          (uint64_t)(bk * bs) * (uint64_t)(sx * sy);
+    const int nsteps = sx + sy + sz - 2;
+    const int npairs = sx * sy;
+    for (int s = 0; s < nsteps; s++) {
+        for (int pr = lane; pr < npairs; pr += 32) {
+            const int i = pr / sy, j = pr - i * sy;
+            const int k = s - i - j;
+            if (k < 0 || k >= sz) continue;
+            T *c = t + (i + 2) * tx + (j + 2) * ty + (k + 2);
+            const T pred = lor_pred(c, tx, ty, a.pd, two);
+            const uint64_t pos = boff + (uint64_t)((i * sy + j) * sz + k);
+            T v;
+            if (!DECOMP) {
+                v = X[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)];
+                T uval;
+                const int code = quant_point<T, QM>(v, pred, a.q, uval);
+                codes[pos] = (uint16_t)code;
+                if (code == 0) scratch[pos] = uval;
+            } else {
+                v = recover_point<T, QM>(pred, (int)codes[pos], pos, a.q, zpos, nzp, unpred);
+            }
+            *c = v;
+        }
+        __syncwarp();
+    }
+    for (int e = lane; e < sx * sy * sz; e += 32) {
+        const int i = e / (sy * sz), r = e - i * sy * sz, j = r / sz, k = r - j * sz;
+        R[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)] = t[(i + 2) * tx + (j + 2) * ty + (k + 2)];
+    }
+}
+
+template <typename T>
+LorArgs make_args(const uint64_t *dims, int bs, int pd, int lo, int lo2, double eb, int radius) {
+    LorArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.d1 = (int64_t)dims[0];
+    a.d2 = (int64_t)dims[1];
+    a.d3 = (int64_t)dims[2];
+    a.bs = bs;
+    a.nx = (a.d1 - 1) / bs + 1;
+    a.ny = (a.d2 - 1) / bs + 1;
+    a.nz = (a.d3 - 1) / bs + 1;
+    a.pd = pd;
+    a.lo = lo;
+    a.lo2 = lo2;
+    a.q.eb = eb;
+    a.q.recip = 1.0 / eb;
+    a.q.radius = radius;
+    a.q.trim = 0;
+    set_fast_path<T>(a.q);
+    return a;
+}
+
+template <typename T>
+void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, uint16_t *codes, T *scratch, const uint16_t *ind,
+                   const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st, Counter &launches) {
+    const bool straight = sizeof(T) == 4 && a.q.fast;
+    const int64_t last = (a.nx - 1) + (a.ny - 1) + (a.nz - 1);
+    const size_t smem = (size_t)kLorWarps * (size_t)((a.bs + 2) * (a.bs + 2) * (a.bs + 2)) * sizeof(T);
+    void (*k)(LorArgs, int64_t, int64_t, const T *, T *, uint16_t *, T *, const uint16_t *, const uint64_t *, uint64_t,
+              const T *);
+    if (!decomp) k = straight ? k_lor_diag<T, false, 1> : k_lor_diag<T, false, 0>;
+    else k = straight ? k_lor_diag<T, true, 1> : k_lor_diag<T, true, 0>;
+    CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (a.nx > 65535) throw Fail{FAZ_ERR_UNSUPPORTED, "too many Lorenzo blocks along the slowest axis"};
+    for (int64_t d = 0; d <= last; d++) {
+        const int64_t bi_lo = std::max<int64_t>(0, d - (a.ny - 1) - (a.nz - 1));
+        const int64_t bi_hi = std::min<int64_t>(a.nx - 1, d);
+        // bj spans at most min(ny, d + 1) values for any bi
+        const int64_t nbj = std::min<int64_t>(a.ny, d + 1);
+        dim3 grid((unsigned)((nbj + kLorWarps - 1) / kLorWarps), (unsigned)(bi_hi - bi_lo + 1));
+        k<<<grid, kLorWarps * 32, smem, st>>>(a, d, bi_lo, X, R, codes, scratch, ind, zpos, nz, unpred);
+        launches(cudaGetLastError());
+    }
+}
+
+// meta_params as written by write(params, c) (include/QoZ/utils/MetaDef.hpp:33-60):
+// 44 bytes, the reference's uninitialised padding written as zeros.
+void put_meta_params(std::vector<uint8_t> &o, int bs, int pd, int lo, int lo2, int reg, double eb) {
+    uint8_t m[44];
+    std::memset(m, 0, sizeof m);
+    const float prec = (float)eb;
+    const float eb_lin = 1.0f * prec / 4 / (float)bs;
+    const float eb_ind = (float)bs * eb_lin;
+    int32_t v = bs;
+    std::memcpy(m + 0, &v, 4);
+    v = pd;
+    std::memcpy(m + 4, &v, 4);
+    m[8] = (uint8_t)(lo != 0);
+    m[9] = (uint8_t)(lo2 != 0);
+    m[10] = (uint8_t)(reg != 0);
+    v = 2;  // lorenzo_padding_layer
+    std::memcpy(m + 12, &v, 4);
+    std::memcpy(m + 20, &eb_ind, 4);
+    std::memcpy(m + 24, &eb_lin, 4);
+    float f = 1.0f;  // reg_eb_base
+    std::memcpy(m + 28, &f, 4);
+    f = (float)bs;   // reg_eb_1
+    std::memcpy(m + 32, &f, 4);
+    f = 1.0f;        // sample_ratio
+    std::memcpy(m + 36, &f, 4);
+    m[40] = 1;       // lossless
+    o.insert(o.end(), m, m + sizeof m);
+}
+
+}  // namespace
+
+void check_lorenzo3(const uint64_t *dims, int bs, int pd, int lo, int lo2, int reg, int radius) {
+    if (reg) throw Fail{FAZ_ERR_UNSUPPORTED, "regression blocks are not implemented on the GPU path"};
+    if (!lo && !lo2) throw Fail{FAZ_ERR_ARG, "all Lorenzo and regression predictors are disabled"};
+    if (bs < 1 || bs > kLorMaxBs) throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo block size must be 1..8 on the GPU path"};
+    if (pd < 1 || pd > 3) throw Fail{FAZ_ERR_ARG, "pred_dim must be 1..3"};
+    if (radius < 1 || radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt above 65536 is not implemented on the GPU path"};
+    for (int i = 0; i < 3; i++)
+        if (dims[i] == 0) throw Fail{FAZ_ERR_ARG, "zero dimension"};
+}
+
+// SZ_compress_LorenzoReg for 3-D data (include/QoZ/api/impl/SZLorenzoReg.hpp:94-114):
+// SZFastFrontend::compress_3d + save, then the general compressor's Huffman
+// stage (SZGeneralCompressor.hpp:30-70).  Returns the pre-zstd payload in
+// `out` (host).
+template <typename T>
+void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int lo2, int reg, double eb, int radius,
+                               const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
+                               std::vector<uint8_t> &out) {
+    check_lorenzo3(dims, bs, pd, lo, lo2, reg, radius);
+    LorArgs a = make_args<T>(dims, bs, pd, lo, lo2, eb, radius);
+    const uint64_t n = dims[0] * dims[1] * dims[2];
+    const uint64_t nb = (uint64_t)(a.nx * a.ny * a.nz);
+    DevMem m(st);
+    T *R = m.alloc<T>(n);
+    T *scratch = m.alloc<T>(n);
+    uint16_t *codes = m.alloc<uint16_t>(n);
+    uint16_t *ind = m.alloc<uint16_t>(nb);
+    unsigned long long *vcount = nullptr;
+    if (verify_fast_path()) {
+        vcount = m.alloc<unsigned long long>(1);
+        CK(cudaMemsetAsync(vcount, 0, 8, st));
+        a.q.verify = vcount;
+    }
+    Events ev_pred, ev_huff;
+    CK(cudaEventRecord(ev_pred.a, st));
+    k_lor_select<T><<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(a, dX, ind);
+    launches(cudaGetLastError());
+    run_wavefront<T>(a, false, dX, R, codes, scratch, ind, nullptr, 0, nullptr, st, launches);
+    CK(cudaEventRecord(ev_pred.b, st));
+    CK(cudaEventRecord(ev_huff.a, st));
+    HuffEncoded hi, hc;
+    huffman_encode_device(ind, nb, 0, m, st, launches, hi, tm);
+    huffman_encode_device(codes, n, radius, m, st, launches, hc, tm);
+    if (vcount) {
+        unsigned long long vc = 0;
+        CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
+        if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
+    }
+    const uint64_t nunpred = hc.nzero;
+    T *unp = m.alloc<T>(nunpred ? nunpred : 1);
+    if (nunpred) launches(launch_compact_zeros<T>(codes, n, hc.zc, hc.zoff, nullptr, scratch, unp, st));
+    CK(cudaEventRecord(ev_huff.b, st));
+    // SZFastFrontend::save: params, precision, meanInfo<T>{false, 0}, reg_count,
+    // indicator tree + bits; LinearQuantizer::save; then the code tree + bits
+    std::vector<uint8_t> h0;
+    put_meta_params(h0, bs, pd, lo, lo2, reg, eb);
+    put<double>(h0, eb);
+    for (size_t i = 0; i < 2 * sizeof(T); i++) h0.push_back(0);
+    put<uint64_t>(h0, 0);  // reg_count
+    append_tree(h0, hi.cb, hi.nbytes);
+    std::vector<uint8_t> h1;
+    put<uint8_t>(h1, 2);
+    put<double>(h1, eb);
+    put<int32_t>(h1, radius);
+    put<uint64_t>(h1, nunpred);
+    std::vector<uint8_t> h2;
+    append_tree(h2, hc.cb, hc.nbytes);
+    const size_t total = h0.size() + hi.nbytes + h1.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes;
+    out.resize(total);
+    uint8_t *p = out.data();
+    std::memcpy(p, h0.data(), h0.size());
+    p += h0.size();
+    if (hi.nbytes) CK(cudaMemcpyAsync(p, hi.bits, hi.nbytes, cudaMemcpyDeviceToHost, st));
+    p += hi.nbytes;
+    std::memcpy(p, h1.data(), h1.size());
+    p += h1.size();
+    if (nunpred) CK(cudaMemcpyAsync(p, unp, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
+    p += nunpred * sizeof(T);
+    std::memcpy(p, h2.data(), h2.size());
+    p += h2.size();
+    if (hc.nbytes) CK(cudaMemcpyAsync(p, hc.bits, hc.nbytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    tm.unpred_count = nunpred;
+    tm.payload_bytes = total;
+    tm.predict_ms += ev_pred.ms();
+    tm.huffman_ms += ev_huff.ms();
+}
+
+// SZ_decompress_LorenzoReg for 3-D data (SZLorenzoReg.hpp:117-135):
+// SZFastFrontend::load + decompress_3d into dOut (device, dims[0]*dims[1]*dims[2] values).
+template <typename T>
+void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, T *dOut, cudaStream_t st,
+                         Counter &launches, faz_timings &tm) {
+    const uint8_t *p = pl, *end = pl + psize;
+    auto need = [&](size_t k) {
+        if ((size_t)(end - p) < k) throw Fail{FAZ_ERR_FORMAT, "truncated Lorenzo stream"};
+    };
+    need(44);
+    int32_t bs, pd;
+    std::memcpy(&bs, p, 4);
+    std::memcpy(&pd, p + 4, 4);
+    const int lo = p[8], lo2 = p[9], reg = p[10];
+    p += 44;
+    need(8 + 2 * sizeof(T) + 8);
+    p += 8;  // precision
+    p += 2 * sizeof(T);  // meanInfo<T>
+    uint64_t reg_count;
+    std::memcpy(&reg_count, p, 8);
+    p += 8;
+    if (reg_count) throw Fail{FAZ_ERR_UNSUPPORTED, "regression blocks are not implemented on the GPU path"};
+    if (bs < 1 || bs > kLorMaxBs) throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo block size must be 1..8 on the GPU path"};
+    if (pd < 1 || pd > 3) throw Fail{FAZ_ERR_FORMAT, "bad pred_dim"};
+    (void)lo;
+    (void)lo2;
+    (void)reg;
+    const uint64_t n = dims[0] * dims[1] * dims[2];
+    DevMem m(st);
+    LorArgs a0 = make_args<T>(dims, bs, pd, 1, 1, 1.0, 1);
+    const uint64_t nb = (uint64_t)(a0.nx * a0.ny * a0.nz);
+    uint16_t *ind = m.alloc<uint16_t>(nb);
+    Events ev_dec, ev_pred;
+    CK(cudaEventRecord(ev_dec.a, st));
+    huffman_decode_device(p, end, nb, ind, m, st, launches);
+    need(1 + 8 + 4 + 8);
+    p += 1;
+    double eb;
+    std::memcpy(&eb, p, 8);
+    p += 8;
+    int32_t radius;
+    std::memcpy(&radius, p, 4);
+    p += 4;
+    uint64_t nunpred;
+    std::memcpy(&nunpred, p, 8);
+    p += 8;
+    if (!(eb > 0)) throw Fail{FAZ_ERR_FORMAT, "bad error bound"};
+    if (radius < 1 || radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt above 65536 is not implemented on the GPU path"};
+    if ((size_t)(end - p) / sizeof(T) < nunpred) throw Fail{FAZ_ERR_FORMAT, "truncated unpredictable values"};
+    T *dunp = m.alloc<T>(nunpred ? nunpred : 1);
+    if (nunpred) CK(cudaMemcpyAsync(dunp, p, nunpred * sizeof(T), cudaMemcpyHostToDevice, st));
+    p += nunpred * sizeof(T);
+    uint16_t *codes = m.alloc<uint16_t>(n);
+    huffman_decode_device(p, end, n, codes, m, st, launches);
+    uint64_t *zpos = nullptr;
+    const uint64_t nz = zero_positions(codes, n, m, st, launches, zpos);
+    if (nz != nunpred) throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
+    CK(cudaEventRecord(ev_dec.b, st));
+    LorArgs a = make_args<T>(dims, bs, pd, 1, 1, eb, radius);
+    unsigned long long *vcount = nullptr;
+    if (verify_fast_path()) {
+        vcount = m.alloc<unsigned long long>(1);
+        CK(cudaMemsetAsync(vcount, 0, 8, st));
+        a.q.verify = vcount;
+    }
+    CK(cudaEventRecord(ev_pred.a, st));
+    run_wavefront<T>(a, true, nullptr, dOut, codes, nullptr, ind, zpos, nz, dunp, st, launches);
+    CK(cudaEventRecord(ev_pred.b, st));
+    CK(cudaStreamSynchronize(st));
+    if (vcount) {
+        unsigned long long vc = 0;
+        CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
+        if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
+    }
+    tm.huffman_ms += ev_dec.ms();
+    tm.predict_ms += ev_pred.ms();
+}
+
+template void lorenzo3_compress_payload<float>(const uint64_t *, int, int, int, int, int, double, int, const float *,
+                                               cudaStream_t, Counter &, faz_timings &, std::vector<uint8_t> &);
+template void lorenzo3_compress_payload<double>(const uint64_t *, int, int, int, int, int, double, int,
+                                                const double *, cudaStream_t, Counter &, faz_timings &,
+                                                std::vector<uint8_t> &);
+template void lorenzo3_decompress<float>(const uint8_t *, size_t, const uint64_t *, float *, cudaStream_t, Counter &,
+                                         faz_timings &);
+template void lorenzo3_decompress<double>(const uint8_t *, size_t, const uint64_t *, double *, cudaStream_t,
+                                          Counter &, faz_timings &);
+
+}  // namespace faz

@@ -265,4 +265,12 @@ __device__ __forceinline__ T recover_point(T pred, int code, uint64_t pos, const
     }
 }
 
+// linear1 evaluates with double constants; float data takes the out-of-line
+// double path
+template <typename T>
+__device__ __forceinline__ T linear1_any(T a, T b) {
+    if constexpr (sizeof(T) == 4) return linear1_dp_f32(a, b);
+    else return i_linear1(a, b);
+}
+
 }  // namespace faz

@@ -1,0 +1,472 @@
+// tuner.cu - the SZ3 tuner of the default configuration (ALGO_INTERP_LORENZO)
+// on the GPU: sampling, the Lorenzo trial, the block-interpolation trials and
+// the quantisation-interval estimate, with the decision logic on the host.
+//
+// Reference: SZ_compress_Interp_lorenzo (include/QoZ/api/impl/SZInterp.hpp
+// 2561-2880) with the SZ3 branch of Tuning (2115-2187), sampling<T,N>
+// (include/QoZ/utils/Extraction.hpp:11-232), do_not_use_this_interp_compress_block_test
+// (SZInterp.hpp:558-577) over SZBlockInterpolationCompressor::compress
+// (include/QoZ/compressor/deprecated/SZBlockInterpolationCompressor.hpp:127-280)
+// and optimize_quant_invl_3d (include/QoZ/utils/QuantOptimization.hpp:88-148).
+// Every trial is a whole compression of the sample whose compressed size
+// (zstd framing included) decides, so the trials run the same GPU stages as
+// the real compressors and hand their payloads to the host zstd.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "host.h"
+#include "internal.h"
+#include "quant.cuh"
+
+namespace faz {
+
+namespace {
+
+struct Dims3 {
+    int64_t v[3];
+};
+
+// sampling<T,N>: corner blocks of every dmin-cube, gathered (one thread per
+// sample point).  Dims are embedded as 3-D with leading 1s.
+template <typename T>
+__global__ void k_sample(const T *__restrict__ X, Dims3 gd, Dims3 sd, int64_t sb, int64_t dmin, int e,
+                         T *__restrict__ out, uint64_t sn) {
+    const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= sn) return;
+    int64_t c[3], g[3];
+    c[2] = (int64_t)(idx % (uint64_t)sd.v[2]);
+    c[1] = (int64_t)((idx / (uint64_t)sd.v[2]) % (uint64_t)sd.v[1]);
+    c[0] = (int64_t)(idx / ((uint64_t)sd.v[2] * (uint64_t)sd.v[1]));
+    for (int a = 0; a < 3; a++) {
+        if (a < e) {
+            g[a] = 0;
+            continue;
+        }
+        const int64_t b = c[a] / (2 * sb), i = c[a] % (2 * sb);
+        const int64_t di = i < sb ? i + sb : dmin - 3 * sb + i;
+        g[a] = b * dmin + di;
+    }
+    out[idx] = X[(g[0] * gd.v[1] + g[1]) * gd.v[2] + g[2]];
+}
+
+// ------------------------------------------------ block interpolation trial
+struct BiSweep {
+    int64_t nb[3];        // blocks per dim (3-D embedding)
+    int64_t bs;           // block edge (all blocks full)
+    int64_t block_codes;  // codes per block
+    int64_t dims[3], offs[3];
+    int axis;             // sweep axis (3-D index)
+    int oth[2];           // other axes, increasing
+    int64_t g[2], cnt[2]; // their grid steps and point counts
+    int64_t s;            // stride along the axis
+    int64_t n, tpl;       // points per line, targets per line
+    int64_t seg_off;      // first code of this (level, sweep) inside a block
+    int cubic;
+};
+
+// block_interpolation_1d targets (SZBlockInterpolationCompressor.hpp:204-280):
+// odd indices in increasing order, one thread each.
+template <typename T, int QM>
+__global__ void k_bi_sweep(BiSweep w, LevelArgs q, T *__restrict__ data, uint16_t *__restrict__ codes,
+                           T *__restrict__ scratch, uint64_t total) {
+    const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const uint64_t lines = (uint64_t)(w.cnt[0] * w.cnt[1]);
+    const int64_t r = (int64_t)(idx % (uint64_t)w.tpl);
+    const uint64_t L = (idx / (uint64_t)w.tpl) % lines;
+    const uint64_t t = idx / ((uint64_t)w.tpl * lines);
+    int64_t bc[3];
+    bc[2] = (int64_t)(t % (uint64_t)w.nb[2]);
+    bc[1] = (int64_t)((t / (uint64_t)w.nb[2]) % (uint64_t)w.nb[1]);
+    bc[0] = (int64_t)(t / ((uint64_t)w.nb[2] * (uint64_t)w.nb[1]));
+    int64_t c[3] = {bc[0] * w.bs, bc[1] * w.bs, bc[2] * w.bs};
+    const int64_t u1 = (int64_t)(L % (uint64_t)w.cnt[1]), u0 = (int64_t)(L / (uint64_t)w.cnt[1]);
+    c[w.oth[0]] += u0 * w.g[0];
+    c[w.oth[1]] += u1 * w.g[1];
+    const int64_t i = 2 * r + 1;
+    c[w.axis] += i * w.s;
+    const int64_t pos = c[0] * w.offs[0] + c[1] * w.offs[1] + c[2] * w.offs[2];
+    const int64_t st = w.s * w.offs[w.axis];
+    T *d = data + pos;
+    const int64_t n = w.n;
+    T pred;
+    if (!w.cubic || n < 5) {
+        if (i + 1 < n) pred = i_linear(d[-st], d[st]);
+        else if (n < 4) pred = d[-st];
+        else pred = linear1_any<T>(d[-3 * st], d[-st]);
+    } else {
+        if (i == 1) pred = i_quad1(d[-st], d[st], d[3 * st]);
+        else if (i + 3 < n) pred = i_cubic(d[-3 * st], d[-st], d[st], d[3 * st]);
+        else if ((n & 1) == 0 && i == n - 1) pred = i_quad3(d[-5 * st], d[-3 * st], d[-st]);
+        else pred = i_quad2(d[-3 * st], d[-st], d[st]);
+    }
+    T v = *d, uval;
+    const int code = quant_point<T, QM>(v, pred, q, uval);
+    const uint64_t cp = t * (uint64_t)w.block_codes + (uint64_t)w.seg_off + L * (uint64_t)w.tpl + (uint64_t)r;
+    codes[cp] = (uint16_t)code;
+    if (code == 0) scratch[cp] = uval;
+    *d = v;
+}
+
+// Each block's corner against prediction 0.
+template <typename T>
+__global__ void k_bi_corner(BiSweep w, LevelArgs q, T *__restrict__ data, uint16_t *__restrict__ codes,
+                            T *__restrict__ scratch, uint64_t nblocks) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nblocks) return;
+    const int64_t b2 = (int64_t)(t % (uint64_t)w.nb[2]);
+    const int64_t b1 = (int64_t)((t / (uint64_t)w.nb[2]) % (uint64_t)w.nb[1]);
+    const int64_t b0 = (int64_t)(t / ((uint64_t)w.nb[2] * (uint64_t)w.nb[1]));
+    const int64_t pos = (b0 * w.offs[0] + b1 * w.offs[1] + b2 * w.offs[2]) * w.bs;
+    T v = data[pos], uval;
+    const int code = quantize<T>(v, (T)0, q.eb, q.recip, q.radius, 0, uval);
+    codes[t * (uint64_t)w.block_codes] = (uint16_t)code;
+    if (code == 0) scratch[t * (uint64_t)w.block_codes] = uval;
+    data[pos] = v;
+}
+
+// optimize_quant_invl_3d: histogram of sampled Lorenzo prediction errors.
+// Samples come as runs (first position, count) with stride 100.
+template <typename T>
+__global__ void k_quant_hist(const T *__restrict__ X, int64_t r23, int64_t r3, const uint64_t *__restrict__ seg_pos,
+                             const uint32_t *__restrict__ seg_cnt, uint64_t nseg, double precision,
+                             unsigned long long *__restrict__ hist) {
+    const uint64_t sgi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (sgi >= nseg) return;
+    const uint64_t p0 = seg_pos[sgi];
+    const uint32_t c = seg_cnt[sgi];
+    for (uint32_t m = 0; m < c; m++) {
+        const T *p = X + p0 + (uint64_t)m * 100;
+        const T pv = p[-1] + p[-r3] + p[-r23] - p[-r3 - 1] - p[-r23 - 1] - p[-r23 - r3] + p[-r23 - r3 - 1];
+        const T diff = pv - *p;
+        const float pe = (float)(diff < 0 ? -diff : diff);
+        uint64_t pi = (uint64_t)(((double)pe / precision + 1) / 2);
+        if (pi >= 32768) pi = 32767;
+        atomicAdd(&hist[pi], 1ull);
+    }
+}
+
+size_t zstd_framed_size(const uint8_t *p, size_t n) {
+    std::string err;
+    const Zstd &z = zstd_lib(err);
+    if (!z.ok) throw Fail{FAZ_ERR_ZSTD, err};
+    std::vector<uint8_t> tmp(z.bound(n) + 1);
+    size_t zs = z.compress(tmp.data(), tmp.size(), p, n, 3);
+    if (z.isError(zs)) throw Fail{FAZ_ERR_ZSTD, "ZSTD_compress failed"};
+    return zs + 8;
+}
+
+// do_not_use_this_interp_compress_block_test: compression ratio of the
+// block-interpolation compressor on the sample (blocks of edge bs, which
+// tile the sample exactly).
+template <typename T>
+double block_interp_ratio(int N, const uint64_t *sdims, const T *dS, double eb, int cubic, int dir, int64_t bs,
+                          cudaStream_t st, Counter &launches, faz_timings &tm) {
+    uint64_t num = 1;
+    for (int i = 0; i < N; i++) {
+        num *= sdims[i];
+        if (sdims[i] % (uint64_t)bs) throw Fail{FAZ_ERR_UNSUPPORTED, "sample does not tile into sampling blocks"};
+    }
+    DevMem m(st);
+    T *data = m.alloc<T>(num);
+    CK(cudaMemcpyAsync(data, dS, num * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    uint16_t *codes = m.alloc<uint16_t>(num);
+    T *scratch = m.alloc<T>(num);
+    LevelArgs q;
+    std::memset(&q, 0, sizeof(q));
+    q.eb = eb;
+    q.recip = 1.0 / eb;
+    q.radius = 32768;
+    q.trim = 0;
+    set_fast_path<T>(q);
+    const bool straight = sizeof(T) == 4 && q.fast;
+    BiSweep w;
+    std::memset(&w, 0, sizeof(w));
+    const int e = 3 - N;
+    for (int i = 0; i < 3; i++) {
+        w.dims[i] = 1;
+        w.nb[i] = 1;
+    }
+    for (int i = 0; i < N; i++) {
+        w.dims[e + i] = (int64_t)sdims[i];
+        w.nb[e + i] = (int64_t)sdims[i] / bs;
+    }
+    w.offs[2] = 1;
+    w.offs[1] = w.dims[2];
+    w.offs[0] = w.dims[1] * w.dims[2];
+    w.bs = bs;
+    int64_t bc = 1;
+    for (int i = 0; i < N; i++) bc *= bs;
+    w.block_codes = bc;
+    w.cubic = cubic;
+    const uint64_t nblocks = (uint64_t)(w.nb[0] * w.nb[1] * w.nb[2]);
+    k_bi_corner<T><<<(unsigned)((nblocks + 255) / 256), 256, 0, st>>>(w, q, data, codes, scratch, nblocks);
+    launches(cudaGetLastError());
+    int perm[3] = {0, 1, 2};
+    if (N == 2 && dir != 0) {
+        perm[0] = 1;
+        perm[1] = 0;
+    }
+    if (N == 3) {
+        static const int P3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+        if (dir < 0 || dir > 5) throw Fail{FAZ_ERR_ARG, "interpolation direction out of range"};
+        for (int i = 0; i < 3; i++) perm[i] = P3[dir][i];
+    }
+    int maxl = 0;
+    while (((int64_t)1 << maxl) < bs) maxl++;
+    if (maxl < 1) maxl = 1;
+    int64_t off = 1;  // the corner
+    for (int level = maxl; level > 0; level--) {
+        const int64_t s = (int64_t)1 << (level - 1);
+        bool swept[3] = {false, false, false};
+        for (int sw = 0; sw < N; sw++) {
+            const int a = e + perm[sw];
+            w.axis = a;
+            int no = 0;
+            for (int i = 0; i < 3; i++)
+                if (i != a) w.oth[no++] = i;
+            for (int u = 0; u < 2; u++) {
+                const int ax = w.oth[u];
+                if (ax < e) {
+                    w.g[u] = 1;
+                    w.cnt[u] = 1;
+                } else {
+                    w.g[u] = swept[ax] ? s : 2 * s;
+                    w.cnt[u] = (bs - 1) / w.g[u] + 1;
+                }
+            }
+            w.s = s;
+            w.n = (bs - 1) / s + 1;
+            w.tpl = w.n / 2;
+            w.seg_off = off;
+            const uint64_t per_block = (uint64_t)(w.cnt[0] * w.cnt[1] * w.tpl);
+            const uint64_t total = per_block * nblocks;
+            if (total) {
+                const unsigned grid = (unsigned)((total + 255) / 256);
+                if (straight) k_bi_sweep<T, 1><<<grid, 256, 0, st>>>(w, q, data, codes, scratch, total);
+                else k_bi_sweep<T, 0><<<grid, 256, 0, st>>>(w, q, data, codes, scratch, total);
+                launches(cudaGetLastError());
+            }
+            off += (int64_t)per_block;
+            swept[a] = true;
+        }
+    }
+    if (off != bc) throw Fail{FAZ_ERR_DEVICE, "block interpolation did not cover its blocks"};
+    HuffEncoded hc;
+    huffman_encode_device(codes, num, 32768, m, st, launches, hc, tm);
+    const uint64_t nunpred = hc.nzero;
+    T *unp = m.alloc<T>(nunpred ? nunpred : 1);
+    if (nunpred) launches(launch_compact_zeros<T>(codes, num, hc.zc, hc.zoff, nullptr, scratch, unp, st));
+    std::vector<uint8_t> h;
+    for (int i = 0; i < N; i++) put<uint64_t>(h, sdims[i]);
+    put<uint32_t>(h, (uint32_t)bs);
+    put<int32_t>(h, cubic);
+    put<int32_t>(h, dir);
+    put<uint8_t>(h, 2);
+    put<double>(h, eb);
+    put<int32_t>(h, 32768);
+    put<uint64_t>(h, nunpred);
+    std::vector<uint8_t> h2;
+    append_tree(h2, hc.cb, hc.nbytes);
+    std::vector<uint8_t> pl(h.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes);
+    std::memcpy(pl.data(), h.data(), h.size());
+    if (nunpred) CK(cudaMemcpyAsync(pl.data() + h.size(), unp, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
+    std::memcpy(pl.data() + h.size() + nunpred * sizeof(T), h2.data(), h2.size());
+    if (hc.nbytes)
+        CK(cudaMemcpyAsync(pl.data() + h.size() + nunpred * sizeof(T) + h2.size(), hc.bits, hc.nbytes,
+                           cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return num * 1.0 * sizeof(T) / zstd_framed_size(pl.data(), pl.size());
+}
+
+template <typename T>
+double lorenzo_ratio(const uint64_t *sdims, uint64_t sn, const T *dS, int bs, int pd, double eb, int radius,
+                     cudaStream_t st, Counter &launches, faz_timings &tm) {
+    std::vector<uint8_t> pl;
+    faz_timings t2;
+    std::memset(&t2, 0, sizeof(t2));
+    lorenzo3_compress_payload<T>(sdims, bs, pd, 1, 1, 0, eb, radius, dS, st, launches, t2, pl);
+    tm.host_ms += t2.host_ms;
+    return sn * 1.0 * sizeof(T) / zstd_framed_size(pl.data(), pl.size());
+}
+
+// optimize_quant_invl_3d: the sample walk (QuantOptimization.hpp:97-139) on
+// the host as runs of stride-100 positions, the error histogram on the GPU,
+// estimate_quantization_intervals (lines 26-39) on the host.
+template <typename T>
+int quant_intervals(const T *dX, const uint64_t *dims, double precision, cudaStream_t st, Counter &launches) {
+    const uint64_t r1 = dims[0], r2 = dims[1], r3 = dims[2];
+    const uint64_t sd = 100, r23 = r2 * r3, len = r1 * r23;
+    std::vector<uint64_t> spos;
+    std::vector<uint32_t> scnt;
+    uint64_t oc = sd - 2, pos = r23 + r3 + oc, n1 = 1, n2 = 1, sample_count = 0;
+    while (pos < len) {
+        if (pos < r23 + r3 + 1) throw Fail{FAZ_ERR_UNSUPPORTED, "field too small for the quantisation-interval estimate"};
+        // positions pos, pos + sd, ... while the column offset stays inside the row
+        uint64_t k = 1;
+        if (oc < r3) k = (r3 - oc + sd - 1) / sd;
+        const uint64_t kmax = (len - pos + sd - 1) / sd;
+        const uint64_t take = k < kmax ? k : kmax;
+        spos.push_back(pos);
+        scnt.push_back((uint32_t)take);
+        sample_count += take;
+        if (take < k) break;
+        pos += (k - 1) * sd;
+        oc += (k - 1) * sd;
+        oc += sd;
+        n2++;
+        if (n2 == r2) {
+            n1++;
+            n2 = 1;
+            pos += r3;
+        }
+        const uint64_t oc2 = (n1 + n2) % sd;
+        pos += (r3 + sd - oc) + (sd - oc2);
+        oc = sd - oc2;
+        if (oc == 0) oc++;
+    }
+    DevMem m(st);
+    const uint64_t nseg = spos.size();
+    unsigned long long *hist = m.alloc<unsigned long long>(32768);
+    CK(cudaMemsetAsync(hist, 0, 32768 * 8, st));
+    if (nseg) {
+        uint64_t *dpos = m.alloc<uint64_t>(nseg);
+        uint32_t *dcnt = m.alloc<uint32_t>(nseg);
+        CK(cudaMemcpyAsync(dpos, spos.data(), nseg * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dcnt, scnt.data(), nseg * 4, cudaMemcpyHostToDevice, st));
+        k_quant_hist<T><<<(unsigned)((nseg + 255) / 256), 256, 0, st>>>(dX, (int64_t)r23, (int64_t)r3, dpos, dcnt,
+                                                                       nseg, precision, hist);
+        launches(cudaGetLastError());
+    }
+    std::vector<unsigned long long> h(32768);
+    CK(cudaMemcpyAsync(h.data(), hist, 32768 * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const uint64_t target = (uint64_t)(sample_count * 0.999);
+    uint64_t sum = 0, i;
+    for (i = 0; i < 32768; i++) {
+        sum += h[i];
+        if (sum > target) break;
+    }
+    if (i == 32768) i = 32767;
+    unsigned acc = (unsigned)(2 * (i + 1));
+    unsigned b = acc - 1;
+    b |= b >> 1;
+    b |= b >> 2;
+    b |= b >> 4;
+    b |= b >> 8;
+    b |= b >> 16;
+    const unsigned ni = 2 * (b + 1);
+    return ni > 32 ? (int)ni : 32;
+}
+
+float cal_sampling_ratio(uint64_t block, uint64_t n, uint64_t dmin, int N, const uint64_t *dims) {
+    uint64_t sample_n = 1;
+    for (int i = 0; i < N; i++) sample_n *= dims[i] / dmin * 2 * block;
+    return (float)(sample_n * 1.0 / n);
+}
+
+void set_dims_defaults(faz_config &c) {
+    c.blockSize = c.N == 1 ? 128 : (c.N == 2 ? 16 : 6);
+    c.pred_dim = c.N;
+    c.stride = c.blockSize;
+}
+
+}  // namespace
+
+// SZ_compress_Interp_lorenzo's tuning for the default configuration (no QoZ
+// or rate-driven tuning): on return c.cmprAlgo is ALGO_INTERP or
+// ALGO_LORENZO_REG and the chosen settings are in c.
+template <typename T>
+void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm) {
+    const int N = c.N;
+    if (c.QoZ || c.autoTuningRate > 0 || c.predictorTuningRate > 0)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ / rate-driven tuning is not implemented on the GPU path"};
+    if (c.preTrim > 0) throw Fail{FAZ_ERR_UNSUPPORTED, "preTrim is not implemented on the GPU path"};
+    if (c.wavelet > 0) throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet modes are not part of the interpolation path"};
+    if (c.rng < 0) c.rng = device_range<T>(dX, c.num, st, launches);
+    if (c.relErrorBound <= 0) c.relErrorBound = c.absErrorBound / c.rng;
+    // sampling<T,N>
+    uint64_t dims[4], dmin = c.dims[0];
+    for (int i = 0; i < N; i++) {
+        dims[i] = c.dims[i];
+        dmin = std::min<uint64_t>(dmin, dims[i]);
+    }
+    uint64_t sb = dmin;
+    while (cal_sampling_ratio(sb, c.num, dmin, N, dims) > 0.035) sb--;
+    if (sb * 2 > dmin) sb = dmin / 2;
+    if (sb < 9) {
+        c.cmprAlgo = FAZ_ALGO_INTERP;
+        return;
+    }
+    if (N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "tuning a sampled field is implemented for 3-D data on the GPU path"};
+    uint64_t sdims[3];
+    Dims3 gd{}, sdd{};
+    for (int i = 0; i < 3; i++) {
+        sdims[i] = dims[i] / dmin * 2 * sb;
+        gd.v[i] = (int64_t)dims[i];
+        sdd.v[i] = (int64_t)sdims[i];
+    }
+    const uint64_t sn = sdims[0] * sdims[1] * sdims[2];
+    DevMem m(st);
+    T *dS = m.alloc<T>(sn);
+    k_sample<T><<<(unsigned)((sn + 255) / 256), 256, 0, st>>>(dX, gd, sdd, (int64_t)sb, (int64_t)dmin, 0, dS, sn);
+    launches(cudaGetLastError());
+    const double eb = c.absErrorBound;
+    // Tuning, SZ3 branch: Lorenzo trial (blockSize 5), interpolation trials
+    double best_l = lorenzo_ratio<T>(sdims, sn, dS, 5, 3, eb, c.quantbinCnt / 2, st, launches, tm);
+    double best_i = 0;
+    for (int op = FAZ_INTERP_ALGO_LINEAR; op <= FAZ_INTERP_ALGO_CUBIC; op++) {
+        double r = block_interp_ratio<T>(N, sdims, dS, eb, op, c.interpDirection, (int64_t)sb, st, launches, tm);
+        if (r > best_i) {
+            best_i = r;
+            c.interpAlgo = op;
+        }
+    }
+    const int dop = 5;  // factorial(N) - 1
+    double r = block_interp_ratio<T>(N, sdims, dS, eb, c.interpAlgo, dop, (int64_t)sb, st, launches, tm);
+    if (r > best_i * 1.02) {
+        best_i = r;
+        c.interpDirection = dop;
+    }
+    const bool use_interp = !(best_l > best_i && best_l < 80 && best_i < 80);
+    if (use_interp) {
+        c.cmprAlgo = FAZ_ALGO_INTERP;
+        return;
+    }
+    // Lorenzo follow-up (SZInterp.hpp:2779-2837)
+    faz_config lc = c;
+    lc.cmprAlgo = FAZ_ALGO_LORENZO_REG;
+    lc.lorenzo = 1;
+    lc.lorenzo2 = 1;
+    lc.regression = 0;
+    lc.regression2 = 0;
+    lc.openmp = 0;
+    lc.blockSize = 5;
+    set_dims_defaults(lc);  // setDims(sample dims)
+    lc.quantbinCnt = quant_intervals<T>(dX, dims, eb, st, launches);
+    if (lc.quantbinCnt > 65536)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo with more than 65536 quantisation bins is not implemented on the GPU path"};
+    lc.pred_dim = 2;
+    r = lorenzo_ratio<T>(sdims, sn, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm);
+    if (r > best_l * 1.02) best_l = r;
+    else lc.pred_dim = 3;
+    if (c.relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
+        const int q0 = lc.quantbinCnt;
+        lc.quantbinCnt = 16384;
+        r = lorenzo_ratio<T>(sdims, sn, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm);
+        if (r > best_l * 1.02) best_l = r;
+        else lc.quantbinCnt = q0;
+    }
+    set_dims_defaults(lc);  // setDims(full dims)
+    c = lc;
+}
+
+template void sz3_tune_device<float>(faz_config &, const float *, cudaStream_t, Counter &, faz_timings &);
+template void sz3_tune_device<double>(faz_config &, const double *, cudaStream_t, Counter &, faz_timings &);
+
+}  // namespace faz

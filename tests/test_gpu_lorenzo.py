@@ -1,0 +1,148 @@
+"""GPU path of the default configuration (ALGO_INTERP_LORENZO: the SZ3 tuner)
+and of the 3-D Lorenzo fast frontend, against the oracle and the reference's
+golden streams.
+
+Lorenzo payloads hold struct padding that the reference writes from
+uninitialised memory, so they are compared with those bytes masked; the
+tuner's decisions and every other byte must match.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import faz_gb300 as F
+from faz_gb300.fields import spectral_field
+from conftest import (cli_config, golden_case, golden_input, golden_manifest, golden_stream,
+                      mask_fast_frontend_padding, mask_first_size)
+
+import oracle.oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ALGO_LORENZO_REG, ALGO_INTERP = 0, 2
+DECISIONS = ("cmprAlgo", "interpAlgo", "interpDirection", "quantbinCnt", "blockSize", "pred_dim", "lorenzo",
+             "lorenzo2", "regression")
+
+
+def _rc(name):
+    return O.read_stream(golden_stream(golden_case(name)))[0]
+
+
+# default configuration, no QoZ tuning, 3-D (the GPU tuner covers sampled 3-D fields)
+SZ3_CASES = [c["name"] for c in golden_manifest()
+             if c["ini"] is None and "-q" not in c["flags"] and len(c["dims"]) == 3 and _rc(c["name"]).quantbinCnt <= 65536]
+# Lorenzo streams without regression blocks
+LOR_DEC_CASES = [c["name"] for c in golden_manifest()
+                 if _rc(c["name"]).cmprAlgo == ALGO_LORENZO_REG and not _rc(c["name"]).regression
+                 and _rc(c["name"]).quantbinCnt <= 65536]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def system_zstd():
+    O.set_zstd(None)  # the oracle uses the same host zstd as the library
+    yield
+
+
+def _same(stream, ref, itemsize):
+    c1, p1 = O.read_stream(stream)
+    c2, p2 = O.read_stream(ref)
+    for f in DECISIONS:
+        assert getattr(c1, f) == getattr(c2, f), f
+    if c1.cmprAlgo == ALGO_LORENZO_REG:
+        assert mask_fast_frontend_padding(p1, itemsize) == mask_fast_frontend_padding(p2, itemsize)
+    else:
+        assert p1 == p2
+        assert mask_first_size(stream) == mask_first_size(ref)
+
+
+@pytest.mark.parametrize("name", SZ3_CASES)
+def test_gpu_default_config_matches_oracle_and_reference(name):
+    case = golden_case(name)
+    x = golden_input(case)
+    stream = F.SZ_compress(cli_config(case), x)
+    ref, _ = O.compress(cli_config(case), x)
+    _same(stream, ref, x.itemsize)
+    # the reference's own decisions (its zstd may differ from the host's, but
+    # not by enough to flip these cases)
+    gc = _rc(name)
+    c1, _ = O.read_stream(stream)
+    for f in DECISIONS:
+        assert getattr(c1, f) == getattr(gc, f), f
+    dec, c2 = F.SZ_decompress(None, stream, dtype=x.dtype)
+    ref_dec, _ = O.decompress(ref, dtype=x.dtype)
+    assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
+
+
+@pytest.mark.parametrize("name", LOR_DEC_CASES)
+def test_gpu_decodes_reference_lorenzo_streams(name):
+    case = golden_case(name)
+    dec, _ = F.SZ_decompress(None, golden_stream(case), dtype=np.dtype(case["dtype"]))
+    assert hashlib.sha256(dec.tobytes()).hexdigest() == case["dec_sha256"]
+
+
+def _lor_conf(dims, rel=None, abs_=None, bs=6, lo2=0, pd=None, qbins=65536):
+    c = F.Config(*dims)
+    c.cmprAlgo = F.ALGO_LORENZO_REG
+    c.lorenzo, c.lorenzo2, c.regression, c.regression2 = 1, lo2, 0, 0
+    c.blockSize = bs
+    if pd is not None:
+        c.pred_dim = pd
+    c.quantbinCnt = qbins
+    if rel is not None:
+        c.errorBoundMode, c.relErrorBound = F.EB_REL, rel
+    else:
+        c.errorBoundMode, c.absErrorBound = F.EB_ABS, abs_
+    return c
+
+
+LOR_CASES = [
+    ((37, 41, 29), dict(rel=1e-3), np.float32),
+    ((64, 72, 80), dict(rel=1e-4, lo2=1), np.float32),
+    ((30, 33, 35), dict(rel=1e-4, lo2=1, bs=5), np.float64),
+    ((50, 40, 33), dict(rel=1e-2, lo2=1, pd=2), np.float32),
+    ((17, 70, 9), dict(rel=1e-3, lo2=1, pd=1, bs=8), np.float32),
+    ((1, 50, 60), dict(rel=1e-3, lo2=1, bs=4), np.float32),
+    ((5, 6, 7), dict(abs_=0.5, bs=6, qbins=1024), np.float32),
+    ((96, 64, 48), dict(rel=1e-5, lo2=1, qbins=4096), np.float32),
+]
+
+
+@pytest.mark.parametrize("dims,kw,dtype", LOR_CASES)
+def test_gpu_lorenzo_matches_oracle(dims, kw, dtype):
+    conf = _lor_conf(dims, **kw)
+    x = spectral_field(dims, slope=-2.5, noise=0.02, seed=sum(dims), dtype=dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, _ = O.compress(conf, x)
+    _same(stream, ref, np.dtype(dtype).itemsize)
+    dec, c2 = F.SZ_decompress(None, stream, dtype=dtype)
+    ref_dec, _ = O.decompress(ref, dtype=dtype)
+    assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
+
+
+def test_gpu_lorenzo_fast_path_agrees_with_double_path(monkeypatch):
+    monkeypatch.setenv("FAZ_VERIFY_FASTPATH", "1")
+    dims = (48, 56, 64)
+    rng = np.random.default_rng(3)
+    x = np.round(spectral_field(dims, slope=-2.0, seed=9).astype(np.float64) / 2 ** -7) * 2 ** -7
+    x[rng.random(dims) < 0.01] = 0
+    x = x.astype(np.float32)
+    conf = _lor_conf(dims, abs_=2.0 ** -6, lo2=1)
+    stream = F.SZ_compress(conf, x)  # raises on any disagreement
+    dec, _ = F.SZ_decompress(None, stream, dtype=np.float32)
+    ref, _ = O.compress(conf, x)
+    _same(stream, ref, 4)
+
+
+def test_gpu_lorenzo_rejects_what_it_does_not_implement():
+    dims = (20, 20, 20)
+    x = spectral_field(dims, slope=-3.0, seed=1)
+    conf = _lor_conf(dims, rel=1e-3)
+    conf.regression = 1
+    with pytest.raises(F.FazError):
+        F.SZ_compress(conf, x)
+    conf = _lor_conf(dims, rel=1e-3, bs=9)
+    with pytest.raises(F.FazError):
+        F.SZ_compress(conf, x)
