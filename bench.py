@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--dims", default="512,512,512")
     ap.add_argument("--eb", type=float, default=1e-3)
     ap.add_argument("--interp", default="cubic", choices=["cubic", "linear"])
+    ap.add_argument("--algo", default="auto", choices=["auto", "interp"],
+                    help="auto: the default configuration (ALGO_INTERP_LORENZO, sampled autotune); "
+                         "interp: ALGO_INTERP with --interp")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -107,10 +110,11 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def make_conf(F, dims, eb, interp):
+def make_conf(F, dims, eb, interp, algo="auto"):
     c = F.Config(*dims)
-    c.cmprAlgo = F.ALGO_INTERP
-    c.interpAlgo = F.INTERP_ALGO_CUBIC if interp == "cubic" else F.INTERP_ALGO_LINEAR
+    if algo == "interp":
+        c.cmprAlgo = F.ALGO_INTERP
+        c.interpAlgo = F.INTERP_ALGO_CUBIC if interp == "cubic" else F.INTERP_ALGO_LINEAR
     c.errorBoundMode = F.EB_REL
     c.relErrorBound = eb
     return c
@@ -137,15 +141,16 @@ def finest_level_bytes(dims, itemsize):
 
 # ------------------------------------------------------------- CPU oracle
 def _cpu_slab_job(args):
-    path, shape, offset, eb, interp, reps = args
+    path, shape, offset, eb, interp, algo, reps = args
     import numpy as np
     sys.path.insert(0, ROOT)
     from oracle import oracle as O
     import faz_gb300.config as C
     x = np.fromfile(path, dtype=np.float32, count=int(np.prod(shape)), offset=offset).reshape(shape)
     conf = C.Config(*shape)
-    conf.cmprAlgo = C.ALGO_INTERP
-    conf.interpAlgo = C.INTERP_ALGO_CUBIC if interp == "cubic" else C.INTERP_ALGO_LINEAR
+    if algo == "interp":
+        conf.cmprAlgo = C.ALGO_INTERP
+        conf.interpAlgo = C.INTERP_ALGO_CUBIC if interp == "cubic" else C.INTERP_ALGO_LINEAR
     conf.errorBoundMode = C.EB_REL
     conf.relErrorBound = eb
     tc = td = 0.0
@@ -161,14 +166,14 @@ def _cpu_slab_job(args):
     return tc, td, size, x.nbytes
 
 
-def cpu_oracle_single(field_np, slab, eb, interp):
+def cpu_oracle_single(field_np, slab, eb, interp, algo):
     """One thread, one slab of the field."""
     shape = (slab,) + tuple(field_np.shape[1:])
     with tempfile.NamedTemporaryFile(suffix=".f32", delete=False) as f:
         field_np[:slab].tofile(f)
         path = f.name
     try:
-        tc, td, size, nb = _cpu_slab_job((path, shape, 0, eb, interp, 1))
+        tc, td, size, nb = _cpu_slab_job((path, shape, 0, eb, interp, algo, 1))
     finally:
         os.unlink(path)
     return nb / tc / 1e9, nb / td / 1e9, shape
@@ -188,7 +193,8 @@ def reference_arm(args, dims):
         x.tofile(f)
         path = f.name
     plane = int(np.prod(dims[1:])) * 4
-    jobs = [(path, (slab,) + tuple(dims[1:]), i * slab * plane, args.eb, args.interp, 1) for i in range(nslab)]
+    jobs = [(path, (slab,) + tuple(dims[1:]), i * slab * plane, args.eb, args.interp, args.algo, 1)
+            for i in range(nslab)]
     ctx = mp.get_context("spawn")
     times_c, times_d, sizes = [], [], []
     try:
@@ -215,13 +221,18 @@ def reference_arm(args, dims):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tc * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded spectral field k^-3.5, aniso 1:2:4, 1% noise",
-            "config": {"workload": f"{dims[0]}x{dims[1]}x{dims[2]} float32 spectral field, rel eb {args.eb:g}, "
-                                   f"ALGO_INTERP {args.interp}", "eb_mode": "REL", "eb": args.eb},
+            "config": {"workload": workload_name(dims, args), "eb_mode": "REL", "eb": args.eb},
             "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": nslab, "kind": "port", "sample": sample},
             "e2e": {"value": round(v, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "decompress": {"value": round(nbytes / td / 1e9, 4), "unit": "GB/s", "ms_per_step": round(td * 1e3, 3)},
             "ratio": round(nbytes / statistics.median(sizes), 3)}
     return line
+
+
+def workload_name(dims, args):
+    what = ("default configuration: SZ3 sampled autotune (Lorenzo vs interpolation trials) then the chosen "
+            "compressor" if args.algo == "auto" else f"ALGO_INTERP {args.interp}")
+    return f"{dims[0]}x{dims[1]}x{dims[2]} float32 spectral field, rel eb {args.eb:g}, {what}"
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -256,7 +267,7 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    conf = make_conf(F, dims, args.eb, args.interp)
+    conf = make_conf(F, dims, args.eb, args.interp, args.algo)
     x = spectral_field(dims, slope=-3.5, aniso=(1, 2, 4), noise=0.01, seed=1000 + rank, device="cuda")
     nbytes = x.numel() * x.element_size()
     stream = torch.cuda.Stream()
@@ -267,7 +278,17 @@ def main():
     launches = 0
     for _ in range(args.warmup):
         payload, conf_out = F.compress_payload_device(conf, x, stream, out=pay_buf)
-        F.decompress_payload_device(len(dims), payload, out, stream)
+    interp_chosen = conf_out.cmprAlgo == F.ALGO_INTERP
+    full_stream = None if interp_chosen else F.compress_device(conf, x, stream)
+
+    def decompress_once():
+        if interp_chosen:
+            F.decompress_payload_device(len(dims), payload, out, stream)
+        else:
+            F.decompress_device(full_stream, out, stream)
+
+    for _ in range(args.warmup):
+        decompress_once()
     barrier()
     t_steps, phases = [], []
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -285,13 +306,27 @@ def main():
         dphases = []
         ev0.record(stream)
         for _ in range(args.steps):
-            F.decompress_payload_device(len(dims), payload, out, stream)
+            decompress_once()
             tm = F.last_timings()
             launches += tm["kernel_launches"]
             dphases.append(tm)
         ev1.record(stream)
         barrier()
         t_dec = ev0.elapsed_time(ev1) / 1e3 / args.steps
+        # the plain interpolation compressor alone (ALGO_INTERP cubic), for reference
+        t_plain = None
+        if args.algo == "auto":
+            pconf = make_conf(F, dims, args.eb, "cubic", "interp")
+            for _ in range(2):
+                F.compress_payload_device(pconf, x, stream, out=pay_buf)
+            barrier()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                F.compress_payload_device(pconf, x, stream, out=pay_buf)
+                launches += F.last_timings()["kernel_launches"]
+            ev1.record(stream)
+            barrier()
+            t_plain = ev0.elapsed_time(ev1) / 1e3 / args.steps
     clocks = clk.summary()
     err = (out.double() - x.double()).abs().max().item()
     assert err <= conf_out.absErrorBound, (err, conf_out.absErrorBound)
@@ -331,17 +366,24 @@ def main():
         return
 
     peak, peak_kind = peaks()
-    fin = statistics.median(p["finest_level_ms"] for p in phases) / 1e3
-    fin_bytes = finest_level_bytes(dims, 4)
-    achieved = fin_bytes / fin / 1e9
     nvals = dims[0] * dims[1] * dims[2]
-    traffic = None
-    if args.interp == "cubic" and args.eb == 1e-3:
-        traffic = int(round(FINEST_TRAFFIC_BYTES * nvals / FINEST_TRAFFIC_VALUES))
+    cubic = conf_out.interpAlgo == F.INTERP_ALGO_CUBIC
+    roof = None
+    if interp_chosen:
+        fin = statistics.median(p["finest_level_ms"] for p in phases) / 1e3
+        fin_bytes = finest_level_bytes(dims, 4)
+        achieved = fin_bytes / fin / 1e9
+        traffic = None
+        if cubic and args.eb == 1e-3:
+            traffic = int(round(FINEST_TRAFFIC_BYTES * nvals / FINEST_TRAFFIC_VALUES))
+        roof = {"kernel": "k_interp_level<float,compress> finest level (%s)" % ("cubic" if cubic else "linear"),
+                "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "bytes_per_launch": fin_bytes,
+                "traffic": traffic}
     cpu = None
     if not args.no_cpu_baseline:
         slab = 64
-        cc, cd, shape = cpu_oracle_single(x[:slab].cpu().numpy(), slab, args.eb, args.interp)
+        cc, cd, shape = cpu_oracle_single(x[:slab].cpu().numpy(), slab, args.eb, args.interp, args.algo)
         cpu = {"value": round(cc, 4), "unit": "GB/s", "cores": 1, "kind": "port",
                "sample": f"compress of a {shape[0]}x{shape[1]}x{shape[2]} slab of the same field, one thread "
                          f"(decompress {cd:.4f} GB/s)"}
@@ -359,9 +401,11 @@ def main():
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic: seeded spectral field k^-3.5, aniso 1:2:4, 1% noise, scaled to [-50,80]",
-        "config": {"workload": f"{dims[0]}x{dims[1]}x{dims[2]} float32 spectral field, rel eb {args.eb:g}, "
-                               f"ALGO_INTERP {args.interp} (one field per GPU)",
+        "config": {"workload": workload_name(dims, args) + " (one field per GPU)",
                    "eb_mode": "REL", "eb": args.eb, "abs_eb": conf_out.absErrorBound,
+                   "chosen": {"cmprAlgo": ["ALGO_LORENZO_REG", "ALGO_INTERP_LORENZO", "ALGO_INTERP"][conf_out.cmprAlgo],
+                              "interpAlgo": "cubic" if cubic else "linear",
+                              "interpDirection": conf_out.interpDirection},
                    "l2": "inputs larger than L2 (field %.0f MB vs 129 MB L2)" % (nbytes / 1e6),
                    "parallelism": f"replicas x{world}"},
         "ratio": round(ratio, 3),
@@ -372,14 +416,13 @@ def main():
                 "d2h_bytes_per_step": int(d2h_bytes), "ms_per_step": round(te2e_c * 1e3, 3),
                 "zstd_ms_compress": round(statistics.median(zc), 3),
                 "zstd_ms_decompress": round(statistics.median(zd), 3)},
-        "roofline": {"kernel": "k_interp_level<float,compress> finest level", "bound": "hbm",
-                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "bytes_per_launch": fin_bytes, "traffic": traffic},
-        "phases_ms": {"compress": {k: med(k, phases) for k in ("predict_ms", "finest_level_ms", "huffman_ms",
-                                                               "host_ms", "gpu_ms")},
+        "roofline": roof,
+        "phases_ms": {"compress": {k: med(k, phases) for k in ("tune_ms", "predict_ms", "finest_level_ms",
+                                                               "huffman_ms", "host_ms", "gpu_ms")},
                       "decompress": {k: med(k, dphases) for k in ("huffman_ms", "predict_ms", "finest_level_ms",
                                                                   "gpu_ms")}},
+        "plain_interp_cubic": None if t_plain is None else {
+            "value": round(world * nbytes / t_plain / 1e9, 3), "unit": "GB/s", "ms_per_step": round(t_plain * 1e3, 3)},
         "gpu_launches": launches,
         "clocks": clocks,
         "cpu_baseline": cpu,

@@ -107,6 +107,7 @@ class FazTimings(ctypes.Structure):
         ("payload_bytes", _u64),
         ("unpred_count", _u64),
         ("kernel_launches", _u64),
+        ("tune_ms", _f64),
     ]
 
     def as_dict(self):

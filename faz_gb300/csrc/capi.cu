@@ -483,7 +483,13 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
     resolve_eb<T>(c, dX, st, launches);
     if (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))
         throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
-    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) sz3_tune_device<T>(c, dX, st, launches, tm);
+    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) {
+        auto tt = clk::now();
+        faz_timings tt_tm;
+        std::memset(&tt_tm, 0, sizeof(tt_tm));
+        sz3_tune_device<T>(c, dX, st, launches, tt_tm);
+        tm.tune_ms = ms_since(tt);
+    }
     if (c.cmprAlgo == FAZ_ALGO_INTERP) {
         compress_payload<T>(c, dX, st, payload, psize, tm, launches, sink);
         return;

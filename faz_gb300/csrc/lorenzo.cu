@@ -154,7 +154,10 @@ __global__ void __launch_bounds__(kLorWarps * 32)
     const int64_t d0 = a.d2 * a.d3, dd1 = a.d3;
     // tile strides: (tx, ty, 1) over (sx + 2) x (sy + 2) x (sz + 2)
     const int tz = sz + 2, ty = tz, tx = (sy + 2) * tz;
-    T *t = reinterpret_cast<T *>(lor_smem) + (size_t)w * (size_t)((bs + 2) * (bs + 2) * (bs + 2));
+    // per warp: the (bs + 2)^3 tile, then (compression) the block's bs^3 original values
+    const int tstride = (bs + 2) * (bs + 2) * (bs + 2) + (DECOMP ? 0 : bs * bs * bs);
+    T *t = reinterpret_cast<T *>(lor_smem) + (size_t)w * (size_t)tstride;
+    T *xs = t + (bs + 2) * (bs + 2) * (bs + 2);
     const int tn = (sx + 2) * (sy + 2) * tz;
     for (int e = lane; e < tn; e += 32) {
         const int i = e / tx, r = e - i * tx, j = r / tz, k = r - j * tz;
@@ -163,6 +166,12 @@ __global__ void __launch_bounds__(kLorWarps * 32)
         const bool inside = i >= 2 && j >= 2 && k >= 2;
         if (!inside && gx >= 0 && gy >= 0 && gz >= 0) v = R[gx * d0 + gy * dd1 + gz];
         t[e] = v;
+    }
+    if (!DECOMP) {
+        for (int e = lane; e < sx * sy * sz; e += 32) {
+            const int i = e / (sy * sz), r = e - i * sy * sz, j = r / sz, k = r - j * sz;
+            xs[e] = X[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)];
+        }
     }
     __syncwarp();
     const int sel = ind[(bi * a.ny + bj) * a.nz + bk];
@@ -181,7 +190,7 @@ __global__ void __launch_bounds__(kLorWarps * 32)
             const uint64_t pos = boff + (uint64_t)((i * sy + j) * sz + k);
             T v;
             if (!DECOMP) {
-                v = X[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)];
+                v = xs[(i * sy + j) * sz + k];
                 T uval;
                 const int code = quant_point<T, QM>(v, pred, a.q, uval);
                 codes[pos] = (uint16_t)code;
@@ -226,7 +235,8 @@ void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, uint16_t *co
                    const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st, Counter &launches) {
     const bool straight = sizeof(T) == 4 && a.q.fast;
     const int64_t last = (a.nx - 1) + (a.ny - 1) + (a.nz - 1);
-    const size_t smem = (size_t)kLorWarps * (size_t)((a.bs + 2) * (a.bs + 2) * (a.bs + 2)) * sizeof(T);
+    const size_t smem = (size_t)kLorWarps *
+                        (size_t)((a.bs + 2) * (a.bs + 2) * (a.bs + 2) + (decomp ? 0 : a.bs * a.bs * a.bs)) * sizeof(T);
     void (*k)(LorArgs, int64_t, int64_t, const T *, T *, uint16_t *, T *, const uint16_t *, const uint64_t *, uint64_t,
               const T *);
     if (!decomp) k = straight ? k_lor_diag<T, false, 1> : k_lor_diag<T, false, 0>;

@@ -14,7 +14,10 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <future>
 #include <string>
 #include <vector>
 
@@ -165,8 +168,8 @@ size_t zstd_framed_size(const uint8_t *p, size_t n) {
 // block-interpolation compressor on the sample (blocks of edge bs, which
 // tile the sample exactly).
 template <typename T>
-double block_interp_ratio(int N, const uint64_t *sdims, const T *dS, double eb, int cubic, int dir, int64_t bs,
-                          cudaStream_t st, Counter &launches, faz_timings &tm) {
+void block_interp_payload(int N, const uint64_t *sdims, const T *dS, double eb, int cubic, int dir, int64_t bs,
+                          cudaStream_t st, Counter &launches, faz_timings &tm, std::vector<uint8_t> &pl) {
     uint64_t num = 1;
     for (int i = 0; i < N; i++) {
         num *= sdims[i];
@@ -273,7 +276,7 @@ double block_interp_ratio(int N, const uint64_t *sdims, const T *dS, double eb, 
     put<uint64_t>(h, nunpred);
     std::vector<uint8_t> h2;
     append_tree(h2, hc.cb, hc.nbytes);
-    std::vector<uint8_t> pl(h.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes);
+    pl.resize(h.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes);
     std::memcpy(pl.data(), h.data(), h.size());
     if (nunpred) CK(cudaMemcpyAsync(pl.data() + h.size(), unp, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
     std::memcpy(pl.data() + h.size() + nunpred * sizeof(T), h2.data(), h2.size());
@@ -281,18 +284,40 @@ double block_interp_ratio(int N, const uint64_t *sdims, const T *dS, double eb, 
         CK(cudaMemcpyAsync(pl.data() + h.size() + nunpred * sizeof(T) + h2.size(), hc.bits, hc.nbytes,
                            cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    return num * 1.0 * sizeof(T) / zstd_framed_size(pl.data(), pl.size());
 }
 
+// One trial on its own host thread and CUDA stream: the trials are
+// independent compressions of the same sample, so they overlap on the GPU and
+// each thread computes its zstd size as soon as its payload is ready.
+struct Trial {
+    std::future<size_t> size;
+    uint64_t launches = 0;
+    double host_ms = 0;
+    template <typename F>
+    void start(cudaEvent_t ready, F body) {
+        size = std::async(std::launch::async, [this, ready, body]() -> size_t {
+            StreamGuard sg(nullptr);
+            CK(cudaStreamWaitEvent(sg.st, ready, 0));
+            Counter c;
+            faz_timings t;
+            std::memset(&t, 0, sizeof(t));
+            std::vector<uint8_t> pl;
+            body(sg.st, c, t, pl);
+            launches = c.n;
+            host_ms = t.host_ms;
+            return zstd_framed_size(pl.data(), pl.size());
+        });
+    }
+    size_t get() { return size.get(); }
+};
+
 template <typename T>
-double lorenzo_ratio(const uint64_t *sdims, uint64_t sn, const T *dS, int bs, int pd, double eb, int radius,
-                     cudaStream_t st, Counter &launches, faz_timings &tm) {
-    std::vector<uint8_t> pl;
+void lorenzo_payload(const uint64_t *sdims, const T *dS, int bs, int pd, double eb, int radius, cudaStream_t st,
+                     Counter &launches, faz_timings &tm, std::vector<uint8_t> &pl) {
     faz_timings t2;
     std::memset(&t2, 0, sizeof(t2));
     lorenzo3_compress_payload<T>(sdims, bs, pd, 1, 1, 0, eb, radius, dS, st, launches, t2, pl);
     tm.host_ms += t2.host_ms;
-    return sn * 1.0 * sizeof(T) / zstd_framed_size(pl.data(), pl.size());
 }
 
 // optimize_quant_invl_3d: the sample walk (QuantOptimization.hpp:97-139) on
@@ -417,18 +442,56 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     k_sample<T><<<(unsigned)((sn + 255) / 256), 256, 0, st>>>(dX, gd, sdd, (int64_t)sb, (int64_t)dmin, 0, dS, sn);
     launches(cudaGetLastError());
     const double eb = c.absErrorBound;
-    // Tuning, SZ3 branch: Lorenzo trial (blockSize 5), interpolation trials
-    double best_l = lorenzo_ratio<T>(sdims, sn, dS, 5, 3, eb, c.quantbinCnt / 2, st, launches, tm);
+    const double sbytes = sn * 1.0 * sizeof(T);
+    // Tuning, SZ3 branch: the Lorenzo trial (blockSize 5), linear and cubic
+    // block-interpolation trials in the configured direction, and the
+    // direction-5 trial of whichever wins, computed for both so that every
+    // zstd size runs on its own host thread while the GPU moves on.
+    const int dop = 5;  // factorial(N) - 1
+    Events ready;
+    CK(cudaEventRecord(ready.a, st));
+    Trial jl, ji[2], jd[2];
+    jl.start(ready.a, [&](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
+        lorenzo_payload<T>(sdims, dS, 5, 3, eb, c.quantbinCnt / 2, s2, c2, t2, pl);
+    });
+    const int dir0 = c.interpDirection;
+    for (int op = 0; op < 2; op++) {
+        ji[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
+            block_interp_payload<T>(N, sdims, dS, eb, op, dir0, (int64_t)sb, s2, c2, t2, pl);
+        });
+        jd[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
+            block_interp_payload<T>(N, sdims, dS, eb, op, dop, (int64_t)sb, s2, c2, t2, pl);
+        });
+    }
+    // every trial finishes (or fails) before the sample is released
+    size_t zl = 0, zi[2] = {0, 0}, zd[2] = {0, 0};
+    std::exception_ptr first_err;
+    auto collect = [&](Trial &t, size_t &out) {
+        try {
+            out = t.get();
+        } catch (...) {
+            if (!first_err) first_err = std::current_exception();
+        }
+        launches.n += t.launches;
+        tm.host_ms += t.host_ms;
+    };
+    collect(jl, zl);
+    for (int op = 0; op < 2; op++) {
+        collect(ji[op], zi[op]);
+        collect(jd[op], zd[op]);
+    }
+    if (first_err) std::rethrow_exception(first_err);
+    double best_l = sbytes / zl;
     double best_i = 0;
     for (int op = FAZ_INTERP_ALGO_LINEAR; op <= FAZ_INTERP_ALGO_CUBIC; op++) {
-        double r = block_interp_ratio<T>(N, sdims, dS, eb, op, c.interpDirection, (int64_t)sb, st, launches, tm);
+        const double r = sbytes / zi[op];
         if (r > best_i) {
             best_i = r;
             c.interpAlgo = op;
         }
     }
-    const int dop = 5;  // factorial(N) - 1
-    double r = block_interp_ratio<T>(N, sdims, dS, eb, c.interpAlgo, dop, (int64_t)sb, st, launches, tm);
+    const double rd_lin = sbytes / zd[0], rd_cub = sbytes / zd[1];
+    double r = c.interpAlgo == FAZ_INTERP_ALGO_CUBIC ? rd_cub : rd_lin;
     if (r > best_i * 1.02) {
         best_i = r;
         c.interpDirection = dop;
@@ -452,13 +515,19 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     if (lc.quantbinCnt > 65536)
         throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo with more than 65536 quantisation bins is not implemented on the GPU path"};
     lc.pred_dim = 2;
-    r = lorenzo_ratio<T>(sdims, sn, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm);
+    {
+        std::vector<uint8_t> pl;
+        lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
+        r = sbytes / zstd_framed_size(pl.data(), pl.size());
+    }
     if (r > best_l * 1.02) best_l = r;
     else lc.pred_dim = 3;
     if (c.relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
         const int q0 = lc.quantbinCnt;
         lc.quantbinCnt = 16384;
-        r = lorenzo_ratio<T>(sdims, sn, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm);
+        std::vector<uint8_t> pl;
+        lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
+        r = sbytes / zstd_framed_size(pl.data(), pl.size());
         if (r > best_l * 1.02) best_l = r;
         else lc.quantbinCnt = q0;
     }

@@ -155,6 +155,7 @@ typedef struct faz_timings {
     uint64_t payload_bytes;    /* pre-zstd payload */
     uint64_t unpred_count;
     uint64_t kernel_launches;  /* kernels this library launched in the call */
+    double tune_ms;        /* the default configuration's tuner (trials included) */
 } faz_timings;
 
 /* QoZ::Config::Config(dims...) - Config.hpp:64-74.  dims[0] slowest. */
