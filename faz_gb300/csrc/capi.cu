@@ -487,8 +487,22 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
         auto tt = clk::now();
         faz_timings tt_tm;
         std::memset(&tt_tm, 0, sizeof(tt_tm));
-        sz3_tune_device<T>(c, dX, st, launches, tt_tm);
+        // the interpolation compression of the tuner's likely choice runs
+        // while the trials' zstd sizes are computed; it is kept when the
+        // final choice is the same
+        bool have = false;
+        faz_config guess;
+        std::memset(&guess, 0, sizeof(guess));
+        auto speculate = [&](const faz_config &g) {
+            guess = g;
+            compress_payload<T>(guess, dX, st, payload, psize, tm, launches, sink);
+            have = true;
+        };
+        sz3_tune_device<T>(c, dX, st, launches, tt_tm, speculate);
         tm.tune_ms = ms_since(tt);
+        if (have && c.cmprAlgo == FAZ_ALGO_INTERP && c.interpAlgo == guess.interpAlgo &&
+            c.interpDirection == guess.interpDirection)
+            return;
     }
     if (c.cmprAlgo == FAZ_ALGO_INTERP) {
         compress_payload<T>(c, dX, st, payload, psize, tm, launches, sink);

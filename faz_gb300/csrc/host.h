@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -93,9 +94,16 @@ inline thread_local Pinned t_pin_small;
 struct StreamGuard {
     cudaStream_t st = nullptr;
     bool own = false;
-    explicit StreamGuard(void *user) {
+    // user stream, or a library stream (at the device's highest priority
+    // when `high` is set)
+    explicit StreamGuard(void *user, bool high = false) {
         if (user) {
             st = (cudaStream_t)user;
+        } else if (high) {
+            int least = 0, greatest = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, greatest));
+            own = true;
         } else {
             CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
             own = true;
@@ -189,7 +197,8 @@ template <typename T>
 void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, T *dOut, cudaStream_t st,
                          Counter &launches, faz_timings &tm);
 template <typename T>
-void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);
+void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
+                     const std::function<void(const faz_config &)> &speculate);
 
 template <typename T>
 double device_range(const T *dX, uint64_t n, cudaStream_t st, Counter &launches);

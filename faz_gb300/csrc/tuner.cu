@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <future>
 #include <string>
 #include <vector>
@@ -289,23 +290,45 @@ void block_interp_payload(int N, const uint64_t *sdims, const T *dS, double eb, 
 // One trial on its own host thread and CUDA stream: the trials are
 // independent compressions of the same sample, so they overlap on the GPU and
 // each thread computes its zstd size as soon as its payload is ready.
+// FAZ_TUNE_TRACE=1 prints the tuner's timeline (trial payloads, zstd sizes,
+// the overlapped compression) to stderr.
+bool tune_trace() {
+    const char *e = std::getenv("FAZ_TUNE_TRACE");
+    return e && e[0] == '1';
+}
+
 struct Trial {
+    const char *name = "";
+    clk::time_point t0;
     std::future<size_t> size;
+    std::promise<size_t> raw;  // pre-zstd payload size, known before the zstd size
+    std::future<size_t> raw_f = raw.get_future();
     uint64_t launches = 0;
     double host_ms = 0;
     template <typename F>
     void start(cudaEvent_t ready, F body) {
         size = std::async(std::launch::async, [this, ready, body]() -> size_t {
-            StreamGuard sg(nullptr);
-            CK(cudaStreamWaitEvent(sg.st, ready, 0));
-            Counter c;
-            faz_timings t;
-            std::memset(&t, 0, sizeof(t));
             std::vector<uint8_t> pl;
-            body(sg.st, c, t, pl);
-            launches = c.n;
-            host_ms = t.host_ms;
-            return zstd_framed_size(pl.data(), pl.size());
+            try {
+                // the trials gate the tuner's decision: they take SMs ahead of
+                // the overlapped compression
+                StreamGuard sg(nullptr, true);
+                CK(cudaStreamWaitEvent(sg.st, ready, 0));
+                Counter c;
+                faz_timings t;
+                std::memset(&t, 0, sizeof(t));
+                body(sg.st, c, t, pl);
+                launches = c.n;
+                host_ms = t.host_ms;
+            } catch (...) {
+                raw.set_exception(std::current_exception());
+                throw;
+            }
+            raw.set_value(pl.size());
+            if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s payload %zu bytes\n", ms_since(t0), name, pl.size());
+            const size_t z = zstd_framed_size(pl.data(), pl.size());
+            if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s zstd %zu bytes\n", ms_since(t0), name, z);
+            return z;
         });
     }
     size_t get() { return size.get(); }
@@ -407,7 +430,8 @@ void set_dims_defaults(faz_config &c) {
 // or rate-driven tuning): on return c.cmprAlgo is ALGO_INTERP or
 // ALGO_LORENZO_REG and the chosen settings are in c.
 template <typename T>
-void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm) {
+void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
+                     const std::function<void(const faz_config &)> &speculate) {
     const int N = c.N;
     if (c.QoZ || c.autoTuningRate > 0 || c.predictorTuningRate > 0)
         throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ / rate-driven tuning is not implemented on the GPU path"};
@@ -451,6 +475,13 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     Events ready;
     CK(cudaEventRecord(ready.a, st));
     Trial jl, ji[2], jd[2];
+    const auto tt0 = clk::now();
+    jl.name = "lorenzo";
+    ji[0].name = "linear";
+    ji[1].name = "cubic";
+    jd[0].name = "linear-dir5";
+    jd[1].name = "cubic-dir5";
+    for (Trial *t : {&jl, &ji[0], &ji[1], &jd[0], &jd[1]}) t->t0 = tt0;
     jl.start(ready.a, [&](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
         lorenzo_payload<T>(sdims, dS, 5, 3, eb, c.quantbinCnt / 2, s2, c2, t2, pl);
     });
@@ -462,6 +493,43 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         jd[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
             block_interp_payload<T>(N, sdims, dS, eb, op, dop, (int64_t)sb, s2, c2, t2, pl);
         });
+    }
+    // While the Lorenzo trial and the zstd sizes are computed, compress the
+    // field with the interpolation choice the pre-zstd sizes point to (the
+    // caller keeps the result if the final choice agrees, which it does unless
+    // Lorenzo wins or two candidates are within zstd's effect of each other).
+    if (speculate) {
+        bool ok = true;
+        size_t ri[2] = {0, 0}, rd[2] = {0, 0};
+        try {
+            for (int op = 0; op < 2; op++) {
+                ri[op] = ji[op].raw_f.get();
+                rd[op] = jd[op].raw_f.get();
+            }
+        } catch (...) {
+            ok = false;  // the trial's own error surfaces below
+        }
+        if (ok) {
+            // the Lorenzo trial is not waited for: interpolation usually wins
+            faz_config g = c;
+            double bi = 0;
+            for (int op = 0; op < 2; op++) {
+                const double rr = sbytes / (ri[op] + 8);
+                if (rr > bi) {
+                    bi = rr;
+                    g.interpAlgo = op;
+                }
+            }
+            const double rr = sbytes / (rd[g.interpAlgo] + 8);
+            if (rr > bi * 1.02) {
+                bi = rr;
+                g.interpDirection = dop;
+            }
+            g.cmprAlgo = FAZ_ALGO_INTERP;
+            if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  overlapped compression starts\n", ms_since(tt0));
+            speculate(g);
+            if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  overlapped compression ends\n", ms_since(tt0));
+        }
     }
     // every trial finishes (or fails) before the sample is released
     size_t zl = 0, zi[2] = {0, 0}, zd[2] = {0, 0};
@@ -535,7 +603,9 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     c = lc;
 }
 
-template void sz3_tune_device<float>(faz_config &, const float *, cudaStream_t, Counter &, faz_timings &);
-template void sz3_tune_device<double>(faz_config &, const double *, cudaStream_t, Counter &, faz_timings &);
+template void sz3_tune_device<float>(faz_config &, const float *, cudaStream_t, Counter &, faz_timings &,
+                                     const std::function<void(const faz_config &)> &);
+template void sz3_tune_device<double>(faz_config &, const double *, cudaStream_t, Counter &, faz_timings &,
+                                      const std::function<void(const faz_config &)> &);
 
 }  // namespace faz
