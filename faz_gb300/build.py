@@ -14,6 +14,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfaz_gb300.so")
+CLI_SRC = os.path.join(HERE, "cli", "faz.cpp")
+CLI = os.path.join(HERE, "faz")  # the command-line tool, linked against LIB
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false keeps every stencil and quantiser operation separately rounded,
@@ -77,6 +79,11 @@ def build(force=False, verbose=False):
                 print(out)
     if jobs or not os.path.exists(LIB):
         run([nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB] + objs + ["-ldl", "-lpthread"])
+    hpp = os.path.join(ROOT, "include", "faz_gb300.hpp")
+    if force or not os.path.exists(CLI) or os.path.getmtime(CLI) < max(
+            os.path.getmtime(CLI_SRC), os.path.getmtime(hpp), os.path.getmtime(LIB)):
+        run(["g++", "-O2", "-std=c++17", "-Wall", "-o", CLI, CLI_SRC, "-L" + HERE, "-lfaz_gb300",
+             "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

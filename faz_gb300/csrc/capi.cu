@@ -199,6 +199,9 @@ void check_config(const faz_config &c) {
     if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
     if (c.cmprAlgo != FAZ_ALGO_INTERP && c.cmprAlgo != FAZ_ALGO_INTERP_LORENZO && c.cmprAlgo != FAZ_ALGO_LORENZO_REG)
         throw Fail{FAZ_ERR_UNSUPPORTED, "cmprAlgo must be ALGO_INTERP, ALGO_INTERP_LORENZO or ALGO_LORENZO_REG"};
+    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.FZ)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "FAZ features (wavelets, SPERR, conditioning; FZ = 1) are not implemented; "
+                                        "set FZ = 0 (faz -F 0)"};
     if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && (c.N != 3 || c.regression2))
         throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG is implemented for 3-D data without regression2"};
     if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};

@@ -150,6 +150,15 @@ def tuned_config(case):
     return conf
 
 
+def write_ini(path, d):
+    """An INI file in the layout tests/golden/make_golden.py gave the reference."""
+    with open(path, "w") as f:
+        for sec, kv in d.items():
+            f.write(f"[{sec}]\n")
+            for k, v in kv.items():
+                f.write(f"{k} = {v}\n")
+
+
 def mask_fast_frontend_padding(payload, itemsize):
     """Zero the padding bytes of the Lorenzo fast frontend's raw structs in a
     pre-zstd payload: meta_params (bytes 11 and 41-43 of its 44) and
