@@ -14,6 +14,7 @@
 // that holds the block and its two-deep halo.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -37,6 +38,8 @@ struct LorArgs {
     int bs;               // block edge
     int pd;               // prediction dimension (1, 2, 3)
     int lo, lo2;          // one- / two-layer Lorenzo allowed
+    int reg;              // linear regression allowed
+    const float *rp;      // per block: the 4 reconstructed regression coefficients
     LevelArgs q;          // quantiser (eb, 1/eb, radius, float split)
 };
 
@@ -104,10 +107,42 @@ __device__ __forceinline__ void meta_est(const T *c, int64_t d0, int64_t d1, T p
     el2 += fabs((double)cd - lp2) + (double)noise2;
 }
 
-// meta_blockwise_selection_3d (SZFastFrontend.hpp:498-540), one thread per
-// block: 0 Lorenzo, 2 two-layer Lorenzo.
+// compute_regression_coeffcients_3d (MetaRegressionPredictor.hpp:104-139),
+// float sums in the reference's loop order.
 template <typename T>
-__global__ void k_lor_select(LorArgs a, const T *__restrict__ X, uint16_t *__restrict__ ind) {
+__device__ void reg_coeffs(const T *d, int sx, int sy, int sz, int64_t d0, int64_t d1, float *rp) {
+    const T *cur = d;
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f, f = 0;
+    for (int i = 0; i < sx; i++) {
+        float sum_x = 0;
+        for (int j = 0; j < sy; j++) {
+            float sum_y = 0;
+            for (int k = 0; k < sz; k++) {
+                const T cd = *cur;
+                sum_y = (float)(sum_y + cd);
+                fz = (float)(fz + (T)(cd * (T)k));
+                cur++;
+            }
+            fy += sum_y * (float)j;
+            sum_x += sum_y;
+            cur += (d1 - sz);
+        }
+        fx += sum_x * (float)i;
+        f += sum_x;
+        cur += (d0 - sy * d1);
+    }
+    const float coeff = (float)(1.0 / (sx * sy * sz));
+    rp[0] = (2 * fx / (float)(sx - 1) - f) * 6 * coeff / (float)(sx + 1);
+    rp[1] = (2 * fy / (float)(sy - 1) - f) * 6 * coeff / (float)(sy + 1);
+    rp[2] = (2 * fz / (float)(sz - 1) - f) * 6 * coeff / (float)(sz + 1);
+    rp[3] = f * coeff - ((float)(sx - 1) * rp[0] / 2 + (float)(sy - 1) * rp[1] / 2 + (float)(sz - 1) * rp[2] / 2);
+}
+
+// meta_blockwise_selection_3d (SZFastFrontend.hpp:498-540), one thread per
+// block: 0 Lorenzo, 1 regression, 2 two-layer Lorenzo.  The block's raw
+// regression coefficients go to raw[4b..4b+3].
+template <typename T>
+__global__ void k_lor_select(LorArgs a, const T *__restrict__ X, uint16_t *__restrict__ ind, float *__restrict__ raw) {
     const int64_t nb = a.nx * a.ny * a.nz;
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nb) return;
@@ -121,16 +156,36 @@ __global__ void k_lor_select(LorArgs a, const T *__restrict__ X, uint16_t *__res
     const int64_t d0 = a.d2 * a.d3, d1 = a.d3;
     const T *dp = X + bi * bs * d0 + bj * bs * d1 + bk * bs;
     const T prec = (T)a.q.eb;
-    double el = 0, el2 = 0;
+    const bool ereg = a.reg && ms >= 2;
+    float rp[4] = {0, 0, 0, 0};
+    if (ereg) reg_coeffs(dp, sx, sy, sz, d0, d1, rp);
+    double el = 0, el2 = 0, er = 0;
+    auto est = [&](int x, int y, int z) {
+        const T *c = dp + x * d0 + y * d1 + z;
+        if (ereg) {
+            // regression_predict_3d<T> (MetaRegressionPredictor.hpp:142-146)
+            const T pr = (T)(rp[0] * (float)x + rp[1] * (float)y + rp[2] * (float)z + rp[3]);
+            const T df = *c - pr;
+            er += (double)(df < 0 ? -df : df);
+        }
+        meta_est(c, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
+    };
     for (int i = 2; i < ms - 1; i++) {
         const int m = ms - i;
-        meta_est(dp + i * d0 + i * d1 + i, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
-        meta_est(dp + i * d0 + i * d1 + m, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
-        meta_est(dp + i * d0 + m * d1 + i, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
-        meta_est(dp + i * d0 + m * d1 + m, d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
+        est(i, i, i);
+        est(i, i, m);
+        est(i, m, i);
+        est(i, m, m);
     }
-    if (ms > 3) meta_est(dp + (ms - 1) * (d0 + d1 + 1), d0, d1, prec, a.pd, a.lo, a.lo2, el, el2);
-    ind[b] = (a.lo2 && (!a.lo || el2 <= el)) ? 2 : 0;
+    if (ms > 3) est(ms - 1, ms - 1, ms - 1);
+    int sel;
+    if (ereg && (!a.lo || er <= el) && (!a.lo2 || er < el2)) sel = 1;
+    else if (a.lo2 && (!a.lo || el2 <= el) && (!ereg || el2 <= er)) sel = 2;
+    else sel = 0;
+    ind[b] = (uint16_t)sel;
+    if (raw) {
+        for (int c = 0; c < 4; c++) raw[4 * b + c] = rp[c];
+    }
 }
 
 // One block diagonal bi + bj + bk = d; one warp per block.
@@ -174,7 +229,8 @@ __global__ void __launch_bounds__(kLorWarps * 32)
         }
     }
     __syncwarp();
-    const int sel = ind[(bi * a.ny + bj) * a.nz + bk];
+    int sel = ind[(bi * a.ny + bj) * a.nz + bk];
+    if (sel == 1 && a.rp == nullptr) sel = 0;  // a stream without coefficients
     const bool two = sel == 2;
     const uint64_t boff = (uint64_t)(bi * bs) * (uint64_t)d0 + (uint64_t)(bj * bs) * (uint64_t)(sx * a.d3) +
                           (uint64_t)(bk * bs) * (uint64_t)(sx * sy);
@@ -186,7 +242,14 @@ __global__ void __launch_bounds__(kLorWarps * 32)
             const int k = s - i - j;
             if (k < 0 || k >= sz) continue;
             T *c = t + (i + 2) * tx + (j + 2) * ty + (k + 2);
-            const T pred = lor_pred(c, tx, ty, a.pd, two);
+            T pred;
+            if (sel == 1) {
+                // regression_predict_quantize_3d (MetaRegressionPredictor.hpp:148-189)
+                const float *rp = a.rp + 4 * ((bi * a.ny + bj) * a.nz + bk);
+                pred = (T)(rp[0] * (float)i + rp[1] * (float)j + rp[2] * (float)k + rp[3]);
+            } else {
+                pred = lor_pred(c, tx, ty, a.pd, two);
+            }
             const uint64_t pos = boff + (uint64_t)((i * sy + j) * sz + k);
             T v;
             if (!DECOMP) {
@@ -209,7 +272,7 @@ __global__ void __launch_bounds__(kLorWarps * 32)
 }
 
 template <typename T>
-LorArgs make_args(const uint64_t *dims, int bs, int pd, int lo, int lo2, double eb, int radius) {
+LorArgs make_args(const uint64_t *dims, int bs, int pd, int lo, int lo2, double eb, int radius, int reg = 0) {
     LorArgs a;
     std::memset(&a, 0, sizeof(a));
     a.d1 = (int64_t)dims[0];
@@ -222,6 +285,8 @@ LorArgs make_args(const uint64_t *dims, int bs, int pd, int lo, int lo2, double 
     a.pd = pd;
     a.lo = lo;
     a.lo2 = lo2;
+    a.reg = reg;
+    a.rp = nullptr;
     a.q.eb = eb;
     a.q.recip = 1.0 / eb;
     a.q.radius = radius;
@@ -283,11 +348,88 @@ void put_meta_params(std::vector<uint8_t> &o, int bs, int pd, int lo, int lo2, i
     o.insert(o.end(), m, m + sizeof m);
 }
 
+// Regression coefficient precisions (MetaDef.hpp:54-59 and
+// SZFastFrontend.hpp:229-235), in the element type T.
+template <typename T>
+void reg_precisions(int bs, double eb, T prec[4], T rprec[4]) {
+    const float fprec = (float)eb;
+    const float eb_lin = 1.0f * fprec / 4 / (float)bs;
+    const float eb_ind = (float)bs * eb_lin;
+    for (int i = 0; i < 3; i++) prec[i] = (T)eb_lin;
+    prec[3] = (T)eb_ind;
+    for (int i = 0; i < 4; i++) rprec[i] = (T)(1.0 / prec[i]);
+}
+
+// compress_regression_coefficient_3d over the regression blocks in block
+// order (MetaRegressionPredictor.hpp:10-40): each coefficient is predicted by
+// the previous regression block's reconstructed one, a serial chain; rec
+// receives the reconstructed coefficients of every regression block.
+template <typename T>
+void reg_chain_compress(const std::vector<uint16_t> &ind, const std::vector<float> &raw, int bs, double eb,
+                        std::vector<float> &rec, std::vector<uint16_t> &types, std::vector<float> &unp) {
+    T prec[4], rprec[4];
+    reg_precisions<T>(bs, eb, prec, rprec);
+    float prev[4] = {0, 0, 0, 0};
+    rec.assign(raw.size(), 0.0f);
+    for (size_t b = 0; b < ind.size(); b++) {
+        if (ind[b] != 1) continue;
+        for (int c = 0; c < 4; c++) {
+            const float pred = prev[c], cur = raw[4 * b + c];
+            const double p = (double)prec[c], rp = (double)rprec[c];
+            const double diff = (double)(float)(cur - pred);
+            double qd = std::fabs(diff) * rp + 1;
+            int code = 0;
+            float dec = cur;
+            if (qd < 65536) {
+                qd = diff > 0 ? qd : -qd;
+                const int qi = (int)(qd / 2) + 32768;
+                const float dd = (float)((double)pred + (double)(2 * (qi - 32768)) * p);
+                dec = dd;
+                if (std::fabs((double)(float)(dd - cur)) <= p) code = qi;
+                else dec = cur;
+            }
+            if (code == 0) unp.push_back(cur);
+            types.push_back((uint16_t)code);
+            rec[4 * b + c] = dec;
+            prev[c] = dec;
+        }
+    }
+}
+
+// decode_regression_coefficients (MetaRegressionPredictor.hpp:42-80)
+template <typename T>
+void reg_chain_decompress(const std::vector<uint16_t> &ind, const std::vector<uint16_t> &types, const float *unp,
+                          uint64_t nunp, float eb_lin, float eb_ind, std::vector<float> &rec) {
+    T prec[4];
+    for (int i = 0; i < 3; i++) prec[i] = (T)eb_lin;
+    prec[3] = (T)eb_ind;
+    float prev[4] = {0, 0, 0, 0};
+    rec.assign(4 * ind.size(), 0.0f);
+    size_t ti = 0;
+    uint64_t ui = 0;
+    for (size_t b = 0; b < ind.size(); b++) {
+        if (ind[b] != 1) continue;
+        for (int c = 0; c < 4; c++) {
+            if (ti >= types.size()) throw Fail{FAZ_ERR_FORMAT, "regression coefficient stream too short"};
+            const int tv = types[ti++];
+            float v;
+            if (tv == 0) {
+                if (ui >= nunp) throw Fail{FAZ_ERR_FORMAT, "regression coefficient unpredictables exhausted"};
+                std::memcpy(&v, unp + ui, 4);
+                ui++;
+            } else {
+                v = (float)((double)prev[c] + (double)(2 * (tv - 32768)) * (double)prec[c]);
+            }
+            rec[4 * b + c] = v;
+            prev[c] = v;
+        }
+    }
+}
+
 }  // namespace
 
 void check_lorenzo3(const uint64_t *dims, int bs, int pd, int lo, int lo2, int reg, int radius) {
-    if (reg) throw Fail{FAZ_ERR_UNSUPPORTED, "regression blocks are not implemented on the GPU path"};
-    if (!lo && !lo2) throw Fail{FAZ_ERR_ARG, "all Lorenzo and regression predictors are disabled"};
+    if (!lo && !lo2 && !reg) throw Fail{FAZ_ERR_ARG, "all Lorenzo and regression predictors are disabled"};
     if (bs < 1 || bs > kLorMaxBs) throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo block size must be 1..8 on the GPU path"};
     if (pd < 1 || pd > 3) throw Fail{FAZ_ERR_ARG, "pred_dim must be 1..3"};
     if (radius < 1 || radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt above 65536 is not implemented on the GPU path"};
@@ -304,7 +446,7 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
                                const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
                                std::vector<uint8_t> &out) {
     check_lorenzo3(dims, bs, pd, lo, lo2, reg, radius);
-    LorArgs a = make_args<T>(dims, bs, pd, lo, lo2, eb, radius);
+    LorArgs a = make_args<T>(dims, bs, pd, lo, lo2, eb, radius, reg);
     const uint64_t n = dims[0] * dims[1] * dims[2];
     const uint64_t nb = (uint64_t)(a.nx * a.ny * a.nz);
     DevMem m(st);
@@ -320,13 +462,40 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     }
     Events ev_pred, ev_huff;
     CK(cudaEventRecord(ev_pred.a, st));
-    k_lor_select<T><<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(a, dX, ind);
+    float *raw = reg ? m.alloc<float>(4 * nb) : nullptr;
+    k_lor_select<T><<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(a, dX, ind, raw);
     launches(cudaGetLastError());
+    // regression coefficients: the serial chain on the host, then the
+    // reconstructed coefficients back to the device for the wavefront
+    std::vector<uint16_t> rtypes;
+    std::vector<float> runp;
+    uint64_t reg_count = 0;
+    uint16_t *drtypes = nullptr;
+    if (reg) {
+        std::vector<uint16_t> hind(nb);
+        std::vector<float> hraw(4 * nb), rec;
+        CK(cudaMemcpyAsync(hind.data(), ind, nb * 2, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hraw.data(), raw, nb * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        auto th = clk::now();
+        reg_chain_compress<T>(hind, hraw, bs, eb, rec, rtypes, runp);
+        reg_count = rtypes.size() / 4;
+        tm.host_ms += ms_since(th);
+        float *drec = m.alloc<float>(4 * nb);
+        CK(cudaMemcpyAsync(drec, rec.data(), nb * 16, cudaMemcpyHostToDevice, st));
+        a.rp = drec;
+        if (reg_count) {
+            drtypes = m.alloc<uint16_t>(rtypes.size());
+            CK(cudaMemcpyAsync(drtypes, rtypes.data(), rtypes.size() * 2, cudaMemcpyHostToDevice, st));
+        }
+        CK(cudaStreamSynchronize(st));  // host vectors leave scope
+    }
     run_wavefront<T>(a, false, dX, R, codes, scratch, ind, nullptr, 0, nullptr, st, launches);
     CK(cudaEventRecord(ev_pred.b, st));
     CK(cudaEventRecord(ev_huff.a, st));
-    HuffEncoded hi, hc;
+    HuffEncoded hi, hc, hr;
     huffman_encode_device(ind, nb, 0, m, st, launches, hi, tm);
+    if (reg_count) huffman_encode_device(drtypes, rtypes.size(), 32768, m, st, launches, hr, tm);
     huffman_encode_device(codes, n, radius, m, st, launches, hc, tm);
     if (vcount) {
         unsigned long long vc = 0;
@@ -343,8 +512,16 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     put_meta_params(h0, bs, pd, lo, lo2, reg, eb);
     put<double>(h0, eb);
     for (size_t i = 0; i < 2 * sizeof(T); i++) h0.push_back(0);
-    put<uint64_t>(h0, 0);  // reg_count
+    put<uint64_t>(h0, reg_count);
     append_tree(h0, hi.cb, hi.nbytes);
+    // encode_regression_coefficients (MetaRegressionPredictor.hpp:82-95)
+    std::vector<uint8_t> hreg;
+    if (reg_count) {
+        put<uint64_t>(hreg, runp.size());
+        const uint8_t *u = reinterpret_cast<const uint8_t *>(runp.data());
+        hreg.insert(hreg.end(), u, u + runp.size() * 4);
+        append_tree(hreg, hr.cb, hr.nbytes);
+    }
     std::vector<uint8_t> h1;
     put<uint8_t>(h1, 2);
     put<double>(h1, eb);
@@ -352,13 +529,19 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     put<uint64_t>(h1, nunpred);
     std::vector<uint8_t> h2;
     append_tree(h2, hc.cb, hc.nbytes);
-    const size_t total = h0.size() + hi.nbytes + h1.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes;
+    const size_t rbits = reg_count ? hr.nbytes : 0;
+    const size_t total =
+        h0.size() + hi.nbytes + hreg.size() + rbits + h1.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes;
     out.resize(total);
     uint8_t *p = out.data();
     std::memcpy(p, h0.data(), h0.size());
     p += h0.size();
     if (hi.nbytes) CK(cudaMemcpyAsync(p, hi.bits, hi.nbytes, cudaMemcpyDeviceToHost, st));
     p += hi.nbytes;
+    if (!hreg.empty()) std::memcpy(p, hreg.data(), hreg.size());
+    p += hreg.size();
+    if (rbits) CK(cudaMemcpyAsync(p, hr.bits, rbits, cudaMemcpyDeviceToHost, st));
+    p += rbits;
     std::memcpy(p, h1.data(), h1.size());
     p += h1.size();
     if (nunpred) CK(cudaMemcpyAsync(p, unp, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
@@ -387,6 +570,9 @@ void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, 
     std::memcpy(&bs, p, 4);
     std::memcpy(&pd, p + 4, 4);
     const int lo = p[8], lo2 = p[9], reg = p[10];
+    float eb_ind, eb_lin;  // meta_params regression_param_eb_independent / _linear
+    std::memcpy(&eb_ind, p + 20, 4);
+    std::memcpy(&eb_lin, p + 24, 4);
     p += 44;
     need(8 + 2 * sizeof(T) + 8);
     p += 8;  // precision
@@ -394,7 +580,6 @@ void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, 
     uint64_t reg_count;
     std::memcpy(&reg_count, p, 8);
     p += 8;
-    if (reg_count) throw Fail{FAZ_ERR_UNSUPPORTED, "regression blocks are not implemented on the GPU path"};
     if (bs < 1 || bs > kLorMaxBs) throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo block size must be 1..8 on the GPU path"};
     if (pd < 1 || pd > 3) throw Fail{FAZ_ERR_FORMAT, "bad pred_dim"};
     (void)lo;
@@ -408,6 +593,32 @@ void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, 
     Events ev_dec, ev_pred;
     CK(cudaEventRecord(ev_dec.a, st));
     huffman_decode_device(p, end, nb, ind, m, st, launches);
+    if (reg_count > nb) throw Fail{FAZ_ERR_FORMAT, "bad regression block count"};
+    float *drec = nullptr;
+    if (reg_count) {
+        // decode_regression_coefficients (MetaRegressionPredictor.hpp:42-80)
+        need(8);
+        uint64_t nrunp;
+        std::memcpy(&nrunp, p, 8);
+        p += 8;
+        if ((size_t)(end - p) / 4 < nrunp) throw Fail{FAZ_ERR_FORMAT, "truncated regression coefficients"};
+        const float *runp = reinterpret_cast<const float *>(p);
+        p += nrunp * 4;
+        uint16_t *dtypes = m.alloc<uint16_t>(4 * reg_count);
+        huffman_decode_device(p, end, 4 * reg_count, dtypes, m, st, launches);
+        std::vector<uint16_t> hind(nb), htypes(4 * reg_count);
+        CK(cudaMemcpyAsync(hind.data(), ind, nb * 2, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(htypes.data(), dtypes, htypes.size() * 2, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        uint64_t nreg = 0;
+        for (uint16_t v : hind) nreg += v == 1;
+        if (nreg != reg_count) throw Fail{FAZ_ERR_FORMAT, "regression block count does not match the indicators"};
+        std::vector<float> rec;
+        reg_chain_decompress<T>(hind, htypes, runp, nrunp, eb_lin, eb_ind, rec);
+        drec = m.alloc<float>(4 * nb);
+        CK(cudaMemcpyAsync(drec, rec.data(), nb * 16, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+    }
     need(1 + 8 + 4 + 8);
     p += 1;
     double eb;
@@ -432,6 +643,7 @@ void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, 
     if (nz != nunpred) throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
     CK(cudaEventRecord(ev_dec.b, st));
     LorArgs a = make_args<T>(dims, bs, pd, 1, 1, eb, radius);
+    a.rp = drec;
     unsigned long long *vcount = nullptr;
     if (verify_fast_path()) {
         vcount = m.alloc<unsigned long long>(1);

@@ -32,10 +32,12 @@ def _rc(name):
 # default configuration, no QoZ tuning, 3-D (the GPU tuner covers sampled 3-D fields)
 SZ3_CASES = [c["name"] for c in golden_manifest()
              if c["ini"] is None and "-q" not in c["flags"] and len(c["dims"]) == 3 and _rc(c["name"]).quantbinCnt <= 65536]
-# Lorenzo streams without regression blocks
+# Lorenzo / regression streams
 LOR_DEC_CASES = [c["name"] for c in golden_manifest()
-                 if _rc(c["name"]).cmprAlgo == ALGO_LORENZO_REG and not _rc(c["name"]).regression
-                 and _rc(c["name"]).quantbinCnt <= 65536]
+                 if _rc(c["name"]).cmprAlgo == ALGO_LORENZO_REG and _rc(c["name"]).quantbinCnt <= 65536]
+# explicit ALGO_LORENZO_REG runs of the reference (INI), compressed on the GPU
+LOR_INI_CASES = [c["name"] for c in golden_manifest()
+                 if c["ini"] is not None and _rc(c["name"]).cmprAlgo == ALGO_LORENZO_REG]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -82,10 +84,20 @@ def test_gpu_decodes_reference_lorenzo_streams(name):
     assert hashlib.sha256(dec.tobytes()).hexdigest() == case["dec_sha256"]
 
 
-def _lor_conf(dims, rel=None, abs_=None, bs=6, lo2=0, pd=None, qbins=65536):
+@pytest.mark.parametrize("name", LOR_INI_CASES)
+def test_gpu_lorenzo_regression_matches_reference(name):
+    case = golden_case(name)
+    x = golden_input(case)
+    stream = F.SZ_compress(cli_config(case), x)
+    _, p1 = O.read_stream(stream)
+    _, p2 = O.read_stream(golden_stream(case))
+    assert mask_fast_frontend_padding(p1, x.itemsize) == mask_fast_frontend_padding(p2, x.itemsize)
+
+
+def _lor_conf(dims, rel=None, abs_=None, bs=6, lo2=0, pd=None, qbins=65536, reg=0, lo=1):
     c = F.Config(*dims)
     c.cmprAlgo = F.ALGO_LORENZO_REG
-    c.lorenzo, c.lorenzo2, c.regression, c.regression2 = 1, lo2, 0, 0
+    c.lorenzo, c.lorenzo2, c.regression, c.regression2 = lo, lo2, reg, 0
     c.blockSize = bs
     if pd is not None:
         c.pred_dim = pd
@@ -106,6 +118,12 @@ LOR_CASES = [
     ((1, 50, 60), dict(rel=1e-3, lo2=1, bs=4), np.float32),
     ((5, 6, 7), dict(abs_=0.5, bs=6, qbins=1024), np.float32),
     ((96, 64, 48), dict(rel=1e-5, lo2=1, qbins=4096), np.float32),
+    # with linear regression blocks
+    ((40, 44, 52), dict(rel=1e-3, reg=1), np.float32),
+    ((37, 41, 29), dict(rel=1e-3, reg=1, lo2=1, bs=4), np.float32),
+    ((30, 33, 35), dict(rel=1e-5, reg=1), np.float64),
+    ((21, 22, 23), dict(rel=1e-2, reg=1, lo=0), np.float32),
+    ((64, 64, 64), dict(rel=1e-4, reg=1, lo2=1, pd=2), np.float32),
 ]
 
 
@@ -139,10 +157,6 @@ def test_gpu_lorenzo_fast_path_agrees_with_double_path(monkeypatch):
 def test_gpu_lorenzo_rejects_what_it_does_not_implement():
     dims = (20, 20, 20)
     x = spectral_field(dims, slope=-3.0, seed=1)
-    conf = _lor_conf(dims, rel=1e-3)
-    conf.regression = 1
-    with pytest.raises(F.FazError):
-        F.SZ_compress(conf, x)
     conf = _lor_conf(dims, rel=1e-3, bs=9)
     with pytest.raises(F.FazError):
         F.SZ_compress(conf, x)
