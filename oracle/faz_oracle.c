@@ -23,6 +23,7 @@
  */
 #define _GNU_SOURCE
 #include <dlfcn.h>
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -740,7 +741,7 @@ int orc_interp_compress(const faz_config *conf, int dtype, const void *data, int
         r.q.radius = radius;
         r.q.trim = conf->trimToZero;
         q_set_eb_f32(&r.q, conf->absErrorBound);
-        levels_f32(&r, &p);
+        levels_f32(&r, &p, 0, 0, NULL);
         unpred = r.q.unpred;
         nun = r.q.nunpred;
         eb = r.q.eb;
@@ -749,7 +750,7 @@ int orc_interp_compress(const faz_config *conf, int dtype, const void *data, int
         r.q.radius = radius;
         r.q.trim = conf->trimToZero;
         q_set_eb_f64(&r.q, conf->absErrorBound);
-        levels_f64(&r, &p);
+        levels_f64(&r, &p, 0, 0, NULL);
         unpred = r.q.unpred;
         nun = r.q.nunpred;
         eb = r.q.eb;
@@ -827,6 +828,188 @@ static double data_range(int dtype, const void *data, size_t n) {
     return mx - mn;
 }
 
+#define T float
+#define SFX f32
+#include "oracle_qoz.inc"
+#undef T
+#undef SFX
+#define T double
+#define SFX f64
+#include "oracle_qoz.inc"
+#undef T
+#undef SFX
+
+/*
+ * QoZ tuning (Tuning with conf.QoZ, include/QoZ/api/impl/SZInterp.hpp:1588-2557,
+ * TUNING_TARGET_RD, no wavelets, no profiling): QoZ defaults, sampled blocks,
+ * per-level interpolator and direction by summed prediction loss (tuning-2
+ * compressions), then the alpha/beta search by bit rate and PSNR of trial
+ * compressions (CompressTest).  On return conf holds the decisions.
+ */
+static int qoz_tune(faz_config *conf, int dtype, const void *data) {
+    int N = conf->N;
+    if (N != 2 && N != 3) { set_err("oracle QoZ tuner covers 2-D and 3-D data"); return -2; }
+    if (conf->tuningTarget != 0 || conf->wavelet > 0 || conf->FZ) { set_err("oracle QoZ tuner covers the RD target"); return -2; }
+    size_t es = dtype == FAZ_FLOAT ? 4 : 8;
+    double rngT = dtype == FAZ_FLOAT ? (double)(float)conf->rng : conf->rng;   /* T rng = conf.rng */
+    double rel_bound = conf->relErrorBound > 0 ? conf->relErrorBound : conf->absErrorBound / rngT;
+    if (conf->autoTuningRate <= 0) conf->autoTuningRate = N == 2 ? 0.01 : 0.005;
+    if (conf->predictorTuningRate <= 0) conf->predictorTuningRate = N == 2 ? 0.01 : 0.005;
+    if (conf->maxStep <= 0) conf->maxStep = N == 2 ? 64 : 32;
+    if (conf->levelwisePredictionSelection <= 0) conf->levelwisePredictionSelection = N == 2 ? 6 : 4;
+    if (conf->sampleBlockSize <= 0) conf->sampleBlockSize = N == 2 ? 64 : 32;
+    /* FAZ features off (SZInterp.hpp:1611-1622); pyBind, sperr, conditioning and
+     * sperrWithoutWave are trailer fields */
+    conf->profiling = 0;
+    conf->testLorenzo = 0;
+    conf->sperr = -1;
+    conf->conditioning = 0;
+    conf->pyBind = 0;
+    conf->sperrWithoutWave = 0;
+    int max_interp_level = -1;
+    for (int i = 0; i < N; i++) {
+        int l = (int)ceil(log2((double)conf->dims[i]));
+        if (max_interp_level < l) max_interp_level = l;
+    }
+    if (conf->maxStep > 0) {
+        int t = (int)(unsigned)log2((double)conf->maxStep);
+        if (t <= max_interp_level) max_interp_level = t;
+        if (conf->levelwisePredictionSelection > max_interp_level) conf->levelwisePredictionSelection = max_interp_level;
+    }
+    size_t shortest = conf->dims[0];
+    for (int i = 0; i < N; i++) if (conf->dims[i] < shortest) shortest = conf->dims[i];
+    size_t minimum_sbs = 16;
+    if ((size_t)conf->sampleBlockSize < minimum_sbs) conf->sampleBlockSize = (int)minimum_sbs;
+    while ((size_t)conf->sampleBlockSize >= shortest) conf->sampleBlockSize /= 2;
+    while (conf->autoTuningRate > 0 && (size_t)conf->sampleBlockSize >= 2 * minimum_sbs &&
+           (pow(conf->sampleBlockSize, N) / (double)conf->num) > 1.5 * conf->autoTuningRate)
+        conf->sampleBlockSize /= 2;
+    size_t sbs = (size_t)conf->sampleBlockSize, bsz = sbs + 1;
+    size_t per = N == 3 ? bsz * bsz * bsz : bsz * bsz;
+    if (!(conf->predictorTuningRate > 0 && conf->predictorTuningRate < 1)) { set_err("predictorTuningRate outside (0,1)"); return -2; }
+    size_t gdims[4];
+    for (int i = 0; i < N; i++) gdims[i] = conf->dims[i];
+    void *blocks;
+    size_t nblk = dtype == FAZ_FLOAT
+                      ? qoz_sample_f32((const float *)data, N, gdims, sbs, conf->predictorTuningRate, (float **)&blocks)
+                      : qoz_sample_f64((const double *)data, N, gdims, sbs, conf->predictorTuningRate, (double **)&blocks);
+    double o_alpha = conf->alpha, o_beta = conf->beta;
+    if (conf->autoTuningRate > 0) {
+        /* setABwithRelBound(rel_bound, 0) (SZInterp.hpp:1394-1420) */
+        double a, b;
+        if (rel_bound >= 0.01) { a = 2; b = 2; }
+        else if (rel_bound >= 0.007) { a = 1.75; b = 2; }
+        else if (rel_bound >= 0.004) { a = 1.5; b = 2; }
+        else if (rel_bound > 0.001) { a = 1.25; b = 1.5; }
+        else { a = 1; b = 1; }
+        conf->alpha = a;
+        conf->beta = b;
+    }
+    int L = conf->levelwisePredictionSelection;
+    uint8_t il[FAZ_MAX_LEVELS], dl[FAZ_MAX_LEVELS];
+    int dirs[2] = {0, N == 3 ? 5 : 1};
+    size_t bd[4] = {bsz, bsz, bsz, bsz};
+    if (L > 0) {
+        /* one compressor (one quantiser) for every trial of this loop */
+        quant_f32 q32; quant_f64 q64;
+        memset(&q32, 0, sizeof q32); memset(&q64, 0, sizeof q64);
+        q32.radius = q64.radius = 32768;
+        q32.trim = q64.trim = conf->trimToZero;
+        q_set_eb_f32(&q32, conf->absErrorBound);
+        q_set_eb_f64(&q64, conf->absErrorBound);
+        void *work = malloc(per * es);
+        for (int level = L; level > 0; level--) {
+            int start_level = level == L ? 9999 : level, end_level = level - 1;
+            int best_op = 1, best_dir = 0;
+            double best = DBL_MAX;
+            for (int op = 0; op < 2; op++)
+                for (int di = 0; di < 2; di++) {
+                    orc_params p = {op, dirs[di], conf->interpBlockSize, conf->fixBlockSize, conf->alpha, conf->beta,
+                                    0, NULL, NULL};
+                    double cur = 0;
+                    for (size_t k = 0; k < nblk; k++) {
+                        orc_ctx c;
+                        ctx_init(&c, N, bd, conf->maxStep);
+                        memcpy(work, (const uint8_t *)blocks + k * per * es, per * es);
+                        if (dtype == FAZ_FLOAT) cur += qoz_run_f32(&q32, &c, (float *)work, 2, &p, start_level, end_level, NULL);
+                        else cur += qoz_run_f64(&q64, &c, (double *)work, 2, &p, start_level, end_level, NULL);
+                        free(c.codes);
+                    }
+                    if (cur < best) { best = cur; best_op = op; best_dir = dirs[di]; }
+                }
+            il[level - 1] = (uint8_t)best_op;
+            dl[level - 1] = (uint8_t)best_dir;
+        }
+        /* the candidate loop leaves its last candidate in the configuration */
+        conf->interpAlgo = 1;
+        conf->interpDirection = (uint8_t)dirs[1];
+        free(work);
+        free(q32.unpred);
+        free(q64.unpred);
+    }
+    conf->alpha = o_alpha;
+    conf->beta = o_beta;
+    /* B-M tuning (SZInterp.hpp:2187-2515) */
+    if (conf->autoTuningRate > 0) {
+        double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
+        static const double alist[] = {1, 1.25, 1.5, 1.75, 2};
+        static const double blist[] = {1.5, 2, 3, 4};
+        double oriabseb = conf->absErrorBound;
+        for (int i = 0; i < 5; i++) {
+            for (int j = 0; j < 4; j++) {
+                double alpha = alist[i], beta = blist[j];
+                conf->absErrorBound = oriabseb;
+                if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
+                orc_params p = {conf->interpAlgo, conf->interpDirection, conf->interpBlockSize, conf->fixBlockSize,
+                                alpha, beta, L, il, dl};
+                double br, m;
+                int rc = dtype == FAZ_FLOAT
+                             ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
+                                                     conf->trimToZero, conf->maxStep, conf->rng, &br, &m)
+                             : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
+                                                     conf->trimToZero, conf->maxStep, conf->rng, &br, &m);
+                if (rc) { free(blocks); return rc; }
+                if (m >= bestm && br <= bestb) {
+                    bestalpha = alpha; bestbeta = beta; bestb = br; bestm = m;
+                } else if (m <= bestm && br >= bestb) {
+                    if ((alpha >= 1 && pow(alpha, max_interp_level - 1) <= beta) ||
+                        (alpha < 1 && alpha * (max_interp_level - 1) <= beta))
+                        break;
+                    continue;
+                } else {
+                    double fix = br / bestb;
+                    double br2, m2;
+                    rc = dtype == FAZ_FLOAT
+                             ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound * fix,
+                                                     conf->trimToZero, conf->maxStep, conf->rng, &br2, &m2)
+                             : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound * fix,
+                                                     conf->trimToZero, conf->maxStep, conf->rng, &br2, &m2);
+                    if (rc) { free(blocks); return rc; }
+                    double a = (m - m2) / (br - br2);
+                    double bb = m - a * br;
+                    double reg = a * bestb + bb;
+                    if (reg > bestm) { bestalpha = alpha; bestbeta = beta; bestb = br; bestm = m; }
+                }
+                if ((alpha >= 1 && pow(alpha, max_interp_level - 1) <= beta) ||
+                    (alpha < 1 && alpha * (max_interp_level - 1) <= beta))
+                    break;
+            }
+        }
+        conf->absErrorBound = oriabseb;
+        conf->alpha = bestalpha;
+        conf->beta = bestbeta;
+        conf->wavelet_rel_coeff = 1;
+        conf->wavelet = 0;
+    }
+    if (L > 0) {
+        conf->interp_list_len = L;
+        for (int i = 0; i < L; i++) { conf->interpAlgo_list[i] = il[i]; conf->interpDirection_list[i] = dl[i]; }
+    }
+    conf->cmprAlgo = FAZ_ALGO_INTERP;
+    free(blocks);
+    return 0;
+}
+
 /* Fast-frontend payload of a 3-D field (SZ_compress_LorenzoReg with N == 3,
  * include/QoZ/api/impl/SZLorenzoReg.hpp:94-114). */
 static int lorenzo3_payload(int dtype, const void *data, const size_t *dims, int bs, int pd, int lo, int lo2, int reg,
@@ -893,9 +1076,9 @@ static int sz3_tune(faz_config *conf, int dtype, const void *data) {
     size_t es = dtype == FAZ_FLOAT ? 4 : 8;
     if (conf->rng < 0) conf->rng = data_range(dtype, data, conf->num);
     if (conf->relErrorBound <= 0) conf->relErrorBound = conf->absErrorBound / conf->rng;
-    if (conf->QoZ || conf->autoTuningRate > 0 || conf->predictorTuningRate > 0 || conf->preTrim > 0 ||
-        conf->wavelet > 0) {
-        set_err("oracle covers the SZ3 tuner only");
+    if (conf->QoZ) return qoz_tune(conf, dtype, data);
+    if (conf->autoTuningRate > 0 || conf->predictorTuningRate > 0 || conf->preTrim > 0 || conf->wavelet > 0) {
+        set_err("oracle covers the SZ3 and QoZ tuners only");
         return -2;
     }
     size_t sn, sd[4], sb;
@@ -1122,7 +1305,7 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
         memcpy(rr.q.unpred, unp, nun * 4);
         rr.q.nunpred = nun;
         q_set_eb_f32(&rr.q, eb);
-        levels_f32(&rr, &p);
+        levels_f32(&rr, &p, 0, 0, NULL);
         free(rr.q.unpred);
     } else {
         run_f64 rr; memset(&rr, 0, sizeof rr); rr.c = &c; rr.data = (double *)dec; rr.decompress = 1;
@@ -1132,7 +1315,7 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
         memcpy(rr.q.unpred, unp, nun * 8);
         rr.q.nunpred = nun;
         q_set_eb_f64(&rr.q, eb);
-        levels_f64(&rr, &p);
+        levels_f64(&rr, &p, 0, 0, NULL);
         free(rr.q.unpred);
     }
     free(c.codes);

@@ -103,6 +103,14 @@ def cases():
     out.append(("sz3_lorenzo_abs", sum2d((56, 60, 64), 0.001, seed=53), ["-M", "ABS", "0.02"], None))
     out.append(("sz3_lorenzo_f64_16384", sum2d((56, 60, 64), 1e-8, seed=54, dtype=np.float64),
                 ["-M", "REL", "5e-7"], None))
+    # QoZ tuner (-q): per-level predictors and alpha/beta from trial compressions
+    out.append(("qoz_2blk_1e3", spectral_field((50, 120, 170), slope=-3.0, aniso=(1, 2, 2), seed=61),
+                ["-M", "REL", "1e-3", "-q"], None))
+    out.append(("qoz_f64_1e5", spectral_field((48, 56, 64), slope=-3.5, seed=62, dtype=np.float64),
+                ["-M", "REL", "1e-5", "-q"], None))
+    out.append(("qoz_1e2", spectral_field((40, 72, 90), slope=-2.5, noise=0.02, seed=63),
+                ["-M", "REL", "1e-2", "-q"], None))
+    out.append(("qoz_2d", spectral_field((400, 500), slope=-3.0, seed=64), ["-M", "REL", "5e-3", "-q"], None))
     # explicit Lorenzo / regression fast frontend
     lor = {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {}}
     out.append(("lorreg_default", spectral_field((40, 44, 52), slope=-3.0, seed=55), ["-M", "REL", "1e-3"], lor))

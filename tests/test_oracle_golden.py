@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from conftest import (cli_config, golden_case, golden_input, golden_manifest, golden_stream,
-                      mask_fast_frontend_padding, mask_first_size, tuned_config)
+                      mask_fast_frontend_padding, mask_first_size, parse_interp_header, tuned_config)
 
 import oracle.oracle as O
 
@@ -27,6 +27,8 @@ INI_CASES = [c["name"] for c in golden_manifest() if c["ini"] is not None]
 TUNED_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None and _trailer_algo(c["name"]) == ALGO_INTERP]
 # default configuration (ALGO_INTERP_LORENZO) without QoZ tuning: the SZ3 tuner
 SZ3_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None and "-q" not in c["flags"]]
+# QoZ tuning (-q)
+QOZ_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None and "-q" in c["flags"]]
 ALL_CASES = [c["name"] for c in golden_manifest()]
 
 
@@ -116,3 +118,19 @@ def test_ska_order_small():
     # iteration visits buckets from high to low
     visited = [b[i] for i in order]
     assert visited == sorted(visited, reverse=True)
+
+
+@pytest.mark.parametrize("name", QOZ_CASES)
+def test_oracle_qoz_tuner_matches_reference(name, zstd_lib):
+    """QoZ tuning: per-level interpolators and directions, alpha/beta, then
+    the interpolation stream."""
+    case = golden_case(name)
+    x = golden_input(case)
+    ref = golden_stream(case)
+    rc, rp = O.read_stream(ref)
+    stream, payload = O.compress(cli_config(case), x)
+    h1 = parse_interp_header(rp, len(case["dims"]))
+    h2 = parse_interp_header(payload, len(case["dims"]))
+    assert h1 == h2
+    assert payload == rp
+    _same_stream(stream, ref, zstd_lib, x.itemsize)
