@@ -254,7 +254,9 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
     uint16_t sym[ENC_PER_THREAD];
     unsigned int mybits = 0;
     const uint64_t t0 = c0 + (uint64_t)threadIdx.x * ENC_PER_THREAD;
-    if (t0 + ENC_PER_THREAD <= n) {
+    // symbols of this thread (every 16-bit value is a valid symbol)
+    const int nvalid = t0 >= n ? 0 : (n - t0 >= ENC_PER_THREAD ? ENC_PER_THREAD : (int)(n - t0));
+    if (nvalid == ENC_PER_THREAD) {
         // 16 codes = two 16-byte loads (codes is 256-byte aligned, t0 a multiple of 16)
         const uint4 *cv = reinterpret_cast<const uint4 *>(codes + t0);
         uint4 qa = cv[0], qb = cv[1];
@@ -270,7 +272,7 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
     } else {
         for (int k = 0; k < ENC_PER_THREAD; k++) {
             uint64_t i = t0 + k;
-            sym[k] = i < n ? (uint16_t)(codes[i] - offset) : 0xffff;
+            sym[k] = i < n ? (uint16_t)(codes[i] - offset) : 0;
             if (i < n) mybits += len[sym[k]];
         }
     }
@@ -307,8 +309,7 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
             wi++;
         }
     };
-    for (int k = 0; k < ENC_PER_THREAD; k++) {
-        if (sym[k] == 0xffff) break;
+    for (int k = 0; k < nvalid; k++) {
         const unsigned long long e = packed[sym[k]];
         const int l = (int)((e >> 32) & 0xff);
         if (l <= 32) {
