@@ -199,7 +199,7 @@ void check_config(const faz_config &c) {
     if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
     if (c.cmprAlgo != FAZ_ALGO_INTERP && c.cmprAlgo != FAZ_ALGO_INTERP_LORENZO && c.cmprAlgo != FAZ_ALGO_LORENZO_REG)
         throw Fail{FAZ_ERR_UNSUPPORTED, "cmprAlgo must be ALGO_INTERP, ALGO_INTERP_LORENZO or ALGO_LORENZO_REG"};
-    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.FZ)
+    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.FZ && !c.QoZ)
         throw Fail{FAZ_ERR_UNSUPPORTED, "FAZ features (wavelets, SPERR, conditioning; FZ = 1) are not implemented; "
                                         "set FZ = 0 (faz -F 0)"};
     if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && (c.N != 3 || c.regression2))
@@ -486,6 +486,12 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
     resolve_eb<T>(c, dX, st, launches);
     if (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))
         throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
+    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.QoZ) {
+        // QoZ tuning (the faz tool's -q), then the interpolation compressor
+        auto tt = clk::now();
+        qoz_tune_device<T>(c, dX, st, launches, tm);
+        tm.tune_ms = ms_since(tt);
+    }
     if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) {
         auto tt = clk::now();
         faz_timings tt_tm;

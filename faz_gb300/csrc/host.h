@@ -201,6 +201,9 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
                      const std::function<void(const faz_config &)> &speculate);
 
 template <typename T>
+void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);
+
+template <typename T>
 double device_range(const T *dX, uint64_t n, cudaStream_t st, Counter &launches);
 
 // ------------------------------------------------------- Huffman stages

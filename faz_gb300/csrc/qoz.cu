@@ -1,0 +1,697 @@
+// qoz.cu - the QoZ tuner (QoZ = 1, the faz tool's -q) on the GPU.
+//
+// Reference: Tuning with conf.QoZ (include/QoZ/api/impl/SZInterp.hpp:1588-2557),
+// sampleBlocks (992-1127), CompressTest (1130-1392), setABwithRelBound
+// (1394-1420), init_alphalist / init_betalist (868-933), and
+// SZInterpolationCompressor::compress in its tuning modes
+// (include/QoZ/compressor/SZInterpolationCompressor.hpp:324-470, 924-978).
+//
+// The tuner compresses a few sampled (sbs+1)^N blocks many times: with every
+// candidate interpolator and direction per level (tuning mode 2: summed
+// absolute prediction loss), then with every alpha/beta candidate (tuning
+// mode 1: codes, bit rate after Huffman + zstd, PSNR from summed squared
+// errors).  On the GPU one launch per level and sweep covers every sampled
+// block (one thread per target); each target's error lands at its stream
+// position and k_qz_sum adds the errors in the reference's nesting (per line,
+// then per level block, then a running total), so the sums and therefore
+// the decisions are those of the reference.  The decision logic is the
+// reference's, on the host.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "host.h"
+#include "internal.h"
+#include "quant.cuh"
+
+namespace faz {
+
+size_t zstd_framed_size_host(const uint8_t *p, size_t n);
+
+namespace {
+
+// One level sweep over all sampled blocks.
+struct QzSweep {
+    int64_t offs[3];       // strides inside a block field (3-D embedding)
+    int64_t cpb;           // stream slots per block
+    int axis;              // sweep axis
+    int oth[2];            // the other axes, outer loop first
+    int64_t g[2], cnt[2];  // their grid steps and counts
+    int64_t s, n, tpl;     // stride along the axis, points and targets per line
+    int64_t seg_off;       // first stream slot of this sweep inside a block
+    int cubic;
+    int64_t per;           // values per block
+};
+
+// target index of rank r in a line of n points (inverse of line_rank)
+__device__ __forceinline__ int64_t target_of_rank(int64_t r, int64_t n, int cubic) {
+    if (!cubic || n < 5) return 2 * r + 1;
+    const int64_t ia = (n & 1) ? n - 2 : n - 3;
+    const int64_t cint = (ia - 3) >> 1;
+    if (r < cint) return 3 + 2 * r;
+    if (r == cint) return 1;
+    if (r == cint + 1) return ia;
+    return n - 1;
+}
+
+// MODE 1: quantise, store code / unpredictable value / squared error;
+// MODE 2: store |d - pred|, quantise without keeping anything.
+template <typename T, int MODE, int QM>
+__global__ void k_qz_sweep(QzSweep w, LevelArgs q, T *__restrict__ data, uint16_t *__restrict__ codes,
+                           T *__restrict__ scratch, double *__restrict__ err, uint64_t total) {
+    const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const uint64_t lines = (uint64_t)(w.cnt[0] * w.cnt[1]);
+    const int64_t r = (int64_t)(idx % (uint64_t)w.tpl);
+    const uint64_t L = (idx / (uint64_t)w.tpl) % lines;
+    const uint64_t k = idx / ((uint64_t)w.tpl * lines);
+    int64_t c[3] = {0, 0, 0};
+    c[w.oth[0]] = (int64_t)(L / (uint64_t)w.cnt[1]) * w.g[0];
+    c[w.oth[1]] = (int64_t)(L % (uint64_t)w.cnt[1]) * w.g[1];
+    const int64_t i = target_of_rank(r, w.n, w.cubic);
+    c[w.axis] = i * w.s;
+    T *d = data + k * (uint64_t)w.per + c[0] * w.offs[0] + c[1] * w.offs[1] + c[2] * w.offs[2];
+    const int64_t st = w.s * w.offs[w.axis];
+    const int64_t n = w.n;
+    T pred;
+    if (!w.cubic || n < 5) {
+        if (i + 1 < n) pred = i_linear(d[-st], d[st]);
+        else if (n < 4) pred = d[-st];
+        else pred = linear1_any<T>(d[-3 * st], d[-st]);
+    } else {
+        if (i == 1) pred = i_quad1(d[-st], d[st], d[3 * st]);
+        else if (i + 3 < n) pred = i_cubic(d[-3 * st], d[-st], d[st], d[3 * st]);
+        else if ((n & 1) == 0 && i == n - 1) pred = i_quad3(d[-5 * st], d[-3 * st], d[-st]);
+        else pred = i_quad2(d[-3 * st], d[-st], d[st]);
+    }
+    const uint64_t pos = k * (uint64_t)w.cpb + (uint64_t)w.seg_off + L * (uint64_t)w.tpl + (uint64_t)r;
+    const T orig = *d;
+    T v = orig, uval;
+    const int code = quant_point<T, QM>(v, pred, q, uval);
+    if (MODE == 1) {
+        codes[pos] = (uint16_t)code;
+        if (code == 0) scratch[pos] = uval;
+        const T df = v - orig;
+        err[pos] = (double)(T)(df * df);
+    } else {
+        const T df = orig - pred;
+        err[pos] = (double)(df < 0 ? -df : df);
+    }
+    *d = v;
+}
+
+// build_grid in tuning mode 1 (SZInterpolationCompressor.hpp:854-900): the
+// maxStep grid from maxStep on, code 0, the value unpredictable.  Axes below
+// `e` are the 3-D embedding's leading ones.
+template <typename T>
+__global__ void k_qz_anchor(const T *__restrict__ data, int64_t per, int64_t cpb, int64_t nax, int64_t nay, int64_t naz,
+                            int64_t ms, int e, int64_t o0, int64_t o1, uint16_t *__restrict__ codes,
+                            T *__restrict__ scratch, uint64_t total) {
+    const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const uint64_t na = (uint64_t)(nax * nay * naz);
+    const uint64_t k = idx / na, a = idx % na;
+    const int64_t z = (int64_t)(a % (uint64_t)naz), y = (int64_t)((a / (uint64_t)naz) % (uint64_t)nay),
+                  x = (int64_t)(a / ((uint64_t)naz * (uint64_t)nay));
+    const int64_t cx = e > 0 ? 0 : (x + 1) * ms, cy = e > 1 ? 0 : (y + 1) * ms, cz = (z + 1) * ms;
+    const T v = data[k * (uint64_t)per + cx * o0 + cy * o1 + cz];
+    codes[k * (uint64_t)cpb + a] = 0;
+    scratch[k * (uint64_t)cpb + a] = v;
+}
+
+// The first point against prediction 0 (no anchor grid).
+template <typename T, int MODE>
+__global__ void k_qz_first(LevelArgs q, T *__restrict__ data, int64_t per, int64_t cpb, uint16_t *__restrict__ codes,
+                           T *__restrict__ scratch, uint64_t nblk) {
+    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nblk) return;
+    T v = data[k * (uint64_t)per], uval;
+    const int code = quantize<T>(v, (T)0, q.eb, q.recip, q.radius, q.trim, uval);
+    if (MODE == 1) {
+        codes[k * (uint64_t)cpb] = (uint16_t)code;
+        if (code == 0) scratch[k * (uint64_t)cpb] = uval;
+    }
+    data[k * (uint64_t)per] = v;
+}
+
+struct SumSeg {
+    int64_t off;    // first slot
+    int64_t lines;  // lines of this sweep
+    int64_t tpl;    // targets per line
+    int level_end;  // 1 when this is the level's last sweep
+};
+constexpr int kMaxSegs = 64;
+struct SumPlan {
+    int nseg;
+    int64_t cpb;
+    SumSeg seg[kMaxSegs];
+};
+
+// Per block: sum of line sums per level block, running total over levels
+// (block_interpolation_1d / block_interpolation / compress accumulation).
+__global__ void k_qz_sum(SumPlan p, const double *__restrict__ err, double *__restrict__ out, uint64_t nblk) {
+    const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nblk) return;
+    const double *e = err + k * (uint64_t)p.cpb;
+    double total = 0, blk = 0;
+    for (int sgi = 0; sgi < p.nseg; sgi++) {
+        const SumSeg sg = p.seg[sgi];
+        const double *x = e + sg.off;
+        for (int64_t l = 0; l < sg.lines; l++) {
+            double ls = 0;
+            for (int64_t t = 0; t < sg.tpl; t++) ls += x[t];
+            blk += ls;
+            x += sg.tpl;
+        }
+        if (sg.level_end) {
+            total += blk;
+            blk = 0;
+        }
+    }
+    out[k] = total;
+}
+
+// q_bins of CompressTest: for each level range, every block's codes of it.
+__global__ void k_qz_regroup(const uint16_t *__restrict__ codes, int64_t cpb, const int64_t *__restrict__ rlo,
+                             const int64_t *__restrict__ rlen, const int64_t *__restrict__ rout, int nr, uint64_t nblk,
+                             uint16_t *__restrict__ out, uint64_t total) {
+    const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    // find the range (few of them)
+    int g = 0;
+    while (g + 1 < nr && idx >= (uint64_t)rout[g + 1]) g++;
+    const uint64_t o = idx - (uint64_t)rout[g];
+    const uint64_t k = o / (uint64_t)rlen[g], m = o % (uint64_t)rlen[g];
+    out[idx] = codes[k * (uint64_t)cpb + (uint64_t)rlo[g] + m];
+}
+
+template <typename T>
+__global__ void k_qz_gather(const T *__restrict__ X, const int64_t *__restrict__ starts, int64_t d1, int64_t d2,
+                            int64_t bsz, int N, T *__restrict__ out, uint64_t total) {
+    const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const uint64_t per = N == 3 ? (uint64_t)(bsz * bsz * bsz) : (uint64_t)(bsz * bsz);
+    const uint64_t k = idx / per, o = idx % per;
+    const int64_t *s = starts + 3 * k;
+    uint64_t src;
+    if (N == 3) {
+        const int64_t z = (int64_t)(o % (uint64_t)bsz), y = (int64_t)((o / (uint64_t)bsz) % (uint64_t)bsz),
+                      x = (int64_t)(o / ((uint64_t)bsz * (uint64_t)bsz));
+        src = (uint64_t)(x + s[0]) * (uint64_t)(d1 * d2) + (uint64_t)(y + s[1]) * (uint64_t)d2 + (uint64_t)(z + s[2]);
+    } else {
+        const int64_t y = (int64_t)(o % (uint64_t)bsz), x = (int64_t)(o / (uint64_t)bsz);
+        src = (uint64_t)(x + s[0]) * (uint64_t)d2 + (uint64_t)(y + s[1]);
+    }
+    out[idx] = X[src];
+}
+
+double level_eb_of(double eb, double alpha, double beta, int level) {
+    if (alpha < 0) return level >= 3 ? eb * 0.5 : eb;
+    if (alpha >= 1) {
+        double cr = std::pow(alpha, level - 1);
+        if (cr > beta) cr = beta;
+        return eb / cr;
+    }
+    double cr = 1 - (level - 1) * alpha;
+    if (cr < beta) cr = beta;
+    return eb * cr;
+}
+
+int ceil_log2_u(uint64_t d) {
+    int l = 0;
+    while (((uint64_t)1 << l) < d) l++;
+    return l;
+}
+
+// Geometry of a sampled block as an N-D field for the interpolation
+// compressor (one interpolation block per level: interpBlockSize >= sbs).
+struct QzGeom {
+    int N, e;              // dims and 3-D embedding offset
+    int64_t bsz, per;
+    int64_t offs[3];
+    int levels;            // interpolation_level after init()
+    bool anchor;
+    int64_t ms;
+    int64_t na[3];         // anchors per axis in tuning mode 1
+    int64_t nanchor;
+    int64_t cpb;           // stream slots per block (full run, mode 1)
+};
+
+QzGeom make_geom(int N, int64_t bsz, int64_t maxStep) {
+    QzGeom g;
+    std::memset(&g, 0, sizeof(g));
+    g.N = N;
+    g.e = 3 - N;
+    g.bsz = bsz;
+    g.per = 1;
+    for (int i = 0; i < N; i++) g.per *= bsz;
+    int64_t d3[3] = {1, 1, 1};
+    for (int i = 0; i < N; i++) d3[g.e + i] = bsz;
+    g.offs[2] = 1;
+    g.offs[1] = d3[2];
+    g.offs[0] = d3[1] * d3[2];
+    g.levels = ceil_log2_u((uint64_t)bsz);
+    g.ms = maxStep;
+    if (maxStep > 0) {
+        g.anchor = true;
+        g.levels += 1;
+        int lm = 0;
+        while (((uint64_t)1 << (lm + 1)) <= (uint64_t)maxStep) lm++;
+        lm += 1;
+        if (lm <= g.levels) g.levels = lm;
+        for (int i = 0; i < 3; i++) g.na[i] = 1;
+        g.nanchor = 1;
+        for (int i = 0; i < N; i++) {
+            // x = maxStep, 2 maxStep, ... < bsz
+            g.na[g.e + i] = bsz > maxStep ? (bsz - 1) / maxStep : 0;
+            g.nanchor *= g.na[g.e + i];
+        }
+    }
+    return g;
+}
+
+const int P3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+
+// One tuning run over levels [start, end+1] of every sampled block.
+struct QzRun {
+    int mode;                   // 1 or 2
+    int start_level, end_level; // after the reference's clamping
+    double eb, alpha, beta;
+    int trim;
+    int interp, dir;            // when no level list
+    const std::vector<uint8_t> *il, *dl;
+};
+
+template <typename T>
+void qz_run(const QzGeom &g, const QzRun &R, T *work, uint16_t *codes, T *scratch, double *err, uint64_t nblk,
+            SumPlan &sp, std::vector<std::pair<int64_t, int64_t>> *level_ranges, cudaStream_t st, Counter &launches) {
+    sp.nseg = 0;
+    sp.cpb = g.cpb;
+    int64_t pos = 0;
+    int start = R.start_level;
+    if (!g.anchor) {
+        LevelArgs q;
+        std::memset(&q, 0, sizeof(q));
+        q.eb = R.eb;
+        q.recip = 1.0 / R.eb;
+        q.radius = 32768;
+        q.trim = R.trim;
+        if (R.mode == 1)
+            k_qz_first<T, 1><<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(q, work, g.per, g.cpb, codes, scratch, nblk);
+        else
+            k_qz_first<T, 2><<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(q, work, g.per, g.cpb, codes, scratch, nblk);
+        launches(cudaGetLastError());
+        pos = 1;
+    } else if (start == g.levels) {
+        if (R.mode == 1 && g.nanchor > 0) {
+            const uint64_t total = (uint64_t)g.nanchor * nblk;
+            // axis strides of the embedded field for the anchor coordinates
+            k_qz_anchor<T><<<(unsigned)((total + 127) / 128), 128, 0, st>>>(
+                work, g.per, g.cpb, g.na[0], g.na[1], g.na[2], g.ms, g.e, g.offs[0], g.offs[1], codes, scratch, total);
+            launches(cudaGetLastError());
+        }
+        pos = R.mode == 1 ? g.nanchor : 0;
+        start--;
+    }
+    if (level_ranges) level_ranges->clear();
+    int64_t range_lo = 0;
+    // stream slots of levels above `start` (full-run layout) for mode 2
+    // runs that begin below the top
+    {
+        int64_t p0 = g.anchor ? g.nanchor : 1;
+        for (int level = g.levels - (g.anchor ? 1 : 0); level > start; level--) {
+            const int64_t s = (int64_t)1 << (level - 1);
+            int64_t lvl = 0;
+            for (int sw = 0; sw < g.N; sw++) {
+                int64_t lines = 1;
+                // line counts do not depend on the direction's axis order
+                for (int u = 0; u < g.N; u++)
+                    if (u != sw) lines *= (g.bsz - 1) / (u < sw ? s : 2 * s) + 1;
+                lvl += lines * (((g.bsz - 1) / s + 1) / 2);
+            }
+            p0 += lvl;
+        }
+        if (R.mode == 2) pos = p0;
+    }
+    for (int level = start; level > R.end_level; level--) {
+        LevelArgs q;
+        std::memset(&q, 0, sizeof(q));
+        q.eb = level_eb_of(R.eb, R.alpha, R.beta, level);
+        q.recip = 1.0 / q.eb;
+        q.radius = 32768;
+        q.trim = R.trim;
+        set_fast_path<T>(q);
+        const bool straight = sizeof(T) == 4 && q.fast && q.trim == 0;
+        int interp = R.interp, dir = R.dir;
+        if (R.il && !R.il->empty()) {
+            const size_t li = (size_t)(level - 1) < R.il->size() ? (size_t)(level - 1) : R.il->size() - 1;
+            interp = (*R.il)[li];
+            dir = (*R.dl)[li];
+        }
+        int perm[3] = {0, 1, 2};
+        if (g.N == 2) {
+            if (dir != 0) {
+                perm[0] = 1;
+                perm[1] = 0;
+            }
+        } else if (g.N == 3) {
+            if (dir < 0 || dir > 5) throw Fail{FAZ_ERR_ARG, "interpolation direction out of range"};
+            for (int i = 0; i < 3; i++) perm[i] = P3[dir][i];
+        }
+        const int64_t s = (int64_t)1 << (level - 1);
+        for (int d = 0; d < g.N; d++) {
+            QzSweep w;
+            std::memset(&w, 0, sizeof(w));
+            for (int i = 0; i < 3; i++) w.offs[i] = g.offs[i];
+            w.cpb = g.cpb;
+            w.per = g.per;
+            w.axis = g.e + perm[d];
+            int no = 0;
+            w.g[0] = w.g[1] = 1;
+            w.cnt[0] = w.cnt[1] = 1;
+            w.oth[0] = w.oth[1] = 0;
+            for (int ee = 0; ee < g.N; ee++) {
+                if (ee == d) continue;
+                w.oth[no] = g.e + perm[ee];
+                w.g[no] = ee < d ? s : 2 * s;
+                w.cnt[no] = (g.bsz - 1) / w.g[no] + 1;
+                no++;
+            }
+            if (g.N == 2) {  // the missing axis: the embedding's leading one
+                w.oth[1] = w.oth[0];
+                w.g[1] = w.g[0];
+                w.cnt[1] = w.cnt[0];
+                w.oth[0] = 0;
+                w.g[0] = 1;
+                w.cnt[0] = 1;
+            } else if (g.N == 1) {
+                w.oth[0] = 0;
+                w.oth[1] = 1;
+            }
+            w.s = s;
+            w.n = (g.bsz - 1) / s + 1;
+            w.tpl = w.n / 2;
+            w.cubic = interp == FAZ_INTERP_ALGO_CUBIC;
+            w.seg_off = pos;
+            const int64_t lines = w.cnt[0] * w.cnt[1];
+            const uint64_t total = (uint64_t)(lines * w.tpl) * nblk;
+            if (total) {
+                const unsigned grid = (unsigned)((total + 255) / 256);
+                if (R.mode == 1) {
+                    if (straight) k_qz_sweep<T, 1, 1><<<grid, 256, 0, st>>>(w, q, work, codes, scratch, err, total);
+                    else k_qz_sweep<T, 1, 0><<<grid, 256, 0, st>>>(w, q, work, codes, scratch, err, total);
+                } else {
+                    if (straight) k_qz_sweep<T, 2, 1><<<grid, 256, 0, st>>>(w, q, work, codes, scratch, err, total);
+                    else k_qz_sweep<T, 2, 0><<<grid, 256, 0, st>>>(w, q, work, codes, scratch, err, total);
+                }
+                launches(cudaGetLastError());
+            }
+            if (sp.nseg >= kMaxSegs) throw Fail{FAZ_ERR_UNSUPPORTED, "too many tuning levels"};
+            sp.seg[sp.nseg++] = SumSeg{pos, lines, w.tpl, d == g.N - 1 ? 1 : 0};
+            pos += lines * w.tpl;
+        }
+        if (level_ranges) {
+            level_ranges->push_back({range_lo, pos});
+            range_lo = pos;
+        }
+    }
+}
+
+// Codes per block of a full tuning-1 run.
+int64_t full_run_slots(const QzGeom &g) {
+    int64_t p = g.anchor ? g.nanchor : 1;
+    for (int level = g.levels - (g.anchor ? 1 : 0); level > 0; level--) {
+        const int64_t s = (int64_t)1 << (level - 1);
+        for (int sw = 0; sw < g.N; sw++) {
+            int64_t lines = 1;
+            for (int u = 0; u < g.N; u++)
+                if (u != sw) lines *= (g.bsz - 1) / (u < sw ? s : 2 * s) + 1;
+            p += lines * (((g.bsz - 1) / s + 1) / 2);
+        }
+    }
+    return p;
+}
+
+}  // namespace
+
+// QoZ Tuning for the RD target on 2-D / 3-D data; on return c holds the
+// decisions (per-level lists, alpha, beta, maxStep, ...).
+template <typename T>
+void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm) {
+    const int N = c.N;
+    if (N != 2 && N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for 2-D and 3-D data"};
+    if (c.tuningTarget != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for the PSNR (RD) target"};
+    if (c.rng < 0) c.rng = device_range<T>(dX, c.num, st, launches);
+    if (c.relErrorBound <= 0) c.relErrorBound = c.absErrorBound / c.rng;
+    const double rngT = (double)(T)c.rng;  // T rng = conf.rng
+    const double rel_bound = c.relErrorBound > 0 ? c.relErrorBound : c.absErrorBound / rngT;
+    // QoZ defaults (SZInterp.hpp:1597-1625)
+    if (c.autoTuningRate <= 0) c.autoTuningRate = N == 2 ? 0.01 : 0.005;
+    if (c.predictorTuningRate <= 0) c.predictorTuningRate = N == 2 ? 0.01 : 0.005;
+    if (c.maxStep <= 0) c.maxStep = N == 2 ? 64 : 32;
+    if (c.levelwisePredictionSelection <= 0) c.levelwisePredictionSelection = N == 2 ? 6 : 4;
+    if (c.sampleBlockSize <= 0) c.sampleBlockSize = N == 2 ? 64 : 32;
+    c.profiling = 0;
+    c.testLorenzo = 0;
+    c.sperr = -1;
+    c.conditioning = 0;
+    c.pyBind = 0;
+    c.sperrWithoutWave = 0;
+    int max_interp_level = -1;
+    for (int i = 0; i < N; i++) {
+        const int l = (int)std::ceil(std::log2((double)c.dims[i]));
+        if (max_interp_level < l) max_interp_level = l;
+    }
+    if (c.maxStep > 0) {
+        const int t = (int)(unsigned)std::log2((double)c.maxStep);
+        if (t <= max_interp_level) max_interp_level = t;
+        if (c.levelwisePredictionSelection > max_interp_level) c.levelwisePredictionSelection = max_interp_level;
+    }
+    uint64_t shortest = c.dims[0];
+    for (int i = 0; i < N; i++) shortest = std::min<uint64_t>(shortest, c.dims[i]);
+    const int minimum_sbs = 16;
+    if (c.sampleBlockSize < minimum_sbs) c.sampleBlockSize = minimum_sbs;
+    while ((uint64_t)c.sampleBlockSize >= shortest) c.sampleBlockSize /= 2;
+    while (c.autoTuningRate > 0 && c.sampleBlockSize >= 2 * minimum_sbs &&
+           (std::pow(c.sampleBlockSize, N) / (double)c.num) > 1.5 * c.autoTuningRate)
+        c.sampleBlockSize /= 2;
+    if (!(c.predictorTuningRate > 0 && c.predictorTuningRate < 1))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning needs predictorTuningRate in (0, 1)"};
+    const int64_t sbs = c.sampleBlockSize, bsz = sbs + 1;
+    if (c.fixBlockSize > 0 || c.interpBlockSize < sbs)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning needs interpBlockSize >= sampleBlockSize and no fixBlockSize"};
+    if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};
+    // sampleBlocks (profiling 0, var_first 0)
+    uint64_t stride = (uint64_t)(1.0 / c.predictorTuningRate);
+    if (stride <= 0) stride = 1;
+    std::vector<int64_t> starts;
+    uint64_t idx = 0;
+    const uint64_t d0 = c.dims[0], d1 = c.dims[1], d2 = N == 3 ? c.dims[2] : 1;
+    for (uint64_t x = 0; x < d0 - sbs; x += sbs)
+        for (uint64_t y = 0; y < d1 - sbs; y += sbs)
+            for (uint64_t z = 0; N == 2 ? z == 0 : z < d2 - sbs; z += (N == 3 ? sbs : 1)) {
+                if (idx % stride == 0) {
+                    starts.push_back((int64_t)x);
+                    starts.push_back((int64_t)y);
+                    starts.push_back((int64_t)z);
+                }
+                idx++;
+            }
+    const uint64_t nblk = starts.size() / 3;
+    if (nblk == 0) throw Fail{FAZ_ERR_UNSUPPORTED, "no block to sample for QoZ tuning"};
+    QzGeom g = make_geom(N, bsz, (int64_t)c.maxStep);
+    g.cpb = full_run_slots(g);
+    DevMem m(st);
+    const uint64_t nv = nblk * (uint64_t)g.per, ns = nblk * (uint64_t)g.cpb;
+    T *blocks = m.alloc<T>(nv), *work = m.alloc<T>(nv), *scratch = m.alloc<T>(ns);
+    uint16_t *codes = m.alloc<uint16_t>(ns);
+    double *err = m.alloc<double>(ns), *bsum = m.alloc<double>(nblk);
+    int64_t *dstarts = m.alloc<int64_t>(starts.size());
+    CK(cudaMemcpyAsync(dstarts, starts.data(), starts.size() * 8, cudaMemcpyHostToDevice, st));
+    k_qz_gather<T><<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(dX, dstarts, (int64_t)c.dims[1],
+                                                                  N == 3 ? (int64_t)c.dims[2] : (int64_t)c.dims[1],
+                                                                  bsz, N, blocks, nv);
+    launches(cudaGetLastError());
+    std::vector<double> hsum(nblk);
+    auto block_sums = [&](const SumPlan &sp) -> double {
+        k_qz_sum<<<(unsigned)((nblk + 63) / 64), 64, 0, st>>>(sp, err, bsum, nblk);
+        launches(cudaGetLastError());
+        CK(cudaMemcpyAsync(hsum.data(), bsum, nblk * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        double s = 0;
+        for (uint64_t k = 0; k < nblk; k++) s += hsum[k];
+        return s;
+    };
+    const double o_alpha = c.alpha, o_beta = c.beta;
+    if (c.autoTuningRate > 0) {
+        // setABwithRelBound(rel_bound, 0) (SZInterp.hpp:1394-1420)
+        double a, b;
+        if (rel_bound >= 0.01) a = 2, b = 2;
+        else if (rel_bound >= 0.007) a = 1.75, b = 2;
+        else if (rel_bound >= 0.004) a = 1.5, b = 2;
+        else if (rel_bound > 0.001) a = 1.25, b = 1.5;
+        else a = 1, b = 1;
+        c.alpha = a;
+        c.beta = b;
+    }
+    const int Lsel = c.levelwisePredictionSelection;
+    std::vector<uint8_t> il(Lsel > 0 ? Lsel : 0), dl(Lsel > 0 ? Lsel : 0);
+    const int dirs[2] = {0, N == 3 ? 5 : 1};
+    SumPlan sp;
+    if (Lsel > 0) {
+        // per-level selection by summed prediction loss (tuning mode 2)
+        for (int level = Lsel; level > 0; level--) {
+            int start_level = level == Lsel ? 9999 : level, end_level = level - 1;
+            if (start_level <= 0 || start_level > g.levels) start_level = g.levels;
+            if (end_level >= start_level || end_level < 0) end_level = 0;
+            int best_op = 1, best_dir = 0;
+            double best = DBL_MAX;
+            for (int op = 0; op < 2; op++)
+                for (int di = 0; di < 2; di++) {
+                    CK(cudaMemcpyAsync(work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, st));
+                    QzRun R{2, start_level, end_level, c.absErrorBound, c.alpha, c.beta, c.trimToZero, op, dirs[di],
+                            nullptr, nullptr};
+                    qz_run<T>(g, R, work, codes, scratch, err, nblk, sp, nullptr, st, launches);
+                    const double cur = block_sums(sp);
+                    if (cur < best) {
+                        best = cur;
+                        best_op = op;
+                        best_dir = dirs[di];
+                    }
+                }
+            il[level - 1] = (uint8_t)best_op;
+            dl[level - 1] = (uint8_t)best_dir;
+        }
+        // the candidate loop leaves its last candidate in the configuration
+        c.interpAlgo = FAZ_INTERP_ALGO_CUBIC;
+        c.interpDirection = (uint8_t)dirs[1];
+    }
+    c.alpha = o_alpha;
+    c.beta = o_beta;
+    if (c.autoTuningRate > 0) {
+        // B-M tuning (SZInterp.hpp:2187-2515): CompressTest per alpha/beta
+        std::vector<std::pair<int64_t, int64_t>> ranges;
+        auto compress_test = [&](double alpha, double beta, double eb, double &bitrate, double &psnr) {
+            CK(cudaMemcpyAsync(work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, st));
+            QzRun R{1, g.levels, 0, eb, alpha, beta, c.trimToZero, c.interpAlgo, c.interpDirection, &il, &dl};
+            qz_run<T>(g, R, work, codes, scratch, err, nblk, sp, &ranges, st, launches);
+            const double se = block_sums(sp);
+            // q_bins: level ranges from the coarsest, each across all blocks
+            // (the anchors travel with the first interpolated level)
+            std::vector<int64_t> rlo, rlen, rout;
+            int64_t o = 0;
+            for (size_t i = 0; i < ranges.size(); i++) {
+                const int64_t lo = i == 0 ? 0 : ranges[i].first, hi = ranges[i].second;
+                if (hi <= lo) continue;
+                rlo.push_back(lo);
+                rlen.push_back(hi - lo);
+                rout.push_back(o);
+                o += (hi - lo) * (int64_t)nblk;
+            }
+            if (o != (int64_t)ns) throw Fail{FAZ_ERR_DEVICE, "tuning codes do not cover the sampled blocks"};
+            int64_t *dr = m.alloc<int64_t>(3 * rlo.size() + 3);
+            std::vector<int64_t> hr;
+            hr.insert(hr.end(), rlo.begin(), rlo.end());
+            hr.insert(hr.end(), rlen.begin(), rlen.end());
+            hr.insert(hr.end(), rout.begin(), rout.end());
+            CK(cudaMemcpyAsync(dr, hr.data(), hr.size() * 8, cudaMemcpyHostToDevice, st));
+            uint16_t *qb = m.alloc<uint16_t>(ns);
+            const int nr = (int)rlo.size();
+            k_qz_regroup<<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(codes, g.cpb, dr, dr + nr, dr + 2 * nr, nr, nblk,
+                                                                       qb, ns);
+            launches(cudaGetLastError());
+            HuffEncoded h;
+            huffman_encode_device(qb, ns, 32768, m, st, launches, h, tm);
+            // unpredictable values in the order the quantiser kept them
+            // (block by block, stream order): zeros of the block-major codes
+            const uint64_t nsub = hist_subchunks(ns);
+            unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1), *zoff = m.alloc<unsigned long long>(nsub + 1);
+            unsigned long long *ztmp = m.alloc<unsigned long long>(scan_temp_words(nsub) + 1);
+            launches(launch_count_zeros(codes, ns, zc, st));
+            launches(launch_scan_u64(zc, zoff, nsub, ztmp, st));
+            const uint64_t nunp = h.nzero;
+            T *unp = m.alloc<T>(nunp ? nunp : 1);
+            if (nunp) launches(launch_compact_zeros<T>(codes, ns, zc, zoff, nullptr, scratch, unp, st));
+            std::vector<uint8_t> head;
+            put<uint8_t>(head, 2);
+            put<double>(head, eb);
+            put<int32_t>(head, 32768);
+            put<uint64_t>(head, nunp);
+            std::vector<uint8_t> tree;
+            append_tree(tree, h.cb, h.nbytes);
+            std::vector<uint8_t> pl(head.size() + nunp * sizeof(T) + tree.size() + h.nbytes);
+            std::memcpy(pl.data(), head.data(), head.size());
+            if (nunp) CK(cudaMemcpyAsync(pl.data() + head.size(), unp, nunp * sizeof(T), cudaMemcpyDeviceToHost, st));
+            std::memcpy(pl.data() + head.size() + nunp * sizeof(T), tree.data(), tree.size());
+            if (h.nbytes)
+                CK(cudaMemcpyAsync(pl.data() + head.size() + nunp * sizeof(T) + tree.size(), h.bits, h.nbytes,
+                                   cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            const double ele = (double)nv;
+            bitrate = 8 * (double)zstd_framed_size_host(pl.data(), pl.size()) / ele;
+            psnr = 20 * std::log10(c.rng) - 10 * std::log10(se / ele);
+        };
+        double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
+        static const double alist[] = {1, 1.25, 1.5, 1.75, 2};
+        static const double blist[] = {1.5, 2, 3, 4};
+        const double oriabseb = c.absErrorBound;
+        auto stop_here = [&](double alpha, double beta) {
+            return (alpha >= 1 && std::pow(alpha, max_interp_level - 1) <= beta) ||
+                   (alpha < 1 && alpha * (max_interp_level - 1) <= beta);
+        };
+        for (double alpha : alist) {
+            for (double beta : blist) {
+                if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
+                double br, mm;
+                compress_test(alpha, beta, oriabseb, br, mm);
+                if (mm >= bestm && br <= bestb) {
+                    bestalpha = alpha;
+                    bestbeta = beta;
+                    bestb = br;
+                    bestm = mm;
+                } else if (mm <= bestm && br >= bestb) {
+                    if (stop_here(alpha, beta)) break;
+                    continue;
+                } else {
+                    const double fix = br / bestb;
+                    double br2, m2;
+                    compress_test(alpha, beta, oriabseb * fix, br2, m2);
+                    const double a = (mm - m2) / (br - br2);
+                    const double b = mm - a * br;
+                    const double reg = a * bestb + b;
+                    if (reg > bestm) {
+                        bestalpha = alpha;
+                        bestbeta = beta;
+                        bestb = br;
+                        bestm = mm;
+                    }
+                }
+                if (stop_here(alpha, beta)) break;
+            }
+        }
+        c.absErrorBound = oriabseb;
+        c.alpha = bestalpha;
+        c.beta = bestbeta;
+        c.wavelet_rel_coeff = 1;
+        c.wavelet = 0;
+    }
+    if (Lsel > 0) {
+        c.interp_list_len = Lsel;
+        for (int i = 0; i < Lsel; i++) {
+            c.interpAlgo_list[i] = il[i];
+            c.interpDirection_list[i] = dl[i];
+        }
+    }
+    c.cmprAlgo = FAZ_ALGO_INTERP;
+}
+
+template void qoz_tune_device<float>(faz_config &, const float *, cudaStream_t, Counter &, faz_timings &);
+template void qoz_tune_device<double>(faz_config &, const double *, cudaStream_t, Counter &, faz_timings &);
+
+}  // namespace faz

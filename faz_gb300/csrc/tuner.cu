@@ -429,6 +429,8 @@ void set_dims_defaults(faz_config &c) {
 // SZ_compress_Interp_lorenzo's tuning for the default configuration (no QoZ
 // or rate-driven tuning): on return c.cmprAlgo is ALGO_INTERP or
 // ALGO_LORENZO_REG and the chosen settings are in c.
+size_t zstd_framed_size_host(const uint8_t *p, size_t n) { return zstd_framed_size(p, n); }
+
 template <typename T>
 void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
                      const std::function<void(const faz_config &)> &speculate) {

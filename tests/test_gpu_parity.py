@@ -224,3 +224,20 @@ def test_double_path_only_matches(monkeypatch):
     monkeypatch.setenv("FAZ_FASTPATH", "0")
     s_dp = F.SZ_compress(conf, x)
     assert s_fast == s_dp
+
+
+def test_gpu_full_code_range():
+    """Prediction errors spread over the whole quantisation range: codes
+    cover 0..65535 (offset 0 and the top symbol 65535 both occur)."""
+    dims = (40, 50, 60)
+    rng = np.random.default_rng(7)
+    eb = 1e-3
+    x = (rng.integers(-70000, 70000, size=dims) * (eb * 1.0001)).astype(np.float32)
+    conf = _conf(dims, abs_=eb, interp=F.INTERP_ALGO_LINEAR)
+    codes, _, ref_payload = O.interp_codes(conf, x)
+    assert codes.min() == 0 and codes.max() == 65535
+    stream = F.SZ_compress(conf, x)
+    assert payload_of(stream) == ref_payload
+    dec, _ = F.SZ_decompress(None, stream, dtype=np.float32)
+    ref_dec, _ = O.decompress(O.compress(conf, x)[0])
+    assert np.array_equal(dec.view(np.uint32), ref_dec.view(np.uint32))

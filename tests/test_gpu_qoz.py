@@ -1,0 +1,64 @@
+"""GPU QoZ tuner (QoZ = 1, the faz tool's -q) against the oracle and the
+reference's -q streams: the per-level interpolators and directions, alpha and
+beta, and the resulting interpolation stream."""
+import numpy as np
+import pytest
+
+import faz_gb300 as F
+from faz_gb300.fields import spectral_field
+from conftest import (cli_config, golden_case, golden_input, golden_manifest, golden_stream, mask_first_size,
+                      parse_interp_header)
+
+import oracle.oracle as O
+
+pytestmark = pytest.mark.gpu
+
+QOZ_CASES = [c["name"] for c in golden_manifest() if c["ini"] is None and "-q" in c["flags"]]
+KEYS = ("interp", "direction", "alpha", "beta", "maxStep", "interp_list", "dir_list")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def system_zstd():
+    O.set_zstd(None)
+    yield
+
+
+@pytest.mark.parametrize("name", QOZ_CASES)
+def test_gpu_qoz_matches_reference(name):
+    case = golden_case(name)
+    x = golden_input(case)
+    N = len(case["dims"])
+    stream = F.SZ_compress(cli_config(case), x)
+    _, p = O.read_stream(stream)
+    _, rp = O.read_stream(golden_stream(case))
+    h, hr = parse_interp_header(p, N), parse_interp_header(rp, N)
+    assert {k: h[k] for k in KEYS} == {k: hr[k] for k in KEYS}
+    assert p == rp
+    ref, _ = O.compress(cli_config(case), x)
+    assert mask_first_size(stream) == mask_first_size(ref)
+    dec, c2 = F.SZ_decompress(None, stream, dtype=x.dtype)
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
+
+
+QOZ_RANDOM = [
+    ((64, 80, 96), 1e-3, np.float32, -3.0),
+    ((70, 70, 70), 1e-4, np.float32, -3.5),
+    ((96, 64, 80), 5e-3, np.float32, -2.5),
+    ((300, 420), 1e-3, np.float32, -3.0),
+    ((50, 60, 70), 1e-6, np.float64, -3.0),
+]
+
+
+@pytest.mark.parametrize("dims,rel,dtype,slope", QOZ_RANDOM)
+def test_gpu_qoz_matches_oracle(dims, rel, dtype, slope):
+    conf = F.Config(*dims)
+    conf.QoZ = 1
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = rel
+    x = spectral_field(dims, slope=slope, noise=0.01, seed=sum(dims) + 7, dtype=dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    _, p = O.read_stream(stream)
+    assert parse_interp_header(p, len(dims)) == parse_interp_header(ref_payload, len(dims))
+    assert p == ref_payload
+    assert mask_first_size(stream) == mask_first_size(ref)
