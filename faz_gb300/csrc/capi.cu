@@ -19,6 +19,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -545,13 +546,17 @@ void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, ch
     auto t0 = clk::now();
     std::vector<uint8_t> trailer;
     config_save(c, trailer);
-    size_t bound = z.bound(psize);
+    // FAZ_ZSTD_THREADS (default the host's cores up to 16) cuts a large payload
+    // into independent frames compressed in parallel; 0 writes exactly the
+    // single frame of ZSTD_compress, as the reference does
+    const int nframes = zstd_frame_count(psize, zstd_threads());
+    size_t bound = zstd_frames_bound(z, psize, nframes);
     size_t cap = 8 + bound + trailer.size() + 4;
     char *buf = (char *)std::malloc(cap);
     if (!buf) throw Fail{FAZ_ERR_ARG, "out of host memory"};
     uint64_t raw = psize;
     std::memcpy(buf, &raw, 8);
-    size_t zs = z.compress(buf + 8, bound, payload, psize, 3);
+    size_t zs = zstd_compress_frames(z, (uint8_t *)buf + 8, bound, payload, psize, nframes);
     if (z.isError(zs)) {
         std::free(buf);
         throw Fail{FAZ_ERR_ZSTD, "ZSTD_compress failed"};
@@ -901,7 +906,7 @@ void open_stream(const char *cmp, size_t cmp_size, faz_config &conf, uint8_t *&p
     if (raw > ((uint64_t)1 << 46)) throw Fail{FAZ_ERR_FORMAT, "implausible payload size"};
     payload = t_pin_payload.get(raw + 64);
     auto t0 = clk::now();
-    size_t got = z.decompress(payload, raw, cmp + 8, body - 8);
+    size_t got = zstd_decompress_frames(z, payload, raw, (const uint8_t *)cmp + 8, body - 8, zstd_threads());
     tm.zstd_ms += ms_since(t0);
     if (z.isError(got) || got != raw) throw Fail{FAZ_ERR_ZSTD, "ZSTD_decompress failed"};
     psize = raw;

@@ -108,7 +108,19 @@ struct Zstd {
     unsigned (*isError)(size_t) = nullptr;
     size_t (*bound)(size_t) = nullptr;
     unsigned long long (*frameContentSize)(const void *, size_t) = nullptr;
+    // advanced API (multi-threaded compression of one frame); null if absent
+    size_t (*findFrameCompressedSize)(const void *, size_t) = nullptr;
+    unsigned long long (*getFrameContentSize)(const void *, size_t) = nullptr;
 };
+// The body of a Lossless_zstd stream as `nframes` independent level-3 frames
+// of consecutive payload slices, compressed on host threads; one frame is
+// exactly ZSTD_compress.  ZSTD_decompress decodes the concatenation.
+int zstd_frame_count(size_t n, int threads);
+size_t zstd_frames_bound(const Zstd &z, size_t n, int nframes);
+size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes);
+// Decodes one or more concatenated frames (independent frames in parallel).
+size_t zstd_decompress_frames(const Zstd &z, uint8_t *dst, size_t raw, const uint8_t *src, size_t n, int threads);
+int zstd_threads();  // FAZ_ZSTD_THREADS, default the host's cores up to 16
 const Zstd &zstd_lib(std::string &err);
 
 // ------------------------------------------------------------------ errors

@@ -9,8 +9,12 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <memory>
+#include <new>
 #include <mutex>
 #include <sstream>
+#include <thread>
+#include <vector>
 
 #include "internal.h"
 
@@ -381,10 +385,111 @@ const Zstd &zstd_lib(std::string &err) {
             return;
         }
         z.version = ver();
+        z.findFrameCompressedSize = (size_t(*)(const void *, size_t))dlsym(h, "ZSTD_findFrameCompressedSize");
+        z.getFrameContentSize = (unsigned long long (*)(const void *, size_t))dlsym(h, "ZSTD_getFrameContentSize");
         z.ok = true;
     });
     if (!z.ok) err = load_err;
     return z;
+}
+
+int zstd_threads() {
+    int t = (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
+    if (const char *env = std::getenv("FAZ_ZSTD_THREADS")) t = std::atoi(env);
+    return t < 0 ? 0 : t;
+}
+
+int zstd_frame_count(size_t n, int threads) {
+    if (threads <= 0) return 1;
+    const size_t kMinFrame = (size_t)4 << 20;  // slices of at least 4 MiB
+    size_t nf = n / kMinFrame;
+    if (nf > (size_t)(2 * threads)) nf = (size_t)(2 * threads);
+    return nf < 1 ? 1 : (int)nf;
+}
+
+size_t zstd_frames_bound(const Zstd &z, size_t n, int nframes) {
+    if (nframes <= 1) return z.bound(n);
+    size_t b = 0;
+    const size_t slice = (n + nframes - 1) / nframes;
+    for (int i = 0; i < nframes; i++) {
+        const size_t lo = std::min(n, slice * i), hi = std::min(n, lo + slice);
+        b += z.bound(hi - lo);
+    }
+    return b;
+}
+
+size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes) {
+    if (nframes <= 1) return z.compress(dst, cap, src, n, 3);
+    const size_t slice = (n + nframes - 1) / nframes;
+    struct Part {
+        size_t lo, len, size = 0, off = 0;
+        std::unique_ptr<uint8_t[]> buf;
+    };
+    std::vector<Part> parts(nframes);
+    for (int i = 0; i < nframes; i++) {
+        parts[i].lo = std::min(n, slice * i);
+        parts[i].len = std::min(n, parts[i].lo + slice) - parts[i].lo;
+    }
+    auto each = [&](auto &&fn) {
+        std::vector<std::thread> pool;
+        for (int i = 0; i < nframes; i++) pool.emplace_back(fn, i);
+        for (auto &t : pool) t.join();
+    };
+    each([&](int i) {
+        Part &p = parts[i];
+        const size_t b = z.bound(p.len);
+        p.buf.reset(new (std::nothrow) uint8_t[b]);
+        p.size = p.buf ? z.compress(p.buf.get(), b, src + p.lo, p.len, 3) : (size_t)-1;
+    });
+    size_t o = 0;
+    for (auto &p : parts) {
+        if (z.isError(p.size)) return p.size;
+        p.off = o;
+        o += p.size;
+    }
+    if (o > cap) return (size_t)-1;
+    each([&](int i) { std::memcpy(dst + parts[i].off, parts[i].buf.get(), parts[i].size); });
+    return o;
+}
+
+size_t zstd_decompress_frames(const Zstd &z, uint8_t *dst, size_t raw, const uint8_t *src, size_t n, int threads) {
+    struct Frame {
+        size_t off, csize, out, dsize;
+    };
+    std::vector<Frame> fr;
+    if (z.findFrameCompressedSize && z.getFrameContentSize && threads > 0) {
+        size_t off = 0, out = 0;
+        while (off < n) {
+            const size_t fs = z.findFrameCompressedSize(src + off, n - off);
+            if (z.isError(fs) || fs == 0) {
+                fr.clear();
+                break;
+            }
+            const unsigned long long ds = z.getFrameContentSize(src + off, fs);
+            if (ds >= (1ull << 62)) {  // unknown or error: decode the whole body in one call
+                fr.clear();
+                break;
+            }
+            fr.push_back({off, fs, out, (size_t)ds});
+            off += fs;
+            out += (size_t)ds;
+        }
+        if (out != raw) fr.clear();
+    }
+    if (fr.size() <= 1) return z.decompress(dst, raw, src, n);
+    std::vector<size_t> got(fr.size(), 0);
+    std::vector<std::thread> pool;
+    const size_t nt = std::min<size_t>(fr.size(), (size_t)threads);
+    for (size_t t = 0; t < nt; t++) {
+        pool.emplace_back([&, t] {
+            for (size_t i = t; i < fr.size(); i += nt)
+                got[i] = z.decompress(dst + fr[i].out, fr[i].dsize, src + fr[i].off, fr[i].csize);
+        });
+    }
+    for (auto &t : pool) t.join();
+    for (size_t i = 0; i < fr.size(); i++)
+        if (z.isError(got[i]) || got[i] != fr[i].dsize) return (size_t)-1;
+    return raw;
 }
 
 }  // namespace faz

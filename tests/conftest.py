@@ -8,6 +8,10 @@ import numpy as np
 import pytest
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+# Full-stream comparisons with the oracle need the frame single-threaded
+# ZSTD_compress writes; the library's default compresses the final frame with
+# worker threads (same payload, different frame).
+os.environ.setdefault("FAZ_ZSTD_THREADS", "0")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)

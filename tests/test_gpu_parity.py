@@ -241,3 +241,44 @@ def test_gpu_full_code_range():
     dec, _ = F.SZ_decompress(None, stream, dtype=np.float32)
     ref_dec, _ = O.decompress(O.compress(conf, x)[0])
     assert np.array_equal(dec.view(np.uint32), ref_dec.view(np.uint32))
+
+
+def _zstd_frames(stream):
+    """Number of zstd frames in a stream's body (system libzstd)."""
+    import ctypes
+    z = ctypes.CDLL("libzstd.so.1")
+    z.ZSTD_findFrameCompressedSize.restype = ctypes.c_size_t
+    z.ZSTD_findFrameCompressedSize.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    z.ZSTD_isError.argtypes = [ctypes.c_size_t]
+    body_end = len(stream) - 4 - int.from_bytes(stream[-4:], "little", signed=True)
+    body = stream[8:body_end]
+    n, off = 0, 0
+    while off < len(body):
+        fs = z.ZSTD_findFrameCompressedSize(body[off:], len(body) - off)
+        assert not z.ZSTD_isError(fs)
+        off += fs
+        n += 1
+    return n
+
+
+def test_gpu_parallel_zstd_frames_hold_the_same_payload(monkeypatch):
+    """FAZ_ZSTD_THREADS > 0 writes a large payload as independent zstd frames
+    compressed in parallel: the same payload, decodable by plain
+    ZSTD_decompress (the oracle) and by the library's parallel frame decoder."""
+    import torch
+    dims = (128, 256, 256)
+    t = F.fields.spectral_field(dims, slope=-3.0, noise=0.01, seed=5, device="cuda")
+    conf = _conf(dims, rel=1e-4)
+    monkeypatch.setenv("FAZ_ZSTD_THREADS", "0")
+    s0 = F.SZ_compress(conf, t)
+    assert _zstd_frames(s0) == 1
+    monkeypatch.setenv("FAZ_ZSTD_THREADS", "8")
+    s8 = F.SZ_compress(conf, t)
+    assert _zstd_frames(s8) > 1
+    assert payload_of(s0) == payload_of(s8)   # the oracle decodes both bodies
+    ref, _ = O.decompress(s0)
+    for threads in ("8", "0"):  # parallel frames, then one call over all of them
+        monkeypatch.setenv("FAZ_ZSTD_THREADS", threads)
+        out = torch.empty(dims, dtype=torch.float32, device="cuda")
+        F.decompress_device(s8, out)
+        assert np.array_equal(out.cpu().numpy().view(np.uint32), ref.view(np.uint32))
