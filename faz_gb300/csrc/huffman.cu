@@ -602,7 +602,7 @@ cudaError_t launch_encode_pack(const uint16_t *codes, uint64_t n, int offset, co
                                const unsigned long long *chunkoff, uint32_t *out, int maxlen, cudaStream_t st) {
     int words = (int)(((uint64_t)ENC_CHUNK * (uint64_t)maxlen + 31) / 32 + 2);
     size_t sm = (size_t)words * 4;
-    cudaError_t e = cudaFuncSetAttribute(k_encode_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = allow_dynamic_smem((const void *)k_encode_pack);
     if (e != cudaSuccess) return e;
     k_encode_pack<<<grid_for(n, ENC_CHUNK), ENC_THREADS, sm, st>>>(codes, n, offset, code64, packed, len, chunkoff,
                                                                     out, words);

@@ -3,13 +3,39 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
+#include <mutex>
+#include <set>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/faz_gb300.h"
 #include "common.cuh"
 
 namespace faz {
+
+// Let a kernel take up to the device's opt-in shared memory per block, once
+// per (device, kernel).  Setting the limit to each launch's own need instead
+// races: host threads launching the same kernel concurrently (the tuner's
+// trials) can lower it between another thread's set and launch.
+inline cudaError_t allow_dynamic_smem(const void *func) {
+    static std::mutex mu;
+    static std::set<std::pair<int, const void *>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(mu);
+    if (done.count({dev, func})) return cudaSuccess;
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, func);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess) done.insert({dev, func});
+    return e;
+}
 
 // ---------------------------------------------------------------- kernels
 template <typename T>

@@ -525,7 +525,7 @@ cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const
         if (!decomp) k = wide ? k_interp_level<T, false, true, 0> : k_interp_level<T, false, false, 0>;
         else k = wide ? k_interp_level<T, true, true, 0> : k_interp_level<T, true, false, 0>;
     }
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = allow_dynamic_smem((const void *)k);
     if (e != cudaSuccess) return e;
     k<<<(unsigned)nblocks, threads, sm, st>>>(a, X, W, codes, scratch, zpos, nz, unpred);
     return cudaGetLastError();

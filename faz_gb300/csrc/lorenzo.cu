@@ -306,7 +306,7 @@ void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, uint16_t *co
               const T *);
     if (!decomp) k = straight ? k_lor_diag<T, false, 1> : k_lor_diag<T, false, 0>;
     else k = straight ? k_lor_diag<T, true, 1> : k_lor_diag<T, true, 0>;
-    CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(allow_dynamic_smem((const void *)k));
     if (a.nx > 65535) throw Fail{FAZ_ERR_UNSUPPORTED, "too many Lorenzo blocks along the slowest axis"};
     for (int64_t d = 0; d <= last; d++) {
         const int64_t bi_lo = std::max<int64_t>(0, d - (a.ny - 1) - (a.nz - 1));
