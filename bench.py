@@ -52,6 +52,7 @@ def parse():
                     help="auto: the default configuration (ALGO_INTERP_LORENZO, sampled autotune); "
                          "interp: ALGO_INTERP with --interp")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-sampled autotune comparison")
     return ap.parse_args()
 
 
@@ -236,6 +237,44 @@ def workload_name(dims, args):
 
 
 # ------------------------------------------------------------------ GPU arm
+def learned_vs_sampled(x, dims, eb):
+    """The learned tuner against the sampled QoZ autotune, end to end through
+    compress_device (tuning + compression + zstd, host clock): on this field
+    and on held-out synthetic fields of the training distribution (128^3 to
+    256^3, spectral slope -4..-2, anisotropy up to 8, 0-5 % noise, optional
+    flat boxes, relative bounds 1e-4..1e-2; a seed outside the training set)."""
+    import faz_gb300 as F
+    import faz_gb300.learned as L
+    import torch
+    if not os.path.exists(L.DEFAULT_MODEL):
+        return None
+    model = L.TunerModel.load()
+    qc = L.qoz_conf(dims, eb)
+    t_plain, s_plain = L._timed(lambda: F.compress_device(qc, x), 2)
+
+    def learned():
+        tuned, info = L.learned_tune(qc, x, model)
+        return F.compress_device(tuned, x), info
+    t_learn, (s_learn, info) = L._timed(learned, 3)
+    nbytes = x.numel() * x.element_size()
+    # the network alone: features + tensor-core MLP on this field
+    f = L.features(qc, x)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(10):
+        model.infer(L.features(qc, x))
+    torch.cuda.synchronize()
+    t_net = (time.perf_counter() - t0) / 10
+    _, held = L.evaluate(model, 6, seed=999, reps=2)
+    return {"this_field": {"sampled_ms": round(t_plain * 1e3, 2), "learned_ms": round(t_learn * 1e3, 2),
+                           "speedup": round(t_plain / t_learn, 2), "ratio_sampled": round(nbytes / len(s_plain), 4),
+                           "ratio_learned": round(nbytes / len(s_learn), 4), "same_stream": s_plain == s_learn,
+                           "fallback": info["used_plain"], "network_ms": round(t_net * 1e3, 3)},
+            "held_out": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in held.items()},
+            "sampled": "QoZ tuner (QoZ = 1: per-level interpolator/direction + alpha/beta search by trial compressions)",
+            "learned": "MLP 64->256->256->27 on block statistics, BF16 tcgen05 inference, plain tuner as fallback"}
+
+
 def main():
     args = parse()
     dims = tuple(int(d) for d in args.dims.split(","))
@@ -387,6 +426,7 @@ def main():
         cpu = {"value": round(cc, 4), "unit": "GB/s", "cores": 1, "kind": "port",
                "sample": f"compress of a {shape[0]}x{shape[1]}x{shape[2]} slab of the same field, one thread "
                          f"(decompress {cd:.4f} GB/s)"}
+    learned = None if args.no_learned else learned_vs_sampled(x, dims, args.eb)
     med = lambda k, ph: round(statistics.median(p[k] for p in ph), 4)  # noqa: E731
     line = {
         "metric": METRIC,
@@ -426,6 +466,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks,
         "cpu_baseline": cpu,
+        "learned_tuner": learned,
         "max_abs_err": err,
     }
     print(json.dumps(line), flush=True)

@@ -19,7 +19,9 @@ STATUS = {0: "FAZ_OK", -1: "FAZ_ERR_ARG", -2: "FAZ_ERR_UNSUPPORTED", -3: "FAZ_ER
 
 EXPORTED = ["faz_config_init", "faz_config_load_ini", "faz_compress", "faz_decompress", "faz_compress_device",
             "faz_decompress_device", "faz_compress_device_payload", "faz_decompress_payload_device",
-            "faz_stream_info", "faz_resolve_eb_noalloc",
+            "faz_stream_info", "faz_resolve_eb_noalloc", "faz_tune_device", "faz_tuner_features",
+            "faz_mlp_forward", "faz_mlp_backward", "faz_mlp_adam", "faz_tuner_model_create",
+            "faz_tuner_model_destroy", "faz_tuner_infer", "faz_learned_tune",
             "faz_config_size", "faz_free", "faz_last_error", "faz_zstd_version"]
 
 
@@ -54,6 +56,17 @@ def library():
         L.faz_stream_info.argtypes = [vp, sz, vp]
         L.faz_resolve_eb_noalloc.argtypes = [vp, ctypes.c_int, vp, vp]
         L.faz_decompress_payload_device.argtypes = [ctypes.c_int, ctypes.c_int, vp, sz, vp, ctypes.c_uint64, vp, vp]
+        i32, i64, f32, f64 = ctypes.c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_double
+        L.faz_tune_device.argtypes = [vp, i32, vp, vp, vp]
+        L.faz_tuner_features.argtypes = [vp, i32, vp, vp, vp]
+        L.faz_mlp_forward.argtypes = [vp, vp, i32, vp, vp, vp, vp]
+        L.faz_mlp_backward.argtypes = [vp, vp, vp, i32, vp, vp, vp, vp, vp, vp]
+        L.faz_mlp_adam.argtypes = [vp, vp, vp, vp, i64, f32, f32, f32, f32, i32, f32, vp]
+        L.faz_tuner_model_create.argtypes = [vp, vp, vp]
+        L.faz_tuner_model_create.restype = vp
+        L.faz_tuner_model_destroy.argtypes = [vp]
+        L.faz_tuner_infer.argtypes = [vp, vp, i32, vp, vp]
+        L.faz_learned_tune.argtypes = [vp, i32, vp, vp, vp, f64, vp]
         _lib = L
         return L
 
@@ -136,6 +149,24 @@ def compress_device(conf, tensor, stream=None):
                                              ctypes.byref(tm)))
     _tls.timings = tm
     return _take_bytes(out, osz.value)
+
+
+def tune_device(conf, tensor, stream=None):
+    """Run the sampled autotune `conf` selects (QoZ = 1: the QoZ tuner;
+    ALGO_INTERP_LORENZO: the SZ3 tuner) on a CUDA tensor without compressing.
+    Returns the tuned Config (the decisions, error bound resolved to ABS)."""
+    import torch
+    t = tensor.contiguous()
+    dt = {torch.float32: FAZ_FLOAT, torch.float64: FAZ_DOUBLE}.get(t.dtype)
+    if dt is None:
+        raise TypeError("FAZ compresses float32 or float64 data")
+    st = (stream or torch.cuda.current_stream(t.device)).cuda_stream
+    s, tm = conf.to_struct(), FazTimings()
+    with torch.cuda.device(t.device):
+        _check(library().faz_tune_device(ctypes.byref(s), dt, ctypes.c_void_p(t.data_ptr()), ctypes.c_void_p(st),
+                                         ctypes.byref(tm)))
+    _tls.timings = tm
+    return Config.from_struct(s)
 
 
 def stream_info(stream_bytes):

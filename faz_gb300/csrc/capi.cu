@@ -239,8 +239,6 @@ double device_range(const T *dX, uint64_t n, cudaStream_t st, Counter &launches)
 template double device_range<float>(const float *, uint64_t, cudaStream_t, Counter &);
 template double device_range<double>(const double *, uint64_t, cudaStream_t, Counter &);
 
-namespace {
-
 // calAbsErrorBound (include/QoZ/utils/Statistic.hpp:34-66); `rng` computed
 // on the device when the mode needs it.
 template <typename T>
@@ -274,7 +272,10 @@ void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     if (c.errorBoundMode != FAZ_EB_L2NORM) c.rng = rng;
     c.errorBoundMode = FAZ_EB_ABS;
 }
+template void resolve_eb<float>(faz_config &, const float *, cudaStream_t, Counter &);
+template void resolve_eb<double>(faz_config &, const double *, cudaStream_t, Counter &);
 
+namespace {
 
 // GPU part of compression: returns the pre-zstd payload in a pinned buffer.
 // Where the payload goes: a caller buffer of `cap` bytes, or (dst == nullptr)
@@ -586,7 +587,7 @@ int compress_payload_impl(const faz_config *conf_in, const void *d_data, void *u
         faz_config c = *conf_in;
         check_config(c);
         init_pool_once();
-        StreamGuard sg(user_stream);
+        StreamGuard sg(user_stream, false, NullStream::Default);
         Counter launches;
         Events ev_gpu;
         uint8_t *payload;
@@ -627,7 +628,7 @@ int compress_impl(const faz_config *conf_in, const void *data, bool on_device, v
         faz_config c = *conf_in;
         check_config(c);
         init_pool_once();
-        StreamGuard sg(user_stream);
+        StreamGuard sg(user_stream, false, on_device ? NullStream::Default : NullStream::Library);
         cudaStream_t st = sg.st;
         Counter launches;
         Events ev_h2d, ev_gpu;
@@ -947,7 +948,7 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
                 if (P.dims[i] != c.dims[i]) throw Fail{FAZ_ERR_FORMAT, "header dims differ from trailer dims"};
         }
         init_pool_once();
-        StreamGuard sg(user_stream);
+        StreamGuard sg(user_stream, false, on_device ? NullStream::Default : NullStream::Library);
         cudaStream_t st = sg.st;
         Counter launches;
         Events ev_gpu, ev_d2h;
@@ -1019,7 +1020,7 @@ int decompress_payload_impl(int N, const char *payload, size_t psize, void *d_ou
         for (int i = 0; i < N; i++) num *= P.dims[i];
         if (cap < num) throw Fail{FAZ_ERR_ARG, "output buffer holds fewer values than the payload's field"};
         init_pool_once();
-        StreamGuard sg(user_stream);
+        StreamGuard sg(user_stream, false, NullStream::Default);
         Counter launches;
         Events ev_gpu;
         CK(cudaEventRecord(ev_gpu.a, sg.st));
@@ -1039,6 +1040,104 @@ int decompress_payload_impl(int N, const char *payload, size_t psize, void *d_ou
     }
     tm.total_ms = ms_since(t0);
     if (tmo) *tmo = tm;
+    return FAZ_OK;
+}
+
+template <typename T>
+int tune_impl(faz_config *conf, const void *d_data, void *user_stream, faz_timings *tmo) {
+    faz_timings tm;
+    std::memset(&tm, 0, sizeof(tm));
+    auto t0 = clk::now();
+    try {
+        if (!conf || !d_data) throw Fail{FAZ_ERR_ARG, "null argument"};
+        faz_config c = *conf;
+        check_config(c);
+        init_pool_once();
+        StreamGuard sg(user_stream, false, NullStream::Default);
+        Counter launches;
+        const T *dX = (const T *)d_data;
+        resolve_eb<T>(c, dX, sg.st, launches);
+        if (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))
+            throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
+        auto tt = clk::now();
+        if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.QoZ) {
+            qoz_tune_device<T>(c, dX, sg.st, launches, tm);
+        } else if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) {
+            faz_timings t2;
+            std::memset(&t2, 0, sizeof(t2));
+            sz3_tune_device<T>(c, dX, sg.st, launches, t2, [](const faz_config &) {});
+        }
+        CK(cudaStreamSynchronize(sg.st));
+        tm.tune_ms = ms_since(tt);
+        tm.kernel_launches = launches.n;
+        *conf = c;
+    } catch (const Fail &f) {
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return FAZ_ERR_ARG;
+    }
+    tm.total_ms = ms_since(t0);
+    if (tmo) *tmo = tm;
+    return FAZ_OK;
+}
+
+template <typename T>
+int features_impl(const faz_config *conf, const void *d_data, void *user_stream, float *dF) {
+    try {
+        if (!conf || !d_data || !dF) throw Fail{FAZ_ERR_ARG, "null argument"};
+        faz_config c = *conf;
+        check_config(c);
+        init_pool_once();
+        StreamGuard sg(user_stream, false, NullStream::Default);
+        Counter launches;
+        if (c.rng < 0 && c.errorBoundMode == FAZ_EB_ABS) c.rng = device_range<T>((const T *)d_data, c.num, sg.st, launches);
+        resolve_eb<T>(c, (const T *)d_data, sg.st, launches);
+        if (c.rng < 0) c.rng = device_range<T>((const T *)d_data, c.num, sg.st, launches);
+        tuner_features_device<T>(c, (const T *)d_data, sg.st, dF, launches);
+        CK(cudaStreamSynchronize(sg.st));
+    } catch (const Fail &f) {
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return FAZ_ERR_ARG;
+    }
+    return FAZ_OK;
+}
+
+template <typename T>
+int learned_impl(faz_config *conf, const void *d_data, void *user_stream, const TunerModel *model, double min_conf,
+                 faz_tuner_choice *choice) {
+    auto t0 = clk::now();
+    try {
+        if (!conf || !d_data || !model) throw Fail{FAZ_ERR_ARG, "null argument"};
+        faz_config c = *conf;
+        check_config(c);
+        init_pool_once();
+        StreamGuard sg(user_stream, false, NullStream::Default);
+        Counter launches;
+        faz_timings tm;
+        std::memset(&tm, 0, sizeof(tm));
+        const T *dX = (const T *)d_data;
+        resolve_eb<T>(c, dX, sg.st, launches);
+        if (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))
+            throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
+        if (c.rng < 0) c.rng = device_range<T>(dX, c.num, sg.st, launches);
+        faz_tuner_choice ch;
+        learned_tune_device<T>(c, dX, sg.st, *model, min_conf, ch, launches, tm);
+        CK(cudaStreamSynchronize(sg.st));
+        ch.tune_ms = ms_since(t0);
+        if (choice) *choice = ch;
+        *conf = c;
+    } catch (const Fail &f) {
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return FAZ_ERR_ARG;
+    }
     return FAZ_OK;
 }
 
@@ -1142,6 +1241,97 @@ unsigned faz_zstd_version(void) {
     std::string err;
     const faz::Zstd &z = faz::zstd_lib(err);
     return z.ok ? z.version : 0;
+}
+
+
+int faz_tune_device(faz_config *conf, int dtype, const void *d_data, void *stream, faz_timings *timings) {
+    if (dtype == FAZ_FLOAT) return faz::tune_impl<float>(conf, d_data, stream, timings);
+    if (dtype == FAZ_DOUBLE) return faz::tune_impl<double>(conf, d_data, stream, timings);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
+
+int faz_tuner_features(const faz_config *conf, int dtype, const void *d_data, void *stream, float *d_features) {
+    if (dtype == FAZ_FLOAT) return faz::features_impl<float>(conf, d_data, stream, d_features);
+    if (dtype == FAZ_DOUBLE) return faz::features_impl<double>(conf, d_data, stream, d_features);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
+
+#define FAZ_GUARD(...)                           \
+    try {                                        \
+        __VA_ARGS__;                             \
+    } catch (const faz::Fail &f) {               \
+        faz::set_error(f.msg);                   \
+        return f.code;                           \
+    } catch (const std::exception &e) {          \
+        faz::set_error(e.what());                \
+        return FAZ_ERR_ARG;                      \
+    }                                            \
+    return FAZ_OK;
+
+int faz_mlp_forward(const float *d_params, const float *d_x, int batch, float *d_h1, float *d_h2, float *d_logits,
+                    void *stream) {
+    FAZ_GUARD({
+        if (!d_params || !d_x || !d_h1 || !d_h2 || !d_logits || batch <= 0) throw faz::Fail{FAZ_ERR_ARG, "bad argument"};
+        faz::Counter launches;
+        faz::mlp_forward(d_params, d_x, batch, d_h1, d_h2, d_logits, (cudaStream_t)stream, launches);
+    })
+}
+
+int faz_mlp_backward(const float *d_params, const float *d_x, const int32_t *d_labels, int batch, const float *d_h1,
+                     const float *d_h2, const float *d_logits, float *d_grads, float *d_loss, void *stream) {
+    FAZ_GUARD({
+        if (!d_params || !d_x || !d_labels || !d_h1 || !d_h2 || !d_logits || !d_grads || !d_loss || batch <= 0)
+            throw faz::Fail{FAZ_ERR_ARG, "bad argument"};
+        faz::Counter launches;
+        faz::mlp_backward(d_params, d_x, d_labels, batch, d_h1, d_h2, d_logits, d_grads, d_loss, (cudaStream_t)stream,
+                          launches);
+    })
+}
+
+int faz_mlp_adam(float *d_params, const float *d_grads, float *d_m, float *d_v, int64_t n, float lr, float beta1,
+                 float beta2, float eps, int step, float weight_decay, void *stream) {
+    FAZ_GUARD({
+        if (!d_params || !d_grads || !d_m || !d_v || n <= 0 || step < 1) throw faz::Fail{FAZ_ERR_ARG, "bad argument"};
+        faz::Counter launches;
+        faz::mlp_adam(d_params, d_grads, d_m, d_v, n, lr, beta1, beta2, eps, step, weight_decay, (cudaStream_t)stream,
+                      launches);
+    })
+}
+
+faz_tuner_model *faz_tuner_model_create(const float *h_params, const float *h_mean, const float *h_std) {
+    if (!h_params || !h_mean || !h_std) {
+        faz::set_error("null argument");
+        return nullptr;
+    }
+    try {
+        return (faz_tuner_model *)faz::tuner_model_create(h_params, h_mean, h_std);
+    } catch (const faz::Fail &f) {
+        faz::set_error(f.msg);
+    }
+    return nullptr;
+}
+
+void faz_tuner_model_destroy(faz_tuner_model *model) { faz::tuner_model_destroy((faz::TunerModel *)model); }
+
+int faz_tuner_infer(const faz_tuner_model *model, const float *d_features, int batch, float *d_logits, void *stream) {
+    FAZ_GUARD({
+        if (!model || !d_features || !d_logits) throw faz::Fail{FAZ_ERR_ARG, "null argument"};
+        faz::init_pool_once();
+        faz::StreamGuard sg(stream, false, faz::NullStream::Default);
+        faz::Counter launches;
+        faz::tuner_infer_device(*(const faz::TunerModel *)model, d_features, batch, d_logits, sg.st, launches);
+    })
+}
+
+int faz_learned_tune(faz_config *conf, int dtype, const void *d_data, void *stream, const faz_tuner_model *model,
+                     double min_confidence, faz_tuner_choice *choice) {
+    const auto *m = (const faz::TunerModel *)model;
+    if (dtype == FAZ_FLOAT) return faz::learned_impl<float>(conf, d_data, stream, m, min_confidence, choice);
+    if (dtype == FAZ_DOUBLE) return faz::learned_impl<double>(conf, d_data, stream, m, min_confidence, choice);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
 }
 
 }  // extern "C"

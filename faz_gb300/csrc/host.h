@@ -91,14 +91,21 @@ struct Pinned {
 inline thread_local Pinned t_pin_payload;
 inline thread_local Pinned t_pin_small;
 
+// How a call on device buffers reads a NULL stream: the legacy default
+// stream, so that the call is ordered after the caller's default-stream work
+// (the data it reads may still be being written there).
+enum class NullStream { Library, Default };
+
 struct StreamGuard {
     cudaStream_t st = nullptr;
     bool own = false;
-    // user stream, or a library stream (at the device's highest priority
-    // when `high` is set)
-    explicit StreamGuard(void *user, bool high = false) {
+    // user stream, or (NULL) the legacy default stream or a library stream
+    // (at the device's highest priority when `high` is set)
+    explicit StreamGuard(void *user, bool high = false, NullStream ns = NullStream::Library) {
         if (user) {
             st = (cudaStream_t)user;
+        } else if (ns == NullStream::Default) {
+            st = cudaStreamLegacy;
         } else if (high) {
             int least = 0, greatest = 0;
             CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
@@ -202,6 +209,27 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
 
 template <typename T>
 void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);
+template <typename T>
+int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);
+// calAbsErrorBound on the device (capi.cu)
+template <typename T>
+void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);
+// learned tuner (learned.cu)
+struct TunerModel;
+template <typename T>
+void tuner_features_device(const faz_config &c, const T *dX, cudaStream_t st, float *dF, Counter &launches);
+void mlp_forward(const float *P, const float *X, int B, float *H1, float *H2, float *Z, cudaStream_t st,
+                 Counter &launches);
+void mlp_backward(const float *P, const float *X, const int32_t *labels, int B, const float *H1, const float *H2,
+                  const float *Z, float *G, float *loss, cudaStream_t st, Counter &launches);
+void mlp_adam(float *P, const float *G, float *M, float *V, int64_t n, float lr, float b1, float b2, float eps, int t,
+              float wd, cudaStream_t st, Counter &launches);
+TunerModel *tuner_model_create(const float *P, const float *mu, const float *sd);
+void tuner_model_destroy(TunerModel *t);
+void tuner_infer_device(const TunerModel &t, const float *dF, int B, float *dZ, cudaStream_t st, Counter &launches);
+template <typename T>
+void learned_tune_device(faz_config &c, const T *dX, cudaStream_t st, const TunerModel &model, double min_conf,
+                         faz_tuner_choice &ch, Counter &launches, faz_timings &tm);
 
 template <typename T>
 double device_range(const T *dX, uint64_t n, cudaStream_t st, Counter &launches);

@@ -440,17 +440,15 @@ int64_t full_run_slots(const QzGeom &g) {
 
 }  // namespace
 
-// QoZ Tuning for the RD target on 2-D / 3-D data; on return c holds the
-// decisions (per-level lists, alpha, beta, maxStep, ...).
+// QoZ defaults and the settings derived from the field before any trial
+// (SZInterp.hpp:1588-1625, 1660-1690, 1800-1812); returns max_interp_level.
 template <typename T>
-void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm) {
+int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) {
     const int N = c.N;
     if (N != 2 && N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for 2-D and 3-D data"};
     if (c.tuningTarget != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for the PSNR (RD) target"};
     if (c.rng < 0) c.rng = device_range<T>(dX, c.num, st, launches);
     if (c.relErrorBound <= 0) c.relErrorBound = c.absErrorBound / c.rng;
-    const double rngT = (double)(T)c.rng;  // T rng = conf.rng
-    const double rel_bound = c.relErrorBound > 0 ? c.relErrorBound : c.absErrorBound / rngT;
     // QoZ defaults (SZInterp.hpp:1597-1625)
     if (c.autoTuningRate <= 0) c.autoTuningRate = N == 2 ? 0.01 : 0.005;
     if (c.predictorTuningRate <= 0) c.predictorTuningRate = N == 2 ? 0.01 : 0.005;
@@ -483,10 +481,23 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         c.sampleBlockSize /= 2;
     if (!(c.predictorTuningRate > 0 && c.predictorTuningRate < 1))
         throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning needs predictorTuningRate in (0, 1)"};
-    const int64_t sbs = c.sampleBlockSize, bsz = sbs + 1;
+    const int64_t sbs = c.sampleBlockSize;
     if (c.fixBlockSize > 0 || c.interpBlockSize < sbs)
         throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning needs interpBlockSize >= sampleBlockSize and no fixBlockSize"};
     if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};
+    return max_interp_level;
+}
+template int qoz_prepare<float>(faz_config &, const float *, cudaStream_t, Counter &);
+template int qoz_prepare<double>(faz_config &, const double *, cudaStream_t, Counter &);
+
+// QoZ Tuning for the RD target on 2-D / 3-D data; on return c holds the
+// decisions (per-level lists, alpha, beta, maxStep, ...).
+template <typename T>
+void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm) {
+    const int N = c.N;
+    const int max_interp_level = qoz_prepare<T>(c, dX, st, launches);
+    const double rel_bound = c.relErrorBound > 0 ? c.relErrorBound : c.absErrorBound / (double)(T)c.rng;
+    const int64_t sbs = c.sampleBlockSize, bsz = sbs + 1;
     // sampleBlocks (profiling 0, var_first 0)
     uint64_t stride = (uint64_t)(1.0 / c.predictorTuningRate);
     if (stride <= 0) stride = 1;

@@ -98,6 +98,14 @@ def _spectral_torch(shape, slope, aniso, noise, seed, lo, hi, spikes, piecewise,
     sd = field.std()
     if noise > 0:
         field.add_(torch.randn(shape, generator=g, device=device) * (noise * sd))
+    for _ in range(int(piecewise)):
+        # a box of a quarter of each extent set to its mean
+        sl = []
+        for n in shape:
+            a = int(torch.randint(0, max(1, n - 1), (1,), generator=g, device=device).item())
+            sl.append(slice(a, min(n, a + max(1, n // 4))))
+        box = field[tuple(sl)]
+        box.fill_(box.mean())
     fmin, fmax = field.min(), field.max()
     span = (fmax - fmin) if fmax > fmin else torch.ones_like(fmax)
     field.sub_(fmin).div_(span).mul_(hi - lo).add_(lo)

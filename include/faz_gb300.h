@@ -24,8 +24,10 @@
  * the last failure on the calling thread is available from faz_last_error().
  * The reference terminates the process on bad input (e.g.
  * include/QoZ/api/impl/SZDispatcher.hpp:49-50); this library returns instead.
- * Threading: calls on different threads are independent; each call uses its
- * own CUDA stream on the current device.
+ * Threading: calls on different threads are independent.  Calls on host
+ * buffers use their own CUDA stream on the current device.  Calls on device
+ * buffers take a `stream` (a cudaStream_t) that orders their work after the
+ * caller's; NULL is the legacy default stream, as everywhere in CUDA.
  */
 #ifndef FAZ_GB300_H
 #define FAZ_GB300_H
@@ -184,7 +186,7 @@ int faz_decompress(faz_config *conf, int dtype, const char *cmp, size_t cmp_size
 int faz_stream_info(const char *cmp, size_t cmp_size, faz_config *conf);
 
 /* Same as faz_compress with the input already in device memory (d_data) and
- * work issued on `stream` (a cudaStream_t, or NULL for a library stream). */
+ * work issued on `stream` (a cudaStream_t; NULL = the legacy default stream). */
 int faz_compress_device(const faz_config *conf, int dtype, const void *d_data,
                         void *stream, char **out, size_t *out_size,
                         faz_timings *timings);
@@ -229,6 +231,86 @@ int faz_decompress_payload_device(int N, int dtype, const char *payload, size_t 
  * first call on each device looks the array's address up; make it before
  * any stream capture. */
 int faz_resolve_eb_noalloc(faz_config *conf, int dtype, const void *d_data, void *stream);
+
+/* Run the sampled autotune that `conf` selects and stop before compressing:
+ * QoZ = 1 runs the QoZ tuner (Tuning, include/QoZ/api/impl/SZInterp.hpp:
+ * 1588-2557), cmprAlgo ALGO_INTERP_LORENZO without QoZ the SZ3 tuner
+ * (SZInterp.hpp:2561-2880).  On return `conf` holds the decisions (cmprAlgo,
+ * interpAlgo / interpDirection, per-level lists, alpha, beta, Lorenzo
+ * settings) with the error bound resolved to ABS; compressing that
+ * configuration writes the stream the tuned compression writes.  No
+ * counterpart in the reference, where tuning happens inside SZ_compress. */
+int faz_tune_device(faz_config *conf, int dtype, const void *d_data, void *stream, faz_timings *timings);
+
+/* ---------------------------------------------------------------------------
+ * Learned tuner (no counterpart in the reference).  A multilayer perceptron
+ * FAZ_TUNER_FEATURES -> FAZ_TUNER_HIDDEN -> FAZ_TUNER_HIDDEN -> FAZ_TUNER_LOGITS
+ * (ReLU hidden layers) predicts, from block statistics of a 3-D field, what the
+ * QoZ tuner decides: per level 1..4 the interpolator and direction (4 classes:
+ * linear dir 0, linear dir 5, cubic dir 0, cubic dir 5), alpha (1, 1.25, 1.5,
+ * 1.75, 2), beta (1.5, 2, 3, 4), and whether the SZ3 tuner picks Lorenzo
+ * (2 classes).  Heads, in logit order: level 1..4 (4 each), alpha (5), beta
+ * (4), Lorenzo (2).  Parameters are one float array: W1[H][F], b1[H],
+ * W2[H][H], b2[H], W3[L][H], b3[L] (row-major, y = W x + b).
+ * ------------------------------------------------------------------------- */
+#define FAZ_TUNER_FEATURES 64
+#define FAZ_TUNER_HIDDEN 256
+#define FAZ_TUNER_LOGITS 27
+#define FAZ_TUNER_HEADS 7
+#define FAZ_TUNER_LABELS 8 /* int32 labels per sample: one per head (-1 = none), 1 unused */
+#define FAZ_TUNER_PARAMS 89371
+#define FAZ_TUNER_MAX_BLOCKS 64 /* feature blocks (33^3 values each) per field */
+
+typedef struct faz_tuner_model faz_tuner_model;
+
+typedef struct faz_tuner_choice {
+    int used_plain;       /* 0: the network decided; 1: low confidence, the plain tuner
+                             decided; 2: Lorenzo predicted, the plain tuner decided;
+                             3: configuration outside the network's scope */
+    float confidence;     /* smallest top-class probability over the heads used */
+    float p_lorenzo;      /* predicted probability that the SZ3 tuner picks Lorenzo */
+    float logits[FAZ_TUNER_LOGITS];
+    double tune_ms;       /* host wall time of the whole decision */
+} faz_tuner_choice;
+
+/* The FAZ_TUNER_FEATURES features of a 3-D field (every extent >= 33) into
+ * d_features (device, float).  The error bound is resolved as for
+ * compression.  Features come from up to FAZ_TUNER_MAX_BLOCKS 33^3 blocks on
+ * the 32-grid: for strides 1, 2, 4, 8 (linear) and 1, 2, 4 (cubic) along each
+ * axis, log2(1 + mean |residual| / eb) and the fraction of residuals within
+ * eb; residual RMS, tails, kurtosis; log2(range / eb), log2(std / eb),
+ * log2 extents, log10 relative bound, flat-neighbour fraction, block count. */
+int faz_tuner_features(const faz_config *conf, int dtype, const void *d_data, void *stream, float *d_features);
+
+/* Training kernels (FP32).  Device pointers; `batch` rows.  forward writes
+ * the hidden activations and logits; backward writes the gradient of the mean
+ * (over rows) summed softmax cross-entropy of the labelled heads into d_grads
+ * (FAZ_TUNER_PARAMS floats) and each row's summed cross-entropy into d_loss;
+ * adam applies one AdamW step (step counts from 1). */
+int faz_mlp_forward(const float *d_params, const float *d_x, int batch, float *d_h1, float *d_h2, float *d_logits,
+                    void *stream);
+int faz_mlp_backward(const float *d_params, const float *d_x, const int32_t *d_labels, int batch, const float *d_h1,
+                     const float *d_h2, const float *d_logits, float *d_grads, float *d_loss, void *stream);
+int faz_mlp_adam(float *d_params, const float *d_grads, float *d_m, float *d_v, int64_t n, float lr, float beta1,
+                 float beta2, float eps, int step, float weight_decay, void *stream);
+
+/* Inference model on the current device: BF16 copies of the weights for the
+ * tensor cores, plus the feature standardisation (x - mean) / std. */
+faz_tuner_model *faz_tuner_model_create(const float *h_params, const float *h_mean, const float *h_std);
+void faz_tuner_model_destroy(faz_tuner_model *model);
+
+/* Logits of `batch` feature rows (device), BF16 operands with FP32
+ * accumulation on the tensor cores (tcgen05.mma). */
+int faz_tuner_infer(const faz_tuner_model *model, const float *d_features, int batch, float *d_logits, void *stream);
+
+/* The learned replacement of the QoZ tuner: for a configuration with QoZ = 1
+ * on a 3-D field, sets the decisions the QoZ tuner would set (per-level lists,
+ * alpha, beta, cmprAlgo = ALGO_INTERP) from the network's prediction.  The
+ * plain QoZ tuner decides instead when the prediction's confidence is below
+ * `min_confidence`, when Lorenzo is predicted, or when the configuration is
+ * outside the network's scope (choice->used_plain says which). */
+int faz_learned_tune(faz_config *conf, int dtype, const void *d_data, void *stream, const faz_tuner_model *model,
+                     double min_confidence, faz_tuner_choice *choice);
 
 /* sizeof(faz_config) as this library was compiled, for bindings that
  * mirror the struct (ctypes, cgo, JNI) to check their layout. */
