@@ -506,6 +506,17 @@ static int huff_decode(rd_t *r, size_t target, int *out) {
 #undef T
 #undef SFX
 
+#define T float
+#define SFX f32
+#include "oracle_general.inc"
+#undef T
+#undef SFX
+#define T double
+#define SFX f64
+#include "oracle_general.inc"
+#undef T
+#undef SFX
+
 /* ----------------------------------------------------- config and trailer */
 
 /* Config::Config(Dims...) - Config.hpp:64-74, member defaults 394-499 */
@@ -1034,6 +1045,23 @@ static int lorenzo3_size(int dtype, const void *data, const size_t *dims, int bs
     return rc;
 }
 
+/* General-frontend payload of a 1-D or 2-D field (SZ_compress_LorenzoReg with
+ * N < 3, include/QoZ/api/impl/SZLorenzoReg.hpp:94-114): Lorenzo predictors only. */
+static int gen_payload(int dtype, const void *data, int N, const size_t *dims, int bs, int lo, int lo2, double eb,
+                       int radius, bytes_t *out) {
+    if (dtype == FAZ_FLOAT) return gen_compress_f32((const float *)data, N, dims, bs, lo, lo2, eb, radius, out);
+    return gen_compress_f64((const double *)data, N, dims, bs, lo, lo2, eb, radius, out);
+}
+
+static int gen_size(int dtype, const void *data, int N, const size_t *dims, int bs, double eb, int radius,
+                    size_t *size) {
+    bytes_t b = {0};
+    int rc = gen_payload(dtype, data, N, dims, bs, 1, 1, eb, radius, &b);
+    if (!rc) rc = z_framed_size(b.p, b.n, size);
+    free(b.p);
+    return rc;
+}
+
 /* do_not_use_this_interp_compress_block_test (SZInterp.hpp:558-577) */
 static int blockinterp_ratio(int dtype, const void *data, int N, const size_t *dims, size_t num, double eb, int op,
                              int dir, int bs, double *ratio) {
@@ -1088,10 +1116,12 @@ static int sz3_tune(faz_config *conf, int dtype, const void *data) {
         conf->cmprAlgo = FAZ_ALGO_INTERP;
         return 0;
     }
-    if (N != 3) { free(smp); set_err("oracle tunes sampled 3-D fields"); return -2; }
+    if (N == 4) { free(smp); set_err("oracle tunes sampled 1-D to 3-D fields"); return -2; }
     double eb = conf->absErrorBound;
     size_t osz;
-    int rc = lorenzo3_size(dtype, smp, sd, 5, 3, eb, conf->quantbinCnt / 2, &osz);
+    /* the Lorenzo trial: lorenzo + lorenzo2, blockSize 5 (SZInterp.hpp:2115-2140) */
+    int rc = N == 3 ? lorenzo3_size(dtype, smp, sd, 5, 3, eb, conf->quantbinCnt / 2, &osz)
+                    : gen_size(dtype, smp, N, sd, 5, eb, conf->quantbinCnt / 2, &osz);
     if (rc) { free(smp); return rc; }
     double best_l = sn * 1.0 * es / osz, best_i = 0, ratio;
     for (int op = 0; op <= 1; op++) {
@@ -1099,7 +1129,7 @@ static int sz3_tune(faz_config *conf, int dtype, const void *data) {
         if (rc) { free(smp); return rc; }
         if (ratio > best_i) { best_i = ratio; conf->interpAlgo = op; }
     }
-    int dop = 5;
+    int dop = N == 3 ? 5 : (N == 2 ? 1 : 0);  /* factorial(N) - 1 */
     rc = blockinterp_ratio(dtype, smp, N, sd, sn, eb, conf->interpAlgo, dop, (int)sb, &ratio);
     if (rc) { free(smp); return rc; }
     if (ratio > best_i * 1.02) { best_i = ratio; conf->interpDirection = dop; }
@@ -1115,19 +1145,22 @@ static int sz3_tune(faz_config *conf, int dtype, const void *data) {
     lc.lorenzo = 1; lc.lorenzo2 = 1; lc.regression = 0; lc.regression2 = 0; lc.openmp = 0;
     lc.blockSize = 5;
     conf_set_dims_defaults(&lc);   /* setDims(sample dims) */
-    if (dtype == FAZ_FLOAT)
-        lc.quantbinCnt = opt_quant_intervals_f32((const float *)data, dims[0], dims[1], dims[2], eb);
-    else
-        lc.quantbinCnt = opt_quant_intervals_f64((const double *)data, dims[0], dims[1], dims[2], eb);
-    lc.pred_dim = 2;
-    rc = lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz);
-    if (rc) { free(smp); return rc; }
-    ratio = sn * 1.0 * es / osz;
-    if (ratio > best_l * 1.02) best_l = ratio; else lc.pred_dim = 3;
+    if (N == 3) {
+        if (dtype == FAZ_FLOAT)
+            lc.quantbinCnt = opt_quant_intervals_f32((const float *)data, dims[0], dims[1], dims[2], eb);
+        else
+            lc.quantbinCnt = opt_quant_intervals_f64((const double *)data, dims[0], dims[1], dims[2], eb);
+        lc.pred_dim = 2;
+        rc = lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz);
+        if (rc) { free(smp); return rc; }
+        ratio = sn * 1.0 * es / osz;
+        if (ratio > best_l * 1.02) best_l = ratio; else lc.pred_dim = 3;
+    }
     if (conf->relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
         int q0 = lc.quantbinCnt;
         lc.quantbinCnt = 16384;
-        rc = lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz);
+        rc = N == 3 ? lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz)
+                    : gen_size(dtype, smp, N, sd, lc.blockSize, eb, lc.quantbinCnt / 2, &osz);
         if (rc) { free(smp); return rc; }
         ratio = sn * 1.0 * es / osz;
         if (ratio > best_l * 1.02) best_l = ratio; else lc.quantbinCnt = q0;
@@ -1143,6 +1176,20 @@ static int sz3_tune(faz_config *conf, int dtype, const void *data) {
 static int payload_for(faz_config *conf, int dtype, const void *data, uint8_t **payload, size_t *psize) {
     if (conf->cmprAlgo == FAZ_ALGO_INTERP)
         return orc_interp_compress(conf, dtype, data, NULL, NULL, NULL, NULL, payload, psize);
+    if (conf->cmprAlgo == FAZ_ALGO_LORENZO_REG && conf->N < 3) {
+        if (conf->regression || conf->regression2) {
+            set_err("oracle covers the 1-D / 2-D general frontend with Lorenzo predictors only");
+            return -2;
+        }
+        size_t dims[2] = {conf->dims[0], conf->N == 2 ? conf->dims[1] : 1};
+        bytes_t b = {0};
+        int rc = gen_payload(dtype, data, conf->N, dims, conf->blockSize, conf->lorenzo, conf->lorenzo2,
+                             conf->absErrorBound, conf->quantbinCnt / 2, &b);
+        if (rc) { free(b.p); return rc; }
+        *payload = b.p;
+        *psize = b.n;
+        return 0;
+    }
     if (conf->cmprAlgo == FAZ_ALGO_LORENZO_REG) {
         if (conf->N != 3 || conf->regression2) { set_err("oracle covers the 3-D fast frontend"); return -2; }
         if (conf->blockSize < 1) { set_err("bad block size"); return -1; }
@@ -1230,6 +1277,25 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
     size_t psize;
     int rc = orc_read_stream(cmp, cmp_size, &conf, &payload, &psize);
     if (rc) return rc;
+    if (conf.cmprAlgo == FAZ_ALGO_LORENZO_REG && conf.N < 3) {
+        /* SZ_decompress_LorenzoReg with N < 3: the general frontend */
+        if (conf.regression || conf.regression2) {
+            free(payload);
+            set_err("oracle decodes 1-D / 2-D Lorenzo streams without regression");
+            return -2;
+        }
+        size_t dims[2] = {conf.dims[0], conf.N == 2 ? conf.dims[1] : 1};
+        size_t es = dtype == FAZ_FLOAT ? 4 : 8;
+        void *dec = malloc(conf.num * es + es);
+        rd_t r = {payload, psize, 0, 0};
+        int rc2 = dtype == FAZ_FLOAT ? gen_decompress_f32(&r, conf.N, dims, conf.lorenzo, conf.lorenzo2, (float *)dec)
+                                     : gen_decompress_f64(&r, conf.N, dims, conf.lorenzo, conf.lorenzo2, (double *)dec);
+        free(payload);
+        if (rc2) { free(dec); return rc2; }
+        *out = dec;
+        if (conf_out) *conf_out = conf;
+        return 0;
+    }
     if (conf.cmprAlgo == FAZ_ALGO_LORENZO_REG) {
         /* SZ_decompress_LorenzoReg with N == 3 (SZLorenzoReg.hpp:117-135) */
         if (conf.N != 3 || conf.regression2) {

@@ -120,7 +120,40 @@ def cases():
     out.append(("lor_only_f64", spectral_field((30, 33, 35), slope=-3.0, seed=57, dtype=np.float64),
                 ["-M", "REL", "1e-4"],
                 {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {"Regression": "NO"}}))
+    # 1-D / 2-D default configuration: the SZ3 tuner's Lorenzo trial runs the
+    # general frontend (Lorenzo + 2-layer Lorenzo), chosen or not
+    out.append(("sz3_2d_interp", spectral_field((300, 400), slope=-4.5, aniso=(4, 1), seed=71), ["-M", "REL", "1e-3"],
+                None))
+    out.append(("sz3_2d_interp_1e2", spectral_field((300, 400), slope=-3.5, seed=71), ["-M", "REL", "1e-2"], None))
+    out.append(("sz3_2d_lorenzo", sum1d((300, 400), 0.0005, seed=72), ["-M", "REL", "1e-3"], None))
+    out.append(("sz3_2d_lorenzo_f64", sum1d((260, 330), 0.0002, seed=73, dtype=np.float64), ["-M", "REL", "1e-4"],
+                None))
+    out.append(("sz3_1d_lorenzo", random_walk((20000,), 74), ["-M", "REL", "1e-3"], None))
+    out.append(("sz3_1d_interp", spectral_field((20000,), slope=-3.5, seed=75), ["-M", "REL", "1e-3"], None))
+    # explicit ALGO_LORENZO_REG on 1-D / 2-D data (general frontend, Lorenzo only)
+    out.append(("lor2d_l2", spectral_field((97, 131), slope=-2.5, noise=0.01, seed=76), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
+                 "AlgoSettings": {"Lorenzo2ndOrder": "YES", "Regression": "NO"}}))
+    out.append(("lor2d_only_f64", spectral_field((60, 77), slope=-3.0, seed=77, dtype=np.float64),
+                ["-M", "REL", "1e-4"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {"Regression": "NO"}}))
+    out.append(("lor2d_l2only_bs8", spectral_field((70, 45), slope=-3.5, seed=78), ["-M", "ABS", "0.02"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
+                 "AlgoSettings": {"Lorenzo": "NO", "Lorenzo2ndOrder": "YES", "Regression": "NO", "BlockSize": "8"}}))
+    out.append(("lor1d_l2", random_walk((3001,), 79), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
+                 "AlgoSettings": {"Lorenzo2ndOrder": "YES", "Regression": "NO"}}))
     return out
+
+
+def sum1d(shape, noise, seed, dtype=np.float32):
+    """f(i) + g(j) plus white noise of `noise` x range (the 2-D Lorenzo
+    predictor reproduces sums of 1-D functions)."""
+    rng = np.random.default_rng(seed)
+    f = rng.standard_normal((shape[0], 1))
+    g = rng.standard_normal((1, shape[1]))
+    base = np.cumsum(f, axis=0) + np.cumsum(g, axis=1)
+    return (base + noise * rng.standard_normal(shape) * (base.max() - base.min())).astype(dtype)
 
 
 def sum2d(shape, noise, seed, dtype=np.float32):
