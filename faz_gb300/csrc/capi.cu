@@ -203,8 +203,11 @@ void check_config(const faz_config &c) {
     if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.FZ && !c.QoZ)
         throw Fail{FAZ_ERR_UNSUPPORTED, "FAZ features (wavelets, SPERR, conditioning; FZ = 1) are not implemented; "
                                         "set FZ = 0 (faz -F 0)"};
-    if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && (c.N != 3 || c.regression2))
+    if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && c.N == 3 && c.regression2)
         throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG is implemented for 3-D data without regression2"};
+    if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && c.N < 3 && (c.regression || c.regression2))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG on 1-D / 2-D data is implemented with Lorenzo predictors "
+                                        "only (Regression = NO)"};
     if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};
     if (c.wavelet != 0 || ((c.wavelet > 0 || c.sperrWithoutWave) && c.sperr >= c.wavelet))
         throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet / SPERR modes are not part of the interpolation path"};
@@ -519,11 +522,18 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
         compress_payload<T>(c, dX, st, payload, psize, tm, launches, sink);
         return;
     }
-    if (c.N != 3 || c.regression2)
-        throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG is implemented for 3-D data without regression2"};
     std::vector<uint8_t> pl;
-    lorenzo3_compress_payload<T>(c.dims, c.blockSize, c.pred_dim, c.lorenzo, c.lorenzo2, c.regression,
-                                 c.absErrorBound, c.quantbinCnt / 2, dX, st, launches, tm, pl);
+    if (c.N < 3) {
+        if (c.regression || c.regression2)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG on 1-D / 2-D data is implemented without regression"};
+        gen_compress_payload<T>(c.N, c.dims, c.blockSize, c.lorenzo, c.lorenzo2, c.absErrorBound, c.quantbinCnt / 2,
+                                dX, st, launches, tm, pl);
+    } else {
+        if (c.N != 3 || c.regression2)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG is implemented for 3-D data without regression2"};
+        lorenzo3_compress_payload<T>(c.dims, c.blockSize, c.pred_dim, c.lorenzo, c.lorenzo2, c.regression,
+                                     c.absErrorBound, c.quantbinCnt / 2, dX, st, launches, tm, pl);
+    }
     psize = pl.size();
     if (sink && sink->dst) {
         if (psize > sink->cap) {
@@ -932,8 +942,9 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
         const bool lor = c.cmprAlgo == FAZ_ALGO_LORENZO_REG;
         if (!lor && c.cmprAlgo != FAZ_ALGO_INTERP)
             throw Fail{FAZ_ERR_UNSUPPORTED, "stream algorithm is neither ALGO_INTERP nor ALGO_LORENZO_REG"};
-        if (lor && (c.N != 3 || c.regression2))
-            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG streams are implemented for 3-D data without regression2"};
+        if (lor && ((c.N == 3 && c.regression2) || (c.N < 3 && (c.regression || c.regression2)) || c.N > 3))
+            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG streams are implemented for 3-D data without "
+                                            "regression2 and for 1-D / 2-D data without regression"};
         if (c.wavelet != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet streams are not part of the interpolation path"};
         if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
         if (caller_buffer && cap < c.num)
@@ -962,7 +973,8 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
             dOut = m.alloc<T>(c.num);
         }
         CK(cudaEventRecord(ev_gpu.a, st));
-        if (lor) lorenzo3_decompress<T>(payload, psize, c.dims, dOut, st, launches, tm);
+        if (lor && c.N < 3) gen_decompress<T>(c.N, payload, psize, c.dims, c.lorenzo, c.lorenzo2, dOut, st, launches, tm);
+        else if (lor) lorenzo3_decompress<T>(payload, psize, c.dims, dOut, st, launches, tm);
         else decompress_device<T>(payload, psize, P, dOut, st, tm, launches);
         CK(cudaEventRecord(ev_gpu.b, st));
         if (!on_device) {

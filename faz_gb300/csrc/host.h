@@ -211,6 +211,13 @@ template <typename T>
 void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);
 template <typename T>
 int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);
+// general Lorenzo frontend for 1-D / 2-D fields (general.cu)
+template <typename T>
+void gen_compress_payload(int N, const uint64_t *dims, int bs, int lo, int lo2, double eb, int radius, const T *dX,
+                          cudaStream_t st, Counter &launches, faz_timings &tm, std::vector<uint8_t> &out);
+template <typename T>
+void gen_decompress(int N, const uint8_t *pl, size_t psize, const uint64_t *dims, int lo, int lo2, T *dOut,
+                    cudaStream_t st, Counter &launches, faz_timings &tm);
 // calAbsErrorBound on the device (capi.cu)
 template <typename T>
 void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);

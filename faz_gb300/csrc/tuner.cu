@@ -454,18 +454,25 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         c.cmprAlgo = FAZ_ALGO_INTERP;
         return;
     }
-    if (N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "tuning a sampled field is implemented for 3-D data on the GPU path"};
-    uint64_t sdims[3];
+    if (N > 3) throw Fail{FAZ_ERR_UNSUPPORTED, "tuning a sampled 4-D field is not implemented on the GPU path"};
+    // sample dims (N of them), embedded as 3-D with leading 1s for the gather
+    uint64_t sdims[3] = {1, 1, 1};
     Dims3 gd{}, sdd{};
+    const int e = 3 - N;
     for (int i = 0; i < 3; i++) {
-        sdims[i] = dims[i] / dmin * 2 * sb;
-        gd.v[i] = (int64_t)dims[i];
-        sdd.v[i] = (int64_t)sdims[i];
+        gd.v[i] = 1;
+        sdd.v[i] = 1;
     }
-    const uint64_t sn = sdims[0] * sdims[1] * sdims[2];
+    uint64_t sn = 1;
+    for (int i = 0; i < N; i++) {
+        sdims[i] = dims[i] / dmin * 2 * sb;
+        gd.v[e + i] = (int64_t)dims[i];
+        sdd.v[e + i] = (int64_t)sdims[i];
+        sn *= sdims[i];
+    }
     DevMem m(st);
     T *dS = m.alloc<T>(sn);
-    k_sample<T><<<(unsigned)((sn + 255) / 256), 256, 0, st>>>(dX, gd, sdd, (int64_t)sb, (int64_t)dmin, 0, dS, sn);
+    k_sample<T><<<(unsigned)((sn + 255) / 256), 256, 0, st>>>(dX, gd, sdd, (int64_t)sb, (int64_t)dmin, e, dS, sn);
     launches(cudaGetLastError());
     const double eb = c.absErrorBound;
     const double sbytes = sn * 1.0 * sizeof(T);
@@ -473,7 +480,7 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     // block-interpolation trials in the configured direction, and the
     // direction-5 trial of whichever wins, computed for both so that every
     // zstd size runs on its own host thread while the GPU moves on.
-    const int dop = 5;  // factorial(N) - 1
+    const int dop = N == 3 ? 5 : (N == 2 ? 1 : 0);  // factorial(N) - 1
     Events ready;
     CK(cudaEventRecord(ready.a, st));
     Trial jl, ji[2], jd[2];
@@ -485,7 +492,8 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     jd[1].name = "cubic-dir5";
     for (Trial *t : {&jl, &ji[0], &ji[1], &jd[0], &jd[1]}) t->t0 = tt0;
     jl.start(ready.a, [&](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
-        lorenzo_payload<T>(sdims, dS, 5, 3, eb, c.quantbinCnt / 2, s2, c2, t2, pl);
+        if (N == 3) lorenzo_payload<T>(sdims, dS, 5, 3, eb, c.quantbinCnt / 2, s2, c2, t2, pl);
+        else gen_compress_payload<T>(N, sdims, 5, 1, 1, eb, c.quantbinCnt / 2, dS, s2, c2, t2, pl);
     });
     const int dir0 = c.interpDirection;
     for (int op = 0; op < 2; op++) {
@@ -581,22 +589,28 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     lc.openmp = 0;
     lc.blockSize = 5;
     set_dims_defaults(lc);  // setDims(sample dims)
-    lc.quantbinCnt = quant_intervals<T>(dX, dims, eb, st, launches);
-    if (lc.quantbinCnt > 65536)
-        throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo with more than 65536 quantisation bins is not implemented on the GPU path"};
-    lc.pred_dim = 2;
-    {
-        std::vector<uint8_t> pl;
-        lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
-        r = sbytes / zstd_framed_size(pl.data(), pl.size());
+    if (N == 3) {
+        lc.quantbinCnt = quant_intervals<T>(dX, dims, eb, st, launches);
+        if (lc.quantbinCnt > 65536)
+            throw Fail{FAZ_ERR_UNSUPPORTED,
+                       "Lorenzo with more than 65536 quantisation bins is not implemented on the GPU path"};
+        lc.pred_dim = 2;
+        {
+            std::vector<uint8_t> pl;
+            lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
+            r = sbytes / zstd_framed_size(pl.data(), pl.size());
+        }
+        if (r > best_l * 1.02) best_l = r;
+        else lc.pred_dim = 3;
     }
-    if (r > best_l * 1.02) best_l = r;
-    else lc.pred_dim = 3;
     if (c.relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
         const int q0 = lc.quantbinCnt;
         lc.quantbinCnt = 16384;
         std::vector<uint8_t> pl;
-        lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
+        if (N == 3)
+            lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
+        else
+            gen_compress_payload<T>(N, sdims, lc.blockSize, 1, 1, eb, lc.quantbinCnt / 2, dS, st, launches, tm, pl);
         r = sbytes / zstd_framed_size(pl.data(), pl.size());
         if (r > best_l * 1.02) best_l = r;
         else lc.quantbinCnt = q0;

@@ -29,9 +29,9 @@ def _rc(name):
     return O.read_stream(golden_stream(golden_case(name)))[0]
 
 
-# default configuration, no QoZ tuning, 3-D (the GPU tuner covers sampled 3-D fields)
+# default configuration, no QoZ tuning (1-D to 3-D fields)
 SZ3_CASES = [c["name"] for c in golden_manifest()
-             if c["ini"] is None and "-q" not in c["flags"] and len(c["dims"]) == 3 and _rc(c["name"]).quantbinCnt <= 65536]
+             if c["ini"] is None and "-q" not in c["flags"] and len(c["dims"]) <= 3 and _rc(c["name"]).quantbinCnt <= 65536]
 # Lorenzo / regression streams
 LOR_DEC_CASES = [c["name"] for c in golden_manifest()
                  if _rc(c["name"]).cmprAlgo == ALGO_LORENZO_REG and _rc(c["name"]).quantbinCnt <= 65536]
@@ -51,8 +51,10 @@ def _same(stream, ref, itemsize):
     c2, p2 = O.read_stream(ref)
     for f in DECISIONS:
         assert getattr(c1, f) == getattr(c2, f), f
-    if c1.cmprAlgo == ALGO_LORENZO_REG:
+    if c1.cmprAlgo == ALGO_LORENZO_REG and c1.N == 3:
         assert mask_fast_frontend_padding(p1, itemsize) == mask_fast_frontend_padding(p2, itemsize)
+    elif c1.cmprAlgo == ALGO_LORENZO_REG:
+        assert p1 == p2  # the general frontend's payload has no padding
     else:
         assert p1 == p2
         assert mask_first_size(stream) == mask_first_size(ref)
@@ -91,7 +93,10 @@ def test_gpu_lorenzo_regression_matches_reference(name):
     stream = F.SZ_compress(cli_config(case), x)
     _, p1 = O.read_stream(stream)
     _, p2 = O.read_stream(golden_stream(case))
-    assert mask_fast_frontend_padding(p1, x.itemsize) == mask_fast_frontend_padding(p2, x.itemsize)
+    if x.ndim == 3:
+        assert mask_fast_frontend_padding(p1, x.itemsize) == mask_fast_frontend_padding(p2, x.itemsize)
+    else:
+        assert p1 == p2
 
 
 def _lor_conf(dims, rel=None, abs_=None, bs=6, lo2=0, pd=None, qbins=65536, reg=0, lo=1):
@@ -160,3 +165,60 @@ def test_gpu_lorenzo_rejects_what_it_does_not_implement():
     conf = _lor_conf(dims, rel=1e-3, bs=9)
     with pytest.raises(F.FazError):
         F.SZ_compress(conf, x)
+
+
+GEN_CASES = [
+    ((97, 131), dict(rel=1e-3, lo2=1, bs=16), np.float32),
+    ((300, 257), dict(rel=1e-4, lo2=1, bs=5), np.float32),
+    ((64, 80), dict(rel=1e-3, lo2=0, bs=16), np.float64),
+    ((70, 45), dict(abs_=0.02, lo=0, lo2=1, bs=8), np.float32),
+    ((33, 2), dict(rel=1e-2, lo2=1, bs=16), np.float32),
+    ((1, 500), dict(rel=1e-3, lo2=1, bs=16), np.float32),
+    ((129, 200), dict(rel=1e-5, lo2=1, bs=64, qbins=4096), np.float32),
+    ((5000,), dict(rel=1e-3, lo2=1, bs=128), np.float32),
+    ((3001,), dict(rel=1e-4, lo2=0, bs=2), np.float64),
+    ((777,), dict(rel=1e-3, lo=0, lo2=1, bs=7), np.float32),
+]
+
+
+@pytest.mark.parametrize("dims,kw,dtype", GEN_CASES)
+def test_gpu_general_frontend_matches_oracle(dims, kw, dtype):
+    """1-D / 2-D ALGO_LORENZO_REG (general frontend, Lorenzo predictors)."""
+    conf = _lor_conf(dims, reg=0, **kw)
+    x = spectral_field(dims, slope=-2.5, noise=0.01, seed=sum(dims), dtype=dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, _ = O.compress(conf, x)
+    _same(stream, ref, np.dtype(dtype).itemsize)
+    assert stream == ref
+    dec, c2 = F.SZ_decompress(None, stream, dtype=dtype)
+    ref_dec, _ = O.decompress(ref, dtype=dtype)
+    assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
+
+
+def test_gpu_general_frontend_rejects_regression():
+    dims = (40, 50)
+    conf = _lor_conf(dims, rel=1e-3, reg=1)
+    with pytest.raises(F.FazError):
+        F.SZ_compress(conf, spectral_field(dims, slope=-3.0, seed=2))
+
+
+@pytest.mark.parametrize("dims,rel,dtype", [((400, 520), 1e-3, np.float32), ((700, 300), 1e-4, np.float64),
+                                            ((60000,), 1e-3, np.float32)])
+def test_gpu_default_config_on_sampled_1d_2d_fields(dims, rel, dtype):
+    """The SZ3 tuner on sampled 1-D / 2-D fields (its Lorenzo trial runs the
+    general frontend), Lorenzo-friendly fields so both branches are met."""
+    rng = np.random.default_rng(sum(dims))
+    if len(dims) == 2:
+        x = (np.cumsum(rng.standard_normal((dims[0], 1)), 0) + np.cumsum(rng.standard_normal((1, dims[1])), 1))
+        x = (x + 0.001 * rng.standard_normal(dims) * np.ptp(x)).astype(dtype)
+    else:
+        x = np.cumsum(rng.standard_normal(dims)).astype(dtype)
+    for arr in (x, spectral_field(dims, slope=-4.0, seed=3, dtype=dtype)):
+        conf = F.Config(*dims)
+        conf.errorBoundMode, conf.relErrorBound = F.EB_REL, rel
+        stream = F.SZ_compress(conf, arr)
+        ref, _ = O.compress(conf, arr)
+        _same(stream, ref, np.dtype(dtype).itemsize)
+        dec, c2 = F.SZ_decompress(None, stream, dtype=dtype)
+        assert np.abs(dec.astype(np.float64) - arr.astype(np.float64)).max() <= c2.absErrorBound
