@@ -15,10 +15,10 @@ from .config import (Config, FazConfigStruct, FazTimings, ALGO_INTERP, ALGO_INTE
                      INTERP_ALGO_LINEAR, INTERP_ALGO_CUBIC, FAZ_FLOAT, FAZ_DOUBLE)
 from .api import (FazError, SZ_compress, SZ_decompress, compress_device, decompress_device, library,
                   last_timings, zstd_version, load_ini, compress_payload_device, decompress_payload_device,
-                  stream_info, tune_device)
+                  stream_info, tune_device, compress_batch)
 
 __all__ = ["Config", "FazConfigStruct", "FazTimings", "FazError", "SZ_compress", "SZ_decompress",
-           "compress_device", "decompress_device", "compress_payload_device", "decompress_payload_device", "stream_info", "tune_device",
+           "compress_device", "decompress_device", "compress_payload_device", "decompress_payload_device", "stream_info", "tune_device", "compress_batch",
            "library", "last_timings", "zstd_version", "load_ini",
            "ALGO_INTERP", "ALGO_INTERP_LORENZO", "ALGO_LORENZO_REG", "ALGO_INTERP_BLOCKED", "EB_ABS", "EB_REL",
            "EB_PSNR", "EB_L2NORM", "EB_ABS_AND_REL", "EB_ABS_OR_REL", "INTERP_ALGO_LINEAR", "INTERP_ALGO_CUBIC",

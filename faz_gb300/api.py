@@ -20,7 +20,7 @@ STATUS = {0: "FAZ_OK", -1: "FAZ_ERR_ARG", -2: "FAZ_ERR_UNSUPPORTED", -3: "FAZ_ER
 EXPORTED = ["faz_config_init", "faz_config_load_ini", "faz_compress", "faz_decompress", "faz_compress_device",
             "faz_decompress_device", "faz_compress_device_payload", "faz_decompress_payload_device",
             "faz_stream_info", "faz_resolve_eb_noalloc", "faz_tune_device", "faz_tuner_features",
-            "faz_mlp_forward", "faz_mlp_backward", "faz_mlp_adam", "faz_tuner_model_create",
+            "faz_compress_batch", "faz_mlp_forward", "faz_mlp_backward", "faz_mlp_adam", "faz_tuner_model_create",
             "faz_tuner_model_destroy", "faz_tuner_infer", "faz_learned_tune",
             "faz_config_size", "faz_free", "faz_last_error", "faz_zstd_version"]
 
@@ -58,6 +58,7 @@ def library():
         L.faz_decompress_payload_device.argtypes = [ctypes.c_int, ctypes.c_int, vp, sz, vp, ctypes.c_uint64, vp, vp]
         i32, i64, f32, f64 = ctypes.c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_double
         L.faz_tune_device.argtypes = [vp, i32, vp, vp, vp]
+        L.faz_compress_batch.argtypes = [i32, vp, i32, vp, vp, vp, vp, i32, vp]
         L.faz_tuner_features.argtypes = [vp, i32, vp, vp, vp]
         L.faz_mlp_forward.argtypes = [vp, vp, i32, vp, vp, vp, vp]
         L.faz_mlp_backward.argtypes = [vp, vp, vp, i32, vp, vp, vp, vp, vp, vp]
@@ -149,6 +150,34 @@ def compress_device(conf, tensor, stream=None):
                                              ctypes.byref(tm)))
     _tls.timings = tm
     return _take_bytes(out, osz.value)
+
+
+def compress_batch(confs, tensors, stream=None, threads=0):
+    """Compress several CUDA tensors (fields of uneven shapes) in one batched
+    call: returns the list of streams, each equal to compress_device's for
+    that field.  All tensors share one dtype and device."""
+    import torch
+    if len(confs) != len(tensors) or not confs:
+        raise ValueError("one configuration per field")
+    ts = [t.contiguous() for t in tensors]
+    dt = {torch.float32: FAZ_FLOAT, torch.float64: FAZ_DOUBLE}.get(ts[0].dtype)
+    if dt is None or any(t.dtype != ts[0].dtype for t in ts):
+        raise TypeError("fields must all be float32 or all float64")
+    for c, t in zip(confs, ts):
+        if c.num != t.numel():
+            raise ValueError("data size does not match conf.dims")
+    n = len(ts)
+    arr = (FazConfigStruct * n)(*[c.to_struct() for c in confs])
+    ptrs = (ctypes.c_void_p * n)(*[t.data_ptr() for t in ts])
+    outs = (ctypes.c_void_p * n)()
+    sizes = (ctypes.c_size_t * n)()
+    st = (stream or torch.cuda.current_stream(ts[0].device)).cuda_stream
+    tm = FazTimings()
+    with torch.cuda.device(ts[0].device):
+        _check(library().faz_compress_batch(n, arr, dt, ptrs, ctypes.c_void_p(st), outs, sizes, int(threads),
+                                            ctypes.byref(tm)))
+    _tls.timings = tm
+    return [_take_bytes(outs[i], sizes[i]) for i in range(n)]
 
 
 def tune_device(conf, tensor, stream=None):

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -244,11 +245,9 @@ template double device_range<double>(const double *, uint64_t, cudaStream_t, Cou
 
 // calAbsErrorBound (include/QoZ/utils/Statistic.hpp:34-66); `rng` computed
 // on the device when the mode needs it.
-template <typename T>
-void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) {
-    if (c.errorBoundMode == FAZ_EB_ABS) return;
-    double rng = 0;
-    if (c.errorBoundMode != FAZ_EB_L2NORM) rng = device_range<T>(dX, c.num, st, launches);
+// the absolute bound of a non-ABS mode from the field's range (max - min in
+// the element type; unused for L2NORM)
+void resolve_eb_range(faz_config &c, double rng) {
     switch (c.errorBoundMode) {
     case FAZ_EB_REL:
         c.absErrorBound = c.relErrorBound * rng;
@@ -274,6 +273,14 @@ void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     }
     if (c.errorBoundMode != FAZ_EB_L2NORM) c.rng = rng;
     c.errorBoundMode = FAZ_EB_ABS;
+}
+
+template <typename T>
+void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) {
+    if (c.errorBoundMode == FAZ_EB_ABS) return;
+    double rng = 0;
+    if (c.errorBoundMode != FAZ_EB_L2NORM) rng = device_range<T>(dX, c.num, st, launches);
+    resolve_eb_range(c, rng);
 }
 template void resolve_eb<float>(faz_config &, const float *, cudaStream_t, Counter &);
 template void resolve_eb<double>(faz_config &, const double *, cudaStream_t, Counter &);
@@ -368,6 +375,79 @@ void append_tree(std::vector<uint8_t> &o, const Codebook &cb, uint64_t nbytes) {
 
 namespace {
 
+// Huffman stage and payload assembly of an interpolation compression whose
+// codes (stream order) and unpredictable values (at their code positions in
+// scratch) are on the device: the bytes SZInterpolationCompressor::compress
+// hands to zstd (SZInterpolationCompressor.hpp:485-512, IntegerQuantizer.hpp:
+// 185-201, HuffmanEncoder.hpp:119-137 and 150-227).
+template <typename T>
+void interp_payload_tail(const faz_config &c, const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
+                         double eb, int radius, uint64_t n, uint16_t *codes, T *scratch, unsigned long long *vcount,
+                         DevMem &m, cudaStream_t st, Counter &launches, faz_timings &tm, Sink *sink,
+                         uint8_t *&payload, size_t &psize, cudaEvent_t huff_end = nullptr) {
+    HuffEncoded he;
+    huffman_encode_device(codes, n, radius, m, st, launches, he, tm);
+    if (vcount) {
+        unsigned long long vc = 0;
+        CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
+        if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
+    }
+    const uint64_t nunpred = he.nzero;
+    const Codebook &cb = he.cb;
+    const uint64_t nbytes = he.nbytes;
+    uint32_t *bits = he.bits;
+    // unpredictable values in stream order
+    T *unpred = m.alloc<T>(nunpred ? nunpred : 1);
+    if (nunpred) launches(launch_compact_zeros<T>(codes, n, he.zc, he.zoff, nullptr, scratch, unpred, st));
+    if (huff_end) CK(cudaEventRecord(huff_end, st));
+    // payload layout (SZInterpolationCompressor.hpp:485-512, IntegerQuantizer.hpp:185-201,
+    // HuffmanEncoder.hpp:119-137 and 150-227)
+    auto th2 = clk::now();
+    std::vector<uint8_t> head;
+    for (int i = 0; i < c.N; i++) put<uint64_t>(head, c.dims[i]);
+    put<uint32_t>(head, (uint32_t)c.interpBlockSize);
+    put<int32_t>(head, (int32_t)c.interpAlgo);
+    put<int32_t>(head, (int32_t)c.interpDirection);
+    put<double>(head, c.alpha);
+    put<double>(head, c.beta);
+    put<uint64_t>(head, c.maxStep);
+    put<int32_t>(head, c.interp_list_len);
+    put<uint8_t>(head, c.blockwiseTuning);
+    put<int32_t>(head, c.fixBlockSize);
+    put<uint64_t>(head, (uint64_t)(int64_t)c.crossBlock);
+    put<int32_t>(head, c.trimToZero);
+    put<int32_t>(head, c.blockOrder);
+    head.insert(head.end(), il.begin(), il.end());
+    head.insert(head.end(), dl.begin(), dl.end());
+    put<uint8_t>(head, 2);
+    put<double>(head, eb);
+    put<int32_t>(head, radius);
+    put<uint64_t>(head, nunpred);
+    std::vector<uint8_t> tree;
+    append_tree(tree, cb, nbytes);
+    psize = head.size() + nunpred * sizeof(T) + tree.size() + nbytes;
+    if (sink && sink->dst) {
+        if (psize > sink->cap) {
+            sink->too_small = true;
+            throw Fail{FAZ_ERR_ARG, "payload buffer too small: need " + std::to_string(psize) + " bytes"};
+        }
+        payload = sink->dst;
+    } else {
+        payload = t_pin_payload.get(psize + 8);
+    }
+    std::memcpy(payload, head.data(), head.size());
+    size_t o = head.size();
+    tm.host_ms += ms_since(th2);
+    if (nunpred) CK(cudaMemcpyAsync(payload + o, unpred, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
+    o += nunpred * sizeof(T);
+    std::memcpy(payload + o, tree.data(), tree.size());
+    o += tree.size();
+    if (nbytes) CK(cudaMemcpyAsync(payload + o, bits, nbytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    tm.unpred_count = nunpred;
+    tm.payload_bytes = psize;
+}
+
 template <typename T>
 void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&payload, size_t &psize,
                       faz_timings &tm, Counter &launches, Sink *sink = nullptr) {
@@ -416,67 +496,8 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     CK(cudaEventRecord(ev_fin.b, st));
     CK(cudaEventRecord(ev_pred.b, st));
     CK(cudaEventRecord(ev_huff.a, st));
-    HuffEncoded he;
-    huffman_encode_device(codes, n, radius, m, st, launches, he, tm);
-    if (vcount) {
-        unsigned long long vc = 0;
-        CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
-        if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
-    }
-    const uint64_t nunpred = he.nzero;
-    const Codebook &cb = he.cb;
-    const uint64_t nbytes = he.nbytes;
-    uint32_t *bits = he.bits;
-    // unpredictable values in stream order
-    T *unpred = m.alloc<T>(nunpred ? nunpred : 1);
-    if (nunpred) launches(launch_compact_zeros<T>(codes, n, he.zc, he.zoff, nullptr, scratch, unpred, st));
-    CK(cudaEventRecord(ev_huff.b, st));
-    // payload layout (SZInterpolationCompressor.hpp:485-512, IntegerQuantizer.hpp:185-201,
-    // HuffmanEncoder.hpp:119-137 and 150-227)
-    auto th2 = clk::now();
-    std::vector<uint8_t> head;
-    for (int i = 0; i < c.N; i++) put<uint64_t>(head, c.dims[i]);
-    put<uint32_t>(head, (uint32_t)c.interpBlockSize);
-    put<int32_t>(head, (int32_t)c.interpAlgo);
-    put<int32_t>(head, (int32_t)c.interpDirection);
-    put<double>(head, c.alpha);
-    put<double>(head, c.beta);
-    put<uint64_t>(head, c.maxStep);
-    put<int32_t>(head, c.interp_list_len);
-    put<uint8_t>(head, c.blockwiseTuning);
-    put<int32_t>(head, c.fixBlockSize);
-    put<uint64_t>(head, (uint64_t)(int64_t)c.crossBlock);
-    put<int32_t>(head, c.trimToZero);
-    put<int32_t>(head, c.blockOrder);
-    head.insert(head.end(), il.begin(), il.end());
-    head.insert(head.end(), dl.begin(), dl.end());
-    put<uint8_t>(head, 2);
-    put<double>(head, eb);
-    put<int32_t>(head, radius);
-    put<uint64_t>(head, nunpred);
-    std::vector<uint8_t> tree;
-    append_tree(tree, cb, nbytes);
-    psize = head.size() + nunpred * sizeof(T) + tree.size() + nbytes;
-    if (sink && sink->dst) {
-        if (psize > sink->cap) {
-            sink->too_small = true;
-            throw Fail{FAZ_ERR_ARG, "payload buffer too small: need " + std::to_string(psize) + " bytes"};
-        }
-        payload = sink->dst;
-    } else {
-        payload = t_pin_payload.get(psize + 8);
-    }
-    std::memcpy(payload, head.data(), head.size());
-    size_t o = head.size();
-    tm.host_ms += ms_since(th2);
-    if (nunpred) CK(cudaMemcpyAsync(payload + o, unpred, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
-    o += nunpred * sizeof(T);
-    std::memcpy(payload + o, tree.data(), tree.size());
-    o += tree.size();
-    if (nbytes) CK(cudaMemcpyAsync(payload + o, bits, nbytes, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    tm.unpred_count = nunpred;
-    tm.payload_bytes = psize;
+    interp_payload_tail<T>(c, il, dl, eb, radius, n, codes, scratch, vcount, m, st, launches, tm, sink, payload, psize,
+                           ev_huff.b);
     tm.predict_ms = ev_pred.ms();
     tm.finest_level_ms = p.lv.empty() ? 0.0 : ev_fin.ms();
     tm.huffman_ms = ev_huff.ms();
@@ -550,7 +571,7 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
 // Lossless_zstd::compress framing (include/QoZ/lossless/Lossless_zstd.hpp:22-32),
 // then Config::save + int32 trailer size (include/QoZ/api/sz.hpp:77-91).
 void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, char **out, size_t *out_size,
-                   faz_timings &tm) {
+                   faz_timings &tm, int zthreads = -1) {
     std::string err;
     const Zstd &z = zstd_lib(err);
     if (!z.ok) throw Fail{FAZ_ERR_ZSTD, err};
@@ -560,7 +581,7 @@ void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, ch
     // FAZ_ZSTD_THREADS (default the host's cores up to 16) cuts a large payload
     // into independent frames compressed in parallel; 0 writes exactly the
     // single frame of ZSTD_compress, as the reference does
-    const int nframes = zstd_frame_count(psize, zstd_threads());
+    const int nframes = zstd_frame_count(psize, zthreads >= 0 ? zthreads : zstd_threads());
     size_t bound = zstd_frames_bound(z, psize, nframes);
     size_t cap = 8 + bound + trailer.size() + 4;
     char *buf = (char *)std::malloc(cap);
@@ -619,6 +640,291 @@ int compress_payload_impl(const faz_config *conf_in, const void *d_data, void *u
         set_error(f.msg);
         return f.code;
     } catch (const std::exception &e) {
+        set_error(e.what());
+        return FAZ_ERR_ARG;
+    }
+    tm.total_ms = ms_since(t0);
+    if (tmo) *tmo = tm;
+    return FAZ_OK;
+}
+
+// Batched compression of device-resident fields: one launch resolves every
+// field's range, one persistent launch runs every ALGO_INTERP field's first
+// point / anchors and all of its levels from a work queue, then the Huffman
+// stage, payload and zstd frame of each field run on a pool of host threads
+// (each with its own stream).  Fields with another algorithm (a tuner, Lorenzo)
+// are compressed one by one afterwards.  Every stream equals the one
+// faz_compress_device writes for the same field and configuration.
+template <typename T>
+int compress_batch_impl(int nf, const faz_config *confs, const void *const *d_data, void *user_stream, char **outs,
+                        size_t *out_sizes, int threads_hint, faz_timings *tmo) {
+    faz_timings tm;
+    std::memset(&tm, 0, sizeof(tm));
+    auto t0 = clk::now();
+    try {
+        if (nf <= 0 || !confs || !d_data || !outs || !out_sizes) throw Fail{FAZ_ERR_ARG, "null argument"};
+        for (int i = 0; i < nf; i++) {
+            outs[i] = nullptr;
+            out_sizes[i] = 0;
+            if (!d_data[i]) throw Fail{FAZ_ERR_ARG, "null field pointer"};
+        }
+        init_pool_once();
+        StreamGuard sg(user_stream, false, NullStream::Default);
+        cudaStream_t st = sg.st;
+        Counter launches;
+        std::vector<faz_config> cs(confs, confs + nf);
+        for (auto &c : cs) check_config(c);
+        DevMem m(st);
+        // ranges of every field that needs one, in one launch
+        {
+            std::vector<const T *> ptr;
+            std::vector<uint64_t> num;
+            std::vector<int> which;
+            for (int i = 0; i < nf; i++)
+                if (cs[i].errorBoundMode != FAZ_EB_ABS && cs[i].errorBoundMode != FAZ_EB_L2NORM) {
+                    which.push_back(i);
+                    ptr.push_back((const T *)d_data[i]);
+                    num.push_back(cs[i].num);
+                }
+            std::vector<double> rng(nf, 0.0);
+            if (!which.empty()) {
+                const int nb = 64, k = (int)which.size();
+                const T **dptr = m.alloc<const T *>(k);
+                uint64_t *dnum = m.alloc<uint64_t>(k);
+                T *pmin = m.alloc<T>((size_t)k * nb), *pmax = m.alloc<T>((size_t)k * nb);
+                CK(cudaMemcpyAsync(dptr, ptr.data(), k * sizeof(T *), cudaMemcpyHostToDevice, st));
+                CK(cudaMemcpyAsync(dnum, num.data(), k * 8, cudaMemcpyHostToDevice, st));
+                launches(launch_minmax_batch<T>(dptr, dnum, k, pmin, pmax, nb, st));
+                std::vector<T> hmin((size_t)k * nb), hmax((size_t)k * nb);
+                CK(cudaMemcpyAsync(hmin.data(), pmin, hmin.size() * sizeof(T), cudaMemcpyDeviceToHost, st));
+                CK(cudaMemcpyAsync(hmax.data(), pmax, hmax.size() * sizeof(T), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                for (int j = 0; j < k; j++) {
+                    T mn = hmin[(size_t)j * nb], mx = hmax[(size_t)j * nb];
+                    for (int b = 0; b < nb; b++) {
+                        mn = std::min(mn, hmin[(size_t)j * nb + b]);
+                        mx = std::max(mx, hmax[(size_t)j * nb + b]);
+                    }
+                    const T r = mx - mn;
+                    rng[which[j]] = (double)r;
+                }
+            }
+            for (int i = 0; i < nf; i++)
+                if (cs[i].errorBoundMode != FAZ_EB_ABS) resolve_eb_range(cs[i], rng[i]);
+        }
+        for (auto &c : cs)
+            if (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))
+                throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
+        // plans and work queue of the ALGO_INTERP fields
+        struct FieldWork {
+            int idx;
+            Plan p;
+            std::vector<uint8_t> il, dl;
+            uint16_t *codes;
+            T *W, *scratch;
+        };
+        std::vector<FieldWork> fw;
+        std::vector<int> rest;
+        const int threads = threads_hint == 256 || threads_hint == 128 ? threads_hint : 512;
+        for (int i = 0; i < nf; i++) {
+            const faz_config &c = cs[i];
+            if (c.cmprAlgo != FAZ_ALGO_INTERP) {
+                rest.push_back(i);
+                continue;
+            }
+            FieldWork w;
+            w.idx = i;
+            w.il.assign(c.interpAlgo_list, c.interpAlgo_list + c.interp_list_len);
+            w.dl.assign(c.interpDirection_list, c.interpDirection_list + c.interp_list_len);
+            w.p = make_plan<T>(c.N, c.dims, c.maxStep, c.interpBlockSize, c.fixBlockSize, c.interpAlgo,
+                               c.interpDirection, w.il, w.dl, c.absErrorBound, c.alpha, c.beta, c.quantbinCnt / 2,
+                               c.trimToZero, smem_limit());
+            w.W = m.alloc<T>(w.p.num);
+            w.scratch = m.alloc<T>(w.p.num);
+            w.codes = m.alloc<uint16_t>(w.p.num);
+            fw.push_back(std::move(w));
+        }
+        Events ev_pred;
+        CK(cudaEventRecord(ev_pred.a, st));
+        if (!fw.empty()) {
+            std::vector<uint64_t> boff;
+            std::vector<BatchField> bf(fw.size());
+            std::vector<LevelArgs> la;
+            std::vector<BatchGroup> groups;
+            std::vector<size_t> boff_base(fw.size());
+            bool wide = false;
+            size_t smem = 16;
+            for (size_t k = 0; k < fw.size(); k++) {
+                boff_base[k] = boff.size();
+                boff.insert(boff.end(), fw[k].p.block_off.begin(), fw[k].p.block_off.end());
+                wide = wide || (int64_t)fw[k].p.num >= ((int64_t)1 << 31);
+            }
+            uint64_t *dboff = m.alloc<uint64_t>(boff.size() + 1);
+            CK(cudaMemcpyAsync(dboff, boff.data(), boff.size() * 8, cudaMemcpyHostToDevice, st));
+            std::vector<int> first_la(fw.size());
+            for (size_t k = 0; k < fw.size(); k++) {
+                const faz_config &c = cs[fw[k].idx];
+                const Plan &p = fw[k].p;
+                BatchField &f = bf[k];
+                std::memset(&f, 0, sizeof(f));
+                f.X = d_data[fw[k].idx];
+                f.W = fw[k].W;
+                f.codes = fw[k].codes;
+                f.scratch = fw[k].scratch;
+                f.eb = c.absErrorBound;
+                f.recip = 1.0 / c.absErrorBound;
+                f.radius = c.quantbinCnt / 2;
+                f.trim = c.trimToZero;
+                f.anchor = p.anchor ? 1 : 0;
+                for (int a = 0; a < 3; a++) {
+                    f.na[a] = p.na[a];
+                    f.offs[a] = p.offs3[a];
+                    f.step[a] = 1;
+                }
+                for (int a = 0; a < p.N; a++) f.step[3 - p.N + a] = (int64_t)p.maxStep;
+                first_la[k] = (int)la.size();
+                for (const LevelPlan &L : p.lv) {
+                    LevelArgs a = L.args;
+                    a.block_off = dboff + boff_base[k] + L.off_index;
+                    a.ncodes = p.num;
+                    a.err = nullptr;
+                    a.verify = nullptr;
+                    la.push_back(a);
+                    smem = std::max(smem, level_smem_bytes<T>(a));
+                }
+            }
+            // groups round by round: first points / anchors, then the coarsest
+            // level of every field, the next level, ...
+            std::vector<int> last(fw.size(), -1);
+            size_t rounds = 0;
+            for (auto &w : fw) rounds = std::max(rounds, w.p.lv.size());
+            int64_t item = 0;
+            for (size_t r = 0; r <= rounds; r++) {
+                for (size_t k = 0; k < fw.size(); k++) {
+                    BatchGroup g;
+                    g.field = (int)k;
+                    g.dep = last[k];
+                    g.item0 = item;
+                    if (r == 0) {
+                        g.args = -1;
+                        if (bf[k].anchor) {
+                            const int64_t nan = bf[k].na[0] * bf[k].na[1] * bf[k].na[2];
+                            g.kind = 1;
+                            g.nitems = (nan + threads - 1) / threads;
+                        } else {
+                            g.kind = 0;
+                            g.nitems = 1;
+                        }
+                    } else {
+                        if (r - 1 >= fw[k].p.lv.size()) continue;
+                        g.kind = 2;
+                        g.args = first_la[k] + (int)(r - 1);
+                        g.nitems = fw[k].p.lv[r - 1].nblocks;
+                    }
+                    if (g.nitems <= 0) continue;
+                    if (g.nitems >= ((int64_t)1 << 31)) throw Fail{FAZ_ERR_UNSUPPORTED, "too many blocks in one level"};
+                    last[k] = (int)groups.size();
+                    groups.push_back(g);
+                    item += g.nitems;
+                }
+            }
+            BatchGroup *dg = m.alloc<BatchGroup>(groups.size());
+            BatchField *dbf = m.alloc<BatchField>(bf.size());
+            LevelArgs *dla = m.alloc<LevelArgs>(la.size() + 1);
+            unsigned *done = m.alloc<unsigned>(groups.size());
+            unsigned long long *counter = m.alloc<unsigned long long>(1);
+            int *err = m.alloc<int>(1);
+            CK(cudaMemcpyAsync(dg, groups.data(), groups.size() * sizeof(BatchGroup), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(dbf, bf.data(), bf.size() * sizeof(BatchField), cudaMemcpyHostToDevice, st));
+            if (!la.empty())
+                CK(cudaMemcpyAsync(dla, la.data(), la.size() * sizeof(LevelArgs), cudaMemcpyHostToDevice, st));
+            CK(cudaMemsetAsync(done, 0, groups.size() * 4, st));
+            CK(cudaMemsetAsync(counter, 0, 8, st));
+            CK(cudaMemsetAsync(err, 0, 4, st));
+            int dev = 0, sms = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            const int occ = std::max(1, wide ? batch_occupancy<T, true>(threads, smem) : batch_occupancy<T, false>(threads, smem));
+            const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(item, (int64_t)sms * occ));
+            launches(launch_interp_batch<T>(dg, (int)groups.size(), dbf, dla, (uint64_t)item, counter, done, err, wide,
+                                            (int)grid, threads, smem, st));
+            int herr = 0;
+            CK(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (herr) throw Fail{FAZ_ERR_DEVICE, "batched levels: an item waited too long for its previous level"};
+        }
+        CK(cudaEventRecord(ev_pred.b, st));
+        CK(cudaStreamSynchronize(st));
+        tm.predict_ms = ev_pred.ms();
+        // Huffman, payload and zstd of each field on a pool of host threads
+        std::atomic<size_t> next{0};
+        std::vector<std::string> errs(fw.size());
+        std::vector<int> codes_rc(fw.size(), 0);
+        std::vector<faz_timings> tms(fw.size());
+        std::vector<uint64_t> nl(fw.size(), 0);
+        auto worker = [&]() {
+            {
+                const size_t k = next.fetch_add(1);
+                if (k >= fw.size()) return;
+                try {
+                    std::memset(&tms[k], 0, sizeof(faz_timings));
+                    StreamGuard s2(nullptr);
+                    DevMem m2(s2.st);
+                    Counter c2;
+                    faz_config c = cs[fw[k].idx];
+                    uint8_t *payload;
+                    size_t psize;
+                    interp_payload_tail<T>(c, fw[k].il, fw[k].dl, c.absErrorBound, c.quantbinCnt / 2, fw[k].p.num,
+                                           fw[k].codes, fw[k].scratch, nullptr, m2, s2.st, c2, tms[k], nullptr,
+                                           payload, psize);
+                    finish_stream(c, payload, psize, &outs[fw[k].idx], &out_sizes[fw[k].idx], tms[k], 0);
+                    nl[k] = c2.n;
+                } catch (const Fail &f) {
+                    codes_rc[k] = f.code;
+                    errs[k] = f.msg;
+                } catch (const std::exception &e) {
+                    codes_rc[k] = FAZ_ERR_ARG;
+                    errs[k] = e.what();
+                }
+            }
+        };
+        {
+            std::vector<std::function<void()>> tasks(fw.size(), worker);
+            HostPool::get().run(tasks);
+        }
+        for (size_t k = 0; k < fw.size(); k++) {
+            if (codes_rc[k]) throw Fail{codes_rc[k], errs[k]};
+            launches.n += nl[k];
+            tm.zstd_ms += tms[k].zstd_ms;
+            tm.huffman_ms += tms[k].huffman_ms;
+            tm.payload_bytes += tms[k].payload_bytes;
+            tm.unpred_count += tms[k].unpred_count;
+        }
+        // the other fields, one by one
+        for (int i : rest) {
+            faz_config c = cs[i];
+            uint8_t *payload;
+            size_t psize;
+            faz_timings t1;
+            std::memset(&t1, 0, sizeof(t1));
+            compress_dispatch<T>(c, (const T *)d_data[i], st, payload, psize, t1, launches);
+            finish_stream(c, payload, psize, &outs[i], &out_sizes[i], t1);
+            tm.zstd_ms += t1.zstd_ms;
+            tm.payload_bytes += t1.payload_bytes;
+        }
+        tm.kernel_launches = launches.n;
+    } catch (const Fail &f) {
+        for (int i = 0; i < nf && outs; i++) {
+            std::free(outs[i]);
+            outs[i] = nullptr;
+        }
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception &e) {
+        for (int i = 0; i < nf && outs; i++) {
+            std::free(outs[i]);
+            outs[i] = nullptr;
+        }
         set_error(e.what());
         return FAZ_ERR_ARG;
     }
@@ -1255,6 +1561,15 @@ unsigned faz_zstd_version(void) {
     return z.ok ? z.version : 0;
 }
 
+
+int faz_compress_batch(int n, const faz_config *confs, int dtype, const void *const *d_data, void *stream, char **outs,
+                       size_t *out_sizes, int threads, faz_timings *timings) {
+    if (dtype == FAZ_FLOAT) return faz::compress_batch_impl<float>(n, confs, d_data, stream, outs, out_sizes, threads, timings);
+    if (dtype == FAZ_DOUBLE)
+        return faz::compress_batch_impl<double>(n, confs, d_data, stream, outs, out_sizes, threads, timings);
+    faz::set_error("dtype must be FAZ_FLOAT or FAZ_DOUBLE");
+    return FAZ_ERR_ARG;
+}
 
 int faz_tune_device(faz_config *conf, int dtype, const void *d_data, void *stream, faz_timings *timings) {
     if (dtype == FAZ_FLOAT) return faz::tune_impl<float>(conf, d_data, stream, timings);

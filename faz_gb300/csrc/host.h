@@ -7,6 +7,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -14,6 +16,7 @@
 #include <functional>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -119,6 +122,70 @@ struct StreamGuard {
     ~StreamGuard() {
         if (own) cudaStreamDestroy(st);
     }
+};
+
+// Host threads that live for the process, so that their thread-local pinned
+// staging buffers are reused from call to call.  run() executes the tasks on
+// the pool (the caller waits) and is safe to call from several threads.
+class HostPool {
+  public:
+    static HostPool &get() {
+        static HostPool pool;
+        return pool;
+    }
+    void run(std::vector<std::function<void()>> &tasks) {
+        if (tasks.empty()) return;
+        struct Batch {
+            std::mutex mu;
+            std::condition_variable cv;
+            size_t left;
+        } b;
+        b.left = tasks.size();
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            for (auto &t : tasks)
+                q_.push_back([&b, &t] {
+                    t();
+                    std::lock_guard<std::mutex> g2(b.mu);
+                    if (--b.left == 0) b.cv.notify_all();
+                });
+        }
+        cv_.notify_all();
+        std::unique_lock<std::mutex> lk(b.mu);
+        b.cv.wait(lk, [&] { return b.left == 0; });
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+
+  private:
+    HostPool() {
+        const unsigned n = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        for (unsigned i = 0; i < n; i++)
+            th_.emplace_back([this] {
+                for (;;) {
+                    std::function<void()> job;
+                    {
+                        std::unique_lock<std::mutex> lk(mu_);
+                        cv_.wait(lk, [this] { return stop_ || !q_.empty(); });
+                        if (stop_ && q_.empty()) return;
+                        job = std::move(q_.front());
+                        q_.pop_front();
+                    }
+                    job();
+                }
+            });
+    }
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<std::function<void()>> q_;
+    std::vector<std::thread> th_;
+    bool stop_ = false;
 };
 
 struct Events {

@@ -52,6 +52,37 @@ template <typename T>
 cudaError_t launch_anchors(bool decomp, const T *X, T *W, uint16_t *codes, T *scratch, const T *unpred,
                            const int64_t *na, const int64_t *step, const int64_t *offs, cudaStream_t st);
 
+// Batched compression: every field's first point / anchors and levels in one
+// persistent launch from a device work queue (interp.cu).
+struct BatchField {
+    const void *X;
+    void *W;
+    uint16_t *codes;
+    void *scratch;
+    double eb, recip;  // base error bound (first point)
+    int radius, trim;
+    int anchor;        // 1: anchor grid (na, step, offs), 0: first point
+    int64_t na[3], step[3], offs[3];
+};
+struct BatchGroup {
+    int field;
+    int kind;        // 0 first point, 1 anchors, 2 level
+    int args;        // level: index into the LevelArgs table
+    int dep;         // group whose items must all be done first (-1: none)
+    int64_t nitems;  // work items (blocks; anchor chunks of `threads` anchors; 1)
+    int64_t item0;   // first ticket of the group
+};
+template <typename T>
+cudaError_t launch_interp_batch(const BatchGroup *groups, int ngroups, const BatchField *fields, const LevelArgs *largs,
+                                uint64_t total, unsigned long long *counter, unsigned *done, int *err, bool wide,
+                                int grid, int threads, size_t smem, cudaStream_t st);
+
+template <typename T>
+cudaError_t launch_minmax_batch(const T *const *X, const uint64_t *n, int nfields, T *pmin, T *pmax, int nblocks,
+                                cudaStream_t st);
+template <typename T, bool WIDE>
+int batch_occupancy(int threads, size_t smem);
+
 uint64_t hist_subchunks(uint64_t n);
 cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, int center, unsigned long long *hist,
                              unsigned long long *first, unsigned long long *zcount, cudaStream_t st);

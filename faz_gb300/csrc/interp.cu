@@ -160,16 +160,17 @@ __device__ __forceinline__ uint64_t owner_pos_sweep2(const LevelArgs &a, const B
 // WIDE selects 64-bit element offsets; fields below 2^31 elements use 32-bit
 // offsets from the block's first element.  QM selects the quantiser path
 // (1: straight-line float path, 0: general).
-template <typename T, bool DECOMP, bool WIDE, int QM>
-__global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
-                                                      uint16_t *__restrict__ codes, T *__restrict__ scratch,
-                                                      const uint64_t *__restrict__ zpos, uint64_t nz,
-                                                      const T *__restrict__ unpred) {
+// COH: coarse values come from W through L2 (ld.global.cg) instead of
+// cp.async (which may hit L1): in the batched launch other SMs write W during
+// the launch, and L1 is not coherent.
+template <typename T, bool DECOMP, bool WIDE, int QM, bool COH>
+__device__ __forceinline__ void level_block(const LevelArgs &a, const int64_t bid, const T *__restrict__ X,
+                                            T *__restrict__ W, uint16_t *__restrict__ codes,
+                                            T *__restrict__ scratch, const uint64_t *__restrict__ zpos, uint64_t nz,
+                                            const T *__restrict__ unpred, unsigned char *smem_raw) {
     using Off = typename std::conditional<WIDE, int64_t, int32_t>::type;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     T *V = reinterpret_cast<T *>(smem_raw);
     uint16_t *stg = reinterpret_cast<uint16_t *>(smem_raw + (((size_t)a.vwords * sizeof(T) + 15) & ~(size_t)15));
-    const int64_t bid = blockIdx.x;
     int64_t bc[3];
     block_coords(a, bid, bc);
     BlockGeom g;
@@ -207,7 +208,11 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
             const T *src = coarse ? W : X;
             const Off rb = m0 * G0 + m1 * G1;
             T *dst = V + r * h2;
-            for (int e = lane; e < h2; e += 32) cp_async<sizeof(T)>(dst + e, src + rb + (Off)(2 * e) * G2);
+            if (COH && coarse) {
+                for (int e = lane; e < h2; e += 32) dst[e] = __ldcg(src + rb + (Off)(2 * e) * G2);
+            } else {
+                for (int e = lane; e < h2; e += 32) cp_async<sizeof(T)>(dst + e, src + rb + (Off)(2 * e) * G2);
+            }
         }
         cp_async_wait_all();
     }
@@ -396,6 +401,137 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     }
 }
 
+template <typename T, bool DECOMP, bool WIDE, int QM>
+__global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
+                                                      uint16_t *__restrict__ codes, T *__restrict__ scratch,
+                                                      const uint64_t *__restrict__ zpos, uint64_t nz,
+                                                      const T *__restrict__ unpred) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    level_block<T, DECOMP, WIDE, QM, false>(a, blockIdx.x, X, W, codes, scratch, zpos, nz, unpred, smem_raw);
+}
+
+// ------------------------------------------------------ batched launch
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+constexpr unsigned kBatchWaitLimit = 1u << 22;  // polls (with back-off) of a dependency before giving up
+
+// Every field's first point / anchor grid and interpolation levels, in one
+// launch of persistent CTAs.  Tickets are work items in queue order: groups
+// (a field's first point, anchor chunk or level) come round by round, the
+// first points and anchors first, then every field's coarsest level, and so
+// on.  A CTA takes a ticket, waits until every item of the group it depends on
+// (the same field's previous level) is done, runs it and counts it done.  The
+// groups waited for hold smaller tickets, taken by CTAs already running, so
+// every wait ends; each is bounded all the same (error flag, then the item
+// runs).  Coarse values written in this launch are read through L2.
+template <typename T, bool WIDE>
+__global__ void __launch_bounds__(512, 2)
+    k_interp_batch(const BatchGroup *__restrict__ groups, int ngroups, const BatchField *__restrict__ fields,
+                   const LevelArgs *__restrict__ largs, uint64_t total, unsigned long long *counter, unsigned *done,
+                   int *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ unsigned long long s_t;
+    __shared__ int s_g;
+    __shared__ int64_t s_local;
+    __shared__ LevelArgs s_a;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long t = atomicAdd(counter, 1ull);
+            s_t = t;
+            if (t < total) {
+                int lo = 0, hi = ngroups - 1;  // last group with item0 <= t
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if ((unsigned long long)groups[mid].item0 <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+                s_g = lo;
+                s_local = (int64_t)(t - (unsigned long long)groups[lo].item0);
+                const int dep = groups[lo].dep;
+                if (dep >= 0) {
+                    const unsigned need = (unsigned)groups[dep].nitems;
+                    unsigned it = 0;
+                    while (ld_acquire_u32(done + dep) < need) {
+                        if (++it > kBatchWaitLimit) {
+                            atomicExch(err, 1);
+                            break;
+                        }
+                        __nanosleep(128);
+                    }
+                }
+                if (groups[lo].kind == 2) s_a = largs[groups[lo].args];
+            }
+        }
+        __syncthreads();
+        if (s_t >= total) return;
+        const BatchGroup g = groups[s_g];
+        const BatchField &f = fields[g.field];
+        const T *X = (const T *)f.X;
+        T *W = (T *)f.W;
+        T *scratch = (T *)f.scratch;
+        if (g.kind == 0) {
+            if (threadIdx.x == 0) {
+                T v = X[0], uv;
+                const int code = quantize(v, (T)0, f.eb, f.recip, f.radius, f.trim, uv);
+                f.codes[0] = (uint16_t)code;
+                if (code == 0) scratch[0] = uv;
+                W[0] = v;
+            }
+        } else if (g.kind == 1) {
+            const int64_t i = s_local * blockDim.x + threadIdx.x;
+            const int64_t nan = f.na[0] * f.na[1] * f.na[2];
+            if (i < nan) {
+                const int64_t z = i % f.na[2], r = i / f.na[2];
+                const int64_t y = r % f.na[1], x = r / f.na[1];
+                const int64_t gi = x * f.step[0] * f.offs[0] + y * f.step[1] * f.offs[1] + z * f.step[2] * f.offs[2];
+                const T v = X[gi];
+                f.codes[i] = 0;
+                scratch[i] = v;
+                W[gi] = v;
+            }
+        } else {
+            const bool straight = sizeof(T) == 4 && s_a.fast && s_a.trim == 0;
+            if (straight)
+                level_block<T, false, WIDE, 1, true>(s_a, s_local, X, W, f.codes, scratch, nullptr, 0, nullptr,
+                                                     smem_raw);
+            else
+                level_block<T, false, WIDE, 0, true>(s_a, s_local, X, W, f.codes, scratch, nullptr, 0, nullptr,
+                                                     smem_raw);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(done + s_g, 1u);
+        }
+    }
+}
+
+template <typename T>
+cudaError_t launch_interp_batch(const BatchGroup *groups, int ngroups, const BatchField *fields, const LevelArgs *largs,
+                                uint64_t total, unsigned long long *counter, unsigned *done, int *err, bool wide,
+                                int grid, int threads, size_t smem, cudaStream_t st) {
+    const void *k = wide ? (const void *)k_interp_batch<T, true> : (const void *)k_interp_batch<T, false>;
+    cudaError_t e = allow_dynamic_smem(k);
+    if (e != cudaSuccess) return e;
+    if (wide)
+        k_interp_batch<T, true><<<grid, threads, smem, st>>>(groups, ngroups, fields, largs, total, counter, done, err);
+    else
+        k_interp_batch<T, false><<<grid, threads, smem, st>>>(groups, ngroups, fields, largs, total, counter, done,
+                                                               err);
+    return cudaGetLastError();
+}
+
+template <typename T, bool WIDE>
+int batch_occupancy(int threads, size_t smem) {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_interp_batch<T, WIDE>, threads, smem);
+    return n;
+}
+
 // ------------------------------------------------- first point / anchors
 // First point quantised against prediction 0 with the base bound
 // (SZInterpolationCompressor.hpp:372-374), or the anchor grid of build_grid
@@ -442,13 +578,14 @@ __global__ void k_anchors(const T *X, T *W, uint16_t *codes, T *scratch, const T
 // ------------------------------------------------------------- min / max
 // 16-byte loads over the aligned body, scalar loads for the ends.
 template <typename T>
-__global__ void k_minmax(const T *__restrict__ X, uint64_t n, T *pmin, T *pmax) {
+__device__ __forceinline__ void minmax_body(const T *__restrict__ X, uint64_t n, unsigned bid, unsigned nblocks,
+                                            T *pmin, T *pmax) {
     T mn = X[0], mx = X[0];
     constexpr int V = 16 / sizeof(T);
     const uint64_t head = ((16 - ((uintptr_t)X & 15)) & 15) / sizeof(T);
     const uint64_t h = head < n ? head : n;
     const uint64_t nvec = (n - h) / V;
-    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nth = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t tid = bid * (uint64_t)blockDim.x + threadIdx.x, nth = (uint64_t)nblocks * blockDim.x;
     const uint4 *xv = reinterpret_cast<const uint4 *>(X + h);
     for (uint64_t i = tid; i < nvec; i += nth) {
         uint4 q = __ldg(xv + i);
@@ -490,8 +627,27 @@ __global__ void k_minmax(const T *__restrict__ X, uint64_t n, T *pmin, T *pmax) 
             mn = a < mn ? a : mn;
             mx = b > mx ? b : mx;
         }
-        if (lane == 0) { pmin[blockIdx.x] = mn; pmax[blockIdx.x] = mx; }
+        if (lane == 0) { pmin[bid] = mn; pmax[bid] = mx; }
     }
+}
+
+template <typename T>
+__global__ void k_minmax(const T *__restrict__ X, uint64_t n, T *pmin, T *pmax) {
+    minmax_body(X, n, blockIdx.x, gridDim.x, pmin, pmax);
+}
+
+// min / max of every field of a batch: CTA (b, f) takes slice b of field f
+template <typename T>
+__global__ void k_minmax_batch(const T *const *__restrict__ X, const uint64_t *__restrict__ n, T *pmin, T *pmax) {
+    const unsigned f = blockIdx.y;
+    minmax_body(X[f], n[f], blockIdx.x, gridDim.x, pmin + (size_t)f * gridDim.x, pmax + (size_t)f * gridDim.x);
+}
+
+template <typename T>
+cudaError_t launch_minmax_batch(const T *const *X, const uint64_t *n, int nfields, T *pmin, T *pmax, int nblocks,
+                                cudaStream_t st) {
+    k_minmax_batch<T><<<dim3(nblocks, nfields), 512, 0, st>>>(X, n, pmin, pmax);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------ launchers
@@ -563,7 +719,14 @@ cudaError_t launch_anchors(bool decomp, const T *X, T *W, uint16_t *codes, T *sc
     template cudaError_t launch_first_point<T>(bool, const T *, T *, uint16_t *, T *, double, int, int,          \
                                                const uint64_t *, uint64_t, const T *, cudaStream_t);             \
     template cudaError_t launch_anchors<T>(bool, const T *, T *, uint16_t *, T *, const T *, const int64_t *,   \
-                                           const int64_t *, const int64_t *, cudaStream_t);
+                                           const int64_t *, const int64_t *, cudaStream_t);                      \
+    template cudaError_t launch_interp_batch<T>(const BatchGroup *, int, const BatchField *, const LevelArgs *,   \
+                                                uint64_t, unsigned long long *, unsigned *, int *, bool, int, int,\
+                                                size_t, cudaStream_t);                                           \
+    template int batch_occupancy<T, false>(int, size_t);                                                         \
+    template cudaError_t launch_minmax_batch<T>(const T *const *, const uint64_t *, int, T *, T *, int,           \
+                                                cudaStream_t);                                                   \
+    template int batch_occupancy<T, true>(int, size_t);
 INST(float)
 INST(double)
 #undef INST

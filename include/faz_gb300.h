@@ -232,6 +232,21 @@ int faz_decompress_payload_device(int N, int dtype, const char *payload, size_t 
  * any stream capture. */
 int faz_resolve_eb_noalloc(faz_config *conf, int dtype, const void *d_data, void *stream);
 
+/* Batched compression of n device-resident fields of uneven shapes (no
+ * counterpart in the reference, which compresses one field per call).  Field
+ * i has configuration confs[i] and data d_data[i] (confs[i].num values of
+ * `dtype`); its stream goes to outs[i] (release each with faz_free) with size
+ * out_sizes[i], byte for byte the stream faz_compress_device writes for it.
+ * One launch resolves every field's error bound; one persistent launch of
+ * `threads` threads per CTA (512, 256 or 128; 0 = 512) runs the first point /
+ * anchor grid and every interpolation level of every ALGO_INTERP field from a
+ * device work queue, a level starting once the field's previous level is
+ * done; Huffman coding, payload and zstd run per field on host threads.
+ * Fields with another cmprAlgo are compressed one by one afterwards.  On
+ * failure no output is returned. */
+int faz_compress_batch(int n, const faz_config *confs, int dtype, const void *const *d_data, void *stream, char **outs,
+                       size_t *out_sizes, int threads, faz_timings *timings);
+
 /* Run the sampled autotune that `conf` selects and stop before compressing:
  * QoZ = 1 runs the QoZ tuner (Tuning, include/QoZ/api/impl/SZInterp.hpp:
  * 1588-2557), cmprAlgo ALGO_INTERP_LORENZO without QoZ the SZ3 tuner
