@@ -53,6 +53,9 @@ def parse():
                          "interp: ALGO_INTERP with --interp")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-sampled autotune comparison")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-fields measurement")
+    ap.add_argument("--batch-fields", type=int, default=32,
+                    help="fields in the batched measurement (the shapes cycle through the four batch shapes)")
     return ap.parse_args()
 
 
@@ -237,6 +240,59 @@ def workload_name(dims, args):
 
 
 # ------------------------------------------------------------------ GPU arm
+BATCH_SHAPES = [(1800, 3600), (721, 1440), (100, 500, 500), (26, 1800, 3600)]
+
+
+def batched_fields(nfields, eb, seed=7):
+    """Uneven fields compressed in one batched call against one call per
+    field: shapes cycle through 2-D 1800x3600, 2-D 721x1440, 3-D 100x500x500
+    and 3-D 26x1800x3600; each a seeded spectral field with slope in [-4, -2],
+    every fourth with 5 % sparse spikes; relative bound `eb`, ALGO_INTERP
+    (cubic).  Inputs stay in HBM; streams (zstd included) come back to the
+    host."""
+    import numpy as np
+    import torch
+    import faz_gb300 as F
+    from faz_gb300.fields import spectral_field
+    rng = np.random.default_rng(seed)
+    confs, xs = [], []
+    for i in range(nfields):
+        dims = BATCH_SHAPES[i % len(BATCH_SHAPES)]
+        x = spectral_field(dims, slope=float(rng.uniform(-4, -2)), noise=0.01, seed=int(rng.integers(1 << 30)),
+                           spikes=0.05 if i % 4 == 3 else 0.0, device="cuda")
+        c = F.Config(*dims)
+        c.cmprAlgo, c.errorBoundMode, c.relErrorBound = F.ALGO_INTERP, F.EB_REL, eb
+        confs.append(c)
+        xs.append(x)
+    nbytes = sum(x.numel() * x.element_size() for x in xs)
+
+    def timed(fn, reps=2):
+        best = None
+        out = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = fn()
+            torch.cuda.synchronize()
+            t = time.perf_counter() - t0
+            best = t if best is None else min(best, t)
+        return best, out
+
+    F.compress_batch(confs[:4], xs[:4])  # warm-up
+    t_batch, sb = timed(lambda: F.compress_batch(confs, xs))
+    tmb = F.last_timings()
+    t_one, so = timed(lambda: [F.compress_device(c, x) for c, x in zip(confs, xs)])
+    assert sb == so, "batched streams differ from single-field streams"
+    return {"fields": nfields, "shapes": [list(d) for d in BATCH_SHAPES], "bytes": nbytes,
+            "batched": {"value": round(nbytes / t_batch / 1e9, 3), "unit": "GB/s", "ms": round(t_batch * 1e3, 2),
+                        "levels_ms": round(tmb["predict_ms"], 2)},
+            "one_call_per_field": {"value": round(nbytes / t_one / 1e9, 3), "unit": "GB/s",
+                                   "ms": round(t_one * 1e3, 2)},
+            "speedup": round(t_one / t_batch, 3),
+            "ratio": round(nbytes / sum(len(s) for s in sb), 3),
+            "identical_streams": True}
+
+
 def learned_vs_sampled(x, dims, eb):
     """The learned tuner against the sampled QoZ autotune, end to end through
     compress_device (tuning + compression + zstd, host clock): on this field
@@ -427,6 +483,7 @@ def main():
                "sample": f"compress of a {shape[0]}x{shape[1]}x{shape[2]} slab of the same field, one thread "
                          f"(decompress {cd:.4f} GB/s)"}
     learned = None if args.no_learned else learned_vs_sampled(x, dims, args.eb)
+    batch = None if args.no_batch else batched_fields(args.batch_fields, args.eb)
     med = lambda k, ph: round(statistics.median(p[k] for p in ph), 4)  # noqa: E731
     line = {
         "metric": METRIC,
@@ -467,6 +524,7 @@ def main():
         "clocks": clocks,
         "cpu_baseline": cpu,
         "learned_tuner": learned,
+        "batch": batch,
         "max_abs_err": err,
     }
     print(json.dumps(line), flush=True)

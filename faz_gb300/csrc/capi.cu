@@ -571,7 +571,7 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
 // Lossless_zstd::compress framing (include/QoZ/lossless/Lossless_zstd.hpp:22-32),
 // then Config::save + int32 trailer size (include/QoZ/api/sz.hpp:77-91).
 void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, char **out, size_t *out_size,
-                   faz_timings &tm, int zthreads = -1) {
+                   faz_timings &tm, bool parallel_frames = true) {
     std::string err;
     const Zstd &z = zstd_lib(err);
     if (!z.ok) throw Fail{FAZ_ERR_ZSTD, err};
@@ -581,14 +581,14 @@ void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, ch
     // FAZ_ZSTD_THREADS (default the host's cores up to 16) cuts a large payload
     // into independent frames compressed in parallel; 0 writes exactly the
     // single frame of ZSTD_compress, as the reference does
-    const int nframes = zstd_frame_count(psize, zthreads >= 0 ? zthreads : zstd_threads());
+    const int nframes = zstd_frame_count(psize, zstd_threads());
     size_t bound = zstd_frames_bound(z, psize, nframes);
     size_t cap = 8 + bound + trailer.size() + 4;
     char *buf = (char *)std::malloc(cap);
     if (!buf) throw Fail{FAZ_ERR_ARG, "out of host memory"};
     uint64_t raw = psize;
     std::memcpy(buf, &raw, 8);
-    size_t zs = zstd_compress_frames(z, (uint8_t *)buf + 8, bound, payload, psize, nframes);
+    size_t zs = zstd_compress_frames(z, (uint8_t *)buf + 8, bound, payload, psize, nframes, parallel_frames);
     if (z.isError(zs)) {
         std::free(buf);
         throw Fail{FAZ_ERR_ZSTD, "ZSTD_compress failed"};
@@ -877,7 +877,8 @@ int compress_batch_impl(int nf, const faz_config *confs, const void *const *d_da
                     interp_payload_tail<T>(c, fw[k].il, fw[k].dl, c.absErrorBound, c.quantbinCnt / 2, fw[k].p.num,
                                            fw[k].codes, fw[k].scratch, nullptr, m2, s2.st, c2, tms[k], nullptr,
                                            payload, psize);
-                    finish_stream(c, payload, psize, &outs[fw[k].idx], &out_sizes[fw[k].idx], tms[k], 0);
+                    // the same frames as a single-field call, compressed on this thread
+                    finish_stream(c, payload, psize, &outs[fw[k].idx], &out_sizes[fw[k].idx], tms[k], false);
                     nl[k] = c2.n;
                 } catch (const Fail &f) {
                     codes_rc[k] = f.code;

@@ -174,7 +174,8 @@ struct Zstd {
 // exactly ZSTD_compress.  ZSTD_decompress decodes the concatenation.
 int zstd_frame_count(size_t n, int threads);
 size_t zstd_frames_bound(const Zstd &z, size_t n, int nframes);
-size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes);
+size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes,
+                            bool parallel = true);
 // Decodes one or more concatenated frames (independent frames in parallel).
 size_t zstd_decompress_frames(const Zstd &z, uint8_t *dst, size_t raw, const uint8_t *src, size_t n, int threads);
 int zstd_threads();  // FAZ_ZSTD_THREADS, default the host's cores up to 16

@@ -418,7 +418,8 @@ size_t zstd_frames_bound(const Zstd &z, size_t n, int nframes) {
     return b;
 }
 
-size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes) {
+size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes,
+                            bool parallel) {
     if (nframes <= 1) return z.compress(dst, cap, src, n, 3);
     const size_t slice = (n + nframes - 1) / nframes;
     struct Part {
@@ -431,6 +432,10 @@ size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8
         parts[i].len = std::min(n, parts[i].lo + slice) - parts[i].lo;
     }
     auto each = [&](auto &&fn) {
+        if (!parallel) {
+            for (int i = 0; i < nframes; i++) fn(i);
+            return;
+        }
         std::vector<std::thread> pool;
         for (int i = 0; i < nframes; i++) pool.emplace_back(fn, i);
         for (auto &t : pool) t.join();

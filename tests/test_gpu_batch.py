@@ -99,3 +99,15 @@ def test_gpu_batch_rejects_mismatched_input():
     x = torch.zeros(10, device="cuda")
     with pytest.raises(ValueError):
         F.compress_batch([_conf((11,))], [x])
+
+
+def test_gpu_batch_writes_the_same_zstd_frames(monkeypatch):
+    """With several zstd frames per stream the batch writes the frames a
+    single-field call writes."""
+    monkeypatch.setenv("FAZ_ZSTD_THREADS", "8")
+    big = spectral_field((128, 256, 256), slope=-3.0, noise=0.01, seed=5, device="cuda")
+    small = spectral_field((40, 50, 60), slope=-3.0, seed=6, device="cuda")
+    confs = [_conf((128, 256, 256), rel=1e-4), _conf((40, 50, 60))]
+    streams = F.compress_batch(confs, [big, small])
+    assert streams[0] == F.compress_device(confs[0], big)
+    assert streams[1] == F.compress_device(confs[1], small)
