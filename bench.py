@@ -9,7 +9,7 @@ field; decompression is timed the same way and reported beside it.
   value       compress GB/s (input bytes / time) with the field resident in
               HBM, through the GPU path up to the pre-zstd payload in host
               memory (CUDA events on the call's stream).
-  e2e         compress GB/s through SZ_compress (host input in pinned
+  e2e         compress GB/s through faz_compress, the C ABI (host input in pinned
               memory, host->device copy, GPU path, payload copy back, host
               zstd, trailer), host clock.
   roofline    the finest interpolation level kernel (the dominant kernel):
@@ -426,28 +426,55 @@ def main():
     err = (out.double() - x.double()).abs().max().item()
     assert err <= conf_out.absErrorBound, (err, conf_out.absErrorBound)
 
-    # ---- end to end through the public API with host buffers
+    # ---- end to end through the C ABI with host buffers (faz_compress /
+    # faz_decompress: the calls a binding of the reference's SZ_compress /
+    # SZ_decompress makes), host clock
+    import ctypes
+    L = F.library()
     host_in = torch.empty(dims, dtype=torch.float32, pin_memory=True)
     host_in.copy_(x.cpu())
     host_np = host_in.numpy()
     host_out = torch.empty(dims, dtype=torch.float32, pin_memory=True).numpy().reshape(-1)
+    cs = conf.to_struct()
+    tmc = F.FazTimings()
+
+    def c_compress():
+        out, osz = ctypes.c_void_p(), ctypes.c_size_t()
+        F.api._check(L.faz_compress(ctypes.byref(cs), F.FAZ_FLOAT, host_np.ctypes.data, ctypes.byref(out),
+                                    ctypes.byref(osz), ctypes.byref(tmc)))
+        return out, osz.value
+
+    def c_decompress(buf, size):
+        ds = F.FazConfigStruct()
+        ds.num = host_out.size
+        ptr = ctypes.c_void_p(host_out.ctypes.data)
+        F.api._check(L.faz_decompress(ctypes.byref(ds), F.FAZ_FLOAT, buf, size, ctypes.byref(ptr),
+                                      ctypes.byref(tmc)))
+
     for _ in range(max(1, args.warmup // 2)):
-        s = F.SZ_compress(conf, host_np)
-        F.SZ_decompress(None, s, out=host_out)
+        o, n_o = c_compress()
+        c_decompress(o, n_o)
+        L.faz_free(o)
     barrier()
     e2e_c, e2e_d, zc, zd, d2h_bytes = [], [], [], [], 0
+    e2e_parts = []
+    stream_len = 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        s = F.SZ_compress(conf, host_np)
+        o, n_o = c_compress()
         e2e_c.append(time.perf_counter() - t0)
-        tm = F.last_timings()
-        zc.append(tm["zstd_ms"])
-        d2h_bytes = tm["payload_bytes"]
+        zc.append(tmc.zstd_ms)
+        e2e_parts.append({"h2d_ms": tmc.h2d_ms, "gpu_ms": tmc.gpu_ms, "zstd_ms": tmc.zstd_ms,
+                          "call_ms": tmc.total_ms})
+        d2h_bytes = tmc.payload_bytes
+        stream_len = n_o
         t0 = time.perf_counter()
-        dec, _ = F.SZ_decompress(None, s, out=host_out)
+        c_decompress(o, n_o)
         e2e_d.append(time.perf_counter() - t0)
-        zd.append(F.last_timings()["zstd_ms"])
-    ratio = nbytes / len(s)
+        zd.append(tmc.zstd_ms)
+        L.faz_free(o)
+    ratio = nbytes / stream_len
+    dec = host_out.reshape(dims)
     assert np.abs(dec.astype(np.float64) - host_np.astype(np.float64)).max() <= conf_out.absErrorBound
 
     # ---- max over ranks
@@ -512,7 +539,10 @@ def main():
         "e2e": {"value": round(world * nbytes / te2e_c / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": int(d2h_bytes), "ms_per_step": round(te2e_c * 1e3, 3),
                 "zstd_ms_compress": round(statistics.median(zc), 3),
-                "zstd_ms_decompress": round(statistics.median(zd), 3)},
+                "zstd_ms_decompress": round(statistics.median(zd), 3),
+                "api": "faz_compress / faz_decompress (C ABI, host buffers in pinned memory)",
+                "compress_parts_ms": {k: round(statistics.median(p[k] for p in e2e_parts), 3)
+                                      for k in ("h2d_ms", "gpu_ms", "zstd_ms", "call_ms")}},
         "roofline": roof,
         "phases_ms": {"compress": {k: med(k, phases) for k in ("tune_ms", "predict_ms", "finest_level_ms",
                                                                "huffman_ms", "host_ms", "gpu_ms")},

@@ -302,7 +302,8 @@ struct Sink {
 // (HuffmanEncoder::preprocess_encode + encode, HuffmanEncoder.hpp:93-227).
 // `center` is the code the histogram's shared-memory window is centred on.
 void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
-                           Counter &launches, HuffEncoded &h, faz_timings &tm) {
+                           Counter &launches, HuffEncoded &h, faz_timings &tm,
+                           const std::function<void(const HuffEncoded &)> &sized) {
     const uint64_t nsub = hist_subchunks(n);
     const int nsym = 65536;
     unsigned long long *hist = m.alloc<unsigned long long>(nsym);
@@ -347,16 +348,17 @@ void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem
     CK(cudaMemcpyAsync(dcode, cb.code.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dpacked, packed.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dlen, cb.len.data(), cb.stateNum, cudaMemcpyHostToDevice, st));
+    // the encoded size from the counts and code lengths (what the device's
+    // chunk scan adds up)
+    uint64_t total_bits = 0;
+    for (size_t i = 0; i < syms.size(); i++) total_bits += cnts[i] * (uint64_t)cb.len[syms[i] - cb.offset];
+    h.nbytes = (total_bits + 7) / 8;
+    if (sized) sized(h);
     const uint64_t nech = encode_chunks(n);
     unsigned long long *cbits = m.alloc<unsigned long long>(nech + 1);
     unsigned long long *coff = m.alloc<unsigned long long>(nech + 1);
     launches(launch_encode_bits(codes, n, cb.offset, dlen, cbits, st));
     launches(launch_scan_u64(cbits, coff, nech, stmp, st));
-    uint64_t total_bits;
-    CK(cudaMemcpyAsync(hb, coff + nech, 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    std::memcpy(&total_bits, hb, 8);
-    h.nbytes = (total_bits + 7) / 8;
     const uint64_t nwords = (total_bits + 31) / 32 + 1;
     h.bits = m.alloc<uint32_t>(nwords);
     CK(cudaMemsetAsync(h.bits, 0, nwords * 4, st));

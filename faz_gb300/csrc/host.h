@@ -316,8 +316,11 @@ struct HuffEncoded {
     uint64_t nzero = 0;        // codes equal to 0 (unpredictable points)
     unsigned long long *zc = nullptr, *zoff = nullptr;  // zero counts per sub-chunk and their exclusive scan
 };
+// `sized`, when given, runs as soon as the codebook, the zero count and the
+// encoded size are known on the host (before the encoding kernels finish).
 void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
-                           Counter &launches, HuffEncoded &h, faz_timings &tm);
+                           Counter &launches, HuffEncoded &h, faz_timings &tm,
+                           const std::function<void(const HuffEncoded &)> &sized = {});
 void append_tree(std::vector<uint8_t> &o, const Codebook &cb, uint64_t nbytes);
 void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, uint16_t *codes, DevMem &m,
                            cudaStream_t st, Counter &launches);

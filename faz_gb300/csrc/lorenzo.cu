@@ -31,6 +31,7 @@ namespace {
 
 constexpr int kLorWarps = 8;     // blocks (warps) per CTA
 constexpr int kLorMaxBs = 8;     // largest block edge on the GPU path
+constexpr int kLorBatch = 8;     // tile loads in flight per lane
 
 struct LorArgs {
     int64_t d1, d2, d3;   // field dims, slowest first
@@ -214,18 +215,34 @@ __global__ void __launch_bounds__(kLorWarps * 32)
     T *t = reinterpret_cast<T *>(lor_smem) + (size_t)w * (size_t)tstride;
     T *xs = t + (bs + 2) * (bs + 2) * (bs + 2);
     const int tn = (sx + 2) * (sy + 2) * tz;
-    for (int e = lane; e < tn; e += 32) {
-        const int i = e / tx, r = e - i * tx, j = r / tz, k = r - j * tz;
-        const int64_t gx = x0 + i - 2, gy = y0 + j - 2, gz = z0 + k - 2;
-        T v = 0;
-        const bool inside = i >= 2 && j >= 2 && k >= 2;
-        if (!inside && gx >= 0 && gy >= 0 && gz >= 0) v = R[gx * d0 + gy * dd1 + gz];
-        t[e] = v;
+    // loads in batches of kLorBatch per lane, all issued before any is used
+    for (int e0 = lane; e0 < tn; e0 += 32 * kLorBatch) {
+        T v[kLorBatch];
+#pragma unroll
+        for (int u = 0; u < kLorBatch; u++) {
+            const int e = e0 + 32 * u;
+            const int i = e / tx, r = e - i * tx, j = r / tz, k = r - j * tz;
+            const int64_t gx = x0 + i - 2, gy = y0 + j - 2, gz = z0 + k - 2;
+            const bool inside = i >= 2 && j >= 2 && k >= 2;
+            v[u] = (e < tn && !inside && gx >= 0 && gy >= 0 && gz >= 0) ? R[gx * d0 + gy * dd1 + gz] : (T)0;
+        }
+#pragma unroll
+        for (int u = 0; u < kLorBatch; u++)
+            if (e0 + 32 * u < tn) t[e0 + 32 * u] = v[u];
     }
     if (!DECOMP) {
-        for (int e = lane; e < sx * sy * sz; e += 32) {
-            const int i = e / (sy * sz), r = e - i * sy * sz, j = r / sz, k = r - j * sz;
-            xs[e] = X[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)];
+        const int nv = sx * sy * sz;
+        for (int e0 = lane; e0 < nv; e0 += 32 * kLorBatch) {
+            T v[kLorBatch];
+#pragma unroll
+            for (int u = 0; u < kLorBatch; u++) {
+                const int e = e0 + 32 * u;
+                const int i = e / (sy * sz), r = e - i * sy * sz, j = r / sz, k = r - j * sz;
+                v[u] = e < nv ? X[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)] : (T)0;
+            }
+#pragma unroll
+            for (int u = 0; u < kLorBatch; u++)
+                if (e0 + 32 * u < nv) xs[e0 + 32 * u] = v[u];
         }
     }
     __syncwarp();

@@ -170,7 +170,8 @@ size_t zstd_framed_size(const uint8_t *p, size_t n) {
 // tile the sample exactly).
 template <typename T>
 void block_interp_payload(int N, const uint64_t *sdims, const T *dS, double eb, int cubic, int dir, int64_t bs,
-                          cudaStream_t st, Counter &launches, faz_timings &tm, std::vector<uint8_t> &pl) {
+                          cudaStream_t st, Counter &launches, faz_timings &tm, std::vector<uint8_t> &pl,
+                          const std::function<void(size_t)> &report = {}) {
     uint64_t num = 1;
     for (int i = 0; i < N; i++) {
         num *= sdims[i];
@@ -262,7 +263,15 @@ void block_interp_payload(int N, const uint64_t *sdims, const T *dS, double eb, 
     }
     if (off != bc) throw Fail{FAZ_ERR_DEVICE, "block interpolation did not cover its blocks"};
     HuffEncoded hc;
-    huffman_encode_device(codes, num, 32768, m, st, launches, hc, tm);
+    // the payload's size is known once the codebook is: report it before the
+    // encoding kernels and copies finish
+    auto sized = [&](const HuffEncoded &e) {
+        if (!report) return;
+        const size_t head = (size_t)N * 8 + 4 + 4 + 4 + 1 + 8 + 4 + 8;
+        const size_t tree = 4 + 4 + 4 + e.cb.tree.size() + 8;
+        report(head + e.nzero * sizeof(T) + tree + e.nbytes);
+    };
+    huffman_encode_device(codes, num, 32768, m, st, launches, hc, tm, sized);
     const uint64_t nunpred = hc.nzero;
     T *unp = m.alloc<T>(nunpred ? nunpred : 1);
     if (nunpred) launches(launch_compact_zeros<T>(codes, num, hc.zc, hc.zoff, nullptr, scratch, unp, st));
@@ -309,6 +318,15 @@ struct Trial {
     void start(cudaEvent_t ready, F body) {
         size = std::async(std::launch::async, [this, ready, body]() -> size_t {
             std::vector<uint8_t> pl;
+            bool reported = false;
+            size_t early = 0;
+            auto report = [&](size_t n) {
+                if (reported) return;
+                reported = true;
+                early = n;
+                raw.set_value(n);
+                if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s size %zu bytes\n", ms_since(t0), name, n);
+            };
             try {
                 // the trials gate the tuner's decision: they take SMs ahead of
                 // the overlapped compression
@@ -317,14 +335,16 @@ struct Trial {
                 Counter c;
                 faz_timings t;
                 std::memset(&t, 0, sizeof(t));
-                body(sg.st, c, t, pl);
+                body(sg.st, c, t, pl, std::function<void(size_t)>(report));
                 launches = c.n;
                 host_ms = t.host_ms;
             } catch (...) {
-                raw.set_exception(std::current_exception());
+                if (!reported) raw.set_exception(std::current_exception());
                 throw;
             }
-            raw.set_value(pl.size());
+            if (reported && early != pl.size())
+                throw Fail{FAZ_ERR_DEVICE, "a trial's reported size differs from its payload"};
+            report(pl.size());
             if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s payload %zu bytes\n", ms_since(t0), name, pl.size());
             const size_t z = zstd_framed_size(pl.data(), pl.size());
             if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s zstd %zu bytes\n", ms_since(t0), name, z);
@@ -491,17 +511,20 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     jd[0].name = "linear-dir5";
     jd[1].name = "cubic-dir5";
     for (Trial *t : {&jl, &ji[0], &ji[1], &jd[0], &jd[1]}) t->t0 = tt0;
-    jl.start(ready.a, [&](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
+    jl.start(ready.a, [&](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
+                          const std::function<void(size_t)> &) {
         if (N == 3) lorenzo_payload<T>(sdims, dS, 5, 3, eb, c.quantbinCnt / 2, s2, c2, t2, pl);
         else gen_compress_payload<T>(N, sdims, 5, 1, 1, eb, c.quantbinCnt / 2, dS, s2, c2, t2, pl);
     });
     const int dir0 = c.interpDirection;
     for (int op = 0; op < 2; op++) {
-        ji[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
-            block_interp_payload<T>(N, sdims, dS, eb, op, dir0, (int64_t)sb, s2, c2, t2, pl);
+        ji[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
+                                      const std::function<void(size_t)> &rep) {
+            block_interp_payload<T>(N, sdims, dS, eb, op, dir0, (int64_t)sb, s2, c2, t2, pl, rep);
         });
-        jd[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl) {
-            block_interp_payload<T>(N, sdims, dS, eb, op, dop, (int64_t)sb, s2, c2, t2, pl);
+        jd[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
+                                      const std::function<void(size_t)> &rep) {
+            block_interp_payload<T>(N, sdims, dS, eb, op, dop, (int64_t)sb, s2, c2, t2, pl, rep);
         });
     }
     // While the Lorenzo trial and the zstd sizes are computed, compress the
