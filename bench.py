@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-sampled autotune comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-fields measurement")
+    ap.add_argument("--no-combined", action="store_true", help="skip the combined f64 learned + batched workload")
+    ap.add_argument("--combined-fields", type=int, default=8,
+                    help="float64 256x384x384 fields per bound in the combined workload")
     ap.add_argument("--batch-fields", type=int, default=32,
                     help="fields in the batched measurement (the shapes cycle through the four batch shapes)")
     return ap.parse_args()
@@ -293,6 +296,62 @@ def batched_fields(nfields, eb, seed=7):
             "identical_streams": True}
 
 
+def combined_f64(nfields, rels=(1e-4, 1e-6), seed=11):
+    """float64 256x384x384 fields (spectral k^-3 plus a smooth Gaussian-bump
+    background, seeded): configurations from the learned tuner (the plain QoZ
+    tuner where it falls back), all fields compressed in one batched call, every
+    output checked in FP64 against its field's bound; against the plain path
+    (QoZ tuner + compression, one call per field)."""
+    import numpy as np
+    import torch
+    import faz_gb300 as F
+    import faz_gb300.learned as L
+    from faz_gb300.fields import spectral_field
+    if not os.path.exists(L.DEFAULT_MODEL):
+        return None
+    model = L.TunerModel.load()
+    dims = (256, 384, 384)
+    rng = np.random.default_rng(seed)
+    out = {"fields_per_bound": nfields, "dims": list(dims), "dtype": "f64"}
+    for rel in rels:
+        xs = [spectral_field(dims, slope=-3.0, noise=0.0, bumps=3, seed=int(rng.integers(1 << 30)),
+                             dtype=np.float64, device="cuda") for _ in range(nfields)]
+        nbytes = sum(x.numel() * 8 for x in xs)
+        qcs = [L.qoz_conf(dims, rel) for _ in xs]
+        F.compress_device(qcs[0], xs[0])  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plain = [F.compress_device(c, x) for c, x in zip(qcs, xs)]
+        torch.cuda.synchronize()
+        t_plain = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        tuned, fallback = [], 0
+        for c, x in zip(qcs, xs):
+            tc, info = L.learned_tune(c, x, model, min_confidence=0.5)
+            tuned.append(tc)
+            fallback += info["used_plain"] != 0
+        streams = F.compress_batch(tuned, xs)
+        torch.cuda.synchronize()
+        t_learn = time.perf_counter() - t0
+        worst = 0.0
+        for s, x in zip(streams, xs):
+            y = torch.empty_like(x)
+            c2 = F.decompress_device(s, y)
+            err = (y - x).abs().max().item()
+            assert err <= c2.absErrorBound, (err, c2.absErrorBound)
+            worst = max(worst, err / c2.absErrorBound)
+        out[f"rel_{rel:g}"] = {
+            "plain_qoz_one_call_per_field": {"ms": round(t_plain * 1e3, 1), "GB_s": round(nbytes / t_plain / 1e9, 3),
+                                             "ratio": round(nbytes / sum(len(s) for s in plain), 4)},
+            "learned_configs_batched": {"ms": round(t_learn * 1e3, 1), "GB_s": round(nbytes / t_learn / 1e9, 3),
+                                        "ratio": round(nbytes / sum(len(s) for s in streams), 4),
+                                        "fallback_fields": fallback},
+            "speedup": round(t_plain / t_learn, 3),
+            "max_err_over_bound": round(worst, 6)}
+        del xs
+    return out
+
+
 def learned_vs_sampled(x, dims, eb):
     """The learned tuner against the sampled QoZ autotune, end to end through
     compress_device (tuning + compression + zstd, host clock): on this field
@@ -511,6 +570,7 @@ def main():
                          f"(decompress {cd:.4f} GB/s)"}
     learned = None if args.no_learned else learned_vs_sampled(x, dims, args.eb)
     batch = None if args.no_batch else batched_fields(args.batch_fields, args.eb)
+    combined = None if args.no_combined else combined_f64(args.combined_fields)
     med = lambda k, ph: round(statistics.median(p[k] for p in ph), 4)  # noqa: E731
     line = {
         "metric": METRIC,
@@ -555,6 +615,7 @@ def main():
         "cpu_baseline": cpu,
         "learned_tuner": learned,
         "batch": batch,
+        "combined_f64": combined,
         "max_abs_err": err,
     }
     print(json.dumps(line), flush=True)

@@ -30,9 +30,26 @@ def _spectral_numpy(shape, slope, aniso, seed):
     return field, rng
 
 
+def _bumps(shape, rng_uniform, count, xp):
+    """Sum of `count` smooth Gaussian bumps on the unit cube of `shape`, with
+    centres, widths (0.1..0.3 of the extent) and signed amplitudes (0.5..2)
+    drawn from rng_uniform(lo, hi, n)."""
+    grids = xp.meshgrid(*[xp.linspace(0.0, 1.0, n) for n in shape], indexing="ij")
+    out = 0.0
+    for _ in range(count):
+        c = rng_uniform(0.0, 1.0, len(shape))
+        w = float(rng_uniform(0.1, 0.3, 1)[0])
+        a = float(rng_uniform(0.5, 2.0, 1)[0]) * (1 if rng_uniform(0.0, 1.0, 1)[0] < 0.5 else -1)
+        r2 = sum((g - float(ci)) ** 2 for g, ci in zip(grids, c))
+        out = out + a * xp.exp(-r2 / (2 * w * w))
+    return out
+
+
 def spectral_field(shape, slope=-3.0, aniso=None, noise=0.01, seed=0, lo=-50.0, hi=80.0,
-                   spikes=0.0, piecewise=0, dtype=np.float32, device=None):
-    """Seeded field of `shape` (slowest axis first).
+                   spikes=0.0, piecewise=0, bumps=0, dtype=np.float32, device=None):
+    """Seeded field of `shape` (slowest axis first).  `bumps` > 0 adds that many
+    smooth Gaussian bumps as a background, at three times the spectral part's
+    standard deviation.
 
     device=None builds on the CPU with numpy; a torch device string builds it
     there with torch.fft (used for the large benchmark fields).
@@ -40,9 +57,11 @@ def spectral_field(shape, slope=-3.0, aniso=None, noise=0.01, seed=0, lo=-50.0, 
     shape = tuple(int(s) for s in shape)
     aniso = tuple(aniso) if aniso is not None else (1.0,) * len(shape)
     if device is not None:
-        return _spectral_torch(shape, slope, aniso, noise, seed, lo, hi, spikes, piecewise, dtype, device)
+        return _spectral_torch(shape, slope, aniso, noise, seed, lo, hi, spikes, piecewise, dtype, device, bumps)
     field, rng = _spectral_numpy(shape, slope, aniso, seed)
     sd = field.std()
+    if bumps > 0:
+        field = field + 3 * sd * _bumps(shape, lambda a, b, n: rng.uniform(a, b, n), bumps, np)
     if noise > 0:
         field = field + rng.standard_normal(shape) * (noise * sd)
     if piecewise > 0:
@@ -70,7 +89,7 @@ def _piecewise(field, rng, regions):
     return out
 
 
-def _spectral_torch(shape, slope, aniso, noise, seed, lo, hi, spikes, piecewise, dtype, device):
+def _spectral_torch(shape, slope, aniso, noise, seed, lo, hi, spikes, piecewise, dtype, device, bumps=0):
     import torch
     g = torch.Generator(device=device).manual_seed(int(seed))
     white = torch.randn(shape, generator=g, device=device, dtype=torch.float32)
@@ -96,6 +115,18 @@ def _spectral_torch(shape, slope, aniso, noise, seed, lo, hi, spikes, piecewise,
     field = torch.fft.irfftn(spec, s=shape)
     del spec
     sd = field.std()
+    if bumps > 0:
+        def uni(a, b, n):
+            return (torch.rand(n, generator=g, device=device) * (b - a) + a).cpu().numpy()
+
+        class _TorchNs:
+            meshgrid = staticmethod(torch.meshgrid)
+            exp = staticmethod(torch.exp)
+
+            @staticmethod
+            def linspace(a, b, n):
+                return torch.linspace(a, b, n, device=device)
+        field.add_(_bumps(shape, uni, bumps, _TorchNs) * (3 * sd))
     if noise > 0:
         field.add_(torch.randn(shape, generator=g, device=device) * (noise * sd))
     for _ in range(int(piecewise)):
