@@ -90,10 +90,12 @@ __device__ __forceinline__ Stencil<T> make_stencil(int m, int n, int cubic, int 
 }
 
 
-template <typename T>
+// CUB = 0: a linear level, whose stencils are copy, (a + b) / 2 or linear1
+template <int CUB, typename T>
 __device__ __forceinline__ T eval_stencil(const Stencil<T> &S, const T *p) {
     T x1 = p[S.i1], x2 = p[S.i2];
     if (S.nt == 5) return linear1_any(x1, x2);
+    if (!CUB) return S.nt == 1 ? x1 : (x1 + x2) * S.scale;
     T x3 = p[S.i3], x4 = p[S.i4];
     T s2 = S.k1 * x1 + S.k2 * x2;
     T s3 = s2 + S.k3 * x3;
@@ -163,7 +165,7 @@ __device__ __forceinline__ uint64_t owner_pos_sweep2(const LevelArgs &a, const B
 // COH: coarse values come from W through L2 (ld.global.cg) instead of
 // cp.async (which may hit L1): in the batched launch other SMs write W during
 // the launch, and L1 is not coherent.
-template <typename T, bool DECOMP, bool WIDE, int QM, bool COH>
+template <typename T, bool DECOMP, bool WIDE, int QM, bool COH, int CUB>
 __device__ __forceinline__ void level_block(const LevelArgs &a, const int64_t bid, const T *__restrict__ X,
                                             T *__restrict__ W, uint16_t *__restrict__ codes,
                                             T *__restrict__ scratch, const uint64_t *__restrict__ zpos, uint64_t nz,
@@ -241,7 +243,7 @@ __device__ __forceinline__ void level_block(const LevelArgs &a, const int64_t bi
             const int col = 2 * e1 * h2 + e2;
             const bool emit = act && e1 >= k1 && e2 >= k2;
             const int rank = ((e1 - k1) * g.ne2 + (e2 - k2)) * g.t0 + rk;
-            const T pred = eval_stencil(S, V + col);
+            const T pred = eval_stencil<CUB>(S, V + col);
             const int idx = m0 * st + col;
             const Off gi = gl + (Off)(2 * e1) * G1 + (Off)(2 * e2) * G2;
             if (!DECOMP) {
@@ -304,7 +306,7 @@ __device__ __forceinline__ void level_block(const LevelArgs &a, const int64_t bi
             const int col = m0 * n1 * h2 + e2;
             const bool emit = act && e2 >= k2;
             const int rank = (q * g.ne2 + (e2 - k2)) * g.t1 + rk;
-            const T pred = eval_stencil(S, V + col);
+            const T pred = eval_stencil<CUB>(S, V + col);
             const int idx = col + m1 * h2;
             const Off gi = (Off)m0 * G0 + gl + (Off)(2 * e2) * G2;
             if (!DECOMP) {
@@ -380,7 +382,7 @@ __device__ __forceinline__ void level_block(const LevelArgs &a, const int64_t bi
             }
             const int q0 = lc.outer, q1 = lc.inner;
             const T *row = V + ((k0 + q0) * n1 + (k1 + q1)) * h2;
-            const T pred = eval_stencil(S, row);
+            const T pred = eval_stencil<CUB>(S, row);
             const int rank = l * g.t2 + rk;
             const Off gi = gl + (Off)q0 * G0 + (Off)q1 * G1;
             if (!DECOMP) {
@@ -401,13 +403,13 @@ __device__ __forceinline__ void level_block(const LevelArgs &a, const int64_t bi
     }
 }
 
-template <typename T, bool DECOMP, bool WIDE, int QM>
+template <typename T, bool DECOMP, bool WIDE, int QM, int CUB>
 __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *__restrict__ X, T *__restrict__ W,
                                                       uint16_t *__restrict__ codes, T *__restrict__ scratch,
                                                       const uint64_t *__restrict__ zpos, uint64_t nz,
                                                       const T *__restrict__ unpred) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    level_block<T, DECOMP, WIDE, QM, false>(a, blockIdx.x, X, W, codes, scratch, zpos, nz, unpred, smem_raw);
+    level_block<T, DECOMP, WIDE, QM, false, CUB>(a, blockIdx.x, X, W, codes, scratch, zpos, nz, unpred, smem_raw);
 }
 
 // ------------------------------------------------------ batched launch
@@ -495,12 +497,18 @@ __global__ void __launch_bounds__(512, 2)
             }
         } else {
             const bool straight = sizeof(T) == 4 && s_a.fast && s_a.trim == 0;
-            if (straight)
-                level_block<T, false, WIDE, 1, true>(s_a, s_local, X, W, f.codes, scratch, nullptr, 0, nullptr,
-                                                     smem_raw);
+            if (straight && s_a.cubic)
+                level_block<T, false, WIDE, 1, true, 1>(s_a, s_local, X, W, f.codes, scratch, nullptr, 0, nullptr,
+                                                        smem_raw);
+            else if (straight)
+                level_block<T, false, WIDE, 1, true, 0>(s_a, s_local, X, W, f.codes, scratch, nullptr, 0, nullptr,
+                                                        smem_raw);
+            else if (s_a.cubic)
+                level_block<T, false, WIDE, 0, true, 1>(s_a, s_local, X, W, f.codes, scratch, nullptr, 0, nullptr,
+                                                        smem_raw);
             else
-                level_block<T, false, WIDE, 0, true>(s_a, s_local, X, W, f.codes, scratch, nullptr, 0, nullptr,
-                                                     smem_raw);
+                level_block<T, false, WIDE, 0, true, 0>(s_a, s_local, X, W, f.codes, scratch, nullptr, 0, nullptr,
+                                                        smem_raw);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -674,13 +682,20 @@ cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const
     const bool wide = a.dims[0] * a.dims[1] * a.dims[2] >= ((int64_t)1 << 31);
     const bool straight = sizeof(T) == 4 && a.fast && a.trim == 0;
     void (*k)(LevelArgs, const T *, T *, uint16_t *, T *, const uint64_t *, uint64_t, const T *);
-    if (straight) {
-        if (!decomp) k = wide ? k_interp_level<T, false, true, 1> : k_interp_level<T, false, false, 1>;
-        else k = wide ? k_interp_level<T, true, true, 1> : k_interp_level<T, true, false, 1>;
-    } else {
-        if (!decomp) k = wide ? k_interp_level<T, false, true, 0> : k_interp_level<T, false, false, 0>;
-        else k = wide ? k_interp_level<T, true, true, 0> : k_interp_level<T, true, false, 0>;
+#define FAZ_PICK(CUB)                                                                                            \
+    if (straight) {                                                                                              \
+        if (!decomp) k = wide ? k_interp_level<T, false, true, 1, CUB> : k_interp_level<T, false, false, 1, CUB>; \
+        else k = wide ? k_interp_level<T, true, true, 1, CUB> : k_interp_level<T, true, false, 1, CUB>;          \
+    } else {                                                                                                     \
+        if (!decomp) k = wide ? k_interp_level<T, false, true, 0, CUB> : k_interp_level<T, false, false, 0, CUB>; \
+        else k = wide ? k_interp_level<T, true, true, 0, CUB> : k_interp_level<T, true, false, 0, CUB>;          \
     }
+    if (a.cubic) {
+        FAZ_PICK(1)
+    } else {
+        FAZ_PICK(0)
+    }
+#undef FAZ_PICK
     cudaError_t e = allow_dynamic_smem((const void *)k);
     if (e != cudaSuccess) return e;
     k<<<(unsigned)nblocks, threads, sm, st>>>(a, X, W, codes, scratch, zpos, nz, unpred);
