@@ -107,12 +107,44 @@ __global__ void __launch_bounds__(1024) k_compact_zeros(const uint16_t *__restri
     uint64_t s1 = s0 + HSUB;
     if (s1 > n) s1 = n;
     unsigned long long run = zoff[sub];
-    for (uint64_t b = s0; b < s1; b += 32) {
-        uint64_t i = b + lane;
-        bool z = i < s1 && codes[i] == 0;
-        unsigned int bal = __ballot_sync(0xffffffffu, z);
+    // 256 codes per warp step: lane L reads codes [b + 8L, b + 8L + 8) with one
+    // 16-byte load (s0 is a multiple of 8192 and codes is 256-byte aligned),
+    // so the zeros of a step come in stream order lane by lane
+    uint64_t b = s0;
+    for (; b + 256 <= s1; b += 256) {
+        const uint4 q = *reinterpret_cast<const uint4 *>(codes + b + 8 * lane);
+        const uint32_t wd[4] = {q.x, q.y, q.z, q.w};
+        unsigned int m = 0;  // bit k: code b + 8 lane + k is zero
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            m |= (wd[k] & 0xffffu) == 0 ? 1u << (2 * k) : 0u;
+            m |= (wd[k] >> 16) == 0 ? 1u << (2 * k + 1) : 0u;
+        }
+        const int c = __popc(m);
+        int x = c;  // inclusive scan of the counts across lanes
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, x, 31);
+        unsigned long long o = run + (unsigned long long)(x - c);
+        while (m) {
+            const int k = __ffs(m) - 1;
+            m &= m - 1;
+            const uint64_t i = b + 8 * lane + k;
+            if (zpos) zpos[o] = i;
+            if (vals) vals[o] = scratch[i];
+            o++;
+        }
+        run += (unsigned long long)total;
+    }
+    for (; b < s1; b += 32) {
+        const uint64_t i = b + lane;
+        const bool z = i < s1 && codes[i] == 0;
+        const unsigned int bal = __ballot_sync(0xffffffffu, z);
         if (z) {
-            unsigned long long o = run + __popc(bal & ((1u << lane) - 1));
+            const unsigned long long o = run + __popc(bal & ((1u << lane) - 1));
             if (zpos) zpos[o] = i;
             if (vals) vals[o] = scratch[i];
         }
