@@ -282,3 +282,18 @@ def test_gpu_parallel_zstd_frames_hold_the_same_payload(monkeypatch):
         out = torch.empty(dims, dtype=torch.float32, device="cuda")
         F.decompress_device(s8, out)
         assert np.array_equal(out.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+
+
+def test_gpu_c1_full_size_matches_oracle():
+    """The CPU-runnable configuration at full size (100x500x500, cubic, REL
+    1e-3): the GPU payload and decompressed array equal the oracle's, which
+    test_c1_reference.py pins to the reference tool."""
+    from test_c1_reference import c1_conf, c1_field
+    x = c1_field()
+    stream = F.SZ_compress(c1_conf(), x)
+    ref, ref_payload = O.compress(c1_conf(), x)
+    assert payload_of(stream) == ref_payload
+    dec, c2 = F.SZ_decompress(None, stream)
+    ref_dec, _ = O.decompress(ref)
+    assert np.array_equal(dec.reshape(-1).view(np.uint32), ref_dec.reshape(-1).view(np.uint32))
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
