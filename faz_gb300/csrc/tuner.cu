@@ -74,12 +74,25 @@ struct BiSweep {
 };
 
 // block_interpolation_1d targets (SZBlockInterpolationCompressor.hpp:204-280):
-// odd indices in increasing order, one thread each.
+// odd indices in increasing order, one thread each.  The four
+// block-interpolation trials (linear / cubic, two directions) run in the same
+// launches: blockIdx.y picks the trial, each with its own copy of the sample,
+// codes and sweep geometry.
+constexpr int kBiTrials = 4;
+template <typename T>
+struct BiTrials {
+    BiSweep w[kBiTrials];
+    T *data[kBiTrials];
+    uint16_t *codes[kBiTrials];
+    T *scratch[kBiTrials];
+};
+
 template <typename T, int QM>
-__global__ void k_bi_sweep(BiSweep w, LevelArgs q, T *__restrict__ data, uint16_t *__restrict__ codes,
-                           T *__restrict__ scratch, uint64_t total) {
+__global__ void k_bi_sweep4(BiTrials<T> b, LevelArgs q, uint64_t total) {
+    const int v = blockIdx.y;
     const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= total) return;
+    const BiSweep &w = b.w[v];
     const uint64_t lines = (uint64_t)(w.cnt[0] * w.cnt[1]);
     const int64_t r = (int64_t)(idx % (uint64_t)w.tpl);
     const uint64_t L = (idx / (uint64_t)w.tpl) % lines;
@@ -96,7 +109,7 @@ __global__ void k_bi_sweep(BiSweep w, LevelArgs q, T *__restrict__ data, uint16_
     c[w.axis] += i * w.s;
     const int64_t pos = c[0] * w.offs[0] + c[1] * w.offs[1] + c[2] * w.offs[2];
     const int64_t st = w.s * w.offs[w.axis];
-    T *d = data + pos;
+    T *d = b.data[v] + pos;
     const int64_t n = w.n;
     T pred;
     if (!w.cubic || n < 5) {
@@ -109,29 +122,30 @@ __global__ void k_bi_sweep(BiSweep w, LevelArgs q, T *__restrict__ data, uint16_
         else if ((n & 1) == 0 && i == n - 1) pred = i_quad3(d[-5 * st], d[-3 * st], d[-st]);
         else pred = i_quad2(d[-3 * st], d[-st], d[st]);
     }
-    T v = *d, uval;
-    const int code = quant_point<T, QM>(v, pred, q, uval);
+    T val = *d, uval;
+    const int code = quant_point<T, QM>(val, pred, q, uval);
     const uint64_t cp = t * (uint64_t)w.block_codes + (uint64_t)w.seg_off + L * (uint64_t)w.tpl + (uint64_t)r;
-    codes[cp] = (uint16_t)code;
-    if (code == 0) scratch[cp] = uval;
-    *d = v;
+    b.codes[v][cp] = (uint16_t)code;
+    if (code == 0) b.scratch[v][cp] = uval;
+    *d = val;
 }
 
 // Each block's corner against prediction 0.
 template <typename T>
-__global__ void k_bi_corner(BiSweep w, LevelArgs q, T *__restrict__ data, uint16_t *__restrict__ codes,
-                            T *__restrict__ scratch, uint64_t nblocks) {
+__global__ void k_bi_corner4(BiTrials<T> b, LevelArgs q, uint64_t nblocks) {
+    const int v = blockIdx.y;
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nblocks) return;
+    const BiSweep &w = b.w[v];
     const int64_t b2 = (int64_t)(t % (uint64_t)w.nb[2]);
     const int64_t b1 = (int64_t)((t / (uint64_t)w.nb[2]) % (uint64_t)w.nb[1]);
     const int64_t b0 = (int64_t)(t / ((uint64_t)w.nb[2] * (uint64_t)w.nb[1]));
     const int64_t pos = (b0 * w.offs[0] + b1 * w.offs[1] + b2 * w.offs[2]) * w.bs;
-    T v = data[pos], uval;
-    const int code = quantize<T>(v, (T)0, q.eb, q.recip, q.radius, 0, uval);
-    codes[t * (uint64_t)w.block_codes] = (uint16_t)code;
-    if (code == 0) scratch[t * (uint64_t)w.block_codes] = uval;
-    data[pos] = v;
+    T val = b.data[v][pos], uval;
+    const int code = quantize<T>(val, (T)0, q.eb, q.recip, q.radius, 0, uval);
+    b.codes[v][t * (uint64_t)w.block_codes] = (uint16_t)code;
+    if (code == 0) b.scratch[v][t * (uint64_t)w.block_codes] = uval;
+    b.data[v][pos] = val;
 }
 
 // optimize_quant_invl_3d: histogram of sampled Lorenzo prediction errors.
@@ -165,23 +179,24 @@ size_t zstd_framed_size(const uint8_t *p, size_t n) {
     return zs + 8;
 }
 
-// do_not_use_this_interp_compress_block_test: compression ratio of the
-// block-interpolation compressor on the sample (blocks of edge bs, which
-// tile the sample exactly).
+// do_not_use_this_interp_compress_block_test (SZInterp.hpp:558-577):
+// SZBlockInterpolationCompressor::compress on the sample (blocks of edge bs,
+// which tile the sample exactly), for the four trials at once.  Each trial's
+// codes (stream order) and unpredictable values (at their code positions)
+// are left in its arrays.
+struct BiTrialSpec {
+    int cubic, dir;
+};
+
+// Buffers come from `m` (ordered on its stream); the work runs on `st`.
 template <typename T>
-void block_interp_payload(int N, const uint64_t *sdims, const T *dS, double eb, int cubic, int dir, int64_t bs,
-                          cudaStream_t st, Counter &launches, faz_timings &tm, std::vector<uint8_t> &pl,
-                          const std::function<void(size_t)> &report = {}) {
+void block_interp_sweeps(int N, const uint64_t *sdims, const T *dS, double eb, const BiTrialSpec *spec, int64_t bs,
+                         DevMem &m, cudaStream_t st, Counter &launches, BiTrials<T> &b) {
     uint64_t num = 1;
     for (int i = 0; i < N; i++) {
         num *= sdims[i];
         if (sdims[i] % (uint64_t)bs) throw Fail{FAZ_ERR_UNSUPPORTED, "sample does not tile into sampling blocks"};
     }
-    DevMem m(st);
-    T *data = m.alloc<T>(num);
-    CK(cudaMemcpyAsync(data, dS, num * sizeof(T), cudaMemcpyDeviceToDevice, st));
-    uint16_t *codes = m.alloc<uint16_t>(num);
-    T *scratch = m.alloc<T>(num);
     LevelArgs q;
     std::memset(&q, 0, sizeof(q));
     q.eb = eb;
@@ -190,81 +205,114 @@ void block_interp_payload(int N, const uint64_t *sdims, const T *dS, double eb, 
     q.trim = 0;
     set_fast_path<T>(q);
     const bool straight = sizeof(T) == 4 && q.fast;
-    BiSweep w;
-    std::memset(&w, 0, sizeof(w));
     const int e = 3 - N;
-    for (int i = 0; i < 3; i++) {
-        w.dims[i] = 1;
-        w.nb[i] = 1;
+    int perm[kBiTrials][3];
+    for (int v = 0; v < kBiTrials; v++) {
+        b.data[v] = m.alloc<T>(num);
+        b.codes[v] = m.alloc<uint16_t>(num);
+        b.scratch[v] = m.alloc<T>(num);
     }
-    for (int i = 0; i < N; i++) {
-        w.dims[e + i] = (int64_t)sdims[i];
-        w.nb[e + i] = (int64_t)sdims[i] / bs;
+    {
+        Events ev;
+        CK(cudaEventRecord(ev.a, m.st));
+        CK(cudaStreamWaitEvent(st, ev.a, 0));
     }
-    w.offs[2] = 1;
-    w.offs[1] = w.dims[2];
-    w.offs[0] = w.dims[1] * w.dims[2];
-    w.bs = bs;
-    int64_t bc = 1;
-    for (int i = 0; i < N; i++) bc *= bs;
-    w.block_codes = bc;
-    w.cubic = cubic;
-    const uint64_t nblocks = (uint64_t)(w.nb[0] * w.nb[1] * w.nb[2]);
-    k_bi_corner<T><<<(unsigned)((nblocks + 255) / 256), 256, 0, st>>>(w, q, data, codes, scratch, nblocks);
+    for (int v = 0; v < kBiTrials; v++) {
+        CK(cudaMemcpyAsync(b.data[v], dS, num * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        BiSweep &w = b.w[v];
+        std::memset(&w, 0, sizeof(w));
+        for (int i = 0; i < 3; i++) {
+            w.dims[i] = 1;
+            w.nb[i] = 1;
+        }
+        for (int i = 0; i < N; i++) {
+            w.dims[e + i] = (int64_t)sdims[i];
+            w.nb[e + i] = (int64_t)sdims[i] / bs;
+        }
+        w.offs[2] = 1;
+        w.offs[1] = w.dims[2];
+        w.offs[0] = w.dims[1] * w.dims[2];
+        w.bs = bs;
+        int64_t bc = 1;
+        for (int i = 0; i < N; i++) bc *= bs;
+        w.block_codes = bc;
+        w.cubic = spec[v].cubic;
+        const int dir = spec[v].dir;
+        perm[v][0] = 0;
+        perm[v][1] = 1;
+        perm[v][2] = 2;
+        if (N == 2 && dir != 0) {
+            perm[v][0] = 1;
+            perm[v][1] = 0;
+        }
+        if (N == 3) {
+            static const int P3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+            if (dir < 0 || dir > 5) throw Fail{FAZ_ERR_ARG, "interpolation direction out of range"};
+            for (int i = 0; i < 3; i++) perm[v][i] = P3[dir][i];
+        }
+    }
+    const uint64_t nblocks = (uint64_t)(b.w[0].nb[0] * b.w[0].nb[1] * b.w[0].nb[2]);
+    k_bi_corner4<T><<<dim3((unsigned)((nblocks + 255) / 256), kBiTrials), 256, 0, st>>>(b, q, nblocks);
     launches(cudaGetLastError());
-    int perm[3] = {0, 1, 2};
-    if (N == 2 && dir != 0) {
-        perm[0] = 1;
-        perm[1] = 0;
-    }
-    if (N == 3) {
-        static const int P3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
-        if (dir < 0 || dir > 5) throw Fail{FAZ_ERR_ARG, "interpolation direction out of range"};
-        for (int i = 0; i < 3; i++) perm[i] = P3[dir][i];
-    }
     int maxl = 0;
     while (((int64_t)1 << maxl) < bs) maxl++;
     if (maxl < 1) maxl = 1;
     int64_t off = 1;  // the corner
     for (int level = maxl; level > 0; level--) {
-        const int64_t s = (int64_t)1 << (level - 1);
-        bool swept[3] = {false, false, false};
+        const int64_t s_ = (int64_t)1 << (level - 1);
+        bool swept[kBiTrials][3] = {};
         for (int sw = 0; sw < N; sw++) {
-            const int a = e + perm[sw];
-            w.axis = a;
-            int no = 0;
-            for (int i = 0; i < 3; i++)
-                if (i != a) w.oth[no++] = i;
-            for (int u = 0; u < 2; u++) {
-                const int ax = w.oth[u];
-                if (ax < e) {
-                    w.g[u] = 1;
-                    w.cnt[u] = 1;
-                } else {
-                    w.g[u] = swept[ax] ? s : 2 * s;
-                    w.cnt[u] = (bs - 1) / w.g[u] + 1;
+            uint64_t total = 0, per_block = 0;
+            for (int v = 0; v < kBiTrials; v++) {
+                BiSweep &w = b.w[v];
+                const int a = e + perm[v][sw];
+                w.axis = a;
+                int no = 0;
+                for (int i = 0; i < 3; i++)
+                    if (i != a) w.oth[no++] = i;
+                for (int u = 0; u < 2; u++) {
+                    const int ax = w.oth[u];
+                    if (ax < e) {
+                        w.g[u] = 1;
+                        w.cnt[u] = 1;
+                    } else {
+                        w.g[u] = swept[v][ax] ? s_ : 2 * s_;
+                        w.cnt[u] = (bs - 1) / w.g[u] + 1;
+                    }
                 }
+                w.s = s_;
+                w.n = (bs - 1) / s_ + 1;
+                w.tpl = w.n / 2;
+                w.seg_off = off;
+                const uint64_t pb = (uint64_t)(w.cnt[0] * w.cnt[1] * w.tpl);
+                // blocks are cubes, so every trial's sweep has the same size
+                if (v > 0 && pb != per_block) throw Fail{FAZ_ERR_DEVICE, "trial sweeps differ in size"};
+                per_block = pb;
+                total = pb * nblocks;
+                swept[v][a] = true;
             }
-            w.s = s;
-            w.n = (bs - 1) / s + 1;
-            w.tpl = w.n / 2;
-            w.seg_off = off;
-            const uint64_t per_block = (uint64_t)(w.cnt[0] * w.cnt[1] * w.tpl);
-            const uint64_t total = per_block * nblocks;
             if (total) {
-                const unsigned grid = (unsigned)((total + 255) / 256);
-                if (straight) k_bi_sweep<T, 1><<<grid, 256, 0, st>>>(w, q, data, codes, scratch, total);
-                else k_bi_sweep<T, 0><<<grid, 256, 0, st>>>(w, q, data, codes, scratch, total);
+                const dim3 grid((unsigned)((total + 255) / 256), kBiTrials);
+                if (straight) k_bi_sweep4<T, 1><<<grid, 256, 0, st>>>(b, q, total);
+                else k_bi_sweep4<T, 0><<<grid, 256, 0, st>>>(b, q, total);
                 launches(cudaGetLastError());
             }
             off += (int64_t)per_block;
-            swept[a] = true;
         }
     }
-    if (off != bc) throw Fail{FAZ_ERR_DEVICE, "block interpolation did not cover its blocks"};
+    if (off != b.w[0].block_codes) throw Fail{FAZ_ERR_DEVICE, "block interpolation did not cover its blocks"};
+}
+
+// The Huffman stage and payload of one block-interpolation trial; `report`
+// gets the payload's size as soon as the codebook is built.
+template <typename T>
+void block_interp_tail(int N, const uint64_t *sdims, double eb, int cubic, int dir, int64_t bs, uint16_t *codes,
+                       T *scratch, cudaStream_t st, Counter &launches, faz_timings &tm, std::vector<uint8_t> &pl,
+                       const std::function<void(size_t)> &report = {}) {
+    uint64_t num = 1;
+    for (int i = 0; i < N; i++) num *= sdims[i];
+    DevMem m(st);
     HuffEncoded hc;
-    // the payload's size is known once the codebook is: report it before the
-    // encoding kernels and copies finish
     auto sized = [&](const HuffEncoded &e) {
         if (!report) return;
         const size_t head = (size_t)N * 8 + 4 + 4 + 4 + 1 + 8 + 4 + 8;
@@ -517,14 +565,25 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         else gen_compress_payload<T>(N, sdims, 5, 1, 1, eb, c.quantbinCnt / 2, dS, s2, c2, t2, pl);
     });
     const int dir0 = c.interpDirection;
+    // the four block-interpolation trials' sweeps in shared launches on a
+    // high-priority stream; each trial's Huffman stage then runs on its own
+    // thread and stream
+    const BiTrialSpec spec[kBiTrials] = {{0, dir0}, {1, dir0}, {0, dop}, {1, dop}};
+    BiTrials<T> bt;
+    StreamGuard sf(nullptr, true);
+    CK(cudaStreamWaitEvent(sf.st, ready.a, 0));
+    block_interp_sweeps<T>(N, sdims, dS, eb, spec, (int64_t)sb, m, sf.st, launches, bt);
+    Events swept;
+    CK(cudaEventRecord(swept.a, sf.st));
     for (int op = 0; op < 2; op++) {
-        ji[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
+        ji[op].start(swept.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
                                       const std::function<void(size_t)> &rep) {
-            block_interp_payload<T>(N, sdims, dS, eb, op, dir0, (int64_t)sb, s2, c2, t2, pl, rep);
+            block_interp_tail<T>(N, sdims, eb, op, dir0, (int64_t)sb, bt.codes[op], bt.scratch[op], s2, c2, t2, pl, rep);
         });
-        jd[op].start(ready.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
+        jd[op].start(swept.a, [&, op](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
                                       const std::function<void(size_t)> &rep) {
-            block_interp_payload<T>(N, sdims, dS, eb, op, dop, (int64_t)sb, s2, c2, t2, pl, rep);
+            block_interp_tail<T>(N, sdims, eb, op, dop, (int64_t)sb, bt.codes[2 + op], bt.scratch[2 + op], s2, c2,
+                                 t2, pl, rep);
         });
     }
     // While the Lorenzo trial and the zstd sizes are computed, compress the
