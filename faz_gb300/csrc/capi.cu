@@ -514,8 +514,9 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
     resolve_eb<T>(c, dX, st, launches);
     if (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))
         throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
-    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.QoZ) {
-        // QoZ tuning (the faz tool's -q), then the interpolation compressor
+    if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && qoz_tuned(c)) {
+        // QoZ tuning (the faz tool's -q, or a predictorTuningRate in (0, 1)),
+        // then the interpolation compressor
         auto tt = clk::now();
         qoz_tune_device<T>(c, dX, st, launches, tm);
         tm.tune_ms = ms_since(tt);
@@ -1381,7 +1382,7 @@ int tune_impl(faz_config *conf, const void *d_data, void *user_stream, faz_timin
         if (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))
             throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
         auto tt = clk::now();
-        if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.QoZ) {
+        if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && qoz_tuned(c)) {
             qoz_tune_device<T>(c, dX, sg.st, launches, tm);
         } else if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) {
             faz_timings t2;

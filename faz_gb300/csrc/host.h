@@ -278,6 +278,11 @@ template <typename T>
 void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);
 template <typename T>
 int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);
+// Tuning runs its QoZ branch (SZInterp.hpp:1857) for QoZ = 1 and for any
+// predictorTuningRate in (0, 1)
+inline bool qoz_tuned(const faz_config &c) {
+    return c.QoZ || (c.predictorTuningRate > 0 && c.predictorTuningRate < 1);
+}
 // general Lorenzo frontend for 1-D / 2-D fields (general.cu)
 template <typename T>
 void gen_compress_payload(int N, const uint64_t *dims, int bs, int lo, int lo2, double eb, int radius, const T *dX,

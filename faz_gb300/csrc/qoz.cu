@@ -449,18 +449,30 @@ int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     if (c.tuningTarget != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for the PSNR (RD) target"};
     if (c.rng < 0) c.rng = device_range<T>(dX, c.num, st, launches);
     if (c.relErrorBound <= 0) c.relErrorBound = c.absErrorBound / c.rng;
-    // QoZ defaults (SZInterp.hpp:1597-1625)
-    if (c.autoTuningRate <= 0) c.autoTuningRate = N == 2 ? 0.01 : 0.005;
-    if (c.predictorTuningRate <= 0) c.predictorTuningRate = N == 2 ? 0.01 : 0.005;
-    if (c.maxStep <= 0) c.maxStep = N == 2 ? 64 : 32;
-    if (c.levelwisePredictionSelection <= 0) c.levelwisePredictionSelection = N == 2 ? 6 : 4;
-    if (c.sampleBlockSize <= 0) c.sampleBlockSize = N == 2 ? 64 : 32;
-    c.profiling = 0;
-    c.testLorenzo = 0;
-    c.sperr = -1;
-    c.conditioning = 0;
-    c.pyBind = 0;
-    c.sperrWithoutWave = 0;
+    // waveAutoFix (default 1, not a Config field here) turns the Lorenzo
+    // trial off above a relative bound of 1e-3 (SZInterp.hpp:1592-1594)
+    if (c.relErrorBound > 1e-3) c.testLorenzo = 0;
+    if (c.QoZ) {
+        // QoZ defaults (SZInterp.hpp:1597-1625)
+        if (c.autoTuningRate <= 0) c.autoTuningRate = N == 2 ? 0.01 : 0.005;
+        if (c.predictorTuningRate <= 0) c.predictorTuningRate = N == 2 ? 0.01 : 0.005;
+        if (c.maxStep <= 0) c.maxStep = N == 2 ? 64 : 32;
+        if (c.levelwisePredictionSelection <= 0) c.levelwisePredictionSelection = N == 2 ? 6 : 4;
+        if (c.sampleBlockSize <= 0) c.sampleBlockSize = N == 2 ? 64 : 32;
+        c.profiling = 0;
+        c.testLorenzo = 0;
+        c.sperr = -1;
+        c.conditioning = 0;
+        c.pyBind = 0;
+        c.sperrWithoutWave = 0;
+    }
+    // without QoZ the tuner runs from the configuration's own rates
+    // (predictorTuningRate in (0, 1)); these variants are not implemented
+    if (c.profiling) throw Fail{FAZ_ERR_UNSUPPORTED, "profiling-driven block sampling is not implemented"};
+    if (c.testLorenzo)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "the tuner's Lorenzo candidate (testLorenzo) is not implemented on the GPU path"};
+    if (!(c.autoTuningRate > 0))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "rate-driven tuning without autoTuningRate is not implemented"};
     int max_interp_level = -1;
     for (int i = 0; i < N; i++) {
         const int l = (int)std::ceil(std::log2((double)c.dims[i]));
@@ -473,6 +485,7 @@ int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     }
     uint64_t shortest = c.dims[0];
     for (int i = 0; i < N; i++) shortest = std::min<uint64_t>(shortest, c.dims[i]);
+    if (c.sampleBlockSize <= 0) c.sampleBlockSize = N == 2 ? 64 : 32;  // SZInterp.hpp:1783-1786
     const int minimum_sbs = 16;
     if (c.sampleBlockSize < minimum_sbs) c.sampleBlockSize = minimum_sbs;
     while ((uint64_t)c.sampleBlockSize >= shortest) c.sampleBlockSize /= 2;
@@ -555,6 +568,70 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     std::vector<uint8_t> il(Lsel > 0 ? Lsel : 0), dl(Lsel > 0 ? Lsel : 0);
     const int dirs[2] = {0, N == 3 ? 5 : 1};
     SumPlan sp;
+    // CompressTest (SZInterp.hpp:1130-1392) of every sampled block: bit rate
+    // after Huffman + zstd, PSNR from the summed squared errors
+    std::vector<std::pair<int64_t, int64_t>> ranges;
+    auto compress_test = [&](int op, int dir, double alpha, double beta, double eb, double &bitrate,
+                             double &psnr) {
+        CK(cudaMemcpyAsync(work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        QzRun R{1, g.levels, 0, eb, alpha, beta, c.trimToZero, op, dir, &il, &dl};
+        qz_run<T>(g, R, work, codes, scratch, err, nblk, sp, &ranges, st, launches);
+        const double se = block_sums(sp);
+        // q_bins: level ranges from the coarsest, each across all blocks
+        // (the anchors travel with the first interpolated level)
+        std::vector<int64_t> rlo, rlen, rout;
+        int64_t o = 0;
+        for (size_t i = 0; i < ranges.size(); i++) {
+            const int64_t lo = i == 0 ? 0 : ranges[i].first, hi = ranges[i].second;
+            if (hi <= lo) continue;
+            rlo.push_back(lo);
+            rlen.push_back(hi - lo);
+            rout.push_back(o);
+            o += (hi - lo) * (int64_t)nblk;
+        }
+        if (o != (int64_t)ns) throw Fail{FAZ_ERR_DEVICE, "tuning codes do not cover the sampled blocks"};
+        int64_t *dr = m.alloc<int64_t>(3 * rlo.size() + 3);
+        std::vector<int64_t> hr;
+        hr.insert(hr.end(), rlo.begin(), rlo.end());
+        hr.insert(hr.end(), rlen.begin(), rlen.end());
+        hr.insert(hr.end(), rout.begin(), rout.end());
+        CK(cudaMemcpyAsync(dr, hr.data(), hr.size() * 8, cudaMemcpyHostToDevice, st));
+        uint16_t *qb = m.alloc<uint16_t>(ns);
+        const int nr = (int)rlo.size();
+        k_qz_regroup<<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(codes, g.cpb, dr, dr + nr, dr + 2 * nr, nr, nblk,
+                                                                   qb, ns);
+        launches(cudaGetLastError());
+        HuffEncoded h;
+        huffman_encode_device(qb, ns, 32768, m, st, launches, h, tm);
+        // unpredictable values in the order the quantiser kept them
+        // (block by block, stream order): zeros of the block-major codes
+        const uint64_t nsub = hist_subchunks(ns);
+        unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1), *zoff = m.alloc<unsigned long long>(nsub + 1);
+        unsigned long long *ztmp = m.alloc<unsigned long long>(scan_temp_words(nsub) + 1);
+        launches(launch_count_zeros(codes, ns, zc, st));
+        launches(launch_scan_u64(zc, zoff, nsub, ztmp, st));
+        const uint64_t nunp = h.nzero;
+        T *unp = m.alloc<T>(nunp ? nunp : 1);
+        if (nunp) launches(launch_compact_zeros<T>(codes, ns, zc, zoff, nullptr, scratch, unp, st));
+        std::vector<uint8_t> head;
+        put<uint8_t>(head, 2);
+        put<double>(head, eb);
+        put<int32_t>(head, 32768);
+        put<uint64_t>(head, nunp);
+        std::vector<uint8_t> tree;
+        append_tree(tree, h.cb, h.nbytes);
+        std::vector<uint8_t> pl(head.size() + nunp * sizeof(T) + tree.size() + h.nbytes);
+        std::memcpy(pl.data(), head.data(), head.size());
+        if (nunp) CK(cudaMemcpyAsync(pl.data() + head.size(), unp, nunp * sizeof(T), cudaMemcpyDeviceToHost, st));
+        std::memcpy(pl.data() + head.size() + nunp * sizeof(T), tree.data(), tree.size());
+        if (h.nbytes)
+            CK(cudaMemcpyAsync(pl.data() + head.size() + nunp * sizeof(T) + tree.size(), h.bits, h.nbytes,
+                               cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        const double ele = (double)nv;
+        bitrate = 8 * (double)zstd_framed_size_host(pl.data(), pl.size()) / ele;
+        psnr = 20 * std::log10(c.rng) - 10 * std::log10(se / ele);
+    };
     if (Lsel > 0) {
         // per-level selection by summed prediction loss (tuning mode 2)
         for (int level = Lsel; level > 0; level--) {
@@ -582,72 +659,29 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         // the candidate loop leaves its last candidate in the configuration
         c.interpAlgo = FAZ_INTERP_ALGO_CUBIC;
         c.interpDirection = (uint8_t)dirs[1];
+    } else {
+        // one interpolator and direction for every level, by the compression
+        // ratio of a CompressTest per candidate (SZInterp.hpp:2036-2076)
+        int best_op = FAZ_INTERP_ALGO_CUBIC, best_dir = 0;
+        double best_cr = 0;
+        for (int op = 0; op < 2; op++)
+            for (int di = 0; di < 2; di++) {
+                double br, mm;
+                compress_test(op, dirs[di], c.alpha, c.beta, c.absErrorBound, br, mm);
+                const double cr = sizeof(T) * 8.0 / br;
+                if (cr > best_cr) {
+                    best_cr = cr;
+                    best_op = op;
+                    best_dir = dirs[di];
+                }
+            }
+        c.interpAlgo = best_op;
+        c.interpDirection = (uint8_t)best_dir;
     }
     c.alpha = o_alpha;
     c.beta = o_beta;
     if (c.autoTuningRate > 0) {
         // B-M tuning (SZInterp.hpp:2187-2515): CompressTest per alpha/beta
-        std::vector<std::pair<int64_t, int64_t>> ranges;
-        auto compress_test = [&](double alpha, double beta, double eb, double &bitrate, double &psnr) {
-            CK(cudaMemcpyAsync(work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, st));
-            QzRun R{1, g.levels, 0, eb, alpha, beta, c.trimToZero, c.interpAlgo, c.interpDirection, &il, &dl};
-            qz_run<T>(g, R, work, codes, scratch, err, nblk, sp, &ranges, st, launches);
-            const double se = block_sums(sp);
-            // q_bins: level ranges from the coarsest, each across all blocks
-            // (the anchors travel with the first interpolated level)
-            std::vector<int64_t> rlo, rlen, rout;
-            int64_t o = 0;
-            for (size_t i = 0; i < ranges.size(); i++) {
-                const int64_t lo = i == 0 ? 0 : ranges[i].first, hi = ranges[i].second;
-                if (hi <= lo) continue;
-                rlo.push_back(lo);
-                rlen.push_back(hi - lo);
-                rout.push_back(o);
-                o += (hi - lo) * (int64_t)nblk;
-            }
-            if (o != (int64_t)ns) throw Fail{FAZ_ERR_DEVICE, "tuning codes do not cover the sampled blocks"};
-            int64_t *dr = m.alloc<int64_t>(3 * rlo.size() + 3);
-            std::vector<int64_t> hr;
-            hr.insert(hr.end(), rlo.begin(), rlo.end());
-            hr.insert(hr.end(), rlen.begin(), rlen.end());
-            hr.insert(hr.end(), rout.begin(), rout.end());
-            CK(cudaMemcpyAsync(dr, hr.data(), hr.size() * 8, cudaMemcpyHostToDevice, st));
-            uint16_t *qb = m.alloc<uint16_t>(ns);
-            const int nr = (int)rlo.size();
-            k_qz_regroup<<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(codes, g.cpb, dr, dr + nr, dr + 2 * nr, nr, nblk,
-                                                                       qb, ns);
-            launches(cudaGetLastError());
-            HuffEncoded h;
-            huffman_encode_device(qb, ns, 32768, m, st, launches, h, tm);
-            // unpredictable values in the order the quantiser kept them
-            // (block by block, stream order): zeros of the block-major codes
-            const uint64_t nsub = hist_subchunks(ns);
-            unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1), *zoff = m.alloc<unsigned long long>(nsub + 1);
-            unsigned long long *ztmp = m.alloc<unsigned long long>(scan_temp_words(nsub) + 1);
-            launches(launch_count_zeros(codes, ns, zc, st));
-            launches(launch_scan_u64(zc, zoff, nsub, ztmp, st));
-            const uint64_t nunp = h.nzero;
-            T *unp = m.alloc<T>(nunp ? nunp : 1);
-            if (nunp) launches(launch_compact_zeros<T>(codes, ns, zc, zoff, nullptr, scratch, unp, st));
-            std::vector<uint8_t> head;
-            put<uint8_t>(head, 2);
-            put<double>(head, eb);
-            put<int32_t>(head, 32768);
-            put<uint64_t>(head, nunp);
-            std::vector<uint8_t> tree;
-            append_tree(tree, h.cb, h.nbytes);
-            std::vector<uint8_t> pl(head.size() + nunp * sizeof(T) + tree.size() + h.nbytes);
-            std::memcpy(pl.data(), head.data(), head.size());
-            if (nunp) CK(cudaMemcpyAsync(pl.data() + head.size(), unp, nunp * sizeof(T), cudaMemcpyDeviceToHost, st));
-            std::memcpy(pl.data() + head.size() + nunp * sizeof(T), tree.data(), tree.size());
-            if (h.nbytes)
-                CK(cudaMemcpyAsync(pl.data() + head.size() + nunp * sizeof(T) + tree.size(), h.bits, h.nbytes,
-                                   cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            const double ele = (double)nv;
-            bitrate = 8 * (double)zstd_framed_size_host(pl.data(), pl.size()) / ele;
-            psnr = 20 * std::log10(c.rng) - 10 * std::log10(se / ele);
-        };
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
         static const double alist[] = {1, 1.25, 1.5, 1.75, 2};
         static const double blist[] = {1.5, 2, 3, 4};
@@ -660,7 +694,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             for (double beta : blist) {
                 if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
                 double br, mm;
-                compress_test(alpha, beta, oriabseb, br, mm);
+                compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb, br, mm);
                 if (mm >= bestm && br <= bestb) {
                     bestalpha = alpha;
                     bestbeta = beta;
@@ -672,7 +706,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
                 } else {
                     const double fix = br / bestb;
                     double br2, m2;
-                    compress_test(alpha, beta, oriabseb * fix, br2, m2);
+                    compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb * fix, br2, m2);
                     const double a = (mm - m2) / (br - br2);
                     const double b = mm - a * br;
                     const double reg = a * bestb + b;

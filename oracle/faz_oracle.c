@@ -864,19 +864,28 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     size_t es = dtype == FAZ_FLOAT ? 4 : 8;
     double rngT = dtype == FAZ_FLOAT ? (double)(float)conf->rng : conf->rng;   /* T rng = conf.rng */
     double rel_bound = conf->relErrorBound > 0 ? conf->relErrorBound : conf->absErrorBound / rngT;
-    if (conf->autoTuningRate <= 0) conf->autoTuningRate = N == 2 ? 0.01 : 0.005;
-    if (conf->predictorTuningRate <= 0) conf->predictorTuningRate = N == 2 ? 0.01 : 0.005;
-    if (conf->maxStep <= 0) conf->maxStep = N == 2 ? 64 : 32;
-    if (conf->levelwisePredictionSelection <= 0) conf->levelwisePredictionSelection = N == 2 ? 6 : 4;
-    if (conf->sampleBlockSize <= 0) conf->sampleBlockSize = N == 2 ? 64 : 32;
-    /* FAZ features off (SZInterp.hpp:1611-1622); pyBind, sperr, conditioning and
-     * sperrWithoutWave are trailer fields */
-    conf->profiling = 0;
-    conf->testLorenzo = 0;
-    conf->sperr = -1;
-    conf->conditioning = 0;
-    conf->pyBind = 0;
-    conf->sperrWithoutWave = 0;
+    /* waveAutoFix (default 1) drops the Lorenzo trial above a relative bound
+     * of 1e-3 (SZInterp.hpp:1592-1594) */
+    if (rel_bound > 1e-3) conf->testLorenzo = 0;
+    if (conf->QoZ) {
+        if (conf->autoTuningRate <= 0) conf->autoTuningRate = N == 2 ? 0.01 : 0.005;
+        if (conf->predictorTuningRate <= 0) conf->predictorTuningRate = N == 2 ? 0.01 : 0.005;
+        if (conf->maxStep <= 0) conf->maxStep = N == 2 ? 64 : 32;
+        if (conf->levelwisePredictionSelection <= 0) conf->levelwisePredictionSelection = N == 2 ? 6 : 4;
+        if (conf->sampleBlockSize <= 0) conf->sampleBlockSize = N == 2 ? 64 : 32;
+        /* FAZ features off (SZInterp.hpp:1611-1622); pyBind, sperr, conditioning and
+         * sperrWithoutWave are trailer fields */
+        conf->profiling = 0;
+        conf->testLorenzo = 0;
+        conf->sperr = -1;
+        conf->conditioning = 0;
+        conf->pyBind = 0;
+        conf->sperrWithoutWave = 0;
+    }
+    if (conf->profiling || conf->testLorenzo || !(conf->autoTuningRate > 0)) {
+        set_err("oracle QoZ-branch tuner covers autoTuningRate > 0 without profiling or testLorenzo");
+        return -2;
+    }
     int max_interp_level = -1;
     for (int i = 0; i < N; i++) {
         int l = (int)ceil(log2((double)conf->dims[i]));
@@ -889,6 +898,7 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     }
     size_t shortest = conf->dims[0];
     for (int i = 0; i < N; i++) if (conf->dims[i] < shortest) shortest = conf->dims[i];
+    if (conf->sampleBlockSize <= 0) conf->sampleBlockSize = N == 2 ? 64 : 32;   /* SZInterp.hpp:1783-1786 */
     size_t minimum_sbs = 16;
     if ((size_t)conf->sampleBlockSize < minimum_sbs) conf->sampleBlockSize = (int)minimum_sbs;
     while ((size_t)conf->sampleBlockSize >= shortest) conf->sampleBlockSize /= 2;
@@ -957,6 +967,27 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         free(work);
         free(q32.unpred);
         free(q64.unpred);
+    } else {
+        /* one interpolator and direction for every level, by the compression
+         * ratio of a CompressTest per candidate (SZInterp.hpp:2036-2076) */
+        int best_op = 1, best_dir = 0;
+        double best_cr = 0;
+        for (int op = 0; op < 2; op++)
+            for (int di = 0; di < 2; di++) {
+                orc_params p = {op, dirs[di], conf->interpBlockSize, conf->fixBlockSize, conf->alpha, conf->beta,
+                                0, NULL, NULL};
+                double br, m;
+                int rc = dtype == FAZ_FLOAT
+                             ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
+                                                     conf->trimToZero, conf->maxStep, conf->rng, &br, &m)
+                             : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
+                                                     conf->trimToZero, conf->maxStep, conf->rng, &br, &m);
+                if (rc) { free(blocks); return rc; }
+                double cr = (double)es * 8.0 / br;
+                if (cr > best_cr) { best_cr = cr; best_op = op; best_dir = dirs[di]; }
+            }
+        conf->interpAlgo = best_op;
+        conf->interpDirection = (uint8_t)best_dir;
     }
     conf->alpha = o_alpha;
     conf->beta = o_beta;
@@ -1104,7 +1135,8 @@ static int sz3_tune(faz_config *conf, int dtype, const void *data) {
     size_t es = dtype == FAZ_FLOAT ? 4 : 8;
     if (conf->rng < 0) conf->rng = data_range(dtype, data, conf->num);
     if (conf->relErrorBound <= 0) conf->relErrorBound = conf->absErrorBound / conf->rng;
-    if (conf->QoZ) return qoz_tune(conf, dtype, data);
+    /* Tuning's QoZ branch: QoZ, or any predictorTuningRate in (0, 1) (SZInterp.hpp:1857) */
+    if (conf->QoZ || (conf->predictorTuningRate > 0 && conf->predictorTuningRate < 1)) return qoz_tune(conf, dtype, data);
     if (conf->autoTuningRate > 0 || conf->predictorTuningRate > 0 || conf->preTrim > 0 || conf->wavelet > 0) {
         set_err("oracle covers the SZ3 and QoZ tuners only");
         return -2;

@@ -60,8 +60,11 @@ def golden_stream(case):
 # INI keys of QoZ::Config::loadcfg (include/QoZ/utils/Config.hpp:91-233) used by the fixtures
 _INI_INT = {"InterpDirection": "interpDirection", "InterpBlockSize": "interpBlockSize",
             "fixBlockSize": "fixBlockSize", "trimToZero": "trimToZero", "maxStep": "maxStep",
-            "QuantizationBinTotal": "quantbinCnt", "blockOrder": "blockOrder", "BlockSize": "blockSize"}
-_INI_REAL = {"alpha": "alpha", "beta": "beta"}
+            "QuantizationBinTotal": "quantbinCnt", "blockOrder": "blockOrder", "BlockSize": "blockSize",
+            "sampleBlockSize": "sampleBlockSize", "levelwisePredictionSelection": "levelwisePredictionSelection",
+            "testLorenzo": "testLorenzo", "profiling": "profiling"}
+_INI_REAL = {"alpha": "alpha", "beta": "beta", "autoTuningRate": "autoTuningRate",
+             "predictorTuningRate": "predictorTuningRate"}
 _INI_BOOL = {"Lorenzo": "lorenzo", "Lorenzo2ndOrder": "lorenzo2", "Regression": "regression",
              "Regression2ndOrder": "regression2"}
 

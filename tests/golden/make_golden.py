@@ -143,6 +143,19 @@ def cases():
     out.append(("lor1d_l2", random_walk((3001,), 79), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
                  "AlgoSettings": {"Lorenzo2ndOrder": "YES", "Regression": "NO"}}))
+    # rate-driven tuning without -q (Tuning's QoZ branch from the INI's rates;
+    # the first is the learned tuner's labelling INI, whose Lorenzo candidate
+    # is dropped above a relative bound of 1e-3)
+    label_ini = {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.005", "predictorTuningRate": "0.005",
+                                                         "maxStep": "32", "levelwisePredictionSelection": "4",
+                                                         "sampleBlockSize": "32", "testLorenzo": "1"}}
+    out.append(("rate_label_ini_1e2", spectral_field((50, 120, 170), slope=-3.0, aniso=(1, 2, 2), seed=81),
+                ["-M", "REL", "1e-2"], label_ini))
+    out.append(("rate_ab_only", spectral_field((48, 56, 64), slope=-3.0, seed=82), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01"}}))
+    out.append(("rate_2d", spectral_field((400, 500), slope=-3.0, seed=83), ["-M", "REL", "5e-3"],
+                {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                                        "levelwisePredictionSelection": "6", "maxStep": "64"}}))
     return out
 
 

@@ -62,3 +62,45 @@ def test_gpu_qoz_matches_oracle(dims, rel, dtype, slope):
     assert parse_interp_header(p, len(dims)) == parse_interp_header(ref_payload, len(dims))
     assert p == ref_payload
     assert mask_first_size(stream) == mask_first_size(ref)
+
+
+# Tuning from the configuration's own rates (QoZ = 0, predictorTuningRate in
+# (0, 1)): levelwisePredictionSelection 0 picks one interpolator and direction
+# for every level by CompressTest ratio; a positive value picks per level.
+RATE_RANDOM = [
+    ((64, 80, 96), 1e-3, np.float32, 0, 0),
+    ((56, 64, 72), 5e-3, np.float32, 3, 16),
+    ((300, 420), 1e-3, np.float32, 0, 0),
+    ((48, 56, 64), 1e-5, np.float64, 0, 0),
+]
+
+
+@pytest.mark.parametrize("dims,rel,dtype,levelwise,max_step", RATE_RANDOM)
+def test_gpu_rate_tuning_matches_oracle(dims, rel, dtype, levelwise, max_step):
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = rel
+    conf.autoTuningRate = conf.predictorTuningRate = 0.01
+    conf.levelwisePredictionSelection = levelwise
+    conf.maxStep = max_step
+    x = spectral_field(dims, slope=-3.0, noise=0.01, seed=sum(dims) + 11, dtype=dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    _, p = O.read_stream(stream)
+    assert parse_interp_header(p, len(dims)) == parse_interp_header(ref_payload, len(dims))
+    assert p == ref_payload
+    assert mask_first_size(stream) == mask_first_size(ref)
+
+
+def test_gpu_rate_tuning_rejects_lorenzo_candidate():
+    """testLorenzo at a relative bound <= 1e-3 needs the tuner's Lorenzo
+    CompressTest, which the GPU path does not build: the call fails loudly."""
+    dims = (48, 56, 64)
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = 1e-3
+    conf.autoTuningRate = conf.predictorTuningRate = 0.01
+    conf.testLorenzo = 1
+    x = spectral_field(dims, slope=-3.0, seed=5)
+    with pytest.raises(F.FazError, match="UNSUPPORTED|Lorenzo"):
+        F.SZ_compress(conf, x)
