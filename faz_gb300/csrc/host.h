@@ -278,6 +278,15 @@ template <typename T>
 void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);
 template <typename T>
 int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);
+// The QoZ tuner's Lorenzo candidate: CompressTest(ALGO_LORENZO_REG) of nblk
+// sampled 3-D blocks of bsz^3 points (bit rate, PSNR).
+template <typename T>
+void lorenzo_compress_test(const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng, cudaStream_t st,
+                           Counter &launches, double &bitrate, double &psnr);
+// Lorenzo settings once the QoZ tuner has chosen Lorenzo (sampling, the
+// quantisation-interval estimate, pred_dim and 16384-bin trials).
+template <typename T>
+void qoz_lorenzo_followup(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);
 // Tuning runs its QoZ branch (SZInterp.hpp:1857) for QoZ = 1 and for any
 // predictorTuningRate in (0, 1)
 inline bool qoz_tuned(const faz_config &c) {

@@ -469,8 +469,8 @@ int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     // without QoZ the tuner runs from the configuration's own rates
     // (predictorTuningRate in (0, 1)); these variants are not implemented
     if (c.profiling) throw Fail{FAZ_ERR_UNSUPPORTED, "profiling-driven block sampling is not implemented"};
-    if (c.testLorenzo)
-        throw Fail{FAZ_ERR_UNSUPPORTED, "the tuner's Lorenzo candidate (testLorenzo) is not implemented on the GPU path"};
+    if (c.testLorenzo && N != 3)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "the tuner's Lorenzo candidate (testLorenzo) is implemented for 3-D data"};
     if (!(c.autoTuningRate > 0))
         throw Fail{FAZ_ERR_UNSUPPORTED, "rate-driven tuning without autoTuningRate is not implemented"};
     int max_interp_level = -1;
@@ -680,6 +680,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     }
     c.alpha = o_alpha;
     c.beta = o_beta;
+    bool use_interp = true;
     if (c.autoTuningRate > 0) {
         // B-M tuning (SZInterp.hpp:2187-2515): CompressTest per alpha/beta
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
@@ -721,10 +722,45 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             }
         }
         c.absErrorBound = oriabseb;
+        if (c.testLorenzo) {
+            // the Lorenzo candidate: CompressTest with ALGO_LORENZO_REG
+            // against the best alpha/beta point (SZInterp.hpp:2428-2486)
+            double br, mm;
+            lorenzo_compress_test<T>(blocks, nblk, bsz, oriabseb, c.rng, st, launches, br, mm);
+            if (mm >= bestm && br <= bestb) {
+                bestb = br;
+                bestm = mm;
+                bestalpha = bestbeta = -1;
+                use_interp = false;
+            } else if (mm <= bestm && br >= bestb) {
+                use_interp = true;
+            } else {
+                const double fix = br / bestb;
+                double br2, m2;
+                lorenzo_compress_test<T>(blocks, nblk, bsz, oriabseb * fix, c.rng, st, launches, br2, m2);
+                const double a = (mm - m2) / (br - br2);
+                if (a > 0) {
+                    const double b = mm - a * br;
+                    const double reg = a * bestb + b;
+                    if (reg > bestm) {
+                        bestb = br;
+                        bestm = mm;
+                        bestalpha = bestbeta = -1;
+                        use_interp = false;
+                    }
+                }
+            }
+        }
         c.alpha = bestalpha;
         c.beta = bestbeta;
         c.wavelet_rel_coeff = 1;
         c.wavelet = 0;
+    }
+    if (!use_interp) {
+        // Lorenzo: its own settings (the caller then runs the Lorenzo compressor)
+        c.cmprAlgo = FAZ_ALGO_LORENZO_REG;
+        qoz_lorenzo_followup<T>(c, dX, st, launches, tm);
+        return;
     }
     if (Lsel > 0) {
         c.interp_list_len = Lsel;

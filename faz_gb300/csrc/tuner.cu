@@ -499,6 +499,104 @@ void set_dims_defaults(faz_config &c) {
 // ALGO_LORENZO_REG and the chosen settings are in c.
 size_t zstd_framed_size_host(const uint8_t *p, size_t n) { return zstd_framed_size(p, n); }
 
+// Sampled field of sampling<T,N> (include/QoZ/utils/Extraction.hpp:89-143):
+// corner blocks of edge 2 * sb of every dmin-cube, dims sdims[0..N).
+template <typename T>
+struct Sample {
+    uint64_t sb = 0, sn = 0;
+    uint64_t sdims[3] = {1, 1, 1};
+    T *dS = nullptr;
+};
+
+// false when the field is too small to sample (sampling_num == num)
+template <typename T>
+bool take_sample(const faz_config &c, const T *dX, DevMem &m, cudaStream_t st, Counter &launches, Sample<T> &s) {
+    const int N = c.N;
+    uint64_t dims[4], dmin = c.dims[0];
+    for (int i = 0; i < N; i++) {
+        dims[i] = c.dims[i];
+        dmin = std::min<uint64_t>(dmin, dims[i]);
+    }
+    uint64_t sb = dmin;
+    while (cal_sampling_ratio(sb, c.num, dmin, N, dims) > 0.035) sb--;
+    if (sb * 2 > dmin) sb = dmin / 2;
+    if (sb < 9) return false;
+    if (N > 3) throw Fail{FAZ_ERR_UNSUPPORTED, "tuning a sampled 4-D field is not implemented on the GPU path"};
+    // sample dims (N of them), embedded as 3-D with leading 1s for the gather
+    Dims3 gd{}, sdd{};
+    const int e = 3 - N;
+    for (int i = 0; i < 3; i++) {
+        gd.v[i] = 1;
+        sdd.v[i] = 1;
+    }
+    uint64_t sn = 1;
+    for (int i = 0; i < N; i++) {
+        s.sdims[i] = dims[i] / dmin * 2 * sb;
+        gd.v[e + i] = (int64_t)dims[i];
+        sdd.v[e + i] = (int64_t)s.sdims[i];
+        sn *= s.sdims[i];
+    }
+    s.sb = sb;
+    s.sn = sn;
+    s.dS = m.alloc<T>(sn);
+    k_sample<T><<<(unsigned)((sn + 255) / 256), 256, 0, st>>>(dX, gd, sdd, (int64_t)sb, (int64_t)dmin, e, s.dS, sn);
+    launches(cudaGetLastError());
+    return true;
+}
+
+// Lorenzo follow-up of both tuners (SZInterp.hpp:2779-2837 and 2797-2845):
+// the Lorenzo settings, the quantisation-interval estimate and the pred_dim
+// and 16384-bin trials on the sample, from the Lorenzo ratio best_l.
+template <typename T>
+void lorenzo_followup(faz_config &c, const T *dX, const Sample<T> &smp, double best_l, cudaStream_t st,
+                      Counter &launches, faz_timings &tm) {
+    const int N = c.N;
+    uint64_t dims[4];
+    for (int i = 0; i < N; i++) dims[i] = c.dims[i];
+    const uint64_t *sdims = smp.sdims;
+    const T *dS = smp.dS;
+    const double eb = c.absErrorBound;
+    const double sbytes = smp.sn * 1.0 * sizeof(T);
+    double r;
+    faz_config lc = c;
+    lc.cmprAlgo = FAZ_ALGO_LORENZO_REG;
+    lc.lorenzo = 1;
+    lc.lorenzo2 = 1;
+    lc.regression = 0;
+    lc.regression2 = 0;
+    lc.openmp = 0;
+    lc.blockSize = 5;
+    set_dims_defaults(lc);  // setDims(sample dims)
+    if (N == 3) {
+        lc.quantbinCnt = quant_intervals<T>(dX, dims, eb, st, launches);
+        if (lc.quantbinCnt > 65536)
+            throw Fail{FAZ_ERR_UNSUPPORTED,
+                       "Lorenzo with more than 65536 quantisation bins is not implemented on the GPU path"};
+        lc.pred_dim = 2;
+        {
+            std::vector<uint8_t> pl;
+            lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
+            r = sbytes / zstd_framed_size(pl.data(), pl.size());
+        }
+        if (r > best_l * 1.02) best_l = r;
+        else lc.pred_dim = 3;
+    }
+    if (c.relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
+        const int q0 = lc.quantbinCnt;
+        lc.quantbinCnt = 16384;
+        std::vector<uint8_t> pl;
+        if (N == 3)
+            lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
+        else
+            gen_compress_payload<T>(N, sdims, lc.blockSize, 1, 1, eb, lc.quantbinCnt / 2, dS, st, launches, tm, pl);
+        r = sbytes / zstd_framed_size(pl.data(), pl.size());
+        if (r > best_l * 1.02) best_l = r;
+        else lc.quantbinCnt = q0;
+    }
+    set_dims_defaults(lc);  // setDims(full dims)
+    c = lc;
+}
+
 template <typename T>
 void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
                      const std::function<void(const faz_config &)> &speculate) {
@@ -509,39 +607,17 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     if (c.wavelet > 0) throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet modes are not part of the interpolation path"};
     if (c.rng < 0) c.rng = device_range<T>(dX, c.num, st, launches);
     if (c.relErrorBound <= 0) c.relErrorBound = c.absErrorBound / c.rng;
-    // sampling<T,N>
-    uint64_t dims[4], dmin = c.dims[0];
-    for (int i = 0; i < N; i++) {
-        dims[i] = c.dims[i];
-        dmin = std::min<uint64_t>(dmin, dims[i]);
-    }
-    uint64_t sb = dmin;
-    while (cal_sampling_ratio(sb, c.num, dmin, N, dims) > 0.035) sb--;
-    if (sb * 2 > dmin) sb = dmin / 2;
-    if (sb < 9) {
+    uint64_t dims[4];
+    for (int i = 0; i < N; i++) dims[i] = c.dims[i];
+    DevMem m(st);
+    Sample<T> smp;
+    if (!take_sample<T>(c, dX, m, st, launches, smp)) {
         c.cmprAlgo = FAZ_ALGO_INTERP;
         return;
     }
-    if (N > 3) throw Fail{FAZ_ERR_UNSUPPORTED, "tuning a sampled 4-D field is not implemented on the GPU path"};
-    // sample dims (N of them), embedded as 3-D with leading 1s for the gather
-    uint64_t sdims[3] = {1, 1, 1};
-    Dims3 gd{}, sdd{};
-    const int e = 3 - N;
-    for (int i = 0; i < 3; i++) {
-        gd.v[i] = 1;
-        sdd.v[i] = 1;
-    }
-    uint64_t sn = 1;
-    for (int i = 0; i < N; i++) {
-        sdims[i] = dims[i] / dmin * 2 * sb;
-        gd.v[e + i] = (int64_t)dims[i];
-        sdd.v[e + i] = (int64_t)sdims[i];
-        sn *= sdims[i];
-    }
-    DevMem m(st);
-    T *dS = m.alloc<T>(sn);
-    k_sample<T><<<(unsigned)((sn + 255) / 256), 256, 0, st>>>(dX, gd, sdd, (int64_t)sb, (int64_t)dmin, e, dS, sn);
-    launches(cudaGetLastError());
+    const uint64_t sb = smp.sb, sn = smp.sn;
+    const uint64_t *sdims = smp.sdims;
+    const T *dS = smp.dS;
     const double eb = c.absErrorBound;
     const double sbytes = sn * 1.0 * sizeof(T);
     // Tuning, SZ3 branch: the Lorenzo trial (blockSize 5), linear and cubic
@@ -661,49 +737,44 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         c.cmprAlgo = FAZ_ALGO_INTERP;
         return;
     }
-    // Lorenzo follow-up (SZInterp.hpp:2779-2837)
-    faz_config lc = c;
-    lc.cmprAlgo = FAZ_ALGO_LORENZO_REG;
-    lc.lorenzo = 1;
-    lc.lorenzo2 = 1;
-    lc.regression = 0;
-    lc.regression2 = 0;
-    lc.openmp = 0;
-    lc.blockSize = 5;
-    set_dims_defaults(lc);  // setDims(sample dims)
-    if (N == 3) {
-        lc.quantbinCnt = quant_intervals<T>(dX, dims, eb, st, launches);
-        if (lc.quantbinCnt > 65536)
-            throw Fail{FAZ_ERR_UNSUPPORTED,
-                       "Lorenzo with more than 65536 quantisation bins is not implemented on the GPU path"};
-        lc.pred_dim = 2;
-        {
-            std::vector<uint8_t> pl;
-            lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
-            r = sbytes / zstd_framed_size(pl.data(), pl.size());
-        }
-        if (r > best_l * 1.02) best_l = r;
-        else lc.pred_dim = 3;
-    }
-    if (c.relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
-        const int q0 = lc.quantbinCnt;
-        lc.quantbinCnt = 16384;
-        std::vector<uint8_t> pl;
-        if (N == 3)
-            lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
-        else
-            gen_compress_payload<T>(N, sdims, lc.blockSize, 1, 1, eb, lc.quantbinCnt / 2, dS, st, launches, tm, pl);
-        r = sbytes / zstd_framed_size(pl.data(), pl.size());
-        if (r > best_l * 1.02) best_l = r;
-        else lc.quantbinCnt = q0;
-    }
-    set_dims_defaults(lc);  // setDims(full dims)
-    c = lc;
+    lorenzo_followup<T>(c, dX, smp, best_l, st, launches, tm);
 }
 
 template void sz3_tune_device<float>(faz_config &, const float *, cudaStream_t, Counter &, faz_timings &,
                                      const std::function<void(const faz_config &)> &);
 template void sz3_tune_device<double>(faz_config &, const double *, cudaStream_t, Counter &, faz_timings &,
                                       const std::function<void(const faz_config &)> &);
+
+
+// After the QoZ tuner chose Lorenzo (SZInterp.hpp:2797-2845): the sample of
+// sampling<T,N>, its Lorenzo ratio under the Lorenzo settings (Config::setDims
+// of the sample dims: block size 6 in 3-D, 16 in 2-D), then the follow-up.
+template <typename T>
+void qoz_lorenzo_followup(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm) {
+    const int N = c.N;
+    c.lorenzo = 1;
+    c.lorenzo2 = 1;
+    c.regression = 0;
+    c.regression2 = 0;
+    c.openmp = 0;
+    c.blockSize = 5;
+    DevMem m(st);
+    Sample<T> smp;
+    if (!take_sample<T>(c, dX, m, st, launches, smp)) return;
+    faz_config lc = c;
+    set_dims_defaults(lc);  // setDims(sample dims)
+    std::vector<uint8_t> pl;
+    if (N == 3)
+        lorenzo_payload<T>(smp.sdims, smp.dS, lc.blockSize, lc.pred_dim, c.absErrorBound, lc.quantbinCnt / 2, st,
+                           launches, tm, pl);
+    else
+        gen_compress_payload<T>(N, smp.sdims, lc.blockSize, 1, 1, c.absErrorBound, lc.quantbinCnt / 2, smp.dS, st,
+                                launches, tm, pl);
+    const double best_l = smp.sn * 1.0 * sizeof(T) / zstd_framed_size(pl.data(), pl.size());
+    lorenzo_followup<T>(c, dX, smp, best_l, st, launches, tm);
+}
+
+template void qoz_lorenzo_followup<float>(faz_config &, const float *, cudaStream_t, Counter &, faz_timings &);
+template void qoz_lorenzo_followup<double>(faz_config &, const double *, cudaStream_t, Counter &, faz_timings &);
 
 }  // namespace faz

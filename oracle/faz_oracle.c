@@ -506,6 +506,8 @@ static int huff_decode(rd_t *r, size_t target, int *out) {
 #undef T
 #undef SFX
 
+static int z_framed_size(const uint8_t *p, size_t n, size_t *out);
+
 #define T float
 #define SFX f32
 #include "oracle_general.inc"
@@ -882,8 +884,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         conf->pyBind = 0;
         conf->sperrWithoutWave = 0;
     }
-    if (conf->profiling || conf->testLorenzo || !(conf->autoTuningRate > 0)) {
-        set_err("oracle QoZ-branch tuner covers autoTuningRate > 0 without profiling or testLorenzo");
+    if (conf->profiling || !(conf->autoTuningRate > 0)) {
+        set_err("oracle QoZ-branch tuner covers autoTuningRate > 0 without profiling");
         return -2;
     }
     int max_interp_level = -1;
@@ -991,6 +993,7 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     }
     conf->alpha = o_alpha;
     conf->beta = o_beta;
+    int use_interp = 1;
     /* B-M tuning (SZInterp.hpp:2187-2515) */
     if (conf->autoTuningRate > 0) {
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
@@ -1038,16 +1041,42 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             }
         }
         conf->absErrorBound = oriabseb;
+        if (conf->testLorenzo) {
+            /* the Lorenzo candidate: CompressTest with ALGO_LORENZO_REG against
+             * the best alpha/beta point (SZInterp.hpp:2428-2486) */
+            double br, m;
+            int rc = dtype == FAZ_FLOAT ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb, conf->rng, &br, &m)
+                                        : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb, conf->rng, &br, &m);
+            if (rc) { free(blocks); return rc; }
+            if (m >= bestm && br <= bestb) {
+                bestb = br; bestm = m; bestalpha = -1; bestbeta = -1; use_interp = 0;
+            } else if (m <= bestm && br >= bestb) {
+                use_interp = 1;
+            } else {
+                double fix = br / bestb, br2, m2;
+                rc = dtype == FAZ_FLOAT
+                         ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, &br2, &m2)
+                         : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, &br2, &m2);
+                if (rc) { free(blocks); return rc; }
+                double a = (m - m2) / (br - br2);
+                if (a > 0) {
+                    double b = m - a * br;
+                    double reg = a * bestb + b;
+                    if (reg > bestm) { bestb = br; bestm = m; bestalpha = -1; bestbeta = -1; use_interp = 0; }
+                }
+            }
+        }
         conf->alpha = bestalpha;
         conf->beta = bestbeta;
         conf->wavelet_rel_coeff = 1;
         conf->wavelet = 0;
     }
-    if (L > 0) {
+    if (L > 0 && use_interp) {
         conf->interp_list_len = L;
         for (int i = 0; i < L; i++) { conf->interpAlgo_list[i] = il[i]; conf->interpDirection_list[i] = dl[i]; }
     }
-    conf->cmprAlgo = FAZ_ALGO_INTERP;
+    /* Lorenzo: the caller runs the Lorenzo follow-up */
+    conf->cmprAlgo = use_interp ? FAZ_ALGO_INTERP : FAZ_ALGO_LORENZO_REG;
     free(blocks);
     return 0;
 }
@@ -1118,6 +1147,50 @@ static void conf_set_dims_defaults(faz_config *c) {
     c->stride = c->blockSize;
 }
 
+/* Lorenzo follow-up of both tuners (SZInterp.hpp:2779-2837, 2797-2845): the
+ * Lorenzo settings, the quantisation-interval estimate and the pred_dim and
+ * 16384-bin trials on the sample smp (sn points, dims sd), from the Lorenzo
+ * ratio best_l. */
+static int lorenzo_followup(faz_config *conf, int dtype, const void *data, const void *smp, size_t sn,
+                            const size_t *sd, double best_l) {
+    const int N = conf->N;
+    size_t dims[4];
+    for (int i = 0; i < N; i++) dims[i] = conf->dims[i];
+    const size_t es = dtype == FAZ_FLOAT ? 4 : 8;
+    const double eb = conf->absErrorBound;
+    size_t osz;
+    double ratio;
+    int rc;
+    faz_config lc = *conf;
+    lc.cmprAlgo = FAZ_ALGO_LORENZO_REG;
+    lc.lorenzo = 1; lc.lorenzo2 = 1; lc.regression = 0; lc.regression2 = 0; lc.openmp = 0;
+    lc.blockSize = 5;
+    conf_set_dims_defaults(&lc);   /* setDims(sample dims) */
+    if (N == 3) {
+        if (dtype == FAZ_FLOAT)
+            lc.quantbinCnt = opt_quant_intervals_f32((const float *)data, dims[0], dims[1], dims[2], eb);
+        else
+            lc.quantbinCnt = opt_quant_intervals_f64((const double *)data, dims[0], dims[1], dims[2], eb);
+        lc.pred_dim = 2;
+        rc = lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz);
+        if (rc) return rc;
+        ratio = sn * 1.0 * es / osz;
+        if (ratio > best_l * 1.02) best_l = ratio; else lc.pred_dim = 3;
+    }
+    if (conf->relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
+        int q0 = lc.quantbinCnt;
+        lc.quantbinCnt = 16384;
+        rc = N == 3 ? lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz)
+                    : gen_size(dtype, smp, N, sd, lc.blockSize, eb, lc.quantbinCnt / 2, &osz);
+        if (rc) return rc;
+        ratio = sn * 1.0 * es / osz;
+        if (ratio > best_l * 1.02) best_l = ratio; else lc.quantbinCnt = q0;
+    }
+    conf_set_dims_defaults(&lc);   /* setDims(full dims) */
+    *conf = lc;
+    return 0;
+}
+
 /*
  * ALGO_INTERP_LORENZO without QoZ tuning (SZ_compress_Interp_lorenzo,
  * SZInterp.hpp:2561-2880, with the SZ3 branch of Tuning, 2115-2187): range and
@@ -1136,7 +1209,25 @@ static int sz3_tune(faz_config *conf, int dtype, const void *data) {
     if (conf->rng < 0) conf->rng = data_range(dtype, data, conf->num);
     if (conf->relErrorBound <= 0) conf->relErrorBound = conf->absErrorBound / conf->rng;
     /* Tuning's QoZ branch: QoZ, or any predictorTuningRate in (0, 1) (SZInterp.hpp:1857) */
-    if (conf->QoZ || (conf->predictorTuningRate > 0 && conf->predictorTuningRate < 1)) return qoz_tune(conf, dtype, data);
+    if (conf->QoZ || (conf->predictorTuningRate > 0 && conf->predictorTuningRate < 1)) {
+        int rc = qoz_tune(conf, dtype, data);
+        if (rc || conf->cmprAlgo != FAZ_ALGO_LORENZO_REG) return rc;
+        /* Lorenzo chosen (SZInterp.hpp:2797-2845): the Lorenzo ratio of the
+         * sample under the Lorenzo settings, then the follow-up */
+        size_t sn, sd[4], sb;
+        void *smp = sample_of(dtype, data, N, dims, &sn, sd, &sb);
+        conf->lorenzo = 1; conf->lorenzo2 = 1; conf->regression = 0; conf->regression2 = 0; conf->openmp = 0;
+        conf->blockSize = 5;
+        if (sn == conf->num) { free(smp); return 0; }
+        faz_config lc = *conf;
+        conf_set_dims_defaults(&lc);   /* setDims(sample dims) */
+        size_t osz;
+        rc = N == 3 ? lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, conf->absErrorBound, lc.quantbinCnt / 2, &osz)
+                    : gen_size(dtype, smp, N, sd, lc.blockSize, conf->absErrorBound, lc.quantbinCnt / 2, &osz);
+        if (!rc) rc = lorenzo_followup(conf, dtype, data, smp, sn, sd, sn * 1.0 * es / osz);
+        free(smp);
+        return rc;
+    }
     if (conf->autoTuningRate > 0 || conf->predictorTuningRate > 0 || conf->preTrim > 0 || conf->wavelet > 0) {
         set_err("oracle covers the SZ3 and QoZ tuners only");
         return -2;
@@ -1171,36 +1262,9 @@ static int sz3_tune(faz_config *conf, int dtype, const void *data) {
         conf->cmprAlgo = FAZ_ALGO_INTERP;
         return 0;
     }
-    /* Lorenzo follow-up (SZInterp.hpp:2779-2837) */
-    faz_config lc = *conf;
-    lc.cmprAlgo = FAZ_ALGO_LORENZO_REG;
-    lc.lorenzo = 1; lc.lorenzo2 = 1; lc.regression = 0; lc.regression2 = 0; lc.openmp = 0;
-    lc.blockSize = 5;
-    conf_set_dims_defaults(&lc);   /* setDims(sample dims) */
-    if (N == 3) {
-        if (dtype == FAZ_FLOAT)
-            lc.quantbinCnt = opt_quant_intervals_f32((const float *)data, dims[0], dims[1], dims[2], eb);
-        else
-            lc.quantbinCnt = opt_quant_intervals_f64((const double *)data, dims[0], dims[1], dims[2], eb);
-        lc.pred_dim = 2;
-        rc = lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz);
-        if (rc) { free(smp); return rc; }
-        ratio = sn * 1.0 * es / osz;
-        if (ratio > best_l * 1.02) best_l = ratio; else lc.pred_dim = 3;
-    }
-    if (conf->relErrorBound < 1.01e-6 && best_l > 5 && lc.quantbinCnt != 16384) {
-        int q0 = lc.quantbinCnt;
-        lc.quantbinCnt = 16384;
-        rc = N == 3 ? lorenzo3_size(dtype, smp, sd, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, &osz)
-                    : gen_size(dtype, smp, N, sd, lc.blockSize, eb, lc.quantbinCnt / 2, &osz);
-        if (rc) { free(smp); return rc; }
-        ratio = sn * 1.0 * es / osz;
-        if (ratio > best_l * 1.02) best_l = ratio; else lc.quantbinCnt = q0;
-    }
-    conf_set_dims_defaults(&lc);   /* setDims(full dims) */
+    rc = lorenzo_followup(conf, dtype, data, smp, sn, sd, best_l);
     free(smp);
-    *conf = lc;
-    return 0;
+    return rc;
 }
 
 /* Pre-zstd payload of a resolved configuration (SZ_compress_dispatcher,

@@ -151,6 +151,11 @@ def cases():
                                                          "sampleBlockSize": "32", "testLorenzo": "1"}}
     out.append(("rate_label_ini_1e2", spectral_field((50, 120, 170), slope=-3.0, aniso=(1, 2, 2), seed=81),
                 ["-M", "REL", "1e-2"], label_ini))
+    # at relative bounds <= 1e-3 the Lorenzo candidate runs: a field the 3-D
+    # Lorenzo predictor reproduces (sums of 2-D functions) selects it
+    out.append(("rate_label_ini_1e3", spectral_field((64, 96, 80), slope=-3.0, seed=84), ["-M", "REL", "1e-3"],
+                label_ini))
+    out.append(("rate_label_ini_lorenzo", sum2d((64, 72, 80), 1e-4, 85), ["-M", "REL", "1e-3"], label_ini))
     out.append(("rate_ab_only", spectral_field((48, 56, 64), slope=-3.0, seed=82), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01"}}))
     out.append(("rate_2d", spectral_field((400, 500), slope=-3.0, seed=83), ["-M", "REL", "5e-3"],

@@ -7,6 +7,7 @@ import pytest
 import faz_gb300 as F
 from faz_gb300.fields import spectral_field
 from conftest import (cli_config, golden_case, golden_input, golden_manifest, golden_stream, mask_first_size,
+                      mask_fast_frontend_padding,
                       parse_interp_header)
 
 import oracle.oracle as O
@@ -92,10 +93,11 @@ def test_gpu_rate_tuning_matches_oracle(dims, rel, dtype, levelwise, max_step):
     assert mask_first_size(stream) == mask_first_size(ref)
 
 
-def test_gpu_rate_tuning_rejects_lorenzo_candidate():
-    """testLorenzo at a relative bound <= 1e-3 needs the tuner's Lorenzo
-    CompressTest, which the GPU path does not build: the call fails loudly."""
-    dims = (48, 56, 64)
+def test_gpu_rate_tuning_rejects_2d_lorenzo_candidate():
+    """testLorenzo on 2-D data at a relative bound <= 1e-3 needs the 2-D
+    general frontend over the sampled blocks, which the GPU path does not
+    build: the call fails loudly."""
+    dims = (300, 420)
     conf = F.Config(*dims)
     conf.errorBoundMode = F.EB_REL
     conf.relErrorBound = 1e-3
@@ -104,3 +106,52 @@ def test_gpu_rate_tuning_rejects_lorenzo_candidate():
     x = spectral_field(dims, slope=-3.0, seed=5)
     with pytest.raises(F.FazError, match="UNSUPPORTED|Lorenzo"):
         F.SZ_compress(conf, x)
+
+
+def _sum_of_planes(shape, noise, seed, dtype):
+    """f(i,j) + g(j,k) + h(i,k) plus white noise: the 3-D Lorenzo predictor
+    reproduces sums of 2-D functions, so the tuner's Lorenzo candidate wins."""
+    rng = np.random.default_rng(seed)
+    base = (rng.standard_normal((shape[0], shape[1], 1)) + rng.standard_normal((1, shape[1], shape[2])) +
+            rng.standard_normal((shape[0], 1, shape[2])))
+    return (base + noise * rng.standard_normal(shape) * (base.max() - base.min())).astype(dtype)
+
+
+# the learned tuner's labelling configuration (testLorenzo = 1): at relative
+# bounds <= 1e-3 the Lorenzo candidate runs against the best alpha/beta point
+LABEL_CASES = [
+    ("planes", (64, 64, 64), 1e-3, np.float32, 1e-3),
+    ("planes", (64, 72, 80), 1e-4, np.float32, 1e-5),
+    ("planes", (48, 56, 64), 1e-3, np.float64, 1e-3),
+    ("spectral", (64, 96, 80), 1e-3, np.float32, 0.01),
+    ("spectral", (80, 64, 72), 2e-4, np.float32, 0.02),
+]
+
+
+@pytest.mark.parametrize("kind,dims,rel,dtype,noise", LABEL_CASES)
+def test_gpu_lorenzo_candidate_matches_oracle(kind, dims, rel, dtype, noise):
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = rel
+    conf.autoTuningRate = conf.predictorTuningRate = 0.005
+    conf.maxStep = 32
+    conf.levelwisePredictionSelection = 4
+    conf.sampleBlockSize = 32
+    conf.testLorenzo = 1
+    if kind == "planes":
+        x = _sum_of_planes(dims, noise, sum(dims), dtype)
+    else:
+        x = spectral_field(dims, slope=-3.0, noise=noise, seed=sum(dims) + 5, dtype=dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    c1, p = O.read_stream(stream)
+    c2, _ = O.read_stream(ref)
+    for f in ("cmprAlgo", "alpha", "beta", "interpAlgo", "interpDirection", "quantbinCnt", "blockSize", "pred_dim"):
+        assert getattr(c1, f) == getattr(c2, f), f
+    if kind == "planes":
+        assert c1.cmprAlgo == 0  # ALGO_LORENZO_REG
+        assert mask_fast_frontend_padding(p, x.itemsize) == mask_fast_frontend_padding(ref_payload, x.itemsize)
+    else:
+        assert p == ref_payload
+    dec, c3 = F.SZ_decompress(None, stream, dtype=x.dtype)
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c3.absErrorBound
