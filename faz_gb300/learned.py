@@ -79,8 +79,10 @@ def features(conf, tensor, out=None):
     return out
 
 
-def labels_of(qoz_conf, sz3_conf):
-    """Label row (int32[8]) from the QoZ tuner's and the SZ3 tuner's decisions."""
+def labels_of(qoz_conf, label_conf_result):
+    """Label row (int32[8]): the QoZ tuner's per-level interpolators and
+    directions, alpha and beta, and whether the labelling configuration
+    (label_conf) chose Lorenzo."""
     lab = np.full(N_LABELS, -1, dtype=np.int32)
     for l, (a, d) in enumerate(zip(qoz_conf.interpAlgo_list[:4], qoz_conf.interpDirection_list[:4])):
         lab[l] = 2 * int(a) + (1 if int(d) != 0 else 0)
@@ -88,8 +90,8 @@ def labels_of(qoz_conf, sz3_conf):
         lab[4] = ALPHAS.index(qoz_conf.alpha)
     if qoz_conf.beta in BETAS:
         lab[5] = BETAS.index(qoz_conf.beta)
-    if sz3_conf is not None:
-        lab[6] = 1 if sz3_conf.cmprAlgo == ALGO_LORENZO_REG else 0
+    if label_conf_result is not None:
+        lab[6] = 1 if label_conf_result.cmprAlgo == ALGO_LORENZO_REG else 0
     return lab
 
 
@@ -281,9 +283,17 @@ def qoz_conf(dims, rel):
     return c
 
 
-def sz3_conf(dims, rel):
+def label_conf(dims, rel):
+    """The labelling configuration: QoZ = 0 with the INI [AlgoSettings]
+    autoTuningRate = predictorTuningRate = 0.005, maxStep = 32,
+    levelwisePredictionSelection = 4, sampleBlockSize = 32, testLorenzo = 1.
+    Its interpolation decisions equal the QoZ tuner's (the same values are the
+    QoZ defaults for 3-D data); at relative bounds <= 1e-3 it also tries the
+    Lorenzo candidate, which gives the Lorenzo label."""
     c = Config(*dims)
     c.errorBoundMode, c.relErrorBound = EB_REL, rel
+    c.autoTuningRate = c.predictorTuningRate = 0.005
+    c.maxStep, c.levelwisePredictionSelection, c.sampleBlockSize, c.testLorenzo = 32, 4, 32, 1
     return c
 
 
@@ -299,7 +309,7 @@ def generate(n, seed, device="cuda", log=None):
         x = make_field(fp, device)
         try:
             q = tune_device(qoz_conf(fp["dims"], fp["rel"]), x)
-            z = tune_device(sz3_conf(fp["dims"], fp["rel"]), x)
+            z = tune_device(label_conf(fp["dims"], fp["rel"]), x)
         except FazError as e:
             if log:
                 log(f"field {i} skipped: {e}")
@@ -312,6 +322,32 @@ def generate(n, seed, device="cuda", log=None):
             log(f"field {i} {time.time() - t0:.1f}s")
     torch.cuda.synchronize()
     return np.array(X, np.float32).reshape(-1, N_FEATURES), np.array(Y, np.int32).reshape(-1, N_LABELS), P
+
+
+def relabel(path, device="cuda", log=None):
+    """Lorenzo labels of a saved dataset recomputed with label_conf on the
+    regenerated fields; returns (X, Y, params, stats)."""
+    import ast
+    import torch
+    d = np.load(path)
+    X, Y, P = d["X"], d["Y"].copy(), d["params"]
+    changed = interp_diff = lorenzo = 0
+    for i, ps in enumerate(P):
+        fp = ast.literal_eval(str(ps))
+        x = make_field(fp, device)
+        z = tune_device(label_conf(fp["dims"], fp["rel"]), x)
+        lab = 1 if z.cmprAlgo == ALGO_LORENZO_REG else 0
+        lorenzo += lab
+        changed += int(Y[i, 6] != lab)
+        Y[i, 6] = lab
+        if not lab:
+            zl = labels_of(z, None)
+            interp_diff += int(not np.array_equal(zl[:6], Y[i, :6]))
+        del x
+        if log and (i % 512 == 0 or i == len(P) - 1):
+            log(f"field {i}: {lorenzo} Lorenzo, {changed} changed, {interp_diff} interpolation labels differ")
+    torch.cuda.synchronize()
+    return X, Y, P, dict(lorenzo=lorenzo, changed=changed, interp_diff=interp_diff, n=len(P))
 
 
 def _timed(fn, reps=3):
@@ -389,6 +425,9 @@ def _main():
     e.add_argument("--model", default=DEFAULT_MODEL)
     e.add_argument("--n", type=int, default=64)
     e.add_argument("--seed", type=int, default=999)
+    r = sub.add_parser("relabel")
+    r.add_argument("--data", required=True)
+    r.add_argument("--out", required=True)
     t = sub.add_parser("train")
     t.add_argument("--data", required=True, nargs="+")
     t.add_argument("--out", default=DEFAULT_MODEL)
@@ -398,6 +437,10 @@ def _main():
     if a.cmd == "gen":
         X, Y, P = generate(a.n, a.seed, log=print)
         np.savez_compressed(a.out, X=X, Y=Y, params=np.array([repr(p) for p in P]))
+    elif a.cmd == "relabel":
+        X, Y, P, stats = relabel(a.data, log=print)
+        np.savez_compressed(a.out, X=X, Y=Y, params=P)
+        print(stats)
     elif a.cmd == "eval":
         _, summary = evaluate(TunerModel.load(a.model), a.n, a.seed, log=print)
         print(summary)
