@@ -938,8 +938,12 @@ int compress_batch_impl(int nf, const faz_config *confs, const void *const *d_da
 }
 
 template <typename T>
+void compress_omp(faz_config &c, const T *dX, cudaStream_t st, char **out, size_t *out_size, faz_timings &tm);
+
+// slab: compress one slab of an OpenMP stream (its openmp flag is not acted on)
+template <typename T>
 int compress_impl(const faz_config *conf_in, const void *data, bool on_device, void *user_stream, char **out,
-                  size_t *out_size, faz_timings *tmo) {
+                  size_t *out_size, faz_timings *tmo, bool slab = false) {
     faz_timings tm;
     std::memset(&tm, 0, sizeof(tm));
     auto t0 = clk::now();
@@ -963,16 +967,22 @@ int compress_impl(const faz_config *conf_in, const void *data, bool on_device, v
         } else {
             dX = (const T *)data;
         }
-        uint8_t *payload;
-        size_t psize;
-        CK(cudaEventRecord(ev_gpu.a, st));
-        compress_dispatch<T>(c, dX, st, payload, psize, tm, launches);
-        CK(cudaEventRecord(ev_gpu.b, st));
-        CK(cudaStreamSynchronize(st));
-        if (!on_device) tm.h2d_ms = ev_h2d.ms();
-        tm.gpu_ms = ev_gpu.ms();
-        finish_stream(c, payload, psize, out, out_size, tm);
-        tm.kernel_launches = launches.n;
+        if (c.openmp && !slab) {
+            CK(cudaStreamSynchronize(st));
+            if (!on_device) tm.h2d_ms = ev_h2d.ms();
+            compress_omp<T>(c, dX, st, out, out_size, tm);
+        } else {
+            uint8_t *payload;
+            size_t psize;
+            CK(cudaEventRecord(ev_gpu.a, st));
+            compress_dispatch<T>(c, dX, st, payload, psize, tm, launches);
+            CK(cudaEventRecord(ev_gpu.b, st));
+            CK(cudaStreamSynchronize(st));
+            if (!on_device) tm.h2d_ms = ev_h2d.ms();
+            tm.gpu_ms = ev_gpu.ms();
+            finish_stream(c, payload, psize, out, out_size, tm);
+            tm.kernel_launches = launches.n;
+        }
     } catch (const Fail &f) {
         set_error(f.msg);
         return f.code;
@@ -983,6 +993,109 @@ int compress_impl(const faz_config *conf_in, const void *data, bool on_device, v
     tm.total_ms = ms_since(t0);
     if (tmo) *tmo = tm;
     return FAZ_OK;
+}
+
+// Slabs of an OpenMP stream: the reference runs one slab per OpenMP thread
+// (omp_get_num_threads), so the count follows OMP_NUM_THREADS when it is set
+// and the host's hardware threads otherwise, at most dims[0].
+int omp_slab_count(uint64_t d0) {
+    long n = 0;
+    if (const char *e = std::getenv("OMP_NUM_THREADS")) n = std::strtol(e, nullptr, 10);
+    if (n <= 0) n = (long)std::max(1u, std::thread::hardware_concurrency());
+    if ((uint64_t)n > d0) n = (long)d0;
+    return (int)n;
+}
+
+// slab t of nt along the slowest axis: rows [lo, hi) (SZImplOMP.hpp:44-46)
+void omp_slab_rows(uint64_t d0, int t, int nt, uint64_t &lo, uint64_t &hi) {
+    lo = (uint64_t)t * d0 / (uint64_t)nt;
+    hi = (uint64_t)(t + 1) * d0 / (uint64_t)nt;
+}
+
+// the slab's Config: the field's, with Config::setDims of the slab's extents
+// (include/QoZ/utils/Config.hpp:77-89)
+faz_config omp_slab_config(const faz_config &c, uint64_t rows) {
+    faz_config ct = c;
+    ct.dims[0] = rows;
+    ct.num = rows;
+    for (int i = 1; i < c.N; i++) ct.num *= c.dims[i];
+    ct.coeffs_num = ct.num;
+    ct.coeffs_dims_len = c.N;
+    for (int i = 0; i < c.N; i++) ct.coeffs_dims[i] = ct.dims[i];
+    ct.blockSize = c.N == 1 ? 128 : (c.N == 2 ? 16 : 6);
+    ct.pred_dim = c.N;
+    ct.stride = ct.blockSize;
+    return ct;
+}
+
+// SZ_compress_OMP (include/QoZ/api/impl/SZImplOMP.hpp:10-95): the error
+// bound from the whole field's range, then every slab compressed as a field
+// of its own; the stream is int nThreads, the slabs' Configs, their sizes
+// (size_t each) and their compressed bytes, then the field's Config.
+template <typename T>
+void compress_omp(faz_config &c, const T *dX, cudaStream_t st, char **out, size_t *out_size, faz_timings &tm) {
+    if (c.errorBoundMode != FAZ_EB_ABS && c.errorBoundMode != FAZ_EB_REL)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "OpenMP streams take the ABS or REL error bound mode"};
+    Counter launches;
+    if (c.errorBoundMode != FAZ_EB_ABS) resolve_eb<T>(c, dX, st, launches);
+    const int nt = omp_slab_count(c.dims[0]);
+    uint64_t base = 1;
+    for (int i = 1; i < c.N; i++) base *= c.dims[i];
+    std::vector<std::vector<uint8_t>> confs(nt), parts(nt);
+    for (int t = 0; t < nt; t++) {
+        uint64_t lo, hi;
+        omp_slab_rows(c.dims[0], t, nt, lo, hi);
+        const faz_config ct = omp_slab_config(c, hi - lo);
+        char *so = nullptr;
+        size_t ss = 0;
+        faz_timings t2;
+        std::memset(&t2, 0, sizeof(t2));
+        const int rc = compress_impl<T>(&ct, dX + lo * base, true, st, &so, &ss, &t2, true);
+        if (rc) throw Fail{rc, std::string("slab ") + std::to_string(t) + ": " + last_error()};
+        int32_t cs;
+        std::memcpy(&cs, so + ss - 4, 4);
+        const size_t body = ss - 4 - (size_t)cs;
+        parts[t].assign((const uint8_t *)so, (const uint8_t *)so + body);
+        confs[t].assign((const uint8_t *)so + body, (const uint8_t *)so + body + cs);
+        std::free(so);
+        tm.gpu_ms += t2.gpu_ms;
+        tm.zstd_ms += t2.zstd_ms;
+        tm.host_ms += t2.host_ms;
+        tm.payload_bytes += t2.payload_bytes;
+        tm.unpred_count += t2.unpred_count;
+        tm.kernel_launches += t2.kernel_launches;
+    }
+    std::vector<uint8_t> trailer;
+    config_save(c, trailer);
+    size_t total = 4 + 4 + trailer.size();
+    for (int t = 0; t < nt; t++) total += confs[t].size() + 8 + parts[t].size();
+    uint8_t *buf = (uint8_t *)std::malloc(total);
+    if (!buf) throw Fail{FAZ_ERR_ARG, "out of host memory"};
+    uint8_t *p = buf;
+    const int32_t n32 = nt;
+    std::memcpy(p, &n32, 4);
+    p += 4;
+    for (int t = 0; t < nt; t++) {
+        std::memcpy(p, confs[t].data(), confs[t].size());
+        p += confs[t].size();
+    }
+    for (int t = 0; t < nt; t++) {
+        const uint64_t sz = parts[t].size();
+        std::memcpy(p, &sz, 8);
+        p += 8;
+    }
+    for (int t = 0; t < nt; t++) {
+        std::memcpy(p, parts[t].data(), parts[t].size());
+        p += parts[t].size();
+    }
+    std::memcpy(p, trailer.data(), trailer.size());
+    p += trailer.size();
+    const int32_t ts = (int32_t)trailer.size();
+    std::memcpy(p, &ts, 4);
+    p += 4;
+    *out = (char *)buf;
+    *out_size = (size_t)(p - buf);
+    tm.kernel_launches += launches.n;
 }
 
 // -------------------------------------------------------------- decompress
@@ -1234,13 +1347,62 @@ void open_stream(const char *cmp, size_t cmp_size, faz_config &conf, uint8_t *&p
 }
 
 template <typename T>
+void decompress_omp(const faz_config &c, const char *cmp, size_t cmp_size, T *dOut, cudaStream_t st,
+                    faz_timings &tm);
+
+// slab: decompress one slab of an OpenMP stream (its openmp flag is not acted on)
+template <typename T>
 int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void **out, bool on_device, void *dOutUser,
-                    void *user_stream, faz_timings *tmo) {
+                    void *user_stream, faz_timings *tmo, bool slab = false) {
     faz_timings tm;
     std::memset(&tm, 0, sizeof(tm));
     auto t0 = clk::now();
     try {
         if (!conf_io) throw Fail{FAZ_ERR_ARG, "null config"};
+        if (!slab) {
+            // an OpenMP stream (SZ_decompress_OMP, include/QoZ/api/impl/SZImplOMP.hpp:97-149)
+            faz_config oc;
+            if (!cmp || cmp_size < 4) throw Fail{FAZ_ERR_FORMAT, "stream too short"};
+            int32_t cs;
+            std::memcpy(&cs, cmp + cmp_size - 4, 4);
+            if (cs <= 0 || (size_t)cs + 4 > cmp_size) throw Fail{FAZ_ERR_FORMAT, "bad trailer size"};
+            if (config_load(oc, (const uint8_t *)cmp + cmp_size - 4 - cs, (size_t)cs)) throw Fail{FAZ_ERR_FORMAT, "bad stream trailer"};
+            if (oc.openmp) {
+                if (oc.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
+                const bool caller_buffer = on_device || (out && *out);
+                if (caller_buffer && conf_io->num < oc.num)
+                    throw Fail{FAZ_ERR_ARG, "output buffer holds fewer values than the stream's field"};
+                init_pool_once();
+                StreamGuard sg(user_stream, false, on_device ? NullStream::Default : NullStream::Library);
+                DevMem m(sg.st);
+                T *dOut = on_device ? (T *)dOutUser : m.alloc<T>(oc.num);
+                if (!dOut) throw Fail{FAZ_ERR_ARG, "null output"};
+                decompress_omp<T>(oc, cmp, cmp_size - 4 - (size_t)cs, dOut, sg.st, tm);
+                if (!on_device) {
+                    if (!out) throw Fail{FAZ_ERR_ARG, "null output"};
+                    const bool alloc = *out == nullptr;
+                    T *h = alloc ? (T *)std::malloc(oc.num * sizeof(T)) : (T *)*out;
+                    if (!h) throw Fail{FAZ_ERR_ARG, "out of host memory"};
+                    Events ev_d2h;
+                    CK(cudaEventRecord(ev_d2h.a, sg.st));
+                    cudaError_t e = cudaMemcpyAsync(h, dOut, oc.num * sizeof(T), cudaMemcpyDeviceToHost, sg.st);
+                    if (e == cudaSuccess) e = cudaEventRecord(ev_d2h.b, sg.st);
+                    if (e == cudaSuccess) e = cudaStreamSynchronize(sg.st);
+                    if (e != cudaSuccess) {
+                        if (alloc) std::free(h);
+                        throw Fail{FAZ_ERR_CUDA, std::string("device to host copy: ") + cudaGetErrorString(e)};
+                    }
+                    tm.d2h_ms = ev_d2h.ms();
+                    *out = h;
+                } else {
+                    CK(cudaStreamSynchronize(sg.st));
+                }
+                *conf_io = oc;
+                tm.total_ms = ms_since(t0);
+                if (tmo) *tmo = tm;
+                return FAZ_OK;
+            }
+        }
         // a caller-provided output holds conf->num values
         const uint64_t cap = conf_io->num;
         const bool caller_buffer = on_device || (out && *out);
@@ -1324,6 +1486,63 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
     tm.total_ms = ms_since(t0);
     if (tmo) *tmo = tm;
     return FAZ_OK;
+}
+
+// SZ_decompress_OMP: nThreads, the slabs' Configs and sizes, then every slab
+// decompressed as a field of its own into its rows of dOut.  body: the
+// stream's bytes before the field's Config.
+template <typename T>
+void decompress_omp(const faz_config &c, const char *cmp, size_t body, T *dOut, cudaStream_t st, faz_timings &tm) {
+    const uint8_t *p = (const uint8_t *)cmp, *end = p + body;
+    if (body < 4) throw Fail{FAZ_ERR_FORMAT, "truncated OpenMP stream"};
+    int32_t nt;
+    std::memcpy(&nt, p, 4);
+    p += 4;
+    if (nt < 1 || (uint64_t)nt > c.dims[0]) throw Fail{FAZ_ERR_FORMAT, "bad OpenMP slab count"};
+    std::vector<const uint8_t *> cp(nt);
+    std::vector<size_t> cl(nt);
+    for (int t = 0; t < nt; t++) {
+        faz_config ct;
+        size_t used = 0;
+        if (config_load(ct, p, (size_t)(end - p), &used)) throw Fail{FAZ_ERR_FORMAT, "bad slab Config"};
+        cp[t] = p;
+        cl[t] = used;
+        p += used;
+    }
+    if ((size_t)(end - p) < (size_t)nt * 8) throw Fail{FAZ_ERR_FORMAT, "truncated OpenMP stream"};
+    std::vector<uint64_t> sz(nt);
+    for (int t = 0; t < nt; t++) {
+        std::memcpy(&sz[t], p, 8);
+        p += 8;
+    }
+    uint64_t base = 1;
+    for (int i = 1; i < c.N; i++) base *= c.dims[i];
+    std::vector<uint8_t> one;
+    for (int t = 0; t < nt; t++) {
+        if ((uint64_t)(end - p) < sz[t]) throw Fail{FAZ_ERR_FORMAT, "truncated OpenMP slab"};
+        uint64_t lo, hi;
+        omp_slab_rows(c.dims[0], t, nt, lo, hi);
+        // the slab as a stream of its own: its bytes, its Config, the Config's size
+        one.assign(p, p + sz[t]);
+        one.insert(one.end(), cp[t], cp[t] + cl[t]);
+        const int32_t cs = (int32_t)cl[t];
+        one.insert(one.end(), (const uint8_t *)&cs, (const uint8_t *)&cs + 4);
+        p += sz[t];
+        faz_config ct;
+        std::memset(&ct, 0, sizeof(ct));
+        ct.num = (hi - lo) * base;
+        faz_timings t2;
+        std::memset(&t2, 0, sizeof(t2));
+        const int rc = decompress_impl<T>(&ct, (const char *)one.data(), one.size(), nullptr, true, dOut + lo * base, st,
+                                          &t2, true);
+        if (rc) throw Fail{rc, std::string("slab ") + std::to_string(t) + ": " + last_error()};
+        if (ct.num != (hi - lo) * base) throw Fail{FAZ_ERR_FORMAT, "slab extents differ from the field's split"};
+        tm.gpu_ms += t2.gpu_ms;
+        tm.zstd_ms += t2.zstd_ms;
+        tm.payload_bytes += t2.payload_bytes;
+        tm.unpred_count += t2.unpred_count;
+        tm.kernel_launches += t2.kernel_launches;
+    }
 }
 
 template <typename T>

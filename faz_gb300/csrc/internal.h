@@ -153,7 +153,8 @@ constexpr int kLutBits = 12;
 
 // -------------------------------------------------------------- stream/io
 void config_save(const faz_config &c, std::vector<uint8_t> &out);
-int config_load(faz_config &c, const uint8_t *p, size_t n);
+// used (optional): bytes the Config occupies
+int config_load(faz_config &c, const uint8_t *p, size_t n, size_t *used = nullptr);
 int config_init(faz_config *c, int N, const uint64_t *dims);
 int config_load_ini(faz_config *c, const char *path, std::string &err);
 

@@ -286,7 +286,7 @@ void config_save(const faz_config &c, std::vector<uint8_t> &o) {
 }
 
 // QoZ::Config::load (include/QoZ/utils/Config.hpp:311-388)
-int config_load(faz_config &c, const uint8_t *p, size_t n) {
+int config_load(faz_config &c, const uint8_t *p, size_t n, size_t *used) {
     Reader r{p, n};
     faz_config t;
     std::memset(&t, 0, sizeof(t));
@@ -355,6 +355,7 @@ int config_load(faz_config &c, const uint8_t *p, size_t n) {
     t.verbose = 1;
     t.wavelet_rel_coeff = 0.75;
     c = t;
+    if (used) *used = r.pos;
     return FAZ_OK;
 }
 

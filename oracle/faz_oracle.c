@@ -1366,6 +1366,24 @@ int orc_read_stream(const uint8_t *cmp, size_t cmp_size, faz_config *conf, uint8
     return 0;
 }
 
+/* Config::save / Config::load bytes (include/QoZ/utils/Config.hpp:240-388),
+ * for the OpenMP stream container */
+int orc_config_save(const faz_config *conf, uint8_t **out, size_t *out_size) {
+    bytes_t b = {0};
+    conf_save(conf, &b);
+    *out = b.p;
+    *out_size = b.n;
+    return 0;
+}
+
+int orc_config_load(const uint8_t *p, size_t n, faz_config *conf, size_t *used) {
+    rd_t r = {p, n, 0, 0};
+    memset(conf, 0, sizeof *conf);
+    if (conf_load(conf, &r)) { set_err("bad Config"); return -4; }
+    *used = r.pos;
+    return 0;
+}
+
 /* SZ_decompress<T> / SZInterpolationCompressor::decompress (lines 42-199) */
 int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, faz_config *conf_out) {
     faz_config conf;

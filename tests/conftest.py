@@ -35,13 +35,16 @@ def pytest_collection_modifyitems(config, items):
             it.add_marker(skip)
 
 
-def golden_manifest():
+def golden_manifest(omp=False):
+    """The golden cases; OpenMP streams (slab containers, "omp_threads" in
+    the manifest) only with omp=True."""
     with open(os.path.join(GOLDEN, "manifest.json")) as f:
-        return json.load(f)["cases"]
+        cases = json.load(f)["cases"]
+    return [c for c in cases if omp or "omp_threads" not in c]
 
 
 def golden_case(name):
-    for c in golden_manifest():
+    for c in golden_manifest(omp=True):
         if c["name"] == name:
             return c
     raise KeyError(name)
@@ -87,6 +90,8 @@ def cli_config(case):
         a = cp["AlgoSettings"] if cp.has_section("AlgoSettings") else {}
         if "CmprAlgo" in g:
             conf.cmprAlgo = ALGO_STR.index(g["CmprAlgo"])
+        if "OpenMP" in g:
+            conf.openmp = 1 if g["OpenMP"].strip().lower() in ("true", "yes", "on", "1") else 0
         if "InterpolationAlgo" in a:
             conf.interpAlgo = INTERP_ALGO_STR.index(a["InterpolationAlgo"])
         for k, f in _INI_INT.items():
@@ -184,3 +189,20 @@ def mask_first_size(stream):
     N = stream[t0]
     a, b = 102 + 8 * N, 110 + 8 * N
     return stream[:t0 + a] + b"\0" * (b - a) + stream[t0 + b:]
+
+
+def mask_omp(stream):
+    """An OpenMP stream with the firstSize bytes of every Config (the slabs'
+    and the field's) zeroed."""
+    import oracle.oracle as O
+    conf, slabs = O.read_omp(stream)
+    n = len(slabs)
+    parts, confs = [], []
+    for _, s in slabs:
+        s = mask_first_size(s)
+        (cs,) = struct.unpack_from("<i", s, len(s) - 4)
+        parts.append(s[:len(s) - 4 - cs])
+        confs.append(s[len(s) - 4 - cs:len(s) - 4])
+    body = struct.pack("<i", n) + b"".join(confs) + b"".join(struct.pack("<Q", len(p)) for p in parts) + b"".join(parts)
+    (cs,) = struct.unpack_from("<i", stream, len(stream) - 4)
+    return body + mask_first_size(stream[len(stream) - 4 - cs:])

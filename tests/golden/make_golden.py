@@ -156,6 +156,15 @@ def cases():
     out.append(("rate_label_ini_1e3", spectral_field((64, 96, 80), slope=-3.0, seed=84), ["-M", "REL", "1e-3"],
                 label_ini))
     out.append(("rate_label_ini_lorenzo", sum2d((64, 72, 80), 1e-4, 85), ["-M", "REL", "1e-3"], label_ini))
+    # OpenMP streams (OpenMP = YES): slabs along the slowest axis, one per
+    # OpenMP thread (OMP_THREADS below)
+    out.append(("omp_interp_3", spectral_field((40, 48, 56), slope=-3.0, seed=86), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP", "OpenMP": "YES"},
+                 "AlgoSettings": {"InterpolationAlgo": "INTERP_ALGO_CUBIC"}}))
+    out.append(("omp_default_4", spectral_field((64, 80, 96), slope=-3.0, seed=87), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"OpenMP": "YES"}, "AlgoSettings": {}}))
+    out.append(("omp_abs2d_5", spectral_field((300, 200), slope=-2.5, seed=88), ["-M", "ABS", "0.05"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP", "OpenMP": "YES"}, "AlgoSettings": {}}))
     out.append(("rate_ab_only", spectral_field((48, 56, 64), slope=-3.0, seed=82), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01"}}))
     out.append(("rate_2d", spectral_field((400, 500), slope=-3.0, seed=83), ["-M", "REL", "5e-3"],
@@ -182,6 +191,10 @@ def sum2d(shape, noise, seed, dtype=np.float32):
     h = rng.standard_normal((shape[0], 1, shape[2]))
     base = f + g + h
     return (base + noise * rng.standard_normal(shape) * (base.max() - base.min())).astype(dtype)
+
+
+# OpenMP thread count of the reference run (the stream's slab count)
+OMP_THREADS = {"omp_interp_3": 3, "omp_default_4": 4, "omp_abs2d_5": 5}
 
 
 def write_ini(path, d):
@@ -226,14 +239,20 @@ def main(only=None):
                 ip = os.path.join(td, "cfg.ini")
                 write_ini(ip, ini)
                 cmd += ["-c", ip]
-            subprocess.check_call(cmd, cwd=td, stdout=subprocess.DEVNULL)
+            env = dict(os.environ)
+            if name in OMP_THREADS:
+                env["OMP_NUM_THREADS"] = str(OMP_THREADS[name])
+            subprocess.check_call(cmd, cwd=td, stdout=subprocess.DEVNULL, env=env)
             dcmd = [FAZ, dt, "-z", os.path.join(HERE, name + ".faz"), "-o", os.path.join(HERE, name + ".dec")] + \
                 cli_dims + ["-M", "ABS", "1"]
             subprocess.check_call(dcmd, cwd=td, stdout=subprocess.DEVNULL)
         decp = os.path.join(HERE, name + ".dec")
-        manifest.append({"name": name, "dtype": str(arr.dtype), "dims": dims, "flags": flags, "ini": ini,
-                         "sha256": {ext: sha(os.path.join(HERE, name + ext)) for ext in (".in", ".faz")},
-                         "dec_sha256": sha(decp)})
+        entry = {"name": name, "dtype": str(arr.dtype), "dims": dims, "flags": flags, "ini": ini,
+                 "sha256": {ext: sha(os.path.join(HERE, name + ext)) for ext in (".in", ".faz")},
+                 "dec_sha256": sha(decp)}
+        if name in OMP_THREADS:
+            entry["omp_threads"] = OMP_THREADS[name]
+        manifest.append(entry)
         os.remove(decp)
         print(name, os.path.getsize(os.path.join(HERE, name + ".faz")))
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
