@@ -9,6 +9,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <future>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -184,6 +185,70 @@ class HostPool {
     std::mutex mu_;
     std::condition_variable cv_;
     std::deque<std::function<void()>> q_;
+    std::vector<std::thread> th_;
+    bool stop_ = false;
+};
+
+// Persistent host threads for the tuner's concurrent trials.  A trial on a
+// fresh thread would allocate its thread-local pinned staging buffers anew
+// (and free them when the thread ends, which synchronises the device); these
+// threads keep them for the process.  A task runs with the submitting
+// thread's device current.  (Each trial still creates its own stream: a
+// stream kept by the worker from call to call measured slower.)
+class TaskThreads {
+  public:
+    static TaskThreads &get() {
+        static TaskThreads pool;
+        return pool;
+    }
+    template <typename R>
+    std::future<R> submit(std::function<R()> f) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        auto task = std::make_shared<std::packaged_task<R()>>(std::move(f));
+        std::future<R> fut = task->get_future();
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            q_.push_back(Job{dev, [task] { (*task)(); }});
+        }
+        cv_.notify_one();
+        return fut;
+    }
+    ~TaskThreads() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+
+  private:
+    struct Job {
+        int dev;
+        std::function<void()> fn;
+    };
+    static constexpr int kThreads = 8;
+    TaskThreads() {
+        for (int i = 0; i < kThreads; i++)
+            th_.emplace_back([this] {
+                for (;;) {
+                    Job job;
+                    {
+                        std::unique_lock<std::mutex> lk(mu_);
+                        cv_.wait(lk, [this] { return stop_ || !q_.empty(); });
+                        if (stop_ && q_.empty()) return;
+                        job = std::move(q_.front());
+                        q_.pop_front();
+                    }
+                    cudaSetDevice(job.dev);
+                    job.fn();
+                }
+            });
+    }
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<Job> q_;
     std::vector<std::thread> th_;
     bool stop_ = false;
 };

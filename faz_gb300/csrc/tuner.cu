@@ -364,7 +364,7 @@ struct Trial {
     double host_ms = 0;
     template <typename F>
     void start(cudaEvent_t ready, F body) {
-        size = std::async(std::launch::async, [this, ready, body]() -> size_t {
+        size = TaskThreads::get().submit<size_t>([this, ready, body]() -> size_t {
             std::vector<uint8_t> pl;
             bool reported = false;
             size_t early = 0;
@@ -400,6 +400,11 @@ struct Trial {
         });
     }
     size_t get() { return size.get(); }
+    // a trial still running holds references to this object and the caller's
+    // buffers: wait for it (as a std::async future would)
+    ~Trial() {
+        if (size.valid()) size.wait();
+    }
 };
 
 template <typename T>
