@@ -344,10 +344,10 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
 template <typename T>
 int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);
 // The QoZ tuner's Lorenzo candidate: CompressTest(ALGO_LORENZO_REG) of nblk
-// sampled 3-D blocks of bsz^3 points (bit rate, PSNR).
+// sampled 2-D / 3-D blocks of bsz^N points (bit rate, PSNR).
 template <typename T>
-void lorenzo_compress_test(const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng, cudaStream_t st,
-                           Counter &launches, double &bitrate, double &psnr);
+void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng,
+                           cudaStream_t st, Counter &launches, double &bitrate, double &psnr);
 // Lorenzo settings once the QoZ tuner has chosen Lorenzo (sampling, the
 // quantisation-interval estimate, pred_dim and 16384-bin trials).
 template <typename T>

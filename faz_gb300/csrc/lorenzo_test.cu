@@ -3,10 +3,10 @@
 // Reference: CompressTest with ALGO_LORENZO_REG and the RD target
 // (include/QoZ/api/impl/SZInterp.hpp:1131-1392, called from 2428-2486).  One
 // general compressor - SZGeneralFrontend with ComposedPredictor over
-// LorenzoPredictor<T,3,1> and LorenzoPredictor<T,3,2> (block size 5), a
+// LorenzoPredictor<T,N,1> and LorenzoPredictor<T,N,2> (block size 5), a
 // LinearQuantizer with radius 65536, HuffmanEncoder<int>, Lossless_zstd
 // (make_lorenzo_regression_compressor, include/QoZ/api/impl/SZLorenzoReg.hpp:
-// 28-90) - compresses every sampled block of (sbs+1)^3 points in turn with
+// 28-90) - compresses every sampled block of (sbs+1)^N points in turn with
 // tuning = 1, so its codes, block selections and unpredictable values
 // accumulate across the blocks; encoding_lossless then writes one payload
 // (include/QoZ/compressor/SZGeneralCompressor.hpp:45-91) whose zstd-framed
@@ -163,6 +163,93 @@ __global__ void __launch_bounds__(kWarps * 32)
     }
 }
 
+// LorenzoPredictor<T,2,L>::do_predict (LorenzoPredictor.hpp:123-128, 189-195)
+// on a 2-D tile of row stride kTe
+template <typename T>
+__device__ __forceinline__ T pred2(const T *p, int L) {
+#define Q(a, b) p[-((a) * kTe + (b))]
+    if (L == 1) return Q(0, 1) + Q(1, 0) - Q(1, 1);
+    return 2 * Q(0, 1) - Q(0, 2) + 2 * Q(1, 0) - 4 * Q(1, 1) + 2 * Q(1, 2) - Q(2, 0) + 2 * Q(2, 1) - Q(2, 2);
+#undef Q
+}
+
+template <typename T>
+__device__ __forceinline__ T est2(const T *p, int L, T noise) {
+    const T d = *p - pred2(p, L);
+    return (T)(fabs((double)d) + (double)noise);
+}
+
+// The 2-D form: one sub-block diagonal bi + bj = d of every sampled block
+// (blockIdx.y), a warp per 5 x 5 sub-block, anti-diagonals of points inside.
+template <typename T>
+__global__ void __launch_bounds__(kWarps * 32)
+    k_lor_test_diag2(TestArgs a, int64_t d, const T *__restrict__ X, T *__restrict__ R, int *__restrict__ codes,
+                     T *__restrict__ scratch, int *__restrict__ sel, T *__restrict__ sq) {
+    __shared__ T tiles[kWarps][kTe * kTe];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t bi = (int64_t)blockIdx.x * kWarps + w, bj = d - bi;
+    if (bi >= a.nb || bj < 0 || bj >= a.nb) return;
+    const int64_t D = a.D, blk = blockIdx.y;
+    const int64_t i0 = bi * kBs, j0 = bj * kBs;
+    const int sx = i0 + kBs < D ? kBs : (int)(D - i0);
+    const int sy = j0 + kBs < D ? kBs : (int)(D - j0);
+    const T *Xb = X + blk * a.per;
+    T *Rb = R + blk * a.per;
+    T *t = tiles[w];
+    for (int e = lane; e < kTe * kTe; e += 32) {
+        const int i = e / kTe, j = e - i * kTe;
+        T v = 0;
+        if (i < sx + 2 && j < sy + 2) {
+            const int64_t gi = i0 + i - 2, gj = j0 + j - 2;
+            if (i >= 2 && j >= 2) v = Xb[gi * D + gj];
+            else if (gi >= 0 && gj >= 0) v = Rb[gi * D + gj];
+        }
+        t[e] = v;
+    }
+    __syncwarp();
+    // ComposedPredictor::precompress_block: the two diagonals of the leading square
+    int s1 = 0;
+    if (lane == 0) {
+        const int m = sx < sy ? sx : sy;
+        const T n1 = (T)a.noise1, n2 = (T)a.noise2;
+        double e1 = 0, e2 = 0;
+        for (int q = 0; q + 2 < m; q++) {
+            const T *p1 = t + (q + 2) * kTe + (q + 2);
+            const T *p2 = t + (q + 2) * kTe + (m - 1 - q + 2);
+            e1 += (double)est2(p1, 1, n1);
+            e1 += (double)est2(p2, 1, n1);
+            e2 += (double)est2(p1, 2, n2);
+            e2 += (double)est2(p2, 2, n2);
+        }
+        s1 = e2 < e1 ? 1 : 0;
+        sel[(blk * a.nb + bi) * a.nb + bj] = s1;
+    }
+    const int L = __shfl_sync(0xffffffffu, s1, 0) + 1;
+    const uint64_t boff = (uint64_t)(blk * a.per + i0 * D + j0 * sx);
+    for (int s = 0; s < sx + sy - 1; s++) {
+        for (int i = lane; i < sx; i += 32) {
+            const int j = s - i;
+            if (j < 0 || j >= sy) continue;
+            T *c = t + (i + 2) * kTe + (j + 2);
+            const T pred = pred2(c, L);
+            const T orig = *c;
+            T v = orig, uval;
+            const int code = quantize<T>(v, pred, a.eb, a.recip, kRadius, 0, uval);
+            const uint64_t pos = boff + (uint64_t)(i * sy + j);
+            codes[pos] = code;
+            if (code == 0) scratch[pos] = uval;
+            *c = v;
+            const T diff = orig - v;
+            sq[blk * a.per + (i0 + i) * D + (j0 + j)] = diff * diff;
+        }
+        __syncwarp();
+    }
+    for (int e = lane; e < sx * sy; e += 32) {
+        const int i = e / sy, j = e - i * sy;
+        Rb[(i0 + i) * D + (j0 + j)] = t[(i + 2) * kTe + (j + 2)];
+    }
+}
+
 // ---------------------------------------------------- 32-bit Huffman codes
 // Symbol counts and first positions; lanes holding the same symbol combine
 // (the lowest lane has the smallest position).
@@ -299,28 +386,38 @@ void huffman_i32(const int *codes, uint64_t n, int nsym, DevMem &m, cudaStream_t
 }  // namespace
 
 // CompressTest(ALGO_LORENZO_REG, TUNING_TARGET_RD) on nblk sampled blocks of
-// bsz^3 points (dBlocks, block after block, row-major): bit rate of the one
+// bsz^N points (N = 2 or 3) (dBlocks, block after block, row-major): bit rate of the one
 // payload the general compressor writes and PSNR of the reconstructions.
 template <typename T>
-void lorenzo_compress_test(const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng, cudaStream_t st,
-                           Counter &launches, double &bitrate, double &psnr) {
+void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng,
+                           cudaStream_t st, Counter &launches, double &bitrate, double &psnr) {
+    if (N != 2 && N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "the Lorenzo candidate covers 2-D and 3-D data"};
     TestArgs a;
     a.D = bsz;
     a.nb = (bsz - 1) / kBs + 1;
-    a.per = bsz * bsz * bsz;
+    a.per = N == 3 ? bsz * bsz * bsz : bsz * bsz;
     a.eb = eb;
     a.recip = 1.0 / eb;
-    a.noise1 = 1.22 * eb;
-    a.noise2 = 6.8 * eb;
+    a.noise1 = (N == 3 ? 1.22 : 0.81) * eb;
+    a.noise2 = (N == 3 ? 6.8 : 2.76) * eb;
     if (nblk > 65535) throw Fail{FAZ_ERR_UNSUPPORTED, "too many sampled blocks for the Lorenzo trial"};
-    const uint64_t n = nblk * (uint64_t)a.per, nsel = nblk * (uint64_t)(a.nb * a.nb * a.nb);
+    const uint64_t nsub = N == 3 ? (uint64_t)(a.nb * a.nb * a.nb) : (uint64_t)(a.nb * a.nb);
+    const uint64_t n = nblk * (uint64_t)a.per, nsel = nblk * nsub;
     DevMem m(st);
     T *R = m.alloc<T>(n), *scratch = m.alloc<T>(n), *sq = m.alloc<T>(n);
     int *codes = m.alloc<int>(n), *sel = m.alloc<int>(nsel);
-    const dim3 grid((unsigned)((a.nb * a.nb + kWarps - 1) / kWarps), (unsigned)nblk);
-    for (int64_t d = 0; d <= 3 * (a.nb - 1); d++) {
-        k_lor_test_diag<T><<<grid, kWarps * 32, 0, st>>>(a, d, dBlocks, R, codes, scratch, sel, sq);
-        launches(cudaGetLastError());
+    if (N == 3) {
+        const dim3 grid((unsigned)((a.nb * a.nb + kWarps - 1) / kWarps), (unsigned)nblk);
+        for (int64_t d = 0; d <= 3 * (a.nb - 1); d++) {
+            k_lor_test_diag<T><<<grid, kWarps * 32, 0, st>>>(a, d, dBlocks, R, codes, scratch, sel, sq);
+            launches(cudaGetLastError());
+        }
+    } else {
+        const dim3 grid((unsigned)((a.nb + kWarps - 1) / kWarps), (unsigned)nblk);
+        for (int64_t d = 0; d <= 2 * (a.nb - 1); d++) {
+            k_lor_test_diag2<T><<<grid, kWarps * 32, 0, st>>>(a, d, dBlocks, R, codes, scratch, sel, sq);
+            launches(cudaGetLastError());
+        }
     }
     Huff32 hs, hc;
     huffman_i32(sel, nsel, 2, m, st, launches, hs);
@@ -334,7 +431,7 @@ void lorenzo_compress_test(const T *dBlocks, uint64_t nblk, int64_t bsz, double 
     // SZGeneralFrontend::save (dims, block size, predictors with the
     // selections, LinearQuantizer::save), then the codes
     std::vector<uint8_t> h0;
-    for (int i = 0; i < 3; i++) put<uint64_t>(h0, (uint64_t)bsz);
+    for (int i = 0; i < N; i++) put<uint64_t>(h0, (uint64_t)bsz);
     put<uint32_t>(h0, (uint32_t)kBs);
     put<uint8_t>(h0, 1);
     put<uint8_t>(h0, 1);
@@ -373,9 +470,9 @@ void lorenzo_compress_test(const T *dBlocks, uint64_t nblk, int64_t bsz, double 
     psnr = 20 * std::log10(rng) - 10 * std::log10(se / ele);
 }
 
-template void lorenzo_compress_test<float>(const float *, uint64_t, int64_t, double, double, cudaStream_t, Counter &,
-                                           double &, double &);
-template void lorenzo_compress_test<double>(const double *, uint64_t, int64_t, double, double, cudaStream_t,
+template void lorenzo_compress_test<float>(int, const float *, uint64_t, int64_t, double, double, cudaStream_t,
+                                           Counter &, double &, double &);
+template void lorenzo_compress_test<double>(int, const double *, uint64_t, int64_t, double, double, cudaStream_t,
                                             Counter &, double &, double &);
 
 }  // namespace faz

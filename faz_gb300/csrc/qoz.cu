@@ -469,8 +469,6 @@ int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     // without QoZ the tuner runs from the configuration's own rates
     // (predictorTuningRate in (0, 1)); these variants are not implemented
     if (c.profiling) throw Fail{FAZ_ERR_UNSUPPORTED, "profiling-driven block sampling is not implemented"};
-    if (c.testLorenzo && N != 3)
-        throw Fail{FAZ_ERR_UNSUPPORTED, "the tuner's Lorenzo candidate (testLorenzo) is implemented for 3-D data"};
     if (!(c.autoTuningRate > 0))
         throw Fail{FAZ_ERR_UNSUPPORTED, "rate-driven tuning without autoTuningRate is not implemented"};
     int max_interp_level = -1;
@@ -726,7 +724,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             // the Lorenzo candidate: CompressTest with ALGO_LORENZO_REG
             // against the best alpha/beta point (SZInterp.hpp:2428-2486)
             double br, mm;
-            lorenzo_compress_test<T>(blocks, nblk, bsz, oriabseb, c.rng, st, launches, br, mm);
+            lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb, c.rng, st, launches, br, mm);
             if (mm >= bestm && br <= bestb) {
                 bestb = br;
                 bestm = mm;
@@ -737,7 +735,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             } else {
                 const double fix = br / bestb;
                 double br2, m2;
-                lorenzo_compress_test<T>(blocks, nblk, bsz, oriabseb * fix, c.rng, st, launches, br2, m2);
+                lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb * fix, c.rng, st, launches, br2, m2);
                 const double a = (mm - m2) / (br - br2);
                 if (a > 0) {
                     const double b = mm - a * br;

@@ -156,6 +156,9 @@ def cases():
     out.append(("rate_label_ini_1e3", spectral_field((64, 96, 80), slope=-3.0, seed=84), ["-M", "REL", "1e-3"],
                 label_ini))
     out.append(("rate_label_ini_lorenzo", sum2d((64, 72, 80), 1e-4, 85), ["-M", "REL", "1e-3"], label_ini))
+    out.append(("rate_2d_lorenzo", sum1d((300, 400), 1e-4, 89), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                                        "testLorenzo": "1"}}))
     # OpenMP streams (OpenMP = YES): slabs along the slowest axis, one per
     # OpenMP thread (OMP_THREADS below)
     out.append(("omp_interp_3", spectral_field((40, 48, 56), slope=-3.0, seed=86), ["-M", "REL", "1e-3"],

@@ -93,19 +93,26 @@ def test_gpu_rate_tuning_matches_oracle(dims, rel, dtype, levelwise, max_step):
     assert mask_first_size(stream) == mask_first_size(ref)
 
 
-def test_gpu_rate_tuning_rejects_2d_lorenzo_candidate():
-    """testLorenzo on 2-D data at a relative bound <= 1e-3 needs the 2-D
-    general frontend over the sampled blocks, which the GPU path does not
-    build: the call fails loudly."""
-    dims = (300, 420)
-    conf = F.Config(*dims)
-    conf.errorBoundMode = F.EB_REL
-    conf.relErrorBound = 1e-3
-    conf.autoTuningRate = conf.predictorTuningRate = 0.01
-    conf.testLorenzo = 1
-    x = spectral_field(dims, slope=-3.0, seed=5)
-    with pytest.raises(F.FazError, match="UNSUPPORTED|Lorenzo"):
-        F.SZ_compress(conf, x)
+def test_gpu_2d_lorenzo_candidate_matches_oracle():
+    """testLorenzo on 2-D data: the 2-D general frontend over the sampled
+    blocks; a sum of 1-D functions selects Lorenzo."""
+    dims = (300, 400)
+    rng = np.random.default_rng(7)
+    base = np.cumsum(rng.standard_normal((dims[0], 1)), 0) + np.cumsum(rng.standard_normal((1, dims[1])), 1)
+    for x in (base.astype(np.float32), spectral_field(dims, slope=-2.5, noise=0.05, seed=5)):
+        conf = F.Config(*dims)
+        conf.errorBoundMode = F.EB_REL
+        conf.relErrorBound = 1e-3
+        conf.autoTuningRate = conf.predictorTuningRate = 0.01
+        conf.testLorenzo = 1
+        stream = F.SZ_compress(conf, x)
+        ref, ref_payload = O.compress(conf, x)
+        c1, p = O.read_stream(stream)
+        c2, _ = O.read_stream(ref)
+        assert (c1.cmprAlgo, c1.alpha, c1.beta, c1.blockSize, c1.quantbinCnt) == \
+            (c2.cmprAlgo, c2.alpha, c2.beta, c2.blockSize, c2.quantbinCnt)
+        assert p == ref_payload
+    assert c1.cmprAlgo == 2 and O.read_stream(F.SZ_compress(conf, base.astype(np.float32)))[0].cmprAlgo == 0
 
 
 def _sum_of_planes(shape, noise, seed, dtype):
