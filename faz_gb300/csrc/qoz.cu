@@ -469,8 +469,7 @@ int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     // without QoZ the tuner runs from the configuration's own rates
     // (predictorTuningRate in (0, 1)); these variants are not implemented
     if (c.profiling) throw Fail{FAZ_ERR_UNSUPPORTED, "profiling-driven block sampling is not implemented"};
-    if (!(c.autoTuningRate > 0))
-        throw Fail{FAZ_ERR_UNSUPPORTED, "rate-driven tuning without autoTuningRate is not implemented"};
+    if (c.autoTuningRate < 0) throw Fail{FAZ_ERR_UNSUPPORTED, "a negative autoTuningRate is not implemented"};
     int max_interp_level = -1;
     for (int i = 0; i < N; i++) {
         const int l = (int)std::ceil(std::log2((double)c.dims[i]));
@@ -569,10 +568,10 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     // CompressTest (SZInterp.hpp:1130-1392) of every sampled block: bit rate
     // after Huffman + zstd, PSNR from the summed squared errors
     std::vector<std::pair<int64_t, int64_t>> ranges;
-    auto compress_test = [&](int op, int dir, double alpha, double beta, double eb, double &bitrate,
-                             double &psnr) {
+    auto compress_test = [&](int op, int dir, double alpha, double beta, double eb, double &bitrate, double &psnr,
+                             bool lists = true) {
         CK(cudaMemcpyAsync(work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, st));
-        QzRun R{1, g.levels, 0, eb, alpha, beta, c.trimToZero, op, dir, &il, &dl};
+        QzRun R{1, g.levels, 0, eb, alpha, beta, c.trimToZero, op, dir, lists ? &il : nullptr, lists ? &dl : nullptr};
         qz_run<T>(g, R, work, codes, scratch, err, nblk, sp, &ranges, st, launches);
         const double se = block_sums(sp);
         // q_bins: level ranges from the coarsest, each across all blocks
@@ -630,6 +629,16 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         bitrate = 8 * (double)zstd_framed_size_host(pl.data(), pl.size()) / ele;
         psnr = 20 * std::log10(c.rng) - 10 * std::log10(se / ele);
     };
+    // without the alpha/beta search (autoTuningRate = 0) the decisions
+    // compare compression ratios of CompressTests (TUNING_TARGET_CR)
+    const bool cr_tests = c.autoTuningRate == 0;
+    double best_lorenzo_ratio = 0, best_interp_cr = 0;
+    if (c.testLorenzo && cr_tests) {
+        // SZInterp.hpp:1925-1932
+        double br, mm;
+        lorenzo_compress_test<T>(N, blocks, nblk, bsz, c.absErrorBound, c.rng, st, launches, br, mm);
+        best_lorenzo_ratio = sizeof(T) * 8.0 / br;
+    }
     if (Lsel > 0) {
         // per-level selection by summed prediction loss (tuning mode 2)
         for (int level = Lsel; level > 0; level--) {
@@ -657,6 +666,14 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         // the candidate loop leaves its last candidate in the configuration
         c.interpAlgo = FAZ_INTERP_ALGO_CUBIC;
         c.interpDirection = (uint8_t)dirs[1];
+        if (cr_tests) {
+            // CompressTest of the Config as the loop leaves it: its last
+            // candidate on every level, the lists not yet in the Config
+            // (SZInterp.hpp:2020-2032)
+            double br, mm;
+            compress_test(FAZ_INTERP_ALGO_CUBIC, dirs[1], c.alpha, c.beta, c.absErrorBound, br, mm, false);
+            best_interp_cr = sizeof(T) * 8.0 / br;
+        }
     } else {
         // one interpolator and direction for every level, by the compression
         // ratio of a CompressTest per candidate (SZInterp.hpp:2036-2076)
@@ -675,10 +692,12 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             }
         c.interpAlgo = best_op;
         c.interpDirection = (uint8_t)best_dir;
+        if (cr_tests) best_interp_cr = best_cr;
     }
     c.alpha = o_alpha;
     c.beta = o_beta;
-    bool use_interp = true;
+    // SZInterp.hpp:2083
+    bool use_interp = best_interp_cr >= best_lorenzo_ratio || best_lorenzo_ratio >= 80 || best_interp_cr >= 80;
     if (c.autoTuningRate > 0) {
         // B-M tuning (SZInterp.hpp:2187-2515): CompressTest per alpha/beta
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;

@@ -884,8 +884,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         conf->pyBind = 0;
         conf->sperrWithoutWave = 0;
     }
-    if (conf->profiling || !(conf->autoTuningRate > 0)) {
-        set_err("oracle QoZ-branch tuner covers autoTuningRate > 0 without profiling");
+    if (conf->profiling || conf->autoTuningRate < 0) {
+        set_err("oracle QoZ-branch tuner covers autoTuningRate >= 0 without profiling");
         return -2;
     }
     int max_interp_level = -1;
@@ -917,6 +917,19 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                       ? qoz_sample_f32((const float *)data, N, gdims, sbs, conf->predictorTuningRate, (float **)&blocks)
                       : qoz_sample_f64((const double *)data, N, gdims, sbs, conf->predictorTuningRate, (double **)&blocks);
     double o_alpha = conf->alpha, o_beta = conf->beta;
+    /* without the alpha/beta search the decisions compare compression ratios
+     * of CompressTests (TUNING_TARGET_CR) */
+    const int cr_tests = conf->autoTuningRate == 0;
+    double best_lorenzo_ratio = 0, best_interp_cr = 0;
+    if (conf->testLorenzo && cr_tests) {
+        /* SZInterp.hpp:1925-1932 */
+        double br, m;
+        int rc = dtype == FAZ_FLOAT
+                     ? gen_test_f32((const float *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, &br, &m)
+                     : gen_test_f64((const double *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, &br, &m);
+        if (rc) { free(blocks); return rc; }
+        best_lorenzo_ratio = (double)es * 8.0 / br;
+    }
     if (conf->autoTuningRate > 0) {
         /* setABwithRelBound(rel_bound, 0) (SZInterp.hpp:1394-1420) */
         double a, b;
@@ -969,6 +982,21 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         free(work);
         free(q32.unpred);
         free(q64.unpred);
+        if (cr_tests) {
+            /* CompressTest of the Config as the loop leaves it: its last
+             * candidate on every level, the lists not yet in the Config
+             * (SZInterp.hpp:2020-2032) */
+            orc_params p = {1, dirs[1], conf->interpBlockSize, conf->fixBlockSize, conf->alpha, conf->beta, 0, NULL,
+                            NULL};
+            double br, m;
+            int rc = dtype == FAZ_FLOAT
+                         ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
+                                                 conf->trimToZero, conf->maxStep, conf->rng, &br, &m)
+                         : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
+                                                 conf->trimToZero, conf->maxStep, conf->rng, &br, &m);
+            if (rc) { free(blocks); return rc; }
+            best_interp_cr = (double)es * 8.0 / br;
+        }
     } else {
         /* one interpolator and direction for every level, by the compression
          * ratio of a CompressTest per candidate (SZInterp.hpp:2036-2076) */
@@ -990,10 +1018,12 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             }
         conf->interpAlgo = best_op;
         conf->interpDirection = (uint8_t)best_dir;
+        if (cr_tests) best_interp_cr = best_cr;
     }
     conf->alpha = o_alpha;
     conf->beta = o_beta;
-    int use_interp = 1;
+    /* SZInterp.hpp:2083 */
+    int use_interp = best_interp_cr >= best_lorenzo_ratio || best_lorenzo_ratio >= 80 || best_interp_cr >= 80;
     /* B-M tuning (SZInterp.hpp:2187-2515) */
     if (conf->autoTuningRate > 0) {
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;

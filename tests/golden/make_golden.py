@@ -168,6 +168,15 @@ def cases():
                 {"GlobalSettings": {"OpenMP": "YES"}, "AlgoSettings": {}}))
     out.append(("omp_abs2d_5", spectral_field((300, 200), slope=-2.5, seed=88), ["-M", "ABS", "0.05"],
                 {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP", "OpenMP": "YES"}, "AlgoSettings": {}}))
+    # predictor tuning alone (autoTuningRate 0): compression-ratio CompressTests
+    pt = lambda **kw: {"GlobalSettings": {}, "AlgoSettings": dict({"predictorTuningRate": "0.01"}, **kw)}  # noqa: E731
+    out.append(("pt_levelwise_3d", spectral_field((64, 80, 96), slope=-3.0, noise=0.01, seed=90), ["-M", "REL", "1e-3"],
+                pt(levelwisePredictionSelection="4", maxStep="32", testLorenzo="1")))
+    out.append(("pt_lorenzo_3d", sum2d((64, 72, 80), 1e-4, 91), ["-M", "REL", "1e-3"], pt(testLorenzo="1")))
+    out.append(("pt_lorenzo_2d", spectral_field((300, 400), slope=-3.0, noise=0.01, seed=92), ["-M", "REL", "5e-4"],
+                pt(testLorenzo="1", sampleBlockSize="32")))
+    out.append(("pt_f64", spectral_field((48, 56, 64), slope=-3.0, noise=0.01, seed=93, dtype=np.float64),
+                ["-M", "REL", "1e-5"], pt(predictorTuningRate="0.02")))
     out.append(("rate_ab_only", spectral_field((48, 56, 64), slope=-3.0, seed=82), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01"}}))
     out.append(("rate_2d", spectral_field((400, 500), slope=-3.0, seed=83), ["-M", "REL", "5e-3"],

@@ -162,3 +162,50 @@ def test_gpu_lorenzo_candidate_matches_oracle(kind, dims, rel, dtype, noise):
         assert p == ref_payload
     dec, c3 = F.SZ_decompress(None, stream, dtype=x.dtype)
     assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c3.absErrorBound
+
+
+# predictor tuning alone (autoTuningRate 0): the interpolation and Lorenzo
+# candidates compared by the compression ratio of CompressTests
+PT_CASES = [
+    ((64, 80, 96), 1e-3, np.float32, 4, 32, 1),
+    ((56, 64, 72), 1e-4, np.float32, 0, 0, 1),
+    ((300, 420), 1e-3, np.float32, 6, 64, 0),
+    ((48, 56, 64), 1e-5, np.float64, 0, 0, 0),
+]
+# without autoTuningRate a 2-D field keeps sampleBlockSize 64, above the
+# interpolation block (32) the GPU tuner's sampled blocks need: set it
+
+
+@pytest.mark.parametrize("dims,rel,dtype,levelwise,max_step,test_lorenzo", PT_CASES)
+def test_gpu_predictor_tuning_only_matches_oracle(dims, rel, dtype, levelwise, max_step, test_lorenzo):
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = rel
+    conf.predictorTuningRate = 0.01
+    conf.levelwisePredictionSelection = levelwise
+    conf.maxStep = max_step
+    conf.testLorenzo = test_lorenzo
+    if len(dims) == 2:
+        conf.sampleBlockSize = 32
+    x = spectral_field(dims, slope=-2.5, noise=0.02, seed=sum(dims) + 13, dtype=dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    c1, p = O.read_stream(stream)
+    c2, _ = O.read_stream(ref)
+    for f in ("cmprAlgo", "interpAlgo", "interpDirection", "alpha", "beta", "quantbinCnt", "blockSize", "pred_dim"):
+        assert getattr(c1, f) == getattr(c2, f), f
+    if c1.cmprAlgo == 0 and len(dims) == 3:
+        assert mask_fast_frontend_padding(p, x.itemsize) == mask_fast_frontend_padding(ref_payload, x.itemsize)
+    else:
+        assert p == ref_payload
+
+
+def test_gpu_tuner_rejects_sampled_blocks_above_the_interpolation_block():
+    """2-D predictor tuning without autoTuningRate keeps sampleBlockSize 64
+    (above interpBlockSize 32): the GPU tuner fails loudly."""
+    conf = F.Config(300, 420)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = 1e-3
+    conf.predictorTuningRate = 0.01
+    with pytest.raises(F.FazError, match="interpBlockSize"):
+        F.SZ_compress(conf, spectral_field((300, 420), slope=-2.5, seed=3))
