@@ -79,9 +79,22 @@ __device__ __forceinline__ int quantize(T &v, T pred, double eb, double recip, i
 // Double-precision fallbacks of the float path, kept out of line: inlined,
 // the compiler may evaluate them unconditionally (as selects), which on GB300's
 // narrow double pipe costs more than the whole float path.
-static __device__ __noinline__ int quantize_dp_f32(float &v, float pred, double eb, double recip, int radius, int trim,
-                                            float &uval) {
-    return quantize<float>(v, pred, eb, recip, radius, trim, uval);
+// The out-of-line part returns the code and the value as one 64-bit word:
+// reference parameters to an out-of-line function would keep the caller's
+// variables in local memory on every path.
+static __device__ __noinline__ unsigned long long quantize_dp_f32_packed(float orig, float pred, double eb,
+                                                                        double recip, int radius, int trim) {
+    float v = orig, uval;
+    const int code = quantize<float>(v, pred, eb, recip, radius, trim, uval);
+    return ((unsigned long long)(unsigned)code << 32) | (unsigned long long)__float_as_uint(v);
+}
+__device__ __forceinline__ int quantize_dp_f32(float &v, float pred, double eb, double recip, int radius, int trim,
+                                               float &uval) {
+    const float orig = v;
+    const unsigned long long r = quantize_dp_f32_packed(orig, pred, eb, recip, radius, trim);
+    v = __uint_as_float((unsigned)r);
+    uval = (trim > 0 && fabs((double)orig) <= eb) ? 0.0f : orig;  // quantize's unpredictable value
+    return (int)(unsigned)(r >> 32);
 }
 static __device__ __noinline__ float dequant_dp_f32(float pred, int q2, double eb) {
     return (float)((double)pred + (double)q2 * eb);
