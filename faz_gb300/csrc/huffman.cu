@@ -302,6 +302,7 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
 #pragma unroll
         for (int k = 0; k < ENC_PER_THREAD; k++) mybits += len[sym[k]];
     } else {
+#pragma unroll
         for (int k = 0; k < ENC_PER_THREAD; k++) {
             uint64_t i = t0 + k;
             sym[k] = i < n ? (uint16_t)(codes[i] - offset) : 0;
@@ -341,7 +342,11 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
             wi++;
         }
     };
-    for (int k = 0; k < nvalid; k++) {
+    // a fixed trip count keeps sym[] in registers (a loop bounded by nvalid
+    // would index it dynamically, from local memory)
+#pragma unroll
+    for (int k = 0; k < ENC_PER_THREAD; k++) {
+        if (k >= nvalid) break;
         const unsigned long long e = packed[sym[k]];
         const int l = (int)((e >> 32) & 0xff);
         if (l <= 32) {

@@ -71,13 +71,13 @@ __global__ void k_qz_sweep(QzSweep w, LevelArgs q, T *__restrict__ data, uint16_
     const int64_t r = (int64_t)(idx % (uint64_t)w.tpl);
     const uint64_t L = (idx / (uint64_t)w.tpl) % lines;
     const uint64_t k = idx / ((uint64_t)w.tpl * lines);
-    int64_t c[3] = {0, 0, 0};
-    c[w.oth[0]] = (int64_t)(L / (uint64_t)w.cnt[1]) * w.g[0];
-    c[w.oth[1]] = (int64_t)(L % (uint64_t)w.cnt[1]) * w.g[1];
+    // offsets as scalars: arrays indexed by the sweep's axes (a local one, or
+    // the parameter struct's) would be kept in local memory
+    auto off = [&](int ax) { return ax == 0 ? w.offs[0] : (ax == 1 ? w.offs[1] : w.offs[2]); };
     const int64_t i = target_of_rank(r, w.n, w.cubic);
-    c[w.axis] = i * w.s;
-    T *d = data + k * (uint64_t)w.per + c[0] * w.offs[0] + c[1] * w.offs[1] + c[2] * w.offs[2];
-    const int64_t st = w.s * w.offs[w.axis];
+    T *d = data + k * (uint64_t)w.per + (int64_t)(L / (uint64_t)w.cnt[1]) * w.g[0] * off(w.oth[0]) +
+           (int64_t)(L % (uint64_t)w.cnt[1]) * w.g[1] * off(w.oth[1]) + i * w.s * off(w.axis);
+    const int64_t st = w.s * off(w.axis);
     const int64_t n = w.n;
     T pred;
     if (!w.cubic || n < 5) {

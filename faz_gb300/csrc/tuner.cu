@@ -101,14 +101,21 @@ __global__ void k_bi_sweep4(BiTrials<T> b, LevelArgs q, uint64_t total) {
     bc[2] = (int64_t)(t % (uint64_t)w.nb[2]);
     bc[1] = (int64_t)((t / (uint64_t)w.nb[2]) % (uint64_t)w.nb[1]);
     bc[0] = (int64_t)(t / ((uint64_t)w.nb[2] * (uint64_t)w.nb[1]));
-    int64_t c[3] = {bc[0] * w.bs, bc[1] * w.bs, bc[2] * w.bs};
+    // coordinates as scalars (an array indexed by the sweep's axes would live
+    // in local memory)
+    int64_t c0 = bc[0] * w.bs, c1 = bc[1] * w.bs, c2 = bc[2] * w.bs;
+    auto add = [&](int ax, int64_t v) {
+        c0 += ax == 0 ? v : 0;
+        c1 += ax == 1 ? v : 0;
+        c2 += ax == 2 ? v : 0;
+    };
     const int64_t u1 = (int64_t)(L % (uint64_t)w.cnt[1]), u0 = (int64_t)(L / (uint64_t)w.cnt[1]);
-    c[w.oth[0]] += u0 * w.g[0];
-    c[w.oth[1]] += u1 * w.g[1];
+    add(w.oth[0], u0 * w.g[0]);
+    add(w.oth[1], u1 * w.g[1]);
     const int64_t i = 2 * r + 1;
-    c[w.axis] += i * w.s;
-    const int64_t pos = c[0] * w.offs[0] + c[1] * w.offs[1] + c[2] * w.offs[2];
-    const int64_t st = w.s * w.offs[w.axis];
+    add(w.axis, i * w.s);
+    const int64_t pos = c0 * w.offs[0] + c1 * w.offs[1] + c2 * w.offs[2];
+    const int64_t st = w.s * (w.axis == 0 ? w.offs[0] : (w.axis == 1 ? w.offs[1] : w.offs[2]));
     T *d = b.data[v] + pos;
     const int64_t n = w.n;
     T pred;
