@@ -347,7 +347,7 @@ int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);
 // sampled 2-D / 3-D blocks of bsz^N points (bit rate, PSNR).
 template <typename T>
 void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng,
-                           cudaStream_t st, Counter &launches, double &bitrate, double &psnr);
+                           double pcoeff, cudaStream_t st, Counter &launches, double &bitrate, double &psnr);
 // Lorenzo settings once the QoZ tuner has chosen Lorenzo (sampling, the
 // quantisation-interval estimate, pred_dim and 16384-bin trials).
 template <typename T>

@@ -390,7 +390,7 @@ void huffman_i32(const int *codes, uint64_t n, int nsym, DevMem &m, cudaStream_t
 // payload the general compressor writes and PSNR of the reconstructions.
 template <typename T>
 void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng,
-                           cudaStream_t st, Counter &launches, double &bitrate, double &psnr) {
+                           double pcoeff, cudaStream_t st, Counter &launches, double &bitrate, double &psnr) {
     if (N != 2 && N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "the Lorenzo candidate covers 2-D and 3-D data"};
     TestArgs a;
     a.D = bsz;
@@ -465,14 +465,18 @@ void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, 
     // reference's loop order), in double
     double se = 0;
     for (uint64_t i = 0; i < n; i++) se += hsq[i];
+    // profiling_coeff scales both (SZInterp.hpp:1364-1370)
     const double ele = (double)n;
     bitrate = 8 * (double)zstd_framed_size_host(pl.data(), pl.size()) / ele;
-    psnr = 20 * std::log10(rng) - 10 * std::log10(se / ele);
+    bitrate *= pcoeff;
+    double mse = se / ele;
+    mse *= pcoeff;
+    psnr = 20 * std::log10(rng) - 10 * std::log10(mse);
 }
 
-template void lorenzo_compress_test<float>(int, const float *, uint64_t, int64_t, double, double, cudaStream_t,
-                                           Counter &, double &, double &);
-template void lorenzo_compress_test<double>(int, const double *, uint64_t, int64_t, double, double, cudaStream_t,
-                                            Counter &, double &, double &);
+template void lorenzo_compress_test<float>(int, const float *, uint64_t, int64_t, double, double, double,
+                                           cudaStream_t, Counter &, double &, double &);
+template void lorenzo_compress_test<double>(int, const double *, uint64_t, int64_t, double, double, double,
+                                            cudaStream_t, Counter &, double &, double &);
 
 }  // namespace faz

@@ -438,6 +438,30 @@ int64_t full_run_slots(const QzGeom &g) {
     return p;
 }
 
+// profiling_block_2d / profiling_block_3d (include/QoZ/utils/Sample.hpp:13-67,
+// 143-180): one thread per candidate block start (multiples of sbs); flag[b]
+// = 1 when the range of the block's points at multiples of `stride` (the
+// reference's loop order and comparisons) exceeds abseb.
+template <typename T>
+__global__ void k_qz_profile(const T *__restrict__ X, int64_t d1, int64_t d2, int64_t nby, int64_t nbz, int64_t sbs,
+                             int64_t stride, int N, double abseb, uint8_t *flag, uint64_t nb) {
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const int64_t bz = (int64_t)(b % (uint64_t)nbz), by = (int64_t)((b / (uint64_t)nbz) % (uint64_t)nby);
+    const int64_t bx = (int64_t)(b / ((uint64_t)nbz * (uint64_t)nby));
+    const int64_t dyz = d1 * d2;
+    const T *s0 = X + bx * sbs * dyz + by * sbs * d2 + bz * sbs;
+    T mn = s0[0], mx = s0[0];
+    for (int64_t ii = 0; ii <= sbs; ii += stride)
+        for (int64_t jj = 0; jj <= sbs; jj += stride)
+            for (int64_t kk = 0; N == 2 ? kk == 0 : kk <= sbs; kk += (N == 3 ? stride : 1)) {
+                const T v = s0[ii * dyz + jj * d2 + kk];
+                if (v < mn) mn = v;
+                else if (v > mx) mx = v;
+            }
+    flag[b] = (double)(T)(mx - mn) > abseb ? 1 : 0;
+}
+
 }  // namespace
 
 // QoZ defaults and the settings derived from the field before any trial
@@ -468,7 +492,6 @@ int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) 
     }
     // without QoZ the tuner runs from the configuration's own rates
     // (predictorTuningRate in (0, 1)); these variants are not implemented
-    if (c.profiling) throw Fail{FAZ_ERR_UNSUPPORTED, "profiling-driven block sampling is not implemented"};
     if (c.autoTuningRate < 0) throw Fail{FAZ_ERR_UNSUPPORTED, "a negative autoTuningRate is not implemented"};
     int max_interp_level = -1;
     for (int i = 0; i < N; i++) {
@@ -508,38 +531,81 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     const int max_interp_level = qoz_prepare<T>(c, dX, st, launches);
     const double rel_bound = c.relErrorBound > 0 ? c.relErrorBound : c.absErrorBound / (double)(T)c.rng;
     const int64_t sbs = c.sampleBlockSize, bsz = sbs + 1;
-    // sampleBlocks (profiling 0, var_first 0)
-    uint64_t stride = (uint64_t)(1.0 / c.predictorTuningRate);
-    if (stride <= 0) stride = 1;
-    std::vector<int64_t> starts;
-    uint64_t idx = 0;
     const uint64_t d0 = c.dims[0], d1 = c.dims[1], d2 = N == 3 ? c.dims[2] : 1;
-    for (uint64_t x = 0; x < d0 - sbs; x += sbs)
-        for (uint64_t y = 0; y < d1 - sbs; y += sbs)
-            for (uint64_t z = 0; N == 2 ? z == 0 : z < d2 - sbs; z += (N == 3 ? sbs : 1)) {
-                if (idx % stride == 0) {
-                    starts.push_back((int64_t)x);
-                    starts.push_back((int64_t)y);
-                    starts.push_back((int64_t)z);
-                }
-                idx++;
-            }
-    const uint64_t nblk = starts.size() / 3;
-    if (nblk == 0) throw Fail{FAZ_ERR_UNSUPPORTED, "no block to sample for QoZ tuning"};
+    // candidate blocks: starts at multiples of sbs (sampleBlocks' loops)
+    const uint64_t nbx = (d0 - 1) / sbs, nby = (d1 - 1) / sbs, nbz = N == 3 ? (d2 - 1) / sbs : 1;
+    const uint64_t totalblock_num = nbx * nby * (N == 3 ? nbz : 1);
+    auto start_of = [&](uint64_t b, std::vector<int64_t> &out) {
+        out.push_back((int64_t)(b / (nbz * nby)) * sbs);
+        out.push_back((int64_t)((b / nbz) % nby) * sbs);
+        out.push_back(N == 3 ? (int64_t)(b % nbz) * sbs : 0);
+    };
+    // sampleBlocks without profiling (var_first 0): every (size_t)(1/rate)-th block
+    auto plain_starts = [&](double rate) {
+        uint64_t stride = (uint64_t)(1.0 / rate);
+        if (stride <= 0) stride = 1;
+        std::vector<int64_t> st;
+        for (uint64_t b = 0; b < totalblock_num; b += stride) start_of(b, st);
+        return st;
+    };
+    DevMem m(st);
+    // profiling (SZInterp.hpp:1820-1842): the blocks whose subsampled range
+    // exceeds the bound; profiling_coeff scales the B-M CompressTests
+    double pcoeff = 1;
+    std::vector<int64_t> starts;
+    if (c.profiling) {
+        uint8_t *dflag = m.alloc<uint8_t>(totalblock_num + 1);
+        int64_t pstride = sbs / 4;
+        if (pstride == 0) pstride = sbs;
+        k_qz_profile<T><<<(unsigned)((totalblock_num + 255) / 256), 256, 0, st>>>(
+            dX, (int64_t)d1, (int64_t)d2, (int64_t)nby, (int64_t)nbz, sbs, pstride, N, c.absErrorBound, dflag,
+            totalblock_num);
+        launches(cudaGetLastError());
+        std::vector<uint8_t> hflag(totalblock_num);
+        CK(cudaMemcpyAsync(hflag.data(), dflag, totalblock_num, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::vector<uint64_t> filt;
+        for (uint64_t b = 0; b < totalblock_num; b++)
+            if (hflag[b]) filt.push_back(b);
+        const uint64_t npst = filt.size();
+        if (npst <= (uint64_t)(int)(0.3 * c.predictorTuningRate)) c.profiling = 0;
+        if (c.profiling) {
+            pcoeff = (double)npst / totalblock_num;
+            // sampleBlocks with profiling: every sample_stride-th filtered block
+            uint64_t sstride = (uint64_t)(npst / (totalblock_num * c.predictorTuningRate));
+            if (sstride <= 0) sstride = 1;
+            for (uint64_t t = 0; t < npst; t += sstride) start_of(filt[t], starts);
+        }
+    }
+    if (!c.profiling) starts = plain_starts(c.predictorTuningRate);
     QzGeom g = make_geom(N, bsz, (int64_t)c.maxStep);
     g.cpb = full_run_slots(g);
-    DevMem m(st);
-    const uint64_t nv = nblk * (uint64_t)g.per, ns = nblk * (uint64_t)g.cpb;
-    T *blocks = m.alloc<T>(nv), *work = m.alloc<T>(nv), *scratch = m.alloc<T>(ns);
-    uint16_t *codes = m.alloc<uint16_t>(ns);
-    double *err = m.alloc<double>(ns), *bsum = m.alloc<double>(nblk);
-    int64_t *dstarts = m.alloc<int64_t>(starts.size());
-    CK(cudaMemcpyAsync(dstarts, starts.data(), starts.size() * 8, cudaMemcpyHostToDevice, st));
-    k_qz_gather<T><<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(dX, dstarts, (int64_t)c.dims[1],
-                                                                  N == 3 ? (int64_t)c.dims[2] : (int64_t)c.dims[1],
-                                                                  bsz, N, blocks, nv);
-    launches(cudaGetLastError());
-    std::vector<double> hsum(nblk);
+    uint64_t nblk = 0, nv = 0, ns = 0;
+    T *blocks = nullptr, *work = nullptr, *scratch = nullptr;
+    uint16_t *codes = nullptr;
+    double *err = nullptr, *bsum = nullptr;
+    std::vector<double> hsum;
+    // the sampled blocks and the buffers sized by their count
+    auto gather = [&](const std::vector<int64_t> &sts) {
+        nblk = sts.size() / 3;
+        if (nblk == 0) throw Fail{FAZ_ERR_UNSUPPORTED, "no block to sample for QoZ tuning"};
+        nv = nblk * (uint64_t)g.per;
+        ns = nblk * (uint64_t)g.cpb;
+        blocks = m.alloc<T>(nv);
+        work = m.alloc<T>(nv);
+        scratch = m.alloc<T>(ns);
+        codes = m.alloc<uint16_t>(ns);
+        err = m.alloc<double>(ns);
+        bsum = m.alloc<double>(nblk);
+        hsum.assign(nblk, 0.0);
+        int64_t *dstarts = m.alloc<int64_t>(sts.size());
+        CK(cudaMemcpyAsync(dstarts, sts.data(), sts.size() * 8, cudaMemcpyHostToDevice, st));
+        k_qz_gather<T><<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(dX, dstarts, (int64_t)c.dims[1],
+                                                                      N == 3 ? (int64_t)c.dims[2] : (int64_t)c.dims[1],
+                                                                      bsz, N, blocks, nv);
+        launches(cudaGetLastError());
+    };
+    gather(starts);
     auto block_sums = [&](const SumPlan &sp) -> double {
         k_qz_sum<<<(unsigned)((nblk + 63) / 64), 64, 0, st>>>(sp, err, bsum, nblk);
         launches(cudaGetLastError());
@@ -569,7 +635,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     // after Huffman + zstd, PSNR from the summed squared errors
     std::vector<std::pair<int64_t, int64_t>> ranges;
     auto compress_test = [&](int op, int dir, double alpha, double beta, double eb, double &bitrate, double &psnr,
-                             bool lists = true) {
+                             bool lists = true, double pc = 1.0) {
         CK(cudaMemcpyAsync(work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, st));
         QzRun R{1, g.levels, 0, eb, alpha, beta, c.trimToZero, op, dir, lists ? &il : nullptr, lists ? &dl : nullptr};
         qz_run<T>(g, R, work, codes, scratch, err, nblk, sp, &ranges, st, launches);
@@ -625,9 +691,13 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             CK(cudaMemcpyAsync(pl.data() + head.size() + nunp * sizeof(T) + tree.size(), h.bits, h.nbytes,
                                cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        // profiling_coeff scales both (SZInterp.hpp:1364-1370)
         const double ele = (double)nv;
         bitrate = 8 * (double)zstd_framed_size_host(pl.data(), pl.size()) / ele;
-        psnr = 20 * std::log10(c.rng) - 10 * std::log10(se / ele);
+        bitrate *= pc;
+        double mse = se / ele;
+        mse *= pc;
+        psnr = 20 * std::log10(c.rng) - 10 * std::log10(mse);
     };
     // without the alpha/beta search (autoTuningRate = 0) the decisions
     // compare compression ratios of CompressTests (TUNING_TARGET_CR)
@@ -636,7 +706,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     if (c.testLorenzo && cr_tests) {
         // SZInterp.hpp:1925-1932
         double br, mm;
-        lorenzo_compress_test<T>(N, blocks, nblk, bsz, c.absErrorBound, c.rng, st, launches, br, mm);
+        lorenzo_compress_test<T>(N, blocks, nblk, bsz, c.absErrorBound, c.rng, 1.0, st, launches, br, mm);
         best_lorenzo_ratio = sizeof(T) * 8.0 / br;
     }
     if (Lsel > 0) {
@@ -698,6 +768,8 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     c.beta = o_beta;
     // SZInterp.hpp:2083
     bool use_interp = best_interp_cr >= best_lorenzo_ratio || best_lorenzo_ratio >= 80 || best_interp_cr >= 80;
+    if (c.autoTuningRate > 0 && use_interp && c.autoTuningRate != c.predictorTuningRate)
+        gather(plain_starts(c.autoTuningRate));  // its own sample, no profiling (SZInterp.hpp:2199-2202)
     if (c.autoTuningRate > 0) {
         // B-M tuning (SZInterp.hpp:2187-2515): CompressTest per alpha/beta
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
@@ -712,7 +784,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             for (double beta : blist) {
                 if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
                 double br, mm;
-                compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb, br, mm);
+                compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb, br, mm, true, pcoeff);
                 if (mm >= bestm && br <= bestb) {
                     bestalpha = alpha;
                     bestbeta = beta;
@@ -724,7 +796,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
                 } else {
                     const double fix = br / bestb;
                     double br2, m2;
-                    compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb * fix, br2, m2);
+                    compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb * fix, br2, m2, true, pcoeff);
                     const double a = (mm - m2) / (br - br2);
                     const double b = mm - a * br;
                     const double reg = a * bestb + b;
@@ -743,7 +815,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             // the Lorenzo candidate: CompressTest with ALGO_LORENZO_REG
             // against the best alpha/beta point (SZInterp.hpp:2428-2486)
             double br, mm;
-            lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb, c.rng, st, launches, br, mm);
+            lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb, c.rng, pcoeff, st, launches, br, mm);
             if (mm >= bestm && br <= bestb) {
                 bestb = br;
                 bestm = mm;
@@ -754,7 +826,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             } else {
                 const double fix = br / bestb;
                 double br2, m2;
-                lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb * fix, c.rng, st, launches, br2, m2);
+                lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb * fix, c.rng, pcoeff, st, launches, br2, m2);
                 const double a = (mm - m2) / (br - br2);
                 if (a > 0) {
                     const double b = mm - a * br;

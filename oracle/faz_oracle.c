@@ -884,8 +884,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         conf->pyBind = 0;
         conf->sperrWithoutWave = 0;
     }
-    if (conf->profiling || conf->autoTuningRate < 0) {
-        set_err("oracle QoZ-branch tuner covers autoTuningRate >= 0 without profiling");
+    if (conf->autoTuningRate < 0) {
+        set_err("oracle QoZ-branch tuner covers autoTuningRate >= 0");
         return -2;
     }
     int max_interp_level = -1;
@@ -912,10 +912,32 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     if (!(conf->predictorTuningRate > 0 && conf->predictorTuningRate < 1)) { set_err("predictorTuningRate outside (0,1)"); return -2; }
     size_t gdims[4];
     for (int i = 0; i < N; i++) gdims[i] = conf->dims[i];
+    /* profiling: the blocks whose subsampled range exceeds the bound
+     * (SZInterp.hpp:1820-1842); profiling_coeff scales the B-M CompressTests */
+    size_t totalblock_num = 1;
+    for (int i = 0; i < N; i++) totalblock_num *= (conf->dims[i] - 1) / sbs;
+    double pcoeff = 1;
+    size_t *pst = NULL, npst = 0;
+    if (conf->profiling) {
+        npst = dtype == FAZ_FLOAT
+                   ? qoz_profile_f32((const float *)data, N, gdims, sbs, conf->absErrorBound, sbs / 4, &pst)
+                   : qoz_profile_f64((const double *)data, N, gdims, sbs, conf->absErrorBound, sbs / 4, &pst);
+        if (npst <= (size_t)(int)(0.3 * conf->predictorTuningRate)) conf->profiling = 0;
+        if (conf->profiling) pcoeff = (double)npst / totalblock_num;
+    }
     void *blocks;
-    size_t nblk = dtype == FAZ_FLOAT
-                      ? qoz_sample_f32((const float *)data, N, gdims, sbs, conf->predictorTuningRate, (float **)&blocks)
-                      : qoz_sample_f64((const double *)data, N, gdims, sbs, conf->predictorTuningRate, (double **)&blocks);
+    size_t nblk;
+    if (conf->profiling)
+        nblk = dtype == FAZ_FLOAT ? qoz_sample_profiled_f32((const float *)data, N, gdims, sbs, conf->predictorTuningRate,
+                                                            pst, npst, totalblock_num, (float **)&blocks)
+                                  : qoz_sample_profiled_f64((const double *)data, N, gdims, sbs,
+                                                            conf->predictorTuningRate, pst, npst, totalblock_num,
+                                                            (double **)&blocks);
+    else
+        nblk = dtype == FAZ_FLOAT
+                   ? qoz_sample_f32((const float *)data, N, gdims, sbs, conf->predictorTuningRate, (float **)&blocks)
+                   : qoz_sample_f64((const double *)data, N, gdims, sbs, conf->predictorTuningRate, (double **)&blocks);
+    free(pst);
     double o_alpha = conf->alpha, o_beta = conf->beta;
     /* without the alpha/beta search the decisions compare compression ratios
      * of CompressTests (TUNING_TARGET_CR) */
@@ -925,8 +947,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         /* SZInterp.hpp:1925-1932 */
         double br, m;
         int rc = dtype == FAZ_FLOAT
-                     ? gen_test_f32((const float *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, &br, &m)
-                     : gen_test_f64((const double *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, &br, &m);
+                     ? gen_test_f32((const float *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, 1.0, &br, &m)
+                     : gen_test_f64((const double *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, 1.0, &br, &m);
         if (rc) { free(blocks); return rc; }
         best_lorenzo_ratio = (double)es * 8.0 / br;
     }
@@ -991,9 +1013,9 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             double br, m;
             int rc = dtype == FAZ_FLOAT
                          ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                 conf->trimToZero, conf->maxStep, conf->rng, &br, &m)
+                                                 conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m)
                          : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                 conf->trimToZero, conf->maxStep, conf->rng, &br, &m);
+                                                 conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m);
             if (rc) { free(blocks); return rc; }
             best_interp_cr = (double)es * 8.0 / br;
         }
@@ -1009,9 +1031,9 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                 double br, m;
                 int rc = dtype == FAZ_FLOAT
                              ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, &br, &m)
+                                                     conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m)
                              : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, &br, &m);
+                                                     conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m);
                 if (rc) { free(blocks); return rc; }
                 double cr = (double)es * 8.0 / br;
                 if (cr > best_cr) { best_cr = cr; best_op = op; best_dir = dirs[di]; }
@@ -1025,6 +1047,13 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     /* SZInterp.hpp:2083 */
     int use_interp = best_interp_cr >= best_lorenzo_ratio || best_lorenzo_ratio >= 80 || best_interp_cr >= 80;
     /* B-M tuning (SZInterp.hpp:2187-2515) */
+    if (conf->autoTuningRate > 0 && use_interp && conf->autoTuningRate != conf->predictorTuningRate) {
+        /* its own sample at autoTuningRate, without profiling (SZInterp.hpp:2199-2202) */
+        free(blocks);
+        nblk = dtype == FAZ_FLOAT
+                   ? qoz_sample_f32((const float *)data, N, gdims, sbs, conf->autoTuningRate, (float **)&blocks)
+                   : qoz_sample_f64((const double *)data, N, gdims, sbs, conf->autoTuningRate, (double **)&blocks);
+    }
     if (conf->autoTuningRate > 0) {
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
         static const double alist[] = {1, 1.25, 1.5, 1.75, 2};
@@ -1040,9 +1069,9 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                 double br, m;
                 int rc = dtype == FAZ_FLOAT
                              ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, &br, &m)
+                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br, &m)
                              : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, &br, &m);
+                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br, &m);
                 if (rc) { free(blocks); return rc; }
                 if (m >= bestm && br <= bestb) {
                     bestalpha = alpha; bestbeta = beta; bestb = br; bestm = m;
@@ -1056,9 +1085,9 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                     double br2, m2;
                     rc = dtype == FAZ_FLOAT
                              ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound * fix,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, &br2, &m2)
+                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br2, &m2)
                              : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound * fix,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, &br2, &m2);
+                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br2, &m2);
                     if (rc) { free(blocks); return rc; }
                     double a = (m - m2) / (br - br2);
                     double bb = m - a * br;
@@ -1075,8 +1104,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             /* the Lorenzo candidate: CompressTest with ALGO_LORENZO_REG against
              * the best alpha/beta point (SZInterp.hpp:2428-2486) */
             double br, m;
-            int rc = dtype == FAZ_FLOAT ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb, conf->rng, &br, &m)
-                                        : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb, conf->rng, &br, &m);
+            int rc = dtype == FAZ_FLOAT ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb, conf->rng, pcoeff, &br, &m)
+                                        : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb, conf->rng, pcoeff, &br, &m);
             if (rc) { free(blocks); return rc; }
             if (m >= bestm && br <= bestb) {
                 bestb = br; bestm = m; bestalpha = -1; bestbeta = -1; use_interp = 0;
@@ -1085,8 +1114,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             } else {
                 double fix = br / bestb, br2, m2;
                 rc = dtype == FAZ_FLOAT
-                         ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, &br2, &m2)
-                         : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, &br2, &m2);
+                         ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, pcoeff, &br2, &m2)
+                         : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, pcoeff, &br2, &m2);
                 if (rc) { free(blocks); return rc; }
                 double a = (m - m2) / (br - br2);
                 if (a > 0) {

@@ -51,7 +51,8 @@ def fuzz_cases(n=N_CASES, seed=20261203):
             atr = float(rng.choice([0.0, 0.005, 0.01]))
             a = {"predictorTuningRate": "0.01", "autoTuningRate": f"{atr:g}",
                  "levelwisePredictionSelection": str(int(rng.choice([0, 3, 4]))),
-                 "testLorenzo": str(int(rng.integers(0, 2))), "maxStep": str(int(rng.choice([0, 16, 32])))}
+                 "testLorenzo": str(int(rng.integers(0, 2))), "maxStep": str(int(rng.choice([0, 16, 32]))),
+                 "profiling": str(int(rng.integers(0, 2)))}
             sbs = int(rng.choice([0, 16, 32]))
             if N == 2 and atr == 0 and sbs == 0:
                 sbs = 32  # keeps the sampled blocks within one interpolation block

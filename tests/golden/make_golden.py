@@ -177,6 +177,21 @@ def cases():
                 pt(testLorenzo="1", sampleBlockSize="32")))
     out.append(("pt_f64", spectral_field((48, 56, 64), slope=-3.0, noise=0.01, seed=93, dtype=np.float64),
                 ["-M", "REL", "1e-5"], pt(predictorTuningRate="0.02")))
+    # profiling-driven sampling (profiling = 1) and a B-M sample of its own
+    # (autoTuningRate != predictorTuningRate); seeds whose decisions are the
+    # same with the host's zstd as with the reference's 1.4.5
+    out.append(("prof_3d", flat_outside((96, 128, 160), 0.6, 95), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                                        "profiling": "1", "levelwisePredictionSelection": "4",
+                                                        "maxStep": "32", "sampleBlockSize": "32"}}))
+    out.append(("prof_rates_3d", flat_outside((96, 128, 160), 0.6, 94), ["-M", "REL", "1e-2"],
+                {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.005", "predictorTuningRate": "0.02",
+                                                        "profiling": "1", "testLorenzo": "1",
+                                                        "sampleBlockSize": "16"}}))
+    out.append(("prof_2d", flat_outside((400, 500), 0.7, 96), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                                        "profiling": "1", "levelwisePredictionSelection": "6",
+                                                        "maxStep": "64"}}))
     out.append(("rate_ab_only", spectral_field((48, 56, 64), slope=-3.0, seed=82), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01"}}))
     out.append(("rate_2d", spectral_field((400, 500), slope=-3.0, seed=83), ["-M", "REL", "5e-3"],
@@ -193,6 +208,15 @@ def sum1d(shape, noise, seed, dtype=np.float32):
     g = rng.standard_normal((1, shape[1]))
     base = np.cumsum(f, axis=0) + np.cumsum(g, axis=1)
     return (base + noise * rng.standard_normal(shape) * (base.max() - base.min())).astype(dtype)
+
+
+def flat_outside(shape, frac, seed, dtype=np.float32):
+    """A spectral field (k^-3, 2% noise) in the leading `frac` of every axis,
+    constant elsewhere (blocks the QoZ tuner's profiling filters out)."""
+    x = spectral_field(shape, slope=-3.0, noise=0.02, seed=seed, dtype=dtype)
+    m = np.zeros(shape, bool)
+    m[tuple(slice(0, int(n * frac)) for n in shape)] = True
+    return np.where(m, x, dtype(1.0)).astype(dtype)
 
 
 def sum2d(shape, noise, seed, dtype=np.float32):

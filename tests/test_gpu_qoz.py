@@ -209,3 +209,43 @@ def test_gpu_tuner_rejects_sampled_blocks_above_the_interpolation_block():
     conf.predictorTuningRate = 0.01
     with pytest.raises(F.FazError, match="interpBlockSize"):
         F.SZ_compress(conf, spectral_field((300, 420), slope=-2.5, seed=3))
+
+
+def _flat_outside(dims, frac, seed):
+    x = spectral_field(dims, slope=-3.0, noise=0.02, seed=seed)
+    m = np.zeros(dims, bool)
+    m[tuple(slice(0, int(n * frac)) for n in dims)] = True
+    return np.where(m, x, np.float32(1.0)).astype(np.float32)
+
+
+# profiling-driven sampling (profiling = 1: blocks whose subsampled range is
+# within the bound are left out, profiling_coeff scales the alpha/beta
+# CompressTests) and a B-M sample of its own when the rates differ
+PROF_CASES = [
+    ((96, 128, 160), 1e-3, dict(autoTuningRate=0.01, predictorTuningRate=0.01, profiling=1,
+                                levelwisePredictionSelection=4, maxStep=32, sampleBlockSize=32), 0.6),
+    ((96, 128, 160), 1e-2, dict(autoTuningRate=0.005, predictorTuningRate=0.02, profiling=1, testLorenzo=1,
+                                sampleBlockSize=16), 0.6),
+    ((128, 128, 128), 1e-4, dict(autoTuningRate=0.01, predictorTuningRate=0.01, profiling=1, testLorenzo=1,
+                                 levelwisePredictionSelection=4, maxStep=32, sampleBlockSize=32), 0.5),
+    ((400, 500), 1e-3, dict(autoTuningRate=0.01, predictorTuningRate=0.01, profiling=1,
+                            levelwisePredictionSelection=6, maxStep=64), 0.7),
+    ((96, 128, 160), 5e-3, dict(autoTuningRate=0.02, predictorTuningRate=0.005, levelwisePredictionSelection=4,
+                                maxStep=32, sampleBlockSize=16), 1.0),
+]
+
+
+@pytest.mark.parametrize("dims,rel,settings,frac", PROF_CASES)
+def test_gpu_profiling_and_rates_match_oracle(dims, rel, settings, frac):
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = rel
+    for k, v in settings.items():
+        setattr(conf, k, v)
+    x = _flat_outside(dims, frac, sum(dims))
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    _, p = O.read_stream(stream)
+    assert parse_interp_header(p, len(dims)) == parse_interp_header(ref_payload, len(dims))
+    assert p == ref_payload
+    assert mask_first_size(stream) == mask_first_size(ref)
