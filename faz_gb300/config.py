@@ -90,6 +90,7 @@ class FazConfigStruct(ctypes.Structure):
         ("conditioning", _i32),
         ("meta", _u8 * 17),
         ("pybind_activated", _u8),
+        ("var_first", _i32),
     ]
 
 

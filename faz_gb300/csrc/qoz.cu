@@ -18,6 +18,7 @@
 // reference's, on the host.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -462,6 +463,35 @@ __global__ void k_qz_profile(const T *__restrict__ X, int64_t d1, int64_t d2, in
     flag[b] = (double)(T)(mx - mn) > abseb ? 1 : 0;
 }
 
+// blockwise_profiling's variance (include/QoZ/utils/Metrics.hpp:24-100) of
+// the blocks of bs points per axis at the given starts: one thread per block,
+// the reference's sequential double sums.
+template <typename T>
+__global__ void k_qz_sigma2(const T *__restrict__ X, const int64_t *__restrict__ starts, uint64_t n, int64_t d1,
+                            int64_t d2, int64_t bs, int N, double *out) {
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const int64_t x = starts[3 * b], y = starts[3 * b + 1], z = starts[3 * b + 2];
+    const int64_t dyz = d1 * d2, zn = N == 3 ? bs : 1;
+    const double ne = (double)(N == 3 ? bs * bs * bs : bs * bs);
+    double sum = 0, sigma2 = 0;
+    for (int64_t i = x; i < x + bs; i++)
+        for (int64_t j = y; j < y + bs; j++)
+            for (int64_t k = z; k < z + zn; k++) {
+                const T value = X[i * dyz + j * d2 + k];
+                sum += value;
+            }
+    const double mean = sum / ne;
+    for (int64_t i = x; i < x + bs; i++)
+        for (int64_t j = y; j < y + bs; j++)
+            for (int64_t k = z; k < z + zn; k++) {
+                const T value = X[i * dyz + j * d2 + k];
+                sigma2 += (value - mean) * (value - mean);
+            }
+    sigma2 /= ne;
+    out[b] = sigma2;
+}
+
 }  // namespace
 
 // QoZ defaults and the settings derived from the field before any trial
@@ -553,6 +583,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     // exceeds the bound; profiling_coeff scales the B-M CompressTests
     double pcoeff = 1;
     std::vector<int64_t> starts;
+    std::vector<uint64_t> filt;  // the profiled blocks
     if (c.profiling) {
         uint8_t *dflag = m.alloc<uint8_t>(totalblock_num + 1);
         int64_t pstride = sbs / 4;
@@ -564,7 +595,6 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         std::vector<uint8_t> hflag(totalblock_num);
         CK(cudaMemcpyAsync(hflag.data(), dflag, totalblock_num, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        std::vector<uint64_t> filt;
         for (uint64_t b = 0; b < totalblock_num; b++)
             if (hflag[b]) filt.push_back(b);
         const uint64_t npst = filt.size();
@@ -577,7 +607,44 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             for (uint64_t t = 0; t < npst; t += sstride) start_of(filt[t], starts);
         }
     }
-    if (!c.profiling) starts = plain_starts(c.predictorTuningRate);
+    if (c.var_first) {
+        // sampleBlocks with var_first (SZInterp.hpp:1020-1037, 1086-1124): the
+        // candidates of largest block variance, largest first (the order a
+        // max-heap of (sigma2, starts) hands them out)
+        if (!c.profiling && N != 3)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "var_first sampling without profiling covers 3-D data"};
+        std::vector<int64_t> cand;
+        if (c.profiling)
+            for (uint64_t b : filt) start_of(b, cand);
+        else
+            for (uint64_t b = 0; b < totalblock_num; b++) start_of(b, cand);
+        const uint64_t nc = cand.size() / 3;
+        int64_t *dc = m.alloc<int64_t>(cand.size());
+        double *ds2 = m.alloc<double>(nc);
+        CK(cudaMemcpyAsync(dc, cand.data(), cand.size() * 8, cudaMemcpyHostToDevice, st));
+        k_qz_sigma2<T><<<(unsigned)((nc + 127) / 128), 128, 0, st>>>(dX, dc, nc, (int64_t)d1, (int64_t)d2, bsz, N, ds2);
+        launches(cudaGetLastError());
+        std::vector<double> s2(nc);
+        CK(cudaMemcpyAsync(s2.data(), ds2, nc * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::vector<uint64_t> ord(nc);
+        for (uint64_t t = 0; t < nc; t++) ord[t] = t;
+        std::sort(ord.begin(), ord.end(), [&](uint64_t a, uint64_t b) {
+            if (s2[a] != s2[b]) return s2[a] > s2[b];
+            for (int q = 0; q < 3; q++)
+                if (cand[3 * a + q] != cand[3 * b + q]) return cand[3 * a + q] > cand[3 * b + q];
+            return false;
+        });
+        uint64_t k = (uint64_t)(totalblock_num * c.predictorTuningRate);
+        if (c.profiling && k > nc) k = nc;
+        if (k == 0) k = 1;
+        if (k > nc) k = nc;
+        starts.clear();
+        for (uint64_t t = 0; t < k; t++)
+            for (int q = 0; q < 3; q++) starts.push_back(cand[3 * ord[t] + q]);
+    } else if (!c.profiling) {
+        starts = plain_starts(c.predictorTuningRate);
+    }
     QzGeom g = make_geom(N, bsz, (int64_t)c.maxStep);
     g.cpb = full_run_slots(g);
     uint64_t nblk = 0, nv = 0, ns = 0;

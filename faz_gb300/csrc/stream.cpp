@@ -186,6 +186,7 @@ int config_load_ini(faz_config *c, const char *path, std::string &err) {
         (int32_t)ini.integer(A, "levelwisePredictionSelection", c->levelwisePredictionSelection);
     c->testLorenzo = (int32_t)ini.integer(A, "testLorenzo", c->testLorenzo);
     c->profiling = (int32_t)ini.integer(A, "profiling", c->profiling);
+    c->var_first = (int32_t)ini.integer(A, "var_first", c->var_first);
     c->SSIMBlockSize = (int32_t)ini.integer(A, "SSIMBlockSize", c->SSIMBlockSize);
     c->fixBlockSize = (int32_t)ini.integer(A, "fixBlockSize", c->fixBlockSize);
     c->verbose = ini.boolean(A, "verbose", c->verbose);

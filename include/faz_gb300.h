@@ -141,6 +141,7 @@ typedef struct faz_config {
     int32_t conditioning;
     uint8_t meta[17];
     uint8_t pybind_activated;
+    int32_t var_first;              /* QoZ-branch sampling by block variance (default 0) */
 } faz_config;
 
 /* Per-call timings in milliseconds, filled when a non-NULL pointer is given. */

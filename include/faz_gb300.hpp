@@ -89,6 +89,7 @@ class Config {
     int stride = 0;
     int pred_dim = 0;
     int profiling = 0;
+    int var_first = 0;
     int SSIMBlockSize = 8;
     int fixBlockSize = 0;
     int blockwiseSampleBlockSize = 0;
@@ -193,6 +194,7 @@ class Config {
         c.stride = stride;
         c.pred_dim = pred_dim;
         c.profiling = profiling;
+        c.var_first = var_first;
         c.SSIMBlockSize = SSIMBlockSize;
         c.fixBlockSize = fixBlockSize;
         c.blockwiseSampleBlockSize = blockwiseSampleBlockSize;
@@ -261,6 +263,7 @@ class Config {
         stride = c.stride;
         pred_dim = c.pred_dim;
         profiling = c.profiling;
+        var_first = c.var_first;
         SSIMBlockSize = c.SSIMBlockSize;
         fixBlockSize = c.fixBlockSize;
         blockwiseSampleBlockSize = c.blockwiseSampleBlockSize;

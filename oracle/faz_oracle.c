@@ -927,7 +927,35 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     }
     void *blocks;
     size_t nblk;
-    if (conf->profiling)
+    if (conf->var_first) {
+        /* sampleBlocks with var_first (SZInterp.hpp:1020-1037, 1086-1124): the
+         * blocks of largest variance; without profiling only 3-D data samples
+         * any block in the reference */
+        if (!conf->profiling && N != 3) {
+            free(pst);
+            set_err("var_first sampling without profiling covers 3-D data");
+            return -2;
+        }
+        size_t *cand = pst, ncand = npst;
+        if (!conf->profiling) {
+            ncand = totalblock_num;
+            cand = (size_t *)malloc(ncand * 3 * sizeof(size_t));
+            size_t t = 0;
+            for (size_t x = 0; x < gdims[0] - sbs; x += sbs)
+                for (size_t y = 0; y < gdims[1] - sbs; y += sbs)
+                    for (size_t z = 0; z < gdims[2] - sbs; z += sbs) {
+                        cand[3 * t] = x; cand[3 * t + 1] = y; cand[3 * t + 2] = z;
+                        t++;
+                    }
+        }
+        size_t k = (size_t)(totalblock_num * conf->predictorTuningRate);
+        if (conf->profiling && k > npst) k = npst;
+        if (k == 0) k = 1;
+        nblk = dtype == FAZ_FLOAT ? qoz_sample_var_f32((const float *)data, N, gdims, sbs, cand, ncand, k, (float **)&blocks)
+                                  : qoz_sample_var_f64((const double *)data, N, gdims, sbs, cand, ncand, k,
+                                                       (double **)&blocks);
+        if (cand != pst) free(cand);
+    } else if (conf->profiling)
         nblk = dtype == FAZ_FLOAT ? qoz_sample_profiled_f32((const float *)data, N, gdims, sbs, conf->predictorTuningRate,
                                                             pst, npst, totalblock_num, (float **)&blocks)
                                   : qoz_sample_profiled_f64((const double *)data, N, gdims, sbs,

@@ -192,6 +192,14 @@ def cases():
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
                                                         "profiling": "1", "levelwisePredictionSelection": "6",
                                                         "maxStep": "64"}}))
+    # sampling by block variance (var_first = 1), with and without profiling
+    out.append(("varfirst_3d", spectral_field((80, 96, 112), slope=-2.5, noise=0.05, seed=97), ["-M", "REL", "5e-3"],
+                {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.005", "predictorTuningRate": "0.02",
+                                                        "var_first": "1", "sampleBlockSize": "16"}}))
+    out.append(("varfirst_prof_2d", flat_outside((400, 500), 0.7, 100), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                                        "var_first": "1", "profiling": "1",
+                                                        "levelwisePredictionSelection": "6", "maxStep": "64"}}))
     out.append(("rate_ab_only", spectral_field((48, 56, 64), slope=-3.0, seed=82), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01"}}))
     out.append(("rate_2d", spectral_field((400, 500), slope=-3.0, seed=83), ["-M", "REL", "5e-3"],

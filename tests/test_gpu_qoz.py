@@ -249,3 +249,29 @@ def test_gpu_profiling_and_rates_match_oracle(dims, rel, settings, frac):
     assert parse_interp_header(p, len(dims)) == parse_interp_header(ref_payload, len(dims))
     assert p == ref_payload
     assert mask_first_size(stream) == mask_first_size(ref)
+
+
+VARFIRST_CASES = [
+    ((96, 128, 160), 1e-3, dict(autoTuningRate=0.01, predictorTuningRate=0.01, var_first=1,
+                                levelwisePredictionSelection=4, maxStep=32, sampleBlockSize=32), 1.0),
+    ((96, 128, 160), 1e-3, dict(autoTuningRate=0.01, predictorTuningRate=0.01, var_first=1, profiling=1,
+                                levelwisePredictionSelection=4, maxStep=32, sampleBlockSize=16), 0.6),
+    ((400, 500), 1e-3, dict(autoTuningRate=0.01, predictorTuningRate=0.01, var_first=1, profiling=1,
+                            levelwisePredictionSelection=6, maxStep=64), 0.7),
+]
+
+
+@pytest.mark.parametrize("dims,rel,settings,frac", VARFIRST_CASES)
+def test_gpu_var_first_sampling_matches_oracle(dims, rel, settings, frac):
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = rel
+    for k, v in settings.items():
+        setattr(conf, k, v)
+    x = _flat_outside(dims, frac, sum(dims) + 1) if frac < 1 else spectral_field(dims, slope=-2.5, noise=0.05,
+                                                                                seed=sum(dims))
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    _, p = O.read_stream(stream)
+    assert p == ref_payload
+    assert mask_first_size(stream) == mask_first_size(ref)
