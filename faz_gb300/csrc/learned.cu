@@ -594,7 +594,9 @@ void learned_tune_device(faz_config &c, const T *dX, cudaStream_t st, const Tune
         if (c.dims[i] < (uint64_t)FEB) return use_plain(3);
     qoz_prepare<T>(c, dX, st, launches);
     const int Lsel = c.levelwisePredictionSelection;
-    if (Lsel < 1 || Lsel > 4 || !(c.autoTuningRate > 0)) return use_plain(3);
+    // the network predicts the RD-target decisions of the default sampling
+    if (Lsel < 1 || Lsel > 4 || !(c.autoTuningRate > 0) || c.tuningTarget != 0 || c.profiling || c.var_first)
+        return use_plain(3);
     DevMem m(st);
     float *dF = m.alloc<float>(IN), *dZ = m.alloc<float>(OUT);
     tuner_features_device<T>(c, dX, st, dF, launches);

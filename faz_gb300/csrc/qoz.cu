@@ -500,7 +500,8 @@ template <typename T>
 int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) {
     const int N = c.N;
     if (N != 2 && N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for 2-D and 3-D data"};
-    if (c.tuningTarget != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for the PSNR (RD) target"};
+    if (c.tuningTarget > 1)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for the PSNR (RD) and ratio (CR) targets"};
     if (c.rng < 0) c.rng = device_range<T>(dX, c.num, st, launches);
     if (c.relErrorBound <= 0) c.relErrorBound = c.absErrorBound / c.rng;
     // waveAutoFix (default 1, not a Config field here) turns the Lorenzo
@@ -840,8 +841,12 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     if (c.autoTuningRate > 0) {
         // B-M tuning (SZInterp.hpp:2187-2515): CompressTest per alpha/beta
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
-        static const double alist[] = {1, 1.25, 1.5, 1.75, 2};
-        static const double blist[] = {1.5, 2, 3, 4};
+        // init_alphalist / init_betalist (SZInterp.hpp:868-933); the CR target
+        // compares bit rates alone (its CompressTest metric is 0)
+        const bool cr = c.tuningTarget == 1;
+        static const std::vector<double> alist_rd{1, 1.25, 1.5, 1.75, 2}, blist_rd{1.5, 2, 3, 4};
+        static const std::vector<double> alist_cr{-1, 1, 1.25, 1.5, 1.75, 2}, blist_cr{-1, 1.5, 2, 3};
+        const std::vector<double> &alist = cr ? alist_cr : alist_rd, &blist = cr ? blist_cr : blist_rd;
         const double oriabseb = c.absErrorBound;
         auto stop_here = [&](double alpha, double beta) {
             return (alpha >= 1 && std::pow(alpha, max_interp_level - 1) <= beta) ||
@@ -852,18 +857,20 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
                 if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
                 double br, mm;
                 compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb, br, mm, true, pcoeff);
-                if (mm >= bestm && br <= bestb) {
+                if (cr) mm = 0;
+                if ((!cr && mm >= bestm && br <= bestb) || (cr && br <= bestb)) {
                     bestalpha = alpha;
                     bestbeta = beta;
                     bestb = br;
                     bestm = mm;
-                } else if (mm <= bestm && br >= bestb) {
+                } else if ((!cr && mm <= bestm && br >= bestb) || (cr && br > bestb)) {
                     if (stop_here(alpha, beta)) break;
                     continue;
                 } else {
                     const double fix = br / bestb;
                     double br2, m2;
                     compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb * fix, br2, m2, true, pcoeff);
+                    if (cr) m2 = 0;
                     const double a = (mm - m2) / (br - br2);
                     const double b = mm - a * br;
                     const double reg = a * bestb + b;
@@ -883,17 +890,19 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             // against the best alpha/beta point (SZInterp.hpp:2428-2486)
             double br, mm;
             lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb, c.rng, pcoeff, st, launches, br, mm);
-            if (mm >= bestm && br <= bestb) {
+            if (cr) mm = 0;
+            if ((!cr && mm >= bestm && br <= bestb) || (cr && br <= bestb)) {
                 bestb = br;
                 bestm = mm;
                 bestalpha = bestbeta = -1;
                 use_interp = false;
-            } else if (mm <= bestm && br >= bestb) {
+            } else if ((!cr && mm <= bestm && br >= bestb) || (cr && br > bestb)) {
                 use_interp = true;
             } else {
                 const double fix = br / bestb;
                 double br2, m2;
                 lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb * fix, c.rng, pcoeff, st, launches, br2, m2);
+                if (cr) m2 = 0;
                 const double a = (mm - m2) / (br - br2);
                 if (a > 0) {
                     const double b = mm - a * br;

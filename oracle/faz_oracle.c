@@ -862,7 +862,7 @@ static double data_range(int dtype, const void *data, size_t n) {
 static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     int N = conf->N;
     if (N != 2 && N != 3) { set_err("oracle QoZ tuner covers 2-D and 3-D data"); return -2; }
-    if (conf->tuningTarget != 0 || conf->wavelet > 0 || conf->FZ) { set_err("oracle QoZ tuner covers the RD target"); return -2; }
+    if (conf->tuningTarget > 1 || conf->wavelet > 0 || conf->FZ) { set_err("oracle QoZ tuner covers the RD and CR targets"); return -2; }
     size_t es = dtype == FAZ_FLOAT ? 4 : 8;
     double rngT = dtype == FAZ_FLOAT ? (double)(float)conf->rng : conf->rng;   /* T rng = conf.rng */
     double rel_bound = conf->relErrorBound > 0 ? conf->relErrorBound : conf->absErrorBound / rngT;
@@ -1084,11 +1084,16 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     }
     if (conf->autoTuningRate > 0) {
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
-        static const double alist[] = {1, 1.25, 1.5, 1.75, 2};
-        static const double blist[] = {1.5, 2, 3, 4};
+        /* init_alphalist / init_betalist (SZInterp.hpp:868-933); the CR
+         * target compares bit rates alone (its CompressTest metric is 0) */
+        const int cr = conf->tuningTarget == 1;
+        static const double alist_rd[] = {1, 1.25, 1.5, 1.75, 2}, blist_rd[] = {1.5, 2, 3, 4};
+        static const double alist_cr[] = {-1, 1, 1.25, 1.5, 1.75, 2}, blist_cr[] = {-1, 1.5, 2, 3};
+        const double *alist = cr ? alist_cr : alist_rd, *blist = cr ? blist_cr : blist_rd;
+        const int na = cr ? 6 : 5, nbeta = 4;
         double oriabseb = conf->absErrorBound;
-        for (int i = 0; i < 5; i++) {
-            for (int j = 0; j < 4; j++) {
+        for (int i = 0; i < na; i++) {
+            for (int j = 0; j < nbeta; j++) {
                 double alpha = alist[i], beta = blist[j];
                 conf->absErrorBound = oriabseb;
                 if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
@@ -1101,9 +1106,10 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                              : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
                                                      conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br, &m);
                 if (rc) { free(blocks); return rc; }
-                if (m >= bestm && br <= bestb) {
+                if (cr) m = 0;
+                if ((!cr && m >= bestm && br <= bestb) || (cr && br <= bestb)) {
                     bestalpha = alpha; bestbeta = beta; bestb = br; bestm = m;
-                } else if (m <= bestm && br >= bestb) {
+                } else if ((!cr && m <= bestm && br >= bestb) || (cr && br > bestb)) {
                     if ((alpha >= 1 && pow(alpha, max_interp_level - 1) <= beta) ||
                         (alpha < 1 && alpha * (max_interp_level - 1) <= beta))
                         break;
@@ -1117,6 +1123,7 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                              : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound * fix,
                                                      conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br2, &m2);
                     if (rc) { free(blocks); return rc; }
+                    if (cr) m2 = 0;
                     double a = (m - m2) / (br - br2);
                     double bb = m - a * br;
                     double reg = a * bestb + bb;
@@ -1135,9 +1142,10 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             int rc = dtype == FAZ_FLOAT ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb, conf->rng, pcoeff, &br, &m)
                                         : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb, conf->rng, pcoeff, &br, &m);
             if (rc) { free(blocks); return rc; }
-            if (m >= bestm && br <= bestb) {
+            if (cr) m = 0;
+            if ((!cr && m >= bestm && br <= bestb) || (cr && br <= bestb)) {
                 bestb = br; bestm = m; bestalpha = -1; bestbeta = -1; use_interp = 0;
-            } else if (m <= bestm && br >= bestb) {
+            } else if ((!cr && m <= bestm && br >= bestb) || (cr && br > bestb)) {
                 use_interp = 1;
             } else {
                 double fix = br / bestb, br2, m2;
@@ -1145,6 +1153,7 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                          ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, pcoeff, &br2, &m2)
                          : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, pcoeff, &br2, &m2);
                 if (rc) { free(blocks); return rc; }
+                if (cr) m2 = 0;
                 double a = (m - m2) / (br - br2);
                 if (a > 0) {
                     double b = m - a * br;

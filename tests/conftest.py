@@ -90,6 +90,9 @@ def cli_config(case):
         a = cp["AlgoSettings"] if cp.has_section("AlgoSettings") else {}
         if "CmprAlgo" in g:
             conf.cmprAlgo = ALGO_STR.index(g["CmprAlgo"])
+        if "tuningTarget" in g:
+            conf.tuningTarget = ["TUNING_TARGET_RD", "TUNING_TARGET_CR", "TUNING_TARGET_SSIM",
+                                 "TUNING_TARGET_AC"].index(g["tuningTarget"])
         if "OpenMP" in g:
             conf.openmp = 1 if g["OpenMP"].strip().lower() in ("true", "yes", "on", "1") else 0
         if "InterpolationAlgo" in a:

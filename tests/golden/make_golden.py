@@ -200,6 +200,16 @@ def cases():
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
                                                         "var_first": "1", "profiling": "1",
                                                         "levelwisePredictionSelection": "6", "maxStep": "64"}}))
+    # the compression-ratio tuning target (TUNING_TARGET_CR: alpha/beta lists
+    # with -1, bit rates compared alone)
+    out.append(("cr_target_3d", spectral_field((64, 80, 96), slope=-3.0, noise=0.01, seed=99), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_CR"},
+                 "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                  "levelwisePredictionSelection": "4", "maxStep": "32", "sampleBlockSize": "16"}}))
+    out.append(("cr_target_lorenzo", sum2d((64, 72, 80), 1e-4, 101), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_CR"},
+                 "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01", "testLorenzo": "1",
+                                  "sampleBlockSize": "16"}}))
     out.append(("rate_ab_only", spectral_field((48, 56, 64), slope=-3.0, seed=82), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01"}}))
     out.append(("rate_2d", spectral_field((400, 500), slope=-3.0, seed=83), ["-M", "REL", "5e-3"],

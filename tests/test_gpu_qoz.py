@@ -275,3 +275,27 @@ def test_gpu_var_first_sampling_matches_oracle(dims, rel, settings, frac):
     _, p = O.read_stream(stream)
     assert p == ref_payload
     assert mask_first_size(stream) == mask_first_size(ref)
+
+
+@pytest.mark.parametrize("dims,rel,kind", [((64, 80, 96), 1e-3, "spectral"), ((300, 420), 1e-3, "spectral"),
+                                           ((64, 72, 80), 1e-3, "planes")])
+def test_gpu_cr_target_matches_oracle(dims, rel, kind):
+    """TUNING_TARGET_CR: the alpha/beta lists with -1 and bit rates compared alone."""
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = rel
+    conf.tuningTarget = 1
+    conf.autoTuningRate = conf.predictorTuningRate = 0.01
+    conf.testLorenzo = 1
+    conf.sampleBlockSize = 16
+    x = _sum_of_planes(dims, 1e-4, 7, np.float32) if kind == "planes" else \
+        spectral_field(dims, slope=-2.5, noise=0.02, seed=sum(dims))
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    c1, p = O.read_stream(stream)
+    c2, _ = O.read_stream(ref)
+    assert (c1.cmprAlgo, c1.alpha, c1.beta) == (c2.cmprAlgo, c2.alpha, c2.beta)
+    if c1.cmprAlgo == 0 and len(dims) == 3:
+        assert mask_fast_frontend_padding(p, x.itemsize) == mask_fast_frontend_padding(ref_payload, x.itemsize)
+    else:
+        assert p == ref_payload
