@@ -844,9 +844,13 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         // init_alphalist / init_betalist (SZInterp.hpp:868-933); the CR target
         // compares bit rates alone (its CompressTest metric is 0)
         const bool cr = c.tuningTarget == 1;
-        static const std::vector<double> alist_rd{1, 1.25, 1.5, 1.75, 2}, blist_rd{1.5, 2, 3, 4};
+        // abList 0, 1, 2: alpha up to 2, 2.5, 3
+        static const std::vector<double> alist0{1, 1.25, 1.5, 1.75, 2}, alist1{1, 1.25, 1.5, 1.75, 2, 2.25, 2.5},
+            alist2{1, 1.25, 1.5, 1.75, 2, 2.25, 2.5, 2.75, 3}, blist_rd{1.5, 2, 3, 4};
         static const std::vector<double> alist_cr{-1, 1, 1.25, 1.5, 1.75, 2}, blist_cr{-1, 1.5, 2, 3};
-        const std::vector<double> &alist = cr ? alist_cr : alist_rd, &blist = cr ? blist_cr : blist_rd;
+        const std::vector<double> &alist =
+            cr ? alist_cr : (c.abList == 0 ? alist0 : (c.abList == 1 ? alist1 : alist2));
+        const std::vector<double> &blist = cr ? blist_cr : blist_rd;
         const double oriabseb = c.absErrorBound;
         auto stop_here = [&](double alpha, double beta) {
             return (alpha >= 1 && std::pow(alpha, max_interp_level - 1) <= beta) ||

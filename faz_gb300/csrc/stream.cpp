@@ -187,6 +187,7 @@ int config_load_ini(faz_config *c, const char *path, std::string &err) {
     c->testLorenzo = (int32_t)ini.integer(A, "testLorenzo", c->testLorenzo);
     c->profiling = (int32_t)ini.integer(A, "profiling", c->profiling);
     c->var_first = (int32_t)ini.integer(A, "var_first", c->var_first);
+    c->abList = (int32_t)ini.integer(A, "abList", c->abList);
     c->SSIMBlockSize = (int32_t)ini.integer(A, "SSIMBlockSize", c->SSIMBlockSize);
     c->fixBlockSize = (int32_t)ini.integer(A, "fixBlockSize", c->fixBlockSize);
     c->verbose = ini.boolean(A, "verbose", c->verbose);
@@ -195,7 +196,6 @@ int config_load_ini(faz_config *c, const char *path, std::string &err) {
     c->sperrWithoutWave = ini.boolean(A, "sperrWithoutWave", c->sperrWithoutWave);
     c->pyBind = ini.boolean(A, "pyBind", c->pyBind);
     c->blockwiseSampleBlockSize = (int32_t)ini.integer(A, "blockwiseSampleBlockSize", c->blockwiseSampleBlockSize);
-    c->abList = (int32_t)ini.integer(A, "abList", c->abList);
     c->crossBlock = (int32_t)ini.integer(A, "crossBlock", c->crossBlock);
     c->sampleBlockSampleBlockSize =
         (int32_t)ini.integer(A, "sampleBlockSampleBlockSize", c->sampleBlockSampleBlockSize);

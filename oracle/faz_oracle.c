@@ -1087,10 +1087,11 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         /* init_alphalist / init_betalist (SZInterp.hpp:868-933); the CR
          * target compares bit rates alone (its CompressTest metric is 0) */
         const int cr = conf->tuningTarget == 1;
-        static const double alist_rd[] = {1, 1.25, 1.5, 1.75, 2}, blist_rd[] = {1.5, 2, 3, 4};
+        static const double alist_rd[] = {1, 1.25, 1.5, 1.75, 2, 2.25, 2.5, 2.75, 3}, blist_rd[] = {1.5, 2, 3, 4};
         static const double alist_cr[] = {-1, 1, 1.25, 1.5, 1.75, 2}, blist_cr[] = {-1, 1.5, 2, 3};
         const double *alist = cr ? alist_cr : alist_rd, *blist = cr ? blist_cr : blist_rd;
-        const int na = cr ? 6 : 5, nbeta = 4;
+        /* abList 0, 1, 2: alpha up to 2, 2.5, 3 */
+        const int na = cr ? 6 : (conf->abList == 0 ? 5 : (conf->abList == 1 ? 7 : 9)), nbeta = 4;
         double oriabseb = conf->absErrorBound;
         for (int i = 0; i < na; i++) {
             for (int j = 0; j < nbeta; j++) {

@@ -299,3 +299,19 @@ def test_gpu_cr_target_matches_oracle(dims, rel, kind):
         assert mask_fast_frontend_padding(p, x.itemsize) == mask_fast_frontend_padding(ref_payload, x.itemsize)
     else:
         assert p == ref_payload
+
+
+@pytest.mark.parametrize("ab", [1, 2])
+def test_gpu_ablist_matches_oracle(ab):
+    """abList 1 / 2: the alpha list runs to 2.5 / 3."""
+    dims = (80, 96, 112)
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = 1e-2
+    conf.autoTuningRate = conf.predictorTuningRate = 0.01
+    conf.abList = ab
+    conf.sampleBlockSize = 16
+    x = spectral_field(dims, slope=-3.5, noise=0.005, seed=ab)
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    assert O.read_stream(stream)[1] == ref_payload
