@@ -2,8 +2,10 @@
 """FAZ interpolation compress/decompress benchmark on GB300.
 
 Workload: one 512x512x512 float32 spectral field (k^-3.5, anisotropic
-correlation lengths 1:2:4, 1% noise, seeded, synthetic), relative error bound
-1e-3, cubic interpolation (ALGO_INTERP).  A step is one compression of the
+correlation lengths 1:2:4, 1% noise, scaled to [-50, 80], seeded, synthetic;
+numpy's generator, so that both arms and the parity tests see the same
+values), relative error bound 1e-3, the default configuration (the SZ3 sampled
+autotune, then the compressor it chooses).  A step is one compression of the
 field; decompression is timed the same way and reported beside it.
 
   value       compress GB/s (input bytes / time) with the field resident in
@@ -11,15 +13,25 @@ field; decompression is timed the same way and reported beside it.
               memory (CUDA events on the call's stream).
   e2e         compress GB/s through faz_compress, the C ABI (host input in pinned
               memory, host->device copy, GPU path, payload copy back, host
-              zstd, trailer), host clock.
+              zstd, trailer), host clock.  The body is one level-3 zstd frame
+              (the reference's format), written by zstd's worker threads;
+              e2e_zstd_single_thread writes it with ZSTD_compress on one
+              thread (the reference's call, byte for byte), e2e_multiframe as
+              independent frames (a format extension).
   roofline    the finest interpolation level kernel (the dominant kernel):
               algorithmic bytes per launch / CUDA-event duration vs the
               measured HBM copy bandwidth.
+  compress_frac / decompress_frac
+              (input bytes + payload bytes) / time / measured HBM bandwidth
+              for the whole device-resident compression / decompression.
+  eb_sweep    value, decompression, ratio and the tuner's choice at relative
+              bounds 1e-2 .. 1e-5.
   cpu_baseline  the CPU oracle (a restatement of the reference) on a slab
               of the same field, one thread.
 
 --impl reference times the CPU restatement of the reference on all host
-cores (one slab per worker process) on the same metric.
+cores: every worker process compresses and decompresses the whole field (the
+same stream as the GPU arm's), independent replicas of the workload.
 Under torchrun every rank compresses its own field (independent replicas,
 weak scaling); rank 0 prints the line.
 """
@@ -52,6 +64,7 @@ def parse():
                     help="auto: the default configuration (ALGO_INTERP_LORENZO, sampled autotune); "
                          "interp: ALGO_INTERP with --interp")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the relative-bound sweep 1e-2 .. 1e-5")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-sampled autotune comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-fields measurement")
     ap.add_argument("--no-combined", action="store_true", help="skip the combined f64 learned + batched workload")
@@ -146,20 +159,48 @@ def finest_level_bytes(dims, itemsize):
     return (n - coarse) * (itemsize + 2) + coarse * itemsize
 
 
+def bench_field(dims, seed):
+    """The benchmark's field (numpy generator, seeded)."""
+    from faz_gb300.fields import spectral_field
+    return spectral_field(dims, slope=-3.5, aniso=(1, 2, 4), noise=0.01, seed=seed)
+
+
+def workload_name(dims, args):
+    what = ("default configuration: SZ3 sampled autotune (Lorenzo vs interpolation trials) then the chosen "
+            "compressor" if args.algo == "auto" else f"ALGO_INTERP {args.interp}")
+    return f"{dims[0]}x{dims[1]}x{dims[2]} float32 spectral field, rel eb {args.eb:g}, {what}"
+
+
+def bench_config(dims, args):
+    """The `config` of the JSON line, the same in both arms."""
+    nbytes = 4 * dims[0] * dims[1] * dims[2]
+    l2 = ("inputs larger than L2" if nbytes > L2_BYTES else "inputs smaller than L2 (not flushed)")
+    return {"workload": workload_name(dims, args), "eb_mode": "REL", "eb": args.eb,
+            "l2": "%s (field %.0f MB vs 129 MB L2)" % (l2, nbytes / 1e6)}
+
+
+DATA = "synthetic: seeded spectral field k^-3.5, aniso 1:2:4, 1% noise, scaled to [-50,80]"
+
+
 # ------------------------------------------------------------- CPU oracle
-def _cpu_slab_job(args):
-    path, shape, offset, eb, interp, algo, reps = args
-    import numpy as np
-    sys.path.insert(0, ROOT)
-    from oracle import oracle as O
+def _oracle_conf(shape, eb, interp, algo):
     import faz_gb300.config as C
-    x = np.fromfile(path, dtype=np.float32, count=int(np.prod(shape)), offset=offset).reshape(shape)
     conf = C.Config(*shape)
     if algo == "interp":
         conf.cmprAlgo = C.ALGO_INTERP
         conf.interpAlgo = C.INTERP_ALGO_CUBIC if interp == "cubic" else C.INTERP_ALGO_LINEAR
     conf.errorBoundMode = C.EB_REL
     conf.relErrorBound = eb
+    return conf
+
+
+def _cpu_slab_job(args):
+    path, shape, offset, eb, interp, algo, reps = args
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    x = np.fromfile(path, dtype=np.float32, count=int(np.prod(shape)), offset=offset).reshape(shape)
+    conf = _oracle_conf(shape, eb, interp, algo)
     tc = td = 0.0
     size = 0
     for _ in range(reps):
@@ -186,60 +227,77 @@ def cpu_oracle_single(field_np, slab, eb, interp, algo):
     return nb / tc / 1e9, nb / td / 1e9, shape
 
 
+# Worker state of the reference arm: the field (loaded once per process) and
+# the last stream it compressed.
+_REF = {}
+
+
+def _ref_init(path, shape, eb, interp, algo):
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    _REF["x"] = np.fromfile(path, dtype=np.float32).reshape(shape)
+    _REF["conf"] = _oracle_conf(shape, eb, interp, algo)
+
+
+def _ref_compress(_):
+    from oracle import oracle as O
+    s, _ = O.compress(_REF["conf"], _REF["x"])
+    _REF["s"] = s
+    return len(s)
+
+
+def _ref_decompress(_):
+    from oracle import oracle as O
+    O.decompress(_REF["s"])
+    return 0
+
+
 def reference_arm(args, dims):
-    """CPU restatement of the reference on all host cores: one slab per worker."""
+    """The CPU restatement of the reference on all host cores: each worker
+    process compresses, then decompresses, the whole field per step (the same
+    field, configuration and stream as the GPU arm: independent replicas);
+    compression and decompression are timed separately across all workers."""
     import multiprocessing as mp
     import numpy as np
-    from faz_gb300.fields import spectral_field
     cores = os.cpu_count() or 1
-    slab = max(8, min(64, dims[0] // max(1, cores)))
-    nslab = min(cores, dims[0] // slab)
-    sdims = (slab * nslab,) + tuple(dims[1:])
-    x = spectral_field(sdims, slope=-3.5, aniso=(1, 2, 4), noise=0.01, seed=2024)
+    x = bench_field(dims, 1000)
     with tempfile.NamedTemporaryFile(suffix=".f32", delete=False, dir="/dev/shm" if os.path.isdir("/dev/shm") else None) as f:
         x.tofile(f)
         path = f.name
-    plane = int(np.prod(dims[1:])) * 4
-    jobs = [(path, (slab,) + tuple(dims[1:]), i * slab * plane, args.eb, args.interp, args.algo, 1)
-            for i in range(nslab)]
+    nbytes = x.nbytes
+    del x
     ctx = mp.get_context("spawn")
     times_c, times_d, sizes = [], [], []
     try:
-        with ctx.Pool(nslab) as pool:
+        with ctx.Pool(cores, initializer=_ref_init, initargs=(path, dims, args.eb, args.interp, args.algo)) as pool:
             for step in range(args.warmup + args.steps):
                 t0 = time.perf_counter()
-                res = pool.map(_cpu_slab_job, jobs)
-                wall = time.perf_counter() - t0
+                res = pool.map(_ref_compress, range(cores), chunksize=1)
+                tc = time.perf_counter() - t0
+                t0 = time.perf_counter()
+                pool.map(_ref_decompress, range(cores), chunksize=1)
+                td = time.perf_counter() - t0
                 if step >= args.warmup:
-                    # workers run compress then decompress; split the wall time by their ratio
-                    tc = sum(r[0] for r in res)
-                    td = sum(r[1] for r in res)
-                    times_c.append(wall * tc / (tc + td))
-                    times_d.append(wall * td / (tc + td))
-                    sizes.append(sum(r[2] for r in res))
+                    times_c.append(tc)
+                    times_d.append(td)
+                    sizes.append(res[0])
     finally:
         os.unlink(path)
-    nbytes = x.nbytes
     tc = statistics.median(times_c)
     td = statistics.median(times_d)
-    v = nbytes / tc / 1e9
-    sample = f"{nslab} slabs of {slab}x{dims[1]}x{dims[2]} float32 ({nbytes / 1e6:.0f} MB) per step, one per process"
+    v = cores * nbytes / tc / 1e9
+    sample = (f"{cores} worker processes, each compressing and decompressing the whole {dims[0]}x{dims[1]}x{dims[2]} "
+              f"float32 field ({nbytes / 1e6:.0f} MB) per step")
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GB/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tc * 1e3, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: seeded spectral field k^-3.5, aniso 1:2:4, 1% noise",
-            "config": {"workload": workload_name(dims, args), "eb_mode": "REL", "eb": args.eb},
-            "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": nslab, "kind": "port", "sample": sample},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": bench_config(dims, args),
+            "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": round(v, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "decompress": {"value": round(nbytes / td / 1e9, 4), "unit": "GB/s", "ms_per_step": round(td * 1e3, 3)},
+            "decompress": {"value": round(cores * nbytes / td / 1e9, 4), "unit": "GB/s",
+                           "ms_per_step": round(td * 1e3, 3)},
             "ratio": round(nbytes / statistics.median(sizes), 3)}
     return line
-
-
-def workload_name(dims, args):
-    what = ("default configuration: SZ3 sampled autotune (Lorenzo vs interpolation trials) then the chosen "
-            "compressor" if args.algo == "auto" else f"ALGO_INTERP {args.interp}")
-    return f"{dims[0]}x{dims[1]}x{dims[2]} float32 spectral field, rel eb {args.eb:g}, {what}"
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -390,6 +448,155 @@ def learned_vs_sampled(x, dims, eb):
             "learned": "MLP 64->256->256->27 on block statistics, BF16 tcgen05 inference, plain tuner as fallback"}
 
 
+def device_compress_timing(F, conf, x, stream, pay_buf, steps, warmup, launches):
+    """Device-resident compression of x (CUDA events on `stream`): seconds per
+    step, the per-step timings, the last payload and the resolved Config."""
+    import torch
+    for _ in range(warmup):
+        payload, conf_out = F.compress_payload_device(conf, x, stream, out=pay_buf)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phases = []
+    ev0.record(stream)
+    for _ in range(steps):
+        payload, conf_out = F.compress_payload_device(conf, x, stream, out=pay_buf)
+        tm = F.last_timings()
+        launches[0] += tm["kernel_launches"]
+        phases.append(tm)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3 / steps, phases, payload, conf_out
+
+
+def device_decompress_timing(F, dims, conf_out, conf, x, payload, out, stream, steps, warmup, launches):
+    """Device-resident decompression (pre-zstd payload for interpolation
+    streams, the whole stream otherwise): seconds per step and timings."""
+    import torch
+    interp = conf_out.cmprAlgo == F.ALGO_INTERP
+    full = None if interp else F.compress_device(conf, x, stream)
+
+    def once():
+        if interp:
+            F.decompress_payload_device(len(dims), payload, out, stream)
+        else:
+            F.decompress_device(full, out, stream)
+    for _ in range(warmup):
+        once()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phases = []
+    ev0.record(stream)
+    for _ in range(steps):
+        once()
+        tm = F.last_timings()
+        launches[0] += tm["kernel_launches"]
+        phases.append(tm)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3 / steps, phases
+
+
+ALGO_NAMES = ["ALGO_LORENZO_REG", "ALGO_INTERP_LORENZO", "ALGO_INTERP", "ALGO_INTERP_BLOCKED"]
+
+
+def chosen(F, c):
+    d = {"cmprAlgo": ALGO_NAMES[c.cmprAlgo]}
+    if c.cmprAlgo == F.ALGO_INTERP:
+        d["interpAlgo"] = "cubic" if c.interpAlgo == F.INTERP_ALGO_CUBIC else "linear"
+        d["interpDirection"] = c.interpDirection
+    else:
+        d["quantbinCnt"] = c.quantbinCnt
+        d["pred_dim"] = c.pred_dim
+    return d
+
+
+def eb_sweep(F, dims, args, x, stream, pay_buf, out, peak, launches, rels=(1e-2, 1e-3, 1e-4, 1e-5)):
+    """The same field and configuration at relative bounds 1e-2 .. 1e-5:
+    device-resident compression and decompression, ratio of the whole stream,
+    the tuner's choice, and the whole-path fractions of the HBM roofline."""
+    nbytes = x.numel() * 4
+    res = {}
+    for rel in rels:
+        conf = make_conf(F, dims, rel, args.interp, args.algo)
+        tc, _, payload, conf_out = device_compress_timing(F, conf, x, stream, pay_buf, 3, 2, launches)
+        td, _ = device_decompress_timing(F, dims, conf_out, conf, x, payload, out, stream, 3, 2, launches)
+        P = len(payload)
+        ratio = nbytes / len(F.compress_device(conf, x, stream))
+        res[f"{rel:g}"] = {"value": round(nbytes / tc / 1e9, 3), "decompress": round(nbytes / td / 1e9, 3),
+                           "unit": "GB/s", "ratio": round(ratio, 3), "payload_bytes": P,
+                           "compress_frac": round((nbytes + P) / tc / 1e9 / peak, 4),
+                           "decompress_frac": round((nbytes + P) / td / 1e9 / peak, 4),
+                           "chosen": chosen(F, conf_out)}
+    return res
+
+
+def e2e_run(F, L, conf, dims, host_np, host_out, steps, warmup):
+    """faz_compress / faz_decompress (the C ABI with host buffers) timed on
+    the host clock: median seconds per compression and decompression, the
+    per-call parts, payload bytes and stream length."""
+    import ctypes
+    cs = conf.to_struct()
+    tmc = F.FazTimings()
+
+    def c_compress():
+        o, osz = ctypes.c_void_p(), ctypes.c_size_t()
+        F.api._check(L.faz_compress(ctypes.byref(cs), F.FAZ_FLOAT, host_np.ctypes.data, ctypes.byref(o),
+                                    ctypes.byref(osz), ctypes.byref(tmc)))
+        return o, osz.value
+
+    def c_decompress(buf, size):
+        ds = F.FazConfigStruct()
+        ds.num = host_out.size
+        ptr = ctypes.c_void_p(host_out.ctypes.data)
+        F.api._check(L.faz_decompress(ctypes.byref(ds), F.FAZ_FLOAT, buf, size, ctypes.byref(ptr),
+                                      ctypes.byref(tmc)))
+    for _ in range(warmup):
+        o, n_o = c_compress()
+        c_decompress(o, n_o)
+        L.faz_free(o)
+    tc, td, zc, zd, parts = [], [], [], [], []
+    d2h = n_stream = 0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o, n_o = c_compress()
+        tc.append(time.perf_counter() - t0)
+        zc.append(tmc.zstd_ms)
+        parts.append({"h2d_ms": tmc.h2d_ms, "gpu_ms": tmc.gpu_ms, "zstd_ms": tmc.zstd_ms, "call_ms": tmc.total_ms})
+        d2h = tmc.payload_bytes
+        n_stream = n_o
+        t0 = time.perf_counter()
+        c_decompress(o, n_o)
+        td.append(time.perf_counter() - t0)
+        zd.append(tmc.zstd_ms)
+        L.faz_free(o)
+    med = statistics.median
+    return {"tc": med(tc), "td": med(td), "zc": med(zc), "zd": med(zd), "d2h": d2h, "stream": n_stream,
+            "parts": {k: round(med(p[k] for p in parts), 3) for k in ("h2d_ms", "gpu_ms", "zstd_ms", "call_ms")}}
+
+
+class _env:
+    """Environment variables set for the duration of a block."""
+
+    def __init__(self, **kv):
+        self.kv = kv
+        self.old = {}
+
+    def __enter__(self):
+        for k, v in self.kv.items():
+            self.old[k] = os.environ.get(k)
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+    def __exit__(self, *a):
+        for k, v in self.old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
 def main():
     args = parse()
     dims = tuple(int(d) for d in args.dims.split(","))
@@ -405,7 +612,6 @@ def main():
     import numpy as np
     import torch
     import faz_gb300 as F
-    from faz_gb300.fields import spectral_field
     from faz_gb300 import build as B
     B.build()
 
@@ -422,123 +628,58 @@ def main():
         torch.cuda.synchronize()
 
     conf = make_conf(F, dims, args.eb, args.interp, args.algo)
-    x = spectral_field(dims, slope=-3.5, aniso=(1, 2, 4), noise=0.01, seed=1000 + rank, device="cuda")
+    x_np = bench_field(dims, 1000 + rank)
+    x = torch.from_numpy(x_np).to("cuda")
     nbytes = x.numel() * x.element_size()
     stream = torch.cuda.Stream()
     out = torch.empty_like(x)
     pay_buf = torch.empty(nbytes + (4 << 20), dtype=torch.uint8, pin_memory=True)
+    peak, peak_kind = peaks()
+    launches = [0]
 
     # ---- device-resident compress (value) and decompress
-    launches = 0
-    for _ in range(args.warmup):
-        payload, conf_out = F.compress_payload_device(conf, x, stream, out=pay_buf)
-    interp_chosen = conf_out.cmprAlgo == F.ALGO_INTERP
-    full_stream = None if interp_chosen else F.compress_device(conf, x, stream)
-
-    def decompress_once():
-        if interp_chosen:
-            F.decompress_payload_device(len(dims), payload, out, stream)
-        else:
-            F.decompress_device(full_stream, out, stream)
-
-    for _ in range(args.warmup):
-        decompress_once()
     barrier()
-    t_steps, phases = [], []
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(local) as clk:
         barrier()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            payload, conf_out = F.compress_payload_device(conf, x, stream, out=pay_buf)
-            tm = F.last_timings()
-            launches += tm["kernel_launches"]
-            phases.append(tm)
-        ev1.record(stream)
+        t_comp, phases, payload, conf_out = device_compress_timing(F, conf, x, stream, pay_buf, args.steps,
+                                                                   args.warmup, launches)
         barrier()
-        t_comp = ev0.elapsed_time(ev1) / 1e3 / args.steps
-        dphases = []
-        ev0.record(stream)
-        for _ in range(args.steps):
-            decompress_once()
-            tm = F.last_timings()
-            launches += tm["kernel_launches"]
-            dphases.append(tm)
-        ev1.record(stream)
+        t_dec, dphases = device_decompress_timing(F, dims, conf_out, conf, x, payload, out, stream, args.steps,
+                                                  args.warmup, launches)
         barrier()
-        t_dec = ev0.elapsed_time(ev1) / 1e3 / args.steps
         # the plain interpolation compressor alone (ALGO_INTERP cubic), for reference
         t_plain = None
         if args.algo == "auto":
             pconf = make_conf(F, dims, args.eb, "cubic", "interp")
-            for _ in range(2):
-                F.compress_payload_device(pconf, x, stream, out=pay_buf)
+            t_plain, _, _, _ = device_compress_timing(F, pconf, x, stream, pay_buf, args.steps, 2, launches)
             barrier()
-            ev0.record(stream)
-            for _ in range(args.steps):
-                F.compress_payload_device(pconf, x, stream, out=pay_buf)
-                launches += F.last_timings()["kernel_launches"]
-            ev1.record(stream)
-            barrier()
-            t_plain = ev0.elapsed_time(ev1) / 1e3 / args.steps
     clocks = clk.summary()
+    psize = len(payload)
     err = (out.double() - x.double()).abs().max().item()
     assert err <= conf_out.absErrorBound, (err, conf_out.absErrorBound)
 
     # ---- end to end through the C ABI with host buffers (faz_compress /
     # faz_decompress: the calls a binding of the reference's SZ_compress /
     # SZ_decompress makes), host clock
-    import ctypes
     L = F.library()
     host_in = torch.empty(dims, dtype=torch.float32, pin_memory=True)
     host_in.copy_(x.cpu())
     host_np = host_in.numpy()
     host_out = torch.empty(dims, dtype=torch.float32, pin_memory=True).numpy().reshape(-1)
-    cs = conf.to_struct()
-    tmc = F.FazTimings()
-
-    def c_compress():
-        out, osz = ctypes.c_void_p(), ctypes.c_size_t()
-        F.api._check(L.faz_compress(ctypes.byref(cs), F.FAZ_FLOAT, host_np.ctypes.data, ctypes.byref(out),
-                                    ctypes.byref(osz), ctypes.byref(tmc)))
-        return out, osz.value
-
-    def c_decompress(buf, size):
-        ds = F.FazConfigStruct()
-        ds.num = host_out.size
-        ptr = ctypes.c_void_p(host_out.ctypes.data)
-        F.api._check(L.faz_decompress(ctypes.byref(ds), F.FAZ_FLOAT, buf, size, ctypes.byref(ptr),
-                                      ctypes.byref(tmc)))
-
-    for _ in range(max(1, args.warmup // 2)):
-        o, n_o = c_compress()
-        c_decompress(o, n_o)
-        L.faz_free(o)
     barrier()
-    e2e_c, e2e_d, zc, zd, d2h_bytes = [], [], [], [], 0
-    e2e_parts = []
-    stream_len = 0
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        o, n_o = c_compress()
-        e2e_c.append(time.perf_counter() - t0)
-        zc.append(tmc.zstd_ms)
-        e2e_parts.append({"h2d_ms": tmc.h2d_ms, "gpu_ms": tmc.gpu_ms, "zstd_ms": tmc.zstd_ms,
-                          "call_ms": tmc.total_ms})
-        d2h_bytes = tmc.payload_bytes
-        stream_len = n_o
-        t0 = time.perf_counter()
-        c_decompress(o, n_o)
-        e2e_d.append(time.perf_counter() - t0)
-        zd.append(tmc.zstd_ms)
-        L.faz_free(o)
-    ratio = nbytes / stream_len
+    e2e_w = max(1, args.warmup // 2)
+    with _env(FAZ_ZSTD_THREADS=None, FAZ_ZSTD_MULTIFRAME=None):
+        e_one = e2e_run(F, L, conf, dims, host_np, host_out, args.steps, e2e_w)
     dec = host_out.reshape(dims)
     assert np.abs(dec.astype(np.float64) - host_np.astype(np.float64)).max() <= conf_out.absErrorBound
+    with _env(FAZ_ZSTD_THREADS="0", FAZ_ZSTD_MULTIFRAME=None):
+        e_st = e2e_run(F, L, conf, dims, host_np, host_out, max(2, args.steps // 4), 1)
+    with _env(FAZ_ZSTD_THREADS=None, FAZ_ZSTD_MULTIFRAME="1"):
+        e_mf = e2e_run(F, L, conf, dims, host_np, host_out, max(2, args.steps // 4), 1)
+    ratio = nbytes / e_one["stream"]
 
     # ---- max over ranks
-    vals = torch.tensor([t_comp, t_dec, statistics.median(e2e_c), statistics.median(e2e_d)], device="cuda",
-                        dtype=torch.float64)
+    vals = torch.tensor([t_comp, t_dec, e_one["tc"], e_one["td"]], device="cuda", dtype=torch.float64)
     if dist is not None:
         dist.all_reduce(vals, op=dist.ReduceOp.MAX)
     t_comp, t_dec, te2e_c, te2e_d = vals.tolist()
@@ -546,8 +687,8 @@ def main():
         dist.destroy_process_group()
         return
 
-    peak, peak_kind = peaks()
     nvals = dims[0] * dims[1] * dims[2]
+    interp_chosen = conf_out.cmprAlgo == F.ALGO_INTERP
     cubic = conf_out.interpAlgo == F.INTERP_ALGO_CUBIC
     roof = None
     if interp_chosen:
@@ -564,14 +705,26 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         slab = 64
-        cc, cd, shape = cpu_oracle_single(x[:slab].cpu().numpy(), slab, args.eb, args.interp, args.algo)
+        cc, cd, shape = cpu_oracle_single(x_np[:slab], slab, args.eb, args.interp, args.algo)
         cpu = {"value": round(cc, 4), "unit": "GB/s", "cores": 1, "kind": "port",
                "sample": f"compress of a {shape[0]}x{shape[1]}x{shape[2]} slab of the same field, one thread "
                          f"(decompress {cd:.4f} GB/s)"}
+    sweep = None if args.no_sweep else eb_sweep(F, dims, args, x, stream, pay_buf, out, peak, launches)
     learned = None if args.no_learned else learned_vs_sampled(x, dims, args.eb)
     batch = None if args.no_batch else batched_fields(args.batch_fields, args.eb)
     combined = None if args.no_combined else combined_f64(args.combined_fields)
     med = lambda k, ph: round(statistics.median(p[k] for p in ph), 4)  # noqa: E731
+
+    def e2e_block(e, how):
+        return {"value": round(world * nbytes / e["tc"] / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": int(e["d2h"]), "ms_per_step": round(e["tc"] * 1e3, 3),
+                "decompress": round(world * nbytes / e["td"] / 1e9, 3),
+                "zstd_ms_compress": round(e["zc"], 3), "zstd_ms_decompress": round(e["zd"], 3),
+                "ratio": round(nbytes / e["stream"], 4), "zstd_body": how, "compress_parts_ms": e["parts"]}
+    e2e = e2e_block(e_one, "one level-3 zstd frame written by zstd's worker threads (the reference's format)")
+    e2e["value"] = round(world * nbytes / te2e_c / 1e9, 3)
+    e2e["decompress"] = round(world * nbytes / te2e_d / 1e9, 3)
+    e2e["api"] = "faz_compress / faz_decompress (C ABI, host buffers in pinned memory)"
     line = {
         "metric": METRIC,
         "value": round(world * nbytes / t_comp / 1e9, 3),
@@ -584,25 +737,22 @@ def main():
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic: seeded spectral field k^-3.5, aniso 1:2:4, 1% noise, scaled to [-50,80]",
-        "config": {"workload": workload_name(dims, args) + " (one field per GPU)",
-                   "eb_mode": "REL", "eb": args.eb, "abs_eb": conf_out.absErrorBound,
-                   "chosen": {"cmprAlgo": ["ALGO_LORENZO_REG", "ALGO_INTERP_LORENZO", "ALGO_INTERP"][conf_out.cmprAlgo],
-                              "interpAlgo": "cubic" if cubic else "linear",
-                              "interpDirection": conf_out.interpDirection},
-                   "l2": "inputs larger than L2 (field %.0f MB vs 129 MB L2)" % (nbytes / 1e6),
-                   "parallelism": f"replicas x{world}"},
+        "data": DATA,
+        "config": bench_config(dims, args),
+        "parallelism": f"replicas x{world} (one field per GPU)",
+        "abs_eb": conf_out.absErrorBound,
+        "chosen": chosen(F, conf_out),
         "ratio": round(ratio, 3),
+        "compress_frac": round((nbytes + psize) / t_comp / 1e9 / peak, 4),
+        "decompress_frac": round((nbytes + psize) / t_dec / 1e9 / peak, 4),
+        "payload_bytes": psize,
         "decompress": {"value": round(world * nbytes / t_dec / 1e9, 3), "unit": "GB/s",
-                       "ms_per_step": round(t_dec * 1e3, 3),
-                       "e2e": round(world * nbytes / te2e_d / 1e9, 3)},
-        "e2e": {"value": round(world * nbytes / te2e_c / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": int(d2h_bytes), "ms_per_step": round(te2e_c * 1e3, 3),
-                "zstd_ms_compress": round(statistics.median(zc), 3),
-                "zstd_ms_decompress": round(statistics.median(zd), 3),
-                "api": "faz_compress / faz_decompress (C ABI, host buffers in pinned memory)",
-                "compress_parts_ms": {k: round(statistics.median(p[k] for p in e2e_parts), 3)
-                                      for k in ("h2d_ms", "gpu_ms", "zstd_ms", "call_ms")}},
+                       "ms_per_step": round(t_dec * 1e3, 3)},
+        "e2e": e2e,
+        "e2e_zstd_single_thread": e2e_block(e_st, "one level-3 frame by ZSTD_compress on one thread "
+                                                  "(the reference's call, byte for byte)"),
+        "e2e_multiframe": e2e_block(e_mf, "independent level-3 frames of 4 MiB+ slices (format extension; "
+                                          "ZSTD_decompress reads it)"),
         "roofline": roof,
         "phases_ms": {"compress": {k: med(k, phases) for k in ("tune_ms", "predict_ms", "finest_level_ms",
                                                                "huffman_ms", "host_ms", "gpu_ms")},
@@ -610,7 +760,8 @@ def main():
                                                                   "gpu_ms")}},
         "plain_interp_cubic": None if t_plain is None else {
             "value": round(world * nbytes / t_plain / 1e9, 3), "unit": "GB/s", "ms_per_step": round(t_plain * 1e3, 3)},
-        "gpu_launches": launches,
+        "eb_sweep": sweep,
+        "gpu_launches": launches[0],
         "clocks": clocks,
         "cpu_baseline": cpu,
         "learned_tuner": learned,

@@ -581,17 +581,18 @@ void finish_stream(const faz_config &c, const uint8_t *payload, size_t psize, ch
     auto t0 = clk::now();
     std::vector<uint8_t> trailer;
     config_save(c, trailer);
-    // FAZ_ZSTD_THREADS (default the host's cores up to 16) cuts a large payload
-    // into independent frames compressed in parallel; 0 writes exactly the
-    // single frame of ZSTD_compress, as the reference does
-    const int nframes = zstd_frame_count(psize, zstd_threads());
-    size_t bound = zstd_frames_bound(z, psize, nframes);
+    // one level-3 frame, by zstd's worker threads (FAZ_ZSTD_THREADS, default
+    // the host's cores up to 16) or, with FAZ_ZSTD_THREADS=0, by ZSTD_compress
+    // itself as the reference calls it; FAZ_ZSTD_MULTIFRAME=1 writes
+    // independent frames instead
+    const ZstdPlan plan = zstd_plan(psize);
+    size_t bound = zstd_body_bound(z, psize, plan);
     size_t cap = 8 + bound + trailer.size() + 4;
     char *buf = (char *)std::malloc(cap);
     if (!buf) throw Fail{FAZ_ERR_ARG, "out of host memory"};
     uint64_t raw = psize;
     std::memcpy(buf, &raw, 8);
-    size_t zs = zstd_compress_frames(z, (uint8_t *)buf + 8, bound, payload, psize, nframes, parallel_frames);
+    size_t zs = zstd_compress_body(z, (uint8_t *)buf + 8, bound, payload, psize, plan, parallel_frames);
     if (z.isError(zs)) {
         std::free(buf);
         throw Fail{FAZ_ERR_ZSTD, "ZSTD_compress failed"};

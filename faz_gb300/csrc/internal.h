@@ -166,17 +166,38 @@ struct Zstd {
     unsigned (*isError)(size_t) = nullptr;
     size_t (*bound)(size_t) = nullptr;
     unsigned long long (*frameContentSize)(const void *, size_t) = nullptr;
-    // advanced API (multi-threaded compression of one frame); null if absent
     size_t (*findFrameCompressedSize)(const void *, size_t) = nullptr;
     unsigned long long (*getFrameContentSize)(const void *, size_t) = nullptr;
+    // advanced API (one frame compressed by worker threads); null if absent
+    void *(*createCCtx)() = nullptr;
+    size_t (*freeCCtx)(void *) = nullptr;
+    size_t (*setParameter)(void *, int, int) = nullptr;
+    size_t (*compress2)(void *, void *, size_t, const void *, size_t) = nullptr;
 };
-// The body of a Lossless_zstd stream as `nframes` independent level-3 frames
-// of consecutive payload slices, compressed on host threads; one frame is
-// exactly ZSTD_compress.  ZSTD_decompress decodes the concatenation.
-int zstd_frame_count(size_t n, int threads);
-size_t zstd_frames_bound(const Zstd &z, size_t n, int nframes);
-size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes,
-                            bool parallel = true);
+
+// How the body of a Lossless_zstd stream (one level-3 frame in the reference,
+// include/QoZ/lossless/Lossless_zstd.hpp:22-32) is written:
+//   Single  - ZSTD_compress on the calling thread: the reference's own call,
+//             byte for byte (FAZ_ZSTD_THREADS=0);
+//   Workers - one level-3 frame compressed by zstd's worker threads in jobs of
+//             a size fixed by the payload length, so the bytes do not depend
+//             on the worker count (the default, FAZ_ZSTD_THREADS workers);
+//   Frames  - independent level-3 frames of consecutive slices, compressed and
+//             decompressed in parallel (FAZ_ZSTD_MULTIFRAME=1): a format
+//             extension that ZSTD_decompress still reads.
+enum class ZstdMode { Single, Workers, Frames };
+struct ZstdPlan {
+    ZstdMode mode = ZstdMode::Single;
+    int threads = 0;   // workers (Workers) or host threads (Frames)
+    int nframes = 1;   // Frames only
+    int job = 0;       // Workers only: job size in bytes
+};
+ZstdPlan zstd_plan(size_t n);
+size_t zstd_body_bound(const Zstd &z, size_t n, const ZstdPlan &p);
+// `parallel` false compresses on the calling thread alone (one worker for
+// Workers, frames one after another for Frames): the same bytes.
+size_t zstd_compress_body(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, const ZstdPlan &p,
+                          bool parallel = true);
 // Decodes one or more concatenated frames (independent frames in parallel).
 size_t zstd_decompress_frames(const Zstd &z, uint8_t *dst, size_t raw, const uint8_t *src, size_t n, int threads);
 int zstd_threads();  // FAZ_ZSTD_THREADS, default the host's cores up to 16

@@ -1,4 +1,4 @@
-// lorenzo_test.cu - the Lorenzo candidate of the QoZ tuner on the GPU.
+// lorenzo_candidate.cu - the Lorenzo candidate of the QoZ tuner on the GPU.
 //
 // Reference: CompressTest with ALGO_LORENZO_REG and the RD target
 // (include/QoZ/api/impl/SZInterp.hpp:1131-1392, called from 2428-2486).  One

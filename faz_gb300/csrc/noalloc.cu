@@ -24,8 +24,17 @@
 //
 // Host code cannot use the array's name as a device address: the array's
 // address is looked up with cudaGetSymbolAddress on the first call on each
-// device, with that device current, and cached.  That first call should
-// therefore come before any stream capture.
+// device, with that device current, and cached for the life of the process.
+// The cache assumes the device's primary context lives as long as the
+// process: after cudaDeviceReset the cached address is stale, so this entry
+// point must not be used after a reset.  Every call copies the two final
+// values to the host and synchronizes `stream`, so no call may be made while
+// `stream` is being captured (such calls are refused).
+//
+// The arguments are checked as faz_compress checks them (1 <= N <= 4, no zero
+// extent, num equal to the product of the extents), and a resolved bound that
+// is not positive and finite (a constant field, NaN values) is refused as
+// faz_compress refuses it; on any failure conf is left unchanged.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -174,26 +183,64 @@ int resolve(faz_config *c, const T *d_data, cudaStream_t st, std::string &err) {
 }  // namespace
 }  // namespace faz
 
+namespace faz {
+namespace {
+
+// The shape checks of faz_compress: 1 <= N <= 4, no zero extent, num equal to
+// the product of the extents.
+bool shape_ok(const faz_config &c, std::string &err) {
+    if (c.N < 1 || c.N > 4) {
+        err = "N must be 1..4";
+        return false;
+    }
+    uint64_t num = 1;
+    for (int i = 0; i < c.N; i++) {
+        if (c.dims[i] == 0) {
+            err = "zero dimension";
+            return false;
+        }
+        num *= c.dims[i];
+    }
+    if (num != c.num) {
+        err = "num does not match dims";
+        return false;
+    }
+    return true;
+}
+
+}  // namespace
+}  // namespace faz
+
 extern "C" int faz_resolve_eb_noalloc(faz_config *conf, int dtype, const void *d_data, void *stream) {
     std::string err;
     int rc = FAZ_OK;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (!conf || !d_data) {
         err = "null argument";
         rc = FAZ_ERR_ARG;
-    } else if (conf->num == 0) {
-        err = "empty field";
+    } else if (!faz::shape_ok(*conf, err)) {
         rc = FAZ_ERR_ARG;
     } else if (conf->num > faz::kNoAllocMaxValues) {
         err = "field of " + std::to_string(conf->num) + " values exceeds the no-allocation limit of " +
               std::to_string(faz::kNoAllocMaxValues) + " values";
         rc = FAZ_ERR_ARG;
-    } else if (dtype == FAZ_FLOAT) {
-        rc = faz::resolve<float>(conf, (const float *)d_data, (cudaStream_t)stream, err);
-    } else if (dtype == FAZ_DOUBLE) {
-        rc = faz::resolve<double>(conf, (const double *)d_data, (cudaStream_t)stream, err);
-    } else {
+    } else if (dtype != FAZ_FLOAT && dtype != FAZ_DOUBLE) {
         err = "dtype must be FAZ_FLOAT or FAZ_DOUBLE";
         rc = FAZ_ERR_ARG;
+    } else if (cudaStreamIsCapturing((cudaStream_t)stream, &cap) != cudaSuccess ||
+               cap != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        err = "the stream is being captured (this call synchronizes its stream)";
+        rc = FAZ_ERR_ARG;
+    } else {
+        faz_config c = *conf;
+        rc = dtype == FAZ_FLOAT ? faz::resolve<float>(&c, (const float *)d_data, (cudaStream_t)stream, err)
+                                : faz::resolve<double>(&c, (const double *)d_data, (cudaStream_t)stream, err);
+        if (rc == FAZ_OK && (!(c.absErrorBound > 0) || !std::isfinite(c.absErrorBound))) {
+            err = "error bound must be positive and finite";
+            rc = FAZ_ERR_ARG;
+        }
+        if (rc == FAZ_OK) *conf = c;
     }
     if (rc) faz::set_error("faz_resolve_eb_noalloc: " + err);
     return rc;

@@ -389,6 +389,10 @@ const Zstd &zstd_lib(std::string &err) {
         z.version = ver();
         z.findFrameCompressedSize = (size_t(*)(const void *, size_t))dlsym(h, "ZSTD_findFrameCompressedSize");
         z.getFrameContentSize = (unsigned long long (*)(const void *, size_t))dlsym(h, "ZSTD_getFrameContentSize");
+        z.createCCtx = (void *(*)())dlsym(h, "ZSTD_createCCtx");
+        z.freeCCtx = (size_t(*)(void *))dlsym(h, "ZSTD_freeCCtx");
+        z.setParameter = (size_t(*)(void *, int, int))dlsym(h, "ZSTD_CCtx_setParameter");
+        z.compress2 = (size_t(*)(void *, void *, size_t, const void *, size_t))dlsym(h, "ZSTD_compress2");
         z.ok = true;
     });
     if (!z.ok) err = load_err;
@@ -401,6 +405,8 @@ int zstd_threads() {
     return t < 0 ? 0 : t;
 }
 
+namespace {
+
 int zstd_frame_count(size_t n, int threads) {
     if (threads <= 0) return 1;
     const size_t kMinFrame = (size_t)4 << 20;  // slices of at least 4 MiB
@@ -409,19 +415,34 @@ int zstd_frame_count(size_t n, int threads) {
     return nf < 1 ? 1 : (int)nf;
 }
 
-size_t zstd_frames_bound(const Zstd &z, size_t n, int nframes) {
-    if (nframes <= 1) return z.bound(n);
-    size_t b = 0;
-    const size_t slice = (n + nframes - 1) / nframes;
-    for (int i = 0; i < nframes; i++) {
-        const size_t lo = std::min(n, slice * i), hi = std::min(n, lo + slice);
-        b += z.bound(hi - lo);
+// Stable parameter ids of zstd's advanced API (zstd.h, ZSTD_cParameter).
+constexpr int kZstdLevel = 100, kZstdWorkers = 400, kZstdJobSize = 401, kZstdOverlapLog = 402;
+
+// Compression context of the calling thread, kept between calls (its worker
+// pool and buffers survive).
+struct CCtxHolder {
+    const Zstd *z = nullptr;
+    void *cctx = nullptr;
+    ~CCtxHolder() {
+        if (cctx && z) z->freeCCtx(cctx);
     }
-    return b;
+};
+
+size_t compress_workers(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int workers, int job) {
+    thread_local CCtxHolder h;
+    if (!h.cctx) {
+        h.z = &z;
+        h.cctx = z.createCCtx();
+        if (!h.cctx) return (size_t)-1;
+    }
+    if (z.isError(z.setParameter(h.cctx, kZstdLevel, 3)) || z.isError(z.setParameter(h.cctx, kZstdWorkers, workers)) ||
+        z.isError(z.setParameter(h.cctx, kZstdJobSize, job)) || z.isError(z.setParameter(h.cctx, kZstdOverlapLog, 0)))
+        return (size_t)-1;
+    return z.compress2(h.cctx, dst, cap, src, n);
 }
 
-size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes,
-                            bool parallel) {
+size_t compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, int nframes,
+                       bool parallel) {
     if (nframes <= 1) return z.compress(dst, cap, src, n, 3);
     const size_t slice = (n + nframes - 1) / nframes;
     struct Part {
@@ -457,6 +478,54 @@ size_t zstd_compress_frames(const Zstd &z, uint8_t *dst, size_t cap, const uint8
     if (o > cap) return (size_t)-1;
     each([&](int i) { std::memcpy(dst + parts[i].off, parts[i].buf.get(), parts[i].size); });
     return o;
+}
+
+}  // namespace
+
+ZstdPlan zstd_plan(size_t n) {
+    std::string err;
+    const Zstd &z = zstd_lib(err);
+    ZstdPlan p;
+    p.threads = zstd_threads();
+    if (p.threads <= 0) return p;  // Single
+    const char *mf = std::getenv("FAZ_ZSTD_MULTIFRAME");
+    if (mf && mf[0] == '1') {
+        p.mode = ZstdMode::Frames;
+        p.nframes = zstd_frame_count(n, p.threads);
+        if (p.nframes <= 1) p.mode = ZstdMode::Single;
+        return p;
+    }
+    const size_t kJobMin = (size_t)1 << 20, kJobMax = (size_t)8 << 20;
+    if (!z.ok || !z.createCCtx || !z.setParameter || !z.compress2 || n < 2 * kJobMin) return p;  // Single
+    // jobs of a size that depends on n alone (about 64 of them), so that the
+    // frame is the same for any worker count
+    size_t job = std::min(kJobMax, std::max(kJobMin, n / 64));
+    p.mode = ZstdMode::Workers;
+    p.job = (int)job;
+    return p;
+}
+
+size_t zstd_body_bound(const Zstd &z, size_t n, const ZstdPlan &p) {
+    if (p.mode != ZstdMode::Frames || p.nframes <= 1) return z.bound(n);
+    size_t b = 0;
+    const size_t slice = (n + p.nframes - 1) / p.nframes;
+    for (int i = 0; i < p.nframes; i++) {
+        const size_t lo = std::min(n, slice * i), hi = std::min(n, lo + slice);
+        b += z.bound(hi - lo);
+    }
+    return b;
+}
+
+size_t zstd_compress_body(const Zstd &z, uint8_t *dst, size_t cap, const uint8_t *src, size_t n, const ZstdPlan &p,
+                          bool parallel) {
+    switch (p.mode) {
+    case ZstdMode::Workers:
+        return compress_workers(z, dst, cap, src, n, parallel ? p.threads : 1, p.job);
+    case ZstdMode::Frames:
+        return compress_frames(z, dst, cap, src, n, p.nframes, parallel);
+    default:
+        return z.compress(dst, cap, src, n, 3);
+    }
 }
 
 size_t zstd_decompress_frames(const Zstd &z, uint8_t *dst, size_t raw, const uint8_t *src, size_t n, int threads) {

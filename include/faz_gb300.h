@@ -229,8 +229,14 @@ int faz_decompress_payload_device(int N, int dtype, const char *payload, size_t 
  * is a 64 KiB array inside this library that every GPU loading the library
  * keeps until exit; fields above 2^28 values are rejected with FAZ_ERR_ARG.
  * All calls share that array: calls whose device work overlaps race.  The
- * first call on each device looks the array's address up; make it before
- * any stream capture. */
+ * first call on each device looks the array's address up and caches it for
+ * the life of the process (the device's primary context must not be reset
+ * afterwards).  Every call synchronizes `stream`, so none may be made while
+ * `stream` is being captured; such a call returns FAZ_ERR_ARG.  Shapes are
+ * checked as faz_compress checks them (1 <= N <= 4, num equal to the product
+ * of dims), a resolved bound that is not positive and finite (constant field,
+ * NaN values) is refused with FAZ_ERR_ARG as faz_compress refuses it, and on
+ * any failure conf is left unchanged. */
 int faz_resolve_eb_noalloc(faz_config *conf, int dtype, const void *d_data, void *stream);
 
 /* Batched compression of n device-resident fields of uneven shapes (no

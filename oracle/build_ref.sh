@@ -2,9 +2,13 @@
 # Builds the reference FAZ command-line tool and its bundled zstd 1.4.5 from the
 # read-only reference checkout into oracle/_ref/ (git-ignored). Used only to pin
 # the oracle and to generate golden fixtures; the product never links it.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   (the reference FAZ checkout)
 set -euo pipefail
-REF=${1:-/root/reference}
+if [ $# -lt 1 ] || [ -z "$1" ]; then
+  echo "usage: $0 REFERENCE_ROOT" >&2
+  exit 2
+fi
+REF=$1
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/include/QoZ" ]; then

@@ -9,7 +9,8 @@ aborts in free() on it.)
 
 The reference tool is oracle/_ref/faz, built from the reference sources by
 oracle/build_ref.sh (with its bundled zstd 1.4.5).  Run from the repository
-root:  python tests/golden/make_golden.py
+root, with FAZ_REFERENCE_ROOT naming the reference checkout when the tool is
+not built yet:  python tests/golden/make_golden.py
 """
 import hashlib
 import json
@@ -267,7 +268,7 @@ def main(only=None):
     """Generate every case, or (names given on the command line) only those,
     replacing their manifest entries."""
     if not os.path.exists(FAZ):
-        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
+        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), os.environ["FAZ_REFERENCE_ROOT"]])
     manifest = []
     old = {}
     mpath = os.path.join(HERE, "manifest.json")
