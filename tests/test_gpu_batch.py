@@ -101,10 +101,14 @@ def test_gpu_batch_rejects_mismatched_input():
         F.compress_batch([_conf((11,))], [x])
 
 
-def test_gpu_batch_writes_the_same_zstd_frames(monkeypatch):
-    """With several zstd frames per stream the batch writes the frames a
-    single-field call writes."""
+@pytest.mark.parametrize("multiframe", [False, True])
+def test_gpu_batch_writes_the_same_zstd_frames(monkeypatch, multiframe):
+    """With zstd's worker threads (one frame per stream; the batch's host
+    threads compress with one worker each) and with independent frames, the
+    batch writes the bytes a single-field call writes."""
     monkeypatch.setenv("FAZ_ZSTD_THREADS", "8")
+    if multiframe:
+        monkeypatch.setenv("FAZ_ZSTD_MULTIFRAME", "1")
     big = spectral_field((128, 256, 256), slope=-3.0, noise=0.01, seed=5, device="cuda")
     small = spectral_field((40, 50, 60), slope=-3.0, seed=6, device="cuda")
     confs = [_conf((128, 256, 256), rel=1e-4), _conf((40, 50, 60))]

@@ -261,10 +261,13 @@ def _zstd_frames(stream):
     return n
 
 
-def test_gpu_parallel_zstd_frames_hold_the_same_payload(monkeypatch):
-    """FAZ_ZSTD_THREADS > 0 writes a large payload as independent zstd frames
-    compressed in parallel: the same payload, decodable by plain
-    ZSTD_decompress (the oracle) and by the library's parallel frame decoder."""
+def test_gpu_zstd_bodies_hold_the_same_payload(monkeypatch):
+    """The three ways of writing the zstd body hold the same payload:
+    FAZ_ZSTD_THREADS=0 is ZSTD_compress itself (one frame, the oracle's bytes);
+    FAZ_ZSTD_THREADS > 0 is one level-3 frame written by zstd's worker
+    threads, the same bytes for any worker count; FAZ_ZSTD_MULTIFRAME=1 writes
+    independent frames in parallel.  Plain ZSTD_decompress (the oracle) and
+    the library's decoder read all of them."""
     import torch
     dims = (128, 256, 256)
     t = F.fields.spectral_field(dims, slope=-3.0, noise=0.01, seed=5, device="cuda")
@@ -272,16 +275,27 @@ def test_gpu_parallel_zstd_frames_hold_the_same_payload(monkeypatch):
     monkeypatch.setenv("FAZ_ZSTD_THREADS", "0")
     s0 = F.SZ_compress(conf, t)
     assert _zstd_frames(s0) == 1
+    ref, ref_payload = O.compress(conf, t.cpu().numpy())
+    assert mask_first_size(s0) == mask_first_size(ref)
     monkeypatch.setenv("FAZ_ZSTD_THREADS", "8")
     s8 = F.SZ_compress(conf, t)
-    assert _zstd_frames(s8) > 1
-    assert payload_of(s0) == payload_of(s8)   # the oracle decodes both bodies
-    ref, _ = O.decompress(s0)
-    for threads in ("8", "0"):  # parallel frames, then one call over all of them
-        monkeypatch.setenv("FAZ_ZSTD_THREADS", threads)
-        out = torch.empty(dims, dtype=torch.float32, device="cuda")
-        F.decompress_device(s8, out)
-        assert np.array_equal(out.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+    monkeypatch.setenv("FAZ_ZSTD_THREADS", "3")
+    s3 = F.SZ_compress(conf, t)
+    assert s8 == s3
+    assert _zstd_frames(s8) == 1
+    monkeypatch.setenv("FAZ_ZSTD_MULTIFRAME", "1")
+    smf = F.SZ_compress(conf, t)
+    monkeypatch.delenv("FAZ_ZSTD_MULTIFRAME")
+    assert _zstd_frames(smf) > 1
+    for s in (s8, smf):
+        assert payload_of(s) == ref_payload  # the oracle decodes every body
+    ref_dec, _ = O.decompress(s0)
+    for s in (s8, smf):
+        for threads in ("8", "0"):
+            monkeypatch.setenv("FAZ_ZSTD_THREADS", threads)
+            out = torch.empty(dims, dtype=torch.float32, device="cuda")
+            F.decompress_device(s, out)
+            assert np.array_equal(out.cpu().numpy().view(np.uint32), ref_dec.view(np.uint32))
 
 
 def test_gpu_c1_full_size_matches_oracle():
