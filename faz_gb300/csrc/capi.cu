@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -450,20 +451,39 @@ void interp_payload_tail(const faz_config &c, const std::vector<uint8_t> &il, co
     tm.payload_bytes = psize;
 }
 
+// The device part of an interpolation compression up to the quantisation
+// codes (stream order) and the unpredictable values at their code positions;
+// interp_finish adds the Huffman stage and the payload.
 template <typename T>
-void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&payload, size_t &psize,
-                      faz_timings &tm, Counter &launches, Sink *sink = nullptr) {
-    auto th0 = clk::now();
+struct InterpCodes {
+    faz_config c;  // error bound resolved
+    double eb = 0;
+    int radius = 0;
+    std::vector<uint8_t> il, dl;
+    uint64_t n = 0;
+    bool have_levels = false;
+    DevMem m;
+    T *scratch = nullptr;
+    uint16_t *codes = nullptr;
+    unsigned long long *vcount = nullptr;
+    Events ev_pred, ev_fin;
+    explicit InterpCodes(cudaStream_t st) : m(st) {}
+};
+
+// First point / anchor grid and every level (SZInterpolationCompressor.hpp:
+// 324-461); resolves the error bound of c.
+template <typename T>
+void interp_levels(InterpCodes<T> &r, faz_config &c, const T *dX, cudaStream_t st, Counter &launches) {
     resolve_eb<T>(c, dX, st, launches);
     const double eb = c.absErrorBound;
     if (!(eb > 0) || !std::isfinite(eb)) throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
     const int radius = c.quantbinCnt / 2;
-    std::vector<uint8_t> il(c.interpAlgo_list, c.interpAlgo_list + c.interp_list_len);
-    std::vector<uint8_t> dl(c.interpDirection_list, c.interpDirection_list + c.interp_list_len);
+    r.il.assign(c.interpAlgo_list, c.interpAlgo_list + c.interp_list_len);
+    r.dl.assign(c.interpDirection_list, c.interpDirection_list + c.interp_list_len);
     Plan p = make_plan<T>(c.N, c.dims, c.maxStep, c.interpBlockSize, c.fixBlockSize, c.interpAlgo, c.interpDirection,
-                          il, dl, eb, c.alpha, c.beta, radius, c.trimToZero, smem_limit());
+                          r.il, r.dl, eb, c.alpha, c.beta, radius, c.trimToZero, smem_limit());
     const uint64_t n = p.num;
-    DevMem m(st);
+    DevMem &m = r.m;
     T *W = m.alloc<T>(n);
     T *scratch = m.alloc<T>(n);
     uint16_t *codes = m.alloc<uint16_t>(n);
@@ -483,8 +503,7 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
         vcount = m.alloc<unsigned long long>(1);
         CK(cudaMemsetAsync(vcount, 0, 8, st));
     }
-    Events ev_pred, ev_fin, ev_huff;
-    CK(cudaEventRecord(ev_pred.a, st));
+    CK(cudaEventRecord(r.ev_pred.a, st));
     for (size_t li = 0; li < p.lv.size(); li++) {
         const LevelPlan &L = p.lv[li];
         LevelArgs a = L.args;
@@ -492,18 +511,42 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
         a.ncodes = n;
         a.err = nullptr;
         a.verify = vcount;
-        if (li + 1 == p.lv.size()) CK(cudaEventRecord(ev_fin.a, st));
-        launches(launch_level<T>(a, L.nblocks, false, dX, W, codes, scratch, nullptr, 0, nullptr, st));
+        if (li + 1 == p.lv.size()) CK(cudaEventRecord(r.ev_fin.a, st));
+        int nl = 0;
+        CK(launch_level<T>(a, L.nblocks, false, dX, W, codes, scratch, nullptr, 0, nullptr, st, &nl));
+        launches.n += nl;
     }
-    CK(cudaEventRecord(ev_fin.b, st));
-    CK(cudaEventRecord(ev_pred.b, st));
+    CK(cudaEventRecord(r.ev_fin.b, st));
+    CK(cudaEventRecord(r.ev_pred.b, st));
+    r.c = c;
+    r.eb = eb;
+    r.radius = radius;
+    r.n = n;
+    r.scratch = scratch;
+    r.codes = codes;
+    r.vcount = vcount;
+    r.have_levels = !p.lv.empty();
+}
+
+// The Huffman stage and payload of interp_levels' codes.
+template <typename T>
+void interp_finish(InterpCodes<T> &r, cudaStream_t st, uint8_t *&payload, size_t &psize, faz_timings &tm,
+                   Counter &launches, Sink *sink) {
+    Events ev_huff;
     CK(cudaEventRecord(ev_huff.a, st));
-    interp_payload_tail<T>(c, il, dl, eb, radius, n, codes, scratch, vcount, m, st, launches, tm, sink, payload, psize,
-                           ev_huff.b);
-    tm.predict_ms = ev_pred.ms();
-    tm.finest_level_ms = p.lv.empty() ? 0.0 : ev_fin.ms();
+    interp_payload_tail<T>(r.c, r.il, r.dl, r.eb, r.radius, r.n, r.codes, r.scratch, r.vcount, r.m, st, launches, tm,
+                           sink, payload, psize, ev_huff.b);
+    tm.predict_ms = r.ev_pred.ms();
+    tm.finest_level_ms = r.have_levels ? r.ev_fin.ms() : 0.0;
     tm.huffman_ms = ev_huff.ms();
-    (void)th0;
+}
+
+template <typename T>
+void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&payload, size_t &psize,
+                      faz_timings &tm, Counter &launches, Sink *sink = nullptr) {
+    InterpCodes<T> r(st);
+    interp_levels<T>(r, c, dX, st, launches);
+    interp_finish<T>(r, st, payload, psize, tm, launches, sink);
 }
 
 // SZ_compress_dispatcher (include/QoZ/api/impl/SZDispatcher.hpp:12-36): error
@@ -525,22 +568,41 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
         auto tt = clk::now();
         faz_timings tt_tm;
         std::memset(&tt_tm, 0, sizeof(tt_tm));
-        // the interpolation compression of the tuner's likely choice runs
-        // while the trials' zstd sizes are computed; it is kept when the
-        // final choice is the same
+        // While the trials' zstd sizes are computed, the interpolation
+        // compression that the pre-zstd sizes point to runs; it is kept when
+        // the final choice is the same.  When the best two candidates are too
+        // close for the pre-zstd sizes to tell, the codes of both are computed
+        // and the Huffman stage of the winner follows the decision.
         bool have = false;
         faz_config guess;
         std::memset(&guess, 0, sizeof(guess));
-        auto speculate = [&](const faz_config &g) {
-            guess = g;
-            compress_payload<T>(guess, dX, st, payload, psize, tm, launches, sink);
-            have = true;
+        std::unique_ptr<InterpCodes<T>> both[2];
+        faz_config both_conf[2];
+        auto speculate = [&](const faz_config &g, const faz_config *alt) {
+            if (!alt) {
+                guess = g;
+                compress_payload<T>(guess, dX, st, payload, psize, tm, launches, sink);
+                have = true;
+                return;
+            }
+            for (int k = 0; k < 2; k++) {
+                both_conf[k] = k ? *alt : g;
+                both[k].reset(new InterpCodes<T>(st));
+                interp_levels<T>(*both[k], both_conf[k], dX, st, launches);
+            }
         };
         sz3_tune_device<T>(c, dX, st, launches, tt_tm, speculate);
         tm.tune_ms = ms_since(tt);
-        if (have && c.cmprAlgo == FAZ_ALGO_INTERP && c.interpAlgo == guess.interpAlgo &&
-            c.interpDirection == guess.interpDirection)
-            return;
+        if (c.cmprAlgo == FAZ_ALGO_INTERP) {
+            if (have && c.interpAlgo == guess.interpAlgo && c.interpDirection == guess.interpDirection) return;
+            for (int k = 0; k < 2; k++) {
+                if (both[k] && c.interpAlgo == both_conf[k].interpAlgo &&
+                    c.interpDirection == both_conf[k].interpDirection) {
+                    interp_finish<T>(*both[k], st, payload, psize, tm, launches, sink);
+                    return;
+                }
+            }
+        }
     }
     if (c.cmprAlgo == FAZ_ALGO_INTERP) {
         compress_payload<T>(c, dX, st, payload, psize, tm, launches, sink);
@@ -1304,7 +1366,9 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
         a.err = kerr;
         a.verify = vcount;
         if (li + 1 == pl_.lv.size()) CK(cudaEventRecord(ev_fin.a, st));
-        launches(launch_level<T>(a, L.nblocks, true, nullptr, dOut, codes, nullptr, zpos, nz, dunpred, st));
+        int nl = 0;
+        CK(launch_level<T>(a, L.nblocks, true, nullptr, dOut, codes, nullptr, zpos, nz, dunpred, st, &nl));
+        launches.n += nl;
     }
     CK(cudaEventRecord(ev_fin.b, st));
     CK(cudaEventRecord(ev_pred.b, st));
@@ -1607,7 +1671,7 @@ int tune_impl(faz_config *conf, const void *d_data, void *user_stream, faz_timin
         } else if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) {
             faz_timings t2;
             std::memset(&t2, 0, sizeof(t2));
-            sz3_tune_device<T>(c, dX, sg.st, launches, t2, [](const faz_config &) {});
+            sz3_tune_device<T>(c, dX, sg.st, launches, t2, {});
         }
         CK(cudaStreamSynchronize(sg.st));
         tm.tune_ms = ms_since(tt);

@@ -335,9 +335,13 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
 template <typename T>
 void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, T *dOut, cudaStream_t st,
                          Counter &launches, faz_timings &tm);
+// The SZ3 tuner of the default configuration.  `speculate` (optional) is
+// called once the pre-zstd sizes of the interpolation trials are known, with
+// the candidate they point to and - when the best two are too close for those
+// sizes to tell - the runner-up (else null).
 template <typename T>
 void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
-                     const std::function<void(const faz_config &)> &speculate);
+                     const std::function<void(const faz_config &, const faz_config *)> &speculate);
 
 template <typename T>
 void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm);

@@ -42,9 +42,11 @@ template <typename T>
 cudaError_t launch_minmax(const T *X, uint64_t n, T *pmin, T *pmax, int nblocks, cudaStream_t st);
 template <typename T>
 size_t level_smem_bytes(const LevelArgs &a);
+// One interpolation level; *nlaunch grows by the kernel launches it made.
 template <typename T>
 cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const T *X, T *W, uint16_t *codes,
-                         T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st);
+                         T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st,
+                         int *nlaunch);
 template <typename T>
 cudaError_t launch_first_point(bool decomp, const T *X, T *W, uint16_t *codes, T *scratch, double eb, int radius,
                                int trim, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st);

@@ -412,6 +412,84 @@ __global__ void __launch_bounds__(512, 2) k_interp_level(LevelArgs a, const T *_
     level_block<T, DECOMP, WIDE, QM, false, CUB>(a, blockIdx.x, X, W, codes, scratch, zpos, nz, unpred, smem_raw);
 }
 
+// ------------------------------------------------------ coarse levels
+// Levels with lattice stride s >= 2 hold 1/8 of the field or less, in few
+// blocks (64 at the third level of a 512^3 field, one at the last): one CTA
+// per block leaves most SMs idle while each block's sweeps run one after
+// another.  Instead, each sweep of the level is one launch over every block,
+// one thread per emitted target in stream order (so code stores are
+// contiguous), neighbours read from the reconstruction W (coarse points and
+// the earlier sweeps' targets, written before this launch began), targets
+// written back to W.  Every line is computed once, by the block that emits it.
+// CTA c takes chunk c % chunks of block c / chunks.
+template <typename T, bool DECOMP, int QM, int CUB>
+__global__ void __launch_bounds__(256) k_level_sweep(LevelArgs a, int sw, int64_t chunks, const T *__restrict__ X,
+                                                    T *__restrict__ W, uint16_t *__restrict__ codes,
+                                                    T *__restrict__ scratch, const uint64_t *__restrict__ zpos,
+                                                    uint64_t nz, const T *__restrict__ unpred) {
+    __shared__ BlockGeom sgeo;
+    __shared__ int64_t sbc[3];
+    const int64_t bid = (int64_t)blockIdx.x / chunks;
+    const int64_t x = ((int64_t)blockIdx.x - bid * chunks) * blockDim.x + threadIdx.x;
+    if (threadIdx.x == 0) {
+        block_coords(a, bid, sbc);
+        block_geom(a, sbc, sgeo);
+    }
+    __syncthreads();
+    const BlockGeom &g = sgeo;
+    const int64_t cnt = sw == 1 ? g.c1 : (sw == 2 ? g.c2 : g.c3);
+    if (x >= cnt) return;
+    const int tl = sw == 1 ? g.t0 : (sw == 2 ? g.t1 : g.t2);  // targets per line
+    const int n = sw == 1 ? g.n0 : (sw == 2 ? g.n1 : g.n2);   // lattice points per line
+    const int64_t L = x / tl;
+    const int r = (int)(x - L * tl);
+    // target of stream rank r in its line (inverse of line_rank)
+    int m;
+    if (!a.cubic || n < 5) {
+        m = 2 * r + 1;
+    } else {
+        const int ia = (n & 1) ? n - 2 : n - 3;
+        const int cint = (ia - 3) >> 1;
+        m = r < cint ? 2 * r + 3 : (r == cint ? 1 : (r == cint + 1 ? ia : n - 1));
+    }
+    // lattice coordinates along P0, P1, P2 of the line's origin
+    int64_t c0, c1, c2;
+    if (sw == 1) {
+        c0 = 0;
+        c1 = 2 * (L / g.ne2 + g.k1);
+        c2 = 2 * (L % g.ne2 + g.k2);
+    } else if (sw == 2) {
+        c0 = g.k0 + L / g.ne2;
+        c1 = 0;
+        c2 = 2 * (L % g.ne2 + g.k2);
+    } else {
+        const int64_t w1 = g.n1 - g.k1;
+        c0 = g.k0 + L / w1;
+        c1 = g.k1 + L % w1;
+        c2 = 0;
+    }
+    const int P0 = a.perm[0], P1 = a.perm[1], P2 = a.perm[2];
+    const int64_t o0 = pick3(P0, a.offs[0], a.offs[1], a.offs[2]), o1 = pick3(P1, a.offs[0], a.offs[1], a.offs[2]),
+                  o2 = pick3(P2, a.offs[0], a.offs[1], a.offs[2]);
+    const int64_t b0 = pick3(P0, g.beg[0], g.beg[1], g.beg[2]), b1 = pick3(P1, g.beg[0], g.beg[1], g.beg[2]),
+                  b2 = pick3(P2, g.beg[0], g.beg[1], g.beg[2]);
+    const int64_t origin = (b0 + c0 * a.s) * o0 + (b1 + c1 * a.s) * o1 + (b2 + c2 * a.s) * o2;
+    const int64_t st = a.s * (sw == 1 ? o0 : (sw == 2 ? o1 : o2));
+    const Stencil<T> S = make_stencil<T>(m, n, a.cubic, (int)st, 0);
+    const T pred = eval_stencil<CUB>(S, W + origin);
+    const int64_t gi = origin + (int64_t)m * st;
+    const uint64_t pos = a.block_off[bid] + (uint64_t)(sw == 1 ? 0 : (sw == 2 ? g.c1 : g.c1 + g.c2)) + (uint64_t)x;
+    if (!DECOMP) {
+        T v = X[gi], uv;
+        const int code = quant_point<T, QM>(v, pred, a, uv);
+        codes[pos] = (uint16_t)code;
+        if (code == 0) scratch[pos] = uv;
+        W[gi] = v;
+    } else {
+        W[gi] = recover_point<T, QM>(pred, (int)codes[pos], pos, a, zpos, nz, unpred);
+    }
+}
+
 // ------------------------------------------------------ batched launch
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     unsigned v;
@@ -672,15 +750,52 @@ size_t level_smem_bytes(const LevelArgs &a) {
     return vb + (size_t)a.stage_cap * sizeof(uint16_t);
 }
 
+// Coarse levels (stride >= 2) of fields below 2^31 values: the three sweep
+// launches of k_level_sweep instead of one CTA per block.
+template <typename T>
+cudaError_t launch_level_sweeps(const LevelArgs &a, int64_t nblocks, bool decomp, const T *X, T *W, uint16_t *codes,
+                                T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st,
+                                int *nlaunch) {
+    const bool straight = sizeof(T) == 4 && a.fast && a.trim == 0;
+    void (*k)(LevelArgs, int, int64_t, const T *, T *, uint16_t *, T *, const uint64_t *, uint64_t, const T *);
+    if (a.cubic) {
+        if (straight) k = decomp ? k_level_sweep<T, true, 1, 1> : k_level_sweep<T, false, 1, 1>;
+        else k = decomp ? k_level_sweep<T, true, 0, 1> : k_level_sweep<T, false, 0, 1>;
+    } else {
+        if (straight) k = decomp ? k_level_sweep<T, true, 1, 0> : k_level_sweep<T, false, 1, 0>;
+        else k = decomp ? k_level_sweep<T, true, 0, 0> : k_level_sweep<T, false, 0, 0>;
+    }
+    // the first block has the most targets in every sweep (no first planes
+    // skipped, full extent)
+    int64_t bc0[3] = {0, 0, 0};
+    BlockGeom g0;
+    block_geom(a, bc0, g0);
+    const int64_t cmax[3] = {g0.c1, g0.c2, g0.c3};
+    for (int sw = 1; sw <= 3; sw++) {
+        if (cmax[sw - 1] <= 0) continue;
+        const int64_t chunks = (cmax[sw - 1] + 255) / 256;
+        k<<<(unsigned)(nblocks * chunks), 256, 0, st>>>(a, sw, chunks, X, W, codes, scratch, zpos, nz, unpred);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        ++*nlaunch;
+    }
+    return cudaSuccess;
+}
+
 template <typename T>
 cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const T *X, T *W, uint16_t *codes,
-                         T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st) {
+                         T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st,
+                         int *nlaunch) {
     size_t sm = level_smem_bytes<T>(a);
     // half-warps take lines: enough threads for the lines of a block
     int64_t vol = (int64_t)a.vwords * 2;
     int threads = vol >= 8192 ? 512 : (vol >= 1024 ? 256 : (vol >= 256 ? 128 : 64));
     const bool wide = a.dims[0] * a.dims[1] * a.dims[2] >= ((int64_t)1 << 31);
     const bool straight = sizeof(T) == 4 && a.fast && a.trim == 0;
+    const int64_t per_block = (a.bs / a.s + 1) * (a.bs / a.s + 1) * (a.bs / a.s + 1) / 256 + 1;
+    if (a.s >= 2 && !wide && nblocks * per_block < (1ll << 31))
+        return launch_level_sweeps<T>(a, nblocks, decomp, X, W, codes, scratch, zpos, nz, unpred, st, nlaunch);
+    ++*nlaunch;
     void (*k)(LevelArgs, const T *, T *, uint16_t *, T *, const uint64_t *, uint64_t, const T *);
 #define FAZ_PICK(CUB)                                                                                            \
     if (straight) {                                                                                              \
@@ -730,7 +845,7 @@ cudaError_t launch_anchors(bool decomp, const T *X, T *W, uint16_t *codes, T *sc
     template cudaError_t launch_minmax<T>(const T *, uint64_t, T *, T *, int, cudaStream_t);                     \
     template size_t level_smem_bytes<T>(const LevelArgs &);                                                      \
     template cudaError_t launch_level<T>(const LevelArgs &, int64_t, bool, const T *, T *, uint16_t *, T *,      \
-                                         const uint64_t *, uint64_t, const T *, cudaStream_t);                   \
+                                         const uint64_t *, uint64_t, const T *, cudaStream_t, int *);            \
     template cudaError_t launch_first_point<T>(bool, const T *, T *, uint16_t *, T *, double, int, int,          \
                                                const uint64_t *, uint64_t, const T *, cudaStream_t);             \
     template cudaError_t launch_anchors<T>(bool, const T *, T *, uint16_t *, T *, const T *, const int64_t *,   \

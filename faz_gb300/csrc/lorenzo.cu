@@ -14,6 +14,7 @@
 // that holds the block and its two-deep halo.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -189,19 +190,32 @@ __global__ void k_lor_select(LorArgs a, const T *__restrict__ X, uint16_t *__res
     }
 }
 
-// One block diagonal bi + bj + bk = d; one warp per block.
+// Loads with the L2 as the point of coherence: the wavefront reads blocks
+// that other SMs wrote during the same launch, and L1 is not coherent.
+template <typename T>
+__device__ __forceinline__ T ld_coherent(const T *p) {
+    return __ldcg(p);
+}
+
+__device__ __forceinline__ unsigned lor_ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void lor_st_release(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// One block (bi, bj, bk), one warp: the (bs + 2)^3 tile with its two-deep
+// halo of reconstructed values, then the point diagonals i + j + k = s in
+// order, each point predicted from its reconstructed neighbours.
 template <typename T, bool DECOMP, int QM>
-__global__ void __launch_bounds__(kLorWarps * 32)
-    k_lor_diag(LorArgs a, int64_t d, int64_t bi_lo, const T *__restrict__ X, T *__restrict__ R,
-               uint16_t *__restrict__ codes, T *__restrict__ scratch, const uint16_t *__restrict__ ind,
-               const uint64_t *__restrict__ zpos, uint64_t nzp, const T *__restrict__ unpred) {
-    extern __shared__ __align__(16) unsigned char lor_smem[];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t bi = bi_lo + blockIdx.y;
-    const int64_t bj_lo = d - bi - (a.nz - 1) > 0 ? d - bi - (a.nz - 1) : 0;
-    const int64_t bj = bj_lo + (int64_t)blockIdx.x * kLorWarps + w;
-    const int64_t bk = d - bi - bj;
-    if (bi >= a.nx || bj >= a.ny || bk < 0 || bk >= a.nz) return;
+__device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t bj, int64_t bk, T *t,
+                                          const T *__restrict__ X, T *__restrict__ R, uint16_t *__restrict__ codes,
+                                          T *__restrict__ scratch, const uint16_t *__restrict__ ind,
+                                          const uint64_t *__restrict__ zpos, uint64_t nzp, const T *__restrict__ unpred) {
+    const int lane = threadIdx.x & 31;
     const int bs = a.bs;
     const int sx = (bi + 1) * bs < a.d1 ? bs : (int)(a.d1 - bi * bs);
     const int sy = (bj + 1) * bs < a.d2 ? bs : (int)(a.d2 - bj * bs);
@@ -210,9 +224,6 @@ __global__ void __launch_bounds__(kLorWarps * 32)
     const int64_t d0 = a.d2 * a.d3, dd1 = a.d3;
     // tile strides: (tx, ty, 1) over (sx + 2) x (sy + 2) x (sz + 2)
     const int tz = sz + 2, ty = tz, tx = (sy + 2) * tz;
-    // per warp: the (bs + 2)^3 tile, then (compression) the block's bs^3 original values
-    const int tstride = (bs + 2) * (bs + 2) * (bs + 2) + (DECOMP ? 0 : bs * bs * bs);
-    T *t = reinterpret_cast<T *>(lor_smem) + (size_t)w * (size_t)tstride;
     T *xs = t + (bs + 2) * (bs + 2) * (bs + 2);
     const int tn = (sx + 2) * (sy + 2) * tz;
     // loads in batches of kLorBatch per lane, all issued before any is used
@@ -224,7 +235,8 @@ __global__ void __launch_bounds__(kLorWarps * 32)
             const int i = e / tx, r = e - i * tx, j = r / tz, k = r - j * tz;
             const int64_t gx = x0 + i - 2, gy = y0 + j - 2, gz = z0 + k - 2;
             const bool inside = i >= 2 && j >= 2 && k >= 2;
-            v[u] = (e < tn && !inside && gx >= 0 && gy >= 0 && gz >= 0) ? R[gx * d0 + gy * dd1 + gz] : (T)0;
+            v[u] = (e < tn && !inside && gx >= 0 && gy >= 0 && gz >= 0) ? ld_coherent(R + (gx * d0 + gy * dd1 + gz))
+                                                                       : (T)0;
         }
 #pragma unroll
         for (int u = 0; u < kLorBatch; u++)
@@ -288,6 +300,61 @@ __global__ void __launch_bounds__(kLorWarps * 32)
     }
 }
 
+constexpr unsigned kLorWaitLimit = 1u << 22;  // polls (with back-off) of a neighbour before giving up
+
+// The whole wavefront in one launch of persistent CTAs.  A warp takes a
+// ticket, and with it the block order[ticket]: blocks come diagonal by
+// diagonal (bi + bj + bk ascending), so the blocks a block reads - its face
+// neighbours (bi-1, bj, bk), (bi, bj-1, bk), (bi, bj, bk-1), which in turn
+// waited for theirs - hold smaller tickets, taken by warps already running,
+// and every wait ends.  Each wait is bounded all the same (error flag, then
+// the block runs).  A finished block publishes done[b] = 1 with release
+// semantics after its reconstruction is written.
+template <typename T, bool DECOMP, int QM>
+__global__ void __launch_bounds__(kLorWarps * 32)
+    k_lor_persist(LorArgs a, const uint32_t *__restrict__ order, uint32_t nblocks, unsigned *counter,
+                  unsigned *done, int *err, const T *__restrict__ X, T *__restrict__ R,
+                  uint16_t *__restrict__ codes, T *__restrict__ scratch, const uint16_t *__restrict__ ind,
+                  const uint64_t *__restrict__ zpos, uint64_t nzp, const T *__restrict__ unpred) {
+    extern __shared__ __align__(16) unsigned char lor_smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bs = a.bs;
+    const int tstride = (bs + 2) * (bs + 2) * (bs + 2) + (DECOMP ? 0 : bs * bs * bs);
+    T *t = reinterpret_cast<T *>(lor_smem) + (size_t)w * (size_t)tstride;
+    const int64_t plane = a.ny * a.nz;
+    for (;;) {
+        unsigned tk = 0;
+        if (lane == 0) tk = atomicAdd(counter, 1u);
+        tk = __shfl_sync(0xffffffffu, tk, 0);
+        if (tk >= nblocks) break;
+        const int64_t b = order[tk];
+        const int64_t bk = b % a.nz, bj = (b / a.nz) % a.ny, bi = b / plane;
+        const unsigned *deps[3] = {bi > 0 ? done + (b - plane) : nullptr, bj > 0 ? done + (b - a.nz) : nullptr,
+                                   bk > 0 ? done + (b - 1) : nullptr};
+        if (lane == 0) {
+            for (int d = 0; d < 3; d++) {
+                if (!deps[d]) continue;
+                unsigned it = 0;
+                while (lor_ld_acquire(deps[d]) == 0u) {
+                    if (++it > kLorWaitLimit) {
+                        atomicExch(err, 1);
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+        }
+        __syncwarp();
+        // every lane acquires the neighbours' completion itself
+        for (int d = 0; d < 3; d++)
+            if (deps[d]) (void)lor_ld_acquire(deps[d]);
+        lor_block<T, DECOMP, QM>(a, bi, bj, bk, t, X, R, codes, scratch, ind, zpos, nzp, unpred);
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) lor_st_release(done + b, 1u);
+    }
+}
+
 template <typename T>
 LorArgs make_args(const uint64_t *dims, int bs, int pd, int lo, int lo2, double eb, int radius, int reg = 0) {
     LorArgs a;
@@ -316,24 +383,58 @@ template <typename T>
 void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, uint16_t *codes, T *scratch, const uint16_t *ind,
                    const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st, Counter &launches) {
     const bool straight = sizeof(T) == 4 && a.q.fast;
-    const int64_t last = (a.nx - 1) + (a.ny - 1) + (a.nz - 1);
     const size_t smem = (size_t)kLorWarps *
                         (size_t)((a.bs + 2) * (a.bs + 2) * (a.bs + 2) + (decomp ? 0 : a.bs * a.bs * a.bs)) * sizeof(T);
-    void (*k)(LorArgs, int64_t, int64_t, const T *, T *, uint16_t *, T *, const uint16_t *, const uint64_t *, uint64_t,
-              const T *);
-    if (!decomp) k = straight ? k_lor_diag<T, false, 1> : k_lor_diag<T, false, 0>;
-    else k = straight ? k_lor_diag<T, true, 1> : k_lor_diag<T, true, 0>;
+    void (*k)(LorArgs, const uint32_t *, uint32_t, unsigned *, unsigned *, int *, const T *, T *, uint16_t *, T *,
+              const uint16_t *, const uint64_t *, uint64_t, const T *);
+    if (!decomp) k = straight ? k_lor_persist<T, false, 1> : k_lor_persist<T, false, 0>;
+    else k = straight ? k_lor_persist<T, true, 1> : k_lor_persist<T, true, 0>;
     CK(allow_dynamic_smem((const void *)k));
-    if (a.nx > 65535) throw Fail{FAZ_ERR_UNSUPPORTED, "too many Lorenzo blocks along the slowest axis"};
+    const uint64_t nb64 = (uint64_t)(a.nx * a.ny * a.nz);
+    if (nb64 >= (1ull << 32)) throw Fail{FAZ_ERR_UNSUPPORTED, "too many Lorenzo blocks"};
+    const uint32_t nb = (uint32_t)nb64;
+    // blocks in diagonal order (bi + bj + bk ascending, then bi, then bj)
+    std::vector<uint32_t> order;
+    order.reserve(nb);
+    const int64_t last = (a.nx - 1) + (a.ny - 1) + (a.nz - 1);
+    size_t widest = 0;  // blocks on the longest diagonal: the most that are ever ready at once
     for (int64_t d = 0; d <= last; d++) {
+        const size_t before = order.size();
         const int64_t bi_lo = std::max<int64_t>(0, d - (a.ny - 1) - (a.nz - 1));
         const int64_t bi_hi = std::min<int64_t>(a.nx - 1, d);
-        // bj spans at most min(ny, d + 1) values for any bi
-        const int64_t nbj = std::min<int64_t>(a.ny, d + 1);
-        dim3 grid((unsigned)((nbj + kLorWarps - 1) / kLorWarps), (unsigned)(bi_hi - bi_lo + 1));
-        k<<<grid, kLorWarps * 32, smem, st>>>(a, d, bi_lo, X, R, codes, scratch, ind, zpos, nz, unpred);
-        launches(cudaGetLastError());
+        for (int64_t bi = bi_lo; bi <= bi_hi; bi++) {
+            const int64_t r = d - bi;
+            const int64_t bj_lo = std::max<int64_t>(0, r - (a.nz - 1)), bj_hi = std::min<int64_t>(a.ny - 1, r);
+            for (int64_t bj = bj_lo; bj <= bj_hi; bj++)
+                order.push_back((uint32_t)((bi * a.ny + bj) * a.nz + (r - bj)));
+        }
+        widest = std::max(widest, order.size() - before);
     }
+    if (order.size() != nb) throw Fail{FAZ_ERR_DEVICE, "Lorenzo block order does not cover the blocks"};
+    DevMem m(st);
+    uint32_t *dorder = m.alloc<uint32_t>(nb);
+    unsigned *sync = m.alloc<unsigned>((size_t)nb + 2);  // counter, done[nb]
+    int *derr = m.alloc<int>(1);
+    CK(cudaMemcpyAsync(dorder, order.data(), (size_t)nb * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(sync, 0, ((size_t)nb + 2) * 4, st));
+    CK(cudaMemsetAsync(derr, 0, 4, st));
+    int dev = 0, sms = 0, per_sm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kLorWarps * 32, smem));
+    if (per_sm < 1) throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo block does not fit on an SM"};
+    // never more CTAs than stay resident (waits rely on it), nor more warps than
+    // blocks on the widest diagonal: more would only wait, and hold SMs that
+    // concurrent work (the tuner's other trials) needs
+    const uint64_t want = (widest + kLorWarps - 1) / kLorWarps;
+    const int grid = (int)std::min<uint64_t>((uint64_t)sms * (uint64_t)per_sm, want);
+    k<<<grid, kLorWarps * 32, smem, st>>>(a, dorder, nb, sync, sync + 1, derr, X, R, codes, scratch, ind, zpos, nz,
+                                          unpred);
+    launches(cudaGetLastError());
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (herr) throw Fail{FAZ_ERR_DEVICE, "Lorenzo wavefront: a block waited too long for its neighbours"};
 }
 
 // meta_params as written by write(params, c) (include/QoZ/utils/MetaDef.hpp:33-60):

@@ -13,6 +13,8 @@
 // the real compressors and hand their payloads to the host zstd.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -611,7 +613,7 @@ void lorenzo_followup(faz_config &c, const T *dX, const Sample<T> &smp, double b
 
 template <typename T>
 void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm,
-                     const std::function<void(const faz_config &)> &speculate) {
+                     const std::function<void(const faz_config &, const faz_config *)> &speculate) {
     const int N = c.N;
     if (c.QoZ || c.autoTuningRate > 0 || c.predictorTuningRate > 0)
         throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ / rate-driven tuning is not implemented on the GPU path"};
@@ -690,24 +692,31 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             ok = false;  // the trial's own error surfaces below
         }
         if (ok) {
-            // the Lorenzo trial is not waited for: interpolation usually wins
+            // the Lorenzo trial is not waited for: interpolation usually wins.
+            // The decision rule below runs on the pre-zstd sizes; zstd moves
+            // a trial's size by a few tenths of a percent at most, so choices
+            // closer than kClose are called for both sides.
+            constexpr double kClose = 0.003;
+            auto ratio = [&](size_t raw) { return sbytes / (raw + 8); };
+            auto pick_dir = [&](int op) { return ratio(rd[op]) > ratio(ri[op]) * 1.02 ? dop : dir0; };
             faz_config g = c;
-            double bi = 0;
-            for (int op = 0; op < 2; op++) {
-                const double rr = sbytes / (ri[op] + 8);
-                if (rr > bi) {
-                    bi = rr;
-                    g.interpAlgo = op;
-                }
-            }
-            const double rr = sbytes / (rd[g.interpAlgo] + 8);
-            if (rr > bi * 1.02) {
-                bi = rr;
-                g.interpDirection = dop;
-            }
             g.cmprAlgo = FAZ_ALGO_INTERP;
-            if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  overlapped compression starts\n", ms_since(tt0));
-            speculate(g);
+            g.interpAlgo = ratio(ri[1]) > ratio(ri[0]) ? 1 : 0;
+            g.interpDirection = pick_dir(g.interpAlgo);
+            faz_config alt = g;
+            const double r0 = ratio(ri[0]), r1 = ratio(ri[1]);
+            if (std::fabs(r0 - r1) < kClose * std::min(r0, r1)) {
+                alt.interpAlgo = 1 - g.interpAlgo;
+                alt.interpDirection = pick_dir(alt.interpAlgo);
+            } else {
+                const double q = ratio(rd[g.interpAlgo]) / (ratio(ri[g.interpAlgo]) * 1.02);
+                if (std::fabs(q - 1.0) < kClose) alt.interpDirection = g.interpDirection == dop ? dir0 : dop;
+            }
+            const bool two = alt.interpAlgo != g.interpAlgo || alt.interpDirection != g.interpDirection;
+            if (tune_trace())
+                std::fprintf(stderr, "tune %8.3f ms  overlapped compression starts (%s)\n", ms_since(tt0),
+                             two ? "two candidates" : "one candidate");
+            speculate(g, two ? &alt : nullptr);
             if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  overlapped compression ends\n", ms_since(tt0));
         }
     }
@@ -753,9 +762,9 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
 }
 
 template void sz3_tune_device<float>(faz_config &, const float *, cudaStream_t, Counter &, faz_timings &,
-                                     const std::function<void(const faz_config &)> &);
+                                     const std::function<void(const faz_config &, const faz_config *)> &);
 template void sz3_tune_device<double>(faz_config &, const double *, cudaStream_t, Counter &, faz_timings &,
-                                      const std::function<void(const faz_config &)> &);
+                                      const std::function<void(const faz_config &, const faz_config *)> &);
 
 
 // After the QoZ tuner chose Lorenzo (SZInterp.hpp:2797-2845): the sample of
