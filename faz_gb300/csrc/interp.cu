@@ -750,8 +750,8 @@ size_t level_smem_bytes(const LevelArgs &a) {
     return vb + (size_t)a.stage_cap * sizeof(uint16_t);
 }
 
-// Coarse levels (stride >= 2) of fields below 2^31 values: the three sweep
-// launches of k_level_sweep instead of one CTA per block.
+// Coarse levels (stride >= 2) with few blocks, of fields below 2^31 values:
+// the three sweep launches of k_level_sweep instead of one CTA per block.
 template <typename T>
 cudaError_t launch_level_sweeps(const LevelArgs &a, int64_t nblocks, bool decomp, const T *X, T *W, uint16_t *codes,
                                 T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st,
@@ -792,8 +792,16 @@ cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const
     int threads = vol >= 8192 ? 512 : (vol >= 1024 ? 256 : (vol >= 256 ? 128 : 64));
     const bool wide = a.dims[0] * a.dims[1] * a.dims[2] >= ((int64_t)1 << 31);
     const bool straight = sizeof(T) == 4 && a.fast && a.trim == 0;
+    // levels with fewer blocks than two per SM (the block kernel would leave
+    // SMs idle) take the sweep launches
+    static const int sms = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
     const int64_t per_block = (a.bs / a.s + 1) * (a.bs / a.s + 1) * (a.bs / a.s + 1) / 256 + 1;
-    if (a.s >= 2 && !wide && nblocks * per_block < (1ll << 31))
+    if (a.s >= 2 && !wide && nblocks < 2 * sms && nblocks * per_block < (1ll << 31))
         return launch_level_sweeps<T>(a, nblocks, decomp, X, W, codes, scratch, zpos, nz, unpred, st, nlaunch);
     ++*nlaunch;
     void (*k)(LevelArgs, const T *, T *, uint16_t *, T *, const uint64_t *, uint64_t, const T *);
