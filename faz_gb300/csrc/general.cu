@@ -310,8 +310,9 @@ void gen_compress_payload(int N, const uint64_t *dims, int bs, int lo, int lo2, 
     std::vector<uint8_t> h2;
     append_tree(h2, hc.cb, hc.nbytes);
     const size_t total = h0.size() + sbits + h1.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes;
-    out.resize(total);
-    uint8_t *p = out.data();
+    // device parts come back through the thread's pinned staging buffer
+    uint8_t *pin = t_pin_payload.get(total + 8);
+    uint8_t *p = pin;
     std::memcpy(p, h0.data(), h0.size());
     p += h0.size();
     if (sbits) CK(cudaMemcpyAsync(p, hs.bits, sbits, cudaMemcpyDeviceToHost, st));
@@ -324,6 +325,7 @@ void gen_compress_payload(int N, const uint64_t *dims, int bs, int lo, int lo2, 
     p += h2.size();
     if (hc.nbytes) CK(cudaMemcpyAsync(p, hc.bits, hc.nbytes, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    out.assign(pin, pin + total);
     tm.unpred_count = nunpred;
     tm.payload_bytes = total;
     tm.predict_ms += ev_pred.ms();

@@ -431,10 +431,13 @@ void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, uint16_t *co
     k<<<grid, kLorWarps * 32, smem, st>>>(a, dorder, nb, sync, sync + 1, derr, X, R, codes, scratch, ind, zpos, nz,
                                           unpred);
     launches(cudaGetLastError());
-    int herr = 0;
-    CK(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, st));
+    // the flag comes back through pinned memory: a copy to pageable memory
+    // would hold the driver's pageable staging path while this kernel runs,
+    // stalling concurrent pageable copies (the tuner's other trials)
+    int *herr = (int *)t_pin_small.get(64);
+    CK(cudaMemcpyAsync(herr, derr, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (herr) throw Fail{FAZ_ERR_DEVICE, "Lorenzo wavefront: a block waited too long for its neighbours"};
+    if (*herr) throw Fail{FAZ_ERR_DEVICE, "Lorenzo wavefront: a block waited too long for its neighbours"};
 }
 
 // meta_params as written by write(params, c) (include/QoZ/utils/MetaDef.hpp:33-60):
@@ -650,8 +653,10 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     const size_t rbits = reg_count ? hr.nbytes : 0;
     const size_t total =
         h0.size() + hi.nbytes + hreg.size() + rbits + h1.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes;
-    out.resize(total);
-    uint8_t *p = out.data();
+    // device parts come back through the thread's pinned staging buffer
+    // (copies to pageable memory serialise with other threads' copies)
+    uint8_t *pin = t_pin_payload.get(total + 8);
+    uint8_t *p = pin;
     std::memcpy(p, h0.data(), h0.size());
     p += h0.size();
     if (hi.nbytes) CK(cudaMemcpyAsync(p, hi.bits, hi.nbytes, cudaMemcpyDeviceToHost, st));
@@ -668,6 +673,7 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     p += h2.size();
     if (hc.nbytes) CK(cudaMemcpyAsync(p, hc.bits, hc.nbytes, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    out.assign(pin, pin + total);
     tm.unpred_count = nunpred;
     tm.payload_bytes = total;
     tm.predict_ms += ev_pred.ms();

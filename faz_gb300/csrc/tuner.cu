@@ -343,14 +343,18 @@ void block_interp_tail(int N, const uint64_t *sdims, double eb, int cubic, int d
     put<uint64_t>(h, nunpred);
     std::vector<uint8_t> h2;
     append_tree(h2, hc.cb, hc.nbytes);
-    pl.resize(h.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes);
-    std::memcpy(pl.data(), h.data(), h.size());
-    if (nunpred) CK(cudaMemcpyAsync(pl.data() + h.size(), unp, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
-    std::memcpy(pl.data() + h.size() + nunpred * sizeof(T), h2.data(), h2.size());
+    // device parts come back through the thread's pinned staging buffer
+    // (copies to pageable memory serialise with the other trials' copies)
+    const size_t total = h.size() + nunpred * sizeof(T) + h2.size() + hc.nbytes;
+    uint8_t *pin = t_pin_payload.get(total + 8);
+    std::memcpy(pin, h.data(), h.size());
+    if (nunpred) CK(cudaMemcpyAsync(pin + h.size(), unp, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
+    std::memcpy(pin + h.size() + nunpred * sizeof(T), h2.data(), h2.size());
     if (hc.nbytes)
-        CK(cudaMemcpyAsync(pl.data() + h.size() + nunpred * sizeof(T) + h2.size(), hc.bits, hc.nbytes,
+        CK(cudaMemcpyAsync(pin + h.size() + nunpred * sizeof(T) + h2.size(), hc.bits, hc.nbytes,
                            cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    pl.assign(pin, pin + total);
 }
 
 // One trial on its own host thread and CUDA stream: the trials are
@@ -649,11 +653,18 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     jd[0].name = "linear-dir5";
     jd[1].name = "cubic-dir5";
     for (Trial *t : {&jl, &ji[0], &ji[1], &jd[0], &jd[1]}) t->t0 = tt0;
-    jl.start(ready.a, [&](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
-                          const std::function<void(size_t)> &) {
-        if (N == 3) lorenzo_payload<T>(sdims, dS, 5, 3, eb, c.quantbinCnt / 2, s2, c2, t2, pl);
-        else gen_compress_payload<T>(N, sdims, 5, 1, 1, eb, c.quantbinCnt / 2, dS, s2, c2, t2, pl);
-    });
+    // The Lorenzo trial is a long wavefront launch; streams share the GPU's
+    // hardware work queues, so started first it can hold up the interpolation
+    // trials' short kernels.  With speculation it starts once their pre-zstd
+    // sizes are in.
+    auto start_lorenzo = [&]() {
+        jl.start(ready.a, [&](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
+                              const std::function<void(size_t)> &) {
+            if (N == 3) lorenzo_payload<T>(sdims, dS, 5, 3, eb, c.quantbinCnt / 2, s2, c2, t2, pl);
+            else gen_compress_payload<T>(N, sdims, 5, 1, 1, eb, c.quantbinCnt / 2, dS, s2, c2, t2, pl);
+        });
+    };
+    if (!speculate) start_lorenzo();
     const int dir0 = c.interpDirection;
     // the four block-interpolation trials' sweeps in shared launches on a
     // high-priority stream; each trial's Huffman stage then runs on its own
@@ -691,6 +702,7 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         } catch (...) {
             ok = false;  // the trial's own error surfaces below
         }
+        start_lorenzo();
         if (ok) {
             // the Lorenzo trial is not waited for: interpolation usually wins.
             // The decision rule below runs on the pre-zstd sizes; zstd moves
