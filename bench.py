@@ -68,9 +68,9 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-sampled autotune comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-fields measurement")
     ap.add_argument("--no-combined", action="store_true", help="skip the combined f64 learned + batched workload")
-    ap.add_argument("--combined-fields", type=int, default=8,
+    ap.add_argument("--combined-fields", type=int, default=64,
                     help="float64 256x384x384 fields per bound in the combined workload")
-    ap.add_argument("--batch-fields", type=int, default=32,
+    ap.add_argument("--batch-fields", type=int, default=256,
                     help="fields in the batched measurement (the shapes cycle through the four batch shapes)")
     return ap.parse_args()
 
@@ -316,6 +316,11 @@ def batched_fields(nfields, eb, seed=7):
     import faz_gb300 as F
     from faz_gb300.fields import spectral_field
     rng = np.random.default_rng(seed)
+    # the batched call holds every field's reconstruction, codes and scratch
+    # (2.5 times the inputs) at once: cap the fields at what the device holds
+    free, _ = torch.cuda.mem_get_info()
+    per_cycle = sum(4 * int(np.prod(d)) for d in BATCH_SHAPES) * 3.6 / len(BATCH_SHAPES)
+    nfields = max(4, min(nfields, int(0.85 * free / per_cycle)))
     confs, xs = [], []
     for i in range(nfields):
         dims = BATCH_SHAPES[i % len(BATCH_SHAPES)]
@@ -340,15 +345,23 @@ def batched_fields(nfields, eb, seed=7):
         return best, out
 
     F.compress_batch(confs[:4], xs[:4])  # warm-up
-    t_batch, sb = timed(lambda: F.compress_batch(confs, xs))
+    # launch autotuner: the persistent launch's CTA size measured on one
+    # cycle of the shapes (levels time of the batched call), the fastest kept
+    tune = {}
+    for th in (512, 256, 128):
+        F.compress_batch(confs[:4], xs[:4], threads=th)
+        tune[th] = round(F.last_timings()["predict_ms"], 3)
+    threads = min(tune, key=tune.get)
+    t_batch, sb = timed(lambda: F.compress_batch(confs, xs, threads=threads), reps=1)
     tmb = F.last_timings()
-    t_one, so = timed(lambda: [F.compress_device(c, x) for c, x in zip(confs, xs)])
+    t_one, so = timed(lambda: [F.compress_device(c, x) for c, x in zip(confs, xs)], reps=1)
     assert sb == so, "batched streams differ from single-field streams"
     return {"fields": nfields, "shapes": [list(d) for d in BATCH_SHAPES], "bytes": nbytes,
             "batched": {"value": round(nbytes / t_batch / 1e9, 3), "unit": "GB/s", "ms": round(t_batch * 1e3, 2),
                         "levels_ms": round(tmb["predict_ms"], 2)},
             "one_call_per_field": {"value": round(nbytes / t_one / 1e9, 3), "unit": "GB/s",
                                    "ms": round(t_one * 1e3, 2)},
+            "launch_autotune": {"levels_ms_by_threads": tune, "threads": threads},
             "speedup": round(t_one / t_batch, 3),
             "ratio": round(nbytes / sum(len(s) for s in sb), 3),
             "identical_streams": True}
@@ -410,6 +423,9 @@ def combined_f64(nfields, rels=(1e-4, 1e-6), seed=11):
     return out
 
 
+HELD_OUT_FIELDS = 256  # held-out fields of the training distribution (seed outside the training set)
+
+
 def learned_vs_sampled(x, dims, eb):
     """The learned tuner against the sampled QoZ autotune, end to end through
     compress_device (tuning + compression + zstd, host clock): on this field
@@ -438,7 +454,7 @@ def learned_vs_sampled(x, dims, eb):
         model.infer(L.features(qc, x))
     torch.cuda.synchronize()
     t_net = (time.perf_counter() - t0) / 10
-    _, held = L.evaluate(model, 6, seed=999, reps=2)
+    _, held = L.evaluate(model, HELD_OUT_FIELDS, seed=999, reps=1)
     return {"this_field": {"sampled_ms": round(t_plain * 1e3, 2), "learned_ms": round(t_learn * 1e3, 2),
                            "speedup": round(t_plain / t_learn, 2), "ratio_sampled": round(nbytes / len(s_plain), 4),
                            "ratio_learned": round(nbytes / len(s_learn), 4), "same_stream": s_plain == s_learn,

@@ -228,9 +228,15 @@ class TaskThreads {
         int dev;
         std::function<void()> fn;
     };
-    static constexpr int kThreads = 8;
+    // one thread per host core, 8 to 32 of them (the tuners' trials and the
+    // QoZ tuner's alpha/beta tests run here concurrently)
+    static int thread_count() {
+        const unsigned hw = std::thread::hardware_concurrency();
+        return (int)std::min(32u, std::max(8u, hw));
+    }
     TaskThreads() {
-        for (int i = 0; i < kThreads; i++)
+        const int n = thread_count();
+        for (int i = 0; i < n; i++)
             th_.emplace_back([this] {
                 for (;;) {
                     Job job;

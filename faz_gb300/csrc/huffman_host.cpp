@@ -9,7 +9,6 @@
 // tree follows save/pad_tree (119-137, 569-633).
 #include <algorithm>
 #include <cstring>
-#include <functional>
 #include <numeric>
 
 #include "internal.h"
@@ -66,47 +65,49 @@ std::vector<int> map_iteration_order(const std::vector<int> &keys) {
     return order;
 }
 
-struct Node {
-    int left = -1, right = -1;
-    uint64_t freq = 0;
-    bool leaf = false;
-    int state = 0;
-};
-
 // Binary min-heap on freq with the reference's sift rules (qinsert stops on
 // parent <= new, qremove descends to the smaller child while parent > child).
+// Entries carry their node's frequency, so comparisons touch the heap array
+// alone.
 struct Heap {
-    std::vector<int> q{-1};  // 1-based
-    const std::vector<Node> *nodes;
-    uint64_t f(int i) const { return (*nodes)[q[i]].freq; }
-    void insert(int nd) {
-        q.push_back(nd);
-        int i = (int)q.size() - 1, j;
-        uint64_t fn = (*nodes)[nd].freq;
+    struct E {
+        uint64_t freq;
+        int node;
+    };
+    std::vector<E> q;  // 1-based
+    explicit Heap(size_t cap) {
+        q.reserve(cap + 1);
+        q.push_back({0, -1});
+    }
+    void insert(int nd, uint64_t fn) {
+        q.push_back({fn, nd});
+        size_t i = q.size() - 1, j;
         while ((j = i >> 1)) {
-            if (f(j) <= fn) break;
+            if (q[j].freq <= fn) break;
             q[i] = q[j];
             i = j;
         }
-        q[i] = nd;
+        q[i] = {fn, nd};
     }
     int remove() {
-        int top = q[1];
-        int last = q.back();
+        const int top = q[1].node;
+        const E last = q.back();
         q.pop_back();
-        int end = (int)q.size();
+        const size_t end = q.size();
         if (end > 1) {
             q[1] = last;
-            int i = 1, l;
+            // the element moved to the top sinks; the choice of the smaller
+            // child is unpredictable, so it is computed without a branch
+            size_t i = 1, l;
+            const E x = q[1];
             while ((l = i << 1) < end) {
-                if (l + 1 < end && f(l + 1) < f(l)) l++;
-                if (f(i) > f(l)) {
-                    std::swap(q[i], q[l]);
-                    i = l;
-                } else {
-                    break;
-                }
+                const size_t r = l + 1 < end ? l + 1 : l;
+                l += (size_t)(q[r].freq < q[l].freq);
+                if (!(x.freq > q[l].freq)) break;
+                q[i] = q[l];
+                i = l;
             }
+            q[i] = x;
         }
         return top;
     }
@@ -130,102 +131,106 @@ int build_codebook(const std::vector<int> &syms, const std::vector<uint64_t> &co
         return FAZ_ERR_ARG;
     }
     // distinct symbols in order of first occurrence = map insertion order
-    std::vector<int> idx(d);
-    std::iota(idx.begin(), idx.end(), 0);
-    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return first[a] < first[b]; });
+    // (first positions are distinct stream positions)
+    std::vector<std::pair<uint64_t, int>> byfirst(d);
+    for (size_t i = 0; i < d; i++) byfirst[i] = {first[i], (int)i};
+    std::sort(byfirst.begin(), byfirst.end());
     std::vector<int> keys(d);
-    for (size_t i = 0; i < d; i++) keys[i] = syms[idx[i]];
+    for (size_t i = 0; i < d; i++) keys[i] = syms[byfirst[i].second];
     std::vector<int> ord = map_iteration_order(keys);
     int mn = *std::min_element(syms.begin(), syms.end());
     int mx = *std::max_element(syms.begin(), syms.end());
     cb.offset = mn;
     cb.stateNum = mx - mn + 2;
-    std::vector<Node> nodes;
-    nodes.reserve(2 * d);
-    Heap h;
-    h.nodes = &nodes;
-    for (int o : ord) {
-        int si = idx[o];
-        Node nd;
-        nd.leaf = true;
-        nd.freq = counts[si];
-        nd.state = syms[si] - mn;
-        nodes.push_back(nd);
-        h.insert((int)nodes.size() - 1);
+    // nodes: leaves 0 .. d-1 in heap insertion order, then the merged nodes;
+    // a merged node's children always have smaller indices
+    const size_t nn = 2 * d - 1;
+    std::vector<int> left(nn, -1), right(nn, -1), state(d);
+    std::vector<uint64_t> freq(nn);
+    Heap h(nn);
+    for (size_t k = 0; k < d; k++) {
+        const int si = byfirst[ord[k]].second;
+        freq[k] = counts[si];
+        state[k] = syms[si] - mn;
+        h.insert((int)k, freq[k]);
     }
+    size_t next = d;
     while (h.size() > 1) {
         // the reference evaluates new_node(0, 0, qremove(), qremove()) right
         // to left: the first node removed is the right child
-        int b = h.remove();
-        int a = h.remove();
-        Node nd;
-        nd.left = a;
-        nd.right = b;
-        nd.freq = nodes[a].freq + nodes[b].freq;
-        nodes.push_back(nd);
-        h.insert((int)nodes.size() - 1);
+        const int b = h.remove();
+        const int a = h.remove();
+        left[next] = a;
+        right[next] = b;
+        freq[next] = freq[a] + freq[b];
+        h.insert((int)next, freq[next]);
+        next++;
     }
-    int root = h.q[1];
+    const int root = h.q[1].node;
+    // code lengths and bits (left 0, right 1), parents before children
+    std::vector<uint8_t> len(nn, 0);
+    std::vector<uint64_t> bits(nn, 0);
+    for (size_t i = nn; i-- > d;) {
+        if (len[i] >= 64) {
+            err = "Huffman code longer than 64 bits";
+            return FAZ_ERR_UNSUPPORTED;
+        }
+        len[left[i]] = len[right[i]] = (uint8_t)(len[i] + 1);
+        bits[left[i]] = bits[i] << 1;
+        bits[right[i]] = (bits[i] << 1) | 1;
+    }
     cb.code.assign(cb.stateNum, 0);
     cb.len.assign(cb.stateNum, 0);
     cb.maxlen = 0;
-    // iterative walk assigning codes (left 0, right 1)
-    struct Item { int node; int len; uint64_t bits; };
-    std::vector<Item> stack{{root, 0, 0}};
-    while (!stack.empty()) {
-        Item it = stack.back();
-        stack.pop_back();
-        const Node &nd = nodes[it.node];
-        if (nd.leaf) {
-            if (it.len > 64) {
-                err = "Huffman code longer than 64 bits";
-                return FAZ_ERR_UNSUPPORTED;
-            }
-            cb.code[nd.state] = it.len == 0 ? 0 : it.bits << (64 - it.len);
-            cb.len[nd.state] = (uint8_t)it.len;
-            cb.maxlen = std::max(cb.maxlen, it.len);
-            continue;
-        }
-        stack.push_back({nd.right, it.len + 1, (it.bits << 1) | 1});
-        stack.push_back({nd.left, it.len + 1, it.bits << 1});
+    for (size_t k = 0; k < d; k++) {
+        const int l = len[k];
+        cb.code[state[k]] = l == 0 ? 0 : bits[k] << (64 - l);
+        cb.len[state[k]] = (uint8_t)l;
+        cb.maxlen = std::max(cb.maxlen, l);
     }
-    // serialise: preorder numbering (pad_tree), L/R/C/t arrays
-    const uint32_t nc = (uint32_t)(2 * d - 1);
+    // serialise (pad_tree): preorder numbering - a node, its left subtree,
+    // its right subtree - from subtree sizes, then the L/R/C/t arrays
+    const uint32_t nc = (uint32_t)nn;
     cb.nodeCount = (int)nc;
+    std::vector<uint32_t> size(nn, 1), num(nn, 0);
+    for (size_t i = d; i < nn; i++) size[i] = 1 + size[left[i]] + size[right[i]];
+    num[root] = 0;
     std::vector<uint32_t> L(nc, 0), R(nc, 0);
     std::vector<int32_t> C(nc, 0);
     std::vector<uint8_t> t(nc, 0);
-    uint32_t counter = 0;
-    // preorder numbering: a node, then its left subtree, then its right
-    // subtree (tree depth <= 64, so recursion is shallow)
-    std::function<void(int, uint32_t)> pad = [&](int node, uint32_t i) {
-        const Node &nd = nodes[node];
-        C[i] = nd.leaf ? nd.state : 0;
-        t[i] = nd.leaf ? 1 : 0;
-        if (nd.left >= 0) {
-            L[i] = ++counter;
-            pad(nd.left, counter);
+    for (size_t i = nn; i-- > 0;) {
+        const uint32_t me = num[i];
+        if (i < d) {
+            C[me] = state[i];
+            t[me] = 1;
+            continue;
         }
-        if (nd.right >= 0) {
-            R[i] = ++counter;
-            pad(nd.right, counter);
-        }
-    };
-    pad(root, 0);
+        num[left[i]] = me + 1;
+        num[right[i]] = me + 1 + size[left[i]];
+        L[me] = num[left[i]];
+        R[me] = num[right[i]];
+    }
+    const int w = nc <= 256 ? 1 : (nc <= 65536 ? 2 : 4);
     std::vector<uint8_t> &o = cb.tree;
-    o.clear();
-    o.push_back(0);  // endian byte: little endian
-    int w = nc <= 256 ? 1 : (nc <= 65536 ? 2 : 4);
+    o.assign(1 + 2 * (size_t)nc * w + (size_t)nc * 4 + nc, 0);
+    uint8_t *p = o.data();
+    *p++ = 0;  // endian byte: little endian
     for (int pass = 0; pass < 2; pass++) {
         const std::vector<uint32_t> &A = pass ? R : L;
-        for (uint32_t i = 0; i < nc; i++) {
-            if (w == 1) o.push_back((uint8_t)A[i]);
-            else if (w == 2) put_le<uint16_t>(o, (uint16_t)A[i]);
-            else put_le<uint32_t>(o, A[i]);
+        for (uint32_t i = 0; i < nc; i++, p += w) {
+            if (w == 1) {
+                *p = (uint8_t)A[i];
+            } else if (w == 2) {
+                const uint16_t v = (uint16_t)A[i];
+                std::memcpy(p, &v, 2);
+            } else {
+                std::memcpy(p, &A[i], 4);
+            }
         }
     }
-    for (uint32_t i = 0; i < nc; i++) put_le<int32_t>(o, C[i]);
-    o.insert(o.end(), t.begin(), t.end());
+    std::memcpy(p, C.data(), (size_t)nc * 4);
+    p += (size_t)nc * 4;
+    std::memcpy(p, t.data(), nc);
     return FAZ_OK;
 }
 

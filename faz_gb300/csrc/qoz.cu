@@ -22,7 +22,12 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
+#include <cstdio>
 #include <cstring>
+#include <future>
+#include <memory>
+#include <exception>
 #include <string>
 #include <vector>
 
@@ -559,7 +564,15 @@ template int qoz_prepare<double>(faz_config &, const double *, cudaStream_t, Cou
 template <typename T>
 void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm) {
     const int N = c.N;
+    // FAZ_TUNE_TRACE=1: the tuner's timeline on stderr
+    const char *trace_env = std::getenv("FAZ_TUNE_TRACE");
+    const bool trace = trace_env && trace_env[0] == '1';
+    const auto t_start = clk::now();
+    auto mark = [&](const char *what, double a = 0, double b = 0) {
+        if (trace) std::fprintf(stderr, "qoz %9.3f ms  %s %g %g\n", ms_since(t_start), what, a, b);
+    };
     const int max_interp_level = qoz_prepare<T>(c, dX, st, launches);
+    mark("prepared");
     const double rel_bound = c.relErrorBound > 0 ? c.relErrorBound : c.absErrorBound / (double)(T)c.rng;
     const int64_t sbs = c.sampleBlockSize, bsz = sbs + 1;
     const uint64_t d0 = c.dims[0], d1 = c.dims[1], d2 = N == 3 ? c.dims[2] : 1;
@@ -674,6 +687,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         launches(cudaGetLastError());
     };
     gather(starts);
+    mark("sampled blocks", (double)nblk, (double)nv);
     auto block_sums = [&](const SumPlan &sp) -> double {
         k_qz_sum<<<(unsigned)((nblk + 63) / 64), 64, 0, st>>>(sp, err, bsum, nblk);
         launches(cudaGetLastError());
@@ -699,21 +713,46 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     std::vector<uint8_t> il(Lsel > 0 ? Lsel : 0), dl(Lsel > 0 ? Lsel : 0);
     const int dirs[2] = {0, N == 3 ? 5 : 1};
     SumPlan sp;
-    // CompressTest (SZInterp.hpp:1130-1392) of every sampled block: bit rate
-    // after Huffman + zstd, PSNR from the summed squared errors
-    std::vector<std::pair<int64_t, int64_t>> ranges;
-    auto compress_test = [&](int op, int dir, double alpha, double beta, double eb, double &bitrate, double &psnr,
-                             bool lists = true, double pc = 1.0) {
-        CK(cudaMemcpyAsync(work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    // One CompressTest (SZInterp.hpp:1130-1392) of every sampled block: bit
+    // rate after Huffman + zstd, PSNR from the summed squared errors.  Its
+    // device buffers and bookkeeping live in a context, so that several tests
+    // can run at once, each on its own stream and host thread.
+    struct CtCtx {
+        DevMem m;
+        T *work, *scratch;
+        uint16_t *codes;
+        double *err, *bsum;
+        std::vector<double> hsum;
+        SumPlan sp;
+        std::vector<std::pair<int64_t, int64_t>> ranges;
+        Counter launches;
+        faz_timings tm;
+        CtCtx(cudaStream_t s, uint64_t nv_, uint64_t ns_, uint64_t nblk_) : m(s), hsum(nblk_, 0.0) {
+            work = m.alloc<T>(nv_);
+            scratch = m.alloc<T>(ns_);
+            codes = m.alloc<uint16_t>(ns_);
+            err = m.alloc<double>(ns_);
+            bsum = m.alloc<double>(nblk_);
+            std::memset(&tm, 0, sizeof(tm));
+        }
+    };
+    auto compress_test_on = [&](CtCtx &x, cudaStream_t s, int op, int dir, double alpha, double beta, double eb,
+                                double &bitrate, double &psnr, bool lists, double pc) {
+        CK(cudaMemcpyAsync(x.work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, s));
         QzRun R{1, g.levels, 0, eb, alpha, beta, c.trimToZero, op, dir, lists ? &il : nullptr, lists ? &dl : nullptr};
-        qz_run<T>(g, R, work, codes, scratch, err, nblk, sp, &ranges, st, launches);
-        const double se = block_sums(sp);
+        qz_run<T>(g, R, x.work, x.codes, x.scratch, x.err, nblk, x.sp, &x.ranges, s, x.launches);
+        k_qz_sum<<<(unsigned)((nblk + 63) / 64), 64, 0, s>>>(x.sp, x.err, x.bsum, nblk);
+        x.launches(cudaGetLastError());
+        CK(cudaMemcpyAsync(x.hsum.data(), x.bsum, nblk * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        double se = 0;
+        for (uint64_t k = 0; k < nblk; k++) se += x.hsum[k];
         // q_bins: level ranges from the coarsest, each across all blocks
         // (the anchors travel with the first interpolated level)
         std::vector<int64_t> rlo, rlen, rout;
         int64_t o = 0;
-        for (size_t i = 0; i < ranges.size(); i++) {
-            const int64_t lo = i == 0 ? 0 : ranges[i].first, hi = ranges[i].second;
+        for (size_t i = 0; i < x.ranges.size(); i++) {
+            const int64_t lo = i == 0 ? 0 : x.ranges[i].first, hi = x.ranges[i].second;
             if (hi <= lo) continue;
             rlo.push_back(lo);
             rlen.push_back(hi - lo);
@@ -721,29 +760,29 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             o += (hi - lo) * (int64_t)nblk;
         }
         if (o != (int64_t)ns) throw Fail{FAZ_ERR_DEVICE, "tuning codes do not cover the sampled blocks"};
-        int64_t *dr = m.alloc<int64_t>(3 * rlo.size() + 3);
+        int64_t *dr = x.m.alloc<int64_t>(3 * rlo.size() + 3);
         std::vector<int64_t> hr;
         hr.insert(hr.end(), rlo.begin(), rlo.end());
         hr.insert(hr.end(), rlen.begin(), rlen.end());
         hr.insert(hr.end(), rout.begin(), rout.end());
-        CK(cudaMemcpyAsync(dr, hr.data(), hr.size() * 8, cudaMemcpyHostToDevice, st));
-        uint16_t *qb = m.alloc<uint16_t>(ns);
+        CK(cudaMemcpyAsync(dr, hr.data(), hr.size() * 8, cudaMemcpyHostToDevice, s));
+        uint16_t *qb = x.m.alloc<uint16_t>(ns);
         const int nr = (int)rlo.size();
-        k_qz_regroup<<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(codes, g.cpb, dr, dr + nr, dr + 2 * nr, nr, nblk,
-                                                                   qb, ns);
-        launches(cudaGetLastError());
+        k_qz_regroup<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(x.codes, g.cpb, dr, dr + nr, dr + 2 * nr, nr, nblk,
+                                                                  qb, ns);
+        x.launches(cudaGetLastError());
         HuffEncoded h;
-        huffman_encode_device(qb, ns, 32768, m, st, launches, h, tm);
+        huffman_encode_device(qb, ns, 32768, x.m, s, x.launches, h, x.tm);
         // unpredictable values in the order the quantiser kept them
         // (block by block, stream order): zeros of the block-major codes
         const uint64_t nsub = hist_subchunks(ns);
-        unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1), *zoff = m.alloc<unsigned long long>(nsub + 1);
-        unsigned long long *ztmp = m.alloc<unsigned long long>(scan_temp_words(nsub) + 1);
-        launches(launch_count_zeros(codes, ns, zc, st));
-        launches(launch_scan_u64(zc, zoff, nsub, ztmp, st));
+        unsigned long long *zc = x.m.alloc<unsigned long long>(nsub + 1), *zoff = x.m.alloc<unsigned long long>(nsub + 1);
+        unsigned long long *ztmp = x.m.alloc<unsigned long long>(scan_temp_words(nsub) + 1);
+        x.launches(launch_count_zeros(x.codes, ns, zc, s));
+        x.launches(launch_scan_u64(zc, zoff, nsub, ztmp, s));
         const uint64_t nunp = h.nzero;
-        T *unp = m.alloc<T>(nunp ? nunp : 1);
-        if (nunp) launches(launch_compact_zeros<T>(codes, ns, zc, zoff, nullptr, scratch, unp, st));
+        T *unp = x.m.alloc<T>(nunp ? nunp : 1);
+        if (nunp) x.launches(launch_compact_zeros<T>(x.codes, ns, zc, zoff, nullptr, x.scratch, unp, s));
         std::vector<uint8_t> head;
         put<uint8_t>(head, 2);
         put<double>(head, eb);
@@ -751,21 +790,36 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         put<uint64_t>(head, nunp);
         std::vector<uint8_t> tree;
         append_tree(tree, h.cb, h.nbytes);
-        std::vector<uint8_t> pl(head.size() + nunp * sizeof(T) + tree.size() + h.nbytes);
-        std::memcpy(pl.data(), head.data(), head.size());
-        if (nunp) CK(cudaMemcpyAsync(pl.data() + head.size(), unp, nunp * sizeof(T), cudaMemcpyDeviceToHost, st));
-        std::memcpy(pl.data() + head.size() + nunp * sizeof(T), tree.data(), tree.size());
+        // the payload through the thread's pinned staging buffer
+        const size_t plen = head.size() + nunp * sizeof(T) + tree.size() + h.nbytes;
+        uint8_t *pl = t_pin_payload.get(plen + 8);
+        std::memcpy(pl, head.data(), head.size());
+        if (nunp) CK(cudaMemcpyAsync(pl + head.size(), unp, nunp * sizeof(T), cudaMemcpyDeviceToHost, s));
+        std::memcpy(pl + head.size() + nunp * sizeof(T), tree.data(), tree.size());
         if (h.nbytes)
-            CK(cudaMemcpyAsync(pl.data() + head.size() + nunp * sizeof(T) + tree.size(), h.bits, h.nbytes,
-                               cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+            CK(cudaMemcpyAsync(pl + head.size() + nunp * sizeof(T) + tree.size(), h.bits, h.nbytes,
+                               cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
         // profiling_coeff scales both (SZInterp.hpp:1364-1370)
         const double ele = (double)nv;
-        bitrate = 8 * (double)zstd_framed_size_host(pl.data(), pl.size()) / ele;
+        mark("  compress test payload", (double)plen, alpha);
+        bitrate = 8 * (double)zstd_framed_size_host(pl, plen) / ele;
+        mark("  compress test zstd", beta, eb);
         bitrate *= pc;
         double mse = se / ele;
         mse *= pc;
         psnr = 20 * std::log10(c.rng) - 10 * std::log10(mse);
+    };
+    // tests on the tuner's own stream
+    std::unique_ptr<CtCtx> main_ctx;
+    auto compress_test = [&](int op, int dir, double alpha, double beta, double eb, double &bitrate, double &psnr,
+                             bool lists = true, double pc = 1.0) {
+        if (!main_ctx || main_ctx->hsum.size() != nblk) main_ctx.reset(new CtCtx(st, nv, ns, nblk));
+        compress_test_on(*main_ctx, st, op, dir, alpha, beta, eb, bitrate, psnr, lists, pc);
+        launches.n += main_ctx->launches.n;
+        main_ctx->launches.n = 0;
+        tm.host_ms += main_ctx->tm.host_ms;
+        main_ctx->tm.host_ms = 0;
     };
     // without the alpha/beta search (autoTuningRate = 0) the decisions
     // compare compression ratios of CompressTests (TUNING_TARGET_CR)
@@ -800,6 +854,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
                 }
             il[level - 1] = (uint8_t)best_op;
             dl[level - 1] = (uint8_t)best_dir;
+            mark("level selected", level, best_op * 10 + best_dir);
         }
         // the candidate loop leaves its last candidate in the configuration
         c.interpAlgo = FAZ_INTERP_ALGO_CUBIC;
@@ -856,11 +911,133 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             return (alpha >= 1 && std::pow(alpha, max_interp_level - 1) <= beta) ||
                    (alpha < 1 && alpha * (max_interp_level - 1) <= beta);
         };
+        // The grid's CompressTests at the bound itself are independent of
+        // one another: all of them run at once, each with its own stream,
+        // buffers and host thread.  The search below reads their results in
+        // the reference's order (a test it never reaches is simply unused)
+        // and runs the tests it derives on the way - a bound scaled by a ratio
+        // found so far - one by one.
+        struct GridRes {
+            double br = 0, mm = 0;
+            uint64_t launches = 0;
+            double host_ms = 0;
+        };
+        std::vector<std::pair<double, double>> grid;
+        for (double alpha : alist)
+            for (double beta : blist)
+                if (!((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1))) grid.emplace_back(alpha, beta);
+        CK(cudaStreamSynchronize(st));  // the sampled blocks are gathered
+        const int op0 = c.interpAlgo, dir0 = c.interpDirection;
+        std::vector<std::future<GridRes>> futs;
+        for (const auto &ab : grid) {
+            const double alpha = ab.first, beta = ab.second;
+            futs.push_back(TaskThreads::get().submit<GridRes>([&, alpha, beta]() {
+                StreamGuard sg(nullptr);
+                CtCtx x(sg.st, nv, ns, nblk);
+                GridRes r;
+                compress_test_on(x, sg.st, op0, dir0, alpha, beta, oriabseb, r.br, r.mm, true, pcoeff);
+                CK(cudaStreamSynchronize(sg.st));
+                r.launches = x.launches.n;
+                r.host_ms = x.tm.host_ms;
+                return r;
+            }));
+        }
+        std::vector<GridRes> gres(grid.size());
+        {
+            std::exception_ptr first;
+            for (size_t i = 0; i < futs.size(); i++) {
+                try {
+                    gres[i] = futs[i].get();
+                    launches.n += gres[i].launches;
+                    tm.host_ms += gres[i].host_ms;
+                } catch (...) {
+                    if (!first) first = std::current_exception();
+                }
+            }
+            if (first) std::rethrow_exception(first);
+        }
+        mark("grid tests", (double)grid.size());
+        auto grid_result = [&](double alpha, double beta, double &br, double &mm) {
+            for (size_t i = 0; i < grid.size(); i++)
+                if (grid[i].first == alpha && grid[i].second == beta) {
+                    br = gres[i].br;
+                    mm = gres[i].mm;
+                    return;
+                }
+            throw Fail{FAZ_ERR_DEVICE, "alpha/beta test missing from the grid"};
+        };
+        // The tests the search derives (at the bound scaled by a point's bit
+        // rate over the best one) follow from the grid's results as long as
+        // no derived test moves the best point, which is rare: walk the
+        // search under that assumption, run the derived tests it meets at
+        // once, and let the search below take a result only where its bound
+        // is the one the search asks for (else that test runs again).
+        struct Derived {
+            double alpha, beta, eb;
+            GridRes r;
+        };
+        std::vector<Derived> derived;
+        {
+            double bb = 9999, bm = 0;
+            for (double alpha : alist) {
+                for (double beta : blist) {
+                    if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
+                    double br, mm;
+                    grid_result(alpha, beta, br, mm);
+                    if (cr) mm = 0;
+                    if ((!cr && mm >= bm && br <= bb) || (cr && br <= bb)) {
+                        bb = br;
+                        bm = mm;
+                    } else if ((!cr && mm <= bm && br >= bb) || (cr && br > bb)) {
+                        if (stop_here(alpha, beta)) break;
+                        continue;
+                    } else {
+                        derived.push_back({alpha, beta, oriabseb * (br / bb), GridRes{}});
+                    }
+                    if (stop_here(alpha, beta)) break;
+                }
+            }
+            std::vector<std::future<GridRes>> dfut;
+            for (const Derived &dv : derived) {
+                const double alpha = dv.alpha, beta = dv.beta, ebd = dv.eb;
+                dfut.push_back(TaskThreads::get().submit<GridRes>([&, alpha, beta, ebd]() {
+                    StreamGuard sg(nullptr);
+                    CtCtx x(sg.st, nv, ns, nblk);
+                    GridRes r;
+                    compress_test_on(x, sg.st, op0, dir0, alpha, beta, ebd, r.br, r.mm, true, pcoeff);
+                    CK(cudaStreamSynchronize(sg.st));
+                    r.launches = x.launches.n;
+                    r.host_ms = x.tm.host_ms;
+                    return r;
+                }));
+            }
+            std::exception_ptr first;
+            for (size_t i = 0; i < dfut.size(); i++) {
+                try {
+                    derived[i].r = dfut[i].get();
+                    launches.n += derived[i].r.launches;
+                    tm.host_ms += derived[i].r.host_ms;
+                } catch (...) {
+                    if (!first) first = std::current_exception();
+                }
+            }
+            if (first) std::rethrow_exception(first);
+        }
+        mark("derived tests", (double)derived.size());
+        auto derived_test = [&](double alpha, double beta, double ebd, double &br, double &mm) {
+            for (const Derived &dv : derived)
+                if (dv.alpha == alpha && dv.beta == beta && dv.eb == ebd) {
+                    br = dv.r.br;
+                    mm = dv.r.mm;
+                    return;
+                }
+            compress_test(op0, dir0, alpha, beta, ebd, br, mm, true, pcoeff);
+        };
         for (double alpha : alist) {
             for (double beta : blist) {
                 if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
                 double br, mm;
-                compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb, br, mm, true, pcoeff);
+                grid_result(alpha, beta, br, mm);
                 if (cr) mm = 0;
                 if ((!cr && mm >= bestm && br <= bestb) || (cr && br <= bestb)) {
                     bestalpha = alpha;
@@ -873,7 +1050,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
                 } else {
                     const double fix = br / bestb;
                     double br2, m2;
-                    compress_test(c.interpAlgo, c.interpDirection, alpha, beta, oriabseb * fix, br2, m2, true, pcoeff);
+                    derived_test(alpha, beta, oriabseb * fix, br2, m2);
                     if (cr) m2 = 0;
                     const double a = (mm - m2) / (br - br2);
                     const double b = mm - a * br;
@@ -925,6 +1102,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         c.wavelet_rel_coeff = 1;
         c.wavelet = 0;
     }
+    mark("tuned", c.alpha, c.beta);
     if (!use_interp) {
         // Lorenzo: its own settings (the caller then runs the Lorenzo compressor)
         c.cmprAlgo = FAZ_ALGO_LORENZO_REG;

@@ -156,3 +156,45 @@ def test_gpu_committed_network_on_held_out_fields():
     for r in recs:
         # the error bound is the quantiser's: every stream decodes within it
         assert r["cr_learned"] > 1.0
+
+
+DATA = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "faz_gb300", "tuner_c4_dataset.npz")
+
+
+@pytest.mark.skipif(not os.path.exists(DATA), reason="no committed dataset")
+def test_stored_labels_match_the_oracle_tuners():
+    """Label audit: the 32 smallest of the 4096 training fields, regenerated
+    on the GPU, go through the oracle's QoZ tuner (the tool's -q) and the
+    labelling configuration (label_conf) on the CPU.  The labels stored in the
+    dataset - per-level interpolator and direction, alpha, beta, Lorenzo or
+    not, made by the library's GPU tuners - must equal the oracle's
+    decisions."""
+    import ast
+    import oracle.oracle as O
+    from conftest import parse_interp_header
+    d = np.load(DATA)
+    P = [ast.literal_eval(str(p)) for p in d["params"]]
+    Y = d["Y"]
+    order = sorted(range(len(P)), key=lambda i: int(np.prod(P[i]["dims"])))[:32]
+    O.set_zstd(None)  # the library's tuners sized their trials with the host zstd
+    mismatches = []
+    for i in order:
+        fp = P[i]
+        x = L.make_field(fp).cpu().numpy()
+        sq, pq = O.compress(L.qoz_conf(fp["dims"], fp["rel"]), x)
+        sl, _ = O.compress(L.label_conf(fp["dims"], fp["rel"]), x)
+        cq, cl = O.read_stream(sq)[0], O.read_stream(sl)[0]
+        lab = np.full(L.N_LABELS, -1, np.int32)
+        if cq.cmprAlgo != 0:  # an interpolation stream: its header holds the decisions
+            h = parse_interp_header(pq, 3)
+            cq.interpAlgo_list, cq.interpDirection_list = h["interp_list"], h["dir_list"]
+            cq.alpha, cq.beta = h["alpha"], h["beta"]
+            lab = L.labels_of(cq, cl)
+            want = Y[i]
+        else:  # the QoZ tuner chose Lorenzo: only the Lorenzo label applies
+            lab[6] = 1 if cl.cmprAlgo == 0 else 0
+            want = np.full(L.N_LABELS, -1, np.int32)
+            want[6] = Y[i][6]
+        if not np.array_equal(lab[:7], want[:7]):
+            mismatches.append((i, lab[:7].tolist(), want[:7].tolist()))
+    assert not mismatches, mismatches

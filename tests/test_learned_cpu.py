@@ -44,21 +44,27 @@ def test_bf16_rounding_is_nearest_even():
 
 
 @pytest.mark.skipif(not os.path.exists(L.DEFAULT_MODEL) or not os.path.exists(DATA), reason="no committed model")
-def test_committed_network_beats_the_majority_rule():
+def test_committed_network_beats_the_majority_rule_on_held_out_fields():
     """What the trained network gains over the method without it: per head,
-    its accuracy on the QoZ tuner's decisions against always answering the
-    most frequent decision."""
+    its accuracy on the QoZ tuner's decisions for the validation fields (the
+    1/8 of the dataset training never saw) against always answering the most
+    frequent decision; the accuracies recorded with the model are these."""
     d = np.load(DATA)
     X, Y = d["X"], d["Y"]
+    _, va = L.split(len(X))
     m = L.TunerModel.load()
-    z = M.forward(m.params, (X - m.mean) / m.std)[2]
-    acc = L.head_accuracy(z, Y)
-    for h, (lo, n) in enumerate(L.HEADS):
-        lab = Y[:, h][Y[:, h] >= 0]
-        majority = np.bincount(lab, minlength=n).max() / lab.size
-        assert acc[h] >= majority - 1e-9, (h, acc[h], majority)
+    z = M.forward(m.params, (X[va] - m.mean) / m.std)[2]
+    acc = L.head_accuracy(z, Y[va])
+    majority = L.majority_rates(Y[va])
+    for h in range(L.N_HEADS):
+        assert acc[h] >= majority[h] - 1e-9, (h, acc[h], majority[h])
     # the per-level interpolator / direction heads carry the tuner's decisions
-    assert min(acc[:4]) > 0.9, acc
+    for h in range(4):
+        assert acc[h] >= majority[h] + 0.15, (h, acc[h], majority[h])
+    assert np.mean(acc[:4]) > 0.85, acc
+    rec = np.load(L.DEFAULT_MODEL)
+    if "val_accuracy" in rec.files:
+        assert np.allclose(rec["val_accuracy"], acc, atol=0.01), (rec["val_accuracy"], acc)
 
 
 @pytest.mark.skipif(not os.path.exists(L.DEFAULT_MODEL), reason="no committed model")
