@@ -213,8 +213,12 @@ void check_config(const faz_config &c) {
     if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};
     if (c.wavelet != 0 || ((c.wavelet > 0 || c.sperrWithoutWave) && c.sperr >= c.wavelet))
         throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet / SPERR modes are not part of the interpolation path"};
-    if (c.quantbinCnt < 2 || c.quantbinCnt > 65536)
-        throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt must be in [2, 65536] on the GPU path"};
+    // 32-bit codes (more than 65536 bins) are implemented for the 3-D Lorenzo
+    // frontend, where the default tuner's interval estimate can ask for them
+    if (c.quantbinCnt < 2 || c.quantbinCnt > 131072 ||
+        (c.quantbinCnt > 65536 && !(c.cmprAlgo == FAZ_ALGO_LORENZO_REG && c.N == 3)))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt must be in [2, 65536] on the GPU path (up to 131072 for "
+                                        "ALGO_LORENZO_REG on 3-D data)"};
     if (c.interp_list_len < 0 || c.interp_list_len > FAZ_MAX_LEVELS) throw Fail{FAZ_ERR_ARG, "bad level list length"};
 }
 
@@ -302,11 +306,12 @@ struct Sink {
 // Histogram, codebook (host) and Huffman encoding of n codes on the device
 // (HuffmanEncoder::preprocess_encode + encode, HuffmanEncoder.hpp:93-227).
 // `center` is the code the histogram's shared-memory window is centred on.
-void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
-                           Counter &launches, HuffEncoded &h, faz_timings &tm,
-                           const std::function<void(const HuffEncoded &)> &sized) {
+template <typename C>
+void huffman_encode_impl(const C *codes, uint64_t n, int center, DevMem &m, cudaStream_t st, Counter &launches,
+                         HuffEncoded &h, faz_timings &tm, const std::function<void(const HuffEncoded &)> &sized) {
     const uint64_t nsub = hist_subchunks(n);
-    const int nsym = 65536;
+    // every value a code of this width can take
+    const int nsym = sizeof(C) == 2 ? 65536 : std::max(65536, 2 * center + 1);
     unsigned long long *hist = m.alloc<unsigned long long>(nsym);
     unsigned long long *first = m.alloc<unsigned long long>(nsym);
     h.zc = m.alloc<unsigned long long>(nsub + 1);
@@ -365,6 +370,18 @@ void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem
     CK(cudaMemsetAsync(h.bits, 0, nwords * 4, st));
     if (total_bits)
         launches(launch_encode_pack(codes, n, cb.offset, dcode, dpacked, dlen, coff, h.bits, std::max(cb.maxlen, 1), st));
+}
+
+void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
+                           Counter &launches, HuffEncoded &h, faz_timings &tm,
+                           const std::function<void(const HuffEncoded &)> &sized) {
+    huffman_encode_impl(codes, n, center, m, st, launches, h, tm, sized);
+}
+void huffman_encode_device(const uint32_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
+                           Counter &launches, HuffEncoded &h, faz_timings &tm,
+                           const std::function<void(const HuffEncoded &)> &sized) {
+    if (center < 0 || center > (1 << 20)) throw Fail{FAZ_ERR_UNSUPPORTED, "quantisation radius too large"};
+    huffman_encode_impl(codes, n, center, m, st, launches, h, tm, sized);
 }
 
 // HuffmanEncoder::save header + tree, then the encoded size (HuffmanEncoder.hpp:119-137, 150-227)
@@ -478,6 +495,7 @@ void interp_levels(InterpCodes<T> &r, faz_config &c, const T *dX, cudaStream_t s
     const double eb = c.absErrorBound;
     if (!(eb > 0) || !std::isfinite(eb)) throw Fail{FAZ_ERR_ARG, "error bound must be positive and finite"};
     const int radius = c.quantbinCnt / 2;
+    if (radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "interpolation with more than 65536 bins is not implemented"};
     r.il.assign(c.interpAlgo_list, c.interpAlgo_list + c.interp_list_len);
     r.dl.assign(c.interpDirection_list, c.interpDirection_list + c.interp_list_len);
     Plan p = make_plan<T>(c.N, c.dims, c.maxStep, c.interpBlockSize, c.fixBlockSize, c.interpAlgo, c.interpDirection,
@@ -1225,8 +1243,9 @@ void parse_payload(const uint8_t *pl, size_t n, int N, Parsed &P) {
 
 // HuffmanEncoder::load + decode (HuffmanEncoder.hpp:236-296) on the device:
 // reads the tree and bit string at p (advancing it) and writes num codes.
-void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, uint16_t *codes, DevMem &m,
-                           cudaStream_t st, Counter &launches) {
+template <typename C>
+void huffman_decode_impl(const uint8_t *&p, const uint8_t *end, uint64_t num, C *codes, DevMem &m, cudaStream_t st,
+                         Counter &launches) {
     DecodeTablesHost t;
     std::string err;
     int rc = parse_tree(p, end, t, err);
@@ -1240,7 +1259,8 @@ void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, 
     p += nbytes;
     if (t.constant || nbytes == 0) {
         int v = t.constant_state + t.offset;
-        launches(launch_fill_u16(codes, num, (uint16_t)v, st));
+        if (v < 0 || (sizeof(C) == 2 && v > 65535)) throw Fail{FAZ_ERR_FORMAT, "Huffman symbol out of range"};
+        launches(launch_fill_u16(codes, num, (C)v, st));
         return;
     }
     const uint64_t nwords = (nbytes + 3) / 4;
@@ -1295,10 +1315,20 @@ void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, 
     launches(launch_decode_write(td, dbits, nwords, nbits, nunits, start, off, num, t.offset, codes, st));
 }
 
+void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, uint16_t *codes, DevMem &m,
+                           cudaStream_t st, Counter &launches) {
+    huffman_decode_impl(p, end, num, codes, m, st, launches);
+}
+void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, uint32_t *codes, DevMem &m,
+                           cudaStream_t st, Counter &launches) {
+    huffman_decode_impl(p, end, num, codes, m, st, launches);
+}
+
 // Sorted positions of the zero codes (the unpredictable points); returns
 // their count.
-uint64_t zero_positions(const uint16_t *codes, uint64_t num, DevMem &m, cudaStream_t st, Counter &launches,
-                        uint64_t *&zpos) {
+template <typename C>
+uint64_t zero_positions_impl(const C *codes, uint64_t num, DevMem &m, cudaStream_t st, Counter &launches,
+                             uint64_t *&zpos) {
     const uint64_t nsub = hist_subchunks(num);
     unsigned long long *zc = m.alloc<unsigned long long>(nsub + 1);
     unsigned long long *zoff = m.alloc<unsigned long long>(nsub + 1);
@@ -1312,6 +1342,14 @@ uint64_t zero_positions(const uint16_t *codes, uint64_t num, DevMem &m, cudaStre
     zpos = m.alloc<uint64_t>(nz ? nz : 1);
     if (nz) launches(launch_compact_zeros<float>(codes, num, zc, zoff, zpos, nullptr, nullptr, st));
     return nz;
+}
+uint64_t zero_positions(const uint16_t *codes, uint64_t num, DevMem &m, cudaStream_t st, Counter &launches,
+                        uint64_t *&zpos) {
+    return zero_positions_impl(codes, num, m, st, launches, zpos);
+}
+uint64_t zero_positions(const uint32_t *codes, uint64_t num, DevMem &m, cudaStream_t st, Counter &launches,
+                        uint64_t *&zpos) {
+    return zero_positions_impl(codes, num, m, st, launches, zpos);
 }
 
 namespace {

@@ -407,13 +407,21 @@ struct HuffEncoded {
 };
 // `sized`, when given, runs as soon as the codebook, the zero count and the
 // encoded size are known on the host (before the encoding kernels finish).
+// The uint32_t overloads serve quantisers of more than 65536 bins.
 void huffman_encode_device(const uint16_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
+                           Counter &launches, HuffEncoded &h, faz_timings &tm,
+                           const std::function<void(const HuffEncoded &)> &sized = {});
+void huffman_encode_device(const uint32_t *codes, uint64_t n, int center, DevMem &m, cudaStream_t st,
                            Counter &launches, HuffEncoded &h, faz_timings &tm,
                            const std::function<void(const HuffEncoded &)> &sized = {});
 void append_tree(std::vector<uint8_t> &o, const Codebook &cb, uint64_t nbytes);
 void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, uint16_t *codes, DevMem &m,
                            cudaStream_t st, Counter &launches);
+void huffman_decode_device(const uint8_t *&p, const uint8_t *end, uint64_t num, uint32_t *codes, DevMem &m,
+                           cudaStream_t st, Counter &launches);
 uint64_t zero_positions(const uint16_t *codes, uint64_t num, DevMem &m, cudaStream_t st, Counter &launches,
+                        uint64_t *&zpos);
+uint64_t zero_positions(const uint32_t *codes, uint64_t num, DevMem &m, cudaStream_t st, Counter &launches,
                         uint64_t *&zpos);
 
 }  // namespace faz

@@ -25,7 +25,10 @@ static constexpr int HWARPS = 32;
 static constexpr uint64_t HSUB = 8192;
 static constexpr uint64_t HCHUNK = HSUB * HWARPS;
 
-__global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__ codes, uint64_t n, int center,
+// C: the code type, uint16_t, or uint32_t for quantisers of more than 65536
+// bins (16-byte loads for 16-bit codes, plain loads otherwise).
+template <typename C>
+__global__ void __launch_bounds__(1024) k_histogram(const C *__restrict__ codes, uint64_t n, int center,
                                                     unsigned long long *hist, unsigned long long *first,
                                                     unsigned long long *zcount) {
     __shared__ unsigned int scnt[HWIN];
@@ -56,7 +59,7 @@ __global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__
             atomicMin(&first[v], (unsigned long long)i);
         }
     };
-    if (s1 - s0 == HSUB) {
+    if (sizeof(C) == 2 && s1 - s0 == HSUB) {
         const uint4 *cv = reinterpret_cast<const uint4 *>(codes + s0);
         for (int it = 0; it < (int)(HSUB / 256); it++) {
             uint4 q = cv[it * 32 + lane];
@@ -66,7 +69,7 @@ __global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__
             for (int k = 0; k < 8; k++) count(e[k], i0 + k);
         }
     } else {
-        for (uint64_t i = s0 + lane; i < s1; i += 32) count(codes[i], i);
+        for (uint64_t i = s0 + lane; i < s1; i += 32) count((int)codes[i], i);
     }
     for (int o = 16; o > 0; o >>= 1) zc += __shfl_down_sync(0xffffffffu, zc, o);
     if (lane == 0) zcount[(uint64_t)blockIdx.x * HWARPS + w] = zc;
@@ -80,7 +83,8 @@ __global__ void __launch_bounds__(1024) k_histogram(const uint16_t *__restrict__
 }
 
 // Zero-code count per warp sub-chunk (decompress side).
-__global__ void __launch_bounds__(1024) k_count_zeros(const uint16_t *__restrict__ codes, uint64_t n,
+template <typename C>
+__global__ void __launch_bounds__(1024) k_count_zeros(const C *__restrict__ codes, uint64_t n,
                                                       unsigned long long *zcount) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint64_t s0 = (uint64_t)blockIdx.x * HCHUNK + (uint64_t)w * HSUB;
@@ -95,8 +99,8 @@ __global__ void __launch_bounds__(1024) k_count_zeros(const uint16_t *__restrict
 // Compaction of the zero codes of each warp sub-chunk, in stream order,
 // starting at zoff[sub-chunk]: positions (zpos) and/or the values recorded at
 // those positions (vals from scratch).
-template <typename T>
-__global__ void __launch_bounds__(1024) k_compact_zeros(const uint16_t *__restrict__ codes, uint64_t n,
+template <typename T, typename C>
+__global__ void __launch_bounds__(1024) k_compact_zeros(const C *__restrict__ codes, uint64_t n,
                                                         const unsigned long long *zcount,
                                                         const unsigned long long *zoff, uint64_t *zpos,
                                                         const T *scratch, T *vals) {
@@ -111,7 +115,7 @@ __global__ void __launch_bounds__(1024) k_compact_zeros(const uint16_t *__restri
     // 16-byte load (s0 is a multiple of 8192 and codes is 256-byte aligned),
     // so the zeros of a step come in stream order lane by lane
     uint64_t b = s0;
-    for (; b + 256 <= s1; b += 256) {
+    for (; sizeof(C) == 2 && b + 256 <= s1; b += 256) {
         const uint4 q = *reinterpret_cast<const uint4 *>(codes + b + 8 * lane);
         const uint32_t wd[4] = {q.x, q.y, q.z, q.w};
         unsigned int m = 0;  // bit k: code b + 8 lane + k is zero
@@ -241,7 +245,8 @@ static constexpr int ENC_PER_THREAD = 16;
 static constexpr int ENC_THREADS = 256;
 static constexpr int ENC_CHUNK = ENC_PER_THREAD * ENC_THREADS;
 
-__global__ void __launch_bounds__(ENC_THREADS) k_encode_bits(const uint16_t *__restrict__ codes, uint64_t n, int offset,
+template <typename C>
+__global__ void __launch_bounds__(ENC_THREADS) k_encode_bits(const C *__restrict__ codes, uint64_t n, int offset,
                                                             const uint8_t *__restrict__ len,
                                                             unsigned long long *chunkbits) {
     __shared__ unsigned long long ws[ENC_THREADS / 32];
@@ -249,7 +254,7 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_bits(const uint16_t *__r
     unsigned long long s = 0;
     for (int k = 0; k < ENC_PER_THREAD; k++) {
         uint64_t i = c0 + (uint64_t)k * ENC_THREADS + threadIdx.x;
-        if (i < n) s += len[codes[i] - offset];
+        if (i < n) s += len[(int)codes[i] - offset];
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -267,7 +272,8 @@ __device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 
 // Words in shared memory follow the global 32-bit word grid of the output.
 // packed[state] = (len << 32) | code right-aligned (codes up to 32 bits);
 // longer codes are read from code64 (MSB-aligned).
-__global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__restrict__ codes, uint64_t n, int offset,
+template <typename C>
+__global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const C *__restrict__ codes, uint64_t n, int offset,
                                                             const unsigned long long *__restrict__ code64,
                                                             const unsigned long long *__restrict__ packed,
                                                             const uint8_t *__restrict__ len,
@@ -283,12 +289,12 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
     const uint64_t wl = (gend - 1) >> 5;
     const int nwords = (int)(wl - w0 + 1);
     for (int i = threadIdx.x; i < nwords && i < smem_words; i += blockDim.x) sw[i] = 0;
-    uint16_t sym[ENC_PER_THREAD];
+    C sym[ENC_PER_THREAD];
     unsigned int mybits = 0;
     const uint64_t t0 = c0 + (uint64_t)threadIdx.x * ENC_PER_THREAD;
     // symbols of this thread (every 16-bit value is a valid symbol)
     const int nvalid = t0 >= n ? 0 : (n - t0 >= ENC_PER_THREAD ? ENC_PER_THREAD : (int)(n - t0));
-    if (nvalid == ENC_PER_THREAD) {
+    if (sizeof(C) == 2 && nvalid == ENC_PER_THREAD) {
         // 16 codes = two 16-byte loads (codes is 256-byte aligned, t0 a multiple of 16)
         const uint4 *cv = reinterpret_cast<const uint4 *>(codes + t0);
         uint4 qa = cv[0], qb = cv[1];
@@ -296,8 +302,8 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
         const uint16_t *pb = reinterpret_cast<const uint16_t *>(&qb);
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            sym[k] = (uint16_t)(pa[k] - offset);
-            sym[k + 8] = (uint16_t)(pb[k] - offset);
+            sym[k] = (C)(pa[k] - offset);
+            sym[k + 8] = (C)(pb[k] - offset);
         }
 #pragma unroll
         for (int k = 0; k < ENC_PER_THREAD; k++) mybits += len[sym[k]];
@@ -305,7 +311,7 @@ __global__ void __launch_bounds__(ENC_THREADS) k_encode_pack(const uint16_t *__r
 #pragma unroll
         for (int k = 0; k < ENC_PER_THREAD; k++) {
             uint64_t i = t0 + k;
-            sym[k] = i < n ? (uint16_t)(codes[i] - offset) : 0;
+            sym[k] = i < n ? (C)((int)codes[i] - offset) : (C)0;
             if (i < n) mybits += len[sym[k]];
         }
     }
@@ -534,10 +540,11 @@ __global__ void __launch_bounds__(DEC_T) k_decode_resync(DecTables t, const uint
 }
 
 // Final pass: decode unit u from its true start into out[off[u]...].
+template <typename C>
 __global__ void __launch_bounds__(DEC_T) k_decode_write(DecTables t, const uint32_t *__restrict__ w32, uint64_t nwords,
                                                        uint64_t nbits, uint64_t nunits, const uint64_t *start,
                                                        const unsigned long long *off, uint64_t nout, int offset,
-                                                       uint16_t *out) {
+                                                       C *out) {
     __shared__ uint32_t slut[1 << LUT_BITS];
     __shared__ uint32_t sw[DEC_SEG];
     const uint64_t u0 = (uint64_t)blockIdx.x * DEC_T;
@@ -550,11 +557,18 @@ __global__ void __launch_bounds__(DEC_T) k_decode_write(DecTables t, const uint3
     uint32_t p = (uint32_t)(start[u] - g0);
     const uint32_t stop = (uint32_t)(lim - g0);
     uint64_t o = off[u];
+    if constexpr (sizeof(C) != 2) {  // wide codes: one store per symbol
+        while (p < stop && o < nout) {
+            int s = dec_sym(t, slut, sw, p);
+            if (s < 0) return;
+            out[o++] = (C)(s + offset);
+        }
+    } else {
     // 2-byte stores up to a 16-byte boundary, then 8 symbols per store
     while (p < stop && o < nout && (o & 7)) {
         int s = dec_sym(t, slut, sw, p);
         if (s < 0) return;
-        out[o++] = (uint16_t)(s + offset);
+        out[o++] = (C)(s + offset);
     }
     uint32_t pk[4];
     int k = 0;
@@ -565,15 +579,17 @@ __global__ void __launch_bounds__(DEC_T) k_decode_write(DecTables t, const uint3
         if (k & 1) pk[k >> 1] |= v << 16;
         else pk[k >> 1] = v;
         if (++k == 8) {
-            *reinterpret_cast<uint4 *>(out + o) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4 *>((uint16_t *)out + o) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
             o += 8;
             k = 0;
         }
     }
-    for (int i = 0; i < k; i++) out[o + i] = (uint16_t)(pk[i >> 1] >> ((i & 1) * 16));
+    for (int i = 0; i < k; i++) out[o + i] = (C)(uint16_t)(pk[i >> 1] >> ((i & 1) * 16));
+    }
 }
 
-__global__ void k_fill_u16(uint16_t *out, uint64_t n, uint16_t v) {
+template <typename C>
+__global__ void k_fill_u16(C *out, uint64_t n, C v) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         out[i] = v;
 }
@@ -591,28 +607,40 @@ uint64_t hist_subchunks(uint64_t n) { return ((n + HCHUNK - 1) / HCHUNK) * HWARP
 
 cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, int center, unsigned long long *hist,
                              unsigned long long *first, unsigned long long *zcount, cudaStream_t st) {
-    k_histogram<<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, center, hist, first, zcount);
+    k_histogram<uint16_t><<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, center, hist, first, zcount);
+    return cudaGetLastError();
+}
+cudaError_t launch_histogram(const uint32_t *codes, uint64_t n, int center, unsigned long long *hist,
+                             unsigned long long *first, unsigned long long *zcount, cudaStream_t st) {
+    k_histogram<uint32_t><<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, center, hist, first, zcount);
     return cudaGetLastError();
 }
 
 cudaError_t launch_count_zeros(const uint16_t *codes, uint64_t n, unsigned long long *zcount, cudaStream_t st) {
-    k_count_zeros<<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, zcount);
+    k_count_zeros<uint16_t><<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, zcount);
+    return cudaGetLastError();
+}
+cudaError_t launch_count_zeros(const uint32_t *codes, uint64_t n, unsigned long long *zcount, cudaStream_t st) {
+    k_count_zeros<uint32_t><<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, zcount);
     return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_compact_zeros(const uint16_t *codes, uint64_t n, const unsigned long long *zcount,
+template <typename T, typename C>
+cudaError_t launch_compact_zeros(const C *codes, uint64_t n, const unsigned long long *zcount,
                                  const unsigned long long *zoff, uint64_t *zpos, const T *scratch, T *vals,
                                  cudaStream_t st) {
-    k_compact_zeros<T><<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, zcount, zoff, zpos, scratch, vals);
+    k_compact_zeros<T, C><<<grid_for(n, HCHUNK), 1024, 0, st>>>(codes, n, zcount, zoff, zpos, scratch, vals);
     return cudaGetLastError();
 }
-template cudaError_t launch_compact_zeros<float>(const uint16_t *, uint64_t, const unsigned long long *,
-                                                 const unsigned long long *, uint64_t *, const float *, float *,
-                                                 cudaStream_t);
-template cudaError_t launch_compact_zeros<double>(const uint16_t *, uint64_t, const unsigned long long *,
-                                                  const unsigned long long *, uint64_t *, const double *, double *,
-                                                  cudaStream_t);
+#define FAZ_INST_COMPACT(T, C)                                                                               \
+    template cudaError_t launch_compact_zeros<T, C>(const C *, uint64_t, const unsigned long long *,       \
+                                                    const unsigned long long *, uint64_t *, const T *, T *, \
+                                                    cudaStream_t);
+FAZ_INST_COMPACT(float, uint16_t)
+FAZ_INST_COMPACT(double, uint16_t)
+FAZ_INST_COMPACT(float, uint32_t)
+FAZ_INST_COMPACT(double, uint32_t)
+#undef FAZ_INST_COMPACT
 
 uint64_t scan_temp_words(uint64_t n) { return (n + SCAN_B - 1) / SCAN_B + 1; }
 
@@ -628,22 +656,42 @@ cudaError_t launch_scan_u64(const unsigned long long *in, unsigned long long *ou
 
 uint64_t encode_chunks(uint64_t n) { return (n + ENC_CHUNK - 1) / ENC_CHUNK; }
 
-cudaError_t launch_encode_bits(const uint16_t *codes, uint64_t n, int offset, const uint8_t *len,
-                               unsigned long long *chunkbits, cudaStream_t st) {
-    k_encode_bits<<<grid_for(n, ENC_CHUNK), ENC_THREADS, 0, st>>>(codes, n, offset, len, chunkbits);
+template <typename C>
+cudaError_t encode_bits_impl(const C *codes, uint64_t n, int offset, const uint8_t *len,
+                             unsigned long long *chunkbits, cudaStream_t st) {
+    k_encode_bits<C><<<grid_for(n, ENC_CHUNK), ENC_THREADS, 0, st>>>(codes, n, offset, len, chunkbits);
     return cudaGetLastError();
 }
+cudaError_t launch_encode_bits(const uint16_t *codes, uint64_t n, int offset, const uint8_t *len,
+                               unsigned long long *chunkbits, cudaStream_t st) {
+    return encode_bits_impl(codes, n, offset, len, chunkbits, st);
+}
+cudaError_t launch_encode_bits(const uint32_t *codes, uint64_t n, int offset, const uint8_t *len,
+                               unsigned long long *chunkbits, cudaStream_t st) {
+    return encode_bits_impl(codes, n, offset, len, chunkbits, st);
+}
 
+template <typename C>
+cudaError_t encode_pack_impl(const C *codes, uint64_t n, int offset, const unsigned long long *code64,
+                             const unsigned long long *packed, const uint8_t *len, const unsigned long long *chunkoff,
+                             uint32_t *out, int maxlen, cudaStream_t st) {
+    int words = (int)(((uint64_t)ENC_CHUNK * (uint64_t)maxlen + 31) / 32 + 2);
+    size_t sm = (size_t)words * 4;
+    cudaError_t e = allow_dynamic_smem((const void *)k_encode_pack<C>);
+    if (e != cudaSuccess) return e;
+    k_encode_pack<C><<<grid_for(n, ENC_CHUNK), ENC_THREADS, sm, st>>>(codes, n, offset, code64, packed, len,
+                                                                       chunkoff, out, words);
+    return cudaGetLastError();
+}
 cudaError_t launch_encode_pack(const uint16_t *codes, uint64_t n, int offset, const unsigned long long *code64,
                                const unsigned long long *packed, const uint8_t *len,
                                const unsigned long long *chunkoff, uint32_t *out, int maxlen, cudaStream_t st) {
-    int words = (int)(((uint64_t)ENC_CHUNK * (uint64_t)maxlen + 31) / 32 + 2);
-    size_t sm = (size_t)words * 4;
-    cudaError_t e = allow_dynamic_smem((const void *)k_encode_pack);
-    if (e != cudaSuccess) return e;
-    k_encode_pack<<<grid_for(n, ENC_CHUNK), ENC_THREADS, sm, st>>>(codes, n, offset, code64, packed, len, chunkoff,
-                                                                    out, words);
-    return cudaGetLastError();
+    return encode_pack_impl(codes, n, offset, code64, packed, len, chunkoff, out, maxlen, st);
+}
+cudaError_t launch_encode_pack(const uint32_t *codes, uint64_t n, int offset, const unsigned long long *code64,
+                               const unsigned long long *packed, const uint8_t *len,
+                               const unsigned long long *chunkoff, uint32_t *out, int maxlen, cudaStream_t st) {
+    return encode_pack_impl(codes, n, offset, code64, packed, len, chunkoff, out, maxlen, st);
 }
 
 uint64_t decode_units(uint64_t nbits) { return (nbits + DEC_UNIT - 1) / DEC_UNIT; }
@@ -667,13 +715,24 @@ cudaError_t launch_decode_resync(const DecodeTablesDev &td, const uint32_t *w32,
     return cudaGetLastError();
 }
 
+template <typename C>
+cudaError_t decode_write_impl(const DecodeTablesDev &td, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
+                              uint64_t nunits, const uint64_t *start, const unsigned long long *off, uint64_t nout,
+                              int offset, C *out, cudaStream_t st) {
+    DecTables t{td.lut, td.left, td.right, td.sym, td.leaf};
+    k_decode_write<C><<<grid_for(nunits, DEC_T), DEC_T, 0, st>>>(t, w32, nwords, nbits, nunits, start, off, nout,
+                                                                  offset, out);
+    return cudaGetLastError();
+}
 cudaError_t launch_decode_write(const DecodeTablesDev &td, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
                                 uint64_t nunits, const uint64_t *start, const unsigned long long *off, uint64_t nout,
                                 int offset, uint16_t *out, cudaStream_t st) {
-    DecTables t{td.lut, td.left, td.right, td.sym, td.leaf};
-    k_decode_write<<<grid_for(nunits, DEC_T), DEC_T, 0, st>>>(t, w32, nwords, nbits, nunits, start, off, nout, offset,
-                                                               out);
-    return cudaGetLastError();
+    return decode_write_impl(td, w32, nwords, nbits, nunits, start, off, nout, offset, out, st);
+}
+cudaError_t launch_decode_write(const DecodeTablesDev &td, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
+                                uint64_t nunits, const uint64_t *start, const unsigned long long *off, uint64_t nout,
+                                int offset, uint32_t *out, cudaStream_t st) {
+    return decode_write_impl(td, w32, nwords, nbits, nunits, start, off, nout, offset, out, st);
 }
 
 __global__ void k_init_starts(uint64_t *start, uint64_t n) {
@@ -692,7 +751,14 @@ cudaError_t launch_fill_u16(uint16_t *out, uint64_t n, uint16_t v, cudaStream_t 
     unsigned g = grid_for(n, 1024);
     if (g > 4096) g = 4096;
     if (g == 0) g = 1;
-    k_fill_u16<<<g, 1024, 0, st>>>(out, n, v);
+    k_fill_u16<uint16_t><<<g, 1024, 0, st>>>(out, n, v);
+    return cudaGetLastError();
+}
+cudaError_t launch_fill_u16(uint32_t *out, uint64_t n, uint32_t v, cudaStream_t st) {
+    unsigned g = grid_for(n, 1024);
+    if (g > 4096) g = 4096;
+    if (g == 0) g = 1;
+    k_fill_u16<uint32_t><<<g, 1024, 0, st>>>(out, n, v);
     return cudaGetLastError();
 }
 

@@ -86,11 +86,16 @@ template <typename T, bool WIDE>
 int batch_occupancy(int threads, size_t smem);
 
 uint64_t hist_subchunks(uint64_t n);
+// Huffman stage kernels; the uint32_t overloads serve quantisers of more than
+// 65536 bins.
 cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, int center, unsigned long long *hist,
                              unsigned long long *first, unsigned long long *zcount, cudaStream_t st);
+cudaError_t launch_histogram(const uint32_t *codes, uint64_t n, int center, unsigned long long *hist,
+                             unsigned long long *first, unsigned long long *zcount, cudaStream_t st);
 cudaError_t launch_count_zeros(const uint16_t *codes, uint64_t n, unsigned long long *zcount, cudaStream_t st);
-template <typename T>
-cudaError_t launch_compact_zeros(const uint16_t *codes, uint64_t n, const unsigned long long *zcount,
+cudaError_t launch_count_zeros(const uint32_t *codes, uint64_t n, unsigned long long *zcount, cudaStream_t st);
+template <typename T, typename C>
+cudaError_t launch_compact_zeros(const C *codes, uint64_t n, const unsigned long long *zcount,
                                  const unsigned long long *zoff, uint64_t *zpos, const T *scratch, T *vals,
                                  cudaStream_t st);
 uint64_t scan_temp_words(uint64_t n);
@@ -99,7 +104,12 @@ cudaError_t launch_scan_u64(const unsigned long long *in, unsigned long long *ou
 uint64_t encode_chunks(uint64_t n);
 cudaError_t launch_encode_bits(const uint16_t *codes, uint64_t n, int offset, const uint8_t *len,
                                unsigned long long *chunkbits, cudaStream_t st);
+cudaError_t launch_encode_bits(const uint32_t *codes, uint64_t n, int offset, const uint8_t *len,
+                               unsigned long long *chunkbits, cudaStream_t st);
 cudaError_t launch_encode_pack(const uint16_t *codes, uint64_t n, int offset, const unsigned long long *code64,
+                               const unsigned long long *packed, const uint8_t *len,
+                               const unsigned long long *chunkoff, uint32_t *out, int maxlen, cudaStream_t st);
+cudaError_t launch_encode_pack(const uint32_t *codes, uint64_t n, int offset, const unsigned long long *code64,
                                const unsigned long long *packed, const uint8_t *len,
                                const unsigned long long *chunkoff, uint32_t *out, int maxlen, cudaStream_t st);
 
@@ -122,7 +132,11 @@ cudaError_t launch_decode_resync(const DecodeTablesDev &t, const uint32_t *w32, 
 cudaError_t launch_decode_write(const DecodeTablesDev &t, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
                                 uint64_t nunits, const uint64_t *start, const unsigned long long *off, uint64_t nout,
                                 int offset, uint16_t *out, cudaStream_t st);
+cudaError_t launch_decode_write(const DecodeTablesDev &t, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
+                                uint64_t nunits, const uint64_t *start, const unsigned long long *off, uint64_t nout,
+                                int offset, uint32_t *out, cudaStream_t st);
 cudaError_t launch_fill_u16(uint16_t *out, uint64_t n, uint16_t v, cudaStream_t st);
+cudaError_t launch_fill_u16(uint32_t *out, uint64_t n, uint32_t v, cudaStream_t st);
 cudaError_t launch_widen_counts(const unsigned int *cnt, unsigned long long *out, uint64_t n, cudaStream_t st);
 
 // ------------------------------------------------------------ Huffman host

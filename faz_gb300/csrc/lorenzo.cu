@@ -33,6 +33,7 @@ namespace {
 constexpr int kLorWarps = 8;     // blocks (warps) per CTA
 constexpr int kLorMaxBs = 8;     // largest block edge on the GPU path
 constexpr int kLorBatch = 8;     // tile loads in flight per lane
+constexpr int kLorMaxRadius = 65536;  // quantbinCnt up to 131072 (32-bit codes above 65536 bins)
 
 struct LorArgs {
     int64_t d1, d2, d3;   // field dims, slowest first
@@ -210,9 +211,9 @@ __device__ __forceinline__ void lor_st_release(unsigned *p, unsigned v) {
 // One block (bi, bj, bk), one warp: the (bs + 2)^3 tile with its two-deep
 // halo of reconstructed values, then the point diagonals i + j + k = s in
 // order, each point predicted from its reconstructed neighbours.
-template <typename T, bool DECOMP, int QM>
+template <typename T, bool DECOMP, int QM, typename C>
 __device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t bj, int64_t bk, T *t,
-                                          const T *__restrict__ X, T *__restrict__ R, uint16_t *__restrict__ codes,
+                                          const T *__restrict__ X, T *__restrict__ R, C *__restrict__ codes,
                                           T *__restrict__ scratch, const uint16_t *__restrict__ ind,
                                           const uint64_t *__restrict__ zpos, uint64_t nzp, const T *__restrict__ unpred) {
     const int lane = threadIdx.x & 31;
@@ -285,7 +286,7 @@ __device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t 
                 v = xs[(i * sy + j) * sz + k];
                 T uval;
                 const int code = quant_point<T, QM>(v, pred, a.q, uval);
-                codes[pos] = (uint16_t)code;
+                codes[pos] = (C)code;
                 if (code == 0) scratch[pos] = uval;
             } else {
                 v = recover_point<T, QM>(pred, (int)codes[pos], pos, a.q, zpos, nzp, unpred);
@@ -310,11 +311,11 @@ constexpr unsigned kLorWaitLimit = 1u << 22;  // polls (with back-off) of a neig
 // and every wait ends.  Each wait is bounded all the same (error flag, then
 // the block runs).  A finished block publishes done[b] = 1 with release
 // semantics after its reconstruction is written.
-template <typename T, bool DECOMP, int QM>
+template <typename T, bool DECOMP, int QM, typename C>
 __global__ void __launch_bounds__(kLorWarps * 32)
     k_lor_persist(LorArgs a, const uint32_t *__restrict__ order, uint32_t nblocks, unsigned *counter,
                   unsigned *done, int *err, const T *__restrict__ X, T *__restrict__ R,
-                  uint16_t *__restrict__ codes, T *__restrict__ scratch, const uint16_t *__restrict__ ind,
+                  C *__restrict__ codes, T *__restrict__ scratch, const uint16_t *__restrict__ ind,
                   const uint64_t *__restrict__ zpos, uint64_t nzp, const T *__restrict__ unpred) {
     extern __shared__ __align__(16) unsigned char lor_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(kLorWarps * 32)
         // every lane acquires the neighbours' completion itself
         for (int d = 0; d < 3; d++)
             if (deps[d]) (void)lor_ld_acquire(deps[d]);
-        lor_block<T, DECOMP, QM>(a, bi, bj, bk, t, X, R, codes, scratch, ind, zpos, nzp, unpred);
+        lor_block<T, DECOMP, QM, C>(a, bi, bj, bk, t, X, R, codes, scratch, ind, zpos, nzp, unpred);
         __threadfence();
         __syncwarp();
         if (lane == 0) lor_st_release(done + b, 1u);
@@ -379,16 +380,17 @@ LorArgs make_args(const uint64_t *dims, int bs, int pd, int lo, int lo2, double 
     return a;
 }
 
-template <typename T>
-void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, uint16_t *codes, T *scratch, const uint16_t *ind,
+// C: uint16_t codes, or uint32_t for more than 65536 quantisation bins
+template <typename T, typename C>
+void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, C *codes, T *scratch, const uint16_t *ind,
                    const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st, Counter &launches) {
     const bool straight = sizeof(T) == 4 && a.q.fast;
     const size_t smem = (size_t)kLorWarps *
                         (size_t)((a.bs + 2) * (a.bs + 2) * (a.bs + 2) + (decomp ? 0 : a.bs * a.bs * a.bs)) * sizeof(T);
-    void (*k)(LorArgs, const uint32_t *, uint32_t, unsigned *, unsigned *, int *, const T *, T *, uint16_t *, T *,
+    void (*k)(LorArgs, const uint32_t *, uint32_t, unsigned *, unsigned *, int *, const T *, T *, C *, T *,
               const uint16_t *, const uint64_t *, uint64_t, const T *);
-    if (!decomp) k = straight ? k_lor_persist<T, false, 1> : k_lor_persist<T, false, 0>;
-    else k = straight ? k_lor_persist<T, true, 1> : k_lor_persist<T, true, 0>;
+    if (!decomp) k = straight ? k_lor_persist<T, false, 1, C> : k_lor_persist<T, false, 0, C>;
+    else k = straight ? k_lor_persist<T, true, 1, C> : k_lor_persist<T, true, 0, C>;
     CK(allow_dynamic_smem((const void *)k));
     const uint64_t nb64 = (uint64_t)(a.nx * a.ny * a.nz);
     if (nb64 >= (1ull << 32)) throw Fail{FAZ_ERR_UNSUPPORTED, "too many Lorenzo blocks"};
@@ -553,7 +555,8 @@ void check_lorenzo3(const uint64_t *dims, int bs, int pd, int lo, int lo2, int r
     if (!lo && !lo2 && !reg) throw Fail{FAZ_ERR_ARG, "all Lorenzo and regression predictors are disabled"};
     if (bs < 1 || bs > kLorMaxBs) throw Fail{FAZ_ERR_UNSUPPORTED, "Lorenzo block size must be 1..8 on the GPU path"};
     if (pd < 1 || pd > 3) throw Fail{FAZ_ERR_ARG, "pred_dim must be 1..3"};
-    if (radius < 1 || radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt above 65536 is not implemented on the GPU path"};
+    if (radius < 1 || radius > kLorMaxRadius)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt above 131072 is not implemented on the GPU path"};
     for (int i = 0; i < 3; i++)
         if (dims[i] == 0) throw Fail{FAZ_ERR_ARG, "zero dimension"};
 }
@@ -573,7 +576,10 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     DevMem m(st);
     T *R = m.alloc<T>(n);
     T *scratch = m.alloc<T>(n);
-    uint16_t *codes = m.alloc<uint16_t>(n);
+    // 16-bit codes, or 32-bit ones for more than 65536 quantisation bins
+    const bool wide = radius > 32768;
+    uint16_t *codes16 = wide ? nullptr : m.alloc<uint16_t>(n);
+    uint32_t *codes32 = wide ? m.alloc<uint32_t>(n) : nullptr;
     uint16_t *ind = m.alloc<uint16_t>(nb);
     unsigned long long *vcount = nullptr;
     if (verify_fast_path()) {
@@ -611,13 +617,15 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
         }
         CK(cudaStreamSynchronize(st));  // host vectors leave scope
     }
-    run_wavefront<T>(a, false, dX, R, codes, scratch, ind, nullptr, 0, nullptr, st, launches);
+    if (wide) run_wavefront<T>(a, false, dX, R, codes32, scratch, ind, nullptr, 0, nullptr, st, launches);
+    else run_wavefront<T>(a, false, dX, R, codes16, scratch, ind, nullptr, 0, nullptr, st, launches);
     CK(cudaEventRecord(ev_pred.b, st));
     CK(cudaEventRecord(ev_huff.a, st));
     HuffEncoded hi, hc, hr;
     huffman_encode_device(ind, nb, 0, m, st, launches, hi, tm);
     if (reg_count) huffman_encode_device(drtypes, rtypes.size(), 32768, m, st, launches, hr, tm);
-    huffman_encode_device(codes, n, radius, m, st, launches, hc, tm);
+    if (wide) huffman_encode_device(codes32, n, radius, m, st, launches, hc, tm);
+    else huffman_encode_device(codes16, n, radius, m, st, launches, hc, tm);
     if (vcount) {
         unsigned long long vc = 0;
         CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
@@ -625,7 +633,8 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     }
     const uint64_t nunpred = hc.nzero;
     T *unp = m.alloc<T>(nunpred ? nunpred : 1);
-    if (nunpred) launches(launch_compact_zeros<T>(codes, n, hc.zc, hc.zoff, nullptr, scratch, unp, st));
+    if (nunpred && wide) launches(launch_compact_zeros<T>(codes32, n, hc.zc, hc.zoff, nullptr, scratch, unp, st));
+    if (nunpred && !wide) launches(launch_compact_zeros<T>(codes16, n, hc.zc, hc.zoff, nullptr, scratch, unp, st));
     CK(cudaEventRecord(ev_huff.b, st));
     // SZFastFrontend::save: params, precision, meanInfo<T>{false, 0}, reg_count,
     // indicator tree + bits; LinearQuantizer::save; then the code tree + bits
@@ -755,15 +764,24 @@ void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, 
     std::memcpy(&nunpred, p, 8);
     p += 8;
     if (!(eb > 0)) throw Fail{FAZ_ERR_FORMAT, "bad error bound"};
-    if (radius < 1 || radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt above 65536 is not implemented on the GPU path"};
+    if (radius < 1 || radius > kLorMaxRadius)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "quantbinCnt above 131072 is not implemented on the GPU path"};
     if ((size_t)(end - p) / sizeof(T) < nunpred) throw Fail{FAZ_ERR_FORMAT, "truncated unpredictable values"};
     T *dunp = m.alloc<T>(nunpred ? nunpred : 1);
     if (nunpred) CK(cudaMemcpyAsync(dunp, p, nunpred * sizeof(T), cudaMemcpyHostToDevice, st));
     p += nunpred * sizeof(T);
-    uint16_t *codes = m.alloc<uint16_t>(n);
-    huffman_decode_device(p, end, n, codes, m, st, launches);
+    const bool wide = radius > 32768;  // 32-bit codes for more than 65536 bins
+    uint16_t *codes16 = wide ? nullptr : m.alloc<uint16_t>(n);
+    uint32_t *codes32 = wide ? m.alloc<uint32_t>(n) : nullptr;
     uint64_t *zpos = nullptr;
-    const uint64_t nz = zero_positions(codes, n, m, st, launches, zpos);
+    uint64_t nz;
+    if (wide) {
+        huffman_decode_device(p, end, n, codes32, m, st, launches);
+        nz = zero_positions(codes32, n, m, st, launches, zpos);
+    } else {
+        huffman_decode_device(p, end, n, codes16, m, st, launches);
+        nz = zero_positions(codes16, n, m, st, launches, zpos);
+    }
     if (nz != nunpred) throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
     CK(cudaEventRecord(ev_dec.b, st));
     LorArgs a = make_args<T>(dims, bs, pd, 1, 1, eb, radius);
@@ -775,7 +793,8 @@ void lorenzo3_decompress(const uint8_t *pl, size_t psize, const uint64_t *dims, 
         a.q.verify = vcount;
     }
     CK(cudaEventRecord(ev_pred.a, st));
-    run_wavefront<T>(a, true, nullptr, dOut, codes, nullptr, ind, zpos, nz, dunp, st, launches);
+    if (wide) run_wavefront<T>(a, true, nullptr, dOut, codes32, nullptr, ind, zpos, nz, dunp, st, launches);
+    else run_wavefront<T>(a, true, nullptr, dOut, codes16, nullptr, ind, zpos, nz, dunp, st, launches);
     CK(cudaEventRecord(ev_pred.b, st));
     CK(cudaStreamSynchronize(st));
     if (vcount) {

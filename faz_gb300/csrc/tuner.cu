@@ -586,10 +586,7 @@ void lorenzo_followup(faz_config &c, const T *dX, const Sample<T> &smp, double b
     lc.blockSize = 5;
     set_dims_defaults(lc);  // setDims(sample dims)
     if (N == 3) {
-        lc.quantbinCnt = quant_intervals<T>(dX, dims, eb, st, launches);
-        if (lc.quantbinCnt > 65536)
-            throw Fail{FAZ_ERR_UNSUPPORTED,
-                       "Lorenzo with more than 65536 quantisation bins is not implemented on the GPU path"};
+        lc.quantbinCnt = quant_intervals<T>(dX, dims, eb, st, launches);  // up to 131072
         lc.pred_dim = 2;
         {
             std::vector<uint8_t> pl;

@@ -104,6 +104,13 @@ def cases():
     out.append(("sz3_lorenzo_abs", sum2d((56, 60, 64), 0.001, seed=53), ["-M", "ABS", "0.02"], None))
     out.append(("sz3_lorenzo_f64_16384", sum2d((56, 60, 64), 1e-8, seed=54, dtype=np.float64),
                 ["-M", "REL", "5e-7"], None))
+    # rough fields at a tight bound: Lorenzo with the interval estimate's
+    # 131072 quantisation bins (codes wider than 16 bits)
+    out.append(("sz3_lorenzo_f64_131072", spectral_field((56, 60, 64), slope=-1.5, noise=0.0, seed=55,
+                                                         dtype=np.float64), ["-M", "REL", "1e-6"], None))
+    # (the float32 version of this field aborts the reference tool in its
+    # Huffman encoder's fixed-size buffer; the GPU tests compare it with the
+    # oracle instead)
     # QoZ tuner (-q): per-level predictors and alpha/beta from trial compressions
     out.append(("qoz_2blk_1e3", spectral_field((50, 120, 170), slope=-3.0, aniso=(1, 2, 2), seed=61),
                 ["-M", "REL", "1e-3", "-q"], None))
@@ -115,6 +122,9 @@ def cases():
     # explicit Lorenzo / regression fast frontend
     lor = {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {}}
     out.append(("lorreg_default", spectral_field((40, 44, 52), slope=-3.0, seed=55), ["-M", "REL", "1e-3"], lor))
+    out.append(("lorreg_qb131072", spectral_field((40, 44, 52), slope=-1.5, seed=58), ["-M", "REL", "1e-6"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
+                 "AlgoSettings": {"QuantizationBinTotal": "131072"}}))
     out.append(("lorreg_l2_bs4", spectral_field((37, 41, 29), slope=-2.5, seed=56), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
                  "AlgoSettings": {"Lorenzo2ndOrder": "YES", "BlockSize": "4"}}))

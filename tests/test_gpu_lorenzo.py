@@ -31,10 +31,9 @@ def _rc(name):
 
 # default configuration, no QoZ tuning (1-D to 3-D fields)
 SZ3_CASES = [c["name"] for c in golden_manifest()
-             if c["ini"] is None and "-q" not in c["flags"] and len(c["dims"]) <= 3 and _rc(c["name"]).quantbinCnt <= 65536]
+             if c["ini"] is None and "-q" not in c["flags"] and len(c["dims"]) <= 3]
 # Lorenzo / regression streams
-LOR_DEC_CASES = [c["name"] for c in golden_manifest()
-                 if _rc(c["name"]).cmprAlgo == ALGO_LORENZO_REG and _rc(c["name"]).quantbinCnt <= 65536]
+LOR_DEC_CASES = [c["name"] for c in golden_manifest() if _rc(c["name"]).cmprAlgo == ALGO_LORENZO_REG]
 # explicit ALGO_LORENZO_REG runs of the reference (INI), compressed on the GPU
 LOR_INI_CASES = [c["name"] for c in golden_manifest()
                  if c["ini"] is not None and _rc(c["name"]).cmprAlgo == ALGO_LORENZO_REG]
@@ -129,7 +128,29 @@ LOR_CASES = [
     ((30, 33, 35), dict(rel=1e-5, reg=1), np.float64),
     ((21, 22, 23), dict(rel=1e-2, reg=1, lo=0), np.float32),
     ((64, 64, 64), dict(rel=1e-4, reg=1, lo2=1, pd=2), np.float32),
+    # more than 65536 quantisation bins: 32-bit codes
+    ((40, 44, 52), dict(rel=1e-7, qbins=131072), np.float32),
+    ((30, 33, 35), dict(rel=1e-7, qbins=131072, lo2=1, reg=1), np.float64),
 ]
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_gpu_default_config_with_131072_bins(dtype):
+    """A rough field at relative bound 1e-6: the default configuration's tuner
+    chooses Lorenzo and its interval estimate asks for 131072 bins (the
+    reference tool aborts on the float32 field; the oracle is the check)."""
+    dims = (56, 60, 64)
+    x = spectral_field(dims, slope=-1.5, noise=0.0, seed=56, dtype=dtype)
+    conf = F.Config(*dims)
+    conf.errorBoundMode, conf.relErrorBound = F.EB_REL, 1e-6
+    stream = F.SZ_compress(conf, x)
+    assert O.read_stream(stream)[0].quantbinCnt == 131072
+    ref, _ = O.compress(conf, x)
+    _same(stream, ref, np.dtype(dtype).itemsize)
+    dec, c2 = F.SZ_decompress(None, stream, dtype=dtype)
+    ref_dec, _ = O.decompress(ref, dtype=dtype)
+    assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
 
 
 @pytest.mark.parametrize("dims,kw,dtype", LOR_CASES)
