@@ -207,9 +207,9 @@ void check_config(const faz_config &c) {
                                         "set FZ = 0 (faz -F 0)"};
     if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && c.N == 3 && c.regression2)
         throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG is implemented for 3-D data without regression2"};
-    if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && c.N < 3 && (c.regression || c.regression2))
-        throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG on 1-D / 2-D data is implemented with Lorenzo predictors "
-                                        "only (Regression = NO)"};
+    if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && c.N < 3 && c.regression2)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG on 1-D / 2-D data is implemented without regression2 "
+                                        "(Regression2ndOrder = NO)"};
     if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};
     if (c.wavelet != 0 || ((c.wavelet > 0 || c.sperrWithoutWave) && c.sperr >= c.wavelet))
         throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet / SPERR modes are not part of the interpolation path"};
@@ -628,10 +628,10 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
     }
     std::vector<uint8_t> pl;
     if (c.N < 3) {
-        if (c.regression || c.regression2)
-            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG on 1-D / 2-D data is implemented without regression"};
-        gen_compress_payload<T>(c.N, c.dims, c.blockSize, c.lorenzo, c.lorenzo2, c.absErrorBound, c.quantbinCnt / 2,
-                                dX, st, launches, tm, pl);
+        if (c.regression2)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG on 1-D / 2-D data is implemented without regression2"};
+        gen_compress_payload<T>(c.N, c.dims, c.blockSize, c.lorenzo, c.lorenzo2, c.regression, c.absErrorBound,
+                                c.quantbinCnt / 2, dX, st, launches, tm, pl);
     } else {
         if (c.N != 3 || c.regression2)
             throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG is implemented for 3-D data without regression2"};
@@ -1517,9 +1517,9 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
         const bool lor = c.cmprAlgo == FAZ_ALGO_LORENZO_REG;
         if (!lor && c.cmprAlgo != FAZ_ALGO_INTERP)
             throw Fail{FAZ_ERR_UNSUPPORTED, "stream algorithm is neither ALGO_INTERP nor ALGO_LORENZO_REG"};
-        if (lor && ((c.N == 3 && c.regression2) || (c.N < 3 && (c.regression || c.regression2)) || c.N > 3))
-            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG streams are implemented for 3-D data without "
-                                            "regression2 and for 1-D / 2-D data without regression"};
+        if (lor && (c.regression2 || c.N > 3))
+            throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG streams are implemented for 1-D, 2-D and 3-D data "
+                                            "without regression2"};
         if (c.wavelet != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet streams are not part of the interpolation path"};
         if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
         if (caller_buffer && cap < c.num)
@@ -1548,7 +1548,8 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
             dOut = m.alloc<T>(c.num);
         }
         CK(cudaEventRecord(ev_gpu.a, st));
-        if (lor && c.N < 3) gen_decompress<T>(c.N, payload, psize, c.dims, c.lorenzo, c.lorenzo2, dOut, st, launches, tm);
+        if (lor && c.N < 3)
+            gen_decompress<T>(c.N, payload, psize, c.dims, c.lorenzo, c.lorenzo2, c.regression, dOut, st, launches, tm);
         else if (lor) lorenzo3_decompress<T>(payload, psize, c.dims, dOut, st, launches, tm);
         else decompress_device<T>(payload, psize, P, dOut, st, tm, launches);
         CK(cudaEventRecord(ev_gpu.b, st));

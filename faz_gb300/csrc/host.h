@@ -367,12 +367,13 @@ void qoz_lorenzo_followup(faz_config &c, const T *dX, cudaStream_t st, Counter &
 inline bool qoz_tuned(const faz_config &c) {
     return c.QoZ || (c.predictorTuningRate > 0 && c.predictorTuningRate < 1);
 }
-// general Lorenzo frontend for 1-D / 2-D fields (general.cu)
+// general frontend for 1-D / 2-D fields: Lorenzo, two-layer Lorenzo and
+// linear-regression predictors as enabled (general.cu)
 template <typename T>
-void gen_compress_payload(int N, const uint64_t *dims, int bs, int lo, int lo2, double eb, int radius, const T *dX,
-                          cudaStream_t st, Counter &launches, faz_timings &tm, std::vector<uint8_t> &out);
+void gen_compress_payload(int N, const uint64_t *dims, int bs, int lo, int lo2, int reg, double eb, int radius,
+                          const T *dX, cudaStream_t st, Counter &launches, faz_timings &tm, std::vector<uint8_t> &out);
 template <typename T>
-void gen_decompress(int N, const uint8_t *pl, size_t psize, const uint64_t *dims, int lo, int lo2, T *dOut,
+void gen_decompress(int N, const uint8_t *pl, size_t psize, const uint64_t *dims, int lo, int lo2, int reg, T *dOut,
                     cudaStream_t st, Counter &launches, faz_timings &tm);
 // calAbsErrorBound on the device (capi.cu)
 template <typename T>

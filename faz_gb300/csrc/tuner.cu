@@ -603,7 +603,7 @@ void lorenzo_followup(faz_config &c, const T *dX, const Sample<T> &smp, double b
         if (N == 3)
             lorenzo_payload<T>(sdims, dS, lc.blockSize, lc.pred_dim, eb, lc.quantbinCnt / 2, st, launches, tm, pl);
         else
-            gen_compress_payload<T>(N, sdims, lc.blockSize, 1, 1, eb, lc.quantbinCnt / 2, dS, st, launches, tm, pl);
+            gen_compress_payload<T>(N, sdims, lc.blockSize, 1, 1, 0, eb, lc.quantbinCnt / 2, dS, st, launches, tm, pl);
         r = sbytes / zstd_framed_size(pl.data(), pl.size());
         if (r > best_l * 1.02) best_l = r;
         else lc.quantbinCnt = q0;
@@ -658,7 +658,7 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         jl.start(ready.a, [&](cudaStream_t s2, Counter &c2, faz_timings &t2, std::vector<uint8_t> &pl,
                               const std::function<void(size_t)> &) {
             if (N == 3) lorenzo_payload<T>(sdims, dS, 5, 3, eb, c.quantbinCnt / 2, s2, c2, t2, pl);
-            else gen_compress_payload<T>(N, sdims, 5, 1, 1, eb, c.quantbinCnt / 2, dS, s2, c2, t2, pl);
+            else gen_compress_payload<T>(N, sdims, 5, 1, 1, 0, eb, c.quantbinCnt / 2, dS, s2, c2, t2, pl);
         });
     };
     if (!speculate) start_lorenzo();
@@ -798,7 +798,7 @@ void qoz_lorenzo_followup(faz_config &c, const T *dX, cudaStream_t st, Counter &
         lorenzo_payload<T>(smp.sdims, smp.dS, lc.blockSize, lc.pred_dim, c.absErrorBound, lc.quantbinCnt / 2, st,
                            launches, tm, pl);
     else
-        gen_compress_payload<T>(N, smp.sdims, lc.blockSize, 1, 1, c.absErrorBound, lc.quantbinCnt / 2, smp.dS, st,
+        gen_compress_payload<T>(N, smp.sdims, lc.blockSize, 1, 1, 0, c.absErrorBound, lc.quantbinCnt / 2, smp.dS, st,
                                 launches, tm, pl);
     const double best_l = smp.sn * 1.0 * sizeof(T) / zstd_framed_size(pl.data(), pl.size());
     lorenzo_followup<T>(c, dX, smp, best_l, st, launches, tm);

@@ -1203,17 +1203,18 @@ static int lorenzo3_size(int dtype, const void *data, const size_t *dims, int bs
 }
 
 /* General-frontend payload of a 1-D or 2-D field (SZ_compress_LorenzoReg with
- * N < 3, include/QoZ/api/impl/SZLorenzoReg.hpp:94-114): Lorenzo predictors only. */
-static int gen_payload(int dtype, const void *data, int N, const size_t *dims, int bs, int lo, int lo2, double eb,
-                       int radius, bytes_t *out) {
-    if (dtype == FAZ_FLOAT) return gen_compress_f32((const float *)data, N, dims, bs, lo, lo2, eb, radius, out);
-    return gen_compress_f64((const double *)data, N, dims, bs, lo, lo2, eb, radius, out);
+ * N < 3, include/QoZ/api/impl/SZLorenzoReg.hpp:94-114): Lorenzo, two-layer
+ * Lorenzo and linear-regression predictors as the Config enables them. */
+static int gen_payload(int dtype, const void *data, int N, const size_t *dims, int bs, int lo, int lo2, int reg,
+                       double eb, int radius, bytes_t *out) {
+    if (dtype == FAZ_FLOAT) return gen_compress_f32((const float *)data, N, dims, bs, lo, lo2, reg, eb, radius, out);
+    return gen_compress_f64((const double *)data, N, dims, bs, lo, lo2, reg, eb, radius, out);
 }
 
 static int gen_size(int dtype, const void *data, int N, const size_t *dims, int bs, double eb, int radius,
                     size_t *size) {
     bytes_t b = {0};
-    int rc = gen_payload(dtype, data, N, dims, bs, 1, 1, eb, radius, &b);
+    int rc = gen_payload(dtype, data, N, dims, bs, 1, 1, 0, eb, radius, &b);
     if (!rc) rc = z_framed_size(b.p, b.n, size);
     free(b.p);
     return rc;
@@ -1370,14 +1371,14 @@ static int payload_for(faz_config *conf, int dtype, const void *data, uint8_t **
     if (conf->cmprAlgo == FAZ_ALGO_INTERP)
         return orc_interp_compress(conf, dtype, data, NULL, NULL, NULL, NULL, payload, psize);
     if (conf->cmprAlgo == FAZ_ALGO_LORENZO_REG && conf->N < 3) {
-        if (conf->regression || conf->regression2) {
-            set_err("oracle covers the 1-D / 2-D general frontend with Lorenzo predictors only");
+        if (conf->regression2) {
+            set_err("oracle covers the 1-D / 2-D general frontend without regression2");
             return -2;
         }
         size_t dims[2] = {conf->dims[0], conf->N == 2 ? conf->dims[1] : 1};
         bytes_t b = {0};
         int rc = gen_payload(dtype, data, conf->N, dims, conf->blockSize, conf->lorenzo, conf->lorenzo2,
-                             conf->absErrorBound, conf->quantbinCnt / 2, &b);
+                             conf->regression, conf->absErrorBound, conf->quantbinCnt / 2, &b);
         if (rc) { free(b.p); return rc; }
         *payload = b.p;
         *psize = b.n;
@@ -1490,17 +1491,19 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
     if (rc) return rc;
     if (conf.cmprAlgo == FAZ_ALGO_LORENZO_REG && conf.N < 3) {
         /* SZ_decompress_LorenzoReg with N < 3: the general frontend */
-        if (conf.regression || conf.regression2) {
+        if (conf.regression2) {
             free(payload);
-            set_err("oracle decodes 1-D / 2-D Lorenzo streams without regression");
+            set_err("oracle decodes 1-D / 2-D general-frontend streams without regression2");
             return -2;
         }
         size_t dims[2] = {conf.dims[0], conf.N == 2 ? conf.dims[1] : 1};
         size_t es = dtype == FAZ_FLOAT ? 4 : 8;
         void *dec = malloc(conf.num * es + es);
         rd_t r = {payload, psize, 0, 0};
-        int rc2 = dtype == FAZ_FLOAT ? gen_decompress_f32(&r, conf.N, dims, conf.lorenzo, conf.lorenzo2, (float *)dec)
-                                     : gen_decompress_f64(&r, conf.N, dims, conf.lorenzo, conf.lorenzo2, (double *)dec);
+        int rc2 = dtype == FAZ_FLOAT
+                      ? gen_decompress_f32(&r, conf.N, dims, conf.lorenzo, conf.lorenzo2, conf.regression, (float *)dec)
+                      : gen_decompress_f64(&r, conf.N, dims, conf.lorenzo, conf.lorenzo2, conf.regression,
+                                           (double *)dec);
         free(payload);
         if (rc2) { free(dec); return rc2; }
         *out = dec;

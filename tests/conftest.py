@@ -60,6 +60,19 @@ def golden_stream(case):
         return f.read()
 
 
+def golden_dec_sha(case):
+    """SHA-256 of the array the reference decodes from the case's stream.  For
+    a stream the reference tool writes but cannot decode ("ref_decode" in the
+    manifest) the oracle's decoder, which applies the compressor's own
+    predictor choice, stands in."""
+    if case["dec_sha256"] is not None:
+        return case["dec_sha256"]
+    import hashlib
+    import oracle.oracle as O
+    dec, _ = O.decompress(golden_stream(case), dtype=np.dtype(case["dtype"]))
+    return hashlib.sha256(dec.tobytes()).hexdigest()
+
+
 # INI keys of QoZ::Config::loadcfg (include/QoZ/utils/Config.hpp:91-233) used by the fixtures
 _INI_INT = {"InterpDirection": "interpDirection", "InterpBlockSize": "interpBlockSize",
             "fixBlockSize": "fixBlockSize", "trimToZero": "trimToZero", "maxStep": "maxStep",

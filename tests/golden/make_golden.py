@@ -154,6 +154,29 @@ def cases():
     out.append(("lor1d_l2", random_walk((3001,), 79), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
                  "AlgoSettings": {"Lorenzo2ndOrder": "YES", "Regression": "NO"}}))
+    # explicit ALGO_LORENZO_REG on 1-D / 2-D data with the linear-regression
+    # predictor (the default Config: Lorenzo + regression, composed)
+    lreg = {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {}}
+    out.append(("reg2d_default", spectral_field((97, 131), slope=-3.5, noise=0.1, seed=86), ["-M", "REL", "1e-3"],
+                lreg))
+    out.append(("reg2d_l1l2reg_bs8", spectral_field((70, 45), slope=-3.0, seed=87), ["-M", "ABS", "0.02"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
+                 "AlgoSettings": {"Lorenzo2ndOrder": "YES", "BlockSize": "8"}}))
+    out.append(("reg2d_l2reg", spectral_field((60, 77), slope=-4.0, aniso=(1, 3), noise=0.03, seed=88),
+                ["-M", "REL", "1e-2"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
+                 "AlgoSettings": {"Lorenzo": "NO", "Lorenzo2ndOrder": "YES"}}))
+    out.append(("reg2d_only_f64", spectral_field((49, 65), slope=-3.0, seed=89, dtype=np.float64),
+                ["-M", "REL", "1e-4"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {"Lorenzo": "NO"}}))
+    out.append(("reg2d_f64_1e7", spectral_field((81, 66), slope=-2.0, noise=0.01, seed=90, dtype=np.float64),
+                ["-M", "REL", "1e-7"], lreg))
+    out.append(("reg1d_default", spectral_field((20000,), slope=-3.5, seed=91), ["-M", "REL", "1e-3"], lreg))
+    out.append(("reg1d_thin", spectral_field((3841,), slope=-4.0, seed=92), ["-M", "REL", "1e-4"], lreg))
+    out.append(("reg1d_only_f64_bs64", spectral_field((4033,), slope=-3.0, seed=93, dtype=np.float64),
+                ["-M", "REL", "1e-5"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
+                 "AlgoSettings": {"Lorenzo": "NO", "BlockSize": "64"}}))
     # rate-driven tuning without -q (Tuning's QoZ branch from the INI's rates;
     # the first is the learned tuner's labelling INI, whose Lorenzo candidate
     # is dropped above a relative bound of 1e-3)
@@ -260,6 +283,13 @@ def sum2d(shape, noise, seed, dtype=np.float32):
 
 # OpenMP thread count of the reference run (the stream's slab count)
 OMP_THREADS = {"omp_interp_3": 3, "omp_default_4": 4, "omp_abs2d_5": 5}
+# Cases whose stream the reference tool writes but cannot decode.  reg1d_thin:
+# the 1-D field's last block holds one point, the composed predictor picks
+# regression for it, regression refuses a one-point block and the frontend
+# falls back to Lorenzo without recording a selection; the decoder still reads
+# one selection per block, past the end of the decoded selections
+# (ComposedPredictor.hpp:65-68, SZGeneralFrontend.hpp:96-100), and crashes.
+REF_DECODE_FAILS = {"reg1d_thin"}
 
 
 def write_ini(path, d):
@@ -310,15 +340,22 @@ def main(only=None):
             subprocess.check_call(cmd, cwd=td, stdout=subprocess.DEVNULL, env=env)
             dcmd = [FAZ, dt, "-z", os.path.join(HERE, name + ".faz"), "-o", os.path.join(HERE, name + ".dec")] + \
                 cli_dims + ["-M", "ABS", "1"]
-            subprocess.check_call(dcmd, cwd=td, stdout=subprocess.DEVNULL)
+            rc = subprocess.call(dcmd, cwd=td, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            if rc != 0 and name not in REF_DECODE_FAILS:
+                raise subprocess.CalledProcessError(rc, dcmd)
+            if rc == 0 and name in REF_DECODE_FAILS:
+                raise RuntimeError(name + ": the reference decoded a stream it is listed as failing on")
         decp = os.path.join(HERE, name + ".dec")
         entry = {"name": name, "dtype": str(arr.dtype), "dims": dims, "flags": flags, "ini": ini,
                  "sha256": {ext: sha(os.path.join(HERE, name + ext)) for ext in (".in", ".faz")},
-                 "dec_sha256": sha(decp)}
+                 "dec_sha256": None if name in REF_DECODE_FAILS else sha(decp)}
+        if name in REF_DECODE_FAILS:
+            entry["ref_decode"] = "the reference tool's decoder exits with signal %d on this stream" % -rc
         if name in OMP_THREADS:
             entry["omp_threads"] = OMP_THREADS[name]
         manifest.append(entry)
-        os.remove(decp)
+        if os.path.exists(decp):
+            os.remove(decp)
         print(name, os.path.getsize(os.path.join(HERE, name + ".faz")))
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "reference_tool": "oracle/_ref/faz (zstd 1.4.5)",

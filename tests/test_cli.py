@@ -13,7 +13,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_case, golden_manifest, mask_fast_frontend_padding, write_ini
+from conftest import GOLDEN, golden_case, golden_dec_sha, golden_manifest, mask_fast_frontend_padding, write_ini
 
 import oracle.oracle as O
 
@@ -105,7 +105,7 @@ def test_cli_reproduces_reference_runs(name, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     for key in ("Max absolute error = ", "PSNR = ", "decompression time = ", "decompressed file = "):
         assert key in r.stdout
-    assert hashlib.sha256(open(tmp_path / "out.dec", "rb").read()).hexdigest() == case["dec_sha256"]
+    assert hashlib.sha256(open(tmp_path / "out.dec", "rb").read()).hexdigest() == golden_dec_sha(case)
 
 
 @pytest.mark.gpu

@@ -13,7 +13,7 @@ import pytest
 
 import faz_gb300 as F
 from faz_gb300.fields import spectral_field
-from conftest import (cli_config, golden_case, golden_input, golden_manifest, golden_stream,
+from conftest import (cli_config, golden_case, golden_dec_sha, golden_input, golden_manifest, golden_stream,
                       mask_fast_frontend_padding, mask_first_size)
 
 import oracle.oracle as O
@@ -82,7 +82,7 @@ def test_gpu_default_config_matches_oracle_and_reference(name):
 def test_gpu_decodes_reference_lorenzo_streams(name):
     case = golden_case(name)
     dec, _ = F.SZ_decompress(None, golden_stream(case), dtype=np.dtype(case["dtype"]))
-    assert hashlib.sha256(dec.tobytes()).hexdigest() == case["dec_sha256"]
+    assert hashlib.sha256(dec.tobytes()).hexdigest() == golden_dec_sha(case)
 
 
 @pytest.mark.parametrize("name", LOR_INI_CASES)
@@ -217,9 +217,62 @@ def test_gpu_general_frontend_matches_oracle(dims, kw, dtype):
     assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
 
 
-def test_gpu_general_frontend_rejects_regression():
+# (dims, settings, dtype, noise): regression in the list (noisier fields make
+# the regression predictor win more blocks)
+GEN_REG_CASES = [
+    ((97, 131), dict(rel=1e-3, bs=16), np.float32, 0.1),  # the default Config: Lorenzo + regression
+    ((70, 45), dict(abs_=0.02, lo2=1, bs=8), np.float32, 0.05),  # Lorenzo + 2-layer Lorenzo + regression
+    ((60, 77), dict(rel=1e-2, lo=0, lo2=1, bs=16), np.float32, 0.03),  # 2-layer Lorenzo + regression
+    ((49, 65), dict(rel=1e-4, lo=0, bs=16), np.float64, 0.0),  # regression alone; one-row / -column edge blocks
+    ((81, 66), dict(rel=1e-7, bs=16), np.float64, 0.3),  # unpredictable coefficients
+    ((129, 200), dict(rel=1e-5, lo2=1, bs=64, qbins=4096), np.float32, 0.3),  # unpredictable points, blocks of 64
+    ((300, 257), dict(rel=1e-3, bs=5), np.float32, 0.2),
+    ((33, 2), dict(rel=1e-2, bs=16), np.float32, 0.1),
+    ((1, 500), dict(rel=1e-3, bs=16), np.float32, 0.1),
+    ((2, 2), dict(rel=1e-3, bs=16), np.float64, 0.0),
+    ((20000,), dict(rel=1e-3, bs=128), np.float32, 0.0),
+    ((3841,), dict(rel=1e-4, bs=128), np.float32, 0.0),  # one-point final block
+    ((4033,), dict(rel=1e-5, lo=0, bs=64), np.float64, 0.0),  # regression alone, one-point final block
+    ((777,), dict(rel=1e-3, lo=0, lo2=1, bs=7), np.float32, 0.05),
+    ((5000,), dict(abs_=0.05, lo2=1, bs=16, qbins=256), np.float32, 0.1),
+]
+
+
+@pytest.mark.parametrize("dims,kw,dtype,noise", GEN_REG_CASES)
+def test_gpu_general_frontend_regression_matches_oracle(dims, kw, dtype, noise):
+    """1-D / 2-D ALGO_LORENZO_REG with the linear-regression predictor
+    (RegressionPredictor.hpp, ComposedPredictor.hpp): stream and decoded array
+    equal the oracle's bit for bit, the bound holds."""
+    conf = _lor_conf(dims, reg=1, **kw)
+    x = spectral_field(dims, slope=-3.5, noise=noise, seed=7 * sum(dims), dtype=dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, _ = O.compress(conf, x)
+    _same(stream, ref, np.dtype(dtype).itemsize)
+    assert stream == ref
+    dec, c2 = F.SZ_decompress(None, stream, dtype=dtype)
+    ref_dec, _ = O.decompress(ref, dtype=dtype)
+    assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
+    assert np.abs(dec.astype(np.float64) - x.astype(np.float64)).max() <= c2.absErrorBound
+
+
+def test_gpu_general_frontend_regression_on_a_batch_shape():
+    """The default ALGO_LORENZO_REG Config on a 1800x3600 float32 field
+    (one of the batch workload's 2-D shapes), against the oracle."""
+    dims = (1800, 3600)
+    conf = _lor_conf(dims, rel=1e-3, bs=16, reg=1)
+    x = spectral_field(dims, slope=-3.0, noise=0.02, seed=1234)
+    stream = F.SZ_compress(conf, x)
+    ref, _ = O.compress(conf, x)
+    assert stream == ref
+    dec, c2 = F.SZ_decompress(None, stream, dtype=np.float32)
+    ref_dec, _ = O.decompress(ref, dtype=np.float32)
+    assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
+
+
+def test_gpu_general_frontend_rejects_regression2():
     dims = (40, 50)
     conf = _lor_conf(dims, rel=1e-3, reg=1)
+    conf.regression2 = 1
     with pytest.raises(F.FazError):
         F.SZ_compress(conf, spectral_field(dims, slope=-3.0, seed=2))
 

@@ -47,9 +47,10 @@ def _same_stream(ours, ref, zstd_lib, itemsize=4):
     c1, p1 = O.read_stream(ours)
     c2, p2 = O.read_stream(ref)
     assert c1.cmprAlgo == c2.cmprAlgo
-    if c1.cmprAlgo == ALGO_LORENZO_REG:
-        # the reference writes uninitialised struct padding into these
-        # payloads, so their zstd frames differ; payload and trailer must not
+    if c1.cmprAlgo == ALGO_LORENZO_REG and c1.N == 3:
+        # the reference writes uninitialised struct padding into the 3-D fast
+        # frontend's payloads, so their zstd frames differ; payload and
+        # trailer must not
         assert mask_fast_frontend_padding(p1, itemsize) == mask_fast_frontend_padding(p2, itemsize)
         n1 = int.from_bytes(ours[-4:], "little", signed=True)
         n2 = int.from_bytes(ref[-4:], "little", signed=True)
@@ -100,12 +101,60 @@ def test_oracle_payload_matches_tuned_reference(name, zstd_lib):
 
 @pytest.mark.parametrize("name", ALL_CASES)
 def test_oracle_decompress_matches_reference(name):
+    """The reference's decoded array, bit for bit.  Where the reference tool
+    cannot decode its own stream (reg1d_thin: its decoder reads a selection
+    past the end of the list for the one-point final block that fell back to
+    the one-layer Lorenzo predictor), the oracle's decode must equal the
+    reconstruction the compressor made, which the error bound and the
+    re-compression below pin."""
     case = golden_case(name)
     dec, conf = O.decompress(golden_stream(case), dtype=np.dtype(case["dtype"]))
-    assert hashlib.sha256(dec.tobytes()).hexdigest() == case["dec_sha256"]
     x = golden_input(case)
+    if case["dec_sha256"] is not None:
+        assert hashlib.sha256(dec.tobytes()).hexdigest() == case["dec_sha256"]
+    else:
+        assert "ref_decode" in case
     err = np.abs(dec.astype(np.float64) - x.astype(np.float64)).max()
     assert err <= conf.absErrorBound
+
+
+def test_oracle_one_point_final_block_falls_back():
+    """reg1d_thin (3841 points, blocks of 128): the composed predictor
+    (Lorenzo, regression) picks regression for the one-point final block,
+    regression refuses it (RegressionPredictor.hpp:48-56) and the frontend
+    predicts it with the one-layer Lorenzo fallback without recording a
+    selection (SZGeneralFrontend.hpp:48-54): the stream holds one selection
+    fewer than blocks.  Decoding the last point with any other predictor would
+    break its error bound."""
+    import struct
+    case = golden_case("reg1d_thin")
+    conf, pl = O.read_stream(golden_stream(case))
+    nb = (case["dims"][0] - 1) // conf.blockSize + 1
+    p = 8 + 4 + 1 + 1  # dims, block size, Lorenzo id, regression id
+    ncoef = struct.unpack_from("<Q", pl, p)[0]
+    p += 8
+    for _ in range(2):  # the two coefficient quantizers
+        nun = struct.unpack_from("<Q", pl, p + 1 + 8 + 4)[0]
+        p += 1 + 8 + 4 + 8 + 4 * nun
+    assert ncoef > 0
+    p = _skip_huffman(pl, p)  # the coefficient codes
+    assert struct.unpack_from("<Q", pl, p)[0] == nb - 1  # selections
+    dec, c2 = O.decompress(golden_stream(case), dtype=np.float32)
+    x = golden_input(case)
+    assert abs(float(dec[-1]) - float(x[-1])) <= c2.absErrorBound
+
+
+def _skip_huffman(pl, p):
+    """Offset past one HuffmanEncoder<int> save + encode (HuffmanEncoder.hpp:
+    119-137, 150-227): offset, big-endian node count and state count, the
+    endianness byte, left / right child arrays (1, 2 or 4 bytes an entry by
+    node count), symbols, leaf flags, then the byte count and the bits."""
+    import struct
+    nc = struct.unpack_from(">i", pl, p + 4)[0]
+    w = 1 if nc <= 256 else (2 if nc <= 65536 else 4)
+    p += 4 + 4 + 4 + 1 + 2 * w * nc + 4 * nc + nc
+    nbytes = struct.unpack_from("<Q", pl, p)[0]
+    return p + 8 + nbytes
 
 
 def test_ska_order_small():
