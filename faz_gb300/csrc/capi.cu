@@ -56,12 +56,6 @@ struct Plan {
     size_t max_smem = 0;
 };
 
-int ceil_log2(uint64_t d) {
-    int l = 0;
-    while (((uint64_t)1 << l) < d) l++;
-    return l;
-}
-
 // permutations of 0..N-1 in lexicographic order (std::next_permutation)
 std::vector<std::vector<int>> permutations(int N) {
     std::vector<int> s(N);
@@ -71,19 +65,6 @@ std::vector<std::vector<int>> permutations(int N) {
         out.push_back(s);
     } while (std::next_permutation(s.begin(), s.end()));
     return out;
-}
-
-// Level error bound (SZInterpolationCompressor.hpp:386-406, eb_ratio 0.5)
-double level_eb(double eb, double alpha, double beta, int level) {
-    if (alpha < 0) return level >= 3 ? eb * 0.5 : eb;
-    if (alpha >= 1) {
-        double cr = std::pow(alpha, level - 1);
-        if (cr > beta) cr = beta;
-        return eb / cr;
-    }
-    double cr = 1 - (level - 1) * alpha;
-    if (cr < beta) cr = beta;
-    return eb * cr;
 }
 
 template <typename T>
@@ -200,8 +181,12 @@ void check_config(const faz_config &c) {
     }
     if (num != c.num) throw Fail{FAZ_ERR_ARG, "num does not match dims"};
     if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
-    if (c.cmprAlgo != FAZ_ALGO_INTERP && c.cmprAlgo != FAZ_ALGO_INTERP_LORENZO && c.cmprAlgo != FAZ_ALGO_LORENZO_REG)
-        throw Fail{FAZ_ERR_UNSUPPORTED, "cmprAlgo must be ALGO_INTERP, ALGO_INTERP_LORENZO or ALGO_LORENZO_REG"};
+    if (c.cmprAlgo != FAZ_ALGO_INTERP && c.cmprAlgo != FAZ_ALGO_INTERP_LORENZO && c.cmprAlgo != FAZ_ALGO_LORENZO_REG &&
+        c.cmprAlgo != FAZ_ALGO_INTERP_BLOCKED)
+        throw Fail{FAZ_ERR_UNSUPPORTED,
+                   "cmprAlgo must be ALGO_INTERP, ALGO_INTERP_LORENZO, ALGO_LORENZO_REG or ALGO_INTERP_BLOCKED"};
+    if (c.cmprAlgo == FAZ_ALGO_INTERP_BLOCKED && c.N != 3)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_INTERP_BLOCKED is defined for 3-D data"};
     if (c.cmprAlgo == FAZ_ALGO_INTERP_LORENZO && c.FZ && !c.QoZ)
         throw Fail{FAZ_ERR_UNSUPPORTED, "FAZ features (wavelets, SPERR, conditioning; FZ = 1) are not implemented; "
                                         "set FZ = 0 (faz -F 0)"};
@@ -210,7 +195,8 @@ void check_config(const faz_config &c) {
     if (c.cmprAlgo == FAZ_ALGO_LORENZO_REG && c.N < 3 && c.regression2)
         throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG on 1-D / 2-D data is implemented without regression2 "
                                         "(Regression2ndOrder = NO)"};
-    if (c.blockwiseTuning) throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is not implemented"};
+    if (c.blockwiseTuning && c.cmprAlgo != FAZ_ALGO_INTERP_BLOCKED)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "blockwiseTuning is set by ALGO_INTERP_BLOCKED only"};
     if (c.wavelet != 0 || ((c.wavelet > 0 || c.sperrWithoutWave) && c.sperr >= c.wavelet))
         throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet / SPERR modes are not part of the interpolation path"};
     // 32-bit codes (more than 65536 bins) are implemented for the 3-D Lorenzo
@@ -567,6 +553,36 @@ void compress_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pay
     interp_finish<T>(r, st, payload, psize, tm, launches, sink);
 }
 
+// ALGO_INTERP_BLOCKED (SZInterp.hpp:3021-3500, compress_block
+// SZInterpolationCompressor.hpp:533-781): the Config becomes ALGO_INTERP with
+// block-wise tuning; the payload is the interpolation payload with the
+// per-block choices after the header.
+template <typename T>
+void blocked_payload(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&payload, size_t &psize, faz_timings &tm,
+                     Counter &launches, Sink *sink) {
+    blocked_prepare(c);
+    const int radius = c.quantbinCnt / 2;
+    if (radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "interpolation with more than 65536 bins is not implemented"};
+    const uint64_t n = c.num;
+    DevMem m(st);
+    T *W = m.alloc<T>(n), *scratch = m.alloc<T>(n);
+    uint16_t *codes = m.alloc<uint16_t>(n);
+    Events ev_pred, ev_huff;
+    CK(cudaEventRecord(ev_pred.a, st));
+    std::vector<uint8_t> ops, dirs;
+    blocked_codes<T>(c, dX, W, codes, scratch, m, st, launches, ops, dirs);
+    CK(cudaEventRecord(ev_pred.b, st));
+    // compress_block (lines 753-757): choice count, interpolators, directions
+    std::vector<uint8_t> il;
+    put<uint64_t>(il, (uint64_t)ops.size());
+    il.insert(il.end(), ops.begin(), ops.end());
+    CK(cudaEventRecord(ev_huff.a, st));
+    interp_payload_tail<T>(c, il, dirs, c.absErrorBound, radius, n, codes, scratch, nullptr, m, st, launches, tm, sink,
+                           payload, psize, ev_huff.b);
+    tm.predict_ms = ev_pred.ms();
+    tm.huffman_ms = ev_huff.ms();
+}
+
 // SZ_compress_dispatcher (include/QoZ/api/impl/SZDispatcher.hpp:12-36): error
 // bound, the default configuration's tuner, then the chosen compressor.
 template <typename T>
@@ -624,6 +640,10 @@ void compress_dispatch(faz_config &c, const T *dX, cudaStream_t st, uint8_t *&pa
     }
     if (c.cmprAlgo == FAZ_ALGO_INTERP) {
         compress_payload<T>(c, dX, st, payload, psize, tm, launches, sink);
+        return;
+    }
+    if (c.cmprAlgo == FAZ_ALGO_INTERP_BLOCKED) {
+        blocked_payload<T>(c, dX, st, payload, psize, tm, launches, sink);
         return;
     }
     std::vector<uint8_t> pl;
@@ -1225,13 +1245,24 @@ void parse_payload(const uint8_t *pl, size_t n, int N, Parsed &P) {
     P.cross = rd<uint64_t>(p, end);
     P.trim = rd<int32_t>(p, end);
     P.border = rd<int32_t>(p, end);
-    if (P.bwt) throw Fail{FAZ_ERR_UNSUPPORTED, "block-wise tuned streams are not implemented"};
-    if (P.nlist < 0 || P.nlist > FAZ_MAX_LEVELS) throw Fail{FAZ_ERR_FORMAT, "bad level list length"};
-    if ((size_t)(end - p) < (size_t)2 * P.nlist) throw Fail{FAZ_ERR_FORMAT, "truncated level lists"};
-    P.il.assign(p, p + P.nlist);
-    p += P.nlist;
-    P.dl.assign(p, p + P.nlist);
-    p += P.nlist;
+    if (P.bwt) {
+        // decompress_block (lines 233-239): one interpolator and direction per
+        // block and level; the level lists are not read
+        const uint64_t nops = rd<uint64_t>(p, end);
+        if ((size_t)(end - p) / 2 < nops) throw Fail{FAZ_ERR_FORMAT, "truncated block-wise choices"};
+        P.il.assign(p, p + nops);
+        p += nops;
+        P.dl.assign(p, p + nops);
+        p += nops;
+        P.nlist = 0;
+    } else {
+        if (P.nlist < 0 || P.nlist > FAZ_MAX_LEVELS) throw Fail{FAZ_ERR_FORMAT, "bad level list length"};
+        if ((size_t)(end - p) < (size_t)2 * P.nlist) throw Fail{FAZ_ERR_FORMAT, "truncated level lists"};
+        P.il.assign(p, p + P.nlist);
+        p += P.nlist;
+        P.dl.assign(p, p + P.nlist);
+        p += P.nlist;
+    }
     rd<uint8_t>(p, end);
     P.eb = rd<double>(p, end);
     P.radius = rd<int32_t>(p, end);
@@ -1362,6 +1393,31 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
     if ((size_t)(end - p) / sizeof(T) < P.nunpred) throw Fail{FAZ_ERR_FORMAT, "truncated unpredictable values"};
     p += P.nunpred * sizeof(T);
     if (!(P.eb > 0)) throw Fail{FAZ_ERR_FORMAT, "bad error bound"};
+    if (P.bwt) {
+        if (P.N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "block-wise tuned streams are implemented for 3-D data"};
+        if (P.cross || P.border)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "block-wise streams with crossBlock or another block order are not "
+                                            "implemented"};
+        const uint64_t num = P.dims[0] * P.dims[1] * P.dims[2];
+        DevMem m(st);
+        uint16_t *codes = m.alloc<uint16_t>(num);
+        T *dunpred = m.alloc<T>(P.nunpred ? P.nunpred : 1);
+        if (P.nunpred) CK(cudaMemcpyAsync(dunpred, P.unpred, P.nunpred * sizeof(T), cudaMemcpyHostToDevice, st));
+        Events ev_dec, ev_pred;
+        CK(cudaEventRecord(ev_dec.a, st));
+        huffman_decode_device(p, end, num, codes, m, st, launches);
+        uint64_t *zpos = nullptr;
+        const uint64_t nz = zero_positions(codes, num, m, st, launches, zpos);
+        if (nz != P.nunpred) throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
+        CK(cudaEventRecord(ev_dec.b, st));
+        CK(cudaEventRecord(ev_pred.a, st));
+        blocked_decompress_levels<T>(P.dims, P.maxStep, (int)P.blocksize, P.eb, P.alpha, P.beta, P.radius, P.trim,
+                                     P.il, P.dl, codes, zpos, nz, dunpred, dOut, m, st, launches);
+        CK(cudaEventRecord(ev_pred.b, st));
+        tm.huffman_ms = ev_dec.ms();
+        tm.predict_ms = ev_pred.ms();
+        return;
+    }
     Plan pl_ = make_plan<T>(P.N, P.dims, P.maxStep, (int)P.blocksize, P.fixbs, P.interp, P.dir, P.il, P.dl, P.eb, P.alpha,
                             P.beta, P.radius, P.trim, smem_limit());
     const uint64_t num = pl_.num;

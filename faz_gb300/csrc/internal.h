@@ -1,6 +1,7 @@
 // internal.h - host-side declarations shared by the library's translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <mutex>
@@ -18,6 +19,26 @@ namespace faz {
 // per (device, kernel).  Setting the limit to each launch's own need instead
 // races: host threads launching the same kernel concurrently (the tuner's
 // trials) can lower it between another thread's set and launch.
+// smallest l with 2^l >= d (ceil(log2(d)) for d >= 1)
+inline int ceil_log2(uint64_t d) {
+    int l = 0;
+    while (((uint64_t)1 << l) < d) l++;
+    return l;
+}
+
+// Level error bound (SZInterpolationCompressor.hpp:386-406, eb_ratio 0.5)
+inline double level_eb(double eb, double alpha, double beta, int level) {
+    if (alpha < 0) return level >= 3 ? eb * 0.5 : eb;
+    if (alpha >= 1) {
+        double cr = std::pow(alpha, level - 1);
+        if (cr > beta) cr = beta;
+        return eb / cr;
+    }
+    double cr = 1 - (level - 1) * alpha;
+    if (cr < beta) cr = beta;
+    return eb * cr;
+}
+
 inline cudaError_t allow_dynamic_smem(const void *func) {
     static std::mutex mu;
     static std::set<std::pair<int, const void *>> done;

@@ -217,24 +217,6 @@ __global__ void k_qz_gather(const T *__restrict__ X, const int64_t *__restrict__
     out[idx] = X[src];
 }
 
-double level_eb_of(double eb, double alpha, double beta, int level) {
-    if (alpha < 0) return level >= 3 ? eb * 0.5 : eb;
-    if (alpha >= 1) {
-        double cr = std::pow(alpha, level - 1);
-        if (cr > beta) cr = beta;
-        return eb / cr;
-    }
-    double cr = 1 - (level - 1) * alpha;
-    if (cr < beta) cr = beta;
-    return eb * cr;
-}
-
-int ceil_log2_u(uint64_t d) {
-    int l = 0;
-    while (((uint64_t)1 << l) < d) l++;
-    return l;
-}
-
 // Geometry of a sampled block as an N-D field for the interpolation
 // compressor (one interpolation block per level: interpBlockSize >= sbs).
 struct QzGeom {
@@ -262,7 +244,7 @@ QzGeom make_geom(int N, int64_t bsz, int64_t maxStep) {
     g.offs[2] = 1;
     g.offs[1] = d3[2];
     g.offs[0] = d3[1] * d3[2];
-    g.levels = ceil_log2_u((uint64_t)bsz);
+    g.levels = ceil_log2((uint64_t)bsz);
     g.ms = maxStep;
     if (maxStep > 0) {
         g.anchor = true;
@@ -348,7 +330,7 @@ void qz_run(const QzGeom &g, const QzRun &R, T *work, uint16_t *codes, T *scratc
     for (int level = start; level > R.end_level; level--) {
         LevelArgs q;
         std::memset(&q, 0, sizeof(q));
-        q.eb = level_eb_of(R.eb, R.alpha, R.beta, level);
+        q.eb = level_eb(R.eb, R.alpha, R.beta, level);
         q.recip = 1.0 / q.eb;
         q.radius = 32768;
         q.trim = R.trim;

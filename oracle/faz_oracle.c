@@ -130,6 +130,11 @@ typedef struct {
     int nperm;
     int *codes;
     size_t ncodes, capcodes, qidx;
+    /* blockwise tuning (compress_block / decompress_block): one interpolator
+     * and direction per block, levels coarse to fine, blocks in order */
+    uint8_t *bops, *bdirs;
+    size_t nbops, capbops, bidx;
+    int bad_blocks;  /* decompress: the list ran out */
 } orc_ctx;
 
 typedef struct {
@@ -137,7 +142,20 @@ typedef struct {
     double alpha, beta;
     int nlist;
     const uint8_t *interp_list, *dir_list;
+    int blockwise;  /* compress_block / decompress_block */
+    int bwsbs;      /* blockwiseSampleBlockSize */
 } orc_params;
+
+static void bops_push(orc_ctx *c, int op, int dir) {
+    if (c->nbops == c->capbops) {
+        c->capbops = c->capbops ? c->capbops * 2 : 256;
+        c->bops = (uint8_t *)realloc(c->bops, c->capbops);
+        c->bdirs = (uint8_t *)realloc(c->bdirs, c->capbops);
+    }
+    c->bops[c->nbops] = (uint8_t)op;
+    c->bdirs[c->nbops] = (uint8_t)dir;
+    c->nbops++;
+}
 
 static void codes_push(orc_ctx *c, int v) {
     if (c->ncodes == c->capcodes) {
@@ -738,7 +756,13 @@ int orc_interp_compress(const faz_config *conf, int dtype, const void *data, int
     ctx_init(&c, conf->N, dims, conf->maxStep);
     orc_params p = {conf->interpAlgo, conf->interpDirection, conf->interpBlockSize, conf->fixBlockSize,
                     conf->alpha, conf->beta, conf->interp_list_len, conf->interpAlgo_list,
-                    conf->interpDirection_list};
+                    conf->interpDirection_list, conf->blockwiseTuning, conf->blockwiseSampleBlockSize};
+    if (conf->blockwiseTuning && (conf->N != 3 || conf->crossBlock || conf->blockOrder || conf->interpBlockSize < 1)) {
+        /* block_interpolation_block3d is written for 3-D data; crossBlock and
+         * other block orders are not covered */
+        set_err("oracle covers blockwise tuning for 3-D data, crossBlock 0, block order 0");
+        return -2;
+    }
     if (conf->interpDirection >= c.nperm) { set_err("bad direction"); return -1; }
     for (int i = 0; i < conf->interp_list_len; i++)
         if (conf->interpDirection_list[i] >= c.nperm) { set_err("bad direction"); return -1; }
@@ -784,10 +808,17 @@ int orc_interp_compress(const faz_config *conf, int dtype, const void *data, int
     PUT(&b, (uint64_t)conf->crossBlock);
     PUT(&b, (int32_t)conf->trimToZero);
     PUT(&b, (int32_t)conf->blockOrder);
-    if (conf->interp_list_len > 0) {
+    if (conf->blockwiseTuning) {
+        /* compress_block (lines 753-757): the per-block choices */
+        PUT(&b, (uint64_t)c.nbops);
+        b_put(&b, c.bops, c.nbops);
+        b_put(&b, c.bdirs, c.nbops);
+    } else if (conf->interp_list_len > 0) {
         b_put(&b, conf->interpAlgo_list, conf->interp_list_len);
         b_put(&b, conf->interpDirection_list, conf->interp_list_len);
     }
+    free(c.bops);
+    free(c.bdirs);
     /* LinearQuantizer::save - IntegerQuantizer.hpp:185-201 */
     PUT(&b, (uint8_t)2);
     PUT(&b, eb);
@@ -1402,13 +1433,22 @@ static int payload_for(faz_config *conf, int dtype, const void *data, uint8_t **
 
 /* SZ_compress<T>: error bound, tuner (ALGO_INTERP_LORENZO), payload,
  * Lossless_zstd framing, Config trailer, int32 trailer size. */
+static int blocked_prepare(faz_config *c);
+
 int orc_compress(const faz_config *conf_in, int dtype, const void *data, uint8_t **out, size_t *out_size,
                  uint8_t **payload_out, size_t *payload_size_out) {
     faz_config conf = *conf_in;
     if (conf.N < 1 || conf.N > 4) { set_err("N must be 1..4"); return -1; }
     if (conf.cmprAlgo != FAZ_ALGO_INTERP && conf.cmprAlgo != FAZ_ALGO_LORENZO_REG &&
-        conf.cmprAlgo != FAZ_ALGO_INTERP_LORENZO) { set_err("unsupported cmprAlgo"); return -2; }
+        conf.cmprAlgo != FAZ_ALGO_INTERP_LORENZO && conf.cmprAlgo != FAZ_ALGO_INTERP_BLOCKED) {
+        set_err("unsupported cmprAlgo");
+        return -2;
+    }
     if (eb_resolve(&conf, dtype, data)) return -1;
+    if (conf.cmprAlgo == FAZ_ALGO_INTERP_BLOCKED) {
+        int rc = blocked_prepare(&conf);
+        if (rc) return rc;
+    }
     if (conf.cmprAlgo == FAZ_ALGO_INTERP_LORENZO) {
         int rc = sz3_tune(&conf, dtype, data);
         if (rc) return rc;
@@ -1432,6 +1472,31 @@ int orc_compress(const faz_config *conf_in, int dtype, const void *data, uint8_t
     else free(payload);
     *out = b.p;
     *out_size = b.n;
+    return 0;
+}
+
+/* SZ_compress_Interp_blocked (include/QoZ/api/impl/SZInterp.hpp:3021-3500)
+ * up to its compress_block call: the stream becomes ALGO_INTERP with
+ * blockwise tuning, blocks of interpBlockSize (default 32 in 3-D) at every
+ * level, per-block trials on blockwiseSampleBlockSize (default the block,
+ * at least 4).  The alpha/beta search it runs for autoTuningRate > 0 is not
+ * covered. */
+static int blocked_prepare(faz_config *c) {
+    if (c->N != 3) { set_err("ALGO_INTERP_BLOCKED is defined for 3-D data"); return -2; }
+    if (c->autoTuningRate > 0) { set_err("oracle covers ALGO_INTERP_BLOCKED without autotuning"); return -2; }
+    if (c->crossBlock || c->blockOrder) { set_err("oracle covers crossBlock 0, block order 0"); return -2; }
+    c->cmprAlgo = FAZ_ALGO_INTERP;
+    if (c->interpBlockSize <= 0) c->interpBlockSize = 32;
+    int max_level = (int)log2((double)c->interpBlockSize) + 1;
+    if (c->maxStep > 0) {
+        int t = (int)log2((double)c->maxStep);
+        if (t < max_level) max_level = t;
+    }
+    if (c->levelwisePredictionSelection > max_level) c->levelwisePredictionSelection = max_level;
+    if (c->blockwiseSampleBlockSize == 0) c->blockwiseSampleBlockSize = c->interpBlockSize;
+    if (c->blockwiseSampleBlockSize < 4) c->blockwiseSampleBlockSize = 4;
+    c->fixBlockSize = c->interpBlockSize;
+    c->blockwiseTuning = 1;
     return 0;
 }
 
@@ -1529,7 +1594,7 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
         if (conf_out) *conf_out = conf;
         return 0;
     }
-    if (conf.cmprAlgo != FAZ_ALGO_INTERP || conf.blockwiseTuning) {
+    if (conf.cmprAlgo != FAZ_ALGO_INTERP) {
         free(payload);
         set_err("oracle decodes ALGO_INTERP streams");
         return -2;
@@ -1556,8 +1621,21 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
     r_get(&r, &trim, 4);
     r_get(&r, &border, 4);
     uint8_t il[FAZ_MAX_LEVELS], dl[FAZ_MAX_LEVELS];
-    if (nlist < 0 || nlist > FAZ_MAX_LEVELS) { free(payload); set_err("bad level list"); return -4; }
-    if (nlist > 0) { r_get(&r, il, nlist); r_get(&r, dl, nlist); }
+    uint64_t nbops = 0;
+    const uint8_t *bops = NULL, *bdirs = NULL;
+    if (bwt) {
+        /* decompress_block (lines 233-239): the per-block choices */
+        if (N != 3 || cross || border) { free(payload); set_err("oracle decodes blockwise 3-D streams"); return -2; }
+        r_get(&r, &nbops, 8);
+        if (r.bad || nbops > (r.n - r.pos) / 2) { free(payload); set_err("bad block list"); return -4; }
+        bops = r.p + r.pos;
+        bdirs = r.p + r.pos + nbops;
+        r.pos += 2 * nbops;
+        nlist = 0;
+    } else {
+        if (nlist < 0 || nlist > FAZ_MAX_LEVELS) { free(payload); set_err("bad level list"); return -4; }
+        if (nlist > 0) { r_get(&r, il, nlist); r_get(&r, dl, nlist); }
+    }
     uint8_t qtag;
     double eb;
     int32_t radius;
@@ -1575,7 +1653,12 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
     c.codes = (int *)malloc(c.num * sizeof(int));
     c.ncodes = c.num;
     if (huff_decode(&r, c.num, c.codes)) { free(payload); free(c.codes); set_err("bad Huffman data"); return -4; }
-    orc_params p = {interp, dir, (int)bsz, fixbs, alpha, beta, nlist, il, dl};
+    orc_params p = {interp, dir, (int)bsz, fixbs, alpha, beta, nlist, il, dl, bwt ? 1 : 0, 0};
+    if (bwt) {
+        c.bops = (uint8_t *)bops;
+        c.bdirs = (uint8_t *)bdirs;
+        c.nbops = nbops;
+    }
     void *dec = malloc(c.num * es);
     if (dtype == FAZ_FLOAT) {
         run_f32 rr; memset(&rr, 0, sizeof rr); rr.c = &c; rr.data = (float *)dec; rr.decompress = 1;
@@ -1600,6 +1683,11 @@ int orc_decompress(const uint8_t *cmp, size_t cmp_size, int dtype, void **out, f
     }
     free(c.codes);
     free(payload);
+    if (c.bad_blocks || (bwt && c.bidx != nbops)) {
+        free(dec);
+        set_err("block list does not match the blocks");
+        return -4;
+    }
     *out = dec;
     if (conf_out) *conf_out = conf;
     return 0;

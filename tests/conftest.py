@@ -78,7 +78,8 @@ _INI_INT = {"InterpDirection": "interpDirection", "InterpBlockSize": "interpBloc
             "fixBlockSize": "fixBlockSize", "trimToZero": "trimToZero", "maxStep": "maxStep",
             "QuantizationBinTotal": "quantbinCnt", "blockOrder": "blockOrder", "BlockSize": "blockSize",
             "sampleBlockSize": "sampleBlockSize", "levelwisePredictionSelection": "levelwisePredictionSelection",
-            "testLorenzo": "testLorenzo", "profiling": "profiling", "var_first": "var_first", "abList": "abList"}
+            "testLorenzo": "testLorenzo", "profiling": "profiling", "var_first": "var_first", "abList": "abList",
+            "blockwiseSampleBlockSize": "blockwiseSampleBlockSize", "crossBlock": "crossBlock"}
 _INI_REAL = {"alpha": "alpha", "beta": "beta", "autoTuningRate": "autoTuningRate",
              "predictorTuningRate": "predictorTuningRate"}
 _INI_BOOL = {"Lorenzo": "lorenzo", "Lorenzo2ndOrder": "lorenzo2", "Regression": "regression",

@@ -154,6 +154,22 @@ def cases():
     out.append(("lor1d_l2", random_walk((3001,), 79), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"},
                  "AlgoSettings": {"Lorenzo2ndOrder": "YES", "Regression": "NO"}}))
+    # ALGO_INTERP_BLOCKED (3-D): per-block interpolator and direction chosen
+    # by trial, blocks of interpBlockSize at every level
+    blk = {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP_BLOCKED"}, "AlgoSettings": {}}
+    out.append(("blk_default", spectral_field((40, 56, 72), slope=-3.0, seed=94), ["-M", "REL", "1e-3"], blk))
+    out.append(("blk_f64_bs16", spectral_field((33, 47, 65), slope=-3.5, aniso=(1, 2, 4), seed=95,
+                                               dtype=np.float64), ["-M", "REL", "1e-5"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP_BLOCKED"}, "AlgoSettings": {"InterpBlockSize": "16"}}))
+    out.append(("blk_sbs8_abs", spectral_field((48, 48, 48), slope=-2.5, noise=0.02, seed=96), ["-M", "ABS", "0.05"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP_BLOCKED"},
+                 "AlgoSettings": {"blockwiseSampleBlockSize": "8"}}))
+    out.append(("blk_anchor_ab", spectral_field((64, 40, 50), slope=-3.0, seed=97), ["-M", "REL", "1e-4"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP_BLOCKED"},
+                 "AlgoSettings": {"maxStep": "16", "alpha": "1.5", "beta": "3"}}))
+    out.append(("blk_odd_bs8", spectral_field((17, 23, 130), slope=-3.0, seed=98), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"CmprAlgo": "ALGO_INTERP_BLOCKED"},
+                 "AlgoSettings": {"InterpBlockSize": "8", "trimToZero": "1"}}))
     # explicit ALGO_LORENZO_REG on 1-D / 2-D data with the linear-regression
     # predictor (the default Config: Lorenzo + regression, composed)
     lreg = {"GlobalSettings": {"CmprAlgo": "ALGO_LORENZO_REG"}, "AlgoSettings": {}}
