@@ -2,7 +2,11 @@
 // include/QoZ/api/impl/SZInterp.hpp:3021-3500) and the streams it writes:
 // SZInterpolationCompressor::compress_block / decompress_block
 // (include/QoZ/compressor/SZInterpolationCompressor.hpp:533-781, 201-323)
-// for 3-D fields.
+// for 3-D fields; and ::compress / ::decompress (lines 324-470, 42-199) with
+// a fixBlockSize that leaves the coarse lattice (not a multiple of 2^levels),
+// where the same block loop runs with the level's interpolator and direction
+// for every block (1-D and 2-D fields embedded as 3-D with leading axes of
+// extent 1).
 //
 // Every level is cut into blocks of interpBlockSize points (not scaled by
 // the level stride).  Compressing, each block first runs every candidate of
@@ -159,8 +163,10 @@ __device__ int64_t blk_pass(const BlkLevel &a, const T *__restrict__ X, T *__res
     return line_base;
 }
 
-// One block of a level: trials and compression, or decompression.
-template <typename T, bool DECOMP>
+// One block of a level.  KIND 0: trials, then compression with the chosen
+// candidate; 1: compression with the candidate in ops / dirs; 2:
+// decompression with it.
+template <typename T, int KIND>
 __device__ void blk_block(const BlkLevel &a, int64_t blk, const T *__restrict__ X, T *__restrict__ W,
                           uint16_t *__restrict__ codes, T *__restrict__ scratch, const uint64_t *__restrict__ zpos,
                           uint64_t nz, const T *__restrict__ unpred, double *lsum) {
@@ -173,7 +179,7 @@ __device__ void blk_block(const BlkLevel &a, int64_t blk, const T *__restrict__ 
         e[i] = std::min<int64_t>(b[i] + a.B, a.dims[i] - 1);
     }
     int op, dir;
-    if (DECOMP) {
+    if (KIND != 0) {
         op = a.ops[blk];
         dir = a.dirs[blk];
         if (op > 1 || dir >= a.ndir) {
@@ -212,7 +218,7 @@ __device__ void blk_block(const BlkLevel &a, int64_t blk, const T *__restrict__ 
         op = s_choice[0];
         dir = s_choice[1];
     }
-    if (DECOMP)
+    if (KIND == 2)
         blk_pass<T, 2>(a, X, W, b, e, a.perm[dir], op == 1, a.block_off[blk], codes, scratch, zpos, nz, unpred, lsum);
     else
         blk_pass<T, 0>(a, X, W, b, e, a.perm[dir], op == 1, a.block_off[blk], codes, scratch, zpos, nz, unpred, lsum);
@@ -220,14 +226,14 @@ __device__ void blk_block(const BlkLevel &a, int64_t blk, const T *__restrict__ 
 }
 
 // The blocks of one anti-diagonal: block list[first + blockIdx.x].
-template <typename T, bool DECOMP>
+template <typename T, int KIND>
 __global__ void __launch_bounds__(kBlkThreads)
     k_blk_level(BlkLevel a, const int64_t *__restrict__ list, int64_t first, const T *__restrict__ X,
                 T *__restrict__ W, uint16_t *__restrict__ codes, T *__restrict__ scratch,
                 const uint64_t *__restrict__ zpos, uint64_t nz, const T *__restrict__ unpred) {
     extern __shared__ __align__(16) unsigned char blk_smem[];
     double *lsum = reinterpret_cast<double *>(blk_smem);
-    blk_block<T, DECOMP>(a, list[first + blockIdx.x], X, W, codes, scratch, zpos, nz, unpred, lsum);
+    blk_block<T, KIND>(a, list[first + blockIdx.x], X, W, codes, scratch, zpos, nz, unpred, lsum);
 }
 
 // Host plan of the block-wise levels.
@@ -305,7 +311,14 @@ BlkPlan make_blk_plan(const uint64_t *dims, uint64_t maxStep, int B) {
             pos += block_codes(b, e, s, perm0);
         }
     }
-    if (pos != p.num) throw Fail{FAZ_ERR_UNSUPPORTED, "block-wise level plan does not cover the field"};
+    // With an anchor grid and blocks smaller than maxStep, the level whose
+    // stride equals the block edge codes the anchor points a second time, so
+    // the stream holds more codes than points, and the reference's decoder
+    // decodes only as many codes as points (its last points then read past
+    // its list); such streams are not produced here.
+    if (pos != p.num)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "blocks smaller than maxStep code the anchor points twice, which the "
+                                        "reference cannot decode; not implemented"};
     // anti-diagonals bx + by + bz
     const int64_t nd = p.nb[0] + p.nb[1] + p.nb[2] - 2;
     std::vector<std::vector<int64_t>> by_d((size_t)nd);
@@ -351,10 +364,10 @@ BlkLevel level_args(const BlkPlan &p, const uint64_t *dims, int B, int bwsbs, in
     return a;
 }
 
-// Every level of a block-wise compression or decompression after the first
-// point / anchors.  ops / dirs: one entry per block per level (device).
-template <typename T, bool DECOMP>
-void blk_levels(const BlkPlan &p, const uint64_t *dims, int B, int bwsbs, double eb, double alpha, double beta,
+// Every level after the first point / anchors.  ops / dirs: one entry per
+// block per level (device), written by KIND 0, read by KIND 1 and 2.
+template <typename T, int KIND>
+void blk_levels(const BlkPlan &p, const uint64_t *dims3, int B, int bwsbs, double eb, double alpha, double beta,
                 int radius, int trim, const T *X, T *W, uint16_t *codes, T *scratch, const uint64_t *zpos, uint64_t nz,
                 const T *unpred, uint8_t *ops, uint8_t *dirs, int *derr, DevMem &m, cudaStream_t st,
                 Counter &launches) {
@@ -362,13 +375,13 @@ void blk_levels(const BlkPlan &p, const uint64_t *dims, int B, int bwsbs, double
     CK(cudaMemcpyAsync(boff, p.block_off.data(), p.block_off.size() * 8, cudaMemcpyHostToDevice, st));
     int64_t *dlist = m.alloc<int64_t>(p.diag_list.size());
     CK(cudaMemcpyAsync(dlist, p.diag_list.data(), p.diag_list.size() * 8, cudaMemcpyHostToDevice, st));
-    auto k = k_blk_level<T, DECOMP>;
+    auto k = k_blk_level<T, KIND>;
     // trial line sums: at most 3 (B + 1)^2 lines per block
-    const size_t smem = (size_t)3 * (B + 1) * (B + 1) * sizeof(double);
+    const size_t smem = KIND == 0 ? (size_t)3 * (B + 1) * (B + 1) * sizeof(double) : 16;
     CK(allow_dynamic_smem((const void *)k));
     int li = 0;
     for (int level = p.top; level > 0; level--, li++) {
-        BlkLevel a = level_args<T>(p, dims, B, bwsbs, level, eb, alpha, beta, radius, trim);
+        BlkLevel a = level_args<T>(p, dims3, B, bwsbs, level, eb, alpha, beta, radius, trim);
         a.block_off = boff + (size_t)li * p.nblocks;
         a.ops = ops + (size_t)li * p.nblocks;
         a.dirs = dirs + (size_t)li * p.nblocks;
@@ -376,8 +389,10 @@ void blk_levels(const BlkPlan &p, const uint64_t *dims, int B, int bwsbs, double
         if (a.s > B) {
             // every line of a block holds one point: no codes, every trial's
             // loss 0, so the first candidate (linear, direction 0) is recorded
-            if (!DECOMP) CK(cudaMemsetAsync(a.ops, 0, p.nblocks, st));
-            if (!DECOMP) CK(cudaMemsetAsync(a.dirs, 0, p.nblocks, st));
+            if (KIND == 0) {
+                CK(cudaMemsetAsync(a.ops, 0, p.nblocks, st));
+                CK(cudaMemsetAsync(a.dirs, 0, p.nblocks, st));
+            }
             continue;
         }
         for (size_t d = 0; d + 1 < p.diag_first.size(); d++) {
@@ -397,6 +412,30 @@ void check_blocked(int N, int B, int bwsbs, int cross, int border) {
     if (bwsbs < 1) throw Fail{FAZ_ERR_ARG, "bad blockwiseSampleBlockSize"};
     if (cross) throw Fail{FAZ_ERR_UNSUPPORTED, "crossBlock is not implemented"};
     if (border) throw Fail{FAZ_ERR_UNSUPPORTED, "block orders other than 0 are not implemented"};
+}
+
+// 1-D / 2-D fields embedded as 3-D with leading axes of extent 1, their
+// directions as the 3-D permutations that keep those axes first
+void embed(int N, const uint64_t *dims, uint64_t *dims3) {
+    const int e = 3 - N;
+    for (int i = 0; i < 3; i++) dims3[i] = 1;
+    for (int i = 0; i < N; i++) dims3[e + i] = dims[i];
+}
+
+int embed_dir(int N, int dir) {
+    if (N == 3) return dir;
+    if (N == 2) return dir == 0 ? 0 : 1;  // (0, 1, 2) and (0, 2, 1)
+    return 0;
+}
+
+void anchor_launch_args(const BlkPlan &p, const uint64_t *dims3, uint64_t maxStep, int N, int64_t *step,
+                        int64_t *offs) {
+    const int e = 3 - N;
+    for (int i = 0; i < 3; i++) step[i] = i < e ? 1 : (int64_t)maxStep;
+    offs[0] = (int64_t)(dims3[1] * dims3[2]);
+    offs[1] = (int64_t)dims3[2];
+    offs[2] = 1;
+    (void)p;
 }
 
 }  // namespace
@@ -423,6 +462,24 @@ void blocked_prepare(faz_config &c) {
     check_blocked(c.N, c.interpBlockSize, c.blockwiseSampleBlockSize, c.crossBlock, c.blockOrder);
 }
 
+// Whether a fixBlockSize keeps every level's blocks on the coarse lattice
+// (fixBlockSize a multiple of 2^top), the case the level kernels cover.
+bool fixbs_aligned(int N, const uint64_t *dims, uint64_t maxStep, int fixbs) {
+    uint64_t dims3[3];
+    embed(N, dims, dims3);
+    int levels = 0;
+    for (int i = 0; i < 3; i++) levels = std::max(levels, ceil_log2(dims3[i]));
+    if (maxStep > 0) {
+        levels += 1;
+        int lm = 0;
+        while (((uint64_t)1 << (lm + 1)) <= maxStep) lm++;
+        lm += 1;
+        if (lm <= levels) levels = lm;
+        levels -= 1;
+    }
+    return levels <= 0 || fixbs % (1 << std::min(levels, 30)) == 0;
+}
+
 // compress_block up to its codes: first point / anchors, then every level
 // block by block.  codes / scratch hold the codes in stream order and the
 // unpredictable values at their code positions; ops / dirs (host) receive
@@ -437,17 +494,17 @@ void blocked_codes(const faz_config &c, const T *dX, T *W, uint16_t *codes, T *s
     if (!p.anchor) {
         launches(launch_first_point<T>(false, dX, W, codes, scratch, eb, radius, c.trimToZero, nullptr, 0, nullptr, st));
     } else {
-        const int64_t step[3] = {(int64_t)c.maxStep, (int64_t)c.maxStep, (int64_t)c.maxStep};
-        const int64_t offs[3] = {(int64_t)(c.dims[1] * c.dims[2]), (int64_t)c.dims[2], 1};
+        int64_t step[3], offs[3];
+        anchor_launch_args(p, c.dims, c.maxStep, 3, step, offs);
         launches(launch_anchors<T>(false, dX, W, codes, scratch, nullptr, p.na, step, offs, st));
     }
     const size_t nops = (size_t)p.top * p.nblocks;
     uint8_t *dops = m.alloc<uint8_t>(2 * nops);
     int *derr = m.alloc<int>(1);
     CK(cudaMemsetAsync(derr, 0, 4, st));
-    blk_levels<T, false>(p, c.dims, c.interpBlockSize, c.blockwiseSampleBlockSize, eb, c.alpha, c.beta, radius,
-                         c.trimToZero, dX, W, codes, scratch, nullptr, 0, nullptr, dops, dops + nops, derr, m, st,
-                         launches);
+    blk_levels<T, 0>(p, c.dims, c.interpBlockSize, c.blockwiseSampleBlockSize, eb, c.alpha, c.beta, radius,
+                     c.trimToZero, dX, W, codes, scratch, nullptr, 0, nullptr, dops, dops + nops, derr, m, st,
+                     launches);
     ops.resize(nops);
     dirs.resize(nops);
     uint8_t *hb = t_pin_small.get(2 * nops + 8);
@@ -457,36 +514,115 @@ void blocked_codes(const faz_config &c, const T *dX, T *W, uint16_t *codes, T *s
     std::memcpy(dirs.data(), hb + nops, nops);
 }
 
-// decompress_block after the codes are decoded: first point / anchors, then
-// every level with the stream's per-block choices.
-template <typename T>
-void blocked_decompress_levels(const uint64_t *dims, uint64_t maxStep, int B, double eb, double alpha, double beta,
-                               int radius, int trim, const std::vector<uint8_t> &ops,
-                               const std::vector<uint8_t> &dirs, const uint16_t *codes, const uint64_t *zpos,
-                               uint64_t nz, const T *unpred, T *dOut, DevMem &m, cudaStream_t st, Counter &launches) {
-    check_blocked(3, B, 1, 0, 0);
-    const BlkPlan p = make_blk_plan(dims, maxStep, B);
+namespace {
+
+// Device choice lists of a fixed-block stream: every block of a level takes
+// the level's interpolator and direction (the level lists, or interpAlgo /
+// interpDirection).
+uint8_t *level_choices(const BlkPlan &p, int N, int interp, int dir, const std::vector<uint8_t> &il,
+                       const std::vector<uint8_t> &dl, DevMem &m, cudaStream_t st) {
     const size_t nops = (size_t)p.top * p.nblocks;
-    if (ops.size() != nops || dirs.size() != nops)
-        throw Fail{FAZ_ERR_FORMAT, "block-wise choice list does not match the blocks"};
-    if (!p.anchor) {
-        launches(launch_first_point<T>(true, nullptr, dOut, const_cast<uint16_t *>(codes), nullptr, eb, radius, trim,
-                                       zpos, nz, unpred, st));
-    } else {
-        const int64_t step[3] = {(int64_t)maxStep, (int64_t)maxStep, (int64_t)maxStep};
-        const int64_t offs[3] = {(int64_t)(dims[1] * dims[2]), (int64_t)dims[2], 1};
-        launches(launch_anchors<T>(true, nullptr, dOut, const_cast<uint16_t *>(codes), nullptr, unpred, p.na, step,
-                                   offs, st));
+    std::vector<uint8_t> h(2 * nops + 1);
+    int li = 0;
+    for (int level = p.top; level > 0; level--, li++) {
+        int op = interp, d = dir;
+        if (!il.empty()) {
+            const size_t k = (size_t)(level - 1) < il.size() ? (size_t)(level - 1) : il.size() - 1;
+            op = il[k];
+            d = dl[k];
+        }
+        const int nd = N == 3 ? 6 : (N == 2 ? 2 : 1);
+        if (d < 0 || d >= nd) throw Fail{FAZ_ERR_ARG, "interpolation direction out of range"};
+        std::memset(h.data() + (size_t)li * p.nblocks, op == FAZ_INTERP_ALGO_CUBIC ? 1 : 0, p.nblocks);
+        std::memset(h.data() + nops + (size_t)li * p.nblocks, embed_dir(N, d), p.nblocks);
     }
     uint8_t *dops = m.alloc<uint8_t>(2 * nops + 1);
-    if (nops) {
-        CK(cudaMemcpyAsync(dops, ops.data(), nops, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(dops + nops, dirs.data(), nops, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dops, h.data(), 2 * nops, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));  // h leaves scope
+    return dops;
+}
+
+void check_fixed(int N, int fixbs) {
+    if (N < 1 || N > 3) throw Fail{FAZ_ERR_UNSUPPORTED, "fixBlockSize is implemented for 1-D to 3-D data"};
+    if (fixbs < 2 || fixbs > kBlkMaxEdge || (fixbs & (fixbs - 1)))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "a fixBlockSize that is not a multiple of 2^levels must be a power of two in "
+                                        "[2, 64] on the GPU path"};
+}
+
+}  // namespace
+
+// SZInterpolationCompressor::compress (lines 324-470) with a fixBlockSize
+// that leaves the coarse lattice: blocks of fixBlockSize at every level, the
+// level's interpolator and direction for every block.
+template <typename T>
+void fixed_block_codes(const faz_config &c, const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
+                       const T *dX, T *W, uint16_t *codes, T *scratch, DevMem &m, cudaStream_t st, Counter &launches) {
+    check_fixed(c.N, c.fixBlockSize);
+    if (c.crossBlock || c.blockOrder)
+        throw Fail{FAZ_ERR_UNSUPPORTED, "crossBlock and other block orders are not implemented"};
+    uint64_t dims3[3];
+    embed(c.N, c.dims, dims3);
+    if (c.maxStep > 0 && c.N < 2) throw Fail{FAZ_ERR_UNSUPPORTED, "an anchor grid needs 2-D or 3-D data"};
+    const BlkPlan p = make_blk_plan(dims3, c.maxStep, c.fixBlockSize);
+    const double eb = c.absErrorBound;
+    const int radius = c.quantbinCnt / 2;
+    if (!p.anchor) {
+        launches(launch_first_point<T>(false, dX, W, codes, scratch, eb, radius, c.trimToZero, nullptr, 0, nullptr, st));
+    } else {
+        int64_t step[3], offs[3];
+        anchor_launch_args(p, dims3, c.maxStep, c.N, step, offs);
+        launches(launch_anchors<T>(false, dX, W, codes, scratch, nullptr, p.na, step, offs, st));
+    }
+    const size_t nops = (size_t)p.top * p.nblocks;
+    uint8_t *dops = level_choices(p, c.N, c.interpAlgo, c.interpDirection, il, dl, m, st);
+    int *derr = m.alloc<int>(1);
+    CK(cudaMemsetAsync(derr, 0, 4, st));
+    blk_levels<T, 1>(p, dims3, c.fixBlockSize, c.fixBlockSize, eb, c.alpha, c.beta, radius, c.trimToZero, dX, W, codes,
+                     scratch, nullptr, 0, nullptr, dops, dops + nops, derr, m, st, launches);
+}
+
+// decompress_block, or decompress with a fixBlockSize off the coarse
+// lattice, after the codes are decoded: first point / anchors, then every
+// level with the per-block choices (block-wise streams) or the level's
+// interpolator and direction (ops empty).
+template <typename T>
+void blocked_decompress_levels(int N, const uint64_t *dims, uint64_t maxStep, int B, double eb, double alpha,
+                               double beta, int radius, int trim, int interp, int dir,
+                               const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
+                               const std::vector<uint8_t> &ops, const std::vector<uint8_t> &dirs, bool blockwise,
+                               const uint16_t *codes, const uint64_t *zpos, uint64_t nz, const T *unpred, T *dOut,
+                               DevMem &m, cudaStream_t st, Counter &launches) {
+    if (blockwise) check_blocked(N, B, 1, 0, 0);
+    else check_fixed(N, B);
+    uint64_t dims3[3];
+    embed(N, dims, dims3);
+    if (maxStep > 0 && N < 2) throw Fail{FAZ_ERR_UNSUPPORTED, "an anchor grid needs 2-D or 3-D data"};
+    const BlkPlan p = make_blk_plan(dims3, maxStep, B);
+    const size_t nops = (size_t)p.top * p.nblocks;
+    uint16_t *cw = const_cast<uint16_t *>(codes);
+    if (!p.anchor) {
+        launches(launch_first_point<T>(true, nullptr, dOut, cw, nullptr, eb, radius, trim, zpos, nz, unpred, st));
+    } else {
+        int64_t step[3], offs[3];
+        anchor_launch_args(p, dims3, maxStep, N, step, offs);
+        launches(launch_anchors<T>(true, nullptr, dOut, cw, nullptr, unpred, p.na, step, offs, st));
+    }
+    uint8_t *dops;
+    if (blockwise) {
+        if (ops.size() != nops || dirs.size() != nops)
+            throw Fail{FAZ_ERR_FORMAT, "block-wise choice list does not match the blocks"};
+        dops = m.alloc<uint8_t>(2 * nops + 1);
+        if (nops) {
+            CK(cudaMemcpyAsync(dops, ops.data(), nops, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(dops + nops, dirs.data(), nops, cudaMemcpyHostToDevice, st));
+        }
+    } else {
+        dops = level_choices(p, N, interp, dir, il, dl, m, st);
     }
     int *derr = m.alloc<int>(1);
     CK(cudaMemsetAsync(derr, 0, 4, st));
-    blk_levels<T, true>(p, dims, B, B, eb, alpha, beta, radius, trim, nullptr, dOut, const_cast<uint16_t *>(codes),
-                        nullptr, zpos, nz, unpred, dops, dops + nops, derr, m, st, launches);
+    blk_levels<T, 2>(p, dims3, B, B, eb, alpha, beta, radius, trim, nullptr, dOut, cw, nullptr, zpos, nz, unpred, dops,
+                     dops + nops, derr, m, st, launches);
     int *he = (int *)t_pin_small.get(64);
     CK(cudaMemcpyAsync(he, derr, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));  // host lists leave scope
@@ -497,12 +633,19 @@ template void blocked_codes<float>(const faz_config &, const float *, float *, u
                                    cudaStream_t, Counter &, std::vector<uint8_t> &, std::vector<uint8_t> &);
 template void blocked_codes<double>(const faz_config &, const double *, double *, uint16_t *, double *, DevMem &,
                                     cudaStream_t, Counter &, std::vector<uint8_t> &, std::vector<uint8_t> &);
-template void blocked_decompress_levels<float>(const uint64_t *, uint64_t, int, double, double, double, int, int,
-                                               const std::vector<uint8_t> &, const std::vector<uint8_t> &,
+template void fixed_block_codes<float>(const faz_config &, const std::vector<uint8_t> &, const std::vector<uint8_t> &,
+                                       const float *, float *, uint16_t *, float *, DevMem &, cudaStream_t, Counter &);
+template void fixed_block_codes<double>(const faz_config &, const std::vector<uint8_t> &, const std::vector<uint8_t> &,
+                                        const double *, double *, uint16_t *, double *, DevMem &, cudaStream_t,
+                                        Counter &);
+template void blocked_decompress_levels<float>(int, const uint64_t *, uint64_t, int, double, double, double, int, int,
+                                               int, int, const std::vector<uint8_t> &, const std::vector<uint8_t> &,
+                                               const std::vector<uint8_t> &, const std::vector<uint8_t> &, bool,
                                                const uint16_t *, const uint64_t *, uint64_t, const float *, float *,
                                                DevMem &, cudaStream_t, Counter &);
-template void blocked_decompress_levels<double>(const uint64_t *, uint64_t, int, double, double, double, int, int,
-                                                const std::vector<uint8_t> &, const std::vector<uint8_t> &,
+template void blocked_decompress_levels<double>(int, const uint64_t *, uint64_t, int, double, double, double, int, int,
+                                                int, int, const std::vector<uint8_t> &, const std::vector<uint8_t> &,
+                                                const std::vector<uint8_t> &, const std::vector<uint8_t> &, bool,
                                                 const uint16_t *, const uint64_t *, uint64_t, const double *, double *,
                                                 DevMem &, cudaStream_t, Counter &);
 

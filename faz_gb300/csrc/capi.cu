@@ -484,6 +484,24 @@ void interp_levels(InterpCodes<T> &r, faz_config &c, const T *dX, cudaStream_t s
     if (radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "interpolation with more than 65536 bins is not implemented"};
     r.il.assign(c.interpAlgo_list, c.interpAlgo_list + c.interp_list_len);
     r.dl.assign(c.interpDirection_list, c.interpDirection_list + c.interp_list_len);
+    if (c.fixBlockSize > 0 && !fixbs_aligned(c.N, c.dims, c.maxStep, c.fixBlockSize)) {
+        // blocks of fixBlockSize that leave the coarse lattice: the block
+        // wavefront of blocked.cu with the level's interpolator and direction
+        DevMem &m = r.m;
+        T *W = m.alloc<T>(c.num);
+        r.scratch = m.alloc<T>(c.num);
+        r.codes = m.alloc<uint16_t>(c.num);
+        CK(cudaEventRecord(r.ev_pred.a, st));
+        fixed_block_codes<T>(c, r.il, r.dl, dX, W, r.codes, r.scratch, m, st, launches);
+        CK(cudaEventRecord(r.ev_pred.b, st));
+        r.c = c;
+        r.eb = eb;
+        r.radius = radius;
+        r.n = c.num;
+        r.vcount = nullptr;
+        r.have_levels = false;
+        return;
+    }
     Plan p = make_plan<T>(c.N, c.dims, c.maxStep, c.interpBlockSize, c.fixBlockSize, c.interpAlgo, c.interpDirection,
                           r.il, r.dl, eb, c.alpha, c.beta, radius, c.trimToZero, smem_limit());
     const uint64_t n = p.num;
@@ -832,7 +850,8 @@ int compress_batch_impl(int nf, const faz_config *confs, const void *const *d_da
         const int threads = threads_hint == 256 || threads_hint == 128 ? threads_hint : 512;
         for (int i = 0; i < nf; i++) {
             const faz_config &c = cs[i];
-            if (c.cmprAlgo != FAZ_ALGO_INTERP) {
+            if (c.cmprAlgo != FAZ_ALGO_INTERP ||
+                (c.fixBlockSize > 0 && !fixbs_aligned(c.N, c.dims, c.maxStep, c.fixBlockSize))) {
                 rest.push_back(i);
                 continue;
             }
@@ -1393,12 +1412,13 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
     if ((size_t)(end - p) / sizeof(T) < P.nunpred) throw Fail{FAZ_ERR_FORMAT, "truncated unpredictable values"};
     p += P.nunpred * sizeof(T);
     if (!(P.eb > 0)) throw Fail{FAZ_ERR_FORMAT, "bad error bound"};
-    if (P.bwt) {
-        if (P.N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "block-wise tuned streams are implemented for 3-D data"};
+    if (P.bwt || (P.fixbs > 0 && P.N <= 3 && !fixbs_aligned(P.N, P.dims, P.maxStep, P.fixbs))) {
+        // decompress_block, or blocks of fixBlockSize off the coarse lattice
+        if (P.bwt && P.N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "block-wise tuned streams are implemented for 3-D data"};
         if (P.cross || P.border)
-            throw Fail{FAZ_ERR_UNSUPPORTED, "block-wise streams with crossBlock or another block order are not "
-                                            "implemented"};
-        const uint64_t num = P.dims[0] * P.dims[1] * P.dims[2];
+            throw Fail{FAZ_ERR_UNSUPPORTED, "streams with crossBlock or another block order are not implemented"};
+        uint64_t num = 1;
+        for (int i = 0; i < P.N; i++) num *= P.dims[i];
         DevMem m(st);
         uint16_t *codes = m.alloc<uint16_t>(num);
         T *dunpred = m.alloc<T>(P.nunpred ? P.nunpred : 1);
@@ -1411,8 +1431,11 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
         if (nz != P.nunpred) throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
         CK(cudaEventRecord(ev_dec.b, st));
         CK(cudaEventRecord(ev_pred.a, st));
-        blocked_decompress_levels<T>(P.dims, P.maxStep, (int)P.blocksize, P.eb, P.alpha, P.beta, P.radius, P.trim,
-                                     P.il, P.dl, codes, zpos, nz, dunpred, dOut, m, st, launches);
+        static const std::vector<uint8_t> none;
+        blocked_decompress_levels<T>(P.N, P.dims, P.maxStep, P.bwt ? (int)P.blocksize : P.fixbs, P.eb, P.alpha, P.beta,
+                                     P.radius, P.trim, P.interp, P.dir, P.bwt ? none : P.il, P.bwt ? none : P.dl,
+                                     P.bwt ? P.il : none, P.bwt ? P.dl : none, P.bwt != 0, codes, zpos, nz, dunpred,
+                                     dOut, m, st, launches);
         CK(cudaEventRecord(ev_pred.b, st));
         tm.huffman_ms = ev_dec.ms();
         tm.predict_ms = ev_pred.ms();

@@ -375,17 +375,24 @@ void gen_compress_payload(int N, const uint64_t *dims, int bs, int lo, int lo2, 
 template <typename T>
 void gen_decompress(int N, const uint8_t *pl, size_t psize, const uint64_t *dims, int lo, int lo2, int reg, T *dOut,
                     cudaStream_t st, Counter &launches, faz_timings &tm);
-// ALGO_INTERP_BLOCKED (blocked.cu): the Config SZ_compress_Interp_blocked
-// leaves, the block-wise codes and choices, and the decoder of such streams
+// ALGO_INTERP_BLOCKED and fixBlockSize off the coarse lattice (blocked.cu):
+// the Config SZ_compress_Interp_blocked leaves, the codes of both kinds of
+// stream, and their decoder
 void blocked_prepare(faz_config &c);
+bool fixbs_aligned(int N, const uint64_t *dims, uint64_t maxStep, int fixbs);
 template <typename T>
 void blocked_codes(const faz_config &c, const T *dX, T *W, uint16_t *codes, T *scratch, DevMem &m, cudaStream_t st,
                    Counter &launches, std::vector<uint8_t> &ops, std::vector<uint8_t> &dirs);
 template <typename T>
-void blocked_decompress_levels(const uint64_t *dims, uint64_t maxStep, int B, double eb, double alpha, double beta,
-                               int radius, int trim, const std::vector<uint8_t> &ops,
-                               const std::vector<uint8_t> &dirs, const uint16_t *codes, const uint64_t *zpos,
-                               uint64_t nz, const T *unpred, T *dOut, DevMem &m, cudaStream_t st, Counter &launches);
+void fixed_block_codes(const faz_config &c, const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
+                       const T *dX, T *W, uint16_t *codes, T *scratch, DevMem &m, cudaStream_t st, Counter &launches);
+template <typename T>
+void blocked_decompress_levels(int N, const uint64_t *dims, uint64_t maxStep, int B, double eb, double alpha,
+                               double beta, int radius, int trim, int interp, int dir,
+                               const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
+                               const std::vector<uint8_t> &ops, const std::vector<uint8_t> &dirs, bool blockwise,
+                               const uint16_t *codes, const uint64_t *zpos, uint64_t nz, const T *unpred, T *dOut,
+                               DevMem &m, cudaStream_t st, Counter &launches);
 // calAbsErrorBound on the device (capi.cu)
 template <typename T>
 void resolve_eb(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);

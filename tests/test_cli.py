@@ -68,7 +68,7 @@ def _cli_case_args(case, td):
 def _gpu_cases():
     out = []
     for c in golden_manifest():
-        if len(c["dims"]) == 4 or c["name"] in ("c3d_fixbs8",):
+        if len(c["dims"]) == 4:
             continue
         rc = O.read_stream(open(os.path.join(GOLDEN, c["name"] + ".faz"), "rb").read())[0]
         if rc.cmprAlgo == 0 and rc.quantbinCnt > 65536:

@@ -85,9 +85,57 @@ def test_gpu_blocked_on_a_larger_field():
     assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
 
 
+# ALGO_INTERP with a fixBlockSize that is not a multiple of 2^levels: the
+# same block loop with the level's interpolator and direction everywhere
+FIX_CASES = [
+    ((30, 30, 30), dict(rel=1e-3, fixBlockSize=8), np.float32),
+    ((70, 45), dict(rel=1e-3, fixBlockSize=16, interpDirection=1), np.float32),
+    ((3000,), dict(rel=1e-3, fixBlockSize=32), np.float32),
+    ((40, 50, 60), dict(rel=1e-4, fixBlockSize=4, interpAlgo=0, interpDirection=3), np.float64),
+    ((33, 65, 17), dict(rel=1e-3, fixBlockSize=16, interpAlgo_list=[1, 0, 1], interpDirection_list=[0, 5, 2],
+                        alpha=1.25, beta=2.0), np.float32),
+    ((100, 120), dict(abs_=0.01, fixBlockSize=2, trimToZero=1), np.float32),
+    ((64, 200), dict(rel=1e-3, fixBlockSize=8, interpAlgo=0), np.float32),
+]
+
+
+@pytest.mark.parametrize("dims,kw,dtype", FIX_CASES)
+def test_gpu_unaligned_fix_block_size_matches_oracle(dims, kw, dtype):
+    conf = _conf(dims, **kw)
+    conf.cmprAlgo = F.ALGO_INTERP
+    x = spectral_field(dims, slope=-3.0, seed=5 * sum(dims), dtype=dtype)
+    if kw.get("trimToZero"):
+        x = (x / np.abs(x).max()).astype(dtype)
+    stream = F.SZ_compress(conf, x)
+    ref, _ = O.compress(conf, x)
+    assert O.read_stream(stream)[1] == O.read_stream(ref)[1]
+    assert mask_first_size(stream) == mask_first_size(ref)
+    dec, c3 = F.SZ_decompress(None, stream, dtype=dtype)
+    ref_dec, _ = O.decompress(ref, dtype=dtype)
+    assert np.array_equal(dec.view(np.uint8), ref_dec.view(np.uint8))
+    # one of them through the batched entry point
+    if dims == (30, 30, 30):
+        import torch
+        assert F.compress_batch([conf], [torch.from_numpy(x).cuda()])[0] == stream
+
+
 @pytest.mark.parametrize("dims,kw", [((40, 50), {}), ((30, 30, 30), dict(autoTuningRate=0.01)),
-                                     ((30, 30, 30), dict(crossBlock=1)), ((30, 30, 30), dict(interpBlockSize=24))])
+                                     ((30, 30, 30), dict(crossBlock=1)), ((30, 30, 30), dict(interpBlockSize=24)),
+                                     ((64, 64, 64), dict(maxStep=32, interpBlockSize=8))])
 def test_gpu_blocked_rejects_what_it_does_not_implement(dims, kw):
+    """Not 3-D, the alpha/beta search, crossBlock, a block edge that is not a
+    power of two, and blocks smaller than maxStep (the anchors are coded twice
+    and the reference's decoder reads past its codes)."""
     conf = _conf(dims, rel=1e-3, **kw)
     with pytest.raises(F.FazError):
         F.SZ_compress(conf, spectral_field(dims, slope=-3.0, seed=5))
+
+
+def test_gpu_fix_block_size_below_max_step_is_refused():
+    """ALGO_INTERP with an anchor grid and fixBlockSize below maxStep: the
+    reference codes the anchors twice and cannot decode its own stream."""
+    dims = (64, 64)
+    conf = _conf(dims, rel=1e-3, fixBlockSize=8, maxStep=32)
+    conf.cmprAlgo = F.ALGO_INTERP
+    with pytest.raises(F.FazError):
+        F.SZ_compress(conf, spectral_field(dims, slope=-3.0, seed=6))

@@ -18,9 +18,8 @@ import oracle.oracle as O
 
 pytestmark = pytest.mark.gpu
 
-# cases outside the GPU path: 4-D fields, and fixBlockSize values that break
-# the coarse-lattice alignment of blocks
-GPU_UNSUPPORTED = {"c4d_cubic", "c3d_fixbs8"}
+# cases outside the GPU path: 4-D fields
+GPU_UNSUPPORTED = {"c4d_cubic"}
 ALGO_INTERP = 2
 
 
