@@ -140,11 +140,12 @@ def make_conf(F, dims, eb, interp, algo="auto"):
     return c
 
 
-# DRAM traffic of one finest-level compress launch, measured with ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum = 342.43 MB + 100.42 MB) on a
-# 256x512x512 float32 field, cubic, rel eb 1e-3; traffic grows with the number
-# of values, so it is scaled to the benchmarked field by its value count.
-FINEST_TRAFFIC_BYTES = 442849280
+# DRAM traffic of one finest-level compress launch (the plane kernel
+# k_finest), measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum =
+# 335.69 MB + 95.54 MB) on a 256x512x512 float32 field, cubic, rel eb 1e-3;
+# traffic grows with the number of values, so it is scaled to the benchmarked
+# field by its value count.
+FINEST_TRAFFIC_BYTES = 431225856
 FINEST_TRAFFIC_VALUES = 256 * 512 * 512
 
 
@@ -714,7 +715,10 @@ def main():
         traffic = None
         if cubic and args.eb == 1e-3:
             traffic = int(round(FINEST_TRAFFIC_BYTES * nvals / FINEST_TRAFFIC_VALUES))
-        roof = {"kernel": "k_interp_level<float,compress> finest level (%s)" % ("cubic" if cubic else "linear"),
+        plane = dims[0] >= 33 and dims[1] >= 33 and dims[2] >= 36 and dims[2] % 4 == 0 and \
+            conf_out.interpDirection in (0, 2) and os.environ.get("FAZ_FINEST_PLANES", "1") != "0"
+        kname = "k_finest<compress>" if plane else "k_interp_level<float,compress>"
+        roof = {"kernel": "%s finest level (%s)" % (kname, "cubic" if cubic else "linear"),
                 "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind, "bytes_per_launch": fin_bytes,
                 "traffic": traffic}

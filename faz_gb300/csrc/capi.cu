@@ -390,9 +390,14 @@ template <typename T>
 void interp_payload_tail(const faz_config &c, const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
                          double eb, int radius, uint64_t n, uint16_t *codes, T *scratch, unsigned long long *vcount,
                          DevMem &m, cudaStream_t st, Counter &launches, faz_timings &tm, Sink *sink,
-                         uint8_t *&payload, size_t &psize, cudaEvent_t huff_end = nullptr) {
+                         uint8_t *&payload, size_t &psize, cudaEvent_t huff_end = nullptr, const int *lerr = nullptr) {
     HuffEncoded he;
     huffman_encode_device(codes, n, radius, m, st, launches, he, tm);
+    if (lerr) {
+        int le = 0;
+        CK(cudaMemcpy(&le, lerr, sizeof(int), cudaMemcpyDeviceToHost));
+        if (le) throw Fail{FAZ_ERR_DEVICE, "an interpolation level kernel gave up waiting for its plane copies"};
+    }
     if (vcount) {
         unsigned long long vc = 0;
         CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
@@ -469,6 +474,7 @@ struct InterpCodes {
     T *scratch = nullptr;
     uint16_t *codes = nullptr;
     unsigned long long *vcount = nullptr;
+    int *lerr = nullptr;  // set by a level kernel whose bounded wait gave up
     Events ev_pred, ev_fin;
     explicit InterpCodes(cudaStream_t st) : m(st) {}
 };
@@ -525,13 +531,15 @@ void interp_levels(InterpCodes<T> &r, faz_config &c, const T *dX, cudaStream_t s
         vcount = m.alloc<unsigned long long>(1);
         CK(cudaMemsetAsync(vcount, 0, 8, st));
     }
+    int *lerr = m.alloc<int>(1);
+    CK(cudaMemsetAsync(lerr, 0, sizeof(int), st));
     CK(cudaEventRecord(r.ev_pred.a, st));
     for (size_t li = 0; li < p.lv.size(); li++) {
         const LevelPlan &L = p.lv[li];
         LevelArgs a = L.args;
         a.block_off = boff + L.off_index;
         a.ncodes = n;
-        a.err = nullptr;
+        a.err = lerr;
         a.verify = vcount;
         if (li + 1 == p.lv.size()) CK(cudaEventRecord(r.ev_fin.a, st));
         int nl = 0;
@@ -547,6 +555,7 @@ void interp_levels(InterpCodes<T> &r, faz_config &c, const T *dX, cudaStream_t s
     r.scratch = scratch;
     r.codes = codes;
     r.vcount = vcount;
+    r.lerr = lerr;
     r.have_levels = !p.lv.empty();
 }
 
@@ -557,7 +566,7 @@ void interp_finish(InterpCodes<T> &r, cudaStream_t st, uint8_t *&payload, size_t
     Events ev_huff;
     CK(cudaEventRecord(ev_huff.a, st));
     interp_payload_tail<T>(r.c, r.il, r.dl, r.eb, r.radius, r.n, r.codes, r.scratch, r.vcount, r.m, st, launches, tm,
-                           sink, payload, psize, ev_huff.b);
+                           sink, payload, psize, ev_huff.b, r.lerr);
     tm.predict_ms = r.ev_pred.ms();
     tm.finest_level_ms = r.have_levels ? r.ev_fin.ms() : 0.0;
     tm.huffman_ms = ev_huff.ms();

@@ -68,6 +68,12 @@ template <typename T>
 cudaError_t launch_level(const LevelArgs &a, int64_t nblocks, bool decomp, const T *X, T *W, uint16_t *codes,
                          T *scratch, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st,
                          int *nlaunch);
+// The finest level of a 3-D float field, plane by plane with TMA-staged
+// planes (finest.cu): whether a level qualifies, and its launch.
+bool finest_eligible(const LevelArgs &a, bool decomp, const void *X, size_t elem);
+cudaError_t launch_finest(const LevelArgs &a, int64_t nblocks, bool decomp, const float *X, float *W,
+                          uint16_t *codes, float *scratch, const uint64_t *zpos, uint64_t nz, const float *unpred,
+                          cudaStream_t st);
 template <typename T>
 cudaError_t launch_first_point(bool decomp, const T *X, T *W, uint16_t *codes, T *scratch, double eb, int radius,
                                int trim, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st);
