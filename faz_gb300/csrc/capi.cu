@@ -180,7 +180,8 @@ void check_config(const faz_config &c) {
         num *= c.dims[i];
     }
     if (num != c.num) throw Fail{FAZ_ERR_ARG, "num does not match dims"};
-    if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
+    if (c.N == 4 && (c.cmprAlgo != FAZ_ALGO_INTERP || c.openmp))
+        throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are implemented for ALGO_INTERP (without openmp) on the GPU path"};
     if (c.cmprAlgo != FAZ_ALGO_INTERP && c.cmprAlgo != FAZ_ALGO_INTERP_LORENZO && c.cmprAlgo != FAZ_ALGO_LORENZO_REG &&
         c.cmprAlgo != FAZ_ALGO_INTERP_BLOCKED)
         throw Fail{FAZ_ERR_UNSUPPORTED,
@@ -490,6 +491,28 @@ void interp_levels(InterpCodes<T> &r, faz_config &c, const T *dX, cudaStream_t s
     if (radius > 32768) throw Fail{FAZ_ERR_UNSUPPORTED, "interpolation with more than 65536 bins is not implemented"};
     r.il.assign(c.interpAlgo_list, c.interpAlgo_list + c.interp_list_len);
     r.dl.assign(c.interpDirection_list, c.interpDirection_list + c.interp_list_len);
+    if (c.N == 4) {
+        // 4-D: one launch per level and sweep (interp4.cu)
+        DevMem &m = r.m;
+        T *W = m.alloc<T>(c.num);
+        r.scratch = m.alloc<T>(c.num);
+        r.codes = m.alloc<uint16_t>(c.num);
+        unsigned long long *vcount = nullptr;
+        if (verify_fast_path()) {
+            vcount = m.alloc<unsigned long long>(1);
+            CK(cudaMemsetAsync(vcount, 0, 8, st));
+        }
+        CK(cudaEventRecord(r.ev_pred.a, st));
+        interp4_codes<T>(c, eb, radius, r.il, r.dl, dX, W, r.codes, r.scratch, vcount, m, st, launches);
+        CK(cudaEventRecord(r.ev_pred.b, st));
+        r.c = c;
+        r.eb = eb;
+        r.radius = radius;
+        r.n = c.num;
+        r.vcount = vcount;
+        r.have_levels = false;
+        return;
+    }
     if (c.fixBlockSize > 0 && !fixbs_aligned(c.N, c.dims, c.maxStep, c.fixBlockSize)) {
         // blocks of fixBlockSize that leave the coarse lattice: the block
         // wavefront of blocked.cu with the level's interpolator and direction
@@ -859,7 +882,7 @@ int compress_batch_impl(int nf, const faz_config *confs, const void *const *d_da
         const int threads = threads_hint == 256 || threads_hint == 128 ? threads_hint : 512;
         for (int i = 0; i < nf; i++) {
             const faz_config &c = cs[i];
-            if (c.cmprAlgo != FAZ_ALGO_INTERP ||
+            if (c.cmprAlgo != FAZ_ALGO_INTERP || c.N == 4 ||
                 (c.fixBlockSize > 0 && !fixbs_aligned(c.N, c.dims, c.maxStep, c.fixBlockSize))) {
                 rest.push_back(i);
                 continue;
@@ -1325,7 +1348,6 @@ void huffman_decode_impl(const uint8_t *&p, const uint8_t *end, uint64_t num, C 
     const uint64_t nwords = (nbytes + 3) / 4;
     uint32_t *dbits = m.alloc<uint32_t>(nwords + 16);
     CK(cudaMemsetAsync(dbits, 0, (nwords + 16) * 4, st));
-    CK(cudaMemcpyAsync(dbits, hbits, nbytes, cudaMemcpyHostToDevice, st));
     uint32_t *lut = m.alloc<uint32_t>(t.lut.size());
     uint32_t *dl = m.alloc<uint32_t>(t.nodeCount), *dr = m.alloc<uint32_t>(t.nodeCount);
     int32_t *ds = m.alloc<int32_t>(t.nodeCount);
@@ -1348,7 +1370,50 @@ void huffman_decode_impl(const uint8_t *&p, const uint8_t *end, uint64_t num, C 
     int *flags = m.alloc<int>(2);  // [0] changed, [1] damaged tree
     CK(cudaMemsetAsync(flags, 0, 8, st));
     launches(launch_init_starts(start, nunits, st));
-    launches(launch_decode_spec(td, dbits, nwords, nbits, nunits, ea, cnt, bnd, flags + 1, st));
+    // The bit string comes over in slices on a copy stream while the
+    // speculative decode of the slices already in runs (a unit reads up to 8
+    // words past its CTA's units: each slice's copy carries the next slice's
+    // first 128 bytes).
+    {
+        const uint64_t cta = decode_cta_units();
+        const uint64_t unit_bytes = decode_unit_bits() / 8;
+        // four slices of a bit string of 16 MB or more: each decode launch
+        // still fills the GPU, three quarters of the copy overlap decoding
+        const uint64_t nslices0 = nbytes >= (16u << 20) ? 4 : 1;
+        const uint64_t slice_units = ((nunits + nslices0 - 1) / nslices0 + cta - 1) / cta * cta;
+        const uint64_t nslices = (nunits + slice_units - 1) / slice_units;
+        if (nslices <= 1) {
+            CK(cudaMemcpyAsync(dbits, hbits, nbytes, cudaMemcpyHostToDevice, st));
+            launches(launch_decode_spec(td, dbits, nwords, nbits, nunits, 0, nunits, ea, cnt, bnd, flags + 1, st));
+        } else {
+            StreamGuard cs(nullptr);
+            Events ready;
+            CK(cudaEventRecord(ready.a, st));  // dbits cleared
+            CK(cudaStreamWaitEvent(cs.st, ready.a, 0));
+            std::vector<cudaEvent_t> done(nslices, nullptr);
+            try {
+                for (uint64_t k = 0; k < nslices; k++) {
+                    CK(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming));
+                    const uint64_t b0 = k * slice_units * unit_bytes;
+                    const uint64_t b1 = std::min<uint64_t>(nbytes, (k + 1) * slice_units * unit_bytes + 128);
+                    CK(cudaMemcpyAsync((uint8_t *)dbits + b0, hbits + b0, b1 - b0, cudaMemcpyHostToDevice, cs.st));
+                    CK(cudaEventRecord(done[k], cs.st));
+                    CK(cudaStreamWaitEvent(st, done[k], 0));
+                    launches(launch_decode_spec(td, dbits, nwords, nbits, nunits, k * slice_units,
+                                                (k + 1) * slice_units, ea, cnt, bnd, flags + 1, st));
+                }
+            } catch (...) {
+                cudaStreamSynchronize(cs.st);
+                for (cudaEvent_t e : done)
+                    if (e) cudaEventDestroy(e);
+                throw;
+            }
+            // the copy stream's work is ordered before st's next launch; the
+            // events go once it has finished
+            CK(cudaStreamSynchronize(cs.st));
+            for (cudaEvent_t e : done) cudaEventDestroy(e);
+        }
+    }
     int *hflag = (int *)t_pin_small.get(64);
     bool converged = false;
     for (int it = 0; it < 1024; it++) {
@@ -1446,6 +1511,41 @@ void decompress_device(const uint8_t *pl, size_t n, Parsed &P, T *dOut, cudaStre
                                      P.bwt ? P.il : none, P.bwt ? P.dl : none, P.bwt != 0, codes, zpos, nz, dunpred,
                                      dOut, m, st, launches);
         CK(cudaEventRecord(ev_pred.b, st));
+        tm.huffman_ms = ev_dec.ms();
+        tm.predict_ms = ev_pred.ms();
+        return;
+    }
+    if (P.N == 4) {
+        if (P.cross || P.border)
+            throw Fail{FAZ_ERR_UNSUPPORTED, "streams with crossBlock or another block order are not implemented"};
+        uint64_t num = 1;
+        for (int i = 0; i < 4; i++) num *= P.dims[i];
+        DevMem m(st);
+        uint16_t *codes = m.alloc<uint16_t>(num);
+        T *dunpred = m.alloc<T>(P.nunpred ? P.nunpred : 1);
+        if (P.nunpred) CK(cudaMemcpyAsync(dunpred, P.unpred, P.nunpred * sizeof(T), cudaMemcpyHostToDevice, st));
+        Events ev_dec, ev_pred;
+        CK(cudaEventRecord(ev_dec.a, st));
+        huffman_decode_device(p, end, num, codes, m, st, launches);
+        uint64_t *zpos = nullptr;
+        const uint64_t nz = zero_positions(codes, num, m, st, launches, zpos);
+        if (nz != P.nunpred) throw Fail{FAZ_ERR_FORMAT, "unpredictable count does not match the zero codes"};
+        CK(cudaEventRecord(ev_dec.b, st));
+        unsigned long long *vcount = nullptr;
+        if (verify_fast_path()) {
+            vcount = m.alloc<unsigned long long>(1);
+            CK(cudaMemsetAsync(vcount, 0, 8, st));
+        }
+        CK(cudaEventRecord(ev_pred.a, st));
+        interp4_decompress<T>(P.dims, P.maxStep, (int)P.blocksize, P.fixbs, P.interp, P.dir, P.il, P.dl, P.eb, P.alpha,
+                              P.beta, P.radius, P.trim, codes, zpos, nz, dunpred, dOut, vcount, m, st, launches);
+        CK(cudaEventRecord(ev_pred.b, st));
+        CK(cudaStreamSynchronize(st));
+        if (vcount) {
+            unsigned long long vc = 0;
+            CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
+            if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
+        }
         tm.huffman_ms = ev_dec.ms();
         tm.predict_ms = ev_pred.ms();
         return;
@@ -1609,7 +1709,6 @@ int decompress_impl(faz_config *conf_io, const char *cmp, size_t cmp_size, void 
             throw Fail{FAZ_ERR_UNSUPPORTED, "ALGO_LORENZO_REG streams are implemented for 1-D, 2-D and 3-D data "
                                             "without regression2"};
         if (c.wavelet != 0) throw Fail{FAZ_ERR_UNSUPPORTED, "wavelet streams are not part of the interpolation path"};
-        if (c.N == 4) throw Fail{FAZ_ERR_UNSUPPORTED, "4-D fields are not implemented on the GPU path"};
         if (caller_buffer && cap < c.num)
             throw Fail{FAZ_ERR_ARG, "output buffer holds fewer values than the stream's field"};
         Parsed P;
@@ -1744,7 +1843,7 @@ int decompress_payload_impl(int N, const char *payload, size_t psize, void *d_ou
     std::memset(&tm, 0, sizeof(tm));
     auto t0 = clk::now();
     try {
-        if (N < 1 || N > 3) throw Fail{N == 4 ? FAZ_ERR_UNSUPPORTED : FAZ_ERR_ARG, "N must be 1..3 on the GPU path"};
+        if (N < 1 || N > 4) throw Fail{FAZ_ERR_ARG, "N must be 1..4"};
         if (!payload || !d_out) throw Fail{FAZ_ERR_ARG, "null argument"};
         Parsed P;
         std::memset(&P.conf, 0, sizeof(P.conf));

@@ -354,10 +354,12 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
 template <typename T>
 int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches);
 // The QoZ tuner's Lorenzo candidate: CompressTest(ALGO_LORENZO_REG) of nblk
-// sampled 2-D / 3-D blocks of bsz^N points (bit rate, PSNR).
+// sampled 2-D / 3-D blocks of bsz^N points (bit rate, PSNR); with `recon`
+// the blocks' reconstructions also come back to the host.
 template <typename T>
 void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng,
-                           double pcoeff, cudaStream_t st, Counter &launches, double &bitrate, double &psnr);
+                           double pcoeff, cudaStream_t st, Counter &launches, double &bitrate, double &psnr,
+                           std::vector<T> *recon = nullptr);
 // Lorenzo settings once the QoZ tuner has chosen Lorenzo (sampling, the
 // quantisation-interval estimate, pred_dim and 16384-bin trials).
 template <typename T>
@@ -386,6 +388,18 @@ void blocked_codes(const faz_config &c, const T *dX, T *W, uint16_t *codes, T *s
 template <typename T>
 void fixed_block_codes(const faz_config &c, const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
                        const T *dX, T *W, uint16_t *codes, T *scratch, DevMem &m, cudaStream_t st, Counter &launches);
+// 4-D fields (interp4.cu): codes and unpredictable values of every level, and
+// the inverse
+template <typename T>
+void interp4_codes(const faz_config &c, double eb, int radius, const std::vector<uint8_t> &il,
+                   const std::vector<uint8_t> &dl, const T *dX, T *W, uint16_t *codes, T *scratch,
+                   unsigned long long *verify, DevMem &m, cudaStream_t st, Counter &launches);
+template <typename T>
+void interp4_decompress(const uint64_t *dims, uint64_t maxStep, int blocksize, int fixbs, int interp, int dir,
+                        const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl, double eb, double alpha,
+                        double beta, int radius, int trim, const uint16_t *codes, const uint64_t *zpos, uint64_t nz,
+                        const T *unpred, T *dOut, unsigned long long *verify, DevMem &m, cudaStream_t st,
+                        Counter &launches);
 template <typename T>
 void blocked_decompress_levels(int N, const uint64_t *dims, uint64_t maxStep, int B, double eb, double alpha,
                                double beta, int radius, int trim, int interp, int dir,

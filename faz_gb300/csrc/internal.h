@@ -150,9 +150,12 @@ uint64_t decode_units(uint64_t nbits);
 uint64_t decode_unit_bits();
 int decode_boundaries();
 cudaError_t launch_init_starts(uint64_t *start, uint64_t n, cudaStream_t st);
+// speculative decode of units [ubase, min(uend, nunits)); ubase a multiple of
+// decode_cta_units()
+uint64_t decode_cta_units();
 cudaError_t launch_decode_spec(const DecodeTablesDev &t, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
-                               uint64_t nunits, uint64_t *end, unsigned int *cnt, uint16_t *bnd, int *err,
-                               cudaStream_t st);
+                               uint64_t nunits, uint64_t ubase, uint64_t uend, uint64_t *end, unsigned int *cnt,
+                               uint16_t *bnd, int *err, cudaStream_t st);
 cudaError_t launch_decode_resync(const DecodeTablesDev &t, const uint32_t *w32, uint64_t nwords, uint64_t nbits,
                                  uint64_t nunits, const uint64_t *end_in, uint64_t *end_out, unsigned int *cnt,
                                  const uint16_t *bnd, uint64_t *start, int *changed, cudaStream_t st);

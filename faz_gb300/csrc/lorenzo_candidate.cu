@@ -387,10 +387,12 @@ void huffman_i32(const int *codes, uint64_t n, int nsym, DevMem &m, cudaStream_t
 
 // CompressTest(ALGO_LORENZO_REG, TUNING_TARGET_RD) on nblk sampled blocks of
 // bsz^N points (N = 2 or 3) (dBlocks, block after block, row-major): bit rate of the one
-// payload the general compressor writes and PSNR of the reconstructions.
+// payload the general compressor writes and PSNR of the reconstructions (which
+// `recon`, when given, receives for the SSIM and autocorrelation targets).
 template <typename T>
 void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, double eb, double rng,
-                           double pcoeff, cudaStream_t st, Counter &launches, double &bitrate, double &psnr) {
+                           double pcoeff, cudaStream_t st, Counter &launches, double &bitrate, double &psnr,
+                           std::vector<T> *recon) {
     if (N != 2 && N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "the Lorenzo candidate covers 2-D and 3-D data"};
     TestArgs a;
     a.D = bsz;
@@ -460,6 +462,10 @@ void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, 
     p += h2.size();
     if (hc.nbytes) CK(cudaMemcpyAsync(p, hc.bits, hc.nbytes, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(hsq.data(), sq, n * sizeof(T), cudaMemcpyDeviceToHost, st));
+    if (recon) {
+        recon->resize(n);
+        CK(cudaMemcpyAsync(recon->data(), R, n * sizeof(T), cudaMemcpyDeviceToHost, st));
+    }
     CK(cudaStreamSynchronize(st));
     // the squared errors summed block by block, point by point (the
     // reference's loop order), in double
@@ -475,8 +481,8 @@ void lorenzo_compress_test(int N, const T *dBlocks, uint64_t nblk, int64_t bsz, 
 }
 
 template void lorenzo_compress_test<float>(int, const float *, uint64_t, int64_t, double, double, double,
-                                           cudaStream_t, Counter &, double &, double &);
+                                           cudaStream_t, Counter &, double &, double &, std::vector<float> *);
 template void lorenzo_compress_test<double>(int, const double *, uint64_t, int64_t, double, double, double,
-                                            cudaStream_t, Counter &, double &, double &);
+                                            cudaStream_t, Counter &, double &, double &, std::vector<double> *);
 
 }  // namespace faz

@@ -35,6 +35,7 @@
 #include "host.h"
 #include "internal.h"
 #include "quant.cuh"
+#include "tuning_metrics.h"
 
 namespace faz {
 
@@ -487,13 +488,13 @@ template <typename T>
 int qoz_prepare(faz_config &c, const T *dX, cudaStream_t st, Counter &launches) {
     const int N = c.N;
     if (N != 2 && N != 3) throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for 2-D and 3-D data"};
-    if (c.tuningTarget > 1)
-        throw Fail{FAZ_ERR_UNSUPPORTED, "QoZ tuning is implemented for the PSNR (RD) and ratio (CR) targets"};
+    if (c.tuningTarget > 3) throw Fail{FAZ_ERR_ARG, "tuningTarget must be RD, CR, SSIM or AC"};
     if (c.rng < 0) c.rng = device_range<T>(dX, c.num, st, launches);
     if (c.relErrorBound <= 0) c.relErrorBound = c.absErrorBound / c.rng;
     // waveAutoFix (default 1, not a Config field here) turns the Lorenzo
-    // trial off above a relative bound of 1e-3 (SZInterp.hpp:1592-1594)
-    if (c.relErrorBound > 1e-3) c.testLorenzo = 0;
+    // trial off above a relative bound of 1e-3 and under the SSIM target
+    // (SZInterp.hpp:1592-1594)
+    if (c.relErrorBound > 1e-3 || c.tuningTarget == 2) c.testLorenzo = 0;
     if (c.QoZ) {
         // QoZ defaults (SZInterp.hpp:1597-1625)
         if (c.autoTuningRate <= 0) c.autoTuningRate = N == 2 ? 0.01 : 0.005;
@@ -718,6 +719,16 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             std::memset(&tm, 0, sizeof(tm));
         }
     };
+    // The SSIM and autocorrelation targets score the alpha/beta search's
+    // tests by the sampled blocks' reconstructions (tuning_metrics.h): set
+    // once the search's sample is in, with the original blocks on the host.
+    int metric_target = 0;
+    std::vector<T> horig;
+    SsimCubes cubes;
+    auto target_metric = [&](const std::vector<T> &cur) -> double {
+        if (metric_target == 2) return ssim_metric<T>(cubes, horig.data(), cur.data(), nblk);
+        return 1.0 - autocorrelation_of<T>(horig.data(), cur.data(), horig.size());
+    };
     auto compress_test_on = [&](CtCtx &x, cudaStream_t s, int op, int dir, double alpha, double beta, double eb,
                                 double &bitrate, double &psnr, bool lists, double pc) {
         CK(cudaMemcpyAsync(x.work, blocks, nv * sizeof(T), cudaMemcpyDeviceToDevice, s));
@@ -791,6 +802,13 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
         double mse = se / ele;
         mse *= pc;
         psnr = 20 * std::log10(c.rng) - 10 * std::log10(mse);
+        if (metric_target >= 2) {
+            // the reconstructions are left in the working copy
+            std::vector<T> cur(nv);
+            CK(cudaMemcpyAsync(cur.data(), x.work, nv * sizeof(T), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            psnr = target_metric(cur);
+        }
     };
     // tests on the tuner's own stream
     std::unique_ptr<CtCtx> main_ctx;
@@ -909,6 +927,14 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             for (double beta : blist)
                 if (!((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1))) grid.emplace_back(alpha, beta);
         CK(cudaStreamSynchronize(st));  // the sampled blocks are gathered
+        if (c.tuningTarget >= 2) {
+            horig.resize(nv);
+            CK(cudaMemcpyAsync(horig.data(), blocks, nv * sizeof(T), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (c.tuningTarget == 2)
+                cubes = ssim_cubes<T>(horig.data(), nblk, N, (size_t)bsz, (size_t)c.SSIMBlockSize);
+            metric_target = c.tuningTarget;
+        }
         const int op0 = c.interpAlgo, dir0 = c.interpDirection;
         std::vector<std::future<GridRes>> futs;
         for (const auto &ab : grid) {
@@ -1020,6 +1046,7 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
                 if ((alpha >= 1 && alpha > beta) || (alpha < 0 && beta != -1)) continue;
                 double br, mm;
                 grid_result(alpha, beta, br, mm);
+                if (trace) std::fprintf(stderr, "qoz ab %g %g bitrate %.17g metric %.17g\n", alpha, beta, br, mm);
                 if (cr) mm = 0;
                 if ((!cr && mm >= bestm && br <= bestb) || (cr && br <= bestb)) {
                     bestalpha = alpha;
@@ -1052,7 +1079,10 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             // the Lorenzo candidate: CompressTest with ALGO_LORENZO_REG
             // against the best alpha/beta point (SZInterp.hpp:2428-2486)
             double br, mm;
-            lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb, c.rng, pcoeff, st, launches, br, mm);
+            std::vector<T> rec;
+            lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb, c.rng, pcoeff, st, launches, br, mm,
+                                     metric_target >= 2 ? &rec : nullptr);
+            if (metric_target >= 2) mm = target_metric(rec);
             if (cr) mm = 0;
             if ((!cr && mm >= bestm && br <= bestb) || (cr && br <= bestb)) {
                 bestb = br;
@@ -1064,7 +1094,9 @@ void qoz_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
             } else {
                 const double fix = br / bestb;
                 double br2, m2;
-                lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb * fix, c.rng, pcoeff, st, launches, br2, m2);
+                lorenzo_compress_test<T>(N, blocks, nblk, bsz, oriabseb * fix, c.rng, pcoeff, st, launches, br2, m2,
+                                         metric_target >= 2 ? &rec : nullptr);
+                if (metric_target >= 2) m2 = target_metric(rec);
                 if (cr) m2 = 0;
                 const double a = (mm - m2) / (br - br2);
                 if (a > 0) {

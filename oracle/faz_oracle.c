@@ -528,6 +528,17 @@ static int z_framed_size(const uint8_t *p, size_t n, size_t *out);
 
 #define T float
 #define SFX f32
+#include "oracle_metrics.inc"
+#undef T
+#undef SFX
+#define T double
+#define SFX f64
+#include "oracle_metrics.inc"
+#undef T
+#undef SFX
+
+#define T float
+#define SFX f32
 #include "oracle_general.inc"
 #undef T
 #undef SFX
@@ -893,13 +904,13 @@ static double data_range(int dtype, const void *data, size_t n) {
 static int qoz_tune(faz_config *conf, int dtype, const void *data) {
     int N = conf->N;
     if (N != 2 && N != 3) { set_err("oracle QoZ tuner covers 2-D and 3-D data"); return -2; }
-    if (conf->tuningTarget > 1 || conf->wavelet > 0 || conf->FZ) { set_err("oracle QoZ tuner covers the RD and CR targets"); return -2; }
+    if (conf->tuningTarget > 3 || conf->wavelet > 0 || conf->FZ) { set_err("oracle QoZ tuner covers the RD, CR, SSIM and AC targets"); return -2; }
     size_t es = dtype == FAZ_FLOAT ? 4 : 8;
     double rngT = dtype == FAZ_FLOAT ? (double)(float)conf->rng : conf->rng;   /* T rng = conf.rng */
     double rel_bound = conf->relErrorBound > 0 ? conf->relErrorBound : conf->absErrorBound / rngT;
     /* waveAutoFix (default 1) drops the Lorenzo trial above a relative bound
      * of 1e-3 (SZInterp.hpp:1592-1594) */
-    if (rel_bound > 1e-3) conf->testLorenzo = 0;
+    if (rel_bound > 1e-3 || conf->tuningTarget == 2) conf->testLorenzo = 0;  /* and with the SSIM target */
     if (conf->QoZ) {
         if (conf->autoTuningRate <= 0) conf->autoTuningRate = N == 2 ? 0.01 : 0.005;
         if (conf->predictorTuningRate <= 0) conf->predictorTuningRate = N == 2 ? 0.01 : 0.005;
@@ -1006,8 +1017,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         /* SZInterp.hpp:1925-1932 */
         double br, m;
         int rc = dtype == FAZ_FLOAT
-                     ? gen_test_f32((const float *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, 1.0, &br, &m)
-                     : gen_test_f64((const double *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, 1.0, &br, &m);
+                     ? gen_test_f32((const float *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, 1.0, &br, &m, NULL)
+                     : gen_test_f64((const double *)blocks, nblk, N, bsz, conf->absErrorBound, conf->rng, 1.0, &br, &m, NULL);
         if (rc) { free(blocks); return rc; }
         best_lorenzo_ratio = (double)es * 8.0 / br;
     }
@@ -1072,9 +1083,9 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             double br, m;
             int rc = dtype == FAZ_FLOAT
                          ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                 conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m)
+                                                 conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m, NULL)
                          : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                 conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m);
+                                                 conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m, NULL);
             if (rc) { free(blocks); return rc; }
             best_interp_cr = (double)es * 8.0 / br;
         }
@@ -1090,9 +1101,9 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                 double br, m;
                 int rc = dtype == FAZ_FLOAT
                              ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m)
+                                                     conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m, NULL)
                              : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m);
+                                                     conf->trimToZero, conf->maxStep, conf->rng, 1.0, &br, &m, NULL);
                 if (rc) { free(blocks); return rc; }
                 double cr = (double)es * 8.0 / br;
                 if (cr > best_cr) { best_cr = cr; best_op = op; best_dir = dirs[di]; }
@@ -1113,6 +1124,37 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                    ? qoz_sample_f32((const float *)data, N, gdims, sbs, conf->autoTuningRate, (float **)&blocks)
                    : qoz_sample_f64((const double *)data, N, gdims, sbs, conf->autoTuningRate, (double **)&blocks);
     }
+    /* the SSIM and AC targets score the search's CompressTests by the
+     * reconstructions of the sampled blocks (oracle_metrics.inc); the
+     * original's SSIM cube statistics are computed once */
+    const int tgt = conf->tuningTarget;
+    tmetric_f32 tm32;
+    tmetric_f64 tm64;
+    memset(&tm32, 0, sizeof tm32);
+    memset(&tm64, 0, sizeof tm64);
+    double *om = NULL, *os = NULL, *orr = NULL;
+    if (conf->autoTuningRate > 0 && (tgt == 2 || tgt == 3)) {
+        const size_t ss = (size_t)conf->SSIMBlockSize;
+        tm32.target = tm64.target = tgt;
+        tm32.N = tm64.N = N;
+        tm32.bsz = tm64.bsz = bsz;
+        tm32.s = tm64.s = ss;
+        if (tgt == 2) {
+            size_t nc = dtype == FAZ_FLOAT ? ssim_stats_f32((const float *)blocks, nblk, N, bsz, ss, &om, &os, &orr)
+                                           : ssim_stats_f64((const double *)blocks, nblk, N, bsz, ss, &om, &os, &orr);
+            tm32.om = tm64.om = om;
+            tm32.os = tm64.os = os;
+            tm32.orr = tm64.orr = orr;
+            tm32.ncube = tm64.ncube = nc;
+        } else if (dtype == FAZ_FLOAT) {
+            tm32.flat = (float *)malloc(nblk * per * sizeof(float));
+        } else {
+            tm64.flat = (double *)malloc(nblk * per * sizeof(double));
+        }
+    }
+#define TM_RESET(t) ((t).metric = 0, (t).idx = 0, (t).nflat = 0, &(t))
+#define TM32 (tgt >= 2 ? TM_RESET(tm32) : NULL)
+#define TM64 (tgt >= 2 ? TM_RESET(tm64) : NULL)
     if (conf->autoTuningRate > 0) {
         double bestalpha = 1, bestbeta = 1, bestb = 9999, bestm = 0;
         /* init_alphalist / init_betalist (SZInterp.hpp:868-933); the CR
@@ -1134,10 +1176,11 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                 double br, m;
                 int rc = dtype == FAZ_FLOAT
                              ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br, &m)
+                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br, &m, TM32)
                              : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br, &m);
+                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br, &m, TM64);
                 if (rc) { free(blocks); return rc; }
+                if (getenv("ORC_TUNE_TRACE")) fprintf(stderr, "orc ab %g %g bitrate %.17g metric %.17g\n", alpha, beta, br, m);
                 if (cr) m = 0;
                 if ((!cr && m >= bestm && br <= bestb) || (cr && br <= bestb)) {
                     bestalpha = alpha; bestbeta = beta; bestb = br; bestm = m;
@@ -1151,9 +1194,9 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
                     double br2, m2;
                     rc = dtype == FAZ_FLOAT
                              ? qoz_compress_test_f32((const float *)blocks, nblk, N, bsz, &p, conf->absErrorBound * fix,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br2, &m2)
+                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br2, &m2, TM32)
                              : qoz_compress_test_f64((const double *)blocks, nblk, N, bsz, &p, conf->absErrorBound * fix,
-                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br2, &m2);
+                                                     conf->trimToZero, conf->maxStep, conf->rng, pcoeff, &br2, &m2, TM64);
                     if (rc) { free(blocks); return rc; }
                     if (cr) m2 = 0;
                     double a = (m - m2) / (br - br2);
@@ -1171,8 +1214,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             /* the Lorenzo candidate: CompressTest with ALGO_LORENZO_REG against
              * the best alpha/beta point (SZInterp.hpp:2428-2486) */
             double br, m;
-            int rc = dtype == FAZ_FLOAT ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb, conf->rng, pcoeff, &br, &m)
-                                        : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb, conf->rng, pcoeff, &br, &m);
+            int rc = dtype == FAZ_FLOAT ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb, conf->rng, pcoeff, &br, &m, TM32)
+                                        : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb, conf->rng, pcoeff, &br, &m, TM64);
             if (rc) { free(blocks); return rc; }
             if (cr) m = 0;
             if ((!cr && m >= bestm && br <= bestb) || (cr && br <= bestb)) {
@@ -1182,8 +1225,8 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
             } else {
                 double fix = br / bestb, br2, m2;
                 rc = dtype == FAZ_FLOAT
-                         ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, pcoeff, &br2, &m2)
-                         : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, pcoeff, &br2, &m2);
+                         ? gen_test_f32((const float *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, pcoeff, &br2, &m2, TM32)
+                         : gen_test_f64((const double *)blocks, nblk, N, bsz, oriabseb * fix, conf->rng, pcoeff, &br2, &m2, TM64);
                 if (rc) { free(blocks); return rc; }
                 if (cr) m2 = 0;
                 double a = (m - m2) / (br - br2);
@@ -1199,6 +1242,14 @@ static int qoz_tune(faz_config *conf, int dtype, const void *data) {
         conf->wavelet_rel_coeff = 1;
         conf->wavelet = 0;
     }
+#undef TM32
+#undef TM64
+#undef TM_RESET
+    free(om);
+    free(os);
+    free(orr);
+    free(tm32.flat);
+    free(tm64.flat);
     if (L > 0 && use_interp) {
         conf->interp_list_len = L;
         for (int i = 0; i < L; i++) { conf->interpAlgo_list[i] = il[i]; conf->interpDirection_list[i] = dl[i]; }

@@ -13,7 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 SRC = [os.path.join(HERE, "faz_oracle.c"), os.path.join(HERE, "oracle_interp.inc"),
        os.path.join(HERE, "oracle_lorenzo.inc"), os.path.join(HERE, "oracle_general.inc"),
-       os.path.join(HERE, "oracle_qoz.inc"), os.path.join(HERE, "..", "include", "faz_gb300.h")]
+       os.path.join(HERE, "oracle_qoz.inc"), os.path.join(HERE, "oracle_metrics.inc"),
+       os.path.join(HERE, "..", "include", "faz_gb300.h")]
 REF_ZSTD = os.path.join(HERE, "_ref", "libzstd145.so")
 
 _lib = None

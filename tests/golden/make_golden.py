@@ -260,6 +260,31 @@ def cases():
                 {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_CR"},
                  "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01", "testLorenzo": "1",
                                   "sampleBlockSize": "16"}}))
+    # the SSIM and autocorrelation tuning targets (the alpha/beta search scores
+    # each CompressTest by the reconstruction's SSIM or 1 - autocorrelation)
+    out.append(("ssim_target_3d", spectral_field((64, 80, 96), slope=-2.0, noise=0.0, seed=150), ["-M", "REL", "1e-4"],
+                {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_SSIM"},
+                 "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                  "levelwisePredictionSelection": "4", "maxStep": "32", "sampleBlockSize": "16"}}))
+    out.append(("ssim_target_2d", spectral_field((400, 500), slope=-2.0, noise=0.05, seed=124), ["-M", "REL", "3e-3"],
+                {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_SSIM"},
+                 "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                  "levelwisePredictionSelection": "6", "maxStep": "64"}}))
+    out.append(("ssim_target_q", spectral_field((48, 56, 64), slope=-2.5, noise=0.02, seed=113),
+                ["-M", "REL", "1e-3", "-q"], {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_SSIM"},
+                                               "AlgoSettings": {}}))
+    out.append(("ac_target_3d", spectral_field((64, 80, 96), slope=-2.0, noise=0.06, seed=200), ["-M", "REL", "1e-4"],
+                {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_AC"},
+                 "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                  "levelwisePredictionSelection": "4", "maxStep": "32", "sampleBlockSize": "16"}}))
+    out.append(("ac_target_2d", spectral_field((400, 500), slope=-3.0, noise=0.02, seed=115), ["-M", "REL", "5e-3"],
+                {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_AC"},
+                 "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01",
+                                  "levelwisePredictionSelection": "6", "maxStep": "64"}}))
+    out.append(("ac_target_lorenzo", sum2d((64, 72, 80), 1e-3, 242), ["-M", "REL", "1e-3"],
+                {"GlobalSettings": {"tuningTarget": "TUNING_TARGET_AC"},
+                 "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01", "testLorenzo": "1",
+                                  "sampleBlockSize": "16"}}))
     out.append(("rate_ab_only", spectral_field((48, 56, 64), slope=-3.0, seed=82), ["-M", "REL", "1e-3"],
                 {"GlobalSettings": {}, "AlgoSettings": {"autoTuningRate": "0.01", "predictorTuningRate": "0.01"}}))
     out.append(("rate_2d", spectral_field((400, 500), slope=-3.0, seed=83), ["-M", "REL", "5e-3"],

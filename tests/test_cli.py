@@ -68,8 +68,6 @@ def _cli_case_args(case, td):
 def _gpu_cases():
     out = []
     for c in golden_manifest():
-        if len(c["dims"]) == 4:
-            continue
         rc = O.read_stream(open(os.path.join(GOLDEN, c["name"] + ".faz"), "rb").read())[0]
         if rc.cmprAlgo == 0 and rc.quantbinCnt > 65536:
             continue

@@ -18,8 +18,8 @@ import oracle.oracle as O
 
 pytestmark = pytest.mark.gpu
 
-# cases outside the GPU path: 4-D fields
-GPU_UNSUPPORTED = {"c4d_cubic"}
+# cases outside the GPU path (none: 4-D fields run through interp4.cu)
+GPU_UNSUPPORTED = set()
 ALGO_INTERP = 2
 
 

@@ -301,6 +301,46 @@ def test_gpu_cr_target_matches_oracle(dims, rel, kind):
         assert p == ref_payload
 
 
+# (dims, bound, target, field): every case but the planes one decides
+# differently from the PSNR target on the oracle (alpha, beta or Lorenzo)
+SSIM_AC_CASES = [
+    ((64, 80, 96), 1e-4, 2, (-2.25, 0.0, 6)), ((300, 420), 1e-4, 2, (-2.25, 0.03, 1)),
+    ((72, 64, 80), 1e-4, 2, (-2.25, 0.03, 1)),
+    ((64, 80, 96), 1e-3, 3, (-3.5, 0.03, 179)), ((300, 420), 5e-3, 3, (-3.5, 0.03, 723)),
+    ((64, 72, 80), 1e-3, 3, "planes"), ((48, 50, 52), 1e-5, 3, "f64"),
+]
+
+
+@pytest.mark.parametrize("dims,rel,target,kind", SSIM_AC_CASES)
+def test_gpu_ssim_and_ac_targets_match_oracle(dims, rel, target, kind):
+    """TUNING_TARGET_SSIM / TUNING_TARGET_AC: the alpha/beta search scores
+    each CompressTest by the reconstructions' SSIM or 1 - autocorrelation
+    (computed from the GPU's reconstructions); decisions and streams equal
+    the oracle's.  The planes case also runs the Lorenzo candidate."""
+    conf = F.Config(*dims)
+    conf.errorBoundMode = F.EB_REL
+    conf.relErrorBound = rel
+    conf.tuningTarget = target
+    conf.autoTuningRate = conf.predictorTuningRate = 0.01
+    conf.testLorenzo = 1
+    conf.sampleBlockSize = 16
+    if kind == "planes":
+        x = _sum_of_planes(dims, 1e-4, 9, np.float32)
+    elif kind == "f64":
+        x = spectral_field(dims, slope=-3.0, noise=0.02, seed=5, dtype=np.float64)
+    else:
+        x = spectral_field(dims, slope=kind[0], noise=kind[1], seed=kind[2])
+    stream = F.SZ_compress(conf, x)
+    ref, ref_payload = O.compress(conf, x)
+    c1, p = O.read_stream(stream)
+    c2, _ = O.read_stream(ref)
+    assert (c1.cmprAlgo, c1.alpha, c1.beta) == (c2.cmprAlgo, c2.alpha, c2.beta)
+    if c1.cmprAlgo == 0 and len(dims) == 3:
+        assert mask_fast_frontend_padding(p, x.itemsize) == mask_fast_frontend_padding(ref_payload, x.itemsize)
+    else:
+        assert p == ref_payload
+
+
 @pytest.mark.parametrize("ab", [1, 2])
 def test_gpu_ablist_matches_oracle(ab):
     """abList 1 / 2: the alpha list runs to 2.5 / 3."""
