@@ -382,18 +382,19 @@ void append_tree(std::vector<uint8_t> &o, const Codebook &cb, uint64_t nbytes) {
 
 namespace {
 
-// Huffman stage and payload assembly of an interpolation compression whose
-// codes (stream order) and unpredictable values (at their code positions in
-// scratch) are on the device: the bytes SZInterpolationCompressor::compress
-// hands to zstd (SZInterpolationCompressor.hpp:485-512, IntegerQuantizer.hpp:
-// 185-201, HuffmanEncoder.hpp:119-137 and 150-227).
+// The Huffman stage of an interpolation compression whose codes (stream order)
+// and unpredictable values (at their code positions in scratch) are on the
+// device: the bit string, and the unpredictable values in stream order.
 template <typename T>
-void interp_payload_tail(const faz_config &c, const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
-                         double eb, int radius, uint64_t n, uint16_t *codes, T *scratch, unsigned long long *vcount,
-                         DevMem &m, cudaStream_t st, Counter &launches, faz_timings &tm, Sink *sink,
-                         uint8_t *&payload, size_t &psize, cudaEvent_t huff_end = nullptr, const int *lerr = nullptr) {
+struct InterpEncoded {
     HuffEncoded he;
-    huffman_encode_device(codes, n, radius, m, st, launches, he, tm);
+    T *unpred = nullptr;
+};
+
+template <typename T>
+void interp_encode(uint64_t n, int radius, uint16_t *codes, T *scratch, unsigned long long *vcount, const int *lerr,
+                   DevMem &m, cudaStream_t st, Counter &launches, faz_timings &tm, InterpEncoded<T> &e) {
+    huffman_encode_device(codes, n, radius, m, st, launches, e.he, tm);
     if (lerr) {
         int le = 0;
         CK(cudaMemcpy(&le, lerr, sizeof(int), cudaMemcpyDeviceToHost));
@@ -404,16 +405,21 @@ void interp_payload_tail(const faz_config &c, const std::vector<uint8_t> &il, co
         CK(cudaMemcpy(&vc, vcount, 8, cudaMemcpyDeviceToHost));
         if (vc) throw Fail{FAZ_ERR_DEVICE, "float fast path disagreed with the double path at " + std::to_string(vc) + " points"};
     }
-    const uint64_t nunpred = he.nzero;
-    const Codebook &cb = he.cb;
-    const uint64_t nbytes = he.nbytes;
-    uint32_t *bits = he.bits;
-    // unpredictable values in stream order
-    T *unpred = m.alloc<T>(nunpred ? nunpred : 1);
-    if (nunpred) launches(launch_compact_zeros<T>(codes, n, he.zc, he.zoff, nullptr, scratch, unpred, st));
-    if (huff_end) CK(cudaEventRecord(huff_end, st));
-    // payload layout (SZInterpolationCompressor.hpp:485-512, IntegerQuantizer.hpp:185-201,
-    // HuffmanEncoder.hpp:119-137 and 150-227)
+    const uint64_t nunpred = e.he.nzero;
+    e.unpred = m.alloc<T>(nunpred ? nunpred : 1);
+    if (nunpred) launches(launch_compact_zeros<T>(codes, n, e.he.zc, e.he.zoff, nullptr, scratch, e.unpred, st));
+}
+
+// The payload of an encoded interpolation compression: the bytes
+// SZInterpolationCompressor::compress hands to zstd (SZInterpolationCompressor.hpp:
+// 485-512, IntegerQuantizer.hpp:185-201, HuffmanEncoder.hpp:119-137 and 150-227).
+template <typename T>
+void interp_emit(const faz_config &c, const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl, double eb,
+                 int radius, const InterpEncoded<T> &e, cudaStream_t st, faz_timings &tm, Sink *sink,
+                 uint8_t *&payload, size_t &psize) {
+    const uint64_t nunpred = e.he.nzero;
+    const Codebook &cb = e.he.cb;
+    const uint64_t nbytes = e.he.nbytes;
     auto th2 = clk::now();
     std::vector<uint8_t> head;
     for (int i = 0; i < c.N; i++) put<uint64_t>(head, c.dims[i]);
@@ -450,14 +456,26 @@ void interp_payload_tail(const faz_config &c, const std::vector<uint8_t> &il, co
     std::memcpy(payload, head.data(), head.size());
     size_t o = head.size();
     tm.host_ms += ms_since(th2);
-    if (nunpred) CK(cudaMemcpyAsync(payload + o, unpred, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
+    if (nunpred) CK(cudaMemcpyAsync(payload + o, e.unpred, nunpred * sizeof(T), cudaMemcpyDeviceToHost, st));
     o += nunpred * sizeof(T);
     std::memcpy(payload + o, tree.data(), tree.size());
     o += tree.size();
-    if (nbytes) CK(cudaMemcpyAsync(payload + o, bits, nbytes, cudaMemcpyDeviceToHost, st));
+    if (nbytes) CK(cudaMemcpyAsync(payload + o, e.he.bits, nbytes, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     tm.unpred_count = nunpred;
     tm.payload_bytes = psize;
+}
+
+// Both stages: the Huffman stage and the payload.
+template <typename T>
+void interp_payload_tail(const faz_config &c, const std::vector<uint8_t> &il, const std::vector<uint8_t> &dl,
+                         double eb, int radius, uint64_t n, uint16_t *codes, T *scratch, unsigned long long *vcount,
+                         DevMem &m, cudaStream_t st, Counter &launches, faz_timings &tm, Sink *sink,
+                         uint8_t *&payload, size_t &psize, cudaEvent_t huff_end = nullptr, const int *lerr = nullptr) {
+    InterpEncoded<T> e;
+    interp_encode<T>(n, radius, codes, scratch, vcount, lerr, m, st, launches, tm, e);
+    if (huff_end) CK(cudaEventRecord(huff_end, st));
+    interp_emit<T>(c, il, dl, eb, radius, e, st, tm, sink, payload, psize);
 }
 
 // The device part of an interpolation compression up to the quantisation
@@ -476,7 +494,9 @@ struct InterpCodes {
     uint16_t *codes = nullptr;
     unsigned long long *vcount = nullptr;
     int *lerr = nullptr;  // set by a level kernel whose bounded wait gave up
-    Events ev_pred, ev_fin;
+    Events ev_pred, ev_fin, ev_huff;
+    InterpEncoded<T> enc;  // the Huffman stage, once interp_encode_codes ran
+    bool encoded = false;
     explicit InterpCodes(cudaStream_t st) : m(st) {}
 };
 
@@ -582,17 +602,26 @@ void interp_levels(InterpCodes<T> &r, faz_config &c, const T *dX, cudaStream_t s
     r.have_levels = !p.lv.empty();
 }
 
-// The Huffman stage and payload of interp_levels' codes.
+// The Huffman stage of interp_levels' codes (the speculative compressions of
+// the SZ3 tuner run it before the tuner's decision).
+template <typename T>
+void interp_encode_codes(InterpCodes<T> &r, cudaStream_t st, faz_timings &tm, Counter &launches) {
+    CK(cudaEventRecord(r.ev_huff.a, st));
+    interp_encode<T>(r.n, r.radius, r.codes, r.scratch, r.vcount, r.lerr, r.m, st, launches, tm, r.enc);
+    CK(cudaEventRecord(r.ev_huff.b, st));
+    r.encoded = true;
+}
+
+// The Huffman stage (unless it ran already) and the payload of
+// interp_levels' codes.
 template <typename T>
 void interp_finish(InterpCodes<T> &r, cudaStream_t st, uint8_t *&payload, size_t &psize, faz_timings &tm,
                    Counter &launches, Sink *sink) {
-    Events ev_huff;
-    CK(cudaEventRecord(ev_huff.a, st));
-    interp_payload_tail<T>(r.c, r.il, r.dl, r.eb, r.radius, r.n, r.codes, r.scratch, r.vcount, r.m, st, launches, tm,
-                           sink, payload, psize, ev_huff.b, r.lerr);
+    if (!r.encoded) interp_encode_codes<T>(r, st, tm, launches);
+    interp_emit<T>(r.c, r.il, r.dl, r.eb, r.radius, r.enc, st, tm, sink, payload, psize);
     tm.predict_ms = r.ev_pred.ms();
     tm.finest_level_ms = r.have_levels ? r.ev_fin.ms() : 0.0;
-    tm.huffman_ms = ev_huff.ms();
+    tm.huffman_ms = r.ev_huff.ms();
 }
 
 template <typename T>

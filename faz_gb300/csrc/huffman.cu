@@ -428,45 +428,6 @@ __device__ __forceinline__ int dec_sym(const DecTables &t, const uint32_t *slut,
     return -1;
 }
 
-// A decoding position with the next 33..64 bits of the segment in a register:
-// short codes (up to LUT_BITS) cost one table lookup and, every 32 bits or so,
-// one word load, instead of three segment loads per symbol.
-struct BitCursor {
-    uint64_t buf;  // upcoming bits, MSB first; the top nb are valid
-    int nb;        // 33..64 after every step
-    uint32_t w;    // next segment word to load
-    uint32_t p;    // segment bit position of buf's first bit
-};
-
-__device__ __forceinline__ void cursor_at(BitCursor &c, const uint32_t *sw, uint32_t p) {
-    const uint32_t w = p >> 5, b = p & 31;
-    c.buf = (((uint64_t)sw[w] << 32) | sw[w + 1]) << b;
-    c.nb = 64 - (int)b;
-    c.w = w + 2;
-    c.p = p;
-}
-
-// one symbol at the cursor (its state, or -1 on a damaged tree)
-__device__ __forceinline__ int cursor_sym(const DecTables &t, const uint32_t *slut, const uint32_t *sw, BitCursor &c) {
-    const uint32_t e = slut[c.buf >> (64 - LUT_BITS)];
-    if (!(e & DEC_NODE)) {
-        const int len = (int)(e >> 24);
-        c.buf <<= len;
-        c.nb -= len;
-        c.p += len;
-        if (c.nb <= 32) {
-            c.buf |= (uint64_t)sw[c.w++] << (32 - c.nb);
-            c.nb += 32;
-        }
-        return (int)(e & 0xffffff);
-    }
-    // a code longer than the table: walk the tree over a 64-bit window
-    uint32_t p = c.p;
-    const int s = dec_sym(t, slut, sw, p);
-    cursor_at(c, sw, p);
-    return s;
-}
-
 __device__ __forceinline__ uint32_t bswap_w(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
 
 // Stage the CTA's segment (as big-endian words) and the lookup table.
@@ -497,20 +458,19 @@ __global__ void __launch_bounds__(DEC_T) k_decode_spec(DecTables t, const uint32
     if (lim > nbits) lim = nbits;
     const uint32_t start = (uint32_t)(u * DEC_UNIT - g0);
     const uint32_t stop = (uint32_t)(lim - g0);
-    BitCursor cur;
-    cursor_at(cur, sw, start);
+    uint32_t p = start;
     unsigned int c = 0;
     uint16_t *b = bnd + u * DEC_NB;
-    while (cur.p < stop) {
-        if (c < DEC_NB) b[c] = (uint16_t)(cur.p - start);
-        if (cursor_sym(t, slut, sw, cur) < 0) {
+    while (p < stop) {
+        if (c < DEC_NB) b[c] = (uint16_t)(p - start);
+        if (dec_sym(t, slut, sw, p) < 0) {
             atomicExch(err, 1);
             break;
         }
         c++;
     }
     for (unsigned int k = c; k < DEC_NB; k++) b[k] = 0xffff;
-    end[u] = g0 + cur.p;
+    end[u] = g0 + p;
     cnt[u] = c;
 }
 
@@ -554,10 +514,8 @@ __global__ void __launch_bounds__(DEC_T) k_decode_resync(DecTables t, const uint
     unsigned int c = 0;
     bool synced = false;
     int j = 0;  // first speculative boundary not yet passed
-    BitCursor cur;
-    cursor_at(cur, sw, p);
-    while (cur.p < stop) {
-        const uint32_t off = cur.p - nominal;
+    while (p < stop) {
+        const uint32_t off = p - nominal;
         while (j < DEC_NB) {
             uint32_t bj = (bw[j >> 1] >> ((j & 1) * 16)) & 0xffffu;
             if (bj >= off) break;
@@ -568,13 +526,13 @@ __global__ void __launch_bounds__(DEC_T) k_decode_resync(DecTables t, const uint
             synced = true;
             break;
         }
-        if (cursor_sym(t, slut, sw, cur) < 0) {
+        if (dec_sym(t, slut, sw, p) < 0) {
             atomicExch(changed, -1);
             return;
         }
         c++;
     }
-    const uint64_t e = synced ? end_in[u] : g0 + cur.p;
+    const uint64_t e = synced ? end_in[u] : g0 + p;
     start[u] = s_true;
     cnt[u] = c;
     end_out[u] = e;
@@ -596,27 +554,26 @@ __global__ void __launch_bounds__(DEC_T) k_decode_write(DecTables t, const uint3
     const uint64_t g0 = u0 * DEC_UNIT;
     uint64_t lim = (u + 1) * DEC_UNIT;
     if (lim > nbits) lim = nbits;
-    BitCursor cur;
-    cursor_at(cur, sw, (uint32_t)(start[u] - g0));
+    uint32_t p = (uint32_t)(start[u] - g0);
     const uint32_t stop = (uint32_t)(lim - g0);
     uint64_t o = off[u];
     if constexpr (sizeof(C) != 2) {  // wide codes: one store per symbol
-        while (cur.p < stop && o < nout) {
-            int s = cursor_sym(t, slut, sw, cur);
+        while (p < stop && o < nout) {
+            int s = dec_sym(t, slut, sw, p);
             if (s < 0) return;
             out[o++] = (C)(s + offset);
         }
     } else {
     // 2-byte stores up to a 16-byte boundary, then 8 symbols per store
-    while (cur.p < stop && o < nout && (o & 7)) {
-        int s = cursor_sym(t, slut, sw, cur);
+    while (p < stop && o < nout && (o & 7)) {
+        int s = dec_sym(t, slut, sw, p);
         if (s < 0) return;
         out[o++] = (C)(s + offset);
     }
     uint32_t pk[4];
     int k = 0;
-    while (cur.p < stop && o + k < nout) {
-        int s = cursor_sym(t, slut, sw, cur);
+    while (p < stop && o + k < nout) {
+        int s = dec_sym(t, slut, sw, p);
         if (s < 0) break;
         uint32_t v = (uint32_t)(uint16_t)(s + offset);
         if (k & 1) pk[k >> 1] |= v << 16;
