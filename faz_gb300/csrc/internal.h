@@ -219,7 +219,12 @@ struct Zstd {
     size_t (*freeCCtx)(void *) = nullptr;
     size_t (*setParameter)(void *, int, int) = nullptr;
     size_t (*compress2)(void *, void *, size_t, const void *, size_t) = nullptr;
+    // ZSTD_compress on a caller's context (the same frame); null if absent
+    size_t (*compressCCtx)(void *, void *, size_t, const void *, size_t, int) = nullptr;
 };
+// ZSTD_compress at level 3 with this thread's reused context and output
+// buffer (no allocation per call); returns the frame size
+size_t zstd_level3_size(const Zstd &z, const void *src, size_t n);
 
 // How the body of a Lossless_zstd stream (one level-3 frame in the reference,
 // include/QoZ/lossless/Lossless_zstd.hpp:22-32) is written:

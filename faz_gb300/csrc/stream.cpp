@@ -393,10 +393,42 @@ const Zstd &zstd_lib(std::string &err) {
         z.freeCCtx = (size_t(*)(void *))dlsym(h, "ZSTD_freeCCtx");
         z.setParameter = (size_t(*)(void *, int, int))dlsym(h, "ZSTD_CCtx_setParameter");
         z.compress2 = (size_t(*)(void *, void *, size_t, const void *, size_t))dlsym(h, "ZSTD_compress2");
+        z.compressCCtx = (size_t(*)(void *, void *, size_t, const void *, size_t, int))dlsym(h, "ZSTD_compressCCtx");
         z.ok = true;
     });
     if (!z.ok) err = load_err;
     return z;
+}
+
+// The tuner's trials need the size of the frame ZSTD_compress writes for
+// each trial payload; ZSTD_compressCCtx writes the same frame with a context
+// that this thread keeps, and the output goes to a buffer it keeps too (a
+// fresh context and a zero-filled buffer per call cost more than the
+// compression of a small payload).
+size_t zstd_level3_size(const Zstd &z, const void *src, size_t n) {
+    struct Scratch {
+        const Zstd *z = nullptr;
+        void *cctx = nullptr;
+        std::unique_ptr<uint8_t[]> buf;
+        size_t cap = 0;
+        ~Scratch() {
+            if (cctx && z && z->freeCCtx) z->freeCCtx(cctx);
+        }
+    };
+    thread_local Scratch s;
+    const size_t need = z.bound(n) + 1;
+    if (need > s.cap) {
+        s.buf.reset(new uint8_t[need]);
+        s.cap = need;
+    }
+    if (z.compressCCtx && z.createCCtx && z.freeCCtx) {
+        if (!s.cctx) {
+            s.cctx = z.createCCtx();
+            s.z = &z;
+        }
+        if (s.cctx) return z.compressCCtx(s.cctx, s.buf.get(), s.cap, src, n, 3);
+    }
+    return z.compress(s.buf.get(), s.cap, src, n, 3);
 }
 
 int zstd_threads() {

@@ -182,8 +182,7 @@ size_t zstd_framed_size(const uint8_t *p, size_t n) {
     std::string err;
     const Zstd &z = zstd_lib(err);
     if (!z.ok) throw Fail{FAZ_ERR_ZSTD, err};
-    std::vector<uint8_t> tmp(z.bound(n) + 1);
-    size_t zs = z.compress(tmp.data(), tmp.size(), p, n, 3);
+    size_t zs = zstd_level3_size(z, p, n);
     if (z.isError(zs)) throw Fail{FAZ_ERR_ZSTD, "ZSTD_compress failed"};
     return zs + 8;
 }
@@ -378,7 +377,10 @@ struct Trial {
     template <typename F>
     void start(cudaEvent_t ready, F body) {
         size = TaskThreads::get().submit<size_t>([this, ready, body]() -> size_t {
-            std::vector<uint8_t> pl;
+            // the payload buffer stays with the (persistent) thread, so that
+            // a few MB are not allocated and faulted in again for each trial
+            thread_local std::vector<uint8_t> pl;
+            pl.clear();
             bool reported = false;
             size_t early = 0;
             auto report = [&](size_t n) {
