@@ -192,37 +192,49 @@ __global__ void __launch_bounds__(FW * 32, 2)
                 for (int i = lane; i < hh1 * h2; i += 32, lc.next())
                     Xs[2 * lc.outer * FX + 2 * lc.inner] = cp[lc.outer * FC + lc.inner];
             } else {
-                // sweep 1: targets (m0, 2e1, 2e2) from the coarse planes
+                // sweep 1: targets (m0, 2e1, 2e2) from the coarse planes; first
+                // the lines this block emits (stream rank = flat index x t0 +
+                // rank in the line), then those on its first planes, which the
+                // previous blocks emit (recomputed in compression, decoded from
+                // their owners' streams in decompression)
                 const Stencil<float> S1 = make_stencil<float>(m0, n0, cubic, FC * FC, 1);
                 const int rk0 = line_rank(m0, n0, cubic);
+                const int ne = g.ne1 * g.ne2;
                 LineCursor lc;
-                lc.init(lane, 32, h2);
-                const int cnt = hh1 * h2;
-                for (int i0 = 0; i0 < cnt; i0 += 32, lc.next()) {
-                    const bool in = i0 + lane < cnt;
-                    const int e1 = in ? lc.outer : 0, e2 = in ? lc.inner : 0;
+                if (ne > 0) lc.init(lane, 32, g.ne2);
+                for (int i0 = 0; i0 < ne; i0 += 32, lc.next()) {
+                    const int i = i0 + lane;
+                    const bool in = i < ne;
+                    const int e1 = k1 + (in ? lc.outer : 0), e2 = k2 + (in ? lc.inner : 0);
                     const float pred = eval_stencil<CUB>(S1, C + e1 * FC + e2);
-                    const bool emit = e1 >= k1 && e2 >= k2;
-                    const int rank = ((e1 - k1) * g.ne2 + (e2 - k2)) * g.t0 + rk0;
+                    const int rank = (in ? i : 0) * g.t0 + rk0;
+                    float *xp = Xs + 2 * e1 * FX + 2 * e2;
+                    float v;
+                    if (!DECOMP) v = finest_point(*xp, pred, a, in, stage + sh1 + rank, ub + rank);
+                    else v = recover_point<float, 1>(pred, (int)stage[sh1 + rank], base + rank, a, zpos, nz, unpred);
+                    if (in) *xp = v;
+                }
+                const int nfirst = k1 * h2 + k2 * (hh1 - k1);
+                for (int j0 = 0; j0 < nfirst; j0 += 32) {
+                    const int j = j0 + lane;
+                    const bool in = j < nfirst;
+                    int e1 = 0, e2 = 0;
+                    if (in) {
+                        if (j < k1 * h2) e2 = j;
+                        else e1 = k1 + (j - k1 * h2);
+                    }
+                    const float pred = eval_stencil<CUB>(S1, C + e1 * FC + e2);
                     float *xp = Xs + 2 * e1 * FX + 2 * e2;
                     float v;
                     if (!DECOMP) {
-                        v = finest_point(*xp, pred, a, in && emit, stage + sh1 + rank, ub + rank);
+                        v = finest_point(*xp, pred, a, false, nullptr, nullptr);
                     } else {
-                        uint64_t pos;
-                        int code;
-                        if (emit) {
-                            pos = base + rank;
-                            code = stage[sh1 + rank];
-                        } else {
-                            pos = owner_pos_sweep1(a, g, bc, P1, a.perm[2], e1, e2, n2) + rk0;
-                            if (pos >= a.ncodes) {
-                                atomicExch(a.err, 1);
-                                pos = 0;
-                            }
-                            code = codes[pos];
+                        uint64_t pos = owner_pos_sweep1(a, g, bc, P1, a.perm[2], e1, e2, n2) + rk0;
+                        if (pos >= a.ncodes) {
+                            atomicExch(a.err, 1);
+                            pos = 0;
                         }
-                        v = recover_point<float, 1>(pred, code, pos, a, zpos, nz, unpred);
+                        v = recover_point<float, 1>(pred, (int)codes[pos], pos, a, zpos, nz, unpred);
                     }
                     if (in) *xp = v;
                 }
@@ -235,17 +247,20 @@ __global__ void __launch_bounds__(FW * 32, 2)
                 const Stencil<float> S2 = make_stencil<float>(m1, n1, cubic, FX, 0);
                 const int rk1 = line_rank(m1, n1, cubic);
                 const int pb = (int)g.c1 + (m0 - k0) * g.ne2 * g.t1 + rk1 - k2 * g.t1;
-                // decompression: stream position of column e2 (its owner's for a
-                // first-plane column), and its code loaded one column ahead
+                // decompression: stream position of column e2 (for the first-plane
+                // column, its owner's: the previous block along P2), and its code
+                // loaded one column ahead
+                uint64_t own = 0;
+                if (DECOMP && k2) {
+                    own = owner_pos_sweep2(a, g, bc, a.perm[2], m0 - k0) + rk1;
+                    if (own >= a.ncodes) {
+                        atomicExch(a.err, 1);
+                        own = 0;
+                    }
+                }
                 auto dpos = [&](int e2) -> uint64_t {
                     const int ec = e2 < h2 ? e2 : h2 - 1;
-                    if (ec >= k2) return base + (uint64_t)(pb + ec * g.t1);
-                    uint64_t pos = owner_pos_sweep2(a, g, bc, a.perm[2], m0 - k0) + rk1;
-                    if (pos >= a.ncodes) {
-                        atomicExch(a.err, 1);
-                        pos = 0;
-                    }
-                    return pos;
+                    return ec >= k2 ? base + (uint64_t)(pb + ec * g.t1) : own;
                 };
                 uint64_t npos = 0;
                 int ncode = a.radius;
@@ -309,11 +324,12 @@ __global__ void __launch_bounds__(FW * 32, 2)
                 // (written by earlier levels) left alone
                 __syncwarp();
                 float *dst = wb + (int64_t)m0 * G0;
-                LineCursor lc;
-                lc.init(lane, 32, w2);  // outer = row - k1, inner = column - k2
-                for (int i = lane; i < w1 * w2; i += 32, lc.next()) {
-                    const int m1 = k1 + lc.outer, m2 = k2 + lc.inner;
-                    if ((m0 | m1 | m2) & 1) dst[(int64_t)m1 * G1 + m2] = Xs[m1 * FX + m2];
+                for (int m1 = k1; m1 < n1; m1++) {
+                    float *drow = dst + (int64_t)m1 * G1;
+                    const float *srow = Xs + m1 * FX;
+                    const bool odd_row = (m0 | m1) & 1;  // no coarse point in the row
+                    for (int m2 = k2 + lane; m2 < n2; m2 += 32)
+                        if (odd_row || (m2 & 1)) drow[m2] = srow[m2];
                 }
             }
         }
