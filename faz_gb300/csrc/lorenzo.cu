@@ -208,9 +208,40 @@ __device__ __forceinline__ void lor_st_release(unsigned *p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// The original values of block (bi, bj, bk) into the warp's tile (after its
+// (bs + 2)^3 halo part); they depend on no other block, so the persistent
+// kernel loads them before it waits for the block's neighbours.
+template <typename T>
+__device__ __forceinline__ void lor_load_x(const LorArgs &a, int64_t bi, int64_t bj, int64_t bk, T *t,
+                                           const T *__restrict__ X) {
+    const int lane = threadIdx.x & 31;
+    const int bs = a.bs;
+    const int sx = (bi + 1) * bs < a.d1 ? bs : (int)(a.d1 - bi * bs);
+    const int sy = (bj + 1) * bs < a.d2 ? bs : (int)(a.d2 - bj * bs);
+    const int sz = (bk + 1) * bs < a.d3 ? bs : (int)(a.d3 - bk * bs);
+    const int64_t x0 = bi * bs, y0 = bj * bs, z0 = bk * bs;
+    const int64_t d0 = a.d2 * a.d3, dd1 = a.d3;
+    T *xs = t + (bs + 2) * (bs + 2) * (bs + 2);
+    const int nv = sx * sy * sz;
+    for (int e0 = lane; e0 < nv; e0 += 32 * kLorBatch) {
+        T v[kLorBatch];
+#pragma unroll
+        for (int u = 0; u < kLorBatch; u++) {
+            const int e = e0 + 32 * u;
+            const int i = e / (sy * sz), r = e - i * sy * sz, j = r / sz, k = r - j * sz;
+            v[u] = e < nv ? X[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)] : (T)0;
+        }
+#pragma unroll
+        for (int u = 0; u < kLorBatch; u++)
+            if (e0 + 32 * u < nv) xs[e0 + 32 * u] = v[u];
+    }
+}
+
 // One block (bi, bj, bk), one warp: the (bs + 2)^3 tile with its two-deep
 // halo of reconstructed values, then the point diagonals i + j + k = s in
-// order, each point predicted from its reconstructed neighbours.
+// order, each point predicted from its reconstructed neighbours (in
+// compression the block's original values are already in the tile:
+// lor_load_x).
 template <typename T, bool DECOMP, int QM, typename C>
 __device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t bj, int64_t bk, T *t,
                                           const T *__restrict__ X, T *__restrict__ R, C *__restrict__ codes,
@@ -242,21 +273,6 @@ __device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t 
 #pragma unroll
         for (int u = 0; u < kLorBatch; u++)
             if (e0 + 32 * u < tn) t[e0 + 32 * u] = v[u];
-    }
-    if (!DECOMP) {
-        const int nv = sx * sy * sz;
-        for (int e0 = lane; e0 < nv; e0 += 32 * kLorBatch) {
-            T v[kLorBatch];
-#pragma unroll
-            for (int u = 0; u < kLorBatch; u++) {
-                const int e = e0 + 32 * u;
-                const int i = e / (sy * sz), r = e - i * sy * sz, j = r / sz, k = r - j * sz;
-                v[u] = e < nv ? X[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)] : (T)0;
-            }
-#pragma unroll
-            for (int u = 0; u < kLorBatch; u++)
-                if (e0 + 32 * u < nv) xs[e0 + 32 * u] = v[u];
-        }
     }
     __syncwarp();
     int sel = ind[(bi * a.ny + bj) * a.nz + bk];
@@ -332,6 +348,8 @@ __global__ void __launch_bounds__(kLorWarps * 32)
         const int64_t bk = b % a.nz, bj = (b / a.nz) % a.ny, bi = b / plane;
         const unsigned *deps[3] = {bi > 0 ? done + (b - plane) : nullptr, bj > 0 ? done + (b - a.nz) : nullptr,
                                    bk > 0 ? done + (b - 1) : nullptr};
+        // the block's own values need no neighbour: their loads overlap the wait
+        if (!DECOMP) lor_load_x<T>(a, bi, bj, bk, t, X);
         if (lane == 0) {
             for (int d = 0; d < 3; d++) {
                 if (!deps[d]) continue;
