@@ -20,9 +20,13 @@
 // sweep-2 and sweep-3 codes of a plane are contiguous and go straight to
 // global memory, 32 bytes per half-warp.
 //
-// Requirements (checked by launch_finest): float data on the exact float
-// quantiser path, P2 the contiguous axis, block edge <= 32, a 3-D field below
-// 2^31 values whose rows are 16-byte multiples (the TMA's global strides).
+// Requirements (finest_eligible): float data on the exact float quantiser
+// path, P2 the contiguous axis, a block edge that is a multiple of 4 up to 32
+// (block begins along P2 are TMA x coordinates, 16-byte multiples), a 3-D
+// field below 2^31 values whose rows are 16-byte multiples (the tensor map's
+// strides).  The compression uses this kernel; the decompression variant
+// (codes in, the plane written back row by row) is correct but slower than
+// the block kernel and runs only with FAZ_FINEST_PLANES=2 (interp.cu).
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -178,7 +182,11 @@ __global__ void __launch_bounds__(FW * 32, 2)
             }
             if (!DECOMP) {
                 if (!tma_wait(bar, phase)) {
+                    // the call fails; wait (bounded again) for the copy in flight
+                    // before the warp leaves, so that it does not land in shared
+                    // memory that another CTA may own by then
                     if (lane == 0 && a.err) atomicExch(a.err, 1);
+                    (void)tma_wait(bar, phase);
                     ok = false;
                     break;
                 }
