@@ -36,6 +36,7 @@ Under torchrun every rank compresses its own field (independent replicas,
 weak scaling); rank 0 prints the line.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -428,11 +429,12 @@ HELD_OUT_FIELDS = 256  # held-out fields of the training distribution (seed outs
 
 
 def learned_vs_sampled(x, dims, eb):
-    """The learned tuner against the sampled QoZ autotune, end to end through
-    compress_device (tuning + compression + zstd, host clock): on this field
-    and on held-out synthetic fields of the training distribution (128^3 to
-    256^3, spectral slope -4..-2, anisotropy up to 8, 0-5 % noise, optional
-    flat boxes, relative bounds 1e-4..1e-2; a seed outside the training set)."""
+    """The learned tuner against the sampled QoZ autotune, end to end (tuning +
+    compression + zstd, host clock): on this field through faz_compress_device
+    (the C ABI), and on held-out synthetic fields of the training distribution
+    (128^3 to 256^3, spectral slope -4..-2, anisotropy up to 8, 0-5 % noise,
+    optional flat boxes, relative bounds 1e-4..1e-2; a seed outside the
+    training set) through the Python API."""
     import faz_gb300 as F
     import faz_gb300.learned as L
     import torch
@@ -440,12 +442,31 @@ def learned_vs_sampled(x, dims, eb):
         return None
     model = L.TunerModel.load()
     qc = L.qoz_conf(dims, eb)
-    t_plain, s_plain = L._timed(lambda: F.compress_device(qc, x), 2)
+
+    def c_compress(conf):
+        # faz_compress_device through the C ABI; the stream stays in the
+        # library's buffer (the Python wrapper would copy its 84 MB into a
+        # bytes object, ~10 ms on one host core, in both arms alike)
+        s = conf.to_struct()
+        out, osz, tm = ctypes.c_void_p(), ctypes.c_size_t(), F.FazTimings()
+        lib = F.library()
+        rc = lib.faz_compress_device(ctypes.byref(s), F.FAZ_FLOAT, ctypes.c_void_p(x.data_ptr()),
+                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), ctypes.byref(out),
+                                     ctypes.byref(osz), ctypes.byref(tm))
+        if rc:
+            raise F.FazError(rc, lib.faz_last_error().decode())
+        lib.faz_free(out)
+        return osz.value
+
+    t_plain, n_plain = L._timed(lambda: c_compress(qc), 2)
 
     def learned():
         tuned, info = L.learned_tune(qc, x, model)
-        return F.compress_device(tuned, x), info
-    t_learn, (s_learn, info) = L._timed(learned, 3)
+        return c_compress(tuned), info
+    t_learn, (n_learn, info) = L._timed(learned, 3)
+    # the streams themselves (untimed)
+    s_plain = F.compress_device(qc, x)
+    s_learn = F.compress_device(L.learned_tune(qc, x, model)[0], x)
     nbytes = x.numel() * x.element_size()
     # the network alone: features + tensor-core MLP on this field
     f = L.features(qc, x)
