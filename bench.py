@@ -45,6 +45,10 @@ import sys
 import tempfile
 import time
 
+# 32 hardware work queues for the autotune's concurrent trial streams (read
+# when the CUDA context is created; faz_gb300 sets the same default)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 

@@ -297,59 +297,112 @@ template <typename C>
 void huffman_encode_impl(const C *codes, uint64_t n, int center, DevMem &m, cudaStream_t st, Counter &launches,
                          HuffEncoded &h, faz_timings &tm, const std::function<void(const HuffEncoded &)> &sized) {
     const uint64_t nsub = hist_subchunks(n);
+    const uint64_t nech = encode_chunks(n);
     // every value a code of this width can take
     const int nsym = sizeof(C) == 2 ? 65536 : std::max(65536, 2 * center + 1);
-    unsigned long long *hist = m.alloc<unsigned long long>(nsym);
-    unsigned long long *first = m.alloc<unsigned long long>(nsym);
-    h.zc = m.alloc<unsigned long long>(nsub + 1);
-    h.zoff = m.alloc<unsigned long long>(nsub + 1);
-    unsigned long long *stmp = m.alloc<unsigned long long>(scan_temp_words(std::max<uint64_t>(nsub, encode_chunks(n))) + 1);
-    CK(cudaMemsetAsync(hist, 0, nsym * 8, st));
-    CK(cudaMemsetAsync(first, 0xff, nsym * 8, st));
+    // the symbols that occur come back as a compact list (the first
+    // kListHead entries with the count, the rest, if any, in a second copy);
+    // at most min(nsym, n) symbols occur, and the head copy reads kListHead
+    constexpr size_t kListHead = 2048;
+    const size_t list_cap = std::max<size_t>(std::min<uint64_t>((uint64_t)nsym, n), kListHead);
+    // One allocation holds the work arrays (CUDA calls are few: the tuners
+    // run several of these encodes on concurrent host threads, whose calls
+    // serialise in the driver).  In 8-byte words, each part 256-byte aligned:
+    // histogram + list count, first positions, zero counts and offsets, scan
+    // scratch, list, codebook tables (stateNum <= nsym + 1 entries of 17
+    // bytes), chunk bit counts and offsets.
+    auto up = [](uint64_t w) { return (w + 31) & ~(uint64_t)31; };
+    const uint64_t w_hist = up((uint64_t)nsym + 1), w_first = up((uint64_t)nsym), w_z = up(nsub + 1),
+                   w_tmp = up(scan_temp_words(std::max<uint64_t>(nsub, nech)) + 1), w_list = up(3 * list_cap),
+                   w_tab = up(((uint64_t)nsym + 1) * 17 / 8 + 1), w_ch = up(nech + 1);
+    unsigned long long *work =
+        m.alloc<unsigned long long>(w_hist + w_first + 2 * w_z + w_tmp + w_list + w_tab + 2 * w_ch);
+    unsigned long long *hist = work;
+    unsigned int *dnl = reinterpret_cast<unsigned int *>(hist + nsym);
+    unsigned long long *first = hist + w_hist;
+    h.zc = first + w_first;
+    h.zoff = h.zc + w_z;
+    unsigned long long *stmp = h.zoff + w_z;
+    unsigned long long *dlist = stmp + w_tmp;
+    uint8_t *dtab = reinterpret_cast<uint8_t *>(dlist + w_list);
+    unsigned long long *cbits = dlist + w_list + w_tab;
+    unsigned long long *coff = cbits + w_ch;
+    CK(cudaMemsetAsync(hist, 0, ((size_t)nsym + 1) * 8, st));
+    CK(cudaMemsetAsync(first, 0xff, (size_t)nsym * 8, st));
     launches(launch_histogram(codes, n, center, hist, first, h.zc, st));
     launches(launch_scan_u64(h.zc, h.zoff, nsub, stmp, st));
-    uint8_t *hb = t_pin_small.get((size_t)nsym * 16 + 8);
-    CK(cudaMemcpyAsync(hb, hist, nsym * 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(hb + nsym * 8, first, nsym * 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(hb + nsym * 16, h.zoff + nsub, 8, cudaMemcpyDeviceToHost, st));
+    launches(launch_hist_compact(hist, first, nsym, dlist, dnl, st));
+    uint8_t *hb = t_pin_small.get(16 + kListHead * 24);
+    CK(cudaMemcpyAsync(hb, dnl, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hb + 8, h.zoff + nsub, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hb + 16, dlist, kListHead * 24, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (tune_trace()) {
+        char msg[96];
+        std::snprintf(msg, sizeof(msg), "huffman histogram of %llu codes on the host", (unsigned long long)n);
+        trace_step(msg);
+    }
     auto th1 = clk::now();
-    const unsigned long long *hh = (const unsigned long long *)hb;
-    const unsigned long long *hf = (const unsigned long long *)(hb + nsym * 8);
-    std::memcpy(&h.nzero, hb + nsym * 16, 8);
-    std::vector<int> syms;
-    std::vector<uint64_t> cnts, firsts;
-    for (int s = 0; s < nsym; s++)
-        if (hh[s]) {
-            syms.push_back(s);
-            cnts.push_back(hh[s]);
-            firsts.push_back(hf[s]);
-        }
+    unsigned int nl = 0;
+    std::memcpy(&nl, hb, 4);
+    std::memcpy(&h.nzero, hb + 8, 8);
+    if (nl > (unsigned int)nsym || nl > list_cap)
+        throw Fail{FAZ_ERR_DEVICE, "histogram list longer than the symbol range"};
+    std::vector<unsigned long long> rest;
+    if (nl > kListHead) {
+        rest.resize(3 * (size_t)(nl - kListHead));
+        CK(cudaMemcpyAsync(rest.data(), dlist + 3 * kListHead, rest.size() * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    std::vector<int> syms(nl);
+    std::vector<uint64_t> cnts(nl), firsts(nl);
+    const unsigned long long *head = (const unsigned long long *)(hb + 16);
+    for (unsigned int k = 0; k < nl; k++) {
+        const unsigned long long *e = k < kListHead ? head + 3 * (size_t)k : rest.data() + 3 * (size_t)(k - kListHead);
+        syms[k] = (int)e[0];
+        cnts[k] = e[1];
+        firsts[k] = e[2];
+    }
+    trace_step("huffman symbols listed");
     std::string err;
     int rc = build_codebook(syms, cnts, firsts, h.cb, err);
     if (rc) throw Fail{rc, err};
+    trace_step("huffman tree built");
     tm.host_ms += ms_since(th1);
     const Codebook &cb = h.cb;
-    unsigned long long *dcode = m.alloc<unsigned long long>(cb.stateNum);
-    unsigned long long *dpacked = m.alloc<unsigned long long>(cb.stateNum);
-    uint8_t *dlen = m.alloc<uint8_t>(cb.stateNum);
-    std::vector<unsigned long long> packed(cb.stateNum);
-    for (int i = 0; i < cb.stateNum; i++) {
+    // The three tables (MSB-aligned codes, packed length|code, lengths) go
+    // up in one copy from the thread's pinned staging: pageable copies from
+    // several threads serialise in the driver.  The staging is refilled once
+    // the thread's previous upload from it has completed.
+    const size_t S = (size_t)cb.stateNum;
+    if (S > (size_t)nsym + 1) throw Fail{FAZ_ERR_DEVICE, "Huffman codebook larger than the symbol range"};
+    TableStage &ts = t_table_stage;
+    uint8_t *htab = ts.acquire(S * 17);
+    unsigned long long *hcode = reinterpret_cast<unsigned long long *>(htab);
+    unsigned long long *hpacked = hcode + S;
+    std::memcpy(hcode, cb.code.data(), S * 8);
+    for (size_t i = 0; i < S; i++) {
         const int l = cb.len[i];
-        packed[i] = ((unsigned long long)l << 32) | (l >= 1 && l <= 32 ? (cb.code[i] >> (64 - l)) : 0ull);
+        hpacked[i] = ((unsigned long long)l << 32) | (l >= 1 && l <= 32 ? (cb.code[i] >> (64 - l)) : 0ull);
     }
-    CK(cudaMemcpyAsync(dcode, cb.code.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(dpacked, packed.data(), cb.stateNum * 8, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(dlen, cb.len.data(), cb.stateNum, cudaMemcpyHostToDevice, st));
+    std::memcpy(htab + S * 16, cb.len.data(), S);
+    CK(cudaMemcpyAsync(dtab, htab, S * 17, cudaMemcpyHostToDevice, st));
+    ts.release(st);
+    unsigned long long *dcode = reinterpret_cast<unsigned long long *>(dtab);
+    unsigned long long *dpacked = dcode + S;
+    uint8_t *dlen = dtab + S * 16;
+    trace_step("huffman tables uploaded");
     // the encoded size from the counts and code lengths (what the device's
     // chunk scan adds up)
     uint64_t total_bits = 0;
     for (size_t i = 0; i < syms.size(); i++) total_bits += cnts[i] * (uint64_t)cb.len[syms[i] - cb.offset];
     h.nbytes = (total_bits + 7) / 8;
+    if (tune_trace()) {
+        char msg[96];
+        std::snprintf(msg, sizeof(msg), "huffman codebook of %llu codes built", (unsigned long long)n);
+        trace_step(msg);
+    }
     if (sized) sized(h);
-    const uint64_t nech = encode_chunks(n);
-    unsigned long long *cbits = m.alloc<unsigned long long>(nech + 1);
-    unsigned long long *coff = m.alloc<unsigned long long>(nech + 1);
     launches(launch_encode_bits(codes, n, cb.offset, dlen, cbits, st));
     launches(launch_scan_u64(cbits, coff, nech, stmp, st));
     const uint64_t nwords = (total_bits + 31) / 32 + 1;

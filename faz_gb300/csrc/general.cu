@@ -830,7 +830,7 @@ void gen_compress_payload(int N, const uint64_t *dims, int bs, int lo, int lo2, 
         }
     }
     CK(cudaStreamSynchronize(st));
-    out.assign(pin, pin + total);
+    emit_payload(out, pin, total);
     tm.unpred_count = nunpred;
     tm.payload_bytes = total;
     tm.predict_ms += ev_pred.ms();

@@ -12,6 +12,7 @@
 #include <future>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
@@ -27,6 +28,24 @@ namespace faz {
 
 using clk = std::chrono::steady_clock;
 inline double ms_since(clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); }
+
+// FAZ_TUNE_TRACE=1 prints the tuner's timeline to stderr: milliseconds since
+// the current tuning call began (trace_epoch), from whichever thread runs the
+// step.
+inline bool tune_trace() {
+    static const bool on = [] {
+        const char *e = std::getenv("FAZ_TUNE_TRACE");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+inline clk::time_point &trace_epoch() {
+    static clk::time_point t0 = clk::now();
+    return t0;
+}
+inline void trace_step(const char *what) {
+    if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s\n", ms_since(trace_epoch()), what);
+}
 
 struct Fail {
     int code;
@@ -94,6 +113,60 @@ struct Pinned {
 };
 inline thread_local Pinned t_pin_payload;
 inline thread_local Pinned t_pin_small;
+inline thread_local Pinned t_pin_flag;  // device status words read after a later synchronisation
+
+// Pinned staging for host-to-device uploads whose copies complete after the
+// call returns: acquire() waits for the thread's previous upload from it,
+// release(st) marks the new one (an event recorded on st).
+struct TableStage {
+    Pinned buf;
+    cudaEvent_t ev = nullptr;
+    int dev = -1;
+    bool pending = false;
+    uint8_t *acquire(size_t n) {
+        if (pending) CK(cudaEventSynchronize(ev));
+        pending = false;
+        return buf.get(n);
+    }
+    void release(cudaStream_t st) {
+        int d = 0;
+        CK(cudaGetDevice(&d));
+        if (ev && d != dev) {
+            cudaEventDestroy(ev);
+            ev = nullptr;
+        }
+        if (!ev) {
+            CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            dev = d;
+        }
+        CK(cudaEventRecord(ev, st));
+        pending = true;
+    }
+    ~TableStage() {
+        if (ev) cudaEventDestroy(ev);
+    }
+};
+inline thread_local TableStage t_table_stage;
+
+// Payload producers assemble their bytes in the thread's pinned staging
+// buffer and end with emit_payload: the bytes are copied into `out`, or, while
+// the thread has a view installed (t_payload_view), left where they are, the
+// view pointing at them until the thread assembles its next payload (a
+// tuning trial only measures its payload's zstd size).
+struct PayloadView {
+    const uint8_t *data = nullptr;
+    size_t size = 0;
+};
+inline thread_local PayloadView *t_payload_view = nullptr;
+inline void emit_payload(std::vector<uint8_t> &out, const uint8_t *pin, size_t n) {
+    if (t_payload_view) {
+        t_payload_view->data = pin;
+        t_payload_view->size = n;
+        out.clear();
+        return;
+    }
+    out.assign(pin, pin + n);
+}
 
 // How a call on device buffers reads a NULL stream: the legacy default
 // stream, so that the call is ordered after the caller's default-stream work

@@ -82,6 +82,28 @@ __global__ void __launch_bounds__(1024) k_histogram(const C *__restrict__ codes,
     }
 }
 
+// The symbols of non-zero count, compacted in no particular order:
+// list[3k], list[3k+1], list[3k+2] = symbol, count, first position;
+// *nlist = their number.
+__global__ void __launch_bounds__(256) k_hist_compact(const unsigned long long *__restrict__ hist,
+                                                     const unsigned long long *__restrict__ first, int nsym,
+                                                     unsigned long long *list, unsigned int *nlist) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool nz = s < nsym && hist[s] != 0;
+    const unsigned int m = __ballot_sync(0xffffffffu, nz);
+    if (m == 0) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(nlist, (unsigned int)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (nz) {
+        const unsigned int k = base + (unsigned int)__popc(m & ((1u << lane) - 1u));
+        list[3 * (size_t)k] = (unsigned long long)s;
+        list[3 * (size_t)k + 1] = hist[s];
+        list[3 * (size_t)k + 2] = first[s];
+    }
+}
+
 // Zero-code count per warp sub-chunk (decompress side).
 template <typename C>
 __global__ void __launch_bounds__(1024) k_count_zeros(const C *__restrict__ codes, uint64_t n,
@@ -604,6 +626,12 @@ __global__ void k_widen_counts(const unsigned int *cnt, unsigned long long *out,
 static inline unsigned grid_for(uint64_t n, uint64_t per) { return (unsigned)((n + per - 1) / per); }
 
 uint64_t hist_subchunks(uint64_t n) { return ((n + HCHUNK - 1) / HCHUNK) * HWARPS; }
+
+cudaError_t launch_hist_compact(const unsigned long long *hist, const unsigned long long *first, int nsym,
+                                unsigned long long *list, unsigned int *nlist, cudaStream_t st) {
+    k_hist_compact<<<(unsigned)((nsym + 255) / 256), 256, 0, st>>>(hist, first, nsym, list, nlist);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, int center, unsigned long long *hist,
                              unsigned long long *first, unsigned long long *zcount, cudaStream_t st) {

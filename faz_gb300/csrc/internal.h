@@ -113,6 +113,10 @@ template <typename T, bool WIDE>
 int batch_occupancy(int threads, size_t smem);
 
 uint64_t hist_subchunks(uint64_t n);
+// the symbols of non-zero count: list[3k..3k+2] = symbol, count, first
+// position, in no particular order; *nlist (zeroed by the caller) their number
+cudaError_t launch_hist_compact(const unsigned long long *hist, const unsigned long long *first, int nsym,
+                                unsigned long long *list, unsigned int *nlist, cudaStream_t st);
 // Huffman stage kernels; the uint32_t overloads serve quantisers of more than
 // 65536 bins.
 cudaError_t launch_histogram(const uint16_t *codes, uint64_t n, int center, unsigned long long *hist,

@@ -198,15 +198,18 @@ __device__ __forceinline__ T ld_coherent(const T *p) {
     return __ldcg(p);
 }
 
-__device__ __forceinline__ unsigned lor_ld_acquire(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
 __device__ __forceinline__ void lor_st_release(unsigned *p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+
+__device__ __forceinline__ unsigned lor_ld_relaxed(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// with a relaxed load that saw a release store before it, an acquire pattern
+__device__ __forceinline__ void lor_fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
 // The original values of block (bi, bj, bk) into the warp's tile (after its
 // (bs + 2)^3 halo part); they depend on no other block, so the persistent
@@ -243,10 +246,11 @@ __device__ __forceinline__ void lor_load_x(const LorArgs &a, int64_t bi, int64_t
 // compression the block's original values are already in the tile:
 // lor_load_x).
 template <typename T, bool DECOMP, int QM, typename C>
-__device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t bj, int64_t bk, T *t,
-                                          const T *__restrict__ X, T *__restrict__ R, C *__restrict__ codes,
-                                          T *__restrict__ scratch, const uint16_t *__restrict__ ind,
-                                          const uint64_t *__restrict__ zpos, uint64_t nzp, const T *__restrict__ unpred) {
+__device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t bj, int64_t bk, T *t, int sel,
+                                          const float (&rp)[4], const uint32_t *halo, T *__restrict__ R,
+                                          C *__restrict__ codes, T *__restrict__ scratch,
+                                          const uint64_t *__restrict__ zpos, uint64_t nzp,
+                                          const T *__restrict__ unpred) {
     const int lane = threadIdx.x & 31;
     const int bs = a.bs;
     const int sx = (bi + 1) * bs < a.d1 ? bs : (int)(a.d1 - bi * bs);
@@ -259,6 +263,26 @@ __device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t 
     T *xs = t + (bs + 2) * (bs + 2) * (bs + 2);
     const int tn = (sx + 2) * (sy + 2) * tz;
     // loads in batches of kLorBatch per lane, all issued before any is used
+    if (sx == bs && sy == bs && sz == bs) {
+        // a full block: the halo positions come from the CTA's table
+        const int nh = tn - bs * bs * bs;
+        for (int h0 = lane; h0 < nh; h0 += 32 * kLorBatch) {
+            T v[kLorBatch];
+#pragma unroll
+            for (int u = 0; u < kLorBatch; u++) {
+                const int h = h0 + 32 * u;
+                const uint32_t p = h < nh ? halo[h] : 0u;
+                const int64_t gx = x0 + (int)(p & 15u) - 2, gy = y0 + (int)((p >> 4) & 15u) - 2,
+                              gz = z0 + (int)((p >> 8) & 15u) - 2;
+                v[u] = (h < nh && gx >= 0 && gy >= 0 && gz >= 0) ? ld_coherent(R + (gx * d0 + gy * dd1 + gz)) : (T)0;
+            }
+#pragma unroll
+            for (int u = 0; u < kLorBatch; u++) {
+                const int h = h0 + 32 * u;
+                if (h < nh) t[halo[h] >> 12] = v[u];
+            }
+        }
+    } else
     for (int e0 = lane; e0 < tn; e0 += 32 * kLorBatch) {
         T v[kLorBatch];
 #pragma unroll
@@ -275,23 +299,26 @@ __device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t 
             if (e0 + 32 * u < tn) t[e0 + 32 * u] = v[u];
     }
     __syncwarp();
-    int sel = ind[(bi * a.ny + bj) * a.nz + bk];
-    if (sel == 1 && a.rp == nullptr) sel = 0;  // a stream without coefficients
     const bool two = sel == 2;
     const uint64_t boff = (uint64_t)(bi * bs) * (uint64_t)d0 + (uint64_t)(bj * bs) * (uint64_t)(sx * a.d3) +
                           (uint64_t)(bk * bs) * (uint64_t)(sx * sy);
     const int nsteps = sx + sy + sz - 2;
     const int npairs = sx * sy;
+    // a lane's (i, j) pairs: lane, lane + 32, ... (one pair for edges up to 5)
+    const int i0 = lane / sy, j0 = lane - i0 * sy;
     for (int s = 0; s < nsteps; s++) {
+        int i = i0, j = j0;
         for (int pr = lane; pr < npairs; pr += 32) {
-            const int i = pr / sy, j = pr - i * sy;
+            if (pr != lane) {
+                i = pr / sy;
+                j = pr - i * sy;
+            }
             const int k = s - i - j;
             if (k < 0 || k >= sz) continue;
             T *c = t + (i + 2) * tx + (j + 2) * ty + (k + 2);
             T pred;
             if (sel == 1) {
                 // regression_predict_quantize_3d (MetaRegressionPredictor.hpp:148-189)
-                const float *rp = a.rp + 4 * ((bi * a.ny + bj) * a.nz + bk);
                 pred = (T)(rp[0] * (float)i + rp[1] * (float)j + rp[2] * (float)k + rp[3]);
             } else {
                 pred = lor_pred(c, tx, ty, a.pd, two);
@@ -308,12 +335,9 @@ __device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t 
                 v = recover_point<T, QM>(pred, (int)codes[pos], pos, a.q, zpos, nzp, unpred);
             }
             *c = v;
+            R[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)] = v;
         }
         __syncwarp();
-    }
-    for (int e = lane; e < sx * sy * sz; e += 32) {
-        const int i = e / (sy * sz), r = e - i * sy * sz, j = r / sz, k = r - j * sz;
-        R[(x0 + i) * d0 + (y0 + j) * dd1 + (z0 + k)] = t[(i + 2) * tx + (j + 2) * ty + (k + 2)];
     }
 }
 
@@ -338,37 +362,68 @@ __global__ void __launch_bounds__(kLorWarps * 32)
     const int bs = a.bs;
     const int tstride = (bs + 2) * (bs + 2) * (bs + 2) + (DECOMP ? 0 : bs * bs * bs);
     T *t = reinterpret_cast<T *>(lor_smem) + (size_t)w * (size_t)tstride;
+    // The halo positions of a full block's tile (i < 2, j < 2 or k < 2 in the
+    // (bs + 2)^3 tile), packed i | j << 4 | k << 8 | tile index << 12, in tile
+    // order: entry = tile index - interior points before it.
+    uint32_t *halo = reinterpret_cast<uint32_t *>(lor_smem + (size_t)kLorWarps * (size_t)tstride * sizeof(T));
+    {
+        const int te = bs + 2, tn = te * te * te;
+        for (int e = threadIdx.x; e < tn; e += blockDim.x) {
+            const int i = e / (te * te), j = (e / te) % te, k = e % te;
+            if (i >= 2 && j >= 2 && k >= 2) continue;
+            int before = (i > 2 ? i - 2 : 0) * bs * bs;
+            if (i >= 2) before += (j > 2 ? j - 2 : 0) * bs;
+            if (i >= 2 && j >= 2) before += k > 2 ? k - 2 : 0;
+            halo[e - before] = (uint32_t)i | ((uint32_t)j << 4) | ((uint32_t)k << 8) | ((uint32_t)e << 12);
+        }
+        __syncthreads();
+    }
     const int64_t plane = a.ny * a.nz;
+    // A warp takes its next ticket as it starts a block, so that the atomic's
+    // round trip overlaps the block.  The smallest unfinished ticket is then
+    // always some warp's current block (a warp's next ticket is larger than
+    // its current one), whose neighbours hold smaller tickets: waits still end.
+    unsigned nxt = 0;
+    if (lane == 0) nxt = atomicAdd(counter, 1u);
     for (;;) {
-        unsigned tk = 0;
-        if (lane == 0) tk = atomicAdd(counter, 1u);
-        tk = __shfl_sync(0xffffffffu, tk, 0);
+        const unsigned tk = __shfl_sync(0xffffffffu, nxt, 0);
         if (tk >= nblocks) break;
+        if (lane == 0) nxt = atomicAdd(counter, 1u);
         const int64_t b = order[tk];
         const int64_t bk = b % a.nz, bj = (b / a.nz) % a.ny, bi = b / plane;
         const unsigned *deps[3] = {bi > 0 ? done + (b - plane) : nullptr, bj > 0 ? done + (b - a.nz) : nullptr,
                                    bk > 0 ? done + (b - 1) : nullptr};
-        // the block's own values need no neighbour: their loads overlap the wait
+        // the block's own values, its predictor selection and regression
+        // coefficients need no neighbour: their loads overlap the wait
         if (!DECOMP) lor_load_x<T>(a, bi, bj, bk, t, X);
-        if (lane == 0) {
-            for (int d = 0; d < 3; d++) {
-                if (!deps[d]) continue;
-                unsigned it = 0;
-                while (lor_ld_acquire(deps[d]) == 0u) {
-                    if (++it > kLorWaitLimit) {
-                        atomicExch(err, 1);
-                        break;
-                    }
-                    __nanosleep(64);
-                }
-            }
+        int sel = ind[b];
+        float rp[4] = {0, 0, 0, 0};
+        if (sel == 1) {
+            if (a.rp == nullptr) sel = 0;  // a stream without coefficients
+            else
+                for (int c = 0; c < 4; c++) rp[c] = a.rp[4 * b + c];
         }
-        __syncwarp();
-        // every lane acquires the neighbours' completion itself
-        for (int d = 0; d < 3; d++)
-            if (deps[d]) (void)lor_ld_acquire(deps[d]);
-        lor_block<T, DECOMP, QM, C>(a, bi, bj, bk, t, X, R, codes, scratch, ind, zpos, nzp, unpred);
-        __threadfence();
+        // every lane polls the (up to three) neighbours' flags together with
+        // relaxed loads; the fence after all are seen set orders the halo
+        // loads after the neighbours' writes
+        {
+            unsigned it = 0;
+            for (;;) {
+                const unsigned f0 = deps[0] ? lor_ld_relaxed(deps[0]) : 1u;
+                const unsigned f1 = deps[1] ? lor_ld_relaxed(deps[1]) : 1u;
+                const unsigned f2 = deps[2] ? lor_ld_relaxed(deps[2]) : 1u;
+                if (__all_sync(0xffffffffu, f0 != 0u && f1 != 0u && f2 != 0u)) break;
+                if (++it > kLorWaitLimit) {
+                    if (lane == 0) atomicExch(err, 1);
+                    break;
+                }
+                __nanosleep(32);
+            }
+            lor_fence_acq_rel();
+        }
+        lor_block<T, DECOMP, QM, C>(a, bi, bj, bk, t, sel, rp, halo, R, codes, scratch, zpos, nzp, unpred);
+        // each lane's reconstruction writes are released before the warp's flag
+        lor_fence_acq_rel();
         __syncwarp();
         if (lane == 0) lor_st_release(done + b, 1u);
     }
@@ -398,13 +453,19 @@ LorArgs make_args(const uint64_t *dims, int bs, int pd, int lo, int lo2, double 
     return a;
 }
 
-// C: uint16_t codes, or uint32_t for more than 65536 quantisation bins
+// Launches the wavefront on `st`; its error flag comes back to the returned
+// pinned word, to be read (check_wavefront) once `st` is synchronised.
+// C: uint16_t codes, or uint32_t for more than 65536 quantisation bins.
 template <typename T, typename C>
-void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, C *codes, T *scratch, const uint16_t *ind,
-                   const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st, Counter &launches) {
+const int *launch_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, C *codes, T *scratch,
+                            const uint16_t *ind, const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st,
+                            Counter &launches) {
     const bool straight = sizeof(T) == 4 && a.q.fast;
+    // the warps' tiles, then the halo table (4 bytes per halo position)
     const size_t smem = (size_t)kLorWarps *
-                        (size_t)((a.bs + 2) * (a.bs + 2) * (a.bs + 2) + (decomp ? 0 : a.bs * a.bs * a.bs)) * sizeof(T);
+                            (size_t)((a.bs + 2) * (a.bs + 2) * (a.bs + 2) + (decomp ? 0 : a.bs * a.bs * a.bs)) *
+                            sizeof(T) +
+                        (size_t)((a.bs + 2) * (a.bs + 2) * (a.bs + 2) - a.bs * a.bs * a.bs) * 4;
     void (*k)(LorArgs, const uint32_t *, uint32_t, unsigned *, unsigned *, int *, const T *, T *, C *, T *,
               const uint16_t *, const uint64_t *, uint64_t, const T *);
     if (!decomp) k = straight ? k_lor_persist<T, false, 1, C> : k_lor_persist<T, false, 0, C>;
@@ -454,10 +515,21 @@ void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, C *codes, T 
     // the flag comes back through pinned memory: a copy to pageable memory
     // would hold the driver's pageable staging path while this kernel runs,
     // stalling concurrent pageable copies (the tuner's other trials)
-    int *herr = (int *)t_pin_small.get(64);
+    int *herr = (int *)t_pin_flag.get(64);
     CK(cudaMemcpyAsync(herr, derr, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    return herr;
+}
+
+void check_wavefront(const int *herr) {
     if (*herr) throw Fail{FAZ_ERR_DEVICE, "Lorenzo wavefront: a block waited too long for its neighbours"};
+}
+
+template <typename T, typename C>
+void run_wavefront(const LorArgs &a, bool decomp, const T *X, T *R, C *codes, T *scratch, const uint16_t *ind,
+                   const uint64_t *zpos, uint64_t nz, const T *unpred, cudaStream_t st, Counter &launches) {
+    const int *herr = launch_wavefront<T, C>(a, decomp, X, R, codes, scratch, ind, zpos, nz, unpred, st, launches);
+    CK(cudaStreamSynchronize(st));
+    check_wavefront(herr);
 }
 
 // meta_params as written by write(params, c) (include/QoZ/utils/MetaDef.hpp:33-60):
@@ -635,13 +707,27 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
         }
         CK(cudaStreamSynchronize(st));  // host vectors leave scope
     }
-    if (wide) run_wavefront<T>(a, false, dX, R, codes32, scratch, ind, nullptr, 0, nullptr, st, launches);
-    else run_wavefront<T>(a, false, dX, R, codes16, scratch, ind, nullptr, 0, nullptr, st, launches);
+    // the predictor selections (and regression types) are final before the
+    // wavefront: their Huffman stages run on a second stream meanwhile
+    Events ev_sel, ev_side;
+    CK(cudaEventRecord(ev_sel.a, st));
+    StreamGuard side(nullptr, true);
+    CK(cudaStreamWaitEvent(side.st, ev_sel.a, 0));
+    DevMem m2(side.st);
+    trace_step("lorenzo wavefront queued");
+    const int *herr =
+        wide ? launch_wavefront<T>(a, false, dX, R, codes32, scratch, ind, nullptr, 0, nullptr, st, launches)
+             : launch_wavefront<T>(a, false, dX, R, codes16, scratch, ind, nullptr, 0, nullptr, st, launches);
     CK(cudaEventRecord(ev_pred.b, st));
-    CK(cudaEventRecord(ev_huff.a, st));
     HuffEncoded hi, hc, hr;
-    huffman_encode_device(ind, nb, 0, m, st, launches, hi, tm);
-    if (reg_count) huffman_encode_device(drtypes, rtypes.size(), 32768, m, st, launches, hr, tm);
+    huffman_encode_device(ind, nb, 0, m2, side.st, launches, hi, tm);
+    if (reg_count) huffman_encode_device(drtypes, rtypes.size(), 32768, m2, side.st, launches, hr, tm);
+    CK(cudaEventRecord(ev_side.a, side.st));
+    CK(cudaStreamWaitEvent(st, ev_side.a, 0));
+    CK(cudaStreamSynchronize(st));
+    check_wavefront(herr);
+    trace_step("lorenzo wavefront done");
+    CK(cudaEventRecord(ev_huff.a, st));
     if (wide) huffman_encode_device(codes32, n, radius, m, st, launches, hc, tm);
     else huffman_encode_device(codes16, n, radius, m, st, launches, hc, tm);
     if (vcount) {
@@ -654,6 +740,7 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     if (nunpred && wide) launches(launch_compact_zeros<T>(codes32, n, hc.zc, hc.zoff, nullptr, scratch, unp, st));
     if (nunpred && !wide) launches(launch_compact_zeros<T>(codes16, n, hc.zc, hc.zoff, nullptr, scratch, unp, st));
     CK(cudaEventRecord(ev_huff.b, st));
+    trace_step("lorenzo codebooks built");
     // SZFastFrontend::save: params, precision, meanInfo<T>{false, 0}, reg_count,
     // indicator tree + bits; LinearQuantizer::save; then the code tree + bits
     std::vector<uint8_t> h0;
@@ -700,7 +787,7 @@ void lorenzo3_compress_payload(const uint64_t *dims, int bs, int pd, int lo, int
     p += h2.size();
     if (hc.nbytes) CK(cudaMemcpyAsync(p, hc.bits, hc.nbytes, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    out.assign(pin, pin + total);
+    emit_payload(out, pin, total);
     tm.unpred_count = nunpred;
     tm.payload_bytes = total;
     tm.predict_ms += ev_pred.ms();

@@ -328,6 +328,7 @@ void block_interp_tail(int N, const uint64_t *sdims, double eb, int cubic, int d
         report(head + e.nzero * sizeof(T) + tree + e.nbytes);
     };
     huffman_encode_device(codes, num, 32768, m, st, launches, hc, tm, sized);
+    trace_step("trial encode queued");
     const uint64_t nunpred = hc.nzero;
     T *unp = m.alloc<T>(nunpred ? nunpred : 1);
     if (nunpred) launches(launch_compact_zeros<T>(codes, num, hc.zc, hc.zoff, nullptr, scratch, unp, st));
@@ -353,7 +354,7 @@ void block_interp_tail(int N, const uint64_t *sdims, double eb, int cubic, int d
         CK(cudaMemcpyAsync(pin + h.size() + nunpred * sizeof(T) + h2.size(), hc.bits, hc.nbytes,
                            cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    pl.assign(pin, pin + total);
+    emit_payload(pl, pin, total);
 }
 
 // One trial on its own host thread and CUDA stream: the trials are
@@ -361,10 +362,6 @@ void block_interp_tail(int N, const uint64_t *sdims, double eb, int cubic, int d
 // each thread computes its zstd size as soon as its payload is ready.
 // FAZ_TUNE_TRACE=1 prints the tuner's timeline (trial payloads, zstd sizes,
 // the overlapped compression) to stderr.
-bool tune_trace() {
-    const char *e = std::getenv("FAZ_TUNE_TRACE");
-    return e && e[0] == '1';
-}
 
 struct Trial {
     const char *name = "";
@@ -381,6 +378,12 @@ struct Trial {
             // a few MB are not allocated and faulted in again for each trial
             thread_local std::vector<uint8_t> pl;
             pl.clear();
+            // the payload stays in the thread's pinned staging buffer
+            PayloadView view;
+            struct ViewScope {
+                explicit ViewScope(PayloadView *v) { t_payload_view = v; }
+                ~ViewScope() { t_payload_view = nullptr; }
+            } scope(&view);
             bool reported = false;
             size_t early = 0;
             auto report = [&](size_t n) {
@@ -393,6 +396,7 @@ struct Trial {
             try {
                 // the trials gate the tuner's decision: they take SMs ahead of
                 // the overlapped compression
+                if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s starts\n", ms_since(t0), name);
                 StreamGuard sg(nullptr, true);
                 CK(cudaStreamWaitEvent(sg.st, ready, 0));
                 Counter c;
@@ -405,11 +409,12 @@ struct Trial {
                 if (!reported) raw.set_exception(std::current_exception());
                 throw;
             }
-            if (reported && early != pl.size())
-                throw Fail{FAZ_ERR_DEVICE, "a trial's reported size differs from its payload"};
-            report(pl.size());
-            if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s payload %zu bytes\n", ms_since(t0), name, pl.size());
-            const size_t z = zstd_framed_size(pl.data(), pl.size());
+            const uint8_t *pd = view.data ? view.data : pl.data();
+            const size_t pn = view.data ? view.size : pl.size();
+            if (reported && early != pn) throw Fail{FAZ_ERR_DEVICE, "a trial's reported size differs from its payload"};
+            report(pn);
+            if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s payload %zu bytes\n", ms_since(t0), name, pn);
+            const size_t z = zstd_framed_size(pd, pn);
             if (tune_trace()) std::fprintf(stderr, "tune %8.3f ms  %s zstd %zu bytes\n", ms_since(t0), name, z);
             return z;
         });
@@ -646,6 +651,7 @@ void sz3_tune_device(faz_config &c, const T *dX, cudaStream_t st, Counter &launc
     CK(cudaEventRecord(ready.a, st));
     Trial jl, ji[2], jd[2];
     const auto tt0 = clk::now();
+    if (tune_trace()) trace_epoch() = tt0;
     jl.name = "lorenzo";
     ji[0].name = "linear";
     ji[1].name = "cubic";
