@@ -100,3 +100,18 @@ def test_unsupported_algo_is_reported(lib):
     with pytest.raises(F.FazError) as ei:
         F.SZ_compress(c, np.zeros((8, 8, 8), np.float32))
     assert ei.value.code in (-2, -3)
+
+
+@pytest.mark.parametrize("preset", [None, "4"])
+def test_package_sets_work_queue_default(preset):
+    """Importing the package defaults CUDA_DEVICE_MAX_CONNECTIONS to 32 (the
+    tuner's concurrent trial streams) and keeps a value the caller set."""
+    import subprocess
+    import sys
+    env = {k: v for k, v in os.environ.items() if k != "CUDA_DEVICE_MAX_CONNECTIONS"}
+    if preset is not None:
+        env["CUDA_DEVICE_MAX_CONNECTIONS"] = preset
+    out = subprocess.run([sys.executable, "-c", "import os, faz_gb300; print(os.environ['CUDA_DEVICE_MAX_CONNECTIONS'])"],
+                         cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == (preset or "32")
