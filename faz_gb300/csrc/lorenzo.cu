@@ -341,7 +341,7 @@ __device__ __forceinline__ void lor_block(const LorArgs &a, int64_t bi, int64_t 
     }
 }
 
-constexpr unsigned kLorWaitLimit = 1u << 22;  // polls (with back-off) of a neighbour before giving up
+constexpr unsigned kLorWaitLimit = 1u << 22;  // polls (with back-off) of a block's neighbours before giving up
 
 // The whole wavefront in one launch of persistent CTAs.  A warp takes a
 // ticket, and with it the block order[ticket]: blocks come diagonal by
